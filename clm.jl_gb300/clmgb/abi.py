@@ -1,0 +1,231 @@
+"""ctypes mirror of include/clmgb.h and the structure-of-arrays field schema.
+
+The field lists below follow the C structs member by member (tests/test_abi.py
+parses the header and checks the order).  Every per-level field is a Julia
+column-major ``Matrix{Float64}(nc, nlev)``: element ``(c, jj)`` lives at
+``c + (jj-1)*ldc``.  Host arrays therefore have numpy shape ``(nlev, ldc)``
+(C order) and device tensors the same shape.
+
+Field kinds (dimension of the leading axis):
+  L  = nlevsno + nlevmaxurbgrnd   (t_soisno, dz, z, h2osoi_*, fact, imelt, thk ...)
+  LZ = L + 1                      (zi)
+  G  = nlevgrnd                   (soil parameters, eflx_fgr, icefrac ...)
+  S  = nlevsno                    (bw, qflx_snomelt_lyr ...)
+  S1 = nlevsno + 1                (sabg_lyr, patch)
+  SOI = nlevsoi                   (qflx_rootsoi)
+"""
+import ctypes as C
+import re
+
+c_double_p = C.POINTER(C.c_double)
+c_int64_p = C.POINTER(C.c_int64)
+c_uint8_p = C.POINTER(C.c_uint8)
+c_uint32_p = C.POINTER(C.c_uint32)
+
+# ---- constants (include/clmgb.h) ----
+CLMGB_OK = 0
+CLMGB_ERR_NULL_ARG = -1
+CLMGB_ERR_DIMS = -2
+CLMGB_ERR_CONFIG = -3
+CLMGB_ERR_UNSUPPORTED = -4
+CLMGB_ERR_CUDA = -5
+CLMGB_ERR_ABI = -6
+CLMGB_ERR_HANDLE = -7
+
+COL_URBAN = 1
+COL_SUBSTEP_CAP = 2
+COL_NONFINITE = 4
+COL_LEVEL_RANGE = 8
+COL_PATCH_RANGE = 16
+
+SNOW_JORDAN1991 = 1
+SNOW_STURM1997 = 2
+
+BC_HEAD, BC_FLUX, BC_ZERO_FLUX, BC_WATERTABLE, BC_AQUIFER = 0, 1, 2, 3, 4
+ZENGDECKER_2009, MOISTURE_FORM = 0, 1
+
+MAX_NLEVSNO = 12
+MAX_NLEVGRND = 25
+MAX_NLEVSOI = 25
+
+
+class Varpar(C.Structure):
+    _fields_ = [("nlevsno", C.c_int32), ("nlevgrnd", C.c_int32), ("nlevsoi", C.c_int32),
+                ("nlevurb", C.c_int32), ("nlevmaxurbgrnd", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Bounds(C.Structure):
+    _fields_ = [("nc", C.c_int64), ("np", C.c_int64), ("nl", C.c_int64),
+                ("ldc", C.c_int64), ("ldp", C.c_int64)]
+
+
+class SwmConfig(C.Structure):
+    """SoilWaterMovementConfig (soil_water_movement.jl:654-671)."""
+    _fields_ = [("soilwater_movement_method", C.c_int32), ("upper_boundary_condition", C.c_int32),
+                ("lower_boundary_condition", C.c_int32), ("flux_calculation", C.c_int32),
+                ("dtmin", C.c_double), ("verySmall", C.c_double), ("xTolerUpper", C.c_double),
+                ("xTolerLower", C.c_double), ("e_ice", C.c_double)]
+
+    @classmethod
+    def clm5_default(cls):
+        """The config clm_drv! builds when use_aquifer_layer=false (clm_driver.jl:2043-2048)."""
+        return cls(MOISTURE_FORM, BC_FLUX, BC_ZERO_FLUX, 1, 60.0, 1.0e-8, 1.0e-1, 1.0e-2, 6.0)
+
+
+# (name, ctype, kind, dims) ; kind: 'c' column, 'p' patch, 'l' landunit
+# dims: None = vector, else level-kind string
+_u8, _i64, _f64 = "u8", "i64", "f64"
+
+SOILTEMP_FIELDS = [
+    ("mask_nolakec", _u8, "c", None),
+    ("mask_nolakep", _u8, "p", None),
+    ("col_snl", _i64, "c", None),
+    ("col_nbedrock", _i64, "c", None),
+    ("col_itype", _i64, "c", None),
+    ("col_landunit", _i64, "c", None),
+    ("col_patchi", _i64, "c", None),
+    ("col_patchf", _i64, "c", None),
+    ("lun_itype", _i64, "l", None),
+    ("lun_urbpoi", _u8, "l", None),
+    ("patch_column", _i64, "p", None),
+    ("patch_landunit", _i64, "p", None),
+    ("patch_wtcol", _f64, "p", None),
+    ("frac_veg_nosno", _i64, "p", None),
+    ("dz", _f64, "c", "L"),
+    ("z", _f64, "c", "L"),
+    ("zi", _f64, "c", "LZ"),
+    ("t_soisno", _f64, "c", "L"),
+    ("t_h2osfc", _f64, "c", None),
+    ("t_grnd", _f64, "c", None),
+    ("xmf", _f64, "c", None),
+    ("xmf_h2osfc", _f64, "c", None),
+    ("fact", _f64, "c", "L"),
+    ("c_h2osfc", _f64, "c", None),
+    ("imelt", _i64, "c", "L"),
+    ("emg", _f64, "c", None),
+    ("htvp", _f64, "c", None),
+    ("eflx_bot", _f64, "c", None),
+    ("eflx_fgr12", _f64, "c", None),
+    ("eflx_fgr", _f64, "c", "G"),
+    ("eflx_snomelt", _f64, "c", None),
+    ("eflx_snomelt_r", _f64, "c", None),
+    ("eflx_snomelt_u", _f64, "c", None),
+    ("eflx_h2osfc_to_snow", _f64, "c", None),
+    ("eflx_gnet", _f64, "p", None),
+    ("dgnetdT", _f64, "p", None),
+    ("dlrad", _f64, "p", None),
+    ("cgrnd", _f64, "p", None),
+    ("eflx_sh_grnd", _f64, "p", None),
+    ("eflx_sh_snow", _f64, "p", None),
+    ("eflx_sh_soil", _f64, "p", None),
+    ("eflx_sh_h2osfc", _f64, "p", None),
+    ("watsat", _f64, "c", "G"),
+    ("bsw", _f64, "c", "G"),
+    ("sucsat", _f64, "c", "G"),
+    ("tkmg", _f64, "c", "G"),
+    ("tkdry", _f64, "c", "G"),
+    ("csol", _f64, "c", "G"),
+    ("thk", _f64, "c", "L"),
+    ("h2osoi_liq", _f64, "c", "L"),
+    ("h2osoi_ice", _f64, "c", "L"),
+    ("excess_ice", _f64, "c", "L"),
+    ("h2osno_no_layers", _f64, "c", None),
+    ("h2osfc", _f64, "c", None),
+    ("int_snow", _f64, "c", None),
+    ("frac_sno_eff", _f64, "c", None),
+    ("frac_h2osfc", _f64, "c", None),
+    ("snow_depth", _f64, "c", None),
+    ("bw", _f64, "c", "S"),
+    ("exice_subs", _f64, "c", "G"),
+    ("snomelt_accum", _f64, "c", None),
+    ("qflx_evap_soi", _f64, "p", None),
+    ("qflx_ev_snow", _f64, "p", None),
+    ("qflx_ev_soil", _f64, "p", None),
+    ("qflx_ev_h2osfc", _f64, "p", None),
+    ("qflx_snomelt", _f64, "c", None),
+    ("qflx_snofrz", _f64, "c", None),
+    ("qflx_snow_drain", _f64, "c", None),
+    ("qflx_h2osfc_to_ice", _f64, "c", None),
+    ("qflx_snomelt_lyr", _f64, "c", "S"),
+    ("qflx_snofrz_lyr", _f64, "c", "S"),
+    ("sabg", _f64, "p", None),
+    ("sabg_soil", _f64, "p", None),
+    ("sabg_snow", _f64, "p", None),
+    ("sabg_lyr", _f64, "p", "S1"),
+    ("sabg_chk", _f64, "p", None),
+    ("forc_lwrad", _f64, "c", None),
+]
+
+SOILWATER_FIELDS = [
+    ("mask_hydrology", _u8, "c", None),
+    ("col_nbedrock", _i64, "c", None),
+    ("dz", _f64, "c", "L"),
+    ("z", _f64, "c", "L"),
+    ("zi", _f64, "c", "LZ"),
+    ("h2osoi_liq", _f64, "c", "L"),
+    ("h2osoi_ice", _f64, "c", "L"),
+    ("excess_ice", _f64, "c", "L"),
+    ("watsat", _f64, "c", "G"),
+    ("hksat", _f64, "c", "G"),
+    ("bsw", _f64, "c", "G"),
+    ("sucsat", _f64, "c", "G"),
+    ("eff_porosity", _f64, "c", "G"),
+    ("icefrac", _f64, "c", "G"),
+    ("smp_l", _f64, "c", "G"),
+    ("hk_l", _f64, "c", "G"),
+    ("qflx_rootsoi", _f64, "c", "SOI"),
+    ("qflx_infl", _f64, "c", None),
+    ("zwt", _f64, "c", None),
+    ("qcharge", _f64, "c", None),
+    ("num_substeps", _f64, "c", None),
+]
+
+# Fields of the synthetic step harness that are not in either struct.
+EXTRA_FIELDS = [
+    ("t_ssbef", _f64, "c", "L"),
+    ("t_h2osfc_bef", _f64, "c", None),
+]
+
+_CT = {_u8: c_uint8_p, _i64: c_int64_p, _f64: c_double_p}
+
+
+def _mk_struct(name, fields):
+    return type(name, (C.Structure,),
+                {"_fields_": [("struct_size", C.c_int64)] + [(n, _CT[t]) for (n, t, _, _) in fields]})
+
+
+SoilTempFields = _mk_struct("SoilTempFields", SOILTEMP_FIELDS)
+SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
+
+
+def all_fields():
+    """Union of every field (first definition wins), in a stable order."""
+    seen, out = set(), []
+    for fl in (SOILTEMP_FIELDS, SOILWATER_FIELDS, EXTRA_FIELDS):
+        for f in fl:
+            if f[0] not in seen:
+                seen.add(f[0])
+                out.append(f)
+    return out
+
+
+def level_count(kind, vp):
+    """Number of levels of a field kind for a Varpar-like object."""
+    L = vp.nlevsno + vp.nlevmaxurbgrnd
+    return {"L": L, "LZ": L + 1, "G": vp.nlevgrnd, "S": vp.nlevsno,
+            "S1": vp.nlevsno + 1, "SOI": vp.nlevsoi}[kind]
+
+
+def header_struct_members(header_text, struct_name):
+    """Member names of `typedef struct <struct_name> {...}` in the C header."""
+    m = re.search(r"typedef struct %s \{(.*?)\} %s;" % (struct_name, struct_name), header_text, re.S)
+    if not m:
+        raise ValueError("struct %s not found" % struct_name)
+    body = re.sub(r"/\*.*?\*/", "", m.group(1), flags=re.S)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        names.append(re.findall(r"([A-Za-z_][A-Za-z0-9_]*)\s*$", decl)[0])
+    return names

@@ -1,0 +1,305 @@
+/*
+ * clmgb.h — C ABI of the GB300-native soil/snow column solve.
+ *
+ * Drop-in boundary for CLM.jl's per-column vertical solve:
+ *   soil_temperature!      src/biogeophys/soil_temperature.jl:358-593
+ *   set_soil_water_fractions! src/biogeophys/soil_hydrology.jl:394-416 (kernel :110-130)
+ *   soil_water! -> soilwater_moisture_form! -> soilwm_moisture_form_solve!
+ *                          src/biogeophys/soil_water_movement.jl:1780-1810, 1532-1601, 1498-1517
+ *   batched_band_solve!    src/infrastructure/band_diagonal.jl:179-189
+ *   tridiagonal_multi!     src/infrastructure/tridiagonal.jl:129-142
+ *
+ * Layout contract (identical to the reference's structure-of-arrays state):
+ *   every per-column level field is a Julia column-major Matrix{Float64}(nc, nlev):
+ *   element (c, jj) — c = 0..nc-1, jj = 1..nlev the Julia level index — lives at
+ *   ptr[c + (jj-1)*ldc].  ldc >= nc (ldc == nc for a plain Julia Matrix).  Patch
+ *   matrices use ldp the same way.  Integer state (snl, nbedrock, imelt, itype,
+ *   landunit, patchi/patchf, ...) is int64_t (Julia Int), Bool masks are uint8_t,
+ *   and every index stored in an array is 1-based as in Julia.
+ *
+ * All compute entry points are stream-ordered and asynchronous: they enqueue work on
+ * `stream` (a cudaStream_t passed as void*; NULL = legacy default stream) and return.
+ * Pointers are device pointers unless stated otherwise.  The library never allocates
+ * inside a compute call: scratch lives in the handle (clmgb_create).  A handle is not
+ * thread-safe; use one handle per stream.
+ *
+ * Return codes: 0 success; negative = invalid argument / unsupported configuration
+ * detected on the host before any launch (nothing was enqueued); the device-side
+ * per-column status (CLMGB_COL_*) is accumulated in the handle and read with
+ * clmgb_device_status().  There is no CPU fallback anywhere behind this ABI.
+ */
+#ifndef CLMGB_H
+#define CLMGB_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CLMGB_ABI_VERSION 1
+
+/* ---- return codes ---- */
+#define CLMGB_OK                 0
+#define CLMGB_ERR_NULL_ARG      -1   /* a required pointer is NULL */
+#define CLMGB_ERR_DIMS          -2   /* level counts / nc / leading dims out of the supported range */
+#define CLMGB_ERR_CONFIG        -3   /* method / boundary condition the reference rejects with error() */
+#define CLMGB_ERR_UNSUPPORTED   -4   /* a configuration this build does not implement (no fallback) */
+#define CLMGB_ERR_CUDA          -5   /* a CUDA launch or copy failed; see clmgb_last_cuda_error */
+#define CLMGB_ERR_ABI           -6   /* struct size / ABI version mismatch */
+#define CLMGB_ERR_HANDLE        -7   /* NULL or foreign handle */
+
+/* ---- per-column device status bits (OR-accumulated in the handle) ---- */
+#define CLMGB_COL_URBAN          1u  /* urban landunit column reached a non-urban kernel */
+#define CLMGB_COL_SUBSTEP_CAP    2u  /* Richards substep attempts hit the safety cap */
+#define CLMGB_COL_NONFINITE      4u  /* a non-finite temperature / water value was produced */
+#define CLMGB_COL_LEVEL_RANGE    8u  /* snl / nbedrock outside the level range */
+#define CLMGB_COL_PATCH_RANGE   16u  /* patchi/patchf outside 1..np */
+
+/* ---- compile-time limits of this build ---- */
+#define CLMGB_MAX_NLEVSNO   12
+#define CLMGB_MAX_NLEVGRND  25
+#define CLMGB_MAX_NLEVSOI   25
+
+/* Level counts: mirrors varpar (src/constants/varpar.jl:113-150). */
+typedef struct clmgb_varpar {
+  int32_t nlevsno;        /* 12 in CLM5 */
+  int32_t nlevgrnd;       /* 25 for 20SL_8.5m */
+  int32_t nlevsoi;        /* 20 for 20SL_8.5m */
+  int32_t nlevurb;        /* urban levels, <= nlevgrnd */
+  int32_t nlevmaxurbgrnd; /* max(nlevurb, nlevgrnd); must equal nlevgrnd here */
+  int32_t reserved;
+} clmgb_varpar;
+
+/* Column / patch / landunit counts and leading dimensions. */
+typedef struct clmgb_bounds {
+  int64_t nc;   /* columns (length of bounds_col) */
+  int64_t np;   /* patches */
+  int64_t nl;   /* landunits */
+  int64_t ldc;  /* leading dimension of [nc, *] matrices, >= nc */
+  int64_t ldp;  /* leading dimension of [np, *] matrices, >= np */
+} clmgb_bounds;
+
+/* Snow thermal conductivity method: varctl.snow_thermal_cond_method (varctl.jl:158). */
+#define CLMGB_SNOW_JORDAN1991 1
+#define CLMGB_SNOW_STURM1997  2
+
+/*
+ * Every field soil_temperature! reads or writes for soil/crop/wetland/glacier
+ * columns (soil_temperature.jl:358-593).  Field names follow the reference
+ * (ColumnData, LandunitData, PatchData, TemperatureData, EnergyFluxData,
+ * SoilStateData, WaterStateBulkData, WaterDiagnosticBulkData, WaterFluxBulkData,
+ * SolarAbsorbedData, CanopyStateData).  Dimensions: L = nlevsno+nlevmaxurbgrnd,
+ * LZ = L+1, G = nlevgrnd, S = nlevsno, S1 = nlevsno+1.
+ */
+typedef struct clmgb_soiltemp_fields {
+  int64_t struct_size;               /* sizeof(clmgb_soiltemp_fields) */
+  /* masks and subgrid topology */
+  const uint8_t* mask_nolakec;       /* [nc]  filt.nolakec */
+  const uint8_t* mask_nolakep;       /* [np]  filt.nolakep */
+  const int64_t* col_snl;            /* [nc]  col.snl (0..-nlevsno) */
+  const int64_t* col_nbedrock;       /* [nc]  col.nbedrock */
+  const int64_t* col_itype;          /* [nc]  col.itype */
+  const int64_t* col_landunit;       /* [nc]  col.landunit (1-based) */
+  const int64_t* col_patchi;         /* [nc]  col.patchi (1-based, first patch) */
+  const int64_t* col_patchf;         /* [nc]  col.patchf (1-based, last patch) */
+  const int64_t* lun_itype;          /* [nl]  lun.itype */
+  const uint8_t* lun_urbpoi;         /* [nl]  lun.urbpoi */
+  const int64_t* patch_column;       /* [np]  patch.column (1-based) */
+  const int64_t* patch_landunit;     /* [np]  patch.landunit (1-based) */
+  const double*  patch_wtcol;        /* [np]  patch.wtcol */
+  const int64_t* frac_veg_nosno;     /* [np]  canopystate.frac_veg_nosno_patch */
+  /* geometry */
+  const double* dz;                  /* [ldc, L]  col.dz */
+  const double* z;                   /* [ldc, L]  col.z */
+  const double* zi;                  /* [ldc, LZ] col.zi */
+  /* temperature */
+  double*  t_soisno;                 /* [ldc, L]  RW */
+  double*  t_h2osfc;                 /* [nc]      RW */
+  double*  t_grnd;                   /* [nc]      W (read by the lw emission) */
+  double*  xmf;                      /* [nc]      W */
+  double*  xmf_h2osfc;               /* [nc]      W */
+  double*  fact;                     /* [ldc, L]  W */
+  double*  c_h2osfc;                 /* [nc]      W */
+  int64_t* imelt;                    /* [ldc, L]  W */
+  const double* emg;                 /* [nc]  temperature.emg_col */
+  /* energy flux */
+  const double* htvp;                /* [nc] */
+  const double* eflx_bot;            /* [nc] */
+  double* eflx_fgr12;                /* [nc]      W */
+  double* eflx_fgr;                  /* [ldc, G]  W */
+  double* eflx_snomelt;              /* [nc]      W */
+  double* eflx_snomelt_r;            /* [nc]      W */
+  double* eflx_snomelt_u;            /* [nc]      W (urban only; untouched here) */
+  double* eflx_h2osfc_to_snow;       /* [nc]      W */
+  double* eflx_gnet;                 /* [np]      W */
+  double* dgnetdT;                   /* [np]      W */
+  const double* dlrad;               /* [np] */
+  const double* cgrnd;               /* [np] */
+  const double* eflx_sh_grnd;        /* [np] */
+  const double* eflx_sh_snow;        /* [np] */
+  const double* eflx_sh_soil;        /* [np] */
+  const double* eflx_sh_h2osfc;      /* [np] */
+  /* soil state */
+  const double* watsat;              /* [ldc, G] */
+  const double* bsw;                 /* [ldc, G] */
+  const double* sucsat;              /* [ldc, G] */
+  const double* tkmg;                /* [ldc, G] */
+  const double* tkdry;               /* [ldc, G] */
+  const double* csol;                /* [ldc, G] */
+  double* thk;                       /* [ldc, L]  W */
+  /* water state (bulk) */
+  double* h2osoi_liq;                /* [ldc, L]  RW */
+  double* h2osoi_ice;                /* [ldc, L]  RW */
+  double* excess_ice;                /* [ldc, L]  RW; indexed [c, j] for soil j as the reference does */
+  double* h2osno_no_layers;          /* [nc]      RW */
+  double* h2osfc;                    /* [nc]      RW */
+  double* int_snow;                  /* [nc]      RW */
+  /* water diagnostic (bulk) */
+  const double* frac_sno_eff;        /* [nc] */
+  const double* frac_h2osfc;         /* [nc] */
+  double* snow_depth;                /* [nc]      RW */
+  double* bw;                        /* [ldc, S]  W */
+  double* exice_subs;                /* [ldc, G]  W */
+  double* snomelt_accum;             /* [nc]      RW */
+  /* water flux (bulk) */
+  const double* qflx_evap_soi;       /* [np] */
+  const double* qflx_ev_snow;        /* [np] */
+  const double* qflx_ev_soil;        /* [np] */
+  const double* qflx_ev_h2osfc;      /* [np] */
+  double* qflx_snomelt;              /* [nc]      W */
+  double* qflx_snofrz;               /* [nc]      W */
+  double* qflx_snow_drain;           /* [nc]      W */
+  double* qflx_h2osfc_to_ice;        /* [nc]      W */
+  double* qflx_snomelt_lyr;          /* [ldc, S]  W */
+  double* qflx_snofrz_lyr;           /* [ldc, S]  W */
+  /* solar absorbed */
+  const double* sabg;                /* [np] */
+  const double* sabg_soil;           /* [np] */
+  const double* sabg_snow;           /* [np] */
+  const double* sabg_lyr;            /* [ldp, S1] */
+  double* sabg_chk;                  /* [np]      W */
+  /* forcing */
+  const double* forc_lwrad;          /* [nc]  atm2lnd forc_lwrad_downscaled_col */
+} clmgb_soiltemp_fields;
+
+/* Lower boundary conditions (soil_water_movement.jl:30-34). */
+#define CLMGB_BC_HEAD        0
+#define CLMGB_BC_FLUX        1
+#define CLMGB_BC_ZERO_FLUX   2
+#define CLMGB_BC_WATERTABLE  3
+#define CLMGB_BC_AQUIFER     4
+/* Methods (soil_water_movement.jl:24-27). */
+#define CLMGB_ZENGDECKER_2009 0
+#define CLMGB_MOISTURE_FORM   1
+
+/* SoilWaterMovementConfig (soil_water_movement.jl:654-671), same defaults. */
+typedef struct clmgb_swm_config {
+  int32_t soilwater_movement_method;   /* CLMGB_MOISTURE_FORM for this path */
+  int32_t upper_boundary_condition;    /* CLMGB_BC_FLUX */
+  int32_t lower_boundary_condition;    /* ZERO_FLUX (CLM5 default), FLUX or WATERTABLE */
+  int32_t flux_calculation;            /* 1 = inexpensive (default), 42 = expensive */
+  double  dtmin;                       /* 60 s */
+  double  verySmall;                   /* 1e-8 */
+  double  xTolerUpper;                 /* 0.1 */
+  double  xTolerLower;                 /* 0.01 */
+  double  e_ice;                       /* 6.0 */
+} clmgb_swm_config;
+
+/* Every field soil_water! (moisture form) and set_soil_water_fractions! touch. */
+typedef struct clmgb_soilwater_fields {
+  int64_t struct_size;               /* sizeof(clmgb_soilwater_fields) */
+  const uint8_t* mask_hydrology;     /* [nc]  filt.hydrologyc */
+  const int64_t* col_nbedrock;       /* [nc] */
+  const double* dz;                  /* [ldc, L] */
+  const double* z;                   /* [ldc, L] */
+  const double* zi;                  /* [ldc, LZ] */
+  double* h2osoi_liq;                /* [ldc, L]  RW (soil part) */
+  const double* h2osoi_ice;          /* [ldc, L] */
+  const double* excess_ice;          /* [ldc, L]  indexed [c, j] for soil j as the reference does */
+  const double* watsat;              /* [ldc, G] */
+  const double* hksat;               /* [ldc, G] */
+  const double* bsw;                 /* [ldc, G] */
+  const double* sucsat;              /* [ldc, G] */
+  double* eff_porosity;              /* [ldc, G]  W (fractions) */
+  double* icefrac;                   /* [ldc, G]  W (fractions), R (moisture form) */
+  double* smp_l;                     /* [ldc, G]  W */
+  double* hk_l;                      /* [ldc, G]  W */
+  const double* qflx_rootsoi;        /* [ldc, nlevsoi] */
+  const double* qflx_infl;           /* [nc] */
+  const double* zwt;                 /* [nc] */
+  double* qcharge;                   /* [nc]  W */
+  double* num_substeps;              /* [nc]  W (Float64 as in the reference) */
+} clmgb_soilwater_fields;
+
+typedef struct clmgb_handle_s* clmgb_handle;
+
+/* ---- library / handle ---- */
+int32_t     clmgb_abi_version(void);
+const char* clmgb_build_info(void);
+const char* clmgb_strerror(int32_t code);
+/* Create a handle bound to the current CUDA device; allocates the handle's device
+ * status word.  Returns CLMGB_OK and writes *out. */
+int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out);
+int32_t clmgb_destroy(clmgb_handle h);
+/* Copy the OR of all per-column status bits since the last reset to *status (host
+ * pointer; synchronises `stream`) and optionally clear it. */
+int32_t clmgb_device_status(clmgb_handle h, void* stream, uint32_t* status, int32_t reset);
+int32_t clmgb_last_cuda_error(clmgb_handle h);
+
+/* ---- drop-in entry points ---- */
+
+/* soil_temperature! (soil_temperature.jl:358) for non-urban, non-lake columns.
+ * snow_method: CLMGB_SNOW_JORDAN1991 | CLMGB_SNOW_STURM1997;
+ * use_excess_ice must be 0 (varctl default, varctl.jl:215);
+ * col_status: optional [nc] uint32 per-column status out (may be NULL). */
+int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b,
+                               const clmgb_soiltemp_fields* f, double dtime,
+                               int32_t snow_method, int32_t use_excess_ice,
+                               uint32_t* col_status, void* stream);
+
+/* set_soil_water_fractions! (soil_hydrology.jl:394-416; kernel :110-130). */
+int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b,
+                                   const clmgb_soilwater_fields* f, void* stream);
+
+/* soil_water! (soil_water_movement.jl:1780) with the moisture-form method: routes to
+ * soilwm_moisture_form_solve! (:1498).  ZENGDECKER_2009 -> CLMGB_ERR_UNSUPPORTED;
+ * BC_AQUIFER/BC_WATERTABLE need compute_qcharge! (:1575) -> CLMGB_ERR_UNSUPPORTED
+ * for AQUIFER; WATERTABLE solves but does not run compute_qcharge!. */
+int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b,
+                         const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
+                         double dtime, uint32_t* col_status, void* stream);
+
+/* One whole column step in a single launch: t_ssbef/t_h2osfc_bef copies, soil_temperature!,
+ * set_soil_water_fractions!, soil_water! (moisture form) — the driver's order
+ * (clm_driver.jl:1801, 1935, 2049) when nothing runs in between.  t_ssbef and
+ * t_h2osfc_bef may be NULL. */
+int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b,
+                          const clmgb_soiltemp_fields* ft, const clmgb_soilwater_fields* fw,
+                          const clmgb_swm_config* cfg, double dtime, int32_t snow_method,
+                          double* t_ssbef, double* t_h2osfc_bef,
+                          uint32_t* col_status, void* stream);
+
+/* ---- solver entry points ---- */
+
+/* batched_band_solve! (band_diagonal.jl:179): bmatrix is [ldc, nband, nlev] (nband =
+ * kl+ku+1 = 5, row-oriented bands: band b of row r is A[r, r+3-b]); rvector/tvector
+ * are [ldc, nlev]; jtop/jbot int64 [nc] in the -nlevsno_off.. level numbering, the
+ * solved rows are jtop+nlevsno_off+1 .. jbot+nlevsno_off+1 (1-based). */
+int32_t clmgb_batched_band_solve(clmgb_handle h, int64_t nc, int64_t ldc, int32_t nlev,
+                                 double* tvector, const double* bmatrix, const double* rvector,
+                                 const int64_t* jtop, const int64_t* jbot, const uint8_t* mask,
+                                 int32_t kl, int32_t ku, int32_t nlevsno_off, void* stream);
+
+/* tridiagonal_multi! (tridiagonal.jl:129): a,b,c,r,u are [ldc, nlevs]; jtop int64 [nc]
+ * 1-based; Thomas with the reference's 1e-30 pivot guard. */
+int32_t clmgb_tridiagonal_multi(clmgb_handle h, int64_t ncols, int64_t ldc, int32_t nlevs,
+                                double* u, const double* a, const double* b, const double* c,
+                                const double* r, const int64_t* jtop, const uint8_t* mask,
+                                void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CLMGB_H */

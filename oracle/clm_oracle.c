@@ -1,0 +1,1347 @@
+/*
+ * clm_oracle.c — TEST INFRASTRUCTURE ONLY: the CPU oracle (parity checker) and the
+ * timed CPU baseline for the soil/snow column solve.  Nothing in the product links,
+ * loads or calls this file; only tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / --impl reference legs do.
+ *
+ * A plain-C restatement of CLM.jl's Float64 CPU path, kernel by kernel, in the
+ * reference's own operation order (compiled with -ffp-contract=off so no a*b+c is
+ * fused, as Julia does not fuse without muladd):
+ *   soil_temperature!            src/biogeophys/soil_temperature.jl:358-593
+ *     _soil_snow_tk_kernel!      :647-716      _soil_tk_interface_kernel! :599-629
+ *     _tk_h2osfc_kernel!         :762-776      _soil_cv_kernel!           :781-813
+ *     _unresolved_snow_cv_kernel!:842-850      _snow_cv_kernel!           :855-869
+ *     _ground_lwrad_emit_kernel! :946-960      _gnet_patch_rural*_kernel! :1003-1044
+ *     scatter_add_1d!            src/infrastructure/kernels.jl:166-170
+ *     _gnet_snicar_kernel!       :1139-1167    _heat_diff_kernel!         :1271-1319
+ *     _h2osfc_thermprop_kernel!  :116-130      set_rhs_vec! kernels       :1365-1542
+ *     set_matrix! kernels        :1549-1748    _tvector_init/extract      :133-167
+ *     _batched_band_solve_kernel! src/infrastructure/band_diagonal.jl:87-170 (dense GE)
+ *     _fn1_kernel!               :170-206      _phase_change_h2osfc_kernel! :1757-1855
+ *     _phase_change_beta_kernel! :1929-2230    _tgrnd_kernel!             :224-247
+ *     _eflx_fgr_kernel!          :250-269
+ *   _soilhyd_water_fractions_kernel!  src/biogeophys/soil_hydrology.jl:110-130
+ *   _soilwm_moisture_form_kernel!     src/biogeophys/soil_water_movement.jl:1250-1489
+ *   tridiagonal_solve! / _tridiag_multi_kernel!  src/infrastructure/tridiagonal.jl:35-127
+ *   tridiagonal_col!                  src/biogeophys/soil_water_movement.jl:736-773
+ *   init_soil_properties!             src/infrastructure/cold_start.jl:225-391
+ *
+ * Transcendentals: the reference uses Julia Base's pow/log10 (openlibm for log10);
+ * this file uses the C library's.  Both are within ~1 ulp, so parity at the 1e-10
+ * level is unaffected; decisions that sit within an ulp of a threshold can flip.
+ * Integer powers follow Julia's literal_pow: x^2 = x*x, x^3 = x*x*x, and x^4 uses
+ * Base.Math.pow_body's compensated squaring (Julia >= 1.10, Project.toml compat).
+ * smooth_min/smooth_max are exact min/max for Float64 (smooth_ad.jl:91-149), with
+ * Julia's NaN-propagating min/max semantics.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "../include/clmgb.h"
+
+/* ---- constants: src/constants/varcon.jl:15-70 ---- */
+#define GRAV   9.80616
+#define SB     5.67e-8
+#define CPLIQ  4188.0
+#define CPICE  2117.27
+#define HFUS   3.337e5
+#define DENH2O 1000.0
+#define DENICE 917.0
+#define TFRZ   273.15
+#define TKAIR  0.023
+#define TKICE  2.290
+#define TKWAT  0.57
+#define CAPR   0.34
+#define CNFAC  0.5
+#define THK_BEDROCK  3.0
+#define CSOL_BEDROCK 2.0e6
+#define THIN_SFCLAYER 1.0e-6
+#define M_TO_MM 1.0e3
+/* landunit / column types: src/constants/landunit_varcon.jl, column_varcon.jl */
+#define ISTSOIL 1
+#define ISTCROP 2
+#define ISTICE  4
+#define ISTWET  6
+#define ICOL_ROOF 71
+#define ICOL_SUNWALL 72
+#define ICOL_SHADEWALL 73
+#define ICOL_ROAD_IMPERV 74
+#define ICOL_ROAD_PERV 75
+
+#define ORC_MAXL 80          /* any CLM level structure (49SL_10m: 12+54) */
+
+/* Julia Base.max / Base.min on Float64: NaN propagates, -0.0 < 0.0. */
+static inline double jl_max(double x, double y) {
+  if (x != x) return x;
+  if (y != y) return y;
+  if (x > y) return x;
+  if (y > x) return y;
+  return signbit(x) ? y : x;
+}
+static inline double jl_min(double x, double y) {
+  if (x != x) return x;
+  if (y != y) return y;
+  if (x < y) return x;
+  if (y < x) return y;
+  return signbit(x) ? x : y;
+}
+/* Julia x^4 for Float64: Base.Math.pow_body(x, 4) — compensated power by squaring. */
+static inline double jl_pow4(double x) {
+  double xnlo = 0.0, err, x2, x4, lo;
+  err = x * 2.0 * xnlo;                 /* n = 4: no odd bit */
+  x2 = x * x; xnlo = fma(x, x, -x2); xnlo += err;
+  err = x2 * 2.0 * xnlo;                /* n = 2 */
+  x4 = x2 * x2; lo = fma(x2, x2, -x4); xnlo = lo + err;
+  err = xnlo;                           /* muladd(1.0, xnlo, x4*0.0) */
+  if (isfinite(x4) && isfinite(err)) return x4 + err;  /* muladd(x4, 1.0, err) */
+  return x4;
+}
+
+#define IX(p, c, jj, ld) ((p)[(int64_t)(c) + ((int64_t)(jj) - 1) * (int64_t)(ld)])
+
+/* ===================================================================== */
+/* Dense pivoted Gaussian elimination — _batched_band_solve_kernel!       */
+/* band_diagonal.jl:87-170, one column.  A is n x n row-major scratch.    */
+/* ===================================================================== */
+static void dense_band_solve_col(double* tvector_col /* 1-based via offset */, int64_t ldt,
+                                 const double* bmatrix, int64_t ldb, int nlev,
+                                 const double* rvector, int64_t ldr, int64_t c,
+                                 int jt, int n, int kl, int ku)
+{
+  double A[ORC_MAXL * ORC_MAXL];
+  double x[ORC_MAXL];
+  const int nband = kl + ku + 1;
+  (void)nband;
+  for (int j = 1; j <= n; j++)
+    for (int i = 1; i <= n; i++) A[(i - 1) * n + (j - 1)] = 0.0;
+  for (int j = 1; j <= n; j++) {
+    int ilo = j - kl > 1 ? j - kl : 1;
+    int ihi = j + ku < n ? j + ku : n;
+    for (int i = ilo; i <= ihi; i++) {
+      int band = (i - j) + kl + 1;              /* 1-based band */
+      int lev = jt + i - 1;                     /* 1-based level */
+      A[(i - 1) * n + (j - 1)] = bmatrix[c + (int64_t)(band - 1) * ldb + (int64_t)(lev - 1) * ldb * (kl + ku + 1)];
+    }
+  }
+  for (int i = 1; i <= n; i++) x[i - 1] = rvector[c + (int64_t)(jt + i - 2) * ldr];
+#define AA(i, j) A[((i) - 1) * n + ((j) - 1)]
+  for (int k = 1; k <= n - 1; k++) {
+    int piv = k;
+    double maxv = fabs(AA(k, k));
+    for (int i = k + 1; i <= n; i++) {
+      double v = fabs(AA(i, k));
+      if (v > maxv) { maxv = v; piv = i; }
+    }
+    double akk = AA(piv, k);
+    if (piv != k) {
+      for (int j = k; j <= n; j++) {
+        double akj = AA(k, j), apj = AA(piv, j);
+        AA(k, j) = apj; AA(piv, j) = akj;
+      }
+      double xk = x[k - 1], xp = x[piv - 1];
+      x[k - 1] = xp; x[piv - 1] = xk;
+    }
+    for (int i = k + 1; i <= n; i++) {
+      double f = AA(i, k) / akk;
+      for (int j = k; j <= n; j++) AA(i, j) = AA(i, j) - f * AA(k, j);
+      x[i - 1] = x[i - 1] - f * x[k - 1];
+    }
+  }
+  for (int i = n; i >= 1; i--) {
+    double s = x[i - 1];
+    for (int j = i + 1; j <= n; j++) s = s - AA(i, j) * x[j - 1];
+    x[i - 1] = s / AA(i, i);
+  }
+#undef AA
+  for (int i = 1; i <= n; i++) tvector_col[c + (int64_t)(jt + i - 2) * ldt] = x[i - 1];
+  (void)nlev;
+}
+
+/* batched_band_solve! (band_diagonal.jl:179-189). bmatrix [ld, nband, nlev]. */
+int orc_batched_band_solve(int64_t nc, int64_t ld, int32_t nlev, double* tvector,
+                           const double* bmatrix, const double* rvector,
+                           const int64_t* jtop, const int64_t* jbot, const uint8_t* mask,
+                           int32_t kl, int32_t ku, int32_t nlevsno_off, int32_t nthreads)
+{
+  if (nlev > ORC_MAXL) return CLMGB_ERR_DIMS;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t c = 0; c < nc; c++) {
+    if (!mask[c]) continue;
+    int jt = (int)(jtop[c] + nlevsno_off + 1);
+    int n = (int)(jbot[c] - jtop[c] + 1);
+    if (n > 0) dense_band_solve_col(tvector, ld, bmatrix, ld, nlev, rvector, ld, c, jt, n, kl, ku);
+  }
+  return 0;
+}
+
+/* tridiagonal_solve! (tridiagonal.jl:35-63), single column, no pivot guard. */
+void orc_tridiagonal_solve(double* u, const double* a, const double* b, const double* c,
+                           const double* r, int32_t jtop, int32_t nlevs)
+{
+  double cp[ORC_MAXL + 1], dp[ORC_MAXL + 1];
+  int j = jtop;
+  cp[j] = c[j - 1] / b[j - 1];
+  dp[j] = r[j - 1] / b[j - 1];
+  for (int jj = j + 1; jj <= nlevs; jj++) {
+    double denom = b[jj - 1] - a[jj - 1] * cp[jj - 1];
+    cp[jj] = c[jj - 1] / denom;
+    dp[jj] = (r[jj - 1] - a[jj - 1] * dp[jj - 1]) / denom;
+  }
+  u[nlevs - 1] = dp[nlevs];
+  for (int jj = nlevs - 1; jj >= j; jj--) u[jj - 1] = dp[jj] - cp[jj] * u[jj];
+}
+
+/* _tridiag_multi_kernel! (tridiagonal.jl:86-127): [ld, nlevs] matrices, 1e-30 guard. */
+int orc_tridiagonal_multi(int64_t ncols, int64_t ld, int32_t nlevs, double* u,
+                          const double* a, const double* b, const double* c, const double* r,
+                          const int64_t* jtop, const uint8_t* mask, int32_t nthreads)
+{
+  if (nlevs > ORC_MAXL) return CLMGB_ERR_DIMS;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t col = 0; col < ncols; col++) {
+    if (!mask[col]) continue;
+    double cpv[ORC_MAXL + 1], dpv[ORC_MAXL + 1];
+    int j = (int)jtop[col];
+    const double tiny = 1e-30;
+    double bet = IX(b, col, j, ld);
+    if (fabs(bet) < tiny) bet = tiny;
+    double cp_prev = IX(c, col, j, ld) / bet;
+    double dp_prev = IX(r, col, j, ld) / bet;
+    cpv[j] = cp_prev; dpv[j] = dp_prev;
+    for (int jj = j + 1; jj <= nlevs; jj++) {
+      double denom = IX(b, col, jj, ld) - IX(a, col, jj, ld) * cp_prev;
+      if (fabs(denom) < tiny) denom = copysign(tiny, denom == 0.0 ? 1.0 : denom);
+      cp_prev = IX(c, col, jj, ld) / denom;
+      dp_prev = (IX(r, col, jj, ld) - IX(a, col, jj, ld) * dp_prev) / denom;
+      cpv[jj] = cp_prev; dpv[jj] = dp_prev;
+    }
+    double u_next = dp_prev;
+    IX(u, col, nlevs, ld) = u_next;
+    for (int jj = nlevs - 1; jj >= j; jj--) {
+      u_next = dpv[jj] - cpv[jj] * u_next;
+      IX(u, col, jj, ld) = u_next;
+    }
+  }
+  return 0;
+}
+
+/* tridiagonal_col! (soil_water_movement.jl:736-773), gam form, 1-based arrays via lbj. */
+void orc_tridiagonal_col(double* u, const double* a, const double* b, const double* c,
+                         const double* r, int32_t jtop, int32_t lbj, int32_t ubj)
+{
+  double gam[ORC_MAXL + 2];
+  for (int j = 0; j < ORC_MAXL + 2; j++) gam[j] = 0.0;
+#define V(arr, j) arr[(j) - lbj]
+  double bet = V(b, jtop);
+  if (fabs(bet) < 1.0e-30) bet = 1.0e-30;
+  for (int j = lbj; j <= ubj; j++) {
+    if (j >= jtop) {
+      if (j == jtop) {
+        V(u, j) = V(r, j) / bet;
+      } else {
+        gam[j - lbj] = V(c, j - 1) / bet;
+        bet = V(b, j) - V(a, j) * gam[j - lbj];
+        if (fabs(bet) < 1.0e-30) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
+        V(u, j) = (V(r, j) - V(a, j) * V(u, j - 1)) / bet;
+      }
+    }
+  }
+  for (int j = ubj - 1; j >= lbj; j--)
+    if (j >= jtop) V(u, j) = V(u, j) - gam[j + 1 - lbj] * V(u, j + 1);
+#undef V
+}
+
+/* ice_impedance (soil_water_movement.jl:722-724). */
+double orc_ice_impedance(double icefrac, double e_ice) { return pow(10.0, -e_ice * icefrac); }
+
+/* ===================================================================== */
+/* soil_temperature! for one column (non-urban subset).                   */
+/* ===================================================================== */
+typedef struct {
+  const clmgb_varpar* vp;
+  const clmgb_bounds* b;
+  const clmgb_soiltemp_fields* f;
+  double dtime;
+  int snow_method;
+} st_ctx;
+
+static int col_is_wallroof(int64_t it) { return it == ICOL_SUNWALL || it == ICOL_SHADEWALL || it == ICOL_ROOF; }
+
+/* phase_change_h2osfc kernel body (soil_temperature.jl:1757-1855) for column c. */
+static void pc_h2osfc_col(const clmgb_varpar* vp, const clmgb_bounds* bd,
+                          const clmgb_soiltemp_fields* f, int64_t c, double dtime,
+                          const double* dhsdT)
+{
+  const int64_t ld = bd->ldc;
+  const int joff = vp->nlevsno;
+  const int64_t snl = f->col_snl[c];
+  double* t = f->t_soisno;
+  f->xmf_h2osfc[c] = 0.0;
+  f->qflx_h2osfc_to_ice[c] = 0.0;
+  f->eflx_h2osfc_to_snow[c] = 0.0;
+  if (f->frac_h2osfc[c] > 0.0 && f->t_h2osfc[c] <= TFRZ) {
+    double tinc = TFRZ - f->t_h2osfc[c];
+    f->t_h2osfc[c] = TFRZ;
+    double fh = f->frac_h2osfc[c];
+    double ch = f->c_h2osfc[c];
+    double hm = fh * (dhsdT[c] * tinc - tinc * ch / dtime);
+    double xm = hm * dtime / HFUS;
+    double temp1 = f->h2osfc[c] + xm;
+    double h2osno_total = f->h2osno_no_layers[c];
+    if (snl < 0)
+      for (int64_t j = snl + 1; j <= 0; j++)
+        h2osno_total += IX(f->h2osoi_ice, c, j + joff, ld) + IX(f->h2osoi_liq, c, j + joff, ld);
+    double fs = f->frac_sno_eff[c];
+    double z_avg = fs * f->snow_depth[c];
+    double rho_avg = z_avg > 0.0 ? jl_min(800.0, h2osno_total / z_avg) : 200.0;
+    if (temp1 >= 0.0) {
+      f->int_snow[c] -= xm;
+      if (snl == 0) f->h2osno_no_layers[c] -= xm;
+      else IX(f->h2osoi_ice, c, joff, ld) -= xm;
+      h2osno_total -= xm;
+      f->h2osfc[c] += xm;
+      f->xmf_h2osfc[c] = hm;
+      f->qflx_h2osfc_to_ice[c] = -xm / dtime;
+      if (fs > 0.0 && snl < 0) f->snow_depth[c] = h2osno_total / (rho_avg * fs);
+      else f->snow_depth[c] = h2osno_total / DENICE;
+      if (snl == 0) {
+        IX(t, c, joff, ld) = f->t_h2osfc[c];
+        f->eflx_h2osfc_to_snow[c] = 0.0;
+      } else {
+        double c1;
+        if (snl == -1) c1 = fs * (dtime / IX(f->fact, c, joff, ld) - dhsdT[c] * dtime);
+        else c1 = fs / IX(f->fact, c, joff, ld) * dtime;
+        double c2 = fh != 0.0 ? (-CPLIQ * xm - fh * dhsdT[c] * dtime) : 0.0;
+        IX(t, c, joff, ld) = (c1 * IX(t, c, joff, ld) + c2 * f->t_h2osfc[c]) / (c1 + c2);
+        f->eflx_h2osfc_to_snow[c] = (f->t_h2osfc[c] - IX(t, c, joff, ld)) * c2 / dtime;
+      }
+    } else {
+      rho_avg = (h2osno_total * rho_avg + f->h2osfc[c] * DENICE) / (h2osno_total + f->h2osfc[c]);
+      f->int_snow[c] += f->h2osfc[c];
+      if (snl == 0) f->h2osno_no_layers[c] += f->h2osfc[c];
+      else IX(f->h2osoi_ice, c, joff, ld) += f->h2osfc[c];
+      h2osno_total += f->h2osfc[c];
+      f->qflx_h2osfc_to_ice[c] = f->h2osfc[c] / dtime;
+      f->t_h2osfc[c] -= temp1 * HFUS / (dtime * dhsdT[c] - ch);
+      f->xmf_h2osfc[c] = hm - fh * temp1 * HFUS / dtime;
+      if (snl == 0) {
+        IX(t, c, joff, ld) = f->t_h2osfc[c];
+      } else {
+        double c1;
+        if (snl == -1) c1 = fs * (dtime / IX(f->fact, c, joff, ld) - dhsdT[c] * dtime);
+        else c1 = fs / IX(f->fact, c, joff, ld) * dtime;
+        double c2 = fh != 0.0 ? fh * (ch - dtime * dhsdT[c]) : 0.0;
+        IX(t, c, joff, ld) = (c1 * IX(t, c, joff, ld) + c2 * f->t_h2osfc[c]) / (c1 + c2);
+        f->t_h2osfc[c] = IX(t, c, joff, ld);
+      }
+      f->h2osfc[c] = 0.0;
+      if (fs > 0.0 && snl < 0) f->snow_depth[c] = h2osno_total / (rho_avg * fs);
+      else f->snow_depth[c] = h2osno_total / DENICE;
+    }
+  }
+}
+
+/* phase_change_beta kernel body (soil_temperature.jl:1929-2230), hard (Float64) path. */
+static void pc_beta_col(const clmgb_varpar* vp, const clmgb_bounds* bd,
+                        const clmgb_soiltemp_fields* f, int64_t c, double dtime,
+                        const double* dhsdT)
+{
+  const int64_t ld = bd->ldc;
+  const int nlevsno = vp->nlevsno, nlevgrnd = vp->nlevgrnd, nlevurb = vp->nlevurb;
+  const int nlevmaxurbgrnd = vp->nlevmaxurbgrnd;
+  const int joff = nlevsno;
+  const int64_t snl = f->col_snl[c];
+  const int64_t l = f->col_landunit[c] - 1;
+  const int64_t it = f->col_itype[c];
+  const int64_t lit = f->lun_itype[l];
+  const int wallroof = col_is_wallroof(it);
+  double hm[ORC_MAXL + 1], xm[ORC_MAXL + 1], xm2[ORC_MAXL + 1], wice0[ORC_MAXL + 1];
+  double wliq0[ORC_MAXL + 1], wexice0[ORC_MAXL + 1], wmass0[ORC_MAXL + 1], tinc[ORC_MAXL + 1];
+  double supercool[ORC_MAXL + 1];
+  for (int k = 0; k <= ORC_MAXL; k++) {
+    hm[k] = xm[k] = xm2[k] = wice0[k] = wliq0[k] = wexice0[k] = wmass0[k] = tinc[k] = 0.0;
+    supercool[k] = 0.0;
+  }
+  double* T = f->t_soisno;
+  double* ICE = f->h2osoi_ice;
+  double* LIQ = f->h2osoi_liq;
+  double* EXI = f->excess_ice;
+  const double fse = f->frac_sno_eff[c];
+  const double fh = f->frac_h2osfc[c];
+
+  f->xmf[c] = 0.0;
+  f->qflx_snomelt[c] = 0.0;
+  f->qflx_snofrz[c] = 0.0;
+  f->qflx_snow_drain[c] = 0.0;
+
+  for (int j = -nlevsno + 1; j <= nlevmaxurbgrnd; j++) {
+    int jj = j + joff;
+    if (j >= snl + 1) {
+      IX(f->imelt, c, jj, ld) = 0;
+      hm[jj] = 0.0; xm[jj] = 0.0; xm2[jj] = 0.0;
+      wice0[jj] = IX(ICE, c, jj, ld);
+      wliq0[jj] = IX(LIQ, c, jj, ld);
+      wexice0[jj] = j >= 1 ? IX(EXI, c, j, ld) : 0.0;
+      wmass0[jj] = IX(ICE, c, jj, ld) + IX(LIQ, c, jj, ld) + wexice0[jj];
+      if (j >= 1) IX(f->exice_subs, c, j, ld) = 0.0;
+    }
+    if (j <= 0) {
+      IX(f->qflx_snomelt_lyr, c, jj, ld) = 0.0;
+      IX(f->qflx_snofrz_lyr, c, jj, ld) = 0.0;
+    }
+  }
+  /* snow layers: melting / freezing identification (hard default) */
+  for (int j = -nlevsno + 1; j <= 0; j++) {
+    int jj = j + joff;
+    if (j >= snl + 1) {
+      if (IX(ICE, c, jj, ld) > 0.0 && IX(T, c, jj, ld) > TFRZ) {
+        IX(f->imelt, c, jj, ld) = 1;
+        tinc[jj] = TFRZ - IX(T, c, jj, ld);
+        IX(T, c, jj, ld) = TFRZ;
+      }
+      if (IX(LIQ, c, jj, ld) > 0.0 && IX(T, c, jj, ld) < TFRZ) {
+        IX(f->imelt, c, jj, ld) = 2;
+        tinc[jj] = TFRZ - IX(T, c, jj, ld);
+        IX(T, c, jj, ld) = TFRZ;
+      }
+    }
+  }
+  /* soil layers */
+  for (int j = 1; j <= nlevmaxurbgrnd; j++) {
+    int jj = j + joff;
+    supercool[j] = 0.0;
+    int active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= nlevurb);
+    if (active) {
+      if (IX(ICE, c, jj, ld) > 0.0 && IX(T, c, jj, ld) > TFRZ) {
+        IX(f->imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - IX(T, c, jj, ld); IX(T, c, jj, ld) = TFRZ;
+      }
+      if (IX(EXI, c, j, ld) > 0.0 && IX(T, c, jj, ld) > TFRZ) {
+        IX(f->imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - IX(T, c, jj, ld); IX(T, c, jj, ld) = TFRZ;
+      }
+      supercool[j] = 0.0;
+      if (lit == ISTSOIL || lit == ISTCROP || it == ICOL_ROAD_PERV) {
+        if (IX(T, c, jj, ld) < TFRZ) {
+          double tt = IX(T, c, jj, ld);
+          double smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
+          supercool[j] = IX(f->watsat, c, j, ld) * pow(smp / IX(f->sucsat, c, j, ld), -1.0 / IX(f->bsw, c, j, ld));
+          supercool[j] *= IX(f->dz, c, jj, ld) * 1000.0;
+        }
+      }
+      if (IX(LIQ, c, jj, ld) > supercool[j] && IX(T, c, jj, ld) < TFRZ) {
+        IX(f->imelt, c, jj, ld) = 2; tinc[jj] = TFRZ - IX(T, c, jj, ld); IX(T, c, jj, ld) = TFRZ;
+      }
+      if (f->h2osno_no_layers[c] > 0.0 && j == 1) {
+        if (IX(T, c, jj, ld) > TFRZ) {
+          IX(f->imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - IX(T, c, jj, ld); IX(T, c, jj, ld) = TFRZ;
+        }
+      }
+    }
+  }
+  /* energy surplus / loss and rate of phase change */
+  for (int j = -nlevsno + 1; j <= nlevmaxurbgrnd; j++) {
+    int jj = j + joff;
+    int active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= nlevurb);
+    if (!(active && j >= snl + 1)) continue;
+    int64_t* im = &IX(f->imelt, c, jj, ld);
+    const double fct = IX(f->fact, c, jj, ld);
+    if (*im > 0) {
+      if (j == snl + 1) {
+        if (j > 0) hm[jj] = dhsdT[c] * tinc[jj] - tinc[jj] / fct;
+        else hm[jj] = fse * (dhsdT[c] * tinc[jj] - tinc[jj] / fct);
+        if (j == 1 && fh != 0.0) hm[jj] -= fh * dhsdT[c] * tinc[jj];
+      } else if (j == 1) {
+        hm[jj] = (1.0 - fse - fh) * dhsdT[c] * tinc[jj] - tinc[jj] / fct;
+      } else {
+        if (j < 1) hm[jj] = -fse * tinc[jj] / fct;
+        else hm[jj] = -tinc[jj] / fct;
+      }
+    }
+    if (*im == 1 && hm[jj] < 0.0) { hm[jj] = 0.0; *im = 0; }
+    if (*im == 2 && hm[jj] > 0.0) { hm[jj] = 0.0; *im = 0; }
+    if (*im > 0 && fabs(hm[jj]) > 0.0) {
+      xm[jj] = hm[jj] * dtime / HFUS;
+      if (j == 1) {
+        if (f->h2osno_no_layers[c] > 0.0 && xm[jj] > 0.0) {
+          double temp1 = f->h2osno_no_layers[c];
+          f->h2osno_no_layers[c] = jl_max(0.0, temp1 - xm[jj]);
+          double propor = f->h2osno_no_layers[c] / temp1;
+          f->snow_depth[c] = propor * f->snow_depth[c];
+          double heatr0 = hm[jj] - HFUS * (temp1 - f->h2osno_no_layers[c]) / dtime;
+          if (heatr0 > 0.0) { xm[jj] = heatr0 * dtime / HFUS; hm[jj] = heatr0; }
+          else { xm[jj] = 0.0; hm[jj] = 0.0; }
+          f->qflx_snomelt[c] = jl_max(0.0, temp1 - f->h2osno_no_layers[c]) / dtime;
+          f->xmf[c] = HFUS * f->qflx_snomelt[c];
+          f->qflx_snow_drain[c] = f->qflx_snomelt[c];
+        }
+      }
+      double heatr = 0.0;
+      if (xm[jj] > 0.0) {
+        IX(ICE, c, jj, ld) = jl_max(0.0, wice0[jj] - xm[jj]);
+        heatr = hm[jj] - HFUS * (wice0[jj] - IX(ICE, c, jj, ld)) / dtime;
+        xm2[jj] = xm[jj] - IX(ICE, c, jj, ld);
+        if (IX(ICE, c, jj, ld) == 0.0) {
+          if (wexice0[jj] >= 0.0 && xm2[jj] > 0.0 && j >= 2) {
+            IX(EXI, c, j, ld) = jl_max(0.0, wexice0[jj] - xm2[jj]);
+            heatr = hm[jj] - HFUS * (wexice0[jj] - IX(EXI, c, j, ld) + wice0[jj] - IX(ICE, c, jj, ld)) / dtime;
+          }
+        }
+      } else if (xm[jj] < 0.0) {
+        if (j <= 0) {
+          IX(ICE, c, jj, ld) = jl_min(wmass0[jj], wice0[jj] - xm[jj]);
+        } else {
+          if (wmass0[jj] - wexice0[jj] < supercool[j]) IX(ICE, c, jj, ld) = 0.0;
+          else IX(ICE, c, jj, ld) = jl_min(wmass0[jj] - wexice0[jj] - supercool[j], wice0[jj] - xm[jj]);
+        }
+        heatr = hm[jj] - HFUS * (wice0[jj] - IX(ICE, c, jj, ld)) / dtime;
+      }
+      double ei_val = j >= 1 ? IX(EXI, c, j, ld) : 0.0;
+      IX(LIQ, c, jj, ld) = jl_max(0.0, wmass0[jj] - IX(ICE, c, jj, ld) - ei_val);
+      if (fabs(heatr) > 0.0) {
+        double* tp = &IX(T, c, jj, ld);
+        if (j == snl + 1) {
+          if (j == 1) {
+            *tp += fct * heatr / (1.0 - (1.0 - fh) * fct * dhsdT[c]);
+          } else {
+            if (fse > 0.0) *tp += (fct / fse) * heatr / (1.0 - fct * dhsdT[c]);
+          }
+        } else if (j == 1) {
+          *tp += fct * heatr / (1.0 - (1.0 - fse - fh) * fct * dhsdT[c]);
+        } else {
+          if (j > 0) *tp += fct * heatr;
+          else if (fse > 0.0) *tp += (fct / fse) * heatr;
+        }
+        if (j <= 0)
+          if (IX(LIQ, c, jj, ld) * IX(ICE, c, jj, ld) > 0.0) *tp = TFRZ;
+      }
+      if (j >= 1) {
+        f->xmf[c] += HFUS * (wice0[jj] - IX(ICE, c, jj, ld)) / dtime +
+                     HFUS * (wexice0[jj] - IX(EXI, c, j, ld)) / dtime;
+        IX(f->exice_subs, c, j, ld) = jl_max(0.0, (wexice0[jj] - IX(EXI, c, j, ld)) / DENICE);
+      } else {
+        f->xmf[c] += HFUS * (wice0[jj] - IX(ICE, c, jj, ld)) / dtime;
+      }
+      if (*im == 1 && j < 1) {
+        double q = jl_max(0.0, wice0[jj] - IX(ICE, c, jj, ld)) / dtime;
+        IX(f->qflx_snomelt_lyr, c, jj, ld) = q;
+        f->qflx_snomelt[c] += q;
+        f->snomelt_accum[c] += q * dtime * 1.0e-3;
+      }
+      if (*im == 2 && j < 1) {
+        double q = jl_max(0.0, IX(ICE, c, jj, ld) - wice0[jj]) / dtime;
+        IX(f->qflx_snofrz_lyr, c, jj, ld) = q;
+        f->qflx_snofrz[c] += q;
+      }
+    }
+  }
+  f->eflx_snomelt[c] = f->qflx_snomelt[c] * HFUS;
+  if (f->lun_urbpoi[l]) f->eflx_snomelt_u[c] = f->eflx_snomelt[c];
+  else if (lit == ISTSOIL || lit == ISTCROP) f->eflx_snomelt_r[c] = f->eflx_snomelt[c];
+  (void)wliq0;
+}
+
+/* Full soil_temperature! on one non-urban column.  Returns a CLMGB_COL_* bit set. */
+static uint32_t soiltemp_col(const st_ctx* X, int64_t c)
+{
+  const clmgb_varpar* vp = X->vp;
+  const clmgb_soiltemp_fields* f = X->f;
+  const int64_t ld = X->b->ldc, ldp = X->b->ldp;
+  const double dtime = X->dtime;
+  const int nlevsno = vp->nlevsno, nlevgrnd = vp->nlevgrnd, nlevsoi = vp->nlevsoi;
+  const int nlevmaxurbgrnd = vp->nlevmaxurbgrnd;
+  const int joff = nlevsno;
+  const int nlev = nlevsno + nlevmaxurbgrnd;
+  const int nlev_total = nlevsno + 1 + nlevmaxurbgrnd;
+  if (!f->mask_nolakec[c]) return 0;
+  const int64_t snl = f->col_snl[c];
+  const int64_t l = f->col_landunit[c] - 1;
+  const int64_t it = f->col_itype[c];
+  const int64_t lit = f->lun_itype[l];
+  if (f->lun_urbpoi[l] || col_is_wallroof(it) || it == ICOL_ROAD_IMPERV || it == ICOL_ROAD_PERV)
+    return CLMGB_COL_URBAN;
+
+  double tk[ORC_MAXL + 2], cv[ORC_MAXL + 2], fn[ORC_MAXL + 2], fn1[ORC_MAXL + 2];
+  for (int k = 0; k < ORC_MAXL + 2; k++) tk[k] = cv[k] = fn[k] = fn1[k] = 0.0;
+  double tk_h2osfc = NAN;
+  double hs_top = 0.0, hs_soil = 0.0, hs_top_snow = 0.0, hs_h2osfc = 0.0, hs = 0.0;
+  double dhsdT_c = 0.0;
+  double sabg_lyr_col[ORC_MAXL + 2];
+  for (int k = 0; k < ORC_MAXL + 2; k++) sabg_lyr_col[k] = 0.0;
+  double fn_h2osfc = 0.0, dz_h2osfc = 0.0;
+  /* bmatrix[band][lev], tvector/rvector 1-based over nlev_total */
+  double bmat[5][ORC_MAXL + 2];
+  double tvec[ORC_MAXL + 2], rvec[ORC_MAXL + 2];
+  for (int k = 0; k < ORC_MAXL + 2; k++) {
+    for (int bb = 0; bb < 5; bb++) bmat[bb][k] = 0.0;
+    tvec[k] = NAN; rvec[k] = NAN;
+  }
+  double* T = f->t_soisno;
+  const double* DZ = f->dz;
+  const double* Z = f->z;
+  const double* ZI = f->zi;
+  double* LIQ = f->h2osoi_liq;
+  double* ICE = f->h2osoi_ice;
+  const double* EXI = f->excess_ice;
+  const int is_special = (lit == ISTWET || lit == ISTICE);
+  const int64_t nbedrock = f->col_nbedrock[c];
+  const double fse = f->frac_sno_eff[c];
+  const double fh = f->frac_h2osfc[c];
+
+  /* ---- soil_therm_prop!: layer conductivity (_soil_snow_tk_kernel!) ---- */
+  for (int jj = 1; jj <= nlevsno + nlevgrnd; jj++) {
+    int j = jj - nlevsno;
+    if (j >= 1) {
+      if (!is_special) {
+        double liq = IX(LIQ, c, jj, ld), ice = IX(ICE, c, jj, ld), exi = IX(EXI, c, j, ld);
+        double dzv = IX(DZ, c, jj, ld), ws = IX(f->watsat, c, j, ld);
+        double satw = (liq / DENH2O + ice / DENICE + exi / DENICE) / (dzv * ws);
+        satw = jl_min(1.0, satw);
+        double thkv;
+        if (satw > 1.0e-7) {
+          double dke;
+          if (IX(T, c, jj, ld) >= TFRZ) dke = jl_max(0.0, log10(satw) + 1.0);
+          else dke = satw;
+          double fl_denom = liq / (DENH2O * dzv) + ice / (DENICE * dzv) + exi / (DENICE * dzv);
+          double fl = (liq / (DENH2O * dzv)) / fl_denom;
+          double dksat = IX(f->tkmg, c, j, ld) * pow(TKWAT, fl * ws) * pow(TKICE, (1.0 - fl) * ws);
+          thkv = dke * dksat + (1.0 - dke) * IX(f->tkdry, c, j, ld);
+        } else {
+          thkv = IX(f->tkdry, c, j, ld);
+        }
+        if (j > nbedrock) thkv = THK_BEDROCK;
+        IX(f->thk, c, jj, ld) = thkv;
+      } else if (lit == ISTICE) {
+        IX(f->thk, c, jj, ld) = IX(T, c, jj, ld) < TFRZ ? TKICE : TKWAT;
+      } else if (lit == ISTWET) {
+        if (j > nlevsoi) IX(f->thk, c, jj, ld) = THK_BEDROCK;
+        else IX(f->thk, c, jj, ld) = IX(T, c, jj, ld) < TFRZ ? TKICE : TKWAT;
+      }
+    }
+    if (snl + 1 < 1 && j >= snl + 1 && j <= 0) {
+      double denom = jl_max(fse, 1.0e-6) * jl_max(IX(DZ, c, jj, ld), 1.0e-6);
+      double bwv = (IX(ICE, c, jj, ld) + IX(LIQ, c, jj, ld)) / denom;
+      IX(f->bw, c, jj, ld) = bwv;
+      if (X->snow_method == CLMGB_SNOW_JORDAN1991) {
+        IX(f->thk, c, jj, ld) = TKAIR + (7.75e-5 * bwv + 1.105e-6 * (bwv * bwv)) * (TKICE - TKAIR);
+      } else {
+        if (bwv <= 156.0) IX(f->thk, c, jj, ld) = 0.023 + 0.234 * (bwv / 1000.0);
+        else IX(f->thk, c, jj, ld) = 0.138 - 1.01 * (bwv / 1000.0) + 3.233 * ((bwv / 1000.0) * (bwv / 1000.0));
+      }
+    }
+  }
+  /* interface conductivity (_soil_tk_interface_kernel!) */
+  for (int jj = 1; jj <= nlev; jj++) {
+    int j = jj - nlevsno;
+    if (j >= snl + 1 && j <= nlevgrnd - 1) {
+      double tkj = IX(f->thk, c, jj, ld), tkj1 = IX(f->thk, c, jj + 1, ld);
+      double zj = IX(Z, c, jj, ld), zj1 = IX(Z, c, jj + 1, ld), zij1 = IX(ZI, c, jj + 1, ld);
+      tk[jj] = tkj * tkj1 * (zj1 - zj) / (tkj * (zj1 - zij1) + tkj1 * (zij1 - zj));
+    } else if (j == nlevgrnd) {
+      tk[jj] = 0.0;
+    }
+  }
+  /* _tk_h2osfc_kernel! */
+  {
+    double zh2osfc = 1.0e-3 * (0.5 * f->h2osfc[c]);
+    double z1 = IX(Z, c, 1 + joff, ld), tk1 = IX(f->thk, c, 1 + joff, ld);
+    double denom = TKWAT * z1 + tk1 * zh2osfc;
+    tk_h2osfc = denom > 0.0 ? TKWAT * tk1 * (z1 + zh2osfc) / denom : tk1;
+  }
+  /* _soil_cv_kernel! */
+  for (int j = 1; j <= nlevgrnd; j++) {
+    int jj = j + nlevsno;
+    double dzv = IX(DZ, c, jj, ld);
+    if (!is_special) {
+      cv[jj] = IX(f->csol, c, j, ld) * (1.0 - IX(f->watsat, c, j, ld)) * dzv +
+               (IX(ICE, c, jj, ld) * CPICE + IX(LIQ, c, jj, ld) * CPLIQ) + IX(EXI, c, j, ld) * CPICE;
+      if (j > nbedrock) cv[jj] = CSOL_BEDROCK * dzv;
+    } else {
+      cv[jj] = IX(ICE, c, jj, ld) * CPICE + IX(LIQ, c, jj, ld) * CPLIQ;
+      if (j > nbedrock) cv[jj] = CSOL_BEDROCK * dzv;
+    }
+  }
+  /* _unresolved_snow_cv_kernel! */
+  if (f->h2osno_no_layers[c] > 0.0) cv[1 + joff] += CPICE * f->h2osno_no_layers[c];
+  /* _snow_cv_kernel! */
+  for (int jj = 1; jj <= nlevsno; jj++) {
+    int j = jj - nlevsno;
+    if (snl + 1 < 1 && j >= snl + 1) {
+      if (fse > 0.0)
+        cv[jj] = jl_max(THIN_SFCLAYER, (CPLIQ * IX(LIQ, c, jj, ld) + CPICE * IX(ICE, c, jj, ld)) / fse);
+      else
+        cv[jj] = THIN_SFCLAYER;
+    }
+  }
+
+  /* ---- compute_ground_heat_flux_and_deriv! ---- */
+  const double eg = f->emg[c];
+  const double tg = f->t_grnd[c];
+  const double lwrad_emit = eg * SB * jl_pow4(tg);
+  const double dlwrad_emit = 4.0 * eg * SB * (tg * tg * tg);
+  const double lwrad_emit_snow = eg * SB * jl_pow4(IX(T, c, snl + 1 + joff, ld));
+  const double lwrad_emit_soil = eg * SB * jl_pow4(IX(T, c, 1 + joff, ld));
+  const double lwrad_emit_h2osfc = eg * SB * jl_pow4(f->t_h2osfc[c]);
+  const double htvp = f->htvp[c];
+  const double forc = f->forc_lwrad[c];
+  const int64_t pi = f->col_patchi[c], pf = f->col_patchf[c];
+  uint32_t status = 0;
+  if (pi < 1 || pf > X->b->np || pf < pi - 1) return CLMGB_COL_PATCH_RANGE;
+  /* rural gnet + contributions, scattered in ascending patch order */
+  for (int64_t p1 = pi; p1 <= pf; p1++) {
+    int64_t p = p1 - 1;
+    if (f->patch_column[p] != c + 1) continue;
+    double hs_p = 0.0, dh_p = 0.0, hsoil_p = 0.0, hh_p = 0.0;
+    if (f->mask_nolakep[p] && !f->lun_urbpoi[f->patch_landunit[p] - 1]) {
+      double base = f->dlrad[p] + (1.0 - (double)f->frac_veg_nosno[p]) * eg * forc;
+      f->eflx_gnet[p] = f->sabg[p] + base - lwrad_emit - (f->eflx_sh_grnd[p] + f->qflx_evap_soi[p] * htvp);
+      f->sabg_chk[p] = fse * f->sabg_snow[p] + (1.0 - fse) * f->sabg_soil[p];
+      f->dgnetdT[p] = -f->cgrnd[p] - dlwrad_emit;
+      double wt = f->patch_wtcol[p];
+      double gsoil = f->sabg_soil[p] + base - lwrad_emit_soil - (f->eflx_sh_soil[p] + f->qflx_ev_soil[p] * htvp);
+      double gh2o = f->sabg_soil[p] + base - lwrad_emit_h2osfc - (f->eflx_sh_h2osfc[p] + f->qflx_ev_h2osfc[p] * htvp);
+      int wnz = wt != 0.0;
+      hs_p = wnz ? f->eflx_gnet[p] * wt : 0.0;
+      dh_p = wnz ? f->dgnetdT[p] * wt : 0.0;
+      hsoil_p = wnz ? gsoil * wt : 0.0;
+      hh_p = wnz ? gh2o * wt : 0.0;
+    }
+    hs += hs_p; dhsdT_c += dh_p; hs_soil += hsoil_p; hs_h2osfc += hh_p;
+  }
+  /* SNICAR top-layer flux + per-layer solar */
+  for (int64_t p1 = pi; p1 <= pf; p1++) {
+    int64_t p = p1 - 1;
+    if (f->patch_column[p] != c + 1) continue;
+    if (!f->mask_nolakep[p]) continue;
+    double wt = f->patch_wtcol[p];
+    int64_t lyr_top = snl + 1;
+    double base = f->dlrad[p] + (1.0 - (double)f->frac_veg_nosno[p]) * eg * forc;
+    double sab = IX(f->sabg_lyr, p, lyr_top + joff, ldp);
+    double gtop = sab + base - lwrad_emit - (f->eflx_sh_grnd[p] + f->qflx_evap_soi[p] * htvp);
+    hs_top += gtop * wt;
+    double gsnow = sab + base - lwrad_emit_snow - (f->eflx_sh_snow[p] + f->qflx_ev_snow[p] * htvp);
+    hs_top_snow += gsnow * wt;
+    for (int64_t j = lyr_top; j <= 1; j++)
+      sabg_lyr_col[j + nlevsno] += IX(f->sabg_lyr, p, j + joff, ldp) * wt;
+  }
+  (void)hs; (void)hs_top;
+
+  /* ---- compute_heat_diff_flux_and_factor! (_heat_diff_kernel!) ---- */
+  for (int jj = 1; jj <= nlev; jj++) {
+    int j = jj - nlevsno;
+    if (j <= nlevgrnd && j >= snl + 1) {
+      double* fc = &IX(f->fact, c, jj, ld);
+      if (j == snl + 1) {
+        *fc = dtime / cv[jj] * IX(DZ, c, jj, ld) /
+              (0.5 * (IX(Z, c, jj, ld) - IX(ZI, c, jj, ld) + CAPR * (IX(Z, c, jj + 1, ld) - IX(ZI, c, jj, ld))));
+        fn[jj] = tk[jj] * (IX(T, c, jj + 1, ld) - IX(T, c, jj, ld)) / (IX(Z, c, jj + 1, ld) - IX(Z, c, jj, ld));
+      } else if (j <= nlevgrnd - 1) {
+        *fc = dtime / cv[jj];
+        fn[jj] = tk[jj] * (IX(T, c, jj + 1, ld) - IX(T, c, jj, ld)) / (IX(Z, c, jj + 1, ld) - IX(Z, c, jj, ld));
+      } else if (j == nlevgrnd) {
+        *fc = dtime / cv[jj];
+        fn[jj] = f->eflx_bot[c];
+      }
+    }
+  }
+  /* ---- _h2osfc_thermprop_kernel! ---- */
+  if (f->h2osfc[c] > THIN_SFCLAYER && fh > THIN_SFCLAYER) {
+    f->c_h2osfc[c] = jl_max(THIN_SFCLAYER, CPLIQ * f->h2osfc[c] / fh);
+    dz_h2osfc = jl_max(THIN_SFCLAYER, 1.0e-3 * f->h2osfc[c] / fh);
+  } else {
+    f->c_h2osfc[c] = THIN_SFCLAYER;
+    dz_h2osfc = THIN_SFCLAYER;
+  }
+  const double ch = f->c_h2osfc[c];
+  const double dhsdT = dhsdT_c;
+
+  /* ---- set_rhs_vec! ---- */
+  for (int s = 1; s <= nlevsno; s++) {
+    int j = s - nlevsno, jj = s;
+    double fc = IX(f->fact, c, jj, ld);
+    if (j == snl + 1) {
+      rvec[s] = IX(T, c, jj, ld) + fc * (hs_top_snow - dhsdT * IX(T, c, jj, ld) + CNFAC * fn[jj]);
+    } else if (j > snl + 1) {
+      rvec[s] = IX(T, c, jj, ld) + CNFAC * fc * (fn[jj] - fn[jj - 1]);
+      rvec[s] += fc * sabg_lyr_col[s];
+    }
+  }
+  {
+    double dzm = 0.5 * dz_h2osfc + IX(Z, c, 1 + joff, ld);
+    double fnh = tk_h2osfc * (IX(T, c, 1 + joff, ld) - f->t_h2osfc[c]) / dzm;
+    fn_h2osfc = fnh;
+    rvec[nlevsno + 1] = f->t_h2osfc[c] + (dtime / ch) * (hs_h2osfc - dhsdT * f->t_h2osfc[c] + CNFAC * fnh);
+  }
+  for (int j = 1; j <= nlevgrnd; j++) {
+    int jj = j + nlevsno, rv = j + nlevsno + 1;
+    double fc = IX(f->fact, c, jj, ld), tt = IX(T, c, jj, ld);
+    if (j == snl + 1) {
+      rvec[rv] = tt + fc * (hs_top_snow - dhsdT * tt + CNFAC * fn[jj]);
+    } else if (j == 1) {
+      rvec[rv] = tt + fc * ((1.0 - fse) * (hs_soil - dhsdT * tt) + CNFAC * (fn[jj] - fse * fn[jj - 1]));
+      rvec[rv] += fse * fc * sabg_lyr_col[j + nlevsno];
+    } else if (j <= nlevgrnd - 1) {
+      rvec[rv] = tt + CNFAC * fc * (fn[jj] - fn[jj - 1]);
+    } else if (j == nlevgrnd) {
+      rvec[rv] = tt - CNFAC * fc * fn[jj - 1] + fc * fn[jj];
+    }
+  }
+  if (fh != 0.0) {
+    int jj = 1 + nlevsno, rv = 1 + nlevsno + 1;
+    rvec[rv] -= fh * IX(f->fact, c, jj, ld) * ((hs_soil - dhsdT * IX(T, c, jj, ld)) + CNFAC * fn_h2osfc);
+  }
+
+  /* ---- set_matrix! (bmat[band-1][row]) ---- */
+  {
+    const double omc = 1.0 - CNFAC;
+    for (int s = 1; s <= nlevsno; s++) {
+      int j = s - nlevsno, jj = s, bm = s;
+      if (j >= snl + 1) {
+        double fc = IX(f->fact, c, jj, ld);
+        double dzp = IX(Z, c, jj + 1, ld) - IX(Z, c, jj, ld);
+        if (j == snl + 1) {
+          bmat[2][bm] = 1.0 + omc * fc * tk[jj] / dzp - fc * dhsdT;
+        } else {
+          double dzm = IX(Z, c, jj, ld) - IX(Z, c, jj - 1, ld);
+          bmat[3][bm] = -omc * fc * tk[jj - 1] / dzm;
+          bmat[2][bm] = 1.0 + omc * fc * (tk[jj] / dzp + tk[jj - 1] / dzm);
+        }
+        if (j != 0) bmat[1][bm] = -omc * fc * tk[jj] / dzp;
+        else bmat[0][bm] = -omc * fc * tk[jj] / dzp;
+      }
+    }
+    {
+      int ssw = nlevsno + 1;
+      double dzm = 0.5 * dz_h2osfc + IX(Z, c, 1 + joff, ld);
+      bmat[2][ssw] = 1.0 + omc * (dtime / ch) * tk_h2osfc / dzm - (dtime / ch) * dhsdT;
+      bmat[1][ssw] = -omc * (dtime / ch) * tk_h2osfc / dzm;
+    }
+    for (int j = 1; j <= nlevgrnd; j++) {
+      int jj = j + nlevsno, bm = j + nlevsno + 1;
+      double fc = IX(f->fact, c, jj, ld);
+      if (j == snl + 1) {
+        double dzp = IX(Z, c, jj + 1, ld) - IX(Z, c, jj, ld);
+        bmat[2][bm] = 1.0 + omc * fc * tk[jj] / dzp - fc * dhsdT;
+        bmat[1][bm] = -omc * fc * tk[jj] / dzp;
+      } else if (j == 1) {
+        double dzm = IX(Z, c, jj, ld) - IX(Z, c, jj - 1, ld);
+        double dzp = IX(Z, c, jj + 1, ld) - IX(Z, c, jj, ld);
+        bmat[1][bm] = -omc * fc * tk[jj] / dzp;
+        bmat[2][bm] = 1.0 + omc * fc * (tk[jj] / dzp + fse * tk[jj - 1] / dzm) - (1.0 - fse) * fc * dhsdT;
+        bmat[4][bm] = -fse * omc * fc * tk[jj - 1] / dzm;
+      } else if (j <= nlevgrnd - 1) {
+        double dzm = IX(Z, c, jj, ld) - IX(Z, c, jj - 1, ld);
+        double dzp = IX(Z, c, jj + 1, ld) - IX(Z, c, jj, ld);
+        bmat[1][bm] = -omc * fc * tk[jj] / dzp;
+        bmat[2][bm] = 1.0 + omc * fc * (tk[jj] / dzp + tk[jj - 1] / dzm);
+        bmat[3][bm] = -omc * fc * tk[jj - 1] / dzm;
+      } else if (j == nlevgrnd) {
+        double dzm = IX(Z, c, jj, ld) - IX(Z, c, jj - 1, ld);
+        bmat[2][bm] = 1.0 + omc * fc * tk[jj - 1] / dzm;
+        bmat[3][bm] = -omc * fc * tk[jj - 1] / dzm;
+      }
+    }
+    if (fh != 0.0) {
+      double dzm = 0.5 * dz_h2osfc + IX(Z, c, 1 + joff, ld);
+      int bm = 1 + nlevsno + 1;
+      double fc = IX(f->fact, c, 1 + joff, ld);
+      bmat[2][bm] += fh * (omc * fc * tk_h2osfc / dzm + fc * dhsdT);
+      bmat[3][bm] = -fh * omc * fc * tk_h2osfc / dzm;
+    }
+  }
+
+  /* ---- _tvector_init_kernel! ---- */
+  for (int64_t j = snl + 1; j <= 0; j++) tvec[j - 1 + nlevsno + 1] = IX(T, c, j + joff, ld);
+  tvec[nlevsno + 1] = f->t_h2osfc[c];
+  for (int j = 1; j <= nlevmaxurbgrnd; j++) tvec[j + nlevsno + 1] = IX(T, c, j + joff, ld);
+
+  /* ---- batched_band_solve! on this column: dense pivoted GE ---- */
+  {
+    const int kl = 2, ku = 2;
+    int jt = (int)(snl + nlevsno + 1);
+    int n = (int)(nlevgrnd - snl + 1);
+    /* bmatrix as [1 column, 5 bands, nlev_total] so the shared dense routine reads it */
+    double bm1[5 * (ORC_MAXL + 2)];
+    for (int lev = 1; lev <= nlev_total; lev++)
+      for (int bb = 1; bb <= 5; bb++) bm1[(bb - 1) + (lev - 1) * 5] = bmat[bb - 1][lev];
+    dense_band_solve_col(tvec + 1, 1, bm1, 1, nlev_total, rvec + 1, 1, 0, jt, n, kl, ku);
+  }
+
+  /* ---- _tvector_extract_kernel! ---- */
+  for (int64_t j = snl + 1; j <= 0; j++) IX(T, c, j + joff, ld) = tvec[j - 1 + nlevsno + 1];
+  for (int j = 1; j <= nlevmaxurbgrnd; j++) IX(T, c, j + joff, ld) = tvec[j + nlevsno + 1];
+  if (fh == 0.0) f->t_h2osfc[c] = IX(T, c, 1 + joff, ld);
+  else f->t_h2osfc[c] = tvec[nlevsno + 1];
+
+  /* ---- _fn1_kernel! ---- */
+  for (int jj = 1; jj <= nlev; jj++) {
+    int j = jj - nlevsno;
+    if (j >= snl + 1) {
+      if (j <= nlevgrnd - 1)
+        fn1[jj] = tk[jj] * (IX(T, c, jj + 1, ld) - IX(T, c, jj, ld)) / (IX(Z, c, jj + 1, ld) - IX(Z, c, jj, ld));
+      else if (j == nlevgrnd)
+        fn1[jj] = 0.0;
+    }
+  }
+
+  /* ---- phase change ---- */
+  double dh_arr[1];
+  dh_arr[0] = dhsdT;
+  {
+    /* the per-column helpers index dhsdT[c]; hand them a pointer offset so [c] is ours */
+    const double* dh = dh_arr - c;
+    pc_h2osfc_col(vp, X->b, f, c, dtime, dh);
+    pc_beta_col(vp, X->b, f, c, dtime, dh);
+  }
+
+  /* ---- _tgrnd_kernel! ---- */
+  {
+    double t1 = IX(T, c, 1 + joff, ld), th = f->t_h2osfc[c];
+    if (snl < 0) {
+      double ts = IX(T, c, snl + 1 + joff, ld);
+      if (fh != 0.0) f->t_grnd[c] = fse * ts + (1.0 - fse - fh) * t1 + fh * th;
+      else f->t_grnd[c] = fse * ts + (1.0 - fse) * t1;
+    } else {
+      if (fh != 0.0) f->t_grnd[c] = (1.0 - fh) * t1 + fh * th;
+      else f->t_grnd[c] = t1;
+    }
+  }
+  /* ---- eflx_fgr12 / eflx_fgr (_eflx_fgr_kernel!) ---- */
+  f->eflx_fgr12[c] = 0.0;
+  {
+    const int issoilcrop = (lit == ISTSOIL || lit == ISTCROP);
+    for (int j = 1; j <= nlevgrnd; j++) {
+      int jj = j + joff;
+      if (j == 1) f->eflx_fgr12[c] = -CNFAC * fn[1 + joff] - (1.0 - CNFAC) * fn1[1 + joff];
+      if (j > 0 && j < nlevgrnd && issoilcrop)
+        IX(f->eflx_fgr, c, j, ld) = -CNFAC * fn[jj] - (1.0 - CNFAC) * fn1[jj];
+      else if (j == nlevgrnd && issoilcrop)
+        IX(f->eflx_fgr, c, j, ld) = 0.0;
+    }
+  }
+  for (int jj = (int)(snl + 1 + joff); jj <= nlev; jj++)
+    if (!isfinite(IX(T, c, jj, ld))) status |= CLMGB_COL_NONFINITE;
+  return status;
+}
+
+static int check_varpar(const clmgb_varpar* vp)
+{
+  if (!vp) return CLMGB_ERR_NULL_ARG;
+  if (vp->nlevsno < 1 || vp->nlevgrnd < 2 || vp->nlevsoi < 1 || vp->nlevsoi > vp->nlevgrnd)
+    return CLMGB_ERR_DIMS;
+  if (vp->nlevmaxurbgrnd != vp->nlevgrnd) return CLMGB_ERR_DIMS;
+  if (vp->nlevsno + vp->nlevmaxurbgrnd + 1 > ORC_MAXL) return CLMGB_ERR_DIMS;
+  return 0;
+}
+
+int orc_soil_temperature(const clmgb_varpar* vp, const clmgb_bounds* b,
+                         const clmgb_soiltemp_fields* f, double dtime, int32_t snow_method,
+                         uint32_t* col_status, int32_t nthreads)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  st_ctx X = {vp, b, f, dtime, snow_method};
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t c = 0; c < b->nc; c++) {
+    uint32_t s = soiltemp_col(&X, c);
+    if (col_status) col_status[c] = s;
+  }
+  return 0;
+}
+
+/* Standalone phase_change_h2osfc! / phase_change_beta! (soil_temperature.jl:1857, 2232). */
+int orc_phase_change_h2osfc(const clmgb_varpar* vp, const clmgb_bounds* b,
+                            const clmgb_soiltemp_fields* f, double dtime, const double* dhsdT)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  for (int64_t c = 0; c < b->nc; c++)
+    if (f->mask_nolakec[c]) pc_h2osfc_col(vp, b, f, c, dtime, dhsdT);
+  return 0;
+}
+int orc_phase_change_beta(const clmgb_varpar* vp, const clmgb_bounds* b,
+                          const clmgb_soiltemp_fields* f, double dtime, const double* dhsdT)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  for (int64_t c = 0; c < b->nc; c++)
+    if (f->mask_nolakec[c]) pc_beta_col(vp, b, f, c, dtime, dhsdT);
+  return 0;
+}
+
+/* ===================================================================== */
+/* set_soil_water_fractions! — _soilhyd_water_fractions_kernel!          */
+/* ===================================================================== */
+static void fractions_col(const clmgb_varpar* vp, const clmgb_bounds* b,
+                          const clmgb_soilwater_fields* f, int64_t c)
+{
+  const int64_t ld = b->ldc;
+  const int joff = vp->nlevsno;
+  if (!f->mask_hydrology[c]) return;
+  for (int j = 1; j <= vp->nlevsoi; j++) {
+    double dn = DENICE;
+    double dz_ext = IX(f->dz, c, j + joff, ld) + IX(f->excess_ice, c, j, ld) / dn;
+    double ws = IX(f->watsat, c, j, ld);
+    double vol_ice = jl_min(ws, (IX(f->h2osoi_ice, c, j + joff, ld) + IX(f->excess_ice, c, j, ld)) / (dz_ext * dn));
+    IX(f->eff_porosity, c, j, ld) = jl_max(0.01, ws - vol_ice);
+    IX(f->icefrac, c, j, ld) = jl_min(1.0, vol_ice / ws);
+  }
+}
+
+int orc_soil_water_fractions(const clmgb_varpar* vp, const clmgb_bounds* b,
+                             const clmgb_soilwater_fields* f, int32_t nthreads)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t c = 0; c < b->nc; c++) fractions_col(vp, b, f, c);
+  return 0;
+}
+
+/* ===================================================================== */
+/* _soilwm_moisture_form_kernel! (soil_water_movement.jl:1250-1489)       */
+/* ===================================================================== */
+typedef struct {
+  double hk, smp, dhkdw, dsmpdw, imped, s2, vwc_liq, dt_dz, qin, qout;
+  double dqidw0, dqidw1, dqodw1, dqodw2, dwat, amx, bmx, cmx, rmx, gam, fluxNet0, fluxNet1;
+} mf_row;
+
+/* Optional capture of the last attempt's scratch rows for golden tests. */
+typedef struct {
+  double* qin;   /* [ld, nlevsoi] */
+  double* qout;  /* [ld, nlevsoi] */
+} orc_mf_capture;
+
+#define MF_ATTEMPT_CAP 100000
+
+static uint32_t moisture_form_col(const clmgb_varpar* vp, const clmgb_bounds* b,
+                                  const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
+                                  double dtime, int64_t c, const orc_mf_capture* cap)
+{
+  const int64_t ld = b->ldc;
+  const int joff = vp->nlevsno, joff_zi = vp->nlevsno + 1, nlevsoi = vp->nlevsoi;
+  if (!f->mask_hydrology[c]) return 0;
+  const int nlayers = (int)f->col_nbedrock[c];
+  if (nlayers < 1 || nlayers > nlevsoi) return CLMGB_COL_LEVEL_RANGE;
+  mf_row R[ORC_MAXL + 2];
+  memset(R, 0, sizeof(R));
+  const double denh2o = DENH2O, m_to_mm = M_TO_MM;
+  const double e_ice = cfg->e_ice, dtmin = cfg->dtmin, xtu = cfg->xTolerUpper, xtl = cfg->xTolerLower;
+  const double verysmall = cfg->verySmall;
+  const int expensive = (cfg->flux_calculation == 42);
+  const int lower_bc = cfg->lower_boundary_condition;
+  int nsubstep = 0;
+  double dtsub = dtime, dtdone = 0.0, qc = 0.0;
+  uint32_t status = 0;
+  for (;;) {
+    nsubstep += 1;
+    if (nsubstep > MF_ATTEMPT_CAP) { status |= CLMGB_COL_SUBSTEP_CAP; break; }
+    for (int j = 1; j <= nlayers; j++) {
+      R[j].vwc_liq = jl_max(IX(f->h2osoi_liq, c, joff + j, ld), 1.0e-6) / (IX(f->dz, c, joff + j, ld) * denh2o);
+      R[j].dt_dz = dtsub / (m_to_mm * IX(f->dz, c, joff + j, ld));
+    }
+    for (int j = 1; j <= nlayers; j++) {
+      double s = R[j].vwc_liq / IX(f->watsat, c, j, ld);
+      s = jl_min(s, 1.0); s = jl_max(0.01, s);
+      R[j].s2 = s;
+    }
+    for (int j = 1; j <= nlayers; j++) {
+      double s1, imp;
+      if (j == nlayers) {
+        s1 = R[j].s2;
+        imp = pow(10.0, -e_ice * IX(f->icefrac, c, j, ld));
+      } else {
+        s1 = 0.5 * (R[j].s2 + R[j + 1].s2);
+        imp = pow(10.0, -e_ice * (0.5 * (IX(f->icefrac, c, j, ld) + IX(f->icefrac, c, j + 1, ld))));
+      }
+      R[j].imped = imp;
+      s1 = jl_min(s1, 1.0); s1 = jl_max(0.01, s1);
+      double bb = IX(f->bsw, c, j, ld);
+      double hkv = imp * IX(f->hksat, c, j, ld) * pow(s1, 2.0 * bb + 3.0);
+      double dhkds = (2.0 * bb + 3.0) * hkv / s1;
+      double sn = R[j].s2;
+      double smpv = -IX(f->sucsat, c, j, ld) * pow(sn, -bb);
+      double dsmpds = -bb * smpv / sn;
+      R[j].hk = hkv; R[j].smp = smpv; R[j].dhkdw = dhkds;
+      R[j].dsmpdw = dsmpds / IX(f->watsat, c, j, ld);
+      IX(f->smp_l, c, j, ld) = smpv;
+      IX(f->hk_l, c, j, ld) = hkv;
+    }
+    for (int j = 1; j <= nlayers; j++) {
+      R[j].qin = 0.0; R[j].qout = 0.0;
+      R[j].dqidw0 = 0.0; R[j].dqidw1 = 0.0; R[j].dqodw1 = 0.0; R[j].dqodw2 = 0.0;
+    }
+    for (int j = 1; j <= nlayers - 1; j++) {
+      double dhkds1 = 0.5 * R[j].dhkdw / IX(f->watsat, c, j, ld);
+      double dhkds2 = 0.5 * R[j].dhkdw / IX(f->watsat, c, j + 1, ld);
+      double num = R[j + 1].smp - R[j].smp;
+      double den = m_to_mm * (IX(f->z, c, joff + j + 1, ld) - IX(f->z, c, joff + j, ld));
+      R[j].qout = -R[j].hk * num / den + R[j].hk;
+      R[j].dqodw1 = (R[j].hk * R[j].dsmpdw - dhkds1 * num) / den + dhkds1;
+      R[j].dqodw2 = (-R[j].hk * R[j + 1].dsmpdw - dhkds2 * num) / den + dhkds2;
+    }
+    {
+      int j = nlayers;
+      if (lower_bc == CLMGB_BC_WATERTABLE) {
+        int jwt = nlevsoi;
+        for (int jj = 1; jj <= nlevsoi; jj++) {
+          if (f->zwt[c] <= IX(f->zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
+        }
+        if (j > jwt) {
+          R[j].qout = 0.0; R[j].dqodw1 = 0.0; R[j].dqodw2 = 0.0;
+        } else {
+          double dhkds1l = R[j].dhkdw / IX(f->watsat, c, j, ld);
+          double num = -R[j].smp;
+          double den = m_to_mm * (f->zwt[c] - IX(f->z, c, joff + j, ld));
+          R[j].qout = -R[j].hk * num / den + R[j].hk;
+          R[j].dqodw1 = (R[j].hk * R[j].dsmpdw - dhkds1l * num) / den + dhkds1l;
+          R[j].dqodw2 = 0.0;
+        }
+      } else if (lower_bc == CLMGB_BC_FLUX) {
+        R[j].qout = R[j].hk;
+        R[j].dqodw1 = R[j].dhkdw / IX(f->watsat, c, j, ld);
+      } else {
+        R[j].qout = 0.0;
+        R[j].dqodw1 = 0.0;
+      }
+    }
+    for (int j = 2; j <= nlayers; j++) {
+      R[j].qin = R[j - 1].qout;
+      R[j].dqidw0 = R[j - 1].dqodw1;
+      R[j].dqidw1 = R[j - 1].dqodw2;
+    }
+    R[1].qin = f->qflx_infl[c];
+    R[1].dqidw1 = 0.0;
+    for (int j = 1; j <= nlayers; j++) {
+      double fluxNet = R[j].qin - R[j].qout - IX(f->qflx_rootsoi, c, j, ld);
+      R[j].rmx = -fluxNet * R[j].dt_dz;
+    }
+    R[1].amx = 0.0;
+    R[1].bmx = -1.0 - (-R[1].dqidw1 + R[1].dqodw1) * R[1].dt_dz;
+    R[1].cmx = -R[1].dqodw2 * R[1].dt_dz;
+    for (int j = 2; j <= nlayers - 1; j++) {
+      R[j].amx = R[j].dqidw0 * R[j].dt_dz;
+      R[j].bmx = -1.0 - (-R[j].dqidw1 + R[j].dqodw1) * R[j].dt_dz;
+      R[j].cmx = -R[j].dqodw2 * R[j].dt_dz;
+    }
+    R[nlayers].amx = R[nlayers].dqidw0 * R[nlayers].dt_dz;
+    R[nlayers].bmx = -1.0 - (-R[nlayers].dqidw1 + R[nlayers].dqodw1) * R[nlayers].dt_dz;
+    R[nlayers].cmx = 0.0;
+    {
+      double bet = R[1].bmx;
+      if (fabs(bet) < 1.0e-30) bet = 1.0e-30;
+      double dwat_prev = R[1].rmx / bet;
+      R[1].dwat = dwat_prev;
+      for (int j = 2; j <= nlayers; j++) {
+        R[j].gam = R[j - 1].cmx / bet;
+        bet = R[j].bmx - R[j].amx * R[j].gam;
+        if (fabs(bet) < 1.0e-30) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
+        dwat_prev = (R[j].rmx - R[j].amx * dwat_prev) / bet;
+        R[j].dwat = dwat_prev;
+      }
+      double dwat_next = dwat_prev;
+      for (int j = nlayers - 1; j >= 1; j--) {
+        dwat_next = R[j].dwat - R[j + 1].gam * dwat_next;
+        R[j].dwat = dwat_next;
+      }
+    }
+    double errorMax = 0.0;
+    for (int j = 1; j <= nlayers; j++) {
+      if (expensive) {
+        double qin_test = j == 1 ? R[j].qin + R[j].dqidw1 * R[j].dwat
+                                 : R[j].qin + R[j].dqidw0 * R[j - 1].dwat + R[j].dqidw1 * R[j].dwat;
+        double qout_test = j == nlayers ? R[j].qout + R[j].dqodw1 * R[j].dwat
+                                        : R[j].qout + R[j].dqodw1 * R[j].dwat + R[j].dqodw2 * R[j + 1].dwat;
+        R[j].fluxNet0 = qin_test - qout_test - IX(f->qflx_rootsoi, c, j, ld);
+      } else {
+        R[j].fluxNet0 = R[j].dwat / R[j].dt_dz;
+      }
+      R[j].fluxNet1 = R[j].qin - R[j].qout - IX(f->qflx_rootsoi, c, j, ld);
+    }
+    for (int j = 1; j <= nlayers; j++) {
+      double ev = fabs(R[j].fluxNet1 - R[j].fluxNet0) * dtsub * 0.5;
+      errorMax = jl_max(errorMax, ev);
+    }
+    if (errorMax > xtu && dtsub > dtmin) {
+      dtsub = jl_max(dtsub / 2.0, dtmin);
+      continue;
+    }
+    for (int j = 1; j <= nlayers; j++)
+      IX(f->h2osoi_liq, c, joff + j, ld) = IX(f->h2osoi_liq, c, joff + j, ld) + R[j].dwat * (m_to_mm * IX(f->dz, c, joff + j, ld));
+    double qcTemp;
+    if (lower_bc == CLMGB_BC_FLUX) qcTemp = R[nlayers].hk + R[nlayers].dhkdw * R[nlayers].dwat;
+    else if (lower_bc == CLMGB_BC_ZERO_FLUX) qcTemp = 0.0;
+    else qcTemp = R[nlayers].qout + R[nlayers].dqodw1 * R[nlayers].dwat;
+    qc += qcTemp * (dtsub / dtime);
+    dtdone += dtsub;
+    if (fabs(dtime - dtdone) < verysmall) break;
+    if (errorMax < xtl) dtsub = dtsub * 2.0;
+    dtsub = jl_min(dtsub, dtime - dtdone);
+  }
+  f->qcharge[c] = qc;
+  f->num_substeps[c] = (double)nsubstep;
+  if (cap) {
+    for (int j = 1; j <= nlayers; j++) {
+      IX(cap->qin, c, j, ld) = R[j].qin;
+      IX(cap->qout, c, j, ld) = R[j].qout;
+    }
+  }
+  for (int j = 1; j <= nlayers; j++)
+    if (!isfinite(IX(f->h2osoi_liq, c, joff + j, ld))) status |= CLMGB_COL_NONFINITE;
+  return status;
+}
+
+int orc_soil_water(const clmgb_varpar* vp, const clmgb_bounds* b,
+                   const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg, double dtime,
+                   uint32_t* col_status, double* cap_qin, double* cap_qout, int32_t nthreads)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  if (cfg->soilwater_movement_method != CLMGB_MOISTURE_FORM) return CLMGB_ERR_UNSUPPORTED;
+  if (cfg->upper_boundary_condition != CLMGB_BC_FLUX) return CLMGB_ERR_CONFIG;
+  if (!(cfg->lower_boundary_condition == CLMGB_BC_WATERTABLE ||
+        cfg->lower_boundary_condition == CLMGB_BC_FLUX ||
+        cfg->lower_boundary_condition == CLMGB_BC_ZERO_FLUX)) return CLMGB_ERR_CONFIG;
+  orc_mf_capture capv = {cap_qin, cap_qout};
+  const orc_mf_capture* cap = (cap_qin && cap_qout) ? &capv : NULL;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 32) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t c = 0; c < b->nc; c++) {
+    uint32_t s = moisture_form_col(vp, b, f, cfg, dtime, c, cap);
+    if (col_status) col_status[c] = s;
+  }
+  return 0;
+}
+
+/* ===================================================================== */
+/* Synthetic multi-step driver: the per-step forcing a test or benchmark  */
+/* applies before the path (the upstream radiation/infiltration modules   */
+/* are out of scope), then the path in the driver's order.                */
+/*   per column, per step t:                                              */
+/*     sabg = sabg_soil = sabg_snow = G[t]; sabg_lyr = 0 except the top   */
+/*     active layer (snl+1) = G[t]; forc_lwrad = SB * t_grnd^4;           */
+/*     qflx_infl = I[t]; t_ssbef = t_soisno; t_h2osfc_bef = t_h2osfc;     */
+/*     soil_temperature!, set_soil_water_fractions!, soil_water!.         */
+/* G and I are [nsteps, nc] row-major with row stride gstride (0 = the    */
+/* same row every step).                                                  */
+/* ===================================================================== */
+void orc_apply_forcing_col(const clmgb_varpar* vp, const clmgb_bounds* b,
+                           const clmgb_soiltemp_fields* ft, const clmgb_soilwater_fields* fw,
+                           int64_t c, double G, double I)
+{
+  const int64_t ldp = b->ldp;
+  const int nlevsno = vp->nlevsno;
+  double* sabg = (double*)ft->sabg;
+  double* sabg_soil = (double*)ft->sabg_soil;
+  double* sabg_snow = (double*)ft->sabg_snow;
+  double* sabg_lyr = (double*)ft->sabg_lyr;
+  for (int64_t p1 = ft->col_patchi[c]; p1 <= ft->col_patchf[c]; p1++) {
+    int64_t p = p1 - 1;
+    sabg[p] = G; sabg_soil[p] = G; sabg_snow[p] = G;
+    for (int k = 1; k <= nlevsno + 1; k++) IX(sabg_lyr, p, k, ldp) = 0.0;
+    IX(sabg_lyr, p, ft->col_snl[c] + 1 + nlevsno, ldp) = G;
+  }
+  ((double*)ft->forc_lwrad)[c] = SB * jl_pow4(ft->t_grnd[c]);
+  ((double*)fw->qflx_infl)[c] = I;
+}
+
+int orc_run_steps(const clmgb_varpar* vp, const clmgb_bounds* b,
+                  const clmgb_soiltemp_fields* ft, const clmgb_soilwater_fields* fw,
+                  const clmgb_swm_config* cfg, double dtime, int32_t snow_method,
+                  int32_t nsteps, const double* G, const double* I, int64_t gstride,
+                  double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
+                  int32_t nthreads)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  st_ctx X = {vp, b, ft, dtime, snow_method};
+  const int64_t ld = b->ldc;
+  const int L = vp->nlevsno + vp->nlevmaxurbgrnd;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t c = 0; c < b->nc; c++) {
+    uint32_t s = 0;
+    for (int32_t t = 0; t < nsteps; t++) {
+      if (ft->mask_nolakec[c]) {
+        orc_apply_forcing_col(vp, b, ft, fw, c, G[t * gstride + c], I[t * gstride + c]);
+        if (t_ssbef)
+          for (int jj = 1; jj <= L; jj++) IX(t_ssbef, c, jj, ld) = IX(ft->t_soisno, c, jj, ld);
+        if (t_h2osfc_bef) t_h2osfc_bef[c] = ft->t_h2osfc[c];
+      }
+      s |= soiltemp_col(&X, c);
+      fractions_col(vp, b, fw, c);
+      s |= moisture_form_col(vp, b, fw, cfg, dtime, c, NULL);
+    }
+    if (col_status) col_status[c] = s;
+  }
+  return 0;
+}
+
+/* ===================================================================== */
+/* init_soil_properties! (cold_start.jl:225-391), per column and level,   */
+/* with the SoilStateParams defaults (types/soil_state.jl:19-35).         */
+/* Inputs sand/clay [%], om_frac (organic fraction after om_frac_sf and   */
+/* the 130 kg/m3 normalisation), zsoi [m]; outputs per level.             */
+/* ===================================================================== */
+void orc_init_soil_properties(int64_t n, const double* sand_in, const double* clay_in,
+                              const double* om_in, const double* zsoi,
+                              double* watsat, double* bsw, double* sucsat, double* hksat,
+                              double* tkmg, double* tkdry, double* csol)
+{
+  const double tkd_sand = 8.8, tkd_clay = 2.92, tkd_om = 0.05, tkm_om = 0.25;
+  const double csol_sand = 2.128, csol_clay = 2.385, csol_om = 2.5, pd = 2700.0;
+  const double bsw_sf = 1.0, hksat_sf = 1.0, sucsat_sf = 1.0, watsat_sf = 1.0;
+  for (int64_t i = 0; i < n; i++) {
+    double sand = sand_in[i], clay = clay_in[i], om_frac = om_in[i];
+    double watsat_mineral = 0.489 - 0.00126 * sand;
+    double bsw_mineral = 2.91 + 0.159 * clay;
+    double sucsat_mineral = 10.0 * pow(10.0, 1.88 - 0.0131 * sand);
+    double xksat_mineral = 0.0070556 * pow(10.0, -0.884 + 0.0153 * sand);
+    double zsapric = 0.5;
+    double depth_ratio = zsoi[i] / zsapric;
+    double watsat_organic = jl_max(0.93 - 0.1 * depth_ratio, 0.83);
+    double bsw_organic = jl_min(2.7 + 9.3 * depth_ratio, 12.0);
+    double sucsat_organic = jl_min(10.3 - 0.2 * depth_ratio, 10.1);
+    double xksat_organic = jl_max(0.28 - 0.2799 * depth_ratio, xksat_mineral);
+    double watsat_val = jl_min(watsat_sf * ((1.0 - om_frac) * watsat_mineral + om_frac * watsat_organic), 0.93);
+    double bsw_val = bsw_sf * ((1.0 - om_frac) * bsw_mineral + om_frac * bsw_organic);
+    double sucsat_val = sucsat_sf * ((1.0 - om_frac) * sucsat_mineral + om_frac * sucsat_organic);
+    double om_hksat = xksat_organic;
+    double pcalpha = 0.5, pcbeta = 0.139, perc_frac;
+    if (om_frac > pcalpha) {
+      double perc_norm = pow(1.0 - pcalpha, -pcbeta);
+      perc_frac = perc_norm * pow(om_frac - pcalpha, pcbeta);
+    } else {
+      perc_frac = 0.0;
+    }
+    double uncon_frac = (1.0 - om_frac) + (1.0 - perc_frac) * om_frac;
+    double uncon_hksat;
+    if (uncon_frac > 0.0)
+      uncon_hksat = uncon_frac / ((1.0 - om_frac) / xksat_mineral + ((1.0 - perc_frac) * om_frac) / om_hksat);
+    else
+      uncon_hksat = 0.0;
+    double hksat_val = hksat_sf * (uncon_frac * uncon_hksat + (perc_frac * om_frac) * om_hksat);
+    watsat[i] = watsat_val; bsw[i] = bsw_val; sucsat[i] = sucsat_val; hksat[i] = hksat_val;
+    double bd = (1.0 - watsat_mineral) * pd;
+    double sc = sand + clay;
+    double tkm = sc > 0.0 ? (1.0 - om_frac) * (tkd_sand * sand + tkd_clay * clay) / sc + tkm_om * om_frac : tkm_om;
+    tkmg[i] = pow(tkm, 1.0 - watsat_val);
+    tkdry[i] = ((0.135 * bd + 64.7) / (pd - 0.947 * bd)) * (1.0 - om_frac) + tkd_om * om_frac;
+    double csol_min = sc > 0.0 ? (csol_sand * 1.0e6 * sand + csol_clay * 1.0e6 * clay) / sc : csol_om * 1.0e6;
+    csol[i] = (1.0 - om_frac) * csol_min + csol_om * 1.0e6 * om_frac;
+  }
+}
+
+int orc_abi_version(void) { return CLMGB_ABI_VERSION; }

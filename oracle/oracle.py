@@ -1,0 +1,166 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference legs
+import this module.  The product package never does.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+_PKG = os.path.join(ROOT, "clm.jl_gb300")
+if _PKG not in sys.path:
+    sys.path.insert(0, _PKG)
+
+from clmgb import abi  # noqa: E402  (interface definitions only)
+
+sys.path.insert(0, HERE)
+import build as _build  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.orc_soil_temperature.argtypes = [P, P, P, C.c_double, C.c_int32, P, C.c_int32]
+        L.orc_soil_water_fractions.argtypes = [P, P, P, C.c_int32]
+        L.orc_soil_water.argtypes = [P, P, P, P, C.c_double, P, P, P, C.c_int32]
+        L.orc_run_steps.argtypes = [P, P, P, P, P, C.c_double, C.c_int32, C.c_int32, P, P,
+                                    C.c_int64, P, P, P, C.c_int32]
+        L.orc_batched_band_solve.argtypes = [C.c_int64, C.c_int64, C.c_int32, P, P, P, P, P, P,
+                                             C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+        L.orc_tridiagonal_multi.argtypes = [C.c_int64, C.c_int64, C.c_int32, P, P, P, P, P, P, P, C.c_int32]
+        L.orc_tridiagonal_solve.argtypes = [P, P, P, P, P, C.c_int32, C.c_int32]
+        L.orc_tridiagonal_col.argtypes = [P, P, P, P, P, C.c_int32, C.c_int32, C.c_int32]
+        L.orc_ice_impedance.argtypes = [C.c_double, C.c_double]
+        L.orc_ice_impedance.restype = C.c_double
+        L.orc_phase_change_h2osfc.argtypes = [P, P, P, C.c_double, P]
+        L.orc_phase_change_beta.argtypes = [P, P, P, C.c_double, P]
+        L.orc_init_soil_properties.argtypes = [C.c_int64] + [P] * 11
+        _lib = L
+    return _lib
+
+
+def default_threads():
+    return int(os.environ.get("CLMGB_ORACLE_THREADS", os.cpu_count() or 1))
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def _chk(rc):
+    if rc != 0:
+        raise RuntimeError("oracle returned %d" % rc)
+
+
+def soil_temperature(st, dtime, snow_method=abi.SNOW_JORDAN1991, nthreads=None):
+    """soil_temperature! on a host ColumnState (in place); returns per-column status."""
+    vp, b, f = st.vp, st.bounds(), st.soiltemp_fields()
+    status = np.zeros(st.nc, dtype=np.uint32)
+    _chk(lib().orc_soil_temperature(C.byref(vp), C.byref(b), C.byref(f), dtime, snow_method,
+                                    _p(status), nthreads or default_threads()))
+    return status
+
+
+def soil_water_fractions(st, nthreads=None):
+    vp, b, f = st.vp, st.bounds(), st.soilwater_fields()
+    _chk(lib().orc_soil_water_fractions(C.byref(vp), C.byref(b), C.byref(f), nthreads or default_threads()))
+
+
+def soil_water(st, dtime, cfg=None, capture=False, nthreads=None):
+    """soil_water! (moisture form) in place; returns status (and captured qin/qout)."""
+    cfg = cfg or abi.SwmConfig.clm5_default()
+    vp, b, f = st.vp, st.bounds(), st.soilwater_fields()
+    status = np.zeros(st.nc, dtype=np.uint32)
+    qin = qout = None
+    if capture:
+        qin = np.zeros((vp.nlevsoi, st.nc))
+        qout = np.zeros((vp.nlevsoi, st.nc))
+    rc = lib().orc_soil_water(C.byref(vp), C.byref(b), C.byref(f), C.byref(cfg), dtime,
+                              _p(status), _p(qin), _p(qout), nthreads or default_threads())
+    if rc != 0:
+        return rc
+    if capture:
+        return status, qin, qout
+    return status
+
+
+def run_steps(st, dtime, G, I, cfg=None, snow_method=abi.SNOW_JORDAN1991, nthreads=None):
+    """Run len(G) synthetic steps (forcing + path) in place.  G, I: [nsteps, nc]."""
+    cfg = cfg or abi.SwmConfig.clm5_default()
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    I = np.ascontiguousarray(I, dtype=np.float64)
+    nsteps = G.shape[0]
+    vp, b = st.vp, st.bounds()
+    ft, fw = st.soiltemp_fields(), st.soilwater_fields()
+    status = np.zeros(st.nc, dtype=np.uint32)
+    _chk(lib().orc_run_steps(C.byref(vp), C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg),
+                             dtime, snow_method, nsteps, _p(G), _p(I), st.nc,
+                             _p(st["t_ssbef"]), _p(st["t_h2osfc_bef"]), _p(status),
+                             nthreads or default_threads()))
+    return status
+
+
+def batched_band_solve(tvector, bmatrix, rvector, jtop, jbot, mask, kl=2, ku=2, nlevsno_off=0,
+                       nthreads=None):
+    """bmatrix: numpy (nlev, nband, nc) == Julia [nc, nband, nlev]; vectors (nlev, nc)."""
+    nlev, nc = tvector.shape
+    _chk(lib().orc_batched_band_solve(nc, nc, nlev, _p(tvector), _p(bmatrix), _p(rvector),
+                                      _p(jtop), _p(jbot), _p(mask), kl, ku, nlevsno_off,
+                                      nthreads or default_threads()))
+
+
+def tridiagonal_multi(u, a, b, c, r, jtop, mask, nthreads=None):
+    nlevs, ncols = u.shape
+    _chk(lib().orc_tridiagonal_multi(ncols, ncols, nlevs, _p(u), _p(a), _p(b), _p(c), _p(r),
+                                     _p(jtop), _p(mask), nthreads or default_threads()))
+
+
+def tridiagonal_solve(a, b, c, r, jtop, nlevs):
+    u = np.zeros(nlevs)
+    arr = [np.ascontiguousarray(x, dtype=np.float64) for x in (a, b, c, r)]
+    lib().orc_tridiagonal_solve(_p(u), *[_p(x) for x in arr], jtop, nlevs)
+    return u
+
+
+def tridiagonal_col(a, b, c, r, jtop, lbj, ubj, u=None):
+    n = ubj - lbj + 1
+    u = np.zeros(n) if u is None else np.array(u, dtype=np.float64)
+    arr = [np.ascontiguousarray(x, dtype=np.float64) for x in (a, b, c, r)]
+    lib().orc_tridiagonal_col(_p(u), *[_p(x) for x in arr], jtop, lbj, ubj)
+    return u
+
+
+def ice_impedance(icefrac, e_ice):
+    return lib().orc_ice_impedance(float(icefrac), float(e_ice))
+
+
+def phase_change_h2osfc(st, dtime, dhsdT):
+    dh = np.ascontiguousarray(dhsdT, dtype=np.float64)
+    _chk(lib().orc_phase_change_h2osfc(C.byref(st.vp), C.byref(st.bounds()),
+                                       C.byref(st.soiltemp_fields()), dtime, _p(dh)))
+
+
+def phase_change_beta(st, dtime, dhsdT):
+    dh = np.ascontiguousarray(dhsdT, dtype=np.float64)
+    _chk(lib().orc_phase_change_beta(C.byref(st.vp), C.byref(st.bounds()),
+                                     C.byref(st.soiltemp_fields()), dtime, _p(dh)))
+
+
+def init_soil_properties(sand, clay, om, zsoi):
+    sand, clay, om, zsoi = [np.ascontiguousarray(np.broadcast_to(x, np.broadcast(sand, clay, om, zsoi).shape),
+                                                 dtype=np.float64) for x in (sand, clay, om, zsoi)]
+    n = sand.size
+    outs = {k: np.zeros(sand.shape) for k in ("watsat", "bsw", "sucsat", "hksat", "tkmg", "tkdry", "csol")}
+    lib().orc_init_soil_properties(n, _p(sand), _p(clay), _p(om), _p(zsoi),
+                                   *[_p(outs[k]) for k in ("watsat", "bsw", "sucsat", "hksat", "tkmg",
+                                                           "tkdry", "csol")])
+    return outs
