@@ -1,0 +1,310 @@
+"""Benchmark: column-steps/s of the soil/snow column solve on GB300.
+
+Workload (default): 262,144 synthetic columns, snl 60% 0 / 40% 1..12, dtime 3600 s,
+diurnal ground heat flux and Bernoulli(0.1) infiltration pulses (the 262,144-column
+scale/roofline workload).  One step = the synthetic forcing update + soil_temperature!
++ set_soil_water_fractions! + soil_water! (moisture form) over every column, as one
+fused FP64 kernel launch through the C ABI.  The state (~1.6 GB) is far larger than
+L2 (129 MB), so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of CLM.jl's Float64 path (the oracle;
+the Julia reference itself cannot run here) on the host cores, on a bounded sample
+of the same workload.  Under torchrun each rank owns a disjoint column shard
+(weak scaling, no collective on the data path).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "clm.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+with open(os.path.join(ROOT, "BASELINE.json")) as _fh:
+    METRIC = json.load(_fh)["metric"]
+UNIT = "column-steps/s"
+WORKLOAD = "scale/roofline: 262,144 columns, snl 60% 0 / 40% 1..12, dtime 3600 s, diurnal G, infiltration pulses"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nc", type=int, default=262144)
+    ap.add_argument("--cfg", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-column-step DRAM bytes of the column-step kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh)
+    return None
+
+
+def cpu_baseline_sample(wl, cfg, nsample, nsteps=1):
+    """Times the oracle (CPU restatement of the reference path) on the first `nsample`
+    columns for `nsteps` steps with every host thread."""
+    from oracle import oracle as orc
+    cols = np.arange(min(nsample, wl.state.nc))
+    st = wl.state.subset(cols)
+    G, I = wl.forcing_block(range(nsteps), cols=cols)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    orc.run_steps(st, wl.dtime, G, I, cfg, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": len(cols) * nsteps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d columns x %d step(s) of the same workload, OpenMP over columns" % (len(cols), nsteps)}
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference's Float64 path."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from clmgb import abi, synth
+    from oracle import oracle as orc
+    cfg = abi.SwmConfig.clm5_default()
+    nsample = min(args.cpu_sample, args.nc)
+    wl = synth.make_workload(args.cfg, nc=nsample, nsteps=args.warmup + args.steps)
+    st = wl.state
+    threads = os.cpu_count() or 1
+    for t in range(args.warmup):
+        G, I = wl.forcing_block([t])
+        orc.run_steps(st, wl.dtime, G, I, cfg, nthreads=threads)
+    t0 = time.perf_counter()
+    for t in range(args.warmup, args.warmup + args.steps):
+        G, I = wl.forcing_block([t])
+        orc.run_steps(st, wl.dtime, G, I, cfg, nthreads=threads)
+    dt = time.perf_counter() - t0
+    value = nsample * args.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "nc": nsample, "dtime": wl.dtime, "variant": "plain FP64",
+                       "note": "CPU restatement of CLM.jl's Float64 path (Julia is not installed)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "%d columns per step of the same workload" % nsample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from clmgb import abi, api, bytes_model, synth
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cfg = abi.SwmConfig.clm5_default()
+    nsteps = args.warmup + args.steps
+    seed = synth.CONFIGS[args.cfg]["seed"] + 1000 * rank
+    wl = synth.make_workload(args.cfg, nc=args.nc, seed=seed, nsteps=nsteps)
+    st = wl.state
+    nc = st.nc
+    h = api.Handle(st.vp)
+    d = st.to_device()
+    # per-step forcing, resident in HBM before the timed region
+    Gd = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")
+    Id = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")
+    for t in range(nsteps):
+        g, i = wl.forcing(t)
+        Gd[t].copy_(torch.from_numpy(g))
+        Id[t].copy_(torch.from_numpy(i))
+    stream = torch.cuda.current_stream()
+
+    def step(t, ev=None):
+        api.synth_forcing(h, d, Gd[t], Id[t], stream=stream)
+        if ev is not None:
+            ev[0].record(stream)
+        api.column_step(h, d, wl.dtime, cfg, stream=stream)
+        if ev is not None:
+            ev[1].record(stream)
+
+    for t in range(args.warmup):
+        step(t)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(args.warmup + k, evs[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    elapsed_ms = t_start.elapsed_time(t_end)
+    kern_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    status = h.device_status()
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    value = args.steps * nc * world / (elapsed_ms / 1000.0)
+
+    # roofline of the dominant kernel (the fused column step)
+    snl = st["col_snl"]
+    bytes_launch = bytes_model.bytes_per_step(snl, st.vp.nlevgrnd, st.vp.nlevsoi)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_launch / (kern_ms / 1000.0) / 1e9
+    tr = profile_traffic()
+    traffic = None
+    if tr and tr.get("bytes_per_column_step"):
+        traffic = tr["bytes_per_column_step"] * nc
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_column_step",
+                "kernel_ms": kern_ms, "algorithmic_bytes_per_launch": bytes_launch}
+
+    # end to end through the C ABI with host buffers: H2D of the state each step,
+    # the step, D2H of every field the step writes
+    e2e = None
+    if args.e2e_steps > 0:
+        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in st.arrays.items()}
+        written = ["t_soisno", "h2osoi_liq", "h2osoi_ice", "t_h2osfc", "t_grnd", "fact", "thk", "imelt", "xmf",
+                   "xmf_h2osfc", "c_h2osfc", "eflx_fgr12", "eflx_fgr", "eflx_snomelt", "eflx_snomelt_r",
+                   "eflx_h2osfc_to_snow", "eflx_gnet", "dgnetdT", "sabg_chk", "excess_ice", "h2osno_no_layers",
+                   "h2osfc", "int_snow", "snow_depth", "bw", "exice_subs", "snomelt_accum", "qflx_snomelt",
+                   "qflx_snofrz", "qflx_snow_drain", "qflx_h2osfc_to_ice", "qflx_snomelt_lyr", "qflx_snofrz_lyr",
+                   "eff_porosity", "icefrac", "smp_l", "hk_l", "qcharge", "num_substeps", "t_ssbef",
+                   "t_h2osfc_bef", "forc_lwrad", "qflx_infl", "sabg", "sabg_soil", "sabg_snow", "sabg_lyr"]
+        h2d = sum(v.numel() * v.element_size() for v in host.values())
+        d2h = sum(host[k].numel() * host[k].element_size() for k in written)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(args.e2e_steps):
+            for name, hv in host.items():
+                d[name].copy_(hv, non_blocking=True)
+            step(k)
+            for name in written:
+                host[name].copy_(d[name], non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1)
+        e2e = {"value": args.e2e_steps * nc * world / (e2e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(wl, cfg, args.cpu_sample, 1)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "nc_per_gpu": nc, "dtime": wl.dtime, "variant": "plain FP64",
+                           "l2": "inputs larger than L2 (state %.2f GB per GPU)" % (sum(
+                               v.numel() * v.element_size() for v in d.arrays.values()) / 1e9),
+                           "device_status": status, "parallelism": "replicas over disjoint column shards"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": 2 * args.steps, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,144 @@
+"""Python mirror of CLM.jl's entry points for the soil/snow column solve, running the
+hand-written sm_103a kernels through the C ABI (include/clmgb.h).
+
+Names and argument meaning follow the reference:
+  soil_temperature(...)             soil_temperature!        soil_temperature.jl:358
+  set_soil_water_fractions(...)     set_soil_water_fractions! soil_hydrology.jl:394
+  soil_water(...)                   soil_water!              soil_water_movement.jl:1780
+  phase_change_h2osfc / _beta       phase_change_*!          soil_temperature.jl:1857, 2232
+  batched_band_solve(...)           batched_band_solve!      band_diagonal.jl:179
+  tridiagonal_multi(...)            tridiagonal_multi!       tridiagonal.jl:129
+Configurations the reference rejects with error() raise CLMGBError.  Every call
+requires CUDA tensors; there is no CPU path.
+"""
+import ctypes as C
+
+from . import abi
+from ._lib import check, load, CLMGBError  # noqa: F401
+
+
+def _stream(stream):
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _dptr(t, what="tensor"):
+    if t is None:
+        return None
+    if not getattr(t, "is_cuda", False):
+        raise TypeError("%s must be a CUDA tensor (no CPU path)" % what)
+    if not t.is_contiguous():
+        raise ValueError("%s must be contiguous" % what)
+    return C.c_void_p(t.data_ptr())
+
+
+class Handle:
+    """A library handle bound to the current CUDA device (owns the status word)."""
+
+    def __init__(self, vp):
+        self.lib = load()
+        self.vp = vp
+        h = C.c_void_p()
+        check(self.lib.clmgb_create(C.byref(vp), C.byref(h)), "clmgb_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.clmgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def device_status(self, reset=True, stream=None):
+        v = C.c_uint32(0)
+        check(self.lib.clmgb_device_status(self.h, _stream(stream), C.byref(v), 1 if reset else 0),
+              "clmgb_device_status")
+        return v.value
+
+
+def _require_device(state):
+    if not state.on_device:
+        raise TypeError("ColumnState must live on the GPU (state.to_device())")
+
+
+def soil_temperature(handle, state, dtime, snow_method=abi.SNOW_JORDAN1991, use_excess_ice=False,
+                     col_status=None, stream=None):
+    _require_device(state)
+    f = state.soiltemp_fields()
+    b = state.bounds()
+    check(handle.lib.clmgb_soil_temperature(handle.h, C.byref(b), C.byref(f), float(dtime), snow_method,
+                                            1 if use_excess_ice else 0, _dptr(col_status, "col_status"),
+                                            _stream(stream)), "soil_temperature")
+
+
+def set_soil_water_fractions(handle, state, stream=None):
+    _require_device(state)
+    f = state.soilwater_fields()
+    b = state.bounds()
+    check(handle.lib.clmgb_soil_water_fractions(handle.h, C.byref(b), C.byref(f), _stream(stream)),
+          "set_soil_water_fractions")
+
+
+def soil_water(handle, state, dtime, cfg=None, col_status=None, stream=None):
+    _require_device(state)
+    cfg = cfg or abi.SwmConfig.clm5_default()
+    f = state.soilwater_fields()
+    b = state.bounds()
+    check(handle.lib.clmgb_soil_water(handle.h, C.byref(b), C.byref(f), C.byref(cfg), float(dtime),
+                                      _dptr(col_status, "col_status"), _stream(stream)), "soil_water")
+
+
+def column_step(handle, state, dtime, cfg=None, snow_method=abi.SNOW_JORDAN1991, col_status=None,
+                save_bef=True, stream=None):
+    """soil_temperature! + set_soil_water_fractions! + soil_water! in one launch."""
+    _require_device(state)
+    cfg = cfg or abi.SwmConfig.clm5_default()
+    ft, fw, b = state.soiltemp_fields(), state.soilwater_fields(), state.bounds()
+    tss = _dptr(state["t_ssbef"]) if save_bef else None
+    thb = _dptr(state["t_h2osfc_bef"]) if save_bef else None
+    check(handle.lib.clmgb_column_step(handle.h, C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg),
+                                       float(dtime), snow_method, tss, thb, _dptr(col_status, "col_status"),
+                                       _stream(stream)), "column_step")
+
+
+def phase_change_h2osfc(handle, state, dtime, dhsdT, stream=None):
+    _require_device(state)
+    check(handle.lib.clmgb_phase_change_h2osfc(handle.h, C.byref(state.bounds()), C.byref(state.soiltemp_fields()),
+                                               float(dtime), _dptr(dhsdT, "dhsdT"), _stream(stream)),
+          "phase_change_h2osfc")
+
+
+def phase_change_beta(handle, state, dtime, dhsdT, stream=None):
+    _require_device(state)
+    check(handle.lib.clmgb_phase_change_beta(handle.h, C.byref(state.bounds()), C.byref(state.soiltemp_fields()),
+                                             float(dtime), _dptr(dhsdT, "dhsdT"), _stream(stream)),
+          "phase_change_beta")
+
+
+def synth_forcing(handle, state, G, I, stream=None):
+    _require_device(state)
+    check(handle.lib.clmgb_synth_forcing(handle.h, C.byref(state.bounds()), C.byref(state.soiltemp_fields()),
+                                         C.byref(state.soilwater_fields()), _dptr(G, "G"), _dptr(I, "I"),
+                                         _stream(stream)), "synth_forcing")
+
+
+def batched_band_solve(handle, tvector, bmatrix, rvector, jtop, jbot, mask, kl=2, ku=2, nlevsno_off=0,
+                       stream=None):
+    """tvector/rvector: (nlev, nc) CUDA tensors; bmatrix (nlev, nband, nc) == Julia [nc, nband, nlev]."""
+    nlev, nc = tvector.shape
+    check(handle.lib.clmgb_batched_band_solve(handle.h, nc, nc, nlev, _dptr(tvector), _dptr(bmatrix),
+                                              _dptr(rvector), _dptr(jtop), _dptr(jbot), _dptr(mask),
+                                              kl, ku, nlevsno_off, _stream(stream)), "batched_band_solve")
+
+
+def tridiagonal_multi(handle, u, a, b, c, r, jtop, mask, stream=None):
+    nlevs, ncols = u.shape
+    check(handle.lib.clmgb_tridiagonal_multi(handle.h, ncols, ncols, nlevs, _dptr(u), _dptr(a), _dptr(b),
+                                             _dptr(c), _dptr(r), _dptr(jtop), _dptr(mask), _stream(stream)),
+          "tridiagonal_multi")

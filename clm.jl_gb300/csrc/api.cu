@@ -1,0 +1,288 @@
+// api.cu — the C ABI (include/clmgb.h): argument validation, handle, launches.
+//
+// Invalid arguments and configurations the reference rejects with error() are
+// reported as negative return codes before anything is enqueued; there is no CPU
+// fallback.  Device-side per-column conditions are OR-ed into the handle's status
+// word, read back with clmgb_device_status().
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include "clmgb_device.cuh"
+#include "launch.h"
+
+#ifndef CLMGB_GIT_DESC
+#define CLMGB_GIT_DESC "dev"
+#endif
+#define CLMGB_STR_(x) #x
+#define CLMGB_XSTR(x) CLMGB_STR_(x)
+
+struct clmgb_handle_s {
+  uint32_t magic;
+  int device;
+  clmgb_varpar vp;
+  uint32_t* dev_status;      // device word: OR of CLMGB_COL_* bits
+  cudaError_t last_error;
+};
+
+static const uint32_t HANDLE_MAGIC = 0xC1A9B300u;
+
+using clmgb::Dims;
+
+static bool handle_ok(clmgb_handle h) { return h && h->magic == HANDLE_MAGIC; }
+
+static int32_t cuda_fail(clmgb_handle h, cudaError_t e) {
+  if (h) h->last_error = e;
+  return CLMGB_ERR_CUDA;
+}
+
+static int32_t check_varpar(const clmgb_varpar* vp) {
+  if (!vp) return CLMGB_ERR_NULL_ARG;
+  if (vp->nlevsno < 1 || vp->nlevsno > CLMGB_MAX_NLEVSNO) return CLMGB_ERR_DIMS;
+  if (vp->nlevgrnd < 2 || vp->nlevgrnd > CLMGB_MAX_NLEVGRND) return CLMGB_ERR_DIMS;
+  if (vp->nlevsoi < 1 || vp->nlevsoi > vp->nlevgrnd || vp->nlevsoi > CLMGB_MAX_NLEVSOI) return CLMGB_ERR_DIMS;
+  if (vp->nlevurb < 0 || vp->nlevurb > vp->nlevgrnd) return CLMGB_ERR_DIMS;
+  if (vp->nlevmaxurbgrnd != vp->nlevgrnd) return CLMGB_ERR_DIMS;
+  return CLMGB_OK;
+}
+
+static int32_t check_bounds(const clmgb_bounds* b, bool need_patches) {
+  if (!b) return CLMGB_ERR_NULL_ARG;
+  if (b->nc < 0 || b->ldc < b->nc || b->np < 0 || b->ldp < b->np || b->nl < 0) return CLMGB_ERR_DIMS;
+  if (need_patches && b->nc > 0 && (b->np < 1 || b->nl < 1)) return CLMGB_ERR_DIMS;
+  return CLMGB_OK;
+}
+
+static Dims make_dims(const clmgb_varpar& vp, const clmgb_bounds& b) {
+  Dims D;
+  D.nlevsno = vp.nlevsno;
+  D.nlevgrnd = vp.nlevgrnd;
+  D.nlevsoi = vp.nlevsoi;
+  D.nlevurb = vp.nlevurb;
+  D.nlevmax = vp.nlevmaxurbgrnd;
+  D.ldc = b.ldc;
+  D.ldp = b.ldp;
+  D.np = b.np;
+  return D;
+}
+
+// every pointer member after struct_size must be non-NULL
+template <typename S>
+static int32_t check_fields(const S* f) {
+  if (!f) return CLMGB_ERR_NULL_ARG;
+  if (f->struct_size != (int64_t)sizeof(S)) return CLMGB_ERR_ABI;
+  const char* base = reinterpret_cast<const char*>(f) + sizeof(int64_t);
+  const size_t nptr = (sizeof(S) - sizeof(int64_t)) / sizeof(void*);
+  for (size_t i = 0; i < nptr; i++) {
+    const void* p;
+    memcpy(&p, base + i * sizeof(void*), sizeof(void*));
+    if (!p) return CLMGB_ERR_NULL_ARG;
+  }
+  return CLMGB_OK;
+}
+
+static int32_t check_cfg(const clmgb_swm_config* cfg) {
+  if (!cfg) return CLMGB_ERR_NULL_ARG;
+  if (cfg->soilwater_movement_method == CLMGB_ZENGDECKER_2009) return CLMGB_ERR_UNSUPPORTED;
+  if (cfg->soilwater_movement_method != CLMGB_MOISTURE_FORM) return CLMGB_ERR_CONFIG;
+  if (cfg->upper_boundary_condition != CLMGB_BC_FLUX) return CLMGB_ERR_CONFIG;
+  const int lb = cfg->lower_boundary_condition;
+  if (lb == CLMGB_BC_AQUIFER) return CLMGB_ERR_UNSUPPORTED;
+  if (!(lb == CLMGB_BC_WATERTABLE || lb == CLMGB_BC_FLUX || lb == CLMGB_BC_ZERO_FLUX)) return CLMGB_ERR_CONFIG;
+  if (cfg->flux_calculation != 1 && cfg->flux_calculation != 42) return CLMGB_ERR_CONFIG;
+  if (!(cfg->dtmin > 0.0)) return CLMGB_ERR_CONFIG;
+  return CLMGB_OK;
+}
+
+extern "C" {
+
+int32_t clmgb_abi_version(void) { return CLMGB_ABI_VERSION; }
+
+const char* clmgb_build_info(void) {
+  return "clmgb " CLMGB_GIT_DESC " sm_103a fp64 fmad=off (CUDA runtime " CLMGB_XSTR(CUDART_VERSION) ")";
+}
+
+const char* clmgb_strerror(int32_t code) {
+  switch (code) {
+    case CLMGB_OK: return "ok";
+    case CLMGB_ERR_NULL_ARG: return "a required pointer is NULL";
+    case CLMGB_ERR_DIMS: return "level counts or column/patch dimensions out of the supported range";
+    case CLMGB_ERR_CONFIG: return "configuration rejected (the reference raises error() for it)";
+    case CLMGB_ERR_UNSUPPORTED: return "configuration not implemented by this library";
+    case CLMGB_ERR_CUDA: return "CUDA launch or copy failed";
+    case CLMGB_ERR_ABI: return "struct size / ABI version mismatch";
+    case CLMGB_ERR_HANDLE: return "invalid handle";
+    default: return "unknown error";
+  }
+}
+
+int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
+  if (!out) return CLMGB_ERR_NULL_ARG;
+  *out = nullptr;
+  int32_t e = check_varpar(vp);
+  if (e) return e;
+  clmgb_handle h = new clmgb_handle_s();
+  h->magic = HANDLE_MAGIC;
+  h->vp = *vp;
+  h->last_error = cudaSuccess;
+  cudaError_t ce = cudaGetDevice(&h->device);
+  if (ce == cudaSuccess) ce = cudaMalloc(&h->dev_status, sizeof(uint32_t));
+  if (ce == cudaSuccess) ce = cudaMemset(h->dev_status, 0, sizeof(uint32_t));
+  if (ce != cudaSuccess) {
+    h->magic = 0;
+    delete h;
+    return CLMGB_ERR_CUDA;
+  }
+  *out = h;
+  return CLMGB_OK;
+}
+
+int32_t clmgb_destroy(clmgb_handle h) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  cudaFree(h->dev_status);
+  h->magic = 0;
+  delete h;
+  return CLMGB_OK;
+}
+
+int32_t clmgb_device_status(clmgb_handle h, void* stream, uint32_t* status, int32_t reset) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (!status) return CLMGB_ERR_NULL_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t v = 0;
+  cudaError_t ce = cudaMemcpyAsync(&v, h->dev_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess && reset) ce = cudaMemsetAsync(h->dev_status, 0, sizeof(uint32_t), s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return cuda_fail(h, ce);
+  *status = v;
+  return CLMGB_OK;
+}
+
+int32_t clmgb_last_cuda_error(clmgb_handle h) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  return (int32_t)h->last_error;
+}
+
+int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* f,
+                               double dtime, int32_t snow_method, int32_t use_excess_ice,
+                               uint32_t* col_status, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, true);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
+  if (use_excess_ice) return CLMGB_ERR_UNSUPPORTED;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  cudaError_t ce = clmgb::launch_soil_temperature(make_dims(h->vp, *b), b->nc, *f, dtime, snow_method, col_status,
+                                                  h->dev_status, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                                   void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, false);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  cudaError_t ce = clmgb::launch_water_fractions(make_dims(h->vp, *b), b->nc, *f, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                         const clmgb_swm_config* cfg, double dtime, uint32_t* col_status, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_cfg(cfg);
+  if (e) return e;
+  if ((e = check_bounds(b, false))) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  cudaError_t ce = clmgb::launch_moisture_form(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status,
+                                               h->dev_status, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                          const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
+                          int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
+                          void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_cfg(cfg);
+  if (e) return e;
+  if ((e = check_bounds(b, true))) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(ft))) return e;
+  if ((e = check_fields(fw))) return e;
+  if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  cudaError_t ce = clmgb::launch_column_step(make_dims(h->vp, *b), b->nc, *ft, *fw, *cfg, dtime, snow_method,
+                                             t_ssbef, t_h2osfc_bef, col_status, h->dev_status,
+                                             (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+static int32_t phase_change_common(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* f,
+                                   double dtime, const double* dhsdT, int which, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, true);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (!dhsdT) return CLMGB_ERR_NULL_ARG;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  cudaError_t ce = clmgb::launch_phase_change(make_dims(h->vp, *b), b->nc, *f, dtime, dhsdT, which,
+                                              (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_phase_change_h2osfc(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* f,
+                                  double dtime, const double* dhsdT, void* stream) {
+  return phase_change_common(h, b, f, dtime, dhsdT, 0, stream);
+}
+
+int32_t clmgb_phase_change_beta(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* f,
+                                double dtime, const double* dhsdT, void* stream) {
+  return phase_change_common(h, b, f, dtime, dhsdT, 1, stream);
+}
+
+int32_t clmgb_synth_forcing(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                            const clmgb_soilwater_fields* fw, const double* G, const double* I, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, true);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(ft))) return e;
+  if ((e = check_fields(fw))) return e;
+  if (!G || !I) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_synth_forcing(make_dims(h->vp, *b), b->nc, *ft, *fw, G, I, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_batched_band_solve(clmgb_handle h, int64_t nc, int64_t ldc, int32_t nlev, double* tvector,
+                                 const double* bmatrix, const double* rvector, const int64_t* jtop,
+                                 const int64_t* jbot, const uint8_t* mask, int32_t kl, int32_t ku,
+                                 int32_t nlevsno_off, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (nc < 0 || ldc < nc || nlev < 1 || nlev > clmgb::MAXROWS + 1) return CLMGB_ERR_DIMS;
+  if (!((kl == 2 && ku == 2) || (kl == 1 && ku == 1))) return CLMGB_ERR_UNSUPPORTED;
+  if (nc == 0) return CLMGB_OK;
+  if (!tvector || !bmatrix || !rvector || !jtop || !jbot || !mask) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_band_solve(nc, ldc, nlev, tvector, bmatrix, rvector, jtop, jbot, mask, kl, ku,
+                                            nlevsno_off, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_tridiagonal_multi(clmgb_handle h, int64_t ncols, int64_t ldc, int32_t nlevs, double* u,
+                                const double* a, const double* b, const double* c, const double* r,
+                                const int64_t* jtop, const uint8_t* mask, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (ncols < 0 || ldc < ncols || nlevs < 1 || nlevs > 64) return CLMGB_ERR_DIMS;
+  if (ncols == 0) return CLMGB_OK;
+  if (!u || !a || !b || !c || !r || !jtop || !mask) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_tridiagonal_multi(ncols, ldc, nlevs, u, a, b, c, r, jtop, mask,
+                                                   (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+}  // extern "C"

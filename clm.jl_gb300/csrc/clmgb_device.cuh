@@ -1,0 +1,951 @@
+// clmgb_device.cuh — per-column device code of the GB300 soil/snow column solve.
+//
+// One CUDA thread owns one column.  Every field is read in CLM.jl's own layout
+// (Julia column-major [nc, nlev]: element (c, jj) at c + (jj-1)*ldc), so the 32
+// threads of a warp touch 32 consecutive doubles of a level: every load and store
+// is a fully coalesced 256-byte transaction with no staging.
+//
+// Arithmetic follows the reference's Float64 expressions operation by operation
+// (this file is compiled with --fmad=false so a*b+c is never fused, as in Julia),
+// which makes the results equal to the CPU oracle except where a transcendental
+// (pow, log10) differs in the last ulp.  Citations are to CLM.jl source files.
+#pragma once
+#include <stdint.h>
+#include <math.h>
+#include "../../include/clmgb.h"
+
+namespace clmgb {
+
+// ---- constants: src/constants/varcon.jl:15-70 ----
+constexpr double GRAV = 9.80616;
+constexpr double SB = 5.67e-8;
+constexpr double CPLIQ = 4188.0;
+constexpr double CPICE = 2117.27;
+constexpr double HFUS = 3.337e5;
+constexpr double DENH2O = 1000.0;
+constexpr double DENICE = 917.0;
+constexpr double TFRZ = 273.15;
+constexpr double TKAIR = 0.023;
+constexpr double TKICE = 2.290;
+constexpr double TKWAT = 0.57;
+constexpr double CAPR = 0.34;
+constexpr double CNFAC = 0.5;
+constexpr double THK_BEDROCK = 3.0;
+constexpr double CSOL_BEDROCK = 2.0e6;
+constexpr double THIN_SFCLAYER = 1.0e-6;
+constexpr double M_TO_MM = 1.0e3;
+// landunit / column types: src/constants/landunit_varcon.jl, column_varcon.jl
+constexpr int64_t ISTSOIL = 1, ISTCROP = 2, ISTICE = 4, ISTWET = 6;
+constexpr int64_t ICOL_ROOF = 71, ICOL_SUNWALL = 72, ICOL_SHADEWALL = 73;
+constexpr int64_t ICOL_ROAD_IMPERV = 74, ICOL_ROAD_PERV = 75;
+
+// compile-time level capacities of the per-thread arrays
+constexpr int MAXSNO = CLMGB_MAX_NLEVSNO;
+constexpr int MAXGRND = CLMGB_MAX_NLEVGRND;
+constexpr int MAXL = MAXSNO + MAXGRND;       // snow + ground levels
+constexpr int MAXROWS = MAXL + 1;            // + the surface-water row of the band system
+constexpr int MAXSOI = CLMGB_MAX_NLEVSOI;
+constexpr int MF_ATTEMPT_CAP = 4096;         // safety cap on Richards substep attempts
+
+struct Dims {
+  int nlevsno, nlevgrnd, nlevsoi, nlevurb, nlevmax;
+  int64_t ldc, ldp, np;
+};
+
+// Julia Base.max / Base.min on Float64 (NaN propagates, -0.0 < 0.0).
+__device__ __forceinline__ double jl_max(double x, double y) {
+  if (x != x) return x;
+  if (y != y) return y;
+  if (x > y) return x;
+  if (y > x) return y;
+  return signbit(x) ? y : x;
+}
+__device__ __forceinline__ double jl_min(double x, double y) {
+  if (x != x) return x;
+  if (y != y) return y;
+  if (x < y) return x;
+  if (y < x) return y;
+  return signbit(x) ? x : y;
+}
+// Julia's Float64 x^4 (Base.Math.pow_body, compensated squaring).
+__device__ __forceinline__ double jl_pow4(double x) {
+  double x2 = __dmul_rn(x, x);
+  double lo1 = __fma_rn(x, x, -x2);
+  double x4 = __dmul_rn(x2, x2);
+  double lo2 = __fma_rn(x2, x2, -x4);
+  double xnlo = lo2 + (x2 * 2.0 * lo1);
+  if (isfinite(x4) && isfinite(xnlo)) return x4 + xnlo;
+  return x4;
+}
+
+// level-indexed access, jj 1-based like the Julia code
+template <typename T>
+__device__ __forceinline__ T& LV(T* p, int64_t c, int jj, int64_t ld) {
+  return p[c + (int64_t)(jj - 1) * ld];
+}
+template <typename T>
+__device__ __forceinline__ T LVc(const T* p, int64_t c, int jj, int64_t ld) {
+  return __ldg(p + c + (int64_t)(jj - 1) * ld);
+}
+
+__device__ __forceinline__ bool is_wallroof(int64_t it) {
+  return it == ICOL_SUNWALL || it == ICOL_SHADEWALL || it == ICOL_ROOF;
+}
+
+// ===========================================================================
+// Banded pivoted LU for one column (band_diagonal.jl:87-170).
+//
+// The reference densifies the 5-band system into an n x n matrix and runs partial-
+// pivot Gaussian elimination over all n columns.  Every entry outside the band is
+// an exact zero, so each elimination it performs there is x - 0*y == x: the banded
+// form below performs exactly the in-band operations, in the same order, and gives
+// the same bits for every finite non-singular system.  With partial pivoting the
+// upper factor widens to kl+ku, so each row keeps 2*kl+ku+1 entries:
+// ab[r*W + d] holds A[r, r-kl+d].
+// ===========================================================================
+template <int KL, int KU>
+__device__ __forceinline__ void band_lu_solve(double* ab, double* x, int n) {
+  constexpr int W = 2 * KL + KU + 1;
+#define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
+  for (int k = 0; k < n - 1; k++) {
+    int piv = k;
+    double maxv = fabs(AB(k, k));
+    const int ilast = min(n - 1, k + KL);
+    for (int i = k + 1; i <= ilast; i++) {
+      double v = fabs(AB(i, k));
+      if (v > maxv) { maxv = v; piv = i; }
+    }
+    const double akk = AB(piv, k);
+    const int clast = min(n - 1, k + KL + KU);
+    if (piv != k) {
+      for (int col = k; col <= clast; col++) {
+        double akj = AB(k, col), apj = AB(piv, col);
+        AB(k, col) = apj;
+        AB(piv, col) = akj;
+      }
+      double xk = x[k], xp = x[piv];
+      x[k] = xp;
+      x[piv] = xk;
+    }
+    for (int i = k + 1; i <= ilast; i++) {
+      const double f = AB(i, k) / akk;
+      for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
+      x[i] = x[i] - f * x[k];
+    }
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    double s = x[i];
+    const int jl = min(n - 1, i + KL + KU);
+    for (int j = i + 1; j <= jl; j++) s = s - AB(i, j) * x[j];
+    x[i] = s / AB(i, i);
+  }
+#undef AB
+}
+
+// ===========================================================================
+// phase_change_h2osfc! (soil_temperature.jl:1757-1855), column c.
+// ===========================================================================
+__device__ inline void phase_change_h2osfc_col(const Dims& D, const clmgb_soiltemp_fields& f,
+                                        int64_t c, double dtime, double dhsdT) {
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno;
+  const int64_t snl = f.col_snl[c];
+  double* T = f.t_soisno;
+  f.xmf_h2osfc[c] = 0.0;
+  f.qflx_h2osfc_to_ice[c] = 0.0;
+  f.eflx_h2osfc_to_snow[c] = 0.0;
+  const double fh = f.frac_h2osfc[c];
+  if (fh > 0.0 && f.t_h2osfc[c] <= TFRZ) {
+    const double tinc = TFRZ - f.t_h2osfc[c];
+    f.t_h2osfc[c] = TFRZ;
+    const double ch = f.c_h2osfc[c];
+    const double hm = fh * (dhsdT * tinc - tinc * ch / dtime);
+    const double xm = hm * dtime / HFUS;
+    const double temp1 = f.h2osfc[c] + xm;
+    double h2osno_total = f.h2osno_no_layers[c];
+    if (snl < 0)
+      for (int j = (int)snl + 1; j <= 0; j++)
+        h2osno_total += LV(f.h2osoi_ice, c, j + joff, ld) + LV(f.h2osoi_liq, c, j + joff, ld);
+    const double fs = f.frac_sno_eff[c];
+    const double z_avg = fs * f.snow_depth[c];
+    double rho_avg = z_avg > 0.0 ? jl_min(800.0, h2osno_total / z_avg) : 200.0;
+    if (temp1 >= 0.0) {
+      f.int_snow[c] -= xm;
+      if (snl == 0) f.h2osno_no_layers[c] -= xm;
+      else LV(f.h2osoi_ice, c, joff, ld) -= xm;
+      h2osno_total -= xm;
+      f.h2osfc[c] += xm;
+      f.xmf_h2osfc[c] = hm;
+      f.qflx_h2osfc_to_ice[c] = -xm / dtime;
+      if (fs > 0.0 && snl < 0) f.snow_depth[c] = h2osno_total / (rho_avg * fs);
+      else f.snow_depth[c] = h2osno_total / DENICE;
+      if (snl == 0) {
+        LV(T, c, joff, ld) = f.t_h2osfc[c];
+        f.eflx_h2osfc_to_snow[c] = 0.0;
+      } else {
+        double c1;
+        if (snl == -1) c1 = fs * (dtime / LV(f.fact, c, joff, ld) - dhsdT * dtime);
+        else c1 = fs / LV(f.fact, c, joff, ld) * dtime;
+        const double c2 = fh != 0.0 ? (-CPLIQ * xm - fh * dhsdT * dtime) : 0.0;
+        LV(T, c, joff, ld) = (c1 * LV(T, c, joff, ld) + c2 * f.t_h2osfc[c]) / (c1 + c2);
+        f.eflx_h2osfc_to_snow[c] = (f.t_h2osfc[c] - LV(T, c, joff, ld)) * c2 / dtime;
+      }
+    } else {
+      rho_avg = (h2osno_total * rho_avg + f.h2osfc[c] * DENICE) / (h2osno_total + f.h2osfc[c]);
+      f.int_snow[c] += f.h2osfc[c];
+      if (snl == 0) f.h2osno_no_layers[c] += f.h2osfc[c];
+      else LV(f.h2osoi_ice, c, joff, ld) += f.h2osfc[c];
+      h2osno_total += f.h2osfc[c];
+      f.qflx_h2osfc_to_ice[c] = f.h2osfc[c] / dtime;
+      f.t_h2osfc[c] -= temp1 * HFUS / (dtime * dhsdT - ch);
+      f.xmf_h2osfc[c] = hm - fh * temp1 * HFUS / dtime;
+      if (snl == 0) {
+        LV(T, c, joff, ld) = f.t_h2osfc[c];
+      } else {
+        double c1;
+        if (snl == -1) c1 = fs * (dtime / LV(f.fact, c, joff, ld) - dhsdT * dtime);
+        else c1 = fs / LV(f.fact, c, joff, ld) * dtime;
+        const double c2 = fh != 0.0 ? fh * (ch - dtime * dhsdT) : 0.0;
+        LV(T, c, joff, ld) = (c1 * LV(T, c, joff, ld) + c2 * f.t_h2osfc[c]) / (c1 + c2);
+        f.t_h2osfc[c] = LV(T, c, joff, ld);
+      }
+      f.h2osfc[c] = 0.0;
+      if (fs > 0.0 && snl < 0) f.snow_depth[c] = h2osno_total / (rho_avg * fs);
+      else f.snow_depth[c] = h2osno_total / DENICE;
+    }
+  }
+}
+
+// ===========================================================================
+// phase_change_beta! (soil_temperature.jl:1929-2230), hard Float64 path, column c.
+// The reference's four sequential level loops per thread are kept; the per-call
+// scratch rows (PcbTmp) become per-thread arrays.
+// ===========================================================================
+__device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp_fields& f,
+                                      int64_t c, double dtime, double dhsdT) {
+  const int64_t ld = D.ldc;
+  const int nlevsno = D.nlevsno, nlevgrnd = D.nlevgrnd, nlevmax = D.nlevmax;
+  const int joff = nlevsno;
+  const int64_t snl = f.col_snl[c];
+  const int64_t l = f.col_landunit[c] - 1;
+  const int64_t it = f.col_itype[c];
+  const int64_t lit = f.lun_itype[l];
+  const bool wallroof = is_wallroof(it);
+  double hm[MAXL + 1], xm[MAXL + 1], wice0[MAXL + 1], wexice0[MAXL + 1], wmass0[MAXL + 1];
+  double tinc[MAXL + 1], supercool[MAXGRND + 1];
+  double* T = f.t_soisno;
+  double* ICE = f.h2osoi_ice;
+  double* LIQ = f.h2osoi_liq;
+  double* EXI = f.excess_ice;
+  const double fse = f.frac_sno_eff[c];
+  const double fh = f.frac_h2osfc[c];
+  f.xmf[c] = 0.0;
+  f.qflx_snomelt[c] = 0.0;
+  f.qflx_snofrz[c] = 0.0;
+  f.qflx_snow_drain[c] = 0.0;
+  for (int j = -nlevsno + 1; j <= nlevmax; j++) {
+    const int jj = j + joff;
+    tinc[jj] = 0.0;
+    if (j >= snl + 1) {
+      LV(f.imelt, c, jj, ld) = 0;
+      hm[jj] = 0.0;
+      xm[jj] = 0.0;
+      wice0[jj] = LV(ICE, c, jj, ld);
+      wexice0[jj] = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
+      wmass0[jj] = LV(ICE, c, jj, ld) + LV(LIQ, c, jj, ld) + wexice0[jj];
+      if (j >= 1) LV(f.exice_subs, c, j, ld) = 0.0;
+    }
+    if (j <= 0) {
+      LV(f.qflx_snomelt_lyr, c, jj, ld) = 0.0;
+      LV(f.qflx_snofrz_lyr, c, jj, ld) = 0.0;
+    }
+  }
+  for (int j = (int)snl + 1; j <= 0; j++) {
+    const int jj = j + joff;
+    if (LV(ICE, c, jj, ld) > 0.0 && LV(T, c, jj, ld) > TFRZ) {
+      LV(f.imelt, c, jj, ld) = 1;
+      tinc[jj] = TFRZ - LV(T, c, jj, ld);
+      LV(T, c, jj, ld) = TFRZ;
+    }
+    if (LV(LIQ, c, jj, ld) > 0.0 && LV(T, c, jj, ld) < TFRZ) {
+      LV(f.imelt, c, jj, ld) = 2;
+      tinc[jj] = TFRZ - LV(T, c, jj, ld);
+      LV(T, c, jj, ld) = TFRZ;
+    }
+  }
+  const bool supercool_type = (lit == ISTSOIL || lit == ISTCROP || it == ICOL_ROAD_PERV);
+  for (int j = 1; j <= nlevmax; j++) {
+    const int jj = j + joff;
+    supercool[j] = 0.0;
+    const bool active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= D.nlevurb);
+    if (!active) continue;
+    if (LV(ICE, c, jj, ld) > 0.0 && LV(T, c, jj, ld) > TFRZ) {
+      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+    }
+    if (LV(EXI, c, j, ld) > 0.0 && LV(T, c, jj, ld) > TFRZ) {
+      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+    }
+    if (supercool_type) {
+      const double tt = LV(T, c, jj, ld);
+      if (tt < TFRZ) {
+        const double smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
+        double sc = LVc(f.watsat, c, j, ld) * pow(smp / LVc(f.sucsat, c, j, ld), -1.0 / LVc(f.bsw, c, j, ld));
+        sc *= LVc(f.dz, c, jj, ld) * 1000.0;
+        supercool[j] = sc;
+      }
+    }
+    if (LV(LIQ, c, jj, ld) > supercool[j] && LV(T, c, jj, ld) < TFRZ) {
+      LV(f.imelt, c, jj, ld) = 2; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+    }
+    if (f.h2osno_no_layers[c] > 0.0 && j == 1) {
+      if (LV(T, c, jj, ld) > TFRZ) {
+        LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+      }
+    }
+  }
+  for (int j = (int)snl + 1; j <= nlevmax; j++) {
+    const int jj = j + joff;
+    const bool active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= D.nlevurb);
+    if (!active) continue;
+    int64_t im = LV(f.imelt, c, jj, ld);
+    const double fct = LV(f.fact, c, jj, ld);
+    if (im > 0) {
+      if (j == snl + 1) {
+        if (j > 0) hm[jj] = dhsdT * tinc[jj] - tinc[jj] / fct;
+        else hm[jj] = fse * (dhsdT * tinc[jj] - tinc[jj] / fct);
+        if (j == 1 && fh != 0.0) hm[jj] -= fh * dhsdT * tinc[jj];
+      } else if (j == 1) {
+        hm[jj] = (1.0 - fse - fh) * dhsdT * tinc[jj] - tinc[jj] / fct;
+      } else {
+        if (j < 1) hm[jj] = -fse * tinc[jj] / fct;
+        else hm[jj] = -tinc[jj] / fct;
+      }
+    }
+    if (im == 1 && hm[jj] < 0.0) { hm[jj] = 0.0; im = 0; }
+    if (im == 2 && hm[jj] > 0.0) { hm[jj] = 0.0; im = 0; }
+    LV(f.imelt, c, jj, ld) = im;
+    if (im > 0 && fabs(hm[jj]) > 0.0) {
+      xm[jj] = hm[jj] * dtime / HFUS;
+      if (j == 1) {
+        if (f.h2osno_no_layers[c] > 0.0 && xm[jj] > 0.0) {
+          const double temp1 = f.h2osno_no_layers[c];
+          f.h2osno_no_layers[c] = jl_max(0.0, temp1 - xm[jj]);
+          const double propor = f.h2osno_no_layers[c] / temp1;
+          f.snow_depth[c] = propor * f.snow_depth[c];
+          const double heatr0 = hm[jj] - HFUS * (temp1 - f.h2osno_no_layers[c]) / dtime;
+          if (heatr0 > 0.0) { xm[jj] = heatr0 * dtime / HFUS; hm[jj] = heatr0; }
+          else { xm[jj] = 0.0; hm[jj] = 0.0; }
+          f.qflx_snomelt[c] = jl_max(0.0, temp1 - f.h2osno_no_layers[c]) / dtime;
+          f.xmf[c] = HFUS * f.qflx_snomelt[c];
+          f.qflx_snow_drain[c] = f.qflx_snomelt[c];
+        }
+      }
+      double heatr = 0.0;
+      double ice = LV(ICE, c, jj, ld);
+      if (xm[jj] > 0.0) {
+        ice = jl_max(0.0, wice0[jj] - xm[jj]);
+        LV(ICE, c, jj, ld) = ice;
+        heatr = hm[jj] - HFUS * (wice0[jj] - ice) / dtime;
+        const double xm2 = xm[jj] - ice;
+        if (ice == 0.0) {
+          if (wexice0[jj] >= 0.0 && xm2 > 0.0 && j >= 2) {
+            const double ex = jl_max(0.0, wexice0[jj] - xm2);
+            LV(EXI, c, j, ld) = ex;
+            heatr = hm[jj] - HFUS * (wexice0[jj] - ex + wice0[jj] - ice) / dtime;
+          }
+        }
+      } else if (xm[jj] < 0.0) {
+        if (j <= 0) {
+          ice = jl_min(wmass0[jj], wice0[jj] - xm[jj]);
+        } else {
+          if (wmass0[jj] - wexice0[jj] < supercool[j]) ice = 0.0;
+          else ice = jl_min(wmass0[jj] - wexice0[jj] - supercool[j], wice0[jj] - xm[jj]);
+        }
+        LV(ICE, c, jj, ld) = ice;
+        heatr = hm[jj] - HFUS * (wice0[jj] - ice) / dtime;
+      }
+      const double ei_val = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
+      const double liq = jl_max(0.0, wmass0[jj] - ice - ei_val);
+      LV(LIQ, c, jj, ld) = liq;
+      if (fabs(heatr) > 0.0) {
+        double tt = LV(T, c, jj, ld);
+        if (j == snl + 1) {
+          if (j == 1) tt += fct * heatr / (1.0 - (1.0 - fh) * fct * dhsdT);
+          else if (fse > 0.0) tt += (fct / fse) * heatr / (1.0 - fct * dhsdT);
+        } else if (j == 1) {
+          tt += fct * heatr / (1.0 - (1.0 - fse - fh) * fct * dhsdT);
+        } else {
+          if (j > 0) tt += fct * heatr;
+          else if (fse > 0.0) tt += (fct / fse) * heatr;
+        }
+        if (j <= 0)
+          if (liq * ice > 0.0) tt = TFRZ;
+        LV(T, c, jj, ld) = tt;
+      }
+      if (j >= 1) {
+        const double ex = LV(EXI, c, j, ld);
+        f.xmf[c] += HFUS * (wice0[jj] - ice) / dtime + HFUS * (wexice0[jj] - ex) / dtime;
+        LV(f.exice_subs, c, j, ld) = jl_max(0.0, (wexice0[jj] - ex) / DENICE);
+      } else {
+        f.xmf[c] += HFUS * (wice0[jj] - ice) / dtime;
+      }
+      if (im == 1 && j < 1) {
+        const double q = jl_max(0.0, wice0[jj] - ice) / dtime;
+        LV(f.qflx_snomelt_lyr, c, jj, ld) = q;
+        f.qflx_snomelt[c] += q;
+        f.snomelt_accum[c] += q * dtime * 1.0e-3;
+      }
+      if (im == 2 && j < 1) {
+        const double q = jl_max(0.0, ice - wice0[jj]) / dtime;
+        LV(f.qflx_snofrz_lyr, c, jj, ld) = q;
+        f.qflx_snofrz[c] += q;
+      }
+    }
+  }
+  f.eflx_snomelt[c] = f.qflx_snomelt[c] * HFUS;
+  if (f.lun_urbpoi[l]) f.eflx_snomelt_u[c] = f.eflx_snomelt[c];
+  else if (lit == ISTSOIL || lit == ISTCROP) f.eflx_snomelt_r[c] = f.eflx_snomelt[c];
+}
+
+// ===========================================================================
+// soil_temperature! (soil_temperature.jl:358-593) for one non-urban column,
+// all of its kernels fused in the reference's call order.
+// ===========================================================================
+__device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soiltemp_fields& f,
+                                         int64_t c, double dtime, int snow_method) {
+  const int64_t ld = D.ldc, ldp = D.ldp;
+  const int nlevsno = D.nlevsno, nlevgrnd = D.nlevgrnd, nlevsoi = D.nlevsoi;
+  const int nlevmax = D.nlevmax;
+  const int joff = nlevsno;
+  const int nlev = nlevsno + nlevmax;
+  const int64_t snl = f.col_snl[c];
+  if (snl > 0 || snl < -nlevsno) return CLMGB_COL_LEVEL_RANGE;
+  const int64_t l = f.col_landunit[c] - 1;
+  const int64_t it = f.col_itype[c];
+  const int64_t lit = f.lun_itype[l];
+  if (f.lun_urbpoi[l] || is_wallroof(it) || it == ICOL_ROAD_IMPERV || it == ICOL_ROAD_PERV)
+    return CLMGB_COL_URBAN;
+  const int jtop = (int)snl + 1;          // top active layer (Fortran numbering)
+  const int jjtop = jtop + joff;          // its 1-based level index
+  const bool is_special = (lit == ISTWET || lit == ISTICE);
+  const int64_t nbedrock = f.col_nbedrock[c];
+  const double fse = f.frac_sno_eff[c];
+  const double fh = f.frac_h2osfc[c];
+  double* T = f.t_soisno;
+  const double* DZ = f.dz;
+  const double* Z = f.z;
+  const double* ZI = f.zi;
+  const double* LIQ = f.h2osoi_liq;
+  const double* ICE = f.h2osoi_ice;
+  const double* EXI = f.excess_ice;
+
+  // per-column working rows (level index jj, 1-based; entries outside the active
+  // range are never read)
+  double tk[MAXL + 2], fn[MAXL + 2], fct[MAXL + 2], tt[MAXL + 2], zz[MAXL + 2];
+
+  // ---- soil_therm_prop!: layer conductivity thk (_soil_snow_tk_kernel! :647-716) ----
+  // thk kept in tk[] first, interface conductivity computed in place afterwards.
+  for (int jj = jjtop; jj <= nlev; jj++) {
+    tt[jj] = LV(T, c, jj, ld);
+    zz[jj] = LVc(Z, c, jj, ld);
+  }
+  for (int jj = jjtop; jj <= nlevsno + nlevgrnd; jj++) {
+    const int j = jj - nlevsno;
+    double thkv = 0.0;
+    if (j >= 1) {
+      if (!is_special) {
+        if (j > nbedrock) {
+          thkv = THK_BEDROCK;             // bedrock overrides the soil value (:684-686)
+        } else {
+          const double liq = LV(LIQ, c, jj, ld), ice = LV(ICE, c, jj, ld), exi = LV(EXI, c, j, ld);
+          const double dzv = LVc(DZ, c, jj, ld), ws = LVc(f.watsat, c, j, ld);
+          double satw = (liq / DENH2O + ice / DENICE + exi / DENICE) / (dzv * ws);
+          satw = jl_min(1.0, satw);
+          if (satw > 1.0e-7) {
+            double dke;
+            if (tt[jj] >= TFRZ) dke = jl_max(0.0, log10(satw) + 1.0);
+            else dke = satw;
+            const double a1 = liq / (DENH2O * dzv);
+            const double fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
+            const double fl = a1 / fl_denom;
+            const double dksat = LVc(f.tkmg, c, j, ld) * pow(TKWAT, fl * ws) * pow(TKICE, (1.0 - fl) * ws);
+            thkv = dke * dksat + (1.0 - dke) * LVc(f.tkdry, c, j, ld);
+          } else {
+            thkv = LVc(f.tkdry, c, j, ld);
+          }
+        }
+      } else if (lit == ISTICE) {
+        thkv = tt[jj] < TFRZ ? TKICE : TKWAT;
+      } else {  // ISTWET
+        if (j > nlevsoi) thkv = THK_BEDROCK;
+        else thkv = tt[jj] < TFRZ ? TKICE : TKWAT;
+      }
+    } else {
+      // snow layer (snl+1 <= j <= 0) — Jordan1991 or Sturm1997
+      const double denom = jl_max(fse, 1.0e-6) * jl_max(LVc(DZ, c, jj, ld), 1.0e-6);
+      const double bwv = (LV(ICE, c, jj, ld) + LV(LIQ, c, jj, ld)) / denom;
+      LV(f.bw, c, jj, ld) = bwv;
+      if (snow_method == CLMGB_SNOW_JORDAN1991) {
+        thkv = TKAIR + (7.75e-5 * bwv + 1.105e-6 * (bwv * bwv)) * (TKICE - TKAIR);
+      } else {
+        if (bwv <= 156.0) thkv = 0.023 + 0.234 * (bwv / 1000.0);
+        else thkv = 0.138 - 1.01 * (bwv / 1000.0) + 3.233 * ((bwv / 1000.0) * (bwv / 1000.0));
+      }
+    }
+    LV(f.thk, c, jj, ld) = thkv;
+    tk[jj] = thkv;
+  }
+  // _tk_h2osfc_kernel! (:762-776): uses the soil-1 layer conductivity
+  double tk_h2osfc;
+  {
+    const double zh2osfc = 1.0e-3 * (0.5 * f.h2osfc[c]);
+    const double z1 = zz[1 + joff], tk1 = tk[1 + joff];
+    const double denom = TKWAT * z1 + tk1 * zh2osfc;
+    tk_h2osfc = denom > 0.0 ? TKWAT * tk1 * (z1 + zh2osfc) / denom : tk1;
+  }
+  // interface conductivity (_soil_tk_interface_kernel! :599-629), ascending so
+  // tk[jj+1] still holds the layer value when tk[jj] is formed
+  for (int jj = jjtop; jj <= nlev; jj++) {
+    const int j = jj - nlevsno;
+    if (j <= nlevgrnd - 1) {
+      const double tkj = tk[jj], tkj1 = tk[jj + 1];
+      const double zj = zz[jj], zj1 = zz[jj + 1], zij1 = LVc(ZI, c, jj + 1, ld);
+      tk[jj] = tkj * tkj1 * (zj1 - zj) / (tkj * (zj1 - zij1) + tkj1 * (zij1 - zj));
+    } else if (j == nlevgrnd) {
+      tk[jj] = 0.0;
+    }
+  }
+
+  // ---- heat capacity cv (_soil_cv, _unresolved_snow_cv, _snow_cv) -> fact, fn ----
+  // (_heat_diff_kernel! :1271-1319): fact = dtime/cv, top layer with the CAPR factor
+  for (int jj = jjtop; jj <= nlevsno + nlevgrnd; jj++) {
+    const int j = jj - nlevsno;
+    const double dzv = LVc(DZ, c, jj, ld);
+    double cv;
+    if (j >= 1) {
+      if (!is_special) {
+        cv = LVc(f.csol, c, j, ld) * (1.0 - LVc(f.watsat, c, j, ld)) * dzv +
+             (LV(ICE, c, jj, ld) * CPICE + LV(LIQ, c, jj, ld) * CPLIQ) + LV(EXI, c, j, ld) * CPICE;
+      } else {
+        cv = LV(ICE, c, jj, ld) * CPICE + LV(LIQ, c, jj, ld) * CPLIQ;
+      }
+      if (j > nbedrock) cv = CSOL_BEDROCK * dzv;
+      if (j == 1 && f.h2osno_no_layers[c] > 0.0) cv += CPICE * f.h2osno_no_layers[c];
+    } else {
+      if (fse > 0.0)
+        cv = jl_max(THIN_SFCLAYER, (CPLIQ * LV(LIQ, c, jj, ld) + CPICE * LV(ICE, c, jj, ld)) / fse);
+      else
+        cv = THIN_SFCLAYER;
+    }
+    double fc;
+    if (j == jtop) {
+      fc = dtime / cv * dzv / (0.5 * (zz[jj] - LVc(ZI, c, jj, ld) + CAPR * (zz[jj + 1] - LVc(ZI, c, jj, ld))));
+      fn[jj] = tk[jj] * (tt[jj + 1] - tt[jj]) / (zz[jj + 1] - zz[jj]);
+    } else if (j <= nlevgrnd - 1) {
+      fc = dtime / cv;
+      fn[jj] = tk[jj] * (tt[jj + 1] - tt[jj]) / (zz[jj + 1] - zz[jj]);
+    } else {
+      fc = dtime / cv;
+      fn[jj] = f.eflx_bot[c];
+    }
+    fct[jj] = fc;
+    LV(f.fact, c, jj, ld) = fc;
+  }
+
+  // ---- compute_ground_heat_flux_and_deriv! (:1200-1263) ----
+  const double eg = f.emg[c];
+  const double tg = f.t_grnd[c];
+  const double lwrad_emit = eg * SB * jl_pow4(tg);
+  const double dlwrad_emit = 4.0 * eg * SB * (tg * tg * tg);
+  const double lwrad_emit_snow = eg * SB * jl_pow4(tt[jjtop]);
+  const double lwrad_emit_soil = eg * SB * jl_pow4(tt[1 + joff]);
+  const double lwrad_emit_h2osfc = eg * SB * jl_pow4(f.t_h2osfc[c]);
+  const double htvp = f.htvp[c];
+  const double forc = f.forc_lwrad[c];
+  const int64_t pi = f.col_patchi[c], pf = f.col_patchf[c];
+  if (pi < 1 || pf > D.np || pf < pi - 1) return CLMGB_COL_PATCH_RANGE;
+  double dhsdT = 0.0, hs_soil = 0.0, hs_h2osfc = 0.0, hs_top_snow = 0.0;
+  double sabg_lyr_col[MAXSNO + 2];
+  for (int k = 0; k <= nlevsno + 1; k++) sabg_lyr_col[k] = 0.0;
+  for (int64_t p1 = pi; p1 <= pf; p1++) {
+    const int64_t p = p1 - 1;
+    if (f.patch_column[p] != c + 1) continue;
+    double dh_p = 0.0, hsoil_p = 0.0, hh_p = 0.0;
+    const bool act = f.mask_nolakep[p] != 0;
+    const double base = f.dlrad[p] + (1.0 - (double)f.frac_veg_nosno[p]) * eg * forc;
+    if (act && !f.lun_urbpoi[f.patch_landunit[p] - 1]) {
+      const double gnet = f.sabg[p] + base - lwrad_emit - (f.eflx_sh_grnd[p] + f.qflx_evap_soi[p] * htvp);
+      f.eflx_gnet[p] = gnet;
+      f.sabg_chk[p] = fse * f.sabg_snow[p] + (1.0 - fse) * f.sabg_soil[p];
+      const double dg = -f.cgrnd[p] - dlwrad_emit;
+      f.dgnetdT[p] = dg;
+      const double wt = f.patch_wtcol[p];
+      const double gsoil = f.sabg_soil[p] + base - lwrad_emit_soil - (f.eflx_sh_soil[p] + f.qflx_ev_soil[p] * htvp);
+      const double gh2o = f.sabg_soil[p] + base - lwrad_emit_h2osfc - (f.eflx_sh_h2osfc[p] + f.qflx_ev_h2osfc[p] * htvp);
+      const bool wnz = wt != 0.0;
+      dh_p = wnz ? dg * wt : 0.0;
+      hsoil_p = wnz ? gsoil * wt : 0.0;
+      hh_p = wnz ? gh2o * wt : 0.0;
+    }
+    dhsdT += dh_p; hs_soil += hsoil_p; hs_h2osfc += hh_p;
+    if (act) {   // SNICAR top-layer flux + per-layer solar (:1139-1167)
+      const double wt = f.patch_wtcol[p];
+      const double sab = LVc(f.sabg_lyr, p, jtop + joff, ldp);
+      const double gsnow = sab + base - lwrad_emit_snow - (f.eflx_sh_snow[p] + f.qflx_ev_snow[p] * htvp);
+      hs_top_snow += gsnow * wt;
+      for (int j = jtop; j <= 1; j++) sabg_lyr_col[j + nlevsno] += LVc(f.sabg_lyr, p, j + joff, ldp) * wt;
+    }
+  }
+
+  // ---- _h2osfc_thermprop_kernel! (:116-130) ----
+  double ch, dz_h2osfc;
+  if (f.h2osfc[c] > THIN_SFCLAYER && fh > THIN_SFCLAYER) {
+    ch = jl_max(THIN_SFCLAYER, CPLIQ * f.h2osfc[c] / fh);
+    dz_h2osfc = jl_max(THIN_SFCLAYER, 1.0e-3 * f.h2osfc[c] / fh);
+  } else {
+    ch = THIN_SFCLAYER;
+    dz_h2osfc = THIN_SFCLAYER;
+  }
+  f.c_h2osfc[c] = ch;
+
+  // ---- set_rhs_vec! + set_matrix! straight into band rows (row r = system row,
+  //      r = 0 is the top active layer; the surface-water row sits between the
+  //      snow layers and soil layer 1), ab[r][d] = A[r, r-2+d] ----
+  constexpr int W = 7;
+  double ab[MAXROWS * W];
+  double x[MAXROWS];
+  const int n = nlevgrnd - (int)snl + 1;
+  const int rsw = -(int)snl;              // row of the surface-water equation
+  const double omc = 1.0 - CNFAC;
+  for (int k = 0; k < n * W; k++) ab[k] = 0.0;
+  // snow rows: r = j - jtop  (j = jtop..0)
+  for (int j = jtop; j <= 0; j++) {
+    const int jj = j + joff;
+    const int r = j - jtop;
+    const double fc = fct[jj];
+    const double dzp = zz[jj + 1] - zz[jj];
+    if (j == jtop) {
+      x[r] = tt[jj] + fc * (hs_top_snow - dhsdT * tt[jj] + CNFAC * fn[jj]);
+      ab[r * W + 2] = 1.0 + omc * fc * tk[jj] / dzp - fc * dhsdT;
+    } else {
+      x[r] = tt[jj] + CNFAC * fc * (fn[jj] - fn[jj - 1]);
+      x[r] += fc * sabg_lyr_col[jj];
+      const double dzm = zz[jj] - zz[jj - 1];
+      ab[r * W + 1] = -omc * fc * tk[jj - 1] / dzm;
+      ab[r * W + 2] = 1.0 + omc * fc * (tk[jj] / dzp + tk[jj - 1] / dzm);
+    }
+    if (j != 0) ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
+    else ab[r * W + 4] = -omc * fc * tk[jj] / dzp;   // snow-soil coupling skips the h2osfc row
+  }
+  // surface-water row
+  double fn_h2osfc;
+  {
+    const double dzm = 0.5 * dz_h2osfc + zz[1 + joff];
+    const double th = f.t_h2osfc[c];
+    const double fnh = tk_h2osfc * (tt[1 + joff] - th) / dzm;
+    fn_h2osfc = fnh;
+    x[rsw] = th + (dtime / ch) * (hs_h2osfc - dhsdT * th + CNFAC * fnh);
+    ab[rsw * W + 2] = 1.0 + omc * (dtime / ch) * tk_h2osfc / dzm - (dtime / ch) * dhsdT;
+    ab[rsw * W + 3] = -omc * (dtime / ch) * tk_h2osfc / dzm;
+  }
+  // soil rows: r = rsw + j
+  for (int j = 1; j <= nlevgrnd; j++) {
+    const int jj = j + joff;
+    const int r = rsw + j;
+    const double fc = fct[jj];
+    const double t0 = tt[jj];
+    if (j == jtop) {   // snl == 0
+      const double dzp = zz[jj + 1] - zz[jj];
+      x[r] = t0 + fc * (hs_top_snow - dhsdT * t0 + CNFAC * fn[jj]);
+      ab[r * W + 2] = 1.0 + omc * fc * tk[jj] / dzp - fc * dhsdT;
+      ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
+    } else if (j == 1) {
+      const double dzm = zz[jj] - zz[jj - 1];
+      const double dzp = zz[jj + 1] - zz[jj];
+      x[r] = t0 + fc * ((1.0 - fse) * (hs_soil - dhsdT * t0) + CNFAC * (fn[jj] - fse * fn[jj - 1]));
+      x[r] += fse * fc * sabg_lyr_col[j + nlevsno];
+      ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
+      ab[r * W + 2] = 1.0 + omc * fc * (tk[jj] / dzp + fse * tk[jj - 1] / dzm) - (1.0 - fse) * fc * dhsdT;
+      ab[r * W + 0] = -fse * omc * fc * tk[jj - 1] / dzm;
+    } else if (j <= nlevgrnd - 1) {
+      const double dzm = zz[jj] - zz[jj - 1];
+      const double dzp = zz[jj + 1] - zz[jj];
+      x[r] = t0 + CNFAC * fc * (fn[jj] - fn[jj - 1]);
+      ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
+      ab[r * W + 2] = 1.0 + omc * fc * (tk[jj] / dzp + tk[jj - 1] / dzm);
+      ab[r * W + 1] = -omc * fc * tk[jj - 1] / dzm;
+    } else {
+      const double dzm = zz[jj] - zz[jj - 1];
+      x[r] = t0 - CNFAC * fc * fn[jj - 1] + fc * fn[jj];
+      ab[r * W + 2] = 1.0 + omc * fc * tk[jj - 1] / dzm;
+      ab[r * W + 1] = -omc * fc * tk[jj - 1] / dzm;
+    }
+  }
+  if (fh != 0.0) {   // surface-water corrections to soil layer 1 (:1480-1494, :1689-1707)
+    const int jj = 1 + joff;
+    const int r = rsw + 1;
+    const double fc = fct[jj];
+    x[r] -= fh * fc * ((hs_soil - dhsdT * tt[jj]) + CNFAC * fn_h2osfc);
+    const double dzm = 0.5 * dz_h2osfc + zz[1 + joff];
+    ab[r * W + 2] += fh * (omc * fc * tk_h2osfc / dzm + fc * dhsdT);
+    ab[r * W + 1] = -fh * omc * fc * tk_h2osfc / dzm;
+  }
+  // the reference's densify drops band entries that fall outside the n x n system
+  ab[0 * W + 0] = 0.0; ab[0 * W + 1] = 0.0;
+  if (n > 1) ab[1 * W + 0] = 0.0;
+
+  // ---- batched_band_solve! (band_diagonal.jl:87-170), banded form ----
+  band_lu_solve<2, 2>(ab, x, n);
+
+  // ---- _tvector_extract_kernel! (:149-167) ----
+  for (int j = jtop; j <= 0; j++) tt[j + joff] = x[j - jtop];
+  for (int j = 1; j <= nlevgrnd; j++) tt[j + joff] = x[rsw + j];
+  for (int jj = jjtop; jj <= nlev; jj++) LV(T, c, jj, ld) = tt[jj];
+  if (fh == 0.0) f.t_h2osfc[c] = tt[1 + joff];
+  else f.t_h2osfc[c] = x[rsw];
+
+  // ---- _fn1_kernel! (:170-206) and _eflx_fgr_kernel! (:250-269) ----
+  const bool issoilcrop = (lit == ISTSOIL || lit == ISTCROP);
+  {
+    f.eflx_fgr12[c] = 0.0;
+    for (int jj = jjtop; jj <= nlev; jj++) {
+      const int j = jj - nlevsno;
+      double fn1v;
+      if (j <= nlevgrnd - 1) fn1v = tk[jj] * (tt[jj + 1] - tt[jj]) / (zz[jj + 1] - zz[jj]);
+      else fn1v = 0.0;
+      if (j == 1) f.eflx_fgr12[c] = -CNFAC * fn[jj] - (1.0 - CNFAC) * fn1v;
+      if (j >= 1 && j < nlevgrnd && issoilcrop) LV(f.eflx_fgr, c, j, ld) = -CNFAC * fn[jj] - (1.0 - CNFAC) * fn1v;
+      else if (j == nlevgrnd && issoilcrop) LV(f.eflx_fgr, c, j, ld) = 0.0;
+    }
+  }
+
+  // ---- phase change (:552-561) ----
+  phase_change_h2osfc_col(D, f, c, dtime, dhsdT);
+  phase_change_beta_col(D, f, c, dtime, dhsdT);
+
+  // ---- _tgrnd_kernel! (:224-247) ----
+  {
+    const double t1 = LV(T, c, 1 + joff, ld), th = f.t_h2osfc[c];
+    double tgn;
+    if (snl < 0) {
+      const double ts = LV(T, c, jjtop, ld);
+      if (fh != 0.0) tgn = fse * ts + (1.0 - fse - fh) * t1 + fh * th;
+      else tgn = fse * ts + (1.0 - fse) * t1;
+    } else {
+      if (fh != 0.0) tgn = (1.0 - fh) * t1 + fh * th;
+      else tgn = t1;
+    }
+    f.t_grnd[c] = tgn;
+  }
+  uint32_t status = 0;
+  for (int jj = jjtop; jj <= nlev; jj++)
+    if (!isfinite(LV(T, c, jj, ld))) status |= CLMGB_COL_NONFINITE;
+  return status;
+}
+
+// ===========================================================================
+// set_soil_water_fractions! kernel (soil_hydrology.jl:110-130), column c.
+// ===========================================================================
+__device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_soilwater_fields& f, int64_t c) {
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno;
+  for (int j = 1; j <= D.nlevsoi; j++) {
+    const double exi = LV(f.excess_ice, c, j, ld);
+    const double dz_ext = LVc(f.dz, c, j + joff, ld) + exi / DENICE;
+    const double ws = LVc(f.watsat, c, j, ld);
+    const double vol_ice = jl_min(ws, (LV(f.h2osoi_ice, c, j + joff, ld) + exi) / (dz_ext * DENICE));
+    LV(f.eff_porosity, c, j, ld) = jl_max(0.01, ws - vol_ice);
+    LV(f.icefrac, c, j, ld) = jl_min(1.0, vol_ice / ws);
+  }
+}
+
+// ===========================================================================
+// _soilwm_moisture_form_kernel! (soil_water_movement.jl:1250-1489), column c.
+//
+// Identical arithmetic to the reference, with two exact hoists:
+//  * the ice impedance 10^(-e_ice*icefrac) depends only on icefrac, which is fixed
+//    during the call, so it is formed once per call instead of once per attempt;
+//  * a rejected attempt leaves h2osoi_liq unchanged, so the hydraulic properties,
+//    fluxes and flux derivatives of the retry equal the previous attempt's bit for
+//    bit; they are recomputed only after an accepted substep.
+// ===========================================================================
+__device__ inline uint32_t moisture_form_col(const Dims& D, const clmgb_soilwater_fields& f,
+                                      const clmgb_swm_config& cfg, double dtime, int64_t c,
+                                      int* attempts_out) {
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
+  const int nlayers = (int)f.col_nbedrock[c];
+  if (nlayers < 1 || nlayers > nlevsoi) return CLMGB_COL_LEVEL_RANGE;
+  const double e_ice = cfg.e_ice, dtmin = cfg.dtmin, xtu = cfg.xTolerUpper, xtl = cfg.xTolerLower;
+  const double verysmall = cfg.verySmall;
+  const bool expensive = (cfg.flux_calculation == 42);
+  const int lower_bc = cfg.lower_boundary_condition;
+
+  double liq[MAXSOI + 1], dzv[MAXSOI + 1], imp[MAXSOI + 1];
+  double hk[MAXSOI + 1], dhkdw[MAXSOI + 1];
+  double qin[MAXSOI + 1], qout[MAXSOI + 1], dqidw0[MAXSOI + 1], dqidw1[MAXSOI + 1];
+  double dqodw1[MAXSOI + 1], dqodw2[MAXSOI + 1], fnet1[MAXSOI + 1];
+  double gam[MAXSOI + 1], dwat[MAXSOI + 1], dt_dz[MAXSOI + 1];
+  for (int j = 1; j <= nlayers; j++) {
+    liq[j] = LV(f.h2osoi_liq, c, joff + j, ld);
+    dzv[j] = LVc(f.dz, c, joff + j, ld);
+  }
+  for (int j = 1; j <= nlayers; j++) {
+    if (j == nlayers) imp[j] = pow(10.0, -e_ice * LV(f.icefrac, c, j, ld));
+    else imp[j] = pow(10.0, -e_ice * (0.5 * (LV(f.icefrac, c, j, ld) + LV(f.icefrac, c, j + 1, ld))));
+  }
+  const double qinfl = f.qflx_infl[c];
+  int nsubstep = 0;
+  double dtsub = dtime, dtdone = 0.0, qc = 0.0;
+  bool fresh = true;   // hydraulics must be (re)computed from liq
+  uint32_t status = 0;
+  for (;;) {
+    nsubstep += 1;
+    if (nsubstep > MF_ATTEMPT_CAP) { status |= CLMGB_COL_SUBSTEP_CAP; break; }
+    for (int j = 1; j <= nlayers; j++) dt_dz[j] = dtsub / (M_TO_MM * dzv[j]);
+    if (fresh) {
+      double s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
+      for (int j = 1; j <= nlayers; j++) {
+        const double vwc = jl_max(liq[j], 1.0e-6) / (dzv[j] * DENH2O);
+        double s = vwc / LVc(f.watsat, c, j, ld);
+        s = jl_min(s, 1.0);
+        s = jl_max(0.01, s);
+        s2[j] = s;
+      }
+      for (int j = 1; j <= nlayers; j++) {
+        double s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
+        s1 = jl_min(s1, 1.0);
+        s1 = jl_max(0.01, s1);
+        const double b = LVc(f.bsw, c, j, ld);
+        const double hkv = imp[j] * LVc(f.hksat, c, j, ld) * pow(s1, 2.0 * b + 3.0);
+        const double dhkds = (2.0 * b + 3.0) * hkv / s1;
+        const double sn = s2[j];
+        const double smpv = -LVc(f.sucsat, c, j, ld) * pow(sn, -b);
+        const double dsmpds = -b * smpv / sn;
+        hk[j] = hkv;
+        smp[j] = smpv;
+        dhkdw[j] = dhkds;
+        dsmpdw[j] = dsmpds / LVc(f.watsat, c, j, ld);
+        LV(f.smp_l, c, j, ld) = smpv;
+        LV(f.hk_l, c, j, ld) = hkv;
+      }
+      for (int j = 1; j <= nlayers; j++) {
+        qin[j] = 0.0; qout[j] = 0.0; dqidw0[j] = 0.0; dqidw1[j] = 0.0; dqodw1[j] = 0.0; dqodw2[j] = 0.0;
+      }
+      for (int j = 1; j <= nlayers - 1; j++) {
+        const double dhkds1 = 0.5 * dhkdw[j] / LVc(f.watsat, c, j, ld);
+        const double dhkds2 = 0.5 * dhkdw[j] / LVc(f.watsat, c, j + 1, ld);
+        const double num = smp[j + 1] - smp[j];
+        const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
+        qout[j] = -hk[j] * num / den + hk[j];
+        dqodw1[j] = (hk[j] * dsmpdw[j] - dhkds1 * num) / den + dhkds1;
+        dqodw2[j] = (-hk[j] * dsmpdw[j + 1] - dhkds2 * num) / den + dhkds2;
+      }
+      {
+        const int j = nlayers;
+        if (lower_bc == CLMGB_BC_WATERTABLE) {
+          int jwt = nlevsoi;
+          for (int jj = 1; jj <= nlevsoi; jj++) {
+            if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
+          }
+          if (j > jwt) {
+            qout[j] = 0.0; dqodw1[j] = 0.0; dqodw2[j] = 0.0;
+          } else {
+            const double dhkds1l = dhkdw[j] / LVc(f.watsat, c, j, ld);
+            const double num = -smp[j];
+            const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
+            qout[j] = -hk[j] * num / den + hk[j];
+            dqodw1[j] = (hk[j] * dsmpdw[j] - dhkds1l * num) / den + dhkds1l;
+            dqodw2[j] = 0.0;
+          }
+        } else if (lower_bc == CLMGB_BC_FLUX) {
+          qout[j] = hk[j];
+          dqodw1[j] = dhkdw[j] / LVc(f.watsat, c, j, ld);
+        } else {
+          qout[j] = 0.0;
+          dqodw1[j] = 0.0;
+        }
+      }
+      for (int j = 2; j <= nlayers; j++) {
+        qin[j] = qout[j - 1];
+        dqidw0[j] = dqodw1[j - 1];
+        dqidw1[j] = dqodw2[j - 1];
+      }
+      qin[1] = qinfl;
+      dqidw1[1] = 0.0;
+      for (int j = 1; j <= nlayers; j++) fnet1[j] = qin[j] - qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
+      fresh = false;
+    }
+    // ---- RHS / LHS assembly fused into the Thomas forward sweep ----
+    double bet, dwat_prev;
+    {
+      const double rmx = -fnet1[1] * dt_dz[1];
+      const double bmx = -1.0 - (-dqidw1[1] + dqodw1[1]) * dt_dz[1];
+      bet = bmx;
+      if (fabs(bet) < 1.0e-30) bet = 1.0e-30;
+      dwat_prev = rmx / bet;
+      dwat[1] = dwat_prev;
+    }
+    double cmx_prev = -dqodw2[1] * dt_dz[1];
+    for (int j = 2; j <= nlayers; j++) {
+      const double amx = dqidw0[j] * dt_dz[j];
+      const double bmx = -1.0 - (-dqidw1[j] + dqodw1[j]) * dt_dz[j];
+      const double cmx = (j == nlayers) ? 0.0 : -dqodw2[j] * dt_dz[j];
+      const double rmx = -fnet1[j] * dt_dz[j];
+      gam[j] = cmx_prev / bet;
+      bet = bmx - amx * gam[j];
+      if (fabs(bet) < 1.0e-30) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
+      dwat_prev = (rmx - amx * dwat_prev) / bet;
+      dwat[j] = dwat_prev;
+      cmx_prev = cmx;
+    }
+    {
+      double dwat_next = dwat_prev;
+      for (int j = nlayers - 1; j >= 1; j--) {
+        dwat_next = dwat[j] - gam[j + 1] * dwat_next;
+        dwat[j] = dwat_next;
+      }
+    }
+    // ---- error estimate ----
+    double errorMax = 0.0;
+    for (int j = 1; j <= nlayers; j++) {
+      double fnet0;
+      if (expensive) {
+        const double qin_test = j == 1 ? qin[j] + dqidw1[j] * dwat[j]
+                                       : qin[j] + dqidw0[j] * dwat[j - 1] + dqidw1[j] * dwat[j];
+        const double qout_test = j == nlayers ? qout[j] + dqodw1[j] * dwat[j]
+                                              : qout[j] + dqodw1[j] * dwat[j] + dqodw2[j] * dwat[j + 1];
+        fnet0 = qin_test - qout_test - LVc(f.qflx_rootsoi, c, j, ld);
+      } else {
+        fnet0 = dwat[j] / dt_dz[j];
+      }
+      const double ev = fabs(fnet1[j] - fnet0) * dtsub * 0.5;
+      errorMax = jl_max(errorMax, ev);
+    }
+    if (errorMax > xtu && dtsub > dtmin) {
+      dtsub = jl_max(dtsub / 2.0, dtmin);
+      continue;
+    }
+    for (int j = 1; j <= nlayers; j++) liq[j] = liq[j] + dwat[j] * (M_TO_MM * dzv[j]);
+    fresh = true;
+    double qcTemp;
+    if (lower_bc == CLMGB_BC_FLUX) qcTemp = hk[nlayers] + dhkdw[nlayers] * dwat[nlayers];
+    else if (lower_bc == CLMGB_BC_ZERO_FLUX) qcTemp = 0.0;
+    else qcTemp = qout[nlayers] + dqodw1[nlayers] * dwat[nlayers];
+    qc += qcTemp * (dtsub / dtime);
+    dtdone += dtsub;
+    if (fabs(dtime - dtdone) < verysmall) break;
+    if (errorMax < xtl) dtsub = dtsub * 2.0;
+    dtsub = jl_min(dtsub, dtime - dtdone);
+  }
+  for (int j = 1; j <= nlayers; j++) {
+    LV(f.h2osoi_liq, c, joff + j, ld) = liq[j];
+    if (!isfinite(liq[j])) status |= CLMGB_COL_NONFINITE;
+  }
+  f.qcharge[c] = qc;
+  f.num_substeps[c] = (double)nsubstep;
+  if (attempts_out) *attempts_out = nsubstep;
+  return status;
+}
+
+}  // namespace clmgb

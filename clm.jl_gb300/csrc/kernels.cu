@@ -1,0 +1,217 @@
+// kernels.cu — CUDA kernels of the soil/snow column solve (one thread per column).
+#include "clmgb_device.cuh"
+#include "launch.h"
+
+namespace clmgb {
+
+constexpr int BLOCK = 128;
+
+static inline unsigned grid_for(int64_t n) { return (unsigned)((n + BLOCK - 1) / BLOCK); }
+
+__device__ __forceinline__ void report(uint32_t st, uint32_t* col_status, uint32_t* dev_status, int64_t c) {
+  if (col_status) col_status[c] = st;
+  if (st && dev_status) atomicOr(dev_status, st);
+}
+
+__global__ void __launch_bounds__(BLOCK)
+k_soil_temperature(Dims D, int64_t nc, clmgb_soiltemp_fields f, double dtime, int snow_method,
+                   uint32_t* col_status, uint32_t* dev_status) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  uint32_t st = 0;
+  if (f.mask_nolakec[c]) st = soil_temperature_col(D, f, c, dtime, snow_method);
+  report(st, col_status, dev_status, c);
+}
+
+__global__ void __launch_bounds__(BLOCK)
+k_water_fractions(Dims D, int64_t nc, clmgb_soilwater_fields f) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  if (f.mask_hydrology[c]) water_fractions_col(D, f, c);
+}
+
+__global__ void __launch_bounds__(BLOCK)
+k_moisture_form(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
+                uint32_t* col_status, uint32_t* dev_status) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  uint32_t st = 0;
+  if (f.mask_hydrology[c]) st = moisture_form_col(D, f, cfg, dtime, c, nullptr);
+  report(st, col_status, dev_status, c);
+}
+
+// soil_temperature! -> set_soil_water_fractions! -> soil_water! for one column, one launch.
+__global__ void __launch_bounds__(BLOCK)
+k_column_step(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw, clmgb_swm_config cfg,
+              double dtime, int snow_method, double* t_ssbef, double* t_h2osfc_bef,
+              uint32_t* col_status, uint32_t* dev_status) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  uint32_t st = 0;
+  if (ft.mask_nolakec[c]) {
+    if (t_ssbef) {
+      const int L = D.nlevsno + D.nlevmax;
+      for (int jj = 1; jj <= L; jj++) LV(t_ssbef, c, jj, D.ldc) = LV(ft.t_soisno, c, jj, D.ldc);
+    }
+    if (t_h2osfc_bef) t_h2osfc_bef[c] = ft.t_h2osfc[c];
+    st |= soil_temperature_col(D, ft, c, dtime, snow_method);
+  }
+  if (fw.mask_hydrology[c]) {
+    water_fractions_col(D, fw, c);
+    st |= moisture_form_col(D, fw, cfg, dtime, c, nullptr);
+  }
+  report(st, col_status, dev_status, c);
+}
+
+__global__ void __launch_bounds__(BLOCK)
+k_phase_change(Dims D, int64_t nc, clmgb_soiltemp_fields f, double dtime, const double* dhsdT, int which) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc || !f.mask_nolakec[c]) return;
+  if (which == 0) phase_change_h2osfc_col(D, f, c, dtime, dhsdT[c]);
+  else phase_change_beta_col(D, f, c, dtime, dhsdT[c]);
+}
+
+template <int KL, int KU>
+__global__ void __launch_bounds__(BLOCK)
+k_band_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const double* __restrict__ bmatrix,
+             const double* __restrict__ rvector, const int64_t* jtop, const int64_t* jbot,
+             const uint8_t* mask, int nlevsno_off) {
+  constexpr int W = 2 * KL + KU + 1;
+  constexpr int NB = KL + KU + 1;
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc || !mask[c]) return;
+  const int64_t jt = jtop[c] + nlevsno_off + 1;
+  const int64_t n64 = jbot[c] - jtop[c] + 1;
+  if (n64 <= 0 || jt < 1 || jt + n64 - 1 > nlev || n64 > MAXROWS + 1) return;
+  const int n = (int)n64;
+  double ab[(MAXROWS + 1) * W];
+  double x[MAXROWS + 1];
+  for (int k = 0; k < n * W; k++) ab[k] = 0.0;
+  for (int i = 0; i < n; i++) {
+    const int64_t lev = jt + i;   // 1-based level of row i
+    for (int j = max(0, i - KL); j <= min(n - 1, i + KU); j++) {
+      const int band = (i - j) + KL;   // 0-based band
+      ab[i * W + (j - i + KL)] = bmatrix[c + (int64_t)band * ldc + (lev - 1) * ldc * NB];
+    }
+    x[i] = rvector[c + (lev - 1) * ldc];
+  }
+  band_lu_solve<KL, KU>(ab, x, n);
+  for (int i = 0; i < n; i++) tvector[c + (jt + i - 1) * ldc] = x[i];
+}
+
+constexpr int MAXTRI = 64;
+
+__global__ void __launch_bounds__(BLOCK)
+k_tridiagonal_multi(int64_t ncols, int64_t ld, int nlevs, double* u, const double* __restrict__ a,
+                    const double* __restrict__ b, const double* __restrict__ cc, const double* __restrict__ r,
+                    const int64_t* jtop, const uint8_t* mask) {
+  const int64_t col = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (col >= ncols || !mask[col]) return;
+  const int64_t j64 = jtop[col];
+  if (j64 < 1 || j64 > nlevs) return;
+  const int j = (int)j64;
+  double cpv[MAXTRI + 1], dpv[MAXTRI + 1];
+  const double tiny = 1e-30;
+  double bet = LVc(b, col, j, ld);
+  if (fabs(bet) < tiny) bet = tiny;
+  double cp_prev = LVc(cc, col, j, ld) / bet;
+  double dp_prev = LVc(r, col, j, ld) / bet;
+  cpv[j] = cp_prev;
+  dpv[j] = dp_prev;
+  for (int jj = j + 1; jj <= nlevs; jj++) {
+    double denom = LVc(b, col, jj, ld) - LVc(a, col, jj, ld) * cp_prev;
+    if (fabs(denom) < tiny) denom = copysign(tiny, denom == 0.0 ? 1.0 : denom);
+    cp_prev = LVc(cc, col, jj, ld) / denom;
+    dp_prev = (LVc(r, col, jj, ld) - LVc(a, col, jj, ld) * dp_prev) / denom;
+    cpv[jj] = cp_prev;
+    dpv[jj] = dp_prev;
+  }
+  double u_next = dp_prev;
+  LV(u, col, nlevs, ld) = u_next;
+  for (int jj = nlevs - 1; jj >= j; jj--) {
+    u_next = dpv[jj] - cpv[jj] * u_next;
+    LV(u, col, jj, ld) = u_next;
+  }
+}
+
+// Synthetic per-step forcing (the upstream radiation / infiltration modules are out
+// of scope): sabg = sabg_soil = sabg_snow = G, sabg_lyr = G on the top active layer
+// and 0 elsewhere, forc_lwrad = SB*t_grnd^4, qflx_infl = I.
+__global__ void __launch_bounds__(BLOCK)
+k_synth_forcing(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw, const double* G,
+                const double* I) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc || !ft.mask_nolakec[c]) return;
+  const double g = G[c];
+  const int64_t snl = ft.col_snl[c];
+  for (int64_t p1 = ft.col_patchi[c]; p1 <= ft.col_patchf[c]; p1++) {
+    if (p1 < 1 || p1 > D.np) break;
+    const int64_t p = p1 - 1;
+    ((double*)ft.sabg)[p] = g;
+    ((double*)ft.sabg_soil)[p] = g;
+    ((double*)ft.sabg_snow)[p] = g;
+    for (int k = 1; k <= D.nlevsno + 1; k++) LV((double*)ft.sabg_lyr, p, k, D.ldp) = 0.0;
+    if (snl <= 0 && snl >= -D.nlevsno) LV((double*)ft.sabg_lyr, p, (int)snl + 1 + D.nlevsno, D.ldp) = g;
+  }
+  ((double*)ft.forc_lwrad)[c] = SB * jl_pow4(ft.t_grnd[c]);
+  ((double*)fw.qflx_infl)[c] = I[c];
+}
+
+// ---------------------------------------------------------------------------
+cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
+                                    int snow_method, uint32_t* col_status, uint32_t* dev_status,
+                                    cudaStream_t s) {
+  k_soil_temperature<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, dtime, snow_method, col_status, dev_status);
+  return cudaGetLastError();
+}
+cudaError_t launch_water_fractions(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f, cudaStream_t s) {
+  k_water_fractions<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f);
+  return cudaGetLastError();
+}
+cudaError_t launch_moisture_form(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                 const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
+                                 uint32_t* dev_status, cudaStream_t s) {
+  k_moisture_form<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, dev_status);
+  return cudaGetLastError();
+}
+cudaError_t launch_column_step(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                               const clmgb_soilwater_fields& fw, const clmgb_swm_config& cfg, double dtime,
+                               int snow_method, double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
+                               uint32_t* dev_status, cudaStream_t s) {
+  k_column_step<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef,
+                                               col_status, dev_status);
+  return cudaGetLastError();
+}
+cudaError_t launch_phase_change(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
+                                const double* dhsdT, int which, cudaStream_t s) {
+  k_phase_change<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, dtime, dhsdT, which);
+  return cudaGetLastError();
+}
+cudaError_t launch_band_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const double* bmatrix,
+                              const double* rvector, const int64_t* jtop, const int64_t* jbot,
+                              const uint8_t* mask, int kl, int ku, int nlevsno_off, cudaStream_t s) {
+  if (kl == 2 && ku == 2)
+    k_band_solve<2, 2><<<grid_for(nc), BLOCK, 0, s>>>(nc, ldc, nlev, tvector, bmatrix, rvector, jtop, jbot, mask,
+                                                      nlevsno_off);
+  else if (kl == 1 && ku == 1)
+    k_band_solve<1, 1><<<grid_for(nc), BLOCK, 0, s>>>(nc, ldc, nlev, tvector, bmatrix, rvector, jtop, jbot, mask,
+                                                      nlevsno_off);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+cudaError_t launch_tridiagonal_multi(int64_t ncols, int64_t ldc, int nlevs, double* u, const double* a,
+                                     const double* b, const double* c, const double* r, const int64_t* jtop,
+                                     const uint8_t* mask, cudaStream_t s) {
+  if (nlevs > MAXTRI) return cudaErrorInvalidValue;
+  k_tridiagonal_multi<<<grid_for(ncols), BLOCK, 0, s>>>(ncols, ldc, nlevs, u, a, b, c, r, jtop, mask);
+  return cudaGetLastError();
+}
+cudaError_t launch_synth_forcing(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                                 const clmgb_soilwater_fields& fw, const double* G, const double* I,
+                                 cudaStream_t s) {
+  k_synth_forcing<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, G, I);
+  return cudaGetLastError();
+}
+
+}  // namespace clmgb

@@ -1,0 +1,36 @@
+// launch.h — internal launchers shared by the host API (api.cu) and the kernel
+// translation units.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/clmgb.h"
+
+namespace clmgb {
+
+struct Dims;
+
+// All launchers return the cudaError_t of the launch (cudaGetLastError()).
+cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
+                                    int snow_method, uint32_t* col_status, uint32_t* dev_status,
+                                    cudaStream_t s);
+cudaError_t launch_water_fractions(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f, cudaStream_t s);
+cudaError_t launch_moisture_form(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                 const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
+                                 uint32_t* dev_status, cudaStream_t s);
+cudaError_t launch_column_step(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                               const clmgb_soilwater_fields& fw, const clmgb_swm_config& cfg, double dtime,
+                               int snow_method, double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
+                               uint32_t* dev_status, cudaStream_t s);
+cudaError_t launch_phase_change(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
+                                const double* dhsdT, int which, cudaStream_t s);
+cudaError_t launch_band_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const double* bmatrix,
+                              const double* rvector, const int64_t* jtop, const int64_t* jbot,
+                              const uint8_t* mask, int kl, int ku, int nlevsno_off, cudaStream_t s);
+cudaError_t launch_tridiagonal_multi(int64_t ncols, int64_t ldc, int nlevs, double* u, const double* a,
+                                     const double* b, const double* c, const double* r, const int64_t* jtop,
+                                     const uint8_t* mask, cudaStream_t s);
+cudaError_t launch_synth_forcing(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                                 const clmgb_soilwater_fields& fw, const double* G, const double* I,
+                                 cudaStream_t s);
+
+}  // namespace clmgb

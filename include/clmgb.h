@@ -281,6 +281,26 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b,
                           double* t_ssbef, double* t_h2osfc_bef,
                           uint32_t* col_status, void* stream);
 
+/* ---- component entry points (the reference exposes these functions too) ---- */
+
+/* phase_change_h2osfc! (soil_temperature.jl:1857) and phase_change_beta!
+ * (soil_temperature.jl:2232) on their own; dhsdT is a device [nc] array. */
+int32_t clmgb_phase_change_h2osfc(clmgb_handle h, const clmgb_bounds* b,
+                                  const clmgb_soiltemp_fields* f, double dtime,
+                                  const double* dhsdT, void* stream);
+int32_t clmgb_phase_change_beta(clmgb_handle h, const clmgb_bounds* b,
+                                const clmgb_soiltemp_fields* f, double dtime,
+                                const double* dhsdT, void* stream);
+
+/* ---- synthetic per-step forcing (benchmark and test harness) ----
+ * Stands in for the upstream modules that write the path's inputs each step
+ * (radiation, infiltration; out of scope): per non-lake column, for its patches
+ * sabg = sabg_soil = sabg_snow = G[c], sabg_lyr = G[c] on the top active layer and 0
+ * elsewhere; forc_lwrad[c] = SB*t_grnd[c]^4; qflx_infl[c] = I[c]. */
+int32_t clmgb_synth_forcing(clmgb_handle h, const clmgb_bounds* b,
+                            const clmgb_soiltemp_fields* ft, const clmgb_soilwater_fields* fw,
+                            const double* G, const double* I, void* stream);
+
 /* ---- solver entry points ---- */
 
 /* batched_band_solve! (band_diagonal.jl:179): bmatrix is [ldc, nband, nlev] (nband =

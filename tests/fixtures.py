@@ -143,3 +143,30 @@ def random_band_system(nc, nlev, kl, ku, rng, pivot_frac=0.0):
         bm[:, kl, :] = np.where(weak, bm[:, kl, :] * 1e-3, bm[:, kl, :])
     rv = rng.uniform(-10.0, 10.0, (nlev, nc))
     return bm, rv
+
+
+def set_snowpack(st, c, k, rng, t_range=(240.0, 273.0)):
+    """Give column c exactly k resolved snow layers (snl = -k), geometry as in the
+    synthetic workloads: z = zi_below - dz/2, zi_above = zi_below - dz."""
+    a = st.arrays
+    nlevsno = st.vp.nlevsno
+    zi_below = 0.0
+    depth = 0.0
+    for j in range(0, -nlevsno, -1):
+        r = j + nlevsno - 1
+        if j >= -k + 1:
+            dz = rng.uniform(0.01, 0.5)
+            a["dz"][r, c] = dz
+            a["z"][r, c] = zi_below - 0.5 * dz
+            a["zi"][r, c] = zi_below - dz
+            a["h2osoi_ice"][r, c] = rng.uniform(100.0, 500.0) * dz
+            a["h2osoi_liq"][r, c] = 0.0
+            a["t_soisno"][r, c] = rng.uniform(*t_range)
+            zi_below -= dz
+            depth += dz
+        else:
+            a["dz"][r, c] = a["z"][r, c] = a["zi"][r, c] = 0.0
+            a["h2osoi_ice"][r, c] = a["h2osoi_liq"][r, c] = a["t_soisno"][r, c] = 0.0
+    a["col_snl"][c] = -k
+    a["snow_depth"][c] = depth
+    a["frac_sno_eff"][c] = 1.0 if k > 0 else 0.0
