@@ -17,8 +17,11 @@ if _PKG not in sys.path:
 
 from clmgb import abi  # noqa: E402  (interface definitions only)
 
-sys.path.insert(0, HERE)
-import build as _build  # noqa: E402
+import importlib.util as _ilu  # noqa: E402
+
+_spec = _ilu.spec_from_file_location("clm_oracle_build", os.path.join(HERE, "build.py"))
+_build = _ilu.module_from_spec(_spec)
+_spec.loader.exec_module(_build)
 
 _lib = None
 
