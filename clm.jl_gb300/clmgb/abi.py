@@ -44,6 +44,13 @@ SNOW_STURM1997 = 2
 BC_HEAD, BC_FLUX, BC_ZERO_FLUX, BC_WATERTABLE, BC_AQUIFER = 0, 1, 2, 3, 4
 ZENGDECKER_2009, MOISTURE_FORM = 0, 1
 
+OPT_STEP_SCHEDULE = 1
+SCHEDULE_FUSED = 0
+SCHEDULE_QUEUE = 1
+OPT_QUEUE_BLOCKS_PER_SM = 2
+OPT_QUEUE_OCCUPANCY = 3
+OPT_NUM_SMS = 4
+
 MAX_NLEVSNO = 12
 MAX_NLEVGRND = 25
 MAX_NLEVSOI = 25

@@ -55,6 +55,14 @@ class Handle:
         except Exception:
             pass
 
+    def set_option(self, key, value):
+        check(self.lib.clmgb_set_option(self.h, key, int(value)), "clmgb_set_option")
+
+    def get_option(self, key):
+        v = C.c_int64(0)
+        check(self.lib.clmgb_get_option(self.h, key, C.byref(v)), "clmgb_get_option")
+        return v.value
+
     def device_status(self, reset=True, stream=None):
         v = C.c_uint32(0)
         check(self.lib.clmgb_device_status(self.h, _stream(stream), C.byref(v), 1 if reset else 0),
@@ -142,3 +150,17 @@ def tridiagonal_multi(handle, u, a, b, c, r, jtop, mask, stream=None):
     check(handle.lib.clmgb_tridiagonal_multi(handle.h, ncols, ncols, nlevs, _dptr(u), _dptr(a), _dptr(b),
                                              _dptr(c), _dptr(r), _dptr(jtop), _dptr(mask), _stream(stream)),
           "tridiagonal_multi")
+
+
+MATH_OPS = {"log": 0, "exp": 1, "pow": 2, "log10": 3}
+
+
+def math_eval(handle, op, x, y=None, out=None, stream=None):
+    """Evaluates the library's binary64 log/exp/pow/log10 on CUDA tensors."""
+    import torch
+    if out is None:
+        out = torch.empty_like(x)
+    check(handle.lib.clmgb_math_eval(handle.h, MATH_OPS[op], x.numel(), _dptr(x, "x"),
+                                     _dptr(y, "y") if y is not None else None, _dptr(out, "out"),
+                                     _stream(stream)), "math_eval")
+    return out

@@ -19,8 +19,16 @@
 struct clmgb_handle_s {
   uint32_t magic;
   int device;
+  int num_sms;
   clmgb_varpar vp;
-  uint32_t* dev_status;      // device word: OR of CLMGB_COL_* bits
+  // device scratch owned by the handle (one allocation): the status word (OR of
+  // CLMGB_COL_* bits) and the Richards work-queue counter
+  unsigned long long* scratch;
+  uint32_t* dev_status;
+  unsigned long long* queue;
+  int64_t step_schedule;        // CLMGB_OPT_STEP_SCHEDULE
+  int64_t queue_blocks_per_sm;  // CLMGB_OPT_QUEUE_BLOCKS_PER_SM (0 = occupancy limit)
+  int occupancy_blocks;         // occupancy limit of the queue kernel
   cudaError_t last_error;
 };
 
@@ -93,6 +101,12 @@ static int32_t check_cfg(const clmgb_swm_config* cfg) {
   return CLMGB_OK;
 }
 
+static int queue_grid(clmgb_handle h) {
+  int per_sm = h->queue_blocks_per_sm > 0 ? (int)h->queue_blocks_per_sm : h->occupancy_blocks;
+  if (per_sm > h->occupancy_blocks) per_sm = h->occupancy_blocks;
+  return per_sm * h->num_sms;
+}
+
 extern "C" {
 
 int32_t clmgb_abi_version(void) { return CLMGB_ABI_VERSION; }
@@ -124,9 +138,18 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->magic = HANDLE_MAGIC;
   h->vp = *vp;
   h->last_error = cudaSuccess;
+  h->step_schedule = CLMGB_SCHEDULE_QUEUE;
+  h->queue_blocks_per_sm = 0;
+  h->scratch = nullptr;
   cudaError_t ce = cudaGetDevice(&h->device);
-  if (ce == cudaSuccess) ce = cudaMalloc(&h->dev_status, sizeof(uint32_t));
-  if (ce == cudaSuccess) ce = cudaMemset(h->dev_status, 0, sizeof(uint32_t));
+  if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (ce == cudaSuccess) ce = cudaMalloc(&h->scratch, 2 * sizeof(unsigned long long));
+  if (ce == cudaSuccess) ce = cudaMemset(h->scratch, 0, 2 * sizeof(unsigned long long));
+  if (ce == cudaSuccess) {
+    h->dev_status = reinterpret_cast<uint32_t*>(h->scratch);
+    h->queue = h->scratch + 1;
+    h->occupancy_blocks = clmgb::queue_blocks_per_sm();
+  }
   if (ce != cudaSuccess) {
     h->magic = 0;
     delete h;
@@ -138,7 +161,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
 
 int32_t clmgb_destroy(clmgb_handle h) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
-  cudaFree(h->dev_status);
+  cudaFree(h->scratch);
   h->magic = 0;
   delete h;
   return CLMGB_OK;
@@ -198,8 +221,13 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soil
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_moisture_form(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status,
-                                               h->dev_status, (cudaStream_t)stream);
+  cudaError_t ce;
+  if (h->step_schedule == CLMGB_SCHEDULE_FUSED)
+    ce = clmgb::launch_moisture_form(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, h->dev_status,
+                                     (cudaStream_t)stream);
+  else
+    ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
+                                           h->dev_status, h->queue, queue_grid(h), (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -216,9 +244,19 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   if ((e = check_fields(fw))) return e;
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_column_step(make_dims(h->vp, *b), b->nc, *ft, *fw, *cfg, dtime, snow_method,
-                                             t_ssbef, t_h2osfc_bef, col_status, h->dev_status,
-                                             (cudaStream_t)stream);
+  const Dims D = make_dims(h->vp, *b);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t ce;
+  if (h->step_schedule == CLMGB_SCHEDULE_FUSED) {
+    ce = clmgb::launch_column_step(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef,
+                                   col_status, h->dev_status, s);
+  } else {
+    ce = clmgb::launch_soiltemp_fractions(D, b->nc, *ft, *fw, dtime, snow_method, t_ssbef, t_h2osfc_bef,
+                                          col_status, h->dev_status, s);
+    if (ce == cudaSuccess)
+      ce = clmgb::launch_moisture_form_queue(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->queue,
+                                             queue_grid(h), s);
+  }
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -270,6 +308,44 @@ int32_t clmgb_batched_band_solve(clmgb_handle h, int64_t nc, int64_t ldc, int32_
   if (!tvector || !bmatrix || !rvector || !jtop || !jbot || !mask) return CLMGB_ERR_NULL_ARG;
   cudaError_t ce = clmgb::launch_band_solve(nc, ldc, nlev, tvector, bmatrix, rvector, jtop, jbot, mask, kl, ku,
                                             nlevsno_off, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  switch (key) {
+    case CLMGB_OPT_STEP_SCHEDULE:
+      if (value != CLMGB_SCHEDULE_FUSED && value != CLMGB_SCHEDULE_QUEUE) return CLMGB_ERR_CONFIG;
+      h->step_schedule = value;
+      return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_BLOCKS_PER_SM:
+      if (value < 0) return CLMGB_ERR_CONFIG;
+      h->queue_blocks_per_sm = value;
+      return CLMGB_OK;
+    default:
+      return CLMGB_ERR_CONFIG;
+  }
+}
+
+int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (!value) return CLMGB_ERR_NULL_ARG;
+  switch (key) {
+    case CLMGB_OPT_STEP_SCHEDULE: *value = h->step_schedule; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_BLOCKS_PER_SM: *value = h->queue_blocks_per_sm; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_OCCUPANCY: *value = h->occupancy_blocks; return CLMGB_OK;
+    case CLMGB_OPT_NUM_SMS: *value = h->num_sms; return CLMGB_OK;
+    default: return CLMGB_ERR_CONFIG;
+  }
+}
+
+int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y, double* out,
+                        void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (op < 0 || op > 3 || n < 0) return CLMGB_ERR_CONFIG;
+  if (n == 0) return CLMGB_OK;
+  if (!x || !out || (op == 2 && !y)) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_math_eval(op, n, x, y, out, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 

@@ -7,12 +7,13 @@
 //
 // Arithmetic follows the reference's Float64 expressions operation by operation
 // (this file is compiled with --fmad=false so a*b+c is never fused, as in Julia),
-// which makes the results equal to the CPU oracle except where a transcendental
-// (pow, log10) differs in the last ulp.  Citations are to CLM.jl source files.
+// and the transcendentals come from clm_math.h, which the CPU oracle shares: the
+// GPU and the oracle produce the same bits.  Citations are to CLM.jl source files.
 #pragma once
 #include <stdint.h>
 #include <math.h>
 #include "../../include/clmgb.h"
+#include "clm_math.h"
 
 namespace clmgb {
 
@@ -289,7 +290,7 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
       const double tt = LV(T, c, jj, ld);
       if (tt < TFRZ) {
         const double smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
-        double sc = LVc(f.watsat, c, j, ld) * pow(smp / LVc(f.sucsat, c, j, ld), -1.0 / LVc(f.bsw, c, j, ld));
+        double sc = LVc(f.watsat, c, j, ld) * cm_pow(smp / LVc(f.sucsat, c, j, ld), -1.0 / LVc(f.bsw, c, j, ld));
         sc *= LVc(f.dz, c, jj, ld) * 1000.0;
         supercool[j] = sc;
       }
@@ -463,12 +464,12 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
           satw = jl_min(1.0, satw);
           if (satw > 1.0e-7) {
             double dke;
-            if (tt[jj] >= TFRZ) dke = jl_max(0.0, log10(satw) + 1.0);
+            if (tt[jj] >= TFRZ) dke = jl_max(0.0, cm_log10(satw) + 1.0);
             else dke = satw;
             const double a1 = liq / (DENH2O * dzv);
             const double fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
             const double fl = a1 / fl_denom;
-            const double dksat = LVc(f.tkmg, c, j, ld) * pow(TKWAT, fl * ws) * pow(TKICE, (1.0 - fl) * ws);
+            const double dksat = LVc(f.tkmg, c, j, ld) * cm_pow(TKWAT, fl * ws) * cm_pow(TKICE, (1.0 - fl) * ws);
             thkv = dke * dksat + (1.0 - dke) * LVc(f.tkdry, c, j, ld);
           } else {
             thkv = LVc(f.tkdry, c, j, ld);
@@ -760,192 +761,267 @@ __device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_s
 }
 
 // ===========================================================================
-// _soilwm_moisture_form_kernel! (soil_water_movement.jl:1250-1489), column c.
+// _soilwm_moisture_form_kernel! (soil_water_movement.jl:1250-1489) as a per-column
+// state machine: mf_begin loads a column, mf_attempt runs one substep attempt of
+// the reference's `while true` loop, mf_end stores the results.  A thread can then
+// work through several columns, one attempt at a time (see k_moisture_form_queue).
 //
-// Identical arithmetic to the reference, with two exact hoists:
-//  * the ice impedance 10^(-e_ice*icefrac) depends only on icefrac, which is fixed
-//    during the call, so it is formed once per call instead of once per attempt;
+// Identical arithmetic to the reference, with three exact hoists:
+//  * the ice impedance 10^(-e_ice*icefrac) depends only on icefrac, fixed during
+//    the call, so it is formed once per column instead of once per attempt;
 //  * a rejected attempt leaves h2osoi_liq unchanged, so the hydraulic properties,
 //    fluxes and flux derivatives of the retry equal the previous attempt's bit for
-//    bit; they are recomputed only after an accepted substep.
+//    bit; they are recomputed only after an accepted substep;
+//  * dt_dz = dtsub/(1000*dz): when dtsub is halved or doubled the quotient scales
+//    by exactly the same power of two, so it is rescaled through its exponent bits
+//    instead of divided again; any other change of dtsub divides afresh.
 // ===========================================================================
-__device__ inline uint32_t moisture_form_col(const Dims& D, const clmgb_soilwater_fields& f,
-                                      const clmgb_swm_config& cfg, double dtime, int64_t c,
-                                      int* attempts_out) {
-  const int64_t ld = D.ldc;
-  const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
-  const int nlayers = (int)f.col_nbedrock[c];
-  if (nlayers < 1 || nlayers > nlevsoi) return CLMGB_COL_LEVEL_RANGE;
-  const double e_ice = cfg.e_ice, dtmin = cfg.dtmin, xtu = cfg.xTolerUpper, xtl = cfg.xTolerLower;
-  const double verysmall = cfg.verySmall;
-  const bool expensive = (cfg.flux_calculation == 42);
-  const int lower_bc = cfg.lower_boundary_condition;
-
+struct MfLane {
+  int64_t c;
+  int nlayers;
+  int nsub;
+  bool fresh;
+  uint32_t status;
+  double dtsub, dtdone, qc, dt_cur;
   double liq[MAXSOI + 1], dzv[MAXSOI + 1], imp[MAXSOI + 1];
   double hk[MAXSOI + 1], dhkdw[MAXSOI + 1];
   double qin[MAXSOI + 1], qout[MAXSOI + 1], dqidw0[MAXSOI + 1], dqidw1[MAXSOI + 1];
   double dqodw1[MAXSOI + 1], dqodw2[MAXSOI + 1], fnet1[MAXSOI + 1];
   double gam[MAXSOI + 1], dwat[MAXSOI + 1], dt_dz[MAXSOI + 1];
-  for (int j = 1; j <= nlayers; j++) {
-    liq[j] = LV(f.h2osoi_liq, c, joff + j, ld);
-    dzv[j] = LVc(f.dz, c, joff + j, ld);
+};
+
+// returns false (and sets L.status) when the column cannot be solved
+__device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
+                                         const clmgb_swm_config& cfg, double dtime, int64_t c) {
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno;
+  L.c = c;
+  L.status = 0;
+  const int64_t nl = f.col_nbedrock[c];
+  if (nl < 1 || nl > D.nlevsoi) {
+    L.status = CLMGB_COL_LEVEL_RANGE;
+    return false;
   }
+  const int nlayers = (int)nl;
+  L.nlayers = nlayers;
   for (int j = 1; j <= nlayers; j++) {
-    if (j == nlayers) imp[j] = pow(10.0, -e_ice * LV(f.icefrac, c, j, ld));
-    else imp[j] = pow(10.0, -e_ice * (0.5 * (LV(f.icefrac, c, j, ld) + LV(f.icefrac, c, j + 1, ld))));
+    L.liq[j] = LV(f.h2osoi_liq, c, joff + j, ld);
+    L.dzv[j] = LVc(f.dz, c, joff + j, ld);
   }
-  const double qinfl = f.qflx_infl[c];
-  int nsubstep = 0;
-  double dtsub = dtime, dtdone = 0.0, qc = 0.0;
-  bool fresh = true;   // hydraulics must be (re)computed from liq
-  uint32_t status = 0;
-  for (;;) {
-    nsubstep += 1;
-    if (nsubstep > MF_ATTEMPT_CAP) { status |= CLMGB_COL_SUBSTEP_CAP; break; }
-    for (int j = 1; j <= nlayers; j++) dt_dz[j] = dtsub / (M_TO_MM * dzv[j]);
-    if (fresh) {
-      double s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
+  const double e_ice = cfg.e_ice;
+  for (int j = 1; j <= nlayers; j++) {
+    if (j == nlayers) L.imp[j] = cm_pow(10.0, -e_ice * LV(f.icefrac, c, j, ld));
+    else L.imp[j] = cm_pow(10.0, -e_ice * (0.5 * (LV(f.icefrac, c, j, ld) + LV(f.icefrac, c, j + 1, ld))));
+  }
+  L.nsub = 0;
+  L.dtsub = dtime;
+  L.dtdone = 0.0;
+  L.qc = 0.0;
+  L.fresh = true;
+  L.dt_cur = -1.0;
+  return true;
+}
+
+// one attempt; returns true when the column's substep loop has finished
+__device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
+                                           const clmgb_swm_config& cfg, double dtime) {
+  const int64_t ld = D.ldc;
+  const int64_t c = L.c;
+  const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
+  const int nlayers = L.nlayers;
+  const int lower_bc = cfg.lower_boundary_condition;
+  L.nsub += 1;
+  if (L.nsub > MF_ATTEMPT_CAP) {
+    L.status |= CLMGB_COL_SUBSTEP_CAP;
+    return true;
+  }
+  const double dtsub = L.dtsub;
+  // ---- dt_dz = dtsub / (1000*dz) ----
+  if (dtsub != L.dt_cur) {
+    const uint64_t a = (uint64_t)__double_as_longlong(dtsub), b = (uint64_t)__double_as_longlong(L.dt_cur);
+    const uint64_t MANT = 0x000fffffffffffffULL;
+    const int ea = (int)((a >> 52) & 0x7ff), eb = (int)((b >> 52) & 0x7ff);
+    if (L.dt_cur > 0.0 && (a & MANT) == (b & MANT) && ea > 0 && eb > 0 && ea < 2047 && eb < 2047) {
+      const long long shift = (long long)(ea - eb) << 52;
       for (int j = 1; j <= nlayers; j++) {
-        const double vwc = jl_max(liq[j], 1.0e-6) / (dzv[j] * DENH2O);
-        double s = vwc / LVc(f.watsat, c, j, ld);
-        s = jl_min(s, 1.0);
-        s = jl_max(0.01, s);
-        s2[j] = s;
+        const long long v = __double_as_longlong(L.dt_dz[j]);
+        const int ev = (int)((v >> 52) & 0x7ff);
+        if (ev + (ea - eb) > 0 && ev + (ea - eb) < 2047 && ev > 0)
+          L.dt_dz[j] = __longlong_as_double(v + shift);
+        else
+          L.dt_dz[j] = dtsub / (M_TO_MM * L.dzv[j]);
       }
-      for (int j = 1; j <= nlayers; j++) {
-        double s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
-        s1 = jl_min(s1, 1.0);
-        s1 = jl_max(0.01, s1);
-        const double b = LVc(f.bsw, c, j, ld);
-        const double hkv = imp[j] * LVc(f.hksat, c, j, ld) * pow(s1, 2.0 * b + 3.0);
-        const double dhkds = (2.0 * b + 3.0) * hkv / s1;
-        const double sn = s2[j];
-        const double smpv = -LVc(f.sucsat, c, j, ld) * pow(sn, -b);
-        const double dsmpds = -b * smpv / sn;
-        hk[j] = hkv;
-        smp[j] = smpv;
-        dhkdw[j] = dhkds;
-        dsmpdw[j] = dsmpds / LVc(f.watsat, c, j, ld);
-        LV(f.smp_l, c, j, ld) = smpv;
-        LV(f.hk_l, c, j, ld) = hkv;
-      }
-      for (int j = 1; j <= nlayers; j++) {
-        qin[j] = 0.0; qout[j] = 0.0; dqidw0[j] = 0.0; dqidw1[j] = 0.0; dqodw1[j] = 0.0; dqodw2[j] = 0.0;
-      }
-      for (int j = 1; j <= nlayers - 1; j++) {
-        const double dhkds1 = 0.5 * dhkdw[j] / LVc(f.watsat, c, j, ld);
-        const double dhkds2 = 0.5 * dhkdw[j] / LVc(f.watsat, c, j + 1, ld);
-        const double num = smp[j + 1] - smp[j];
-        const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
-        qout[j] = -hk[j] * num / den + hk[j];
-        dqodw1[j] = (hk[j] * dsmpdw[j] - dhkds1 * num) / den + dhkds1;
-        dqodw2[j] = (-hk[j] * dsmpdw[j + 1] - dhkds2 * num) / den + dhkds2;
-      }
-      {
-        const int j = nlayers;
-        if (lower_bc == CLMGB_BC_WATERTABLE) {
-          int jwt = nlevsoi;
-          for (int jj = 1; jj <= nlevsoi; jj++) {
-            if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
-          }
-          if (j > jwt) {
-            qout[j] = 0.0; dqodw1[j] = 0.0; dqodw2[j] = 0.0;
-          } else {
-            const double dhkds1l = dhkdw[j] / LVc(f.watsat, c, j, ld);
-            const double num = -smp[j];
-            const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
-            qout[j] = -hk[j] * num / den + hk[j];
-            dqodw1[j] = (hk[j] * dsmpdw[j] - dhkds1l * num) / den + dhkds1l;
-            dqodw2[j] = 0.0;
-          }
-        } else if (lower_bc == CLMGB_BC_FLUX) {
-          qout[j] = hk[j];
-          dqodw1[j] = dhkdw[j] / LVc(f.watsat, c, j, ld);
-        } else {
-          qout[j] = 0.0;
-          dqodw1[j] = 0.0;
-        }
-      }
-      for (int j = 2; j <= nlayers; j++) {
-        qin[j] = qout[j - 1];
-        dqidw0[j] = dqodw1[j - 1];
-        dqidw1[j] = dqodw2[j - 1];
-      }
-      qin[1] = qinfl;
-      dqidw1[1] = 0.0;
-      for (int j = 1; j <= nlayers; j++) fnet1[j] = qin[j] - qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
-      fresh = false;
+    } else {
+      for (int j = 1; j <= nlayers; j++) L.dt_dz[j] = dtsub / (M_TO_MM * L.dzv[j]);
     }
-    // ---- RHS / LHS assembly fused into the Thomas forward sweep ----
-    double bet, dwat_prev;
-    {
-      const double rmx = -fnet1[1] * dt_dz[1];
-      const double bmx = -1.0 - (-dqidw1[1] + dqodw1[1]) * dt_dz[1];
-      bet = bmx;
-      if (fabs(bet) < 1.0e-30) bet = 1.0e-30;
-      dwat_prev = rmx / bet;
-      dwat[1] = dwat_prev;
-    }
-    double cmx_prev = -dqodw2[1] * dt_dz[1];
-    for (int j = 2; j <= nlayers; j++) {
-      const double amx = dqidw0[j] * dt_dz[j];
-      const double bmx = -1.0 - (-dqidw1[j] + dqodw1[j]) * dt_dz[j];
-      const double cmx = (j == nlayers) ? 0.0 : -dqodw2[j] * dt_dz[j];
-      const double rmx = -fnet1[j] * dt_dz[j];
-      gam[j] = cmx_prev / bet;
-      bet = bmx - amx * gam[j];
-      if (fabs(bet) < 1.0e-30) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
-      dwat_prev = (rmx - amx * dwat_prev) / bet;
-      dwat[j] = dwat_prev;
-      cmx_prev = cmx;
-    }
-    {
-      double dwat_next = dwat_prev;
-      for (int j = nlayers - 1; j >= 1; j--) {
-        dwat_next = dwat[j] - gam[j + 1] * dwat_next;
-        dwat[j] = dwat_next;
-      }
-    }
-    // ---- error estimate ----
-    double errorMax = 0.0;
+    L.dt_cur = dtsub;
+  }
+  if (L.fresh) {
+    // ---- hydraulic properties (Clapp-Hornberger inlined, :1280-1308) ----
+    double s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
     for (int j = 1; j <= nlayers; j++) {
-      double fnet0;
-      if (expensive) {
-        const double qin_test = j == 1 ? qin[j] + dqidw1[j] * dwat[j]
-                                       : qin[j] + dqidw0[j] * dwat[j - 1] + dqidw1[j] * dwat[j];
-        const double qout_test = j == nlayers ? qout[j] + dqodw1[j] * dwat[j]
-                                              : qout[j] + dqodw1[j] * dwat[j] + dqodw2[j] * dwat[j + 1];
-        fnet0 = qin_test - qout_test - LVc(f.qflx_rootsoi, c, j, ld);
+      const double vwc = jl_max(L.liq[j], 1.0e-6) / (L.dzv[j] * DENH2O);
+      double s = vwc / LVc(f.watsat, c, j, ld);
+      s = jl_min(s, 1.0);
+      s = jl_max(0.01, s);
+      s2[j] = s;
+    }
+    for (int j = 1; j <= nlayers; j++) {
+      double s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
+      s1 = jl_min(s1, 1.0);
+      s1 = jl_max(0.01, s1);
+      const double b = LVc(f.bsw, c, j, ld);
+      const double hkv = L.imp[j] * LVc(f.hksat, c, j, ld) * cm_pow(s1, 2.0 * b + 3.0);
+      const double dhkds = (2.0 * b + 3.0) * hkv / s1;
+      const double sn = s2[j];
+      const double smpv = -LVc(f.sucsat, c, j, ld) * cm_pow(sn, -b);
+      const double dsmpds = -b * smpv / sn;
+      L.hk[j] = hkv;
+      smp[j] = smpv;
+      L.dhkdw[j] = dhkds;
+      dsmpdw[j] = dsmpds / LVc(f.watsat, c, j, ld);
+      LV(f.smp_l, c, j, ld) = smpv;
+      LV(f.hk_l, c, j, ld) = hkv;
+    }
+    // ---- fluxes and derivatives (:1310-1378) ----
+    for (int j = 1; j <= nlayers; j++) {
+      L.qin[j] = 0.0; L.qout[j] = 0.0; L.dqidw0[j] = 0.0; L.dqidw1[j] = 0.0;
+      L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
+    }
+    for (int j = 1; j <= nlayers - 1; j++) {
+      const double dhkds1 = 0.5 * L.dhkdw[j] / LVc(f.watsat, c, j, ld);
+      const double dhkds2 = 0.5 * L.dhkdw[j] / LVc(f.watsat, c, j + 1, ld);
+      const double num = smp[j + 1] - smp[j];
+      const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
+      L.qout[j] = -L.hk[j] * num / den + L.hk[j];
+      L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1 * num) / den + dhkds1;
+      L.dqodw2[j] = (-L.hk[j] * dsmpdw[j + 1] - dhkds2 * num) / den + dhkds2;
+    }
+    {
+      const int j = nlayers;
+      if (lower_bc == CLMGB_BC_WATERTABLE) {
+        int jwt = nlevsoi;
+        for (int jj = 1; jj <= nlevsoi; jj++) {
+          if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
+        }
+        if (j > jwt) {
+          L.qout[j] = 0.0; L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
+        } else {
+          const double dhkds1l = L.dhkdw[j] / LVc(f.watsat, c, j, ld);
+          const double num = -smp[j];
+          const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
+          L.qout[j] = -L.hk[j] * num / den + L.hk[j];
+          L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1l * num) / den + dhkds1l;
+          L.dqodw2[j] = 0.0;
+        }
+      } else if (lower_bc == CLMGB_BC_FLUX) {
+        L.qout[j] = L.hk[j];
+        L.dqodw1[j] = L.dhkdw[j] / LVc(f.watsat, c, j, ld);
       } else {
-        fnet0 = dwat[j] / dt_dz[j];
+        L.qout[j] = 0.0;
+        L.dqodw1[j] = 0.0;
       }
-      const double ev = fabs(fnet1[j] - fnet0) * dtsub * 0.5;
-      errorMax = jl_max(errorMax, ev);
     }
-    if (errorMax > xtu && dtsub > dtmin) {
-      dtsub = jl_max(dtsub / 2.0, dtmin);
-      continue;
+    for (int j = 2; j <= nlayers; j++) {
+      L.qin[j] = L.qout[j - 1];
+      L.dqidw0[j] = L.dqodw1[j - 1];
+      L.dqidw1[j] = L.dqodw2[j - 1];
     }
-    for (int j = 1; j <= nlayers; j++) liq[j] = liq[j] + dwat[j] * (M_TO_MM * dzv[j]);
-    fresh = true;
-    double qcTemp;
-    if (lower_bc == CLMGB_BC_FLUX) qcTemp = hk[nlayers] + dhkdw[nlayers] * dwat[nlayers];
-    else if (lower_bc == CLMGB_BC_ZERO_FLUX) qcTemp = 0.0;
-    else qcTemp = qout[nlayers] + dqodw1[nlayers] * dwat[nlayers];
-    qc += qcTemp * (dtsub / dtime);
-    dtdone += dtsub;
-    if (fabs(dtime - dtdone) < verysmall) break;
-    if (errorMax < xtl) dtsub = dtsub * 2.0;
-    dtsub = jl_min(dtsub, dtime - dtdone);
+    L.qin[1] = f.qflx_infl[c];
+    L.dqidw1[1] = 0.0;
+    for (int j = 1; j <= nlayers; j++) L.fnet1[j] = L.qin[j] - L.qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
+    L.fresh = false;
   }
+  // ---- RHS / LHS (:1380-1397) fused into the Thomas forward sweep (:1421-1438) ----
+  double bet, dwat_prev;
+  {
+    const double rmx = -L.fnet1[1] * L.dt_dz[1];
+    const double bmx = -1.0 - (-L.dqidw1[1] + L.dqodw1[1]) * L.dt_dz[1];
+    bet = bmx;
+    if (fabs(bet) < 1.0e-30) bet = 1.0e-30;
+    dwat_prev = rmx / bet;
+    L.dwat[1] = dwat_prev;
+  }
+  double cmx_prev = -L.dqodw2[1] * L.dt_dz[1];
+  for (int j = 2; j <= nlayers; j++) {
+    const double amx = L.dqidw0[j] * L.dt_dz[j];
+    const double bmx = -1.0 - (-L.dqidw1[j] + L.dqodw1[j]) * L.dt_dz[j];
+    const double cmx = (j == nlayers) ? 0.0 : -L.dqodw2[j] * L.dt_dz[j];
+    const double rmx = -L.fnet1[j] * L.dt_dz[j];
+    L.gam[j] = cmx_prev / bet;
+    bet = bmx - amx * L.gam[j];
+    if (fabs(bet) < 1.0e-30) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
+    dwat_prev = (rmx - amx * dwat_prev) / bet;
+    L.dwat[j] = dwat_prev;
+    cmx_prev = cmx;
+  }
+  {
+    double dwat_next = dwat_prev;
+    for (int j = nlayers - 1; j >= 1; j--) {
+      dwat_next = L.dwat[j] - L.gam[j + 1] * dwat_next;
+      L.dwat[j] = dwat_next;
+    }
+  }
+  // ---- error estimate (:1440-1457) ----
+  const bool expensive = (cfg.flux_calculation == 42);
+  double errorMax = 0.0;
   for (int j = 1; j <= nlayers; j++) {
-    LV(f.h2osoi_liq, c, joff + j, ld) = liq[j];
-    if (!isfinite(liq[j])) status |= CLMGB_COL_NONFINITE;
+    double fnet0;
+    if (expensive) {
+      const double qin_test = j == 1 ? L.qin[j] + L.dqidw1[j] * L.dwat[j]
+                                     : L.qin[j] + L.dqidw0[j] * L.dwat[j - 1] + L.dqidw1[j] * L.dwat[j];
+      const double qout_test = j == nlayers ? L.qout[j] + L.dqodw1[j] * L.dwat[j]
+                                            : L.qout[j] + L.dqodw1[j] * L.dwat[j] + L.dqodw2[j] * L.dwat[j + 1];
+      fnet0 = qin_test - qout_test - LVc(f.qflx_rootsoi, c, j, ld);
+    } else {
+      fnet0 = L.dwat[j] / L.dt_dz[j];
+    }
+    const double ev = fabs(L.fnet1[j] - fnet0) * dtsub * 0.5;
+    errorMax = jl_max(errorMax, ev);
   }
-  f.qcharge[c] = qc;
-  f.num_substeps[c] = (double)nsubstep;
-  if (attempts_out) *attempts_out = nsubstep;
+  // ---- reject (:1460-1463) ----
+  if (errorMax > cfg.xTolerUpper && dtsub > cfg.dtmin) {
+    L.dtsub = jl_max(dtsub / 2.0, cfg.dtmin);
+    return false;
+  }
+  // ---- accept (:1466-1483) ----
+  for (int j = 1; j <= nlayers; j++) L.liq[j] = L.liq[j] + L.dwat[j] * (M_TO_MM * L.dzv[j]);
+  L.fresh = true;
+  double qcTemp;
+  if (lower_bc == CLMGB_BC_FLUX) qcTemp = L.hk[nlayers] + L.dhkdw[nlayers] * L.dwat[nlayers];
+  else if (lower_bc == CLMGB_BC_ZERO_FLUX) qcTemp = 0.0;
+  else qcTemp = L.qout[nlayers] + L.dqodw1[nlayers] * L.dwat[nlayers];
+  L.qc += qcTemp * (dtsub / dtime);
+  L.dtdone += dtsub;
+  if (fabs(dtime - L.dtdone) < cfg.verySmall) return true;
+  double nd = dtsub;
+  if (errorMax < cfg.xTolerLower) nd = dtsub * 2.0;
+  L.dtsub = jl_min(nd, dtime - L.dtdone);
+  return false;
+}
+
+__device__ __forceinline__ uint32_t mf_end(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f) {
+  const int64_t ld = D.ldc;
+  const int64_t c = L.c;
+  const int joff = D.nlevsno;
+  uint32_t status = L.status;
+  for (int j = 1; j <= L.nlayers; j++) {
+    LV(f.h2osoi_liq, c, joff + j, ld) = L.liq[j];
+    if (!isfinite(L.liq[j])) status |= CLMGB_COL_NONFINITE;
+  }
+  f.qcharge[c] = L.qc;
+  f.num_substeps[c] = (double)L.nsub;
   return status;
+}
+
+// The whole substep loop for one column (one thread, one column).
+__device__ inline uint32_t moisture_form_col(const Dims& D, const clmgb_soilwater_fields& f,
+                                             const clmgb_swm_config& cfg, double dtime, int64_t c) {
+  MfLane L;
+  if (!mf_begin(L, D, f, cfg, dtime, c)) return L.status;
+  while (!mf_attempt(L, D, f, cfg, dtime)) {
+  }
+  return mf_end(L, D, f);
 }
 
 }  // namespace clmgb

@@ -1,0 +1,80 @@
+"""Generates clm_math_tables.h: the lookup tables of clm_math.h (log/exp).
+
+Run from this directory:  python gen_math_tables.py > clm_math_tables.h
+Needs mpmath (bundled with sympy).  Values are computed at 200-bit precision and
+rounded once to binary64, written as C99 hex-float literals so C and CUDA compile
+exactly the same bits.
+
+log table (Tang's table-driven logarithm): the reduced argument z = x*2^-k lies in
+[0.75, 1.5) and is split into 128 subintervals by the top 7 bits of (bits(x) -
+bits(0.75)): 64 intervals of width 1/256 on [0.75, 1) and 64 of width 1/128 on
+[1, 1.5).  For the centre c_i of interval i the table stores invc_i = RN(1/c_i) and
+logc_i = RN(-log(invc_i)), so log(z) = logc_i + log1p(z*invc_i - 1) with
+|z*invc_i - 1| < 0.004.
+
+exp table (Tang's table-driven exponential, N = 64): T_j = RN(2^(j/64)), j = 0..63.
+Also the split constants ln2/N = hi + lo with hi holding 36 significant bits (k*hi
+exact for |k| < 2^17) and ln2 = hi + lo with 42-bit hi (k*hi exact for |k| < 2^11).
+"""
+import mpmath as mp
+
+mp.mp.prec = 200
+
+
+def hexd(v):
+    return float(v).hex()
+
+
+def round_bits(v, bits):
+    """Round mpf v to `bits` significant bits (returned as a Python float)."""
+    m, e = mp.frexp(v)
+    scale = mp.mpf(2) ** bits
+    return float(mp.nint(m * scale) / scale * mp.mpf(2) ** e)
+
+
+def main():
+    lines = ["// clm_math_tables.h — generated by gen_math_tables.py; do not edit.", "#pragma once", ""]
+    invc, logc = [], []
+    for i in range(128):
+        if i < 64:
+            lo = mp.mpf(0.75) + mp.mpf(i) / 256
+            w = mp.mpf(1) / 256
+        else:
+            lo = mp.mpf(1) + mp.mpf(i - 64) / 128
+            w = mp.mpf(1) / 128
+        c = lo + w / 2
+        ic = float(1 / c)
+        invc.append(ic)
+        logc.append(float(-mp.log(mp.mpf(ic))))
+    lines.append("CM_TABLE(CM_LOG_INVC, 128) = {")
+    lines += ["  %s," % hexd(v) for v in invc]
+    lines.append("};")
+    lines.append("CM_TABLE(CM_LOG_LOGC, 128) = {")
+    lines += ["  %s," % hexd(v) for v in logc]
+    lines.append("};")
+    lines.append("CM_TABLE(CM_EXP_T, 64) = {")
+    lines += ["  %s," % hexd(mp.mpf(2) ** (mp.mpf(j) / 64)) for j in range(64)]
+    lines.append("};")
+    ln2 = mp.log(2)
+    ln2n = ln2 / 64
+    hi_n = round_bits(ln2n, 36)
+    lo_n = float(ln2n - mp.mpf(hi_n))
+    hi = round_bits(ln2, 42)
+    lo = float(ln2 - mp.mpf(hi))
+    consts = {
+        "CM_LN2N_HI": hi_n, "CM_LN2N_LO": lo_n, "CM_INVLN2N": float(64 / ln2),
+        "CM_LN2_HI": hi, "CM_LN2_LO": lo, "CM_INVLN10": float(1 / mp.log(10)),
+    }
+    lines.append("")
+    for k, v in consts.items():
+        lines.append("#define %s (%s)" % (k, hexd(v)))
+    # log1p(r) = r - r^2/2 + ... : coefficients 1/n, n = 2..7 (signs applied in code)
+    for n in range(2, 8):
+        lines.append("#define CM_LOG_C%d (%s)" % (n, hexd(mp.mpf((-1) ** (n + 1)) / n)))
+    for n in range(2, 7):
+        lines.append("#define CM_EXP_C%d (%s)" % (n, hexd(1 / mp.factorial(n))))
+    print("\n".join(lines))
+
+
+if __name__ == "__main__":
+    main()

@@ -36,7 +36,7 @@ k_moisture_form(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config c
   const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
   if (c >= nc) return;
   uint32_t st = 0;
-  if (f.mask_hydrology[c]) st = moisture_form_col(D, f, cfg, dtime, c, nullptr);
+  if (f.mask_hydrology[c]) st = moisture_form_col(D, f, cfg, dtime, c);
   report(st, col_status, dev_status, c);
 }
 
@@ -58,9 +58,97 @@ k_column_step(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fiel
   }
   if (fw.mask_hydrology[c]) {
     water_fractions_col(D, fw, c);
-    st |= moisture_form_col(D, fw, cfg, dtime, c, nullptr);
+    st |= moisture_form_col(D, fw, cfg, dtime, c);
   }
   report(st, col_status, dev_status, c);
+}
+
+// soil_temperature! then set_soil_water_fractions! for one column per thread (the
+// first half of a column step; the Richards solve follows in k_moisture_form_queue).
+__global__ void __launch_bounds__(BLOCK)
+k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw,
+                             double dtime, int snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                             uint32_t* col_status, uint32_t* dev_status) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  uint32_t st = 0;
+  if (ft.mask_nolakec[c]) {
+    if (t_ssbef) {
+      const int L = D.nlevsno + D.nlevmax;
+      for (int jj = 1; jj <= L; jj++) LV(t_ssbef, c, jj, D.ldc) = LV(ft.t_soisno, c, jj, D.ldc);
+    }
+    if (t_h2osfc_bef) t_h2osfc_bef[c] = ft.t_h2osfc[c];
+    st |= soil_temperature_col(D, ft, c, dtime, snow_method);
+  }
+  if (fw.mask_hydrology[c]) water_fractions_col(D, fw, c);
+  report(st, col_status, dev_status, c);
+}
+
+// soilwm_moisture_form_solve! as a persistent kernel fed by a device work queue.
+// Each lane owns one column at a time and advances it one substep attempt per loop
+// trip; when its column finishes it takes the next column index from the queue
+// (one atomicAdd per warp for all lanes that need work).  Columns need from 1 to
+// ~50 attempts, so lanes stay busy instead of waiting for the slowest column of
+// the warp.  The per-column arithmetic is unchanged, so results do not depend on
+// the schedule.  `queue` must be zero at launch.
+__global__ void __launch_bounds__(BLOCK)
+k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
+                      uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  MfLane L;
+  bool active = false, exhausted = false;
+  for (;;) {
+    const bool need = !active && !exhausted;
+    const unsigned m = __ballot_sync(FULL, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        const int64_t c = (int64_t)(base + (unsigned long long)__popc(m & ((1u << lane) - 1u)));
+        if (c >= nc) {
+          exhausted = true;
+        } else if (f.mask_hydrology[c]) {
+          if (mf_begin(L, D, f, cfg, dtime, c)) {
+            active = true;
+          } else {
+            const uint32_t st = L.status;
+            if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
+            if (st && dev_status) atomicOr(dev_status, st);
+          }
+        } else if (col_status && !or_status) {
+          col_status[c] = 0;
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) {
+      if (__all_sync(FULL, exhausted)) break;
+      continue;
+    }
+    if (active && mf_attempt(L, D, f, cfg, dtime)) {
+      const uint32_t st = mf_end(L, D, f);
+      if (col_status) col_status[L.c] = or_status ? (col_status[L.c] | st) : st;
+      if (st && dev_status) atomicOr(dev_status, st);
+      active = false;
+    }
+  }
+}
+
+// Evaluates the shared transcendentals (clm_math.h) elementwise; op 0 log, 1 exp,
+// 2 pow, 3 log10.  Used to check that GPU and CPU builds return identical bits.
+__global__ void __launch_bounds__(BLOCK)
+k_math_eval(int op, int64_t n, const double* x, const double* y, double* out) {
+  const int64_t i = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (i >= n) return;
+  const double a = x[i];
+  double r;
+  if (op == 0) r = cm_log(a);
+  else if (op == 1) r = cm_exp(a);
+  else if (op == 2) r = cm_pow(a, y[i]);
+  else r = cm_log10(a);
+  out[i] = r;
 }
 
 __global__ void __launch_bounds__(BLOCK)
@@ -180,6 +268,35 @@ cudaError_t launch_column_step(const Dims& D, int64_t nc, const clmgb_soiltemp_f
                                uint32_t* dev_status, cudaStream_t s) {
   k_column_step<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef,
                                                col_status, dev_status);
+  return cudaGetLastError();
+}
+cudaError_t launch_soiltemp_fractions(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                                      const clmgb_soilwater_fields& fw, double dtime, int snow_method,
+                                      double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
+                                      uint32_t* dev_status, cudaStream_t s) {
+  k_soil_temperature_fractions<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, dtime, snow_method, t_ssbef,
+                                                              t_h2osfc_bef, col_status, dev_status);
+  return cudaGetLastError();
+}
+int queue_blocks_per_sm() {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_moisture_form_queue, BLOCK, 0) != cudaSuccess) nb = 1;
+  return nb > 0 ? nb : 1;
+}
+cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
+                                       int or_status, uint32_t* dev_status, unsigned long long* queue,
+                                       int grid_blocks, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  const int64_t need = (nc + BLOCK - 1) / BLOCK;
+  const int grid = (int)(need < grid_blocks ? need : grid_blocks);
+  k_moisture_form_queue<<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
+                                                              dev_status, queue);
+  return cudaGetLastError();
+}
+cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {
+  k_math_eval<<<grid_for(n), BLOCK, 0, s>>>(op, n, x, y, out);
   return cudaGetLastError();
 }
 cudaError_t launch_phase_change(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,

@@ -33,4 +33,15 @@ cudaError_t launch_synth_forcing(const Dims& D, int64_t nc, const clmgb_soiltemp
                                  const clmgb_soilwater_fields& fw, const double* G, const double* I,
                                  cudaStream_t s);
 
+cudaError_t launch_soiltemp_fractions(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                                      const clmgb_soilwater_fields& fw, double dtime, int snow_method,
+                                      double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
+                                      uint32_t* dev_status, cudaStream_t s);
+int queue_blocks_per_sm();
+cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
+                                       int or_status, uint32_t* dev_status, unsigned long long* queue,
+                                       int grid_blocks, cudaStream_t s);
+cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s);
+
 }  // namespace clmgb

@@ -248,6 +248,22 @@ int32_t clmgb_destroy(clmgb_handle h);
 int32_t clmgb_device_status(clmgb_handle h, void* stream, uint32_t* status, int32_t reset);
 int32_t clmgb_last_cuda_error(clmgb_handle h);
 
+/* ---- tunables (clmgb_set_option / clmgb_get_option keys) ---- */
+#define CLMGB_OPT_STEP_SCHEDULE        1  /* how the Richards solve is scheduled: */
+#define   CLMGB_SCHEDULE_FUSED         0  /*   one column per thread, whole step in one kernel */
+#define   CLMGB_SCHEDULE_QUEUE         1  /*   persistent kernel fed by a device work queue (default) */
+#define CLMGB_OPT_QUEUE_BLOCKS_PER_SM  2  /* resident blocks per SM of the queue kernel (0 = occupancy limit) */
+#define CLMGB_OPT_QUEUE_OCCUPANCY      3  /* read-only: occupancy limit of the queue kernel */
+#define CLMGB_OPT_NUM_SMS              4  /* read-only: SMs of the handle's device */
+int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
+int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value);
+
+/* Evaluates the library's binary64 log (op 0), exp (1), pow (2) or log10 (3)
+ * elementwise on device arrays; y is read for pow only.  The oracle and the tests
+ * use it to check that the GPU rounds exactly as the CPU build does. */
+int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y,
+                        double* out, void* stream);
+
 /* ---- drop-in entry points ---- */
 
 /* soil_temperature! (soil_temperature.jl:358) for non-urban, non-lake columns.

@@ -42,6 +42,9 @@
 #include <omp.h>
 #endif
 #include "../include/clmgb.h"
+/* Transcendentals: the same table-driven binary64 log/exp/pow as the CUDA kernels
+ * (published method, see clm_math.h), so the oracle and the GPU round identically. */
+#include "../clm.jl_gb300/csrc/clm_math.h"
 
 /* ---- constants: src/constants/varcon.jl:15-70 ---- */
 #define GRAV   9.80616
@@ -260,7 +263,7 @@ void orc_tridiagonal_col(double* u, const double* a, const double* b, const doub
 }
 
 /* ice_impedance (soil_water_movement.jl:722-724). */
-double orc_ice_impedance(double icefrac, double e_ice) { return pow(10.0, -e_ice * icefrac); }
+double orc_ice_impedance(double icefrac, double e_ice) { return cm_pow(10.0, -e_ice * icefrac); }
 
 /* ===================================================================== */
 /* soil_temperature! for one column (non-urban subset).                   */
@@ -431,7 +434,7 @@ static void pc_beta_col(const clmgb_varpar* vp, const clmgb_bounds* bd,
         if (IX(T, c, jj, ld) < TFRZ) {
           double tt = IX(T, c, jj, ld);
           double smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
-          supercool[j] = IX(f->watsat, c, j, ld) * pow(smp / IX(f->sucsat, c, j, ld), -1.0 / IX(f->bsw, c, j, ld));
+          supercool[j] = IX(f->watsat, c, j, ld) * cm_pow(smp / IX(f->sucsat, c, j, ld), -1.0 / IX(f->bsw, c, j, ld));
           supercool[j] *= IX(f->dz, c, jj, ld) * 1000.0;
         }
       }
@@ -606,11 +609,11 @@ static uint32_t soiltemp_col(const st_ctx* X, int64_t c)
         double thkv;
         if (satw > 1.0e-7) {
           double dke;
-          if (IX(T, c, jj, ld) >= TFRZ) dke = jl_max(0.0, log10(satw) + 1.0);
+          if (IX(T, c, jj, ld) >= TFRZ) dke = jl_max(0.0, cm_log10(satw) + 1.0);
           else dke = satw;
           double fl_denom = liq / (DENH2O * dzv) + ice / (DENICE * dzv) + exi / (DENICE * dzv);
           double fl = (liq / (DENH2O * dzv)) / fl_denom;
-          double dksat = IX(f->tkmg, c, j, ld) * pow(TKWAT, fl * ws) * pow(TKICE, (1.0 - fl) * ws);
+          double dksat = IX(f->tkmg, c, j, ld) * cm_pow(TKWAT, fl * ws) * cm_pow(TKICE, (1.0 - fl) * ws);
           thkv = dke * dksat + (1.0 - dke) * IX(f->tkdry, c, j, ld);
         } else {
           thkv = IX(f->tkdry, c, j, ld);
@@ -1059,18 +1062,18 @@ static uint32_t moisture_form_col(const clmgb_varpar* vp, const clmgb_bounds* b,
       double s1, imp;
       if (j == nlayers) {
         s1 = R[j].s2;
-        imp = pow(10.0, -e_ice * IX(f->icefrac, c, j, ld));
+        imp = cm_pow(10.0, -e_ice * IX(f->icefrac, c, j, ld));
       } else {
         s1 = 0.5 * (R[j].s2 + R[j + 1].s2);
-        imp = pow(10.0, -e_ice * (0.5 * (IX(f->icefrac, c, j, ld) + IX(f->icefrac, c, j + 1, ld))));
+        imp = cm_pow(10.0, -e_ice * (0.5 * (IX(f->icefrac, c, j, ld) + IX(f->icefrac, c, j + 1, ld))));
       }
       R[j].imped = imp;
       s1 = jl_min(s1, 1.0); s1 = jl_max(0.01, s1);
       double bb = IX(f->bsw, c, j, ld);
-      double hkv = imp * IX(f->hksat, c, j, ld) * pow(s1, 2.0 * bb + 3.0);
+      double hkv = imp * IX(f->hksat, c, j, ld) * cm_pow(s1, 2.0 * bb + 3.0);
       double dhkds = (2.0 * bb + 3.0) * hkv / s1;
       double sn = R[j].s2;
-      double smpv = -IX(f->sucsat, c, j, ld) * pow(sn, -bb);
+      double smpv = -IX(f->sucsat, c, j, ld) * cm_pow(sn, -bb);
       double dsmpds = -bb * smpv / sn;
       R[j].hk = hkv; R[j].smp = smpv; R[j].dhkdw = dhkds;
       R[j].dsmpdw = dsmpds / IX(f->watsat, c, j, ld);
@@ -1307,8 +1310,8 @@ void orc_init_soil_properties(int64_t n, const double* sand_in, const double* cl
     double sand = sand_in[i], clay = clay_in[i], om_frac = om_in[i];
     double watsat_mineral = 0.489 - 0.00126 * sand;
     double bsw_mineral = 2.91 + 0.159 * clay;
-    double sucsat_mineral = 10.0 * pow(10.0, 1.88 - 0.0131 * sand);
-    double xksat_mineral = 0.0070556 * pow(10.0, -0.884 + 0.0153 * sand);
+    double sucsat_mineral = 10.0 * cm_pow(10.0, 1.88 - 0.0131 * sand);
+    double xksat_mineral = 0.0070556 * cm_pow(10.0, -0.884 + 0.0153 * sand);
     double zsapric = 0.5;
     double depth_ratio = zsoi[i] / zsapric;
     double watsat_organic = jl_max(0.93 - 0.1 * depth_ratio, 0.83);
@@ -1321,8 +1324,8 @@ void orc_init_soil_properties(int64_t n, const double* sand_in, const double* cl
     double om_hksat = xksat_organic;
     double pcalpha = 0.5, pcbeta = 0.139, perc_frac;
     if (om_frac > pcalpha) {
-      double perc_norm = pow(1.0 - pcalpha, -pcbeta);
-      perc_frac = perc_norm * pow(om_frac - pcalpha, pcbeta);
+      double perc_norm = cm_pow(1.0 - pcalpha, -pcbeta);
+      perc_frac = perc_norm * cm_pow(om_frac - pcalpha, pcbeta);
     } else {
       perc_frac = 0.0;
     }
@@ -1337,7 +1340,7 @@ void orc_init_soil_properties(int64_t n, const double* sand_in, const double* cl
     double bd = (1.0 - watsat_mineral) * pd;
     double sc = sand + clay;
     double tkm = sc > 0.0 ? (1.0 - om_frac) * (tkd_sand * sand + tkd_clay * clay) / sc + tkm_om * om_frac : tkm_om;
-    tkmg[i] = pow(tkm, 1.0 - watsat_val);
+    tkmg[i] = cm_pow(tkm, 1.0 - watsat_val);
     tkdry[i] = ((0.135 * bd + 64.7) / (pd - 0.947 * bd)) * (1.0 - om_frac) + tkd_om * om_frac;
     double csol_min = sc > 0.0 ? (csol_sand * 1.0e6 * sand + csol_clay * 1.0e6 * clay) / sc : csol_om * 1.0e6;
     csol[i] = (1.0 - om_frac) * csol_min + csol_om * 1.0e6 * om_frac;
@@ -1345,3 +1348,9 @@ void orc_init_soil_properties(int64_t n, const double* sand_in, const double* cl
 }
 
 int orc_abi_version(void) { return CLMGB_ABI_VERSION; }
+
+/* Shared transcendentals, exported for the accuracy and GPU bit-parity tests. */
+double orc_cm_log(double x) { return cm_log(x); }
+double orc_cm_exp(double x) { return cm_exp(x); }
+double orc_cm_pow(double x, double y) { return cm_pow(x, y); }
+double orc_cm_log10(double x) { return cm_log10(x); }

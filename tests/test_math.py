@@ -1,0 +1,91 @@
+"""Accuracy of the shared table-driven log/exp/pow/log10 (clm_math.h) against
+200-bit mpmath, over the argument ranges of the column solve and beyond."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+mp = pytest.importorskip("mpmath")
+from oracle import oracle as orc  # noqa: E402
+
+mp.mp.prec = 200
+
+
+def _fn(name, nargs):
+    f = getattr(orc.lib(), name)
+    f.argtypes = [C.c_double] * nargs
+    f.restype = C.c_double
+    return f
+
+
+def ulp(x):
+    return math.ulp(abs(x)) if x != 0 else 5e-324
+
+
+def test_log_and_log10_accuracy():
+    rng = np.random.default_rng(1)
+    xs = np.concatenate([10 ** rng.uniform(-300, 300, 3000), rng.uniform(0.5, 2.0, 3000),
+                         1 + rng.uniform(-1e-6, 1e-6, 500), 10 ** rng.uniform(-7, 0, 2000),
+                         [5e-324, 1e-310, 2.2250738585072014e-308, 1.0, 2.0, 0.75, 1.5, 1.7976931348623157e308]])
+    flog, flog10 = _fn("orc_cm_log", 1), _fn("orc_cm_log10", 1)
+    worst = worst10 = 0.0
+    for x in xs:
+        x = float(x)
+        ref = mp.log(mp.mpf(x))
+        got = flog(x)
+        worst = max(worst, float(abs(mp.mpf(got) - ref)) / ulp(max(1.0, abs(float(ref)))))
+        ref10 = mp.log10(mp.mpf(x))
+        got10 = flog10(x)
+        worst10 = max(worst10, float(abs(mp.mpf(got10) - ref10)) / ulp(max(1.0, abs(float(ref10)))))
+    assert worst < 2.0, worst
+    assert worst10 < 2.5, worst10
+    assert flog(1.0) == 0.0 and flog10(1.0) == 0.0
+    assert flog(0.0) == -math.inf and math.isnan(flog(-1.0)) and flog(math.inf) == math.inf
+
+
+def test_exp_accuracy():
+    rng = np.random.default_rng(2)
+    xs = np.concatenate([rng.uniform(-745, 709.7, 4000), rng.uniform(-1, 1, 2000), [0.0, 1e-300, -1e-300,
+                                                                                    709.78, -708.4, -744.0]])
+    fexp = _fn("orc_cm_exp", 1)
+    worst = 0.0
+    for x in xs:
+        x = float(x)
+        ref = mp.exp(mp.mpf(x))
+        got = fexp(x)
+        if float(ref) < 2.2250738585072014e-308:      # subnormal results: absolute
+            assert abs(mp.mpf(got) - ref) <= 5e-324
+            continue
+        worst = max(worst, float(abs(mp.mpf(got) - ref) / ref) / (2.0 ** -52))
+    assert worst < 2.0, worst
+    assert fexp(710.0) == math.inf and fexp(-746.0) == 0.0 and fexp(0.0) == 1.0
+
+
+@pytest.mark.parametrize("xr,yr", [((0.01, 1.0), (5.0, 45.0)),      # s^(2b+3)
+                                   ((0.01, 1.0), (-20.0, -2.0)),    # s^(-b)
+                                   ((0.57, 0.57), (0.0, 0.95)),     # TKWAT^(fl*watsat)
+                                   ((2.29, 2.29), (0.0, 0.95)),     # TKICE^((1-fl)*watsat)
+                                   ((10.0, 10.0), (-6.0, 0.0)),     # ice impedance
+                                   ((1.0, 1e7), (-0.5, -0.04)),     # supercool (smp/sucsat)^(-1/b)
+                                   ((1e-3, 1e3), (-60.0, 60.0))])
+def test_pow_accuracy(xr, yr):
+    rng = np.random.default_rng(int(xr[0] * 100 + yr[0] * 7) & 0xffff)
+    fpow = _fn("orc_cm_pow", 2)
+    xs = rng.uniform(*xr, 1500) if xr[0] != xr[1] else np.full(1500, xr[0])
+    ys = rng.uniform(*yr, 1500)
+    for x, y in zip(xs, ys):
+        x, y = float(x), float(y)
+        ref = mp.power(mp.mpf(x), mp.mpf(y))
+        got = fpow(x, y)
+        err_ulp = float(abs(mp.mpf(got) - ref) / ref) / (2.0 ** -52)
+        bound = 3.0 + abs(y) + abs(y * math.log(x))
+        assert err_ulp < bound, (x, y, err_ulp, bound)
+
+
+def test_pow_special_values():
+    fpow = _fn("orc_cm_pow", 2)
+    assert fpow(2.0, 0.0) == 1.0 and fpow(1.0, 1e300) == 1.0 and fpow(math.nan, 0.0) == 1.0
+    assert fpow(0.0, 2.0) == 0.0 and fpow(0.0, -1.0) == math.inf
+    assert math.isnan(fpow(-2.0, 0.5)) and fpow(-2.0, 3.0) == pytest.approx(-8.0, rel=1e-15)
+    assert fpow(math.inf, 2.0) == math.inf and fpow(math.inf, -2.0) == 0.0
