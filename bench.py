@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--schedule", type=int, default=None, help="CLMGB_OPT_STEP_SCHEDULE override")
+    ap.add_argument("--queue-bps", type=int, default=None, help="CLMGB_OPT_QUEUE_BLOCKS_PER_SM override")
     return ap.parse_args()
 
 
@@ -188,6 +190,10 @@ def run_ours(args):
     st = wl.state
     nc = st.nc
     h = api.Handle(st.vp)
+    if args.schedule is not None:
+        h.set_option(abi.OPT_STEP_SCHEDULE, args.schedule)
+    if args.queue_bps is not None:
+        h.set_option(abi.OPT_QUEUE_BLOCKS_PER_SM, args.queue_bps)
     d = st.to_device()
     # per-step forcing, resident in HBM before the timed region
     Gd = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")
@@ -289,7 +295,10 @@ def run_ours(args):
                 "config": {"workload": WORKLOAD, "nc_per_gpu": nc, "dtime": wl.dtime, "variant": "plain FP64",
                            "l2": "inputs larger than L2 (state %.2f GB per GPU)" % (sum(
                                v.numel() * v.element_size() for v in d.arrays.values()) / 1e9),
-                           "device_status": status, "parallelism": "replicas over disjoint column shards"},
+                           "device_status": status, "parallelism": "replicas over disjoint column shards",
+                           "schedule": h.get_option(abi.OPT_STEP_SCHEDULE),
+                           "queue_blocks_per_sm": h.get_option(abi.OPT_QUEUE_BLOCKS_PER_SM),
+                           "queue_occupancy": h.get_option(abi.OPT_QUEUE_OCCUPANCY)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": 2 * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)

@@ -1,0 +1,132 @@
+# CLMGB300Ext — CLM.jl package extension that routes the soil/snow column solve of
+# CuArray-backed state to the GB300 kernels in libclmgb.so (include/clmgb.h).
+#
+# Untested in this build environment (no Julia); it is written to the C header's
+# struct member order, which tests/test_abi.py pins for the Python mirror.
+module CLMGB300Ext
+
+using CLM
+using CUDA
+
+const lib = get(ENV, "CLMGB_LIB", "libclmgb.so")
+
+struct Varpar
+    nlevsno::Int32; nlevgrnd::Int32; nlevsoi::Int32; nlevurb::Int32; nlevmaxurbgrnd::Int32; reserved::Int32
+end
+struct Bounds
+    nc::Int64; np::Int64; nl::Int64; ldc::Int64; ldp::Int64
+end
+struct SwmConfig
+    soilwater_movement_method::Int32; upper_boundary_condition::Int32
+    lower_boundary_condition::Int32; flux_calculation::Int32
+    dtmin::Float64; verySmall::Float64; xTolerUpper::Float64; xTolerLower::Float64; e_ice::Float64
+end
+
+ptr(x::CuArray) = reinterpret(Ptr{Cvoid}, pointer(x))
+strerror(rc) = unsafe_string(ccall((:clmgb_strerror, lib), Cstring, (Int32,), rc))
+check(rc, what) = rc == 0 || error(what, ": ", strerror(rc))
+
+const HANDLE = Ref{Ptr{Cvoid}}(C_NULL)
+function handle()
+    if HANDLE[] == C_NULL
+        vp = Varpar(CLM.varpar.nlevsno, CLM.varpar.nlevgrnd, CLM.varpar.nlevsoi,
+                    CLM.varpar.nlevurb, CLM.varpar.nlevmaxurbgrnd, 0)
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:clmgb_create, lib), Int32, (Ref{Varpar}, Ref{Ptr{Cvoid}}), vp, h), "clmgb_create")
+        HANDLE[] = h[]
+    end
+    HANDLE[]
+end
+
+# clmgb_soiltemp_fields: struct_size followed by the pointers, in header order.
+function soiltemp_fields(col, lun, patch, temp, ef, ss, wsb, wdb, wfb, sa, cs, forc_lwrad,
+                         mask_nolakec, mask_nolakep)
+    p = Ptr{Cvoid}[
+        ptr(mask_nolakec), ptr(mask_nolakep), ptr(col.snl), ptr(col.nbedrock), ptr(col.itype),
+        ptr(col.landunit), ptr(col.patchi), ptr(col.patchf), ptr(lun.itype), ptr(lun.urbpoi),
+        ptr(patch.column), ptr(patch.landunit), ptr(patch.wtcol), ptr(cs.frac_veg_nosno_patch),
+        ptr(col.dz), ptr(col.z), ptr(col.zi),
+        ptr(temp.t_soisno_col), ptr(temp.t_h2osfc_col), ptr(temp.t_grnd_col), ptr(temp.xmf_col),
+        ptr(temp.xmf_h2osfc_col), ptr(temp.fact_col), ptr(temp.c_h2osfc_col), ptr(temp.imelt_col),
+        ptr(temp.emg_col),
+        ptr(ef.htvp_col), ptr(ef.eflx_bot_col), ptr(ef.eflx_fgr12_col), ptr(ef.eflx_fgr_col),
+        ptr(ef.eflx_snomelt_col), ptr(ef.eflx_snomelt_r_col), ptr(ef.eflx_snomelt_u_col),
+        ptr(ef.eflx_h2osfc_to_snow_col), ptr(ef.eflx_gnet_patch), ptr(ef.dgnetdT_patch),
+        ptr(ef.dlrad_patch), ptr(ef.cgrnd_patch), ptr(ef.eflx_sh_grnd_patch), ptr(ef.eflx_sh_snow_patch),
+        ptr(ef.eflx_sh_soil_patch), ptr(ef.eflx_sh_h2osfc_patch),
+        ptr(ss.watsat_col), ptr(ss.bsw_col), ptr(ss.sucsat_col), ptr(ss.tkmg_col), ptr(ss.tkdry_col),
+        ptr(ss.csol_col), ptr(ss.thk_col),
+        ptr(wsb.ws.h2osoi_liq_col), ptr(wsb.ws.h2osoi_ice_col), ptr(wsb.ws.excess_ice_col),
+        ptr(wsb.ws.h2osno_no_layers_col), ptr(wsb.ws.h2osfc_col), ptr(wsb.int_snow_col),
+        ptr(wdb.frac_sno_eff_col), ptr(wdb.frac_h2osfc_col), ptr(wdb.snow_depth_col), ptr(wdb.bw_col),
+        ptr(wdb.exice_subs_col), ptr(wdb.snomelt_accum_col),
+        ptr(wfb.wf.qflx_evap_soi_patch), ptr(wfb.qflx_ev_snow_patch), ptr(wfb.qflx_ev_soil_patch),
+        ptr(wfb.qflx_ev_h2osfc_patch), ptr(wfb.wf.qflx_snomelt_col), ptr(wfb.wf.qflx_snofrz_col),
+        ptr(wfb.wf.qflx_snow_drain_col), ptr(wfb.wf.qflx_h2osfc_to_ice_col),
+        ptr(wfb.wf.qflx_snomelt_lyr_col), ptr(wfb.wf.qflx_snofrz_lyr_col),
+        ptr(sa.sabg_patch), ptr(sa.sabg_soil_patch), ptr(sa.sabg_snow_patch), ptr(sa.sabg_lyr_patch),
+        ptr(sa.sabg_chk_patch), ptr(forc_lwrad)]
+    buf = Vector{UInt8}(undef, 8 * (1 + length(p)))
+    GC.@preserve buf begin
+        unsafe_store!(Ptr{Int64}(pointer(buf)), Int64(length(buf)))
+        for (i, q) in enumerate(p)
+            unsafe_store!(Ptr{Ptr{Cvoid}}(pointer(buf) + 8i), q)
+        end
+    end
+    buf
+end
+
+function CLM.soil_temperature!(col::CLM.ColumnData{<:Any,<:CuArray}, lun, patch, temp, ef, ss, wsb, wdb,
+                               wfb, sa, cs, up, tbmax, forc_lwrad, mask_nolakec, mask_nolakep,
+                               mask_urbanl, mask_urbanc, bounds_col, bounds_lun, bounds_patch, dtime;
+                               urbantv_p_ac = nothing)
+    f = soiltemp_fields(col, lun, patch, temp, ef, ss, wsb, wdb, wfb, sa, cs, forc_lwrad,
+                        mask_nolakec, mask_nolakep)
+    b = Bounds(length(bounds_col), length(bounds_patch), length(bounds_lun),
+               size(temp.t_soisno_col, 1), size(sa.sabg_lyr_patch, 1))
+    snow = CLM.varctl.snow_thermal_cond_method == "Jordan1991" ? Int32(1) :
+           CLM.varctl.snow_thermal_cond_method == "Sturm1997" ? Int32(2) :
+           error("Unknown snow_thermal_cond_method")
+    GC.@preserve f begin
+        check(ccall((:clmgb_soil_temperature, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Float64, Int32, Int32, Ptr{UInt32}, Ptr{Cvoid}),
+                    handle(), b, f, dtime, snow, Int32(CLM.varctl.use_excess_ice), C_NULL,
+                    CUDA.stream().handle), "clmgb_soil_temperature")
+    end
+    nothing
+end
+
+function soilwater_fields(col, mask_hydrology, sh, ss, wfb, wsb)
+    p = Ptr{Cvoid}[ptr(mask_hydrology), ptr(col.nbedrock), ptr(col.dz), ptr(col.z), ptr(col.zi),
+                   ptr(wsb.ws.h2osoi_liq_col), ptr(wsb.ws.h2osoi_ice_col), ptr(wsb.ws.excess_ice_col),
+                   ptr(ss.watsat_col), ptr(ss.hksat_col), ptr(ss.bsw_col), ptr(ss.sucsat_col),
+                   ptr(ss.eff_porosity_col), ptr(sh.icefrac_col), ptr(ss.smp_l_col), ptr(ss.hk_l_col),
+                   ptr(wfb.qflx_rootsoi_col), ptr(wfb.wf.qflx_infl_col), ptr(sh.zwt_col),
+                   ptr(sh.qcharge_col), ptr(sh.num_substeps_col)]
+    buf = Vector{UInt8}(undef, 8 * (1 + length(p)))
+    GC.@preserve buf begin
+        unsafe_store!(Ptr{Int64}(pointer(buf)), Int64(length(buf)))
+        for (i, q) in enumerate(p)
+            unsafe_store!(Ptr{Ptr{Cvoid}}(pointer(buf) + 8i), q)
+        end
+    end
+    buf
+end
+
+function CLM.soil_water!(col::CLM.ColumnData{<:Any,<:CuArray}, mask_hydrology, mask_urban, sh, ss, wfb,
+                         wsb, temp, cs, ef, swrc, cfg::CLM.SoilWaterMovementConfig, dtime;
+                         use_flexibleCN::Bool = false)
+    use_flexibleCN && error("use_flexibleCN is not implemented by the GB300 path")
+    c = SwmConfig(cfg.soilwater_movement_method, cfg.upper_boundary_condition, cfg.lower_boundary_condition,
+                  cfg.flux_calculation, cfg.dtmin, cfg.verySmall, cfg.xTolerUpper, cfg.xTolerLower, cfg.e_ice)
+    f = soilwater_fields(col, mask_hydrology, sh, ss, wfb, wsb)
+    b = Bounds(length(mask_hydrology), 0, 0, size(col.dz, 1), 0)
+    GC.@preserve f begin
+        check(ccall((:clmgb_soil_water, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Ptr{UInt32}, Ptr{Cvoid}),
+                    handle(), b, f, c, dtime, C_NULL, CUDA.stream().handle), "clmgb_soil_water")
+    end
+    nothing
+end
+
+end # module
