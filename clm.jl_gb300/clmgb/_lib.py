@@ -32,6 +32,7 @@ _SIGS = {
     "clmgb_set_option": ([P, I32, I64], I32),
     "clmgb_get_option": ([P, I32, P], I32),
     "clmgb_math_eval": ([P, I32, I64, P, P, P, P], I32),
+    "clmgb_soil_water_noalloc": ([P, P, P, P, F64, P, P], I32),
 }
 
 

@@ -51,6 +51,8 @@ OPT_QUEUE_BLOCKS_PER_SM = 2
 OPT_QUEUE_OCCUPANCY = 3
 OPT_NUM_SMS = 4
 
+CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20
+
 MAX_NLEVSNO = 12
 MAX_NLEVGRND = 25
 MAX_NLEVSOI = 25

@@ -42,6 +42,9 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
                                        int grid_blocks, cudaStream_t s);
+cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                      const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
+                                      cudaStream_t s);
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s);
 
 }  // namespace clmgb

@@ -297,6 +297,22 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b,
                           double* t_ssbef, double* t_h2osfc_bef,
                           uint32_t* col_status, void* stream);
 
+/* soil_water! (moisture form) for callers that cannot allocate GPU memory (a host
+ * runtime that owns the device memory pool, code inside stream capture, allocator-free
+ * embedded callers).  No counterpart in the reference: it is the same solve as
+ * clmgb_soil_water, without a handle.  It calls no cudaMalloc/cudaFree; its scratch
+ * is a static device array of 16 bytes plus 4 bytes per column that every GPU
+ * loading this library keeps until exit, so nc is limited to
+ * CLMGB_NOALLOC_MAX_COLUMNS (larger -> CLMGB_ERR_DIMS).  All calls share that array:
+ * calls that overlap on the GPU race, so issue them in order on one stream.  The
+ * first call on a device looks up the array's address; make it before any stream
+ * capture.  col_status (optional, device [nc]) receives the per-column status; there
+ * is no accumulated device status word. */
+#define CLMGB_NOALLOC_MAX_COLUMNS (1 << 20)
+int32_t clmgb_soil_water_noalloc(const clmgb_varpar* vp, const clmgb_bounds* b,
+                                 const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
+                                 double dtime, uint32_t* col_status, void* stream);
+
 /* ---- component entry points (the reference exposes these functions too) ---- */
 
 /* phase_change_h2osfc! (soil_temperature.jl:1857) and phase_change_beta!
