@@ -3,8 +3,10 @@
 Workload (default): 262,144 synthetic columns, snl 60% 0 / 40% 1..12, dtime 3600 s,
 diurnal ground heat flux and Bernoulli(0.1) infiltration pulses (the 262,144-column
 scale/roofline workload).  One step = the synthetic forcing update + soil_temperature!
-+ set_soil_water_fractions! + soil_water! (moisture form) over every column, as one
-fused FP64 kernel launch through the C ABI.  The state (~1.6 GB) is far larger than
++ set_soil_water_fractions! + soil_water! (moisture form) over every column, through
+the C ABI (clmgb_column_step: a soil-temperature kernel and the work-queue Richards
+kernel, schedule chosen by the autotuner before timing).  The same sequence is also
+replayed as one captured CUDA graph ("graph" in the output line).  The state (~1.6 GB) is far larger than
 L2 (129 MB), so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -48,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", type=int, default=None, help="CLMGB_OPT_STEP_SCHEDULE override")
     ap.add_argument("--queue-bps", type=int, default=None, help="CLMGB_OPT_QUEUE_BLOCKS_PER_SM override")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
     return ap.parse_args()
 
 
@@ -203,12 +207,19 @@ def run_ours(args):
         Gd[t].copy_(torch.from_numpy(g))
         Id[t].copy_(torch.from_numpy(i))
     stream = torch.cuda.current_stream()
+    tune = None
+    if not args.no_autotune and args.schedule is None and args.queue_bps is None:
+        from clmgb import autotune
+        tune = autotune.tune_column_step(h, d, wl.dtime, cfg, Gd, Id, steps=2, warm=1)
 
     def step(t, ev=None):
+        # one timestep through the drop-in entry points, in the driver's order
         api.synth_forcing(h, d, Gd[t], Id[t], stream=stream)
+        api.soil_temperature(h, d, wl.dtime, stream=stream)
+        api.set_soil_water_fractions(h, d, stream=stream)
         if ev is not None:
             ev[0].record(stream)
-        api.column_step(h, d, wl.dtime, cfg, stream=stream)
+        api.soil_water(h, d, wl.dtime, cfg, stream=stream)
         if ev is not None:
             ev[1].record(stream)
 
@@ -235,24 +246,47 @@ def run_ours(args):
     elapsed_ms = t_start.elapsed_time(t_end)
     kern_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
     status = h.device_status()
+    graph = None
+    if not args.no_graph:
+        # the same timestep sequence captured once as a CUDA graph and replayed
+        from clmgb import autotune
+        gsteps = min(args.steps, nsteps - args.warmup)
+        g = autotune.capture_steps(h, d, wl.dtime, Gd, Id, gsteps, first_step=args.warmup, cfg=cfg)
+        g.replay()
+        torch.cuda.synchronize()
+        g0 = torch.cuda.Event(enable_timing=True)
+        g1 = torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        g.replay()
+        g1.record(stream)
+        torch.cuda.synchronize()
+        gms = g0.elapsed_time(g1)
+        graph = {"steps": gsteps, "ms_per_step": gms / gsteps,
+                 "value": gsteps * nc * world / (gms / 1000.0), "launches_per_step": 2,
+                 "note": "clmgb_column_step (fused entry) replayed from one captured graph"}
+        del g
     if world > 1:
         t = torch.tensor([elapsed_ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed_ms = float(t.item())
     value = args.steps * nc * world / (elapsed_ms / 1000.0)
 
-    # roofline of the dominant kernel (the fused column step)
-    snl = st["col_snl"]
-    bytes_launch = bytes_model.bytes_per_step(snl, st.vp.nlevgrnd, st.vp.nlevsoi)
+    # roofline of the dominant kernel: the work-queue Richards solve (soil_water!)
+    bytes_launch = bytes_model.richards_bytes_per_call(nc, st.vp.nlevsoi)
     peak, peak_kind = measured_peaks()
     achieved = bytes_launch / (kern_ms / 1000.0) / 1e9
     tr = profile_traffic()
     traffic = None
-    if tr and tr.get("bytes_per_column_step"):
-        traffic = tr["bytes_per_column_step"] * nc
+    if tr and tr.get("k_moisture_form_queue_bytes_per_column"):
+        traffic = tr["k_moisture_form_queue_bytes_per_column"] * nc
+    step_bytes = bytes_model.bytes_per_step(st["col_snl"], st.vp.nlevgrnd, st.vp.nlevsoi)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_column_step",
-                "kernel_ms": kern_ms, "algorithmic_bytes_per_launch": bytes_launch}
+                "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_moisture_form_queue",
+                "kernel_ms": kern_ms, "kernel_share_of_step": kern_ms / (elapsed_ms / args.steps),
+                "algorithmic_bytes_per_launch": bytes_launch,
+                "step_algorithmic_bytes": step_bytes,
+                "step_achieved_gbs": step_bytes / (elapsed_ms / args.steps / 1000.0) / 1e9,
+                "note": "FP64-pipe bound on GB300 (1.19 TFLOP/s measured DFMA); see profiles/"}
 
     # end to end through the C ABI with host buffers: H2D of the state each step,
     # the step, D2H of every field the step writes
@@ -299,8 +333,8 @@ def run_ours(args):
                            "schedule": h.get_option(abi.OPT_STEP_SCHEDULE),
                            "queue_blocks_per_sm": h.get_option(abi.OPT_QUEUE_BLOCKS_PER_SM),
                            "queue_occupancy": h.get_option(abi.OPT_QUEUE_OCCUPANCY)},
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": 2 * args.steps, "clocks": clocks}
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "graph": graph, "autotune": tune,
+                "gpu_launches": 4 * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)
     h.close()
     if world > 1:

@@ -34,3 +34,15 @@ def bytes_per_step(snl, nlevgrnd=25, nlevsoi=20):
     """Total algorithmic bytes of one timestep over all columns (snl <= 0 per column)."""
     nsnow = -np.asarray(snl, dtype=np.int64)
     return int(np.sum(bytes_per_column_step(nsnow, nlevgrnd, nlevsoi)))
+
+
+# The moisture-form Richards kernel alone (soilwm_moisture_form_solve!), per column:
+# per active layer read h2osoi_liq, dz, z, watsat, bsw, sucsat, hksat, qflx_rootsoi,
+# icefrac (9 words) and write h2osoi_liq, smp_l, hk_l (3 words); per column mask,
+# nbedrock, qflx_infl, qcharge, num_substeps (5 words).
+RICHARDS_WORDS_PER_LAYER = 12
+RICHARDS_COLUMN_WORDS = 5
+
+
+def richards_bytes_per_call(nc, nlevsoi=20):
+    return int(WORD * nc * (RICHARDS_WORDS_PER_LAYER * nlevsoi + RICHARDS_COLUMN_WORDS))

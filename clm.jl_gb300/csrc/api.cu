@@ -33,6 +33,12 @@ struct clmgb_handle_s {
 };
 
 static const uint32_t HANDLE_MAGIC = 0xC1A9B300u;
+// Resident 128-thread blocks per SM of the work-queue kernel when not tuned: fewer
+// resident warps give every lane more columns to balance over, and the FP64 pipe
+// (about 1.9 FMA/clk/SM) stays busy with a handful of warps.  Measured on GB300 at
+// 262,144 columns: 1 -> 6.8, 2 -> 7.9, 3 -> 7.5, 4 -> 7.2, occupancy limit -> 5.2
+// M column-steps/s.
+static const int64_t CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM = 2;
 
 using clmgb::Dims;
 
@@ -139,7 +145,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->vp = *vp;
   h->last_error = cudaSuccess;
   h->step_schedule = CLMGB_SCHEDULE_QUEUE;
-  h->queue_blocks_per_sm = 0;
+  h->queue_blocks_per_sm = CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM;
   h->scratch = nullptr;
   cudaError_t ce = cudaGetDevice(&h->device);
   if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);

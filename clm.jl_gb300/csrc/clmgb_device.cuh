@@ -53,20 +53,30 @@ struct Dims {
   int64_t ldc, ldp, np;
 };
 
-// Julia Base.max / Base.min on Float64 (NaN propagates, -0.0 < 0.0).
+// Julia Base.max / Base.min on Float64 (NaN propagates, -0.0 < 0.0).  They only
+// select one argument, so they are done on the integer pipes: the bit pattern
+// mapped to a two's-complement key orders doubles exactly (-0.0 below +0.0), and
+// NaN is recognised from its bits.  No FP64 instruction is spent on them.
+__device__ __forceinline__ long long ord_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool isnan_bits(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
 __device__ __forceinline__ double jl_max(double x, double y) {
-  if (x != x) return x;
-  if (y != y) return y;
-  if (x > y) return x;
-  if (y > x) return y;
-  return signbit(x) ? y : x;
+  if (isnan_bits(x)) return x;
+  if (isnan_bits(y)) return y;
+  return ord_key(x) >= ord_key(y) ? x : y;
 }
 __device__ __forceinline__ double jl_min(double x, double y) {
-  if (x != x) return x;
-  if (y != y) return y;
-  if (x < y) return x;
-  if (y < x) return y;
-  return signbit(x) ? x : y;
+  if (isnan_bits(x)) return x;
+  if (isnan_bits(y)) return y;
+  return ord_key(x) <= ord_key(y) ? x : y;
+}
+// |x| < t for a positive threshold t, on the integer pipes (false for NaN, as in IEEE).
+__device__ __forceinline__ bool abs_lt(double x, double t) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) < __double_as_longlong(t);
 }
 // Julia's Float64 x^4 (Base.Math.pow_body, compensated squaring).
 __device__ __forceinline__ double jl_pow4(double x) {
@@ -938,7 +948,7 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
     const double rmx = -L.fnet1[1] * L.dt_dz[1];
     const double bmx = -1.0 - (-L.dqidw1[1] + L.dqodw1[1]) * L.dt_dz[1];
     bet = bmx;
-    if (fabs(bet) < 1.0e-30) bet = 1.0e-30;
+    if (abs_lt(bet, 1.0e-30)) bet = 1.0e-30;
     dwat_prev = rmx / bet;
     L.dwat[1] = dwat_prev;
   }
@@ -950,7 +960,7 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
     const double rmx = -L.fnet1[j] * L.dt_dz[j];
     L.gam[j] = cmx_prev / bet;
     bet = bmx - amx * L.gam[j];
-    if (fabs(bet) < 1.0e-30) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
+    if (abs_lt(bet, 1.0e-30)) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
     dwat_prev = (rmx - amx * dwat_prev) / bet;
     L.dwat[j] = dwat_prev;
     cmx_prev = cmx;
