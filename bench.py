@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--schedule", type=int, default=None, help="CLMGB_OPT_STEP_SCHEDULE override")
     ap.add_argument("--queue-bps", type=int, default=None, help="CLMGB_OPT_QUEUE_BLOCKS_PER_SM override")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-reserve", action="store_true", help="run without clmgb_reserve scratch")
+    ap.add_argument("--queue-order", type=int, default=None)
     ap.add_argument("--no-graph", action="store_true")
     return ap.parse_args()
 
@@ -194,10 +196,14 @@ def run_ours(args):
     st = wl.state
     nc = st.nc
     h = api.Handle(st.vp)
+    if not args.no_reserve:
+        h.reserve(nc)
     if args.schedule is not None:
         h.set_option(abi.OPT_STEP_SCHEDULE, args.schedule)
     if args.queue_bps is not None:
         h.set_option(abi.OPT_QUEUE_BLOCKS_PER_SM, args.queue_bps)
+    if args.queue_order is not None:
+        h.set_option(abi.OPT_QUEUE_ORDER, args.queue_order)
     d = st.to_device()
     # per-step forcing, resident in HBM before the timed region
     Gd = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")
@@ -332,7 +338,9 @@ def run_ours(args):
                            "device_status": status, "parallelism": "replicas over disjoint column shards",
                            "schedule": h.get_option(abi.OPT_STEP_SCHEDULE),
                            "queue_blocks_per_sm": h.get_option(abi.OPT_QUEUE_BLOCKS_PER_SM),
-                           "queue_occupancy": h.get_option(abi.OPT_QUEUE_OCCUPANCY)},
+                           "queue_occupancy": h.get_option(abi.OPT_QUEUE_OCCUPANCY),
+                           "reserved_columns": h.get_option(abi.OPT_RESERVED_COLUMNS),
+                           "queue_order": h.get_option(abi.OPT_QUEUE_ORDER)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "graph": graph, "autotune": tune,
                 "gpu_launches": 4 * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)

@@ -30,6 +30,7 @@ _SIGS = {
     "clmgb_batched_band_solve": ([P, I64, I64, I32, P, P, P, P, P, P, I32, I32, I32, P], I32),
     "clmgb_tridiagonal_multi": ([P, I64, I64, I32, P, P, P, P, P, P, P, P], I32),
     "clmgb_set_option": ([P, I32, I64], I32),
+    "clmgb_reserve": ([P, I64], I32),
     "clmgb_get_option": ([P, I32, P], I32),
     "clmgb_math_eval": ([P, I32, I64, P, P, P, P], I32),
     "clmgb_soil_water_noalloc": ([P, P, P, P, F64, P, P], I32),

@@ -50,6 +50,8 @@ SCHEDULE_QUEUE = 1
 OPT_QUEUE_BLOCKS_PER_SM = 2
 OPT_QUEUE_OCCUPANCY = 3
 OPT_NUM_SMS = 4
+OPT_QUEUE_ORDER = 5
+OPT_RESERVED_COLUMNS = 6
 
 CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20
 

@@ -58,6 +58,10 @@ class Handle:
     def set_option(self, key, value):
         check(self.lib.clmgb_set_option(self.h, key, int(value)), "clmgb_set_option")
 
+    def reserve(self, max_nc):
+        """Per-column scratch for up to max_nc columns (impedance pre-pass, queue order)."""
+        check(self.lib.clmgb_reserve(self.h, int(max_nc)), "clmgb_reserve")
+
     def get_option(self, key):
         v = C.c_int64(0)
         check(self.lib.clmgb_get_option(self.h, key, C.byref(v)), "clmgb_get_option")

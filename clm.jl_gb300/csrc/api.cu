@@ -29,6 +29,10 @@ struct clmgb_handle_s {
   int64_t step_schedule;        // CLMGB_OPT_STEP_SCHEDULE
   int64_t queue_blocks_per_sm;  // CLMGB_OPT_QUEUE_BLOCKS_PER_SM (0 = occupancy limit)
   int occupancy_blocks;         // occupancy limit of the queue kernel
+  int64_t queue_order;          // CLMGB_OPT_QUEUE_ORDER
+  // per-column scratch from clmgb_reserve (one allocation)
+  void* reserve_block;
+  clmgb::QueueScratch qs;
   cudaError_t last_error;
 };
 
@@ -107,6 +111,12 @@ static int32_t check_cfg(const clmgb_swm_config* cfg) {
   return CLMGB_OK;
 }
 
+static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
+  clmgb::QueueScratch q = h->qs;
+  q.longest_first = h->queue_order == 1 ? 1 : 0;
+  return q;
+}
+
 static int queue_grid(clmgb_handle h) {
   int per_sm = h->queue_blocks_per_sm > 0 ? (int)h->queue_blocks_per_sm : h->occupancy_blocks;
   if (per_sm > h->occupancy_blocks) per_sm = h->occupancy_blocks;
@@ -147,6 +157,13 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->step_schedule = CLMGB_SCHEDULE_QUEUE;
   h->queue_blocks_per_sm = CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM;
   h->scratch = nullptr;
+  h->queue_order = 1;
+  h->reserve_block = nullptr;
+  h->qs.capacity = 0;
+  h->qs.imp = nullptr;
+  h->qs.order = nullptr;
+  h->qs.bins = nullptr;
+  h->qs.longest_first = 1;
   cudaError_t ce = cudaGetDevice(&h->device);
   if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   if (ce == cudaSuccess) ce = cudaMalloc(&h->scratch, 2 * sizeof(unsigned long long));
@@ -168,6 +185,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
 int32_t clmgb_destroy(clmgb_handle h) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   cudaFree(h->scratch);
+  if (h->reserve_block) cudaFree(h->reserve_block);
   h->magic = 0;
   delete h;
   return CLMGB_OK;
@@ -233,7 +251,8 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soil
                                      (cudaStream_t)stream);
   else
     ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
-                                           h->dev_status, h->queue, queue_grid(h), (cudaStream_t)stream);
+                                           h->dev_status, h->queue, queue_grid(h), queue_scratch(h),
+                                           (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -261,7 +280,7 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
                                           col_status, h->dev_status, s);
     if (ce == cudaSuccess)
       ce = clmgb::launch_moisture_form_queue(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->queue,
-                                             queue_grid(h), s);
+                                             queue_grid(h), queue_scratch(h), s);
   }
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -317,6 +336,28 @@ int32_t clmgb_batched_band_solve(clmgb_handle h, int64_t nc, int64_t ldc, int32_
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (max_nc < 0 || max_nc > 0xffffffffLL) return CLMGB_ERR_DIMS;
+  if (max_nc <= h->qs.capacity) return CLMGB_OK;
+  const size_t nsoi = (size_t)h->vp.nlevsoi;
+  const size_t imp_bytes = nsoi * (size_t)max_nc * sizeof(double);
+  const size_t order_bytes = ((size_t)max_nc * sizeof(uint32_t) + 255) & ~(size_t)255;
+  const size_t bins_bytes = 256 * sizeof(unsigned int);
+  void* blk = nullptr;
+  cudaError_t ce = cudaDeviceSynchronize();
+  if (ce == cudaSuccess) ce = cudaMalloc(&blk, imp_bytes + order_bytes + bins_bytes);
+  if (ce != cudaSuccess) return cuda_fail(h, ce);
+  if (h->reserve_block) cudaFree(h->reserve_block);
+  h->reserve_block = blk;
+  char* p = static_cast<char*>(blk);
+  h->qs.imp = reinterpret_cast<double*>(p);
+  h->qs.order = reinterpret_cast<uint32_t*>(p + imp_bytes);
+  h->qs.bins = reinterpret_cast<unsigned int*>(p + imp_bytes + order_bytes);
+  h->qs.capacity = max_nc;
+  return CLMGB_OK;
+}
+
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   switch (key) {
@@ -327,6 +368,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
     case CLMGB_OPT_QUEUE_BLOCKS_PER_SM:
       if (value < 0) return CLMGB_ERR_CONFIG;
       h->queue_blocks_per_sm = value;
+      return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_ORDER:
+      if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
+      h->queue_order = value;
       return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
@@ -341,6 +386,8 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_QUEUE_BLOCKS_PER_SM: *value = h->queue_blocks_per_sm; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_OCCUPANCY: *value = h->occupancy_blocks; return CLMGB_OK;
     case CLMGB_OPT_NUM_SMS: *value = h->num_sms; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_ORDER: *value = h->queue_order; return CLMGB_OK;
+    case CLMGB_OPT_RESERVED_COLUMNS: *value = h->qs.capacity; return CLMGB_OK;
     default: return CLMGB_ERR_CONFIG;
   }
 }

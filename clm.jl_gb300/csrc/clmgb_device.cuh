@@ -800,9 +800,20 @@ struct MfLane {
   double gam[MAXSOI + 1], dwat[MAXSOI + 1], dt_dz[MAXSOI + 1];
 };
 
-// returns false (and sets L.status) when the column cannot be solved
+// Ice impedance 10^(-e_ice*icefrac) of layer j (interface mean above the bottom
+// layer), as formed at soil_water_movement.jl:1287-1293.
+__device__ __forceinline__ double mf_impedance(const Dims& D, const clmgb_soilwater_fields& f, double e_ice,
+                                               int64_t c, int j, int nlayers) {
+  const int64_t ld = D.ldc;
+  if (j == nlayers) return cm_pow(10.0, -e_ice * LV(f.icefrac, c, j, ld));
+  return cm_pow(10.0, -e_ice * (0.5 * (LV(f.icefrac, c, j, ld) + LV(f.icefrac, c, j + 1, ld))));
+}
+
+// returns false (and sets L.status) when the column cannot be solved.  imp_cache,
+// when given, holds the impedances formed by k_impedance ([nlevsoi, ld_imp]).
 __device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
-                                         const clmgb_swm_config& cfg, double dtime, int64_t c) {
+                                         const clmgb_swm_config& cfg, double dtime, int64_t c,
+                                         const double* imp_cache = nullptr, int64_t ld_imp = 0) {
   const int64_t ld = D.ldc;
   const int joff = D.nlevsno;
   L.c = c;
@@ -818,10 +829,10 @@ __device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_s
     L.liq[j] = LV(f.h2osoi_liq, c, joff + j, ld);
     L.dzv[j] = LVc(f.dz, c, joff + j, ld);
   }
-  const double e_ice = cfg.e_ice;
-  for (int j = 1; j <= nlayers; j++) {
-    if (j == nlayers) L.imp[j] = cm_pow(10.0, -e_ice * LV(f.icefrac, c, j, ld));
-    else L.imp[j] = cm_pow(10.0, -e_ice * (0.5 * (LV(f.icefrac, c, j, ld) + LV(f.icefrac, c, j + 1, ld))));
+  if (imp_cache) {
+    for (int j = 1; j <= nlayers; j++) L.imp[j] = imp_cache[(int64_t)(j - 1) * ld_imp + c];
+  } else {
+    for (int j = 1; j <= nlayers; j++) L.imp[j] = mf_impedance(D, f, cfg.e_ice, c, j, nlayers);
   }
   L.nsub = 0;
   L.dtsub = dtime;

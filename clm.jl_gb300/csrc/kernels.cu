@@ -88,14 +88,20 @@ k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb
 // Each lane owns one column at a time and advances it one substep attempt per loop
 // trip; when its column finishes it takes the next column index from the queue
 // (one atomicAdd per warp for all lanes that need work).  Columns need from 1 to
-// ~50 attempts, so lanes stay busy instead of waiting for the slowest column of
-// the warp.  The per-column arithmetic is unchanged, so results do not depend on
-// the schedule.  `queue` must be zero at launch.
+// ~70 attempts, so lanes stay busy instead of waiting for the slowest column of
+// the warp.  With `order` the queue hands out columns in that order (longest
+// expected first) and the impedances come precomputed in imp_cache.  The
+// per-column arithmetic is unchanged, so results do not depend on the schedule.
+// `queue` must be zero at launch.
 __global__ void __launch_bounds__(BLOCK)
 k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
-                      uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue) {
+                      uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
+                      const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
+                      int64_t ld_imp) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  const unsigned long long nq = order ? (unsigned long long)(*(volatile const unsigned int*)nlisted_ptr)
+                                      : (unsigned long long)nc;
   MfLane L;
   bool active = false, exhausted = false;
   for (;;) {
@@ -107,19 +113,22 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
       if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(m));
       base = __shfl_sync(FULL, base, leader);
       if (need) {
-        const int64_t c = (int64_t)(base + (unsigned long long)__popc(m & ((1u << lane) - 1u)));
-        if (c >= nc) {
+        const unsigned long long k = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+        if (k >= nq) {
           exhausted = true;
-        } else if (f.mask_hydrology[c]) {
-          if (mf_begin(L, D, f, cfg, dtime, c)) {
-            active = true;
-          } else {
-            const uint32_t st = L.status;
-            if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
-            if (st && dev_status) atomicOr(dev_status, st);
+        } else {
+          const int64_t c = order ? (int64_t)order[k] : (int64_t)k;
+          if (order || f.mask_hydrology[c]) {
+            if (mf_begin(L, D, f, cfg, dtime, c, imp_cache, ld_imp)) {
+              active = true;
+            } else {
+              const uint32_t st = L.status;
+              if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
+              if (st && dev_status) atomicOr(dev_status, st);
+            }
+          } else if (col_status && !or_status) {
+            col_status[c] = 0;
           }
-        } else if (col_status && !or_status) {
-          col_status[c] = 0;
         }
       }
     }
@@ -134,6 +143,62 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
       active = false;
     }
   }
+}
+
+// Ice impedances of every hydrology column, one thread per column, into imp_cache
+// [nlevsoi, ld_imp] (uniform work: no lane waits on another column).
+__global__ void __launch_bounds__(BLOCK)
+k_impedance(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* imp_cache, int64_t ld_imp) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc || !f.mask_hydrology[c]) return;
+  const int64_t nl = f.col_nbedrock[c];
+  if (nl < 1 || nl > D.nlevsoi) return;
+  const int nlayers = (int)nl;
+  for (int j = 1; j <= nlayers; j++) imp_cache[(int64_t)(j - 1) * ld_imp + c] = mf_impedance(D, f, e_ice, c, j, nlayers);
+}
+
+// Longest-expected-first order of the hydrology columns: counting sort on the
+// previous call's substep count (num_substeps, the state field), descending.
+// Bins 0..63; NaN or non-positive counts go to bin 0.  The order within a bin is
+// arbitrary and does not affect any result.
+constexpr int ORDER_BINS = 64;
+__device__ __forceinline__ int order_bin(double ns) {
+  if (!(ns > 0.0)) return 0;
+  return ns >= (double)(ORDER_BINS - 1) ? ORDER_BINS - 1 : (int)ns;
+}
+__global__ void __launch_bounds__(BLOCK)
+k_order_hist(int64_t nc, const uint8_t* mask, const double* num_substeps, unsigned int* bins) {
+  __shared__ unsigned int sh[ORDER_BINS];
+  for (int i = threadIdx.x; i < ORDER_BINS; i += BLOCK) sh[i] = 0;
+  __syncthreads();
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c < nc && mask[c]) atomicAdd(&sh[order_bin(num_substeps[c])], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < ORDER_BINS; i += BLOCK)
+    if (sh[i]) atomicAdd(&bins[i], sh[i]);
+}
+// bins[0..63] counts -> bins[64+b] start offset of bin b (descending bins first),
+// bins[128] = total listed
+__global__ void k_order_scan(unsigned int* bins) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned int run = 0;
+  for (int b = ORDER_BINS - 1; b >= 0; b--) {
+    bins[ORDER_BINS + b] = run;
+    run += bins[b];
+  }
+  bins[2 * ORDER_BINS] = run;
+}
+__global__ void __launch_bounds__(BLOCK)
+k_order_scatter(int64_t nc, const uint8_t* mask, const double* num_substeps, unsigned int* bins, uint32_t* order,
+                uint32_t* col_status, int or_status) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  if (!mask[c]) {
+    if (col_status && !or_status) col_status[c] = 0;
+    return;
+  }
+  const unsigned int slot = atomicAdd(&bins[ORDER_BINS + order_bin(num_substeps[c])], 1u);
+  order[slot] = (uint32_t)c;
 }
 
 // Evaluates the shared transcendentals (clm_math.h) elementwise; op 0 log, 1 exp,
@@ -286,13 +351,29 @@ int queue_blocks_per_sm() {
 cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
-                                       int grid_blocks, cudaStream_t s) {
+                                       int grid_blocks, const QueueScratch& qs, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
+  const bool use = qs.capacity >= nc && qs.order && qs.bins && qs.imp;
+  if (use) {
+    k_impedance<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg.e_ice, qs.imp, qs.capacity);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (qs.longest_first) {
+      if ((e = cudaMemsetAsync(qs.bins, 0, (2 * ORDER_BINS + 1) * sizeof(unsigned int), s)) != cudaSuccess) return e;
+      k_order_hist<<<grid_for(nc), BLOCK, 0, s>>>(nc, f.mask_hydrology, f.num_substeps, qs.bins);
+      k_order_scan<<<1, 32, 0, s>>>(qs.bins);
+      k_order_scatter<<<grid_for(nc), BLOCK, 0, s>>>(nc, f.mask_hydrology, f.num_substeps, qs.bins, qs.order,
+                                                     col_status, or_status);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+  }
   const int64_t need = (nc + BLOCK - 1) / BLOCK;
   const int grid = (int)(need < grid_blocks ? need : grid_blocks);
-  k_moisture_form_queue<<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
-                                                              dev_status, queue);
+  const bool listed = use && qs.longest_first;
+  k_moisture_form_queue<<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status,
+                                                              queue, listed ? qs.order : nullptr,
+                                                              listed ? qs.bins + 2 * ORDER_BINS : nullptr,
+                                                              use ? qs.imp : nullptr, use ? qs.capacity : 0);
   return cudaGetLastError();
 }
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {

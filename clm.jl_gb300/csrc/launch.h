@@ -9,6 +9,17 @@ namespace clmgb {
 
 struct Dims;
 
+// Per-column scratch of a handle reserved with clmgb_reserve (capacity columns):
+// precomputed ice impedances [nlevsoi, capacity], the work-queue order and its
+// counting-sort bins (2*64+1 words).
+struct QueueScratch {
+  int64_t capacity;
+  double* imp;
+  uint32_t* order;
+  unsigned int* bins;
+  int longest_first;
+};
+
 // All launchers return the cudaError_t of the launch (cudaGetLastError()).
 cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
                                     int snow_method, uint32_t* col_status, uint32_t* dev_status,
@@ -41,7 +52,7 @@ int queue_blocks_per_sm();
 cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
-                                       int grid_blocks, cudaStream_t s);
+                                       int grid_blocks, const QueueScratch& qs, cudaStream_t s);
 cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                       cudaStream_t s);

@@ -255,23 +255,31 @@ def test_moisture_form_conserves_mass_gpu(handle_factory):
     assert not bad, rep
 
 
+@pytest.mark.parametrize("reserved", [False, True])
 @pytest.mark.parametrize("lower_bc", [abi.BC_ZERO_FLUX, abi.BC_FLUX, abi.BC_WATERTABLE])
 @pytest.mark.parametrize("cfg_id", [0, 2])
-def test_soil_water_workloads(handle_factory, cfg_id, lower_bc):
+def test_soil_water_workloads(cfg_id, lower_bc, reserved):
     wl = synth.make_workload(cfg_id, nc=4096)
     st = wl.state
     cfg = abi.SwmConfig.clm5_default()
     cfg.lower_boundary_condition = lower_bc
     orc.soil_water_fractions(st)
     st["zwt"][:] = np.linspace(0.5, 9.0, st.nc)
+    st["num_substeps"][:] = np.arange(st.nc) % 9     # a previous-call history for the queue order
+    st["mask_hydrology"][::11] = 0
     ref = st.copy()
     orc.soil_water(ref, wl.dtime, cfg)
     d = st.to_device()
-    h = handle_factory(st.vp)
-    api.soil_water(h, d, wl.dtime, cfg)
+    h = api.Handle(st.vp)
+    if reserved:
+        h.reserve(st.nc)
+    status = torch.full((st.nc,), 5, dtype=torch.int32, device="cuda")
+    api.soil_water(h, d, wl.dtime, cfg, col_status=status)
     got = d.to_host()
+    h.close()
     rep, bad = compare(got, ref, fields=["h2osoi_liq", "smp_l", "hk_l", "qcharge", "num_substeps"])
-    assert len(bad) <= max(1, st.nc // 1000), (len(bad), rep)
+    assert not bad, (len(bad), rep)
+    assert np.all(status.cpu().numpy() == 0)
 
 
 def test_soil_water_rejects_configs(handle_factory):
@@ -328,17 +336,20 @@ def test_math_bit_identical_to_cpu_build(handle_factory, op):
 
 # ---------------------------------------------------------------- multi-step column step
 # ---------------------------------------------------------------- multi-step column step
-@pytest.mark.parametrize("schedule", [abi.SCHEDULE_QUEUE, abi.SCHEDULE_FUSED])
+@pytest.mark.parametrize("mode", ["queue", "queue_reserved", "fused"])
 @pytest.mark.parametrize("cfg_id,nc,nsteps", [(0, 1024, 48), (1, 4096, 48), (2, 4096, 24)])
-def test_column_step_multistep_vs_oracle(handle_factory, cfg_id, nc, nsteps, schedule):
+def test_column_step_multistep_vs_oracle(cfg_id, nc, nsteps, mode):
     wl = synth.make_workload(cfg_id, nc=nc)
     st = wl.state
     Gf, If = wl.forcing_block(range(nsteps))
     ref = st.copy()
     status_ref = orc.run_steps(ref, wl.dtime, Gf, If)
     d = st.to_device()
-    h = handle_factory(st.vp)
-    h.set_option(abi.OPT_STEP_SCHEDULE, schedule)
+    h = api.Handle(st.vp)       # own handle: reserve state must not leak into other tests
+    h.set_option(abi.OPT_STEP_SCHEDULE, abi.SCHEDULE_FUSED if mode == "fused" else abi.SCHEDULE_QUEUE)
+    if mode == "queue_reserved":
+        h.reserve(nc)
+        assert h.get_option(abi.OPT_RESERVED_COLUMNS) == nc
     Gd, Id = _dev(Gf), _dev(If)
     for t in range(nsteps):
         api.synth_forcing(h, d, Gd[t], Id[t])
@@ -346,7 +357,7 @@ def test_column_step_multistep_vs_oracle(handle_factory, cfg_id, nc, nsteps, sch
     torch.cuda.synchronize()
     assert h.device_status() == 0
     assert np.all(status_ref == 0)
-    h.set_option(abi.OPT_STEP_SCHEDULE, abi.SCHEDULE_QUEUE)
+    h.close()
     got = d.to_host()
     rep, bad = compare(got, ref)
     assert not bad, (len(bad), rep)
