@@ -47,11 +47,14 @@ ZENGDECKER_2009, MOISTURE_FORM = 0, 1
 OPT_STEP_SCHEDULE = 1
 SCHEDULE_FUSED = 0
 SCHEDULE_QUEUE = 1
+SCHEDULE_WAVES = 2
 OPT_QUEUE_BLOCKS_PER_SM = 2
 OPT_QUEUE_OCCUPANCY = 3
 OPT_NUM_SMS = 4
 OPT_QUEUE_ORDER = 5
 OPT_RESERVED_COLUMNS = 6
+OPT_WAVES_BLOCKS_PER_SM = 7
+OPT_WAVES_OCCUPANCY = 8
 
 CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20
 

@@ -6,7 +6,8 @@ every candidate does the same work) and leaves the fastest one set on the handle
   * CLMGB_SCHEDULE_QUEUE with 1..4 resident 128-thread blocks per SM of the
     work-queue Richards kernel (fewer resident warps give each lane more columns to
     balance over; more warps hide more latency);
-  * CLMGB_SCHEDULE_FUSED (one column per thread, whole step in one kernel).
+  * CLMGB_SCHEDULE_FUSED (one column per thread, whole step in one kernel);
+  * CLMGB_SCHEDULE_WAVES (all columns in synchronous rounds; needs clmgb_reserve).
 
 Results never depend on the choice: the per-column arithmetic is the same in every
 schedule, only the order in which columns are visited changes.
@@ -16,7 +17,7 @@ import torch
 from . import abi, api
 
 DEFAULT_CANDIDATES = [(abi.SCHEDULE_QUEUE, 1), (abi.SCHEDULE_QUEUE, 2), (abi.SCHEDULE_QUEUE, 3),
-                      (abi.SCHEDULE_QUEUE, 4), (abi.SCHEDULE_FUSED, 0)]
+                      (abi.SCHEDULE_QUEUE, 4), (abi.SCHEDULE_FUSED, 0), (abi.SCHEDULE_WAVES, 0)]
 
 
 def tune_column_step(handle, state, dtime, cfg=None, G=None, I=None, candidates=None, steps=2, warm=1,

@@ -33,6 +33,9 @@ struct clmgb_handle_s {
   // per-column scratch from clmgb_reserve (one allocation)
   void* reserve_block;
   clmgb::QueueScratch qs;
+  clmgb::WaveScratch ws;
+  int waves_blocks;             // co-resident blocks per SM of the wave kernel (0 = cannot launch)
+  int64_t waves_blocks_per_sm;  // CLMGB_OPT_WAVES_BLOCKS_PER_SM (0 = all co-resident)
   cudaError_t last_error;
 };
 
@@ -117,6 +120,15 @@ static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
   return q;
 }
 
+static bool use_waves(clmgb_handle h, int64_t nc) {
+  return h->step_schedule == CLMGB_SCHEDULE_WAVES && h->waves_blocks > 0 && h->ws.cap >= nc;
+}
+static int waves_grid(clmgb_handle h) {
+  int per_sm = h->waves_blocks_per_sm > 0 ? (int)h->waves_blocks_per_sm : h->waves_blocks;
+  if (per_sm > h->waves_blocks) per_sm = h->waves_blocks;
+  return per_sm * h->num_sms;
+}
+
 static int queue_grid(clmgb_handle h) {
   int per_sm = h->queue_blocks_per_sm > 0 ? (int)h->queue_blocks_per_sm : h->occupancy_blocks;
   if (per_sm > h->occupancy_blocks) per_sm = h->occupancy_blocks;
@@ -164,6 +176,9 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->qs.order = nullptr;
   h->qs.bins = nullptr;
   h->qs.longest_first = 1;
+  memset(&h->ws, 0, sizeof(h->ws));
+  h->waves_blocks = 0;
+  h->waves_blocks_per_sm = 0;
   cudaError_t ce = cudaGetDevice(&h->device);
   if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   if (ce == cudaSuccess) ce = cudaMalloc(&h->scratch, 2 * sizeof(unsigned long long));
@@ -172,6 +187,9 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
     h->dev_status = reinterpret_cast<uint32_t*>(h->scratch);
     h->queue = h->scratch + 1;
     h->occupancy_blocks = clmgb::queue_blocks_per_sm();
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device);
+    h->waves_blocks = coop ? clmgb::waves_blocks_per_sm() : 0;
   }
   if (ce != cudaSuccess) {
     h->magic = 0;
@@ -249,6 +267,9 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soil
   if (h->step_schedule == CLMGB_SCHEDULE_FUSED)
     ce = clmgb::launch_moisture_form(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, h->dev_status,
                                      (cudaStream_t)stream);
+  else if (use_waves(h, b->nc))
+    ce = clmgb::launch_moisture_form_waves(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
+                                           h->dev_status, h->ws, waves_grid(h), (cudaStream_t)stream);
   else
     ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
                                            h->dev_status, h->queue, queue_grid(h), queue_scratch(h),
@@ -278,9 +299,14 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   } else {
     ce = clmgb::launch_soiltemp_fractions(D, b->nc, *ft, *fw, dtime, snow_method, t_ssbef, t_h2osfc_bef,
                                           col_status, h->dev_status, s);
-    if (ce == cudaSuccess)
-      ce = clmgb::launch_moisture_form_queue(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->queue,
-                                             queue_grid(h), queue_scratch(h), s);
+    if (ce == cudaSuccess) {
+      if (use_waves(h, b->nc))
+        ce = clmgb::launch_moisture_form_waves(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->ws,
+                                               waves_grid(h), s);
+      else
+        ce = clmgb::launch_moisture_form_queue(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->queue,
+                                               queue_grid(h), queue_scratch(h), s);
+    }
   }
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -340,20 +366,45 @@ int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (max_nc < 0 || max_nc > 0xffffffffLL) return CLMGB_ERR_DIMS;
   if (max_nc <= h->qs.capacity) return CLMGB_OK;
+  const size_t n = (size_t)max_nc;
   const size_t nsoi = (size_t)h->vp.nlevsoi;
-  const size_t imp_bytes = nsoi * (size_t)max_nc * sizeof(double);
-  const size_t order_bytes = ((size_t)max_nc * sizeof(uint32_t) + 255) & ~(size_t)255;
-  const size_t bins_bytes = 256 * sizeof(unsigned int);
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t lev = al(nsoi * n * sizeof(double));   // one [nlevsoi][n] array
+  const size_t col8 = al(n * 8), col4 = al(n * 4);
+  // imp + 5 wave level arrays, 6 per-column doubles, nsub + status, order + 4 lists, bins
+  const size_t total = 6 * lev + 6 * col8 + 2 * col4 + 5 * col4 + al(256 * sizeof(unsigned int));
   void* blk = nullptr;
   cudaError_t ce = cudaDeviceSynchronize();
-  if (ce == cudaSuccess) ce = cudaMalloc(&blk, imp_bytes + order_bytes + bins_bytes);
+  if (ce == cudaSuccess) ce = cudaMalloc(&blk, total);
   if (ce != cudaSuccess) return cuda_fail(h, ce);
   if (h->reserve_block) cudaFree(h->reserve_block);
   h->reserve_block = blk;
   char* p = static_cast<char*>(blk);
-  h->qs.imp = reinterpret_cast<double*>(p);
-  h->qs.order = reinterpret_cast<uint32_t*>(p + imp_bytes);
-  h->qs.bins = reinterpret_cast<unsigned int*>(p + imp_bytes + order_bytes);
+  auto take = [&p](size_t b) { char* q = p; p += b; return q; };
+  clmgb::WaveScratch& w = h->ws;
+  w.cap = max_nc;
+  w.imp = reinterpret_cast<double*>(take(lev));
+  w.qout = reinterpret_cast<double*>(take(lev));
+  w.dqodw1 = reinterpret_cast<double*>(take(lev));
+  w.dqodw2 = reinterpret_cast<double*>(take(lev));
+  w.fnet1 = reinterpret_cast<double*>(take(lev));
+  w.dtdz = reinterpret_cast<double*>(take(lev));
+  w.dtsub = reinterpret_cast<double*>(take(col8));
+  w.dtdone = reinterpret_cast<double*>(take(col8));
+  w.qc = reinterpret_cast<double*>(take(col8));
+  w.dtcur = reinterpret_cast<double*>(take(col8));
+  w.hk_bot = reinterpret_cast<double*>(take(col8));
+  w.dhkdw_bot = reinterpret_cast<double*>(take(col8));
+  w.nsub = reinterpret_cast<int*>(take(col4));
+  w.status = reinterpret_cast<uint32_t*>(take(col4));
+  h->qs.order = reinterpret_cast<uint32_t*>(take(col4));
+  w.listA[0] = reinterpret_cast<uint32_t*>(take(col4));
+  w.listA[1] = reinterpret_cast<uint32_t*>(take(col4));
+  w.listH[0] = reinterpret_cast<uint32_t*>(take(col4));
+  w.listH[1] = reinterpret_cast<uint32_t*>(take(col4));
+  h->qs.bins = reinterpret_cast<unsigned int*>(take(al(256 * sizeof(unsigned int))));
+  w.counters = h->qs.bins + 192;   // bins use words 0..128
+  h->qs.imp = w.imp;
   h->qs.capacity = max_nc;
   return CLMGB_OK;
 }
@@ -362,7 +413,8 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   switch (key) {
     case CLMGB_OPT_STEP_SCHEDULE:
-      if (value != CLMGB_SCHEDULE_FUSED && value != CLMGB_SCHEDULE_QUEUE) return CLMGB_ERR_CONFIG;
+      if (value != CLMGB_SCHEDULE_FUSED && value != CLMGB_SCHEDULE_QUEUE && value != CLMGB_SCHEDULE_WAVES)
+        return CLMGB_ERR_CONFIG;
       h->step_schedule = value;
       return CLMGB_OK;
     case CLMGB_OPT_QUEUE_BLOCKS_PER_SM:
@@ -372,6 +424,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
     case CLMGB_OPT_QUEUE_ORDER:
       if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
       h->queue_order = value;
+      return CLMGB_OK;
+    case CLMGB_OPT_WAVES_BLOCKS_PER_SM:
+      if (value < 0) return CLMGB_ERR_CONFIG;
+      h->waves_blocks_per_sm = value;
       return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
@@ -388,6 +444,8 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_NUM_SMS: *value = h->num_sms; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_ORDER: *value = h->queue_order; return CLMGB_OK;
     case CLMGB_OPT_RESERVED_COLUMNS: *value = h->qs.capacity; return CLMGB_OK;
+    case CLMGB_OPT_WAVES_BLOCKS_PER_SM: *value = h->waves_blocks_per_sm; return CLMGB_OK;
+    case CLMGB_OPT_WAVES_OCCUPANCY: *value = h->waves_blocks; return CLMGB_OK;
     default: return CLMGB_ERR_CONFIG;
   }
 }

@@ -20,6 +20,19 @@ struct QueueScratch {
   int longest_first;
 };
 
+// Per-column state of the wave-synchronous Richards solve (richards_waves.cu), from
+// the same reserved block: level arrays are [nlevsoi][cap], the rest [cap].
+struct WaveScratch {
+  int64_t cap;
+  double *imp, *qout, *dqodw1, *dqodw2, *fnet1, *dtdz;
+  double *dtsub, *dtdone, *qc, *dtcur, *hk_bot, *dhkdw_bot;
+  int* nsub;
+  uint32_t* status;
+  uint32_t* listA[2];
+  uint32_t* listH[2];
+  unsigned int* counters;
+};
+
 // All launchers return the cudaError_t of the launch (cudaGetLastError()).
 cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
                                     int snow_method, uint32_t* col_status, uint32_t* dev_status,
@@ -56,6 +69,11 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
 cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                       cudaStream_t s);
+int waves_blocks_per_sm();
+cudaError_t launch_moisture_form_waves(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
+                                       int or_status, uint32_t* dev_status, const WaveScratch& w, int grid_blocks,
+                                       cudaStream_t s);
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s);
 
 }  // namespace clmgb

@@ -252,16 +252,21 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
 #define CLMGB_OPT_STEP_SCHEDULE        1  /* how the Richards solve is scheduled: */
 #define   CLMGB_SCHEDULE_FUSED         0  /*   one column per thread, whole step in one kernel */
 #define   CLMGB_SCHEDULE_QUEUE         1  /*   persistent kernel fed by a device work queue (default) */
+#define   CLMGB_SCHEDULE_WAVES         2  /*   cooperative kernel, all columns in synchronous rounds of
+                                              uniform phases (needs clmgb_reserve; otherwise QUEUE runs) */
 #define CLMGB_OPT_QUEUE_BLOCKS_PER_SM  2  /* resident blocks per SM of the queue kernel (0 = occupancy limit) */
 #define CLMGB_OPT_QUEUE_OCCUPANCY      3  /* read-only: occupancy limit of the queue kernel */
 #define CLMGB_OPT_NUM_SMS              4  /* read-only: SMs of the handle's device */
 #define CLMGB_OPT_QUEUE_ORDER          5  /* with reserved scratch: 1 = hand out columns longest-expected-first
                                              (by the previous call's num_substeps, default), 0 = index order */
 #define CLMGB_OPT_RESERVED_COLUMNS     6  /* read-only: columns covered by clmgb_reserve */
+#define CLMGB_OPT_WAVES_BLOCKS_PER_SM  7  /* co-resident blocks per SM of the wave kernel (0 = occupancy limit) */
+#define CLMGB_OPT_WAVES_OCCUPANCY      8  /* read-only: occupancy limit of the wave kernel (0 = unavailable) */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
-/* Gives the handle per-column scratch for up to max_nc columns (8*nlevsoi + 4 bytes
- * per column): the Richards solve then forms the ice impedances in a uniform
- * pre-pass and hands out columns longest-expected-first.  Calls with more columns
+/* Gives the handle per-column scratch for up to max_nc columns (about 48*nlevsoi + 80
+ * bytes per column): the Richards solve then forms the ice impedances in a uniform
+ * pre-pass and hands out columns longest-expected-first, and the WAVES schedule
+ * becomes available.  Calls with more columns
  * than reserved run without it.  Synchronises the device; call it at set-up, not
  * inside stream capture. */
 int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc);

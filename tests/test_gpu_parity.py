@@ -255,10 +255,10 @@ def test_moisture_form_conserves_mass_gpu(handle_factory):
     assert not bad, rep
 
 
-@pytest.mark.parametrize("reserved", [False, True])
+@pytest.mark.parametrize("schedule", ["queue", "queue_reserved", "waves"])
 @pytest.mark.parametrize("lower_bc", [abi.BC_ZERO_FLUX, abi.BC_FLUX, abi.BC_WATERTABLE])
 @pytest.mark.parametrize("cfg_id", [0, 2])
-def test_soil_water_workloads(cfg_id, lower_bc, reserved):
+def test_soil_water_workloads(cfg_id, lower_bc, schedule):
     wl = synth.make_workload(cfg_id, nc=4096)
     st = wl.state
     cfg = abi.SwmConfig.clm5_default()
@@ -271,8 +271,10 @@ def test_soil_water_workloads(cfg_id, lower_bc, reserved):
     orc.soil_water(ref, wl.dtime, cfg)
     d = st.to_device()
     h = api.Handle(st.vp)
-    if reserved:
+    if schedule != "queue":
         h.reserve(st.nc)
+    if schedule == "waves":
+        h.set_option(abi.OPT_STEP_SCHEDULE, abi.SCHEDULE_WAVES)
     status = torch.full((st.nc,), 5, dtype=torch.int32, device="cuda")
     api.soil_water(h, d, wl.dtime, cfg, col_status=status)
     got = d.to_host()
@@ -336,7 +338,7 @@ def test_math_bit_identical_to_cpu_build(handle_factory, op):
 
 # ---------------------------------------------------------------- multi-step column step
 # ---------------------------------------------------------------- multi-step column step
-@pytest.mark.parametrize("mode", ["queue", "queue_reserved", "fused"])
+@pytest.mark.parametrize("mode", ["queue", "queue_reserved", "waves", "fused"])
 @pytest.mark.parametrize("cfg_id,nc,nsteps", [(0, 1024, 48), (1, 4096, 48), (2, 4096, 24)])
 def test_column_step_multistep_vs_oracle(cfg_id, nc, nsteps, mode):
     wl = synth.make_workload(cfg_id, nc=nc)
@@ -346,8 +348,11 @@ def test_column_step_multistep_vs_oracle(cfg_id, nc, nsteps, mode):
     status_ref = orc.run_steps(ref, wl.dtime, Gf, If)
     d = st.to_device()
     h = api.Handle(st.vp)       # own handle: reserve state must not leak into other tests
-    h.set_option(abi.OPT_STEP_SCHEDULE, abi.SCHEDULE_FUSED if mode == "fused" else abi.SCHEDULE_QUEUE)
-    if mode == "queue_reserved":
+    h.set_option(abi.OPT_STEP_SCHEDULE, {"fused": abi.SCHEDULE_FUSED, "waves": abi.SCHEDULE_WAVES}.get(
+        mode, abi.SCHEDULE_QUEUE))
+    if mode == "waves":
+        assert h.get_option(abi.OPT_WAVES_OCCUPANCY) > 0
+    if mode in ("queue_reserved", "waves"):
         h.reserve(nc)
         assert h.get_option(abi.OPT_RESERVED_COLUMNS) == nc
     Gd, Id = _dev(Gf), _dev(If)
