@@ -281,13 +281,15 @@ def run_ours(args):
     bytes_launch = bytes_model.richards_bytes_per_call(nc, st.vp.nlevsoi)
     peak, peak_kind = measured_peaks()
     achieved = bytes_launch / (kern_ms / 1000.0) / 1e9
+    kname = {abi.SCHEDULE_FUSED: "k_moisture_form", abi.SCHEDULE_QUEUE: "k_moisture_form_queue",
+             abi.SCHEDULE_WAVES: "k_moisture_form_waves"}[h.get_option(abi.OPT_STEP_SCHEDULE)]
     tr = profile_traffic()
     traffic = None
-    if tr and tr.get("k_moisture_form_queue_bytes_per_column"):
-        traffic = tr["k_moisture_form_queue_bytes_per_column"] * nc
+    if tr and tr.get(kname + "_bytes_per_column"):
+        traffic = tr[kname + "_bytes_per_column"] * nc
     step_bytes = bytes_model.bytes_per_step(st["col_snl"], st.vp.nlevgrnd, st.vp.nlevsoi)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_moisture_form_queue",
+                "traffic": traffic, "peak_kind": peak_kind, "kernel": kname,
                 "kernel_ms": kern_ms, "kernel_share_of_step": kern_ms / (elapsed_ms / args.steps),
                 "algorithmic_bytes_per_launch": bytes_launch,
                 "step_algorithmic_bytes": step_bytes,

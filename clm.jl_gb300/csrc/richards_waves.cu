@@ -6,14 +6,14 @@
 // of the hydraulic properties and fluxes.  Run one column per thread, the lanes of a
 // warp disagree about which of the two they need and idle through the other.
 //
-// Here one cooperative persistent kernel advances all columns together in rounds.
-// Each round has two phases separated by grid-wide barriers:
-//   H: hydraulic properties, fluxes and flux derivatives for every column that
-//      starts a new substep (all columns in round 0, then those that accepted);
-//   A: one attempt for every unfinished column; accepted columns update their
-//      water, finished ones write their outputs, and the others are appended to
-//      the next round's lists (compacted with one atomic per warp).
-// Every thread in a phase does the same work, so lanes never wait on each other.
+// Here one cooperative persistent kernel advances all columns together in rounds
+// separated by grid-wide barriers.  In a round every unfinished column makes one
+// attempt; the columns that start a new substep (all in round 0, then those that
+// accepted in the previous round) first evaluate the hydraulic properties, fluxes
+// and flux derivatives.  The round's work list holds those columns first and the
+// rejected ones after them, and warps take 32 consecutive entries at a time, so the
+// lanes of a warp run the same code.  Outcomes are appended to the next round's
+// two lists with one atomic per warp.
 // The per-column state between phases lives in the handle's reserved scratch,
 // level-major ([level][column]) for coalesced access.  The arithmetic is the same
 // expressions in the same order as the one-column-per-thread form (clmgb_device.cuh),
@@ -263,15 +263,20 @@ __device__ __forceinline__ uint32_t wave_finish(const Dims& D, const clmgb_soilw
   return st;
 }
 
-// counters: [0],[1] A-list lengths of the two buffers, [2],[3] H-list lengths
+// counters: three sets of {length of the "hydraulics then attempt" list, length of the
+// "attempt only" list, chunk counter}.  Round r reads set r%3, appends into set
+// (r+1)%3 and clears set (r+2)%3, which no thread touches during round r (it was
+// last read before the barrier that ended round r-1).  The lists are double buffered.
 __global__ void __launch_bounds__(WAVE_BLOCK)
 k_moisture_form_waves(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                       uint32_t* col_status, int or_status, uint32_t* dev_status, WaveScratch w) {
   cg::grid_group grid = cg::this_grid();
   const int64_t nthr = (int64_t)gridDim.x * WAVE_BLOCK;
   const int64_t tid = (int64_t)blockIdx.x * WAVE_BLOCK + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
   volatile unsigned int* cnt = w.counters;
-  // round 0 set-up: impedances, per-column scalars, all columns in both lists
+  // set-up: impedances, per-column scalars; every column starts with hydraulics
   for (int64_t base = 0; base < nc; base += nthr) {
     const int64_t c = base + tid;
     bool take = false;
@@ -297,25 +302,37 @@ k_moisture_form_waves(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
         }
       }
     }
-    append(w.listA[0], w.counters + 0, take, (uint32_t)c);
-    append(w.listH[0], w.counters + 2, take, (uint32_t)c);
+    append(w.listH[0], w.counters + 0, take, (uint32_t)c);  // set 0, list 0
   }
   grid.sync();
-  int cur = 0;
+  int cur = 0;  // list buffer
+  int cs = 0;   // counter set
   for (int round = 0; round <= MF_ATTEMPT_CAP + 1; round++) {
-    const unsigned int nA = cnt[cur], nH = cnt[2 + cur];
-    if (nA == 0) break;
-    // H phase
-    for (int64_t i = tid; i < (int64_t)nH; i += nthr) wave_hydraulics(D, f, cfg, w, (int64_t)__ldcg(&w.listH[cur][i]));
-    grid.sync();
-    // A phase
+    const unsigned int nHA = cnt[3 * cs], nA = cnt[3 * cs + 1];
+    const unsigned int total = nHA + nA;
+    if (total == 0) break;
     const int nxt = cur ^ 1;
-    for (int64_t base = 0; base < (int64_t)nA; base += nthr) {
-      const int64_t i = base + tid;
+    const int cn = cs == 2 ? 0 : cs + 1;
+    const int cc = cn == 2 ? 0 : cn + 1;
+    if (tid == 0) {
+      cnt[3 * cc] = 0;
+      cnt[3 * cc + 1] = 0;
+      cnt[3 * cc + 2] = 0;
+    }
+    // warps take 32 consecutive items: first the columns that need hydraulics, then
+    // the rest, so all lanes of a warp (but one) run the same code
+    for (;;) {
+      unsigned int base = 0;
+      if (lane == 0) base = atomicAdd(&w.counters[3 * cs + 2], 32u);
+      base = __shfl_sync(FULL, base, 0);
+      if (base >= total) break;
+      const unsigned int i = base + (unsigned int)lane;
       int r = -1;
       int64_t c = 0;
-      if (i < (int64_t)nA) {
-        c = (int64_t)__ldcg(&w.listA[cur][i]);
+      if (i < total) {
+        const bool needH = i < nHA;
+        c = (int64_t)(needH ? __ldcg(&w.listH[cur][i]) : __ldcg(&w.listA[cur][i - nHA]));
+        if (needH) wave_hydraulics(D, f, cfg, w, c);
         r = wave_attempt(D, f, cfg, dtime, w, c);
         if (r == WAVE_DONE) {
           const uint32_t st = wave_finish(D, f, w, c);
@@ -323,15 +340,12 @@ k_moisture_form_waves(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
           if (st && dev_status) atomicOr(dev_status, st);
         }
       }
-      append(w.listA[nxt], w.counters + nxt, r == WAVE_REJECT || r == WAVE_ACCEPT, (uint32_t)c);
-      append(w.listH[nxt], w.counters + 2 + nxt, r == WAVE_ACCEPT, (uint32_t)c);
+      append(w.listH[nxt], w.counters + 3 * cn, r == WAVE_ACCEPT, (uint32_t)c);
+      append(w.listA[nxt], w.counters + 3 * cn + 1, r == WAVE_REJECT, (uint32_t)c);
     }
     grid.sync();
-    if (tid == 0) {
-      cnt[cur] = 0;
-      cnt[2 + cur] = 0;
-    }
     cur = nxt;
+    cs = cn;
   }
 }
 
@@ -347,7 +361,7 @@ cudaError_t launch_moisture_form_waves(const Dims& D, int64_t nc, const clmgb_so
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, const WaveScratch& w, int grid_blocks,
                                        cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(w.counters, 0, 4 * sizeof(unsigned int), s);
+  cudaError_t e = cudaMemsetAsync(w.counters, 0, 9 * sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   Dims d = D;
   int64_t n = nc;
