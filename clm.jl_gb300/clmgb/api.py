@@ -8,6 +8,8 @@ Names and argument meaning follow the reference:
   phase_change_h2osfc / _beta       phase_change_*!          soil_temperature.jl:1857, 2232
   batched_band_solve(...)           batched_band_solve!      band_diagonal.jl:179
   tridiagonal_multi(...)            tridiagonal_multi!       tridiagonal.jl:129
+  batched_band_solve_factor / _adjoint   band_solve! reverse rule   enzyme_rules.jl:80-107
+  tridiagonal_adjoint(...)          tridiagonal_solve! reverse rule enzyme_rules.jl:160-201
 Configurations the reference rejects with error() raise CLMGBError.  Every call
 requires CUDA tensors; there is no CPU path.
 """
@@ -154,6 +156,37 @@ def tridiagonal_multi(handle, u, a, b, c, r, jtop, mask, stream=None):
     check(handle.lib.clmgb_tridiagonal_multi(handle.h, ncols, ncols, nlevs, _dptr(u), _dptr(a), _dptr(b),
                                              _dptr(c), _dptr(r), _dptr(jtop), _dptr(mask), _stream(stream)),
           "tridiagonal_multi")
+
+
+def batched_band_solve_factor(handle, tvector, bmatrix, rvector, jtop, jbot, mask, lu, piv, kl=2, ku=2,
+                              nlevsno_off=0, stream=None):
+    """batched_band_solve that also stores its factorisation: lu (nlev, 2*kl+ku+1, nc)
+    float64, piv (nlev, nc) uint8."""
+    nlev, nc = tvector.shape
+    check(handle.lib.clmgb_batched_band_solve_factor(handle.h, nc, nc, nlev, _dptr(tvector), _dptr(bmatrix),
+                                                     _dptr(rvector), _dptr(jtop), _dptr(jbot), _dptr(mask),
+                                                     kl, ku, nlevsno_off, _dptr(lu), _dptr(piv), _stream(stream)),
+          "batched_band_solve_factor")
+
+
+def batched_band_solve_adjoint(handle, tvector, tvector_bar, lu, piv, bmatrix_bar, rvector_bar, jtop, jbot, mask,
+                               kl=2, ku=2, nlevsno_off=0, stream=None):
+    """Reverse of batched_band_solve from the stored factors; bars accumulate (None = inactive)."""
+    nlev, nc = tvector.shape
+    check(handle.lib.clmgb_batched_band_solve_adjoint(handle.h, nc, nc, nlev, _dptr(tvector), _dptr(tvector_bar),
+                                                      _dptr(lu), _dptr(piv), _dptr(bmatrix_bar),
+                                                      _dptr(rvector_bar), _dptr(jtop), _dptr(jbot), _dptr(mask),
+                                                      kl, ku, nlevsno_off, _stream(stream)),
+          "batched_band_solve_adjoint")
+
+
+def tridiagonal_adjoint(handle, u, a, b, c, u_bar, a_bar, b_bar, c_bar, r_bar, jtop, mask, stream=None):
+    """tridiagonal_solve! reverse rule per column of (nlevs, ncols) tensors; bars accumulate."""
+    nlevs, ncols = u.shape
+    check(handle.lib.clmgb_tridiagonal_adjoint(handle.h, ncols, ncols, nlevs, _dptr(u), _dptr(a), _dptr(b),
+                                               _dptr(c), _dptr(u_bar), _dptr(a_bar), _dptr(b_bar), _dptr(c_bar),
+                                               _dptr(r_bar), _dptr(jtop), _dptr(mask), _stream(stream)),
+          "tridiagonal_adjoint")
 
 
 MATH_OPS = {"log": 0, "exp": 1, "pow": 2, "log10": 3}

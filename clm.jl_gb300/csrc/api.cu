@@ -472,4 +472,47 @@ int32_t clmgb_tridiagonal_multi(clmgb_handle h, int64_t ncols, int64_t ldc, int3
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_batched_band_solve_factor(clmgb_handle h, int64_t nc, int64_t ldc, int32_t nlev, double* tvector,
+                                        const double* bmatrix, const double* rvector, const int64_t* jtop,
+                                        const int64_t* jbot, const uint8_t* mask, int32_t kl, int32_t ku,
+                                        int32_t nlevsno_off, double* lu, uint8_t* piv, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (nc < 0 || ldc < nc || nlev < 1 || nlev > clmgb::MAXROWS + 1) return CLMGB_ERR_DIMS;
+  if (!((kl == 2 && ku == 2) || (kl == 1 && ku == 1))) return CLMGB_ERR_UNSUPPORTED;
+  if (nc == 0) return CLMGB_OK;
+  if (!tvector || !bmatrix || !rvector || !jtop || !jbot || !mask || !lu || !piv) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_band_factor_solve(nc, ldc, nlev, tvector, bmatrix, rvector, jtop, jbot, mask, kl,
+                                                   ku, nlevsno_off, lu, piv, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_batched_band_solve_adjoint(clmgb_handle h, int64_t nc, int64_t ldc, int32_t nlev,
+                                         const double* tvector, double* tvector_bar, const double* lu,
+                                         const uint8_t* piv, double* bmatrix_bar, double* rvector_bar,
+                                         const int64_t* jtop, const int64_t* jbot, const uint8_t* mask, int32_t kl,
+                                         int32_t ku, int32_t nlevsno_off, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (nc < 0 || ldc < nc || nlev < 1 || nlev > clmgb::MAXROWS + 1) return CLMGB_ERR_DIMS;
+  if (!((kl == 2 && ku == 2) || (kl == 1 && ku == 1))) return CLMGB_ERR_UNSUPPORTED;
+  if (nc == 0) return CLMGB_OK;
+  if (!tvector || !tvector_bar || !lu || !piv || !jtop || !jbot || !mask) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_band_solve_adjoint(nc, ldc, nlev, tvector, tvector_bar, lu, piv, bmatrix_bar,
+                                                    rvector_bar, jtop, jbot, mask, kl, ku, nlevsno_off,
+                                                    (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_tridiagonal_adjoint(clmgb_handle h, int64_t ncols, int64_t ldc, int32_t nlevs, const double* u,
+                                  const double* a, const double* b, const double* c, double* u_bar, double* a_bar,
+                                  double* b_bar, double* c_bar, double* r_bar, const int64_t* jtop,
+                                  const uint8_t* mask, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (ncols < 0 || ldc < ncols || nlevs < 1 || nlevs > 64) return CLMGB_ERR_DIMS;
+  if (ncols == 0) return CLMGB_OK;
+  if (!u || !a || !b || !c || !u_bar || !jtop || !mask) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_tridiagonal_adjoint(ncols, ldc, nlevs, u, a, b, c, u_bar, a_bar, b_bar, c_bar,
+                                                     r_bar, jtop, mask, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 }  // extern "C"

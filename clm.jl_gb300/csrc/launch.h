@@ -75,5 +75,17 @@ cudaError_t launch_moisture_form_waves(const Dims& D, int64_t nc, const clmgb_so
                                        int or_status, uint32_t* dev_status, const WaveScratch& w, int grid_blocks,
                                        cudaStream_t s);
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s);
+cudaError_t launch_band_factor_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const double* bmatrix,
+                                     const double* rvector, const int64_t* jtop, const int64_t* jbot,
+                                     const uint8_t* mask, int kl, int ku, int nlevsno_off, double* lu, uint8_t* piv,
+                                     cudaStream_t s);
+cudaError_t launch_band_solve_adjoint(int64_t nc, int64_t ldc, int nlev, const double* tvector, double* tbar,
+                                      const double* lu, const uint8_t* piv, double* bbar, double* rbar,
+                                      const int64_t* jtop, const int64_t* jbot, const uint8_t* mask, int kl, int ku,
+                                      int nlevsno_off, cudaStream_t s);
+cudaError_t launch_tridiagonal_adjoint(int64_t ncols, int64_t ldc, int nlevs, const double* u, const double* a,
+                                       const double* b, const double* c, double* ubar, double* abar, double* bbar,
+                                       double* cbar, double* rbar, const int64_t* jtop, const uint8_t* mask,
+                                       cudaStream_t s);
 
 }  // namespace clmgb

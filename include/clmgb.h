@@ -365,6 +365,41 @@ int32_t clmgb_tridiagonal_multi(clmgb_handle h, int64_t ncols, int64_t ldc, int3
                                 const double* r, const int64_t* jtop, const uint8_t* mask,
                                 void* stream);
 
+/* ---- reverse-mode rules of the solves (enzyme_rules.jl) ---- */
+
+/* The forward of batched_band_solve! that also keeps its factorisation for the
+ * reverse pass (the augmented primal of the band_solve! rule, enzyme_rules.jl:80-89).
+ * tvector is bit-identical to clmgb_batched_band_solve.  lu is [ldc, W, nlev] doubles,
+ * W = 2*kl+ku+1 (row i of a column's system, at level jt+i, holds A's factor entries
+ * U(i, i..i+kl+ku) and the multipliers of the eliminations it received); piv is
+ * [ldc, nlev] bytes (row exchange of elimination step k as an offset 0..kl). */
+int32_t clmgb_batched_band_solve_factor(clmgb_handle h, int64_t nc, int64_t ldc, int32_t nlev,
+                                        double* tvector, const double* bmatrix, const double* rvector,
+                                        const int64_t* jtop, const int64_t* jbot, const uint8_t* mask,
+                                        int32_t kl, int32_t ku, int32_t nlevsno_off, double* lu,
+                                        uint8_t* piv, void* stream);
+
+/* band_solve! reverse rule (enzyme_rules.jl:91-107) over the batched layout:
+ * A^T lambda = tvector_bar solved from the stored factors (LAPACK gbtrs 'T' order),
+ * rvector_bar += lambda, bmatrix_bar -= lambda x^T on the band entries the forward
+ * read, tvector_bar consumed (zeroed) over the solved rows.  bmatrix_bar and
+ * rvector_bar may be NULL (inactive). */
+int32_t clmgb_batched_band_solve_adjoint(clmgb_handle h, int64_t nc, int64_t ldc, int32_t nlev,
+                                         const double* tvector, double* tvector_bar, const double* lu,
+                                         const uint8_t* piv, double* bmatrix_bar, double* rvector_bar,
+                                         const int64_t* jtop, const int64_t* jbot, const uint8_t* mask,
+                                         int32_t kl, int32_t ku, int32_t nlevsno_off, void* stream);
+
+/* tridiagonal_solve! reverse rule (enzyme_rules.jl:160-201) per column of the
+ * [ldc, nlevs] layout, system jtop..nlevs: lambda = A^-T u_bar by the same Thomas
+ * sweep on the transposed bands, r_bar += lambda, b_bar -= lambda*u,
+ * a_bar[j] -= lambda[j]*u[j-1] (j > jtop), c_bar[j] -= lambda[j]*u[j+1] (j < nlevs),
+ * u_bar consumed.  a_bar, b_bar, c_bar, r_bar may be NULL (inactive). */
+int32_t clmgb_tridiagonal_adjoint(clmgb_handle h, int64_t ncols, int64_t ldc, int32_t nlevs,
+                                  const double* u, const double* a, const double* b, const double* c,
+                                  double* u_bar, double* a_bar, double* b_bar, double* c_bar,
+                                  double* r_bar, const int64_t* jtop, const uint8_t* mask, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -262,6 +262,166 @@ void orc_tridiagonal_col(double* u, const double* a, const double* b, const doub
 #undef V
 }
 
+/* ===================================================================== */
+/* Reverse-mode rules of the linear solves (enzyme_rules.jl)             */
+/* ===================================================================== */
+
+/* tridiagonal_solve! reverse rule (enzyme_rules.jl:160-201), arrays 1-based through
+ * 0-based pointers: lambda = A^-T ubar, solved with tridiagonal_solve! on the
+ * transposed bands over jtop..n (sub = c[j-1], diag = b[j], super = a[j+1]);
+ * rbar += lambda; bbar -= lambda*u; abar[j] -= lambda[j]*u[j-1] for j > jtop;
+ * cbar[j] -= lambda[j]*u[j+1] for j < n; ubar[jtop..n] is consumed (set to 0).
+ * abar, bbar, cbar, rbar may be NULL (inactive arguments). */
+void orc_tridiagonal_adjoint(const double* u, const double* a, const double* b, const double* c,
+                             double* ubar, double* abar, double* bbar, double* cbar, double* rbar,
+                             int32_t jtop, int32_t n)
+{
+  double aT[ORC_MAXL], bT[ORC_MAXL], cT[ORC_MAXL], rT[ORC_MAXL], lam[ORC_MAXL];
+  for (int j = 1; j <= n; j++) {
+    aT[j - 1] = 0.0; bT[j - 1] = 0.0; cT[j - 1] = 0.0; rT[j - 1] = 0.0; lam[j - 1] = 0.0;
+  }
+  for (int j = jtop; j <= n; j++) {
+    bT[j - 1] = b[j - 1];
+    rT[j - 1] = ubar[j - 1];
+    if (j > jtop) aT[j - 1] = c[j - 2];
+    if (j < n) cT[j - 1] = a[j];
+  }
+  orc_tridiagonal_solve(lam, aT, bT, cT, rT, jtop, n);
+  if (rbar) for (int j = jtop; j <= n; j++) rbar[j - 1] += lam[j - 1];
+  if (bbar) for (int j = jtop; j <= n; j++) bbar[j - 1] -= lam[j - 1] * u[j - 1];
+  if (abar) for (int j = jtop + 1; j <= n; j++) abar[j - 1] -= lam[j - 1] * u[j - 2];
+  if (cbar) for (int j = jtop; j <= n - 1; j++) cbar[j - 1] -= lam[j - 1] * u[j];
+  for (int j = jtop; j <= n; j++) ubar[j - 1] = 0.0;
+}
+
+/* The same rule over the batched [ld, nlevs] layout of tridiagonal_multi!
+ * (tridiagonal.jl:129), one system per masked column from jtop[col] to nlevs. */
+int orc_tridiagonal_adjoint_multi(int64_t ncols, int64_t ld, int32_t nlevs, const double* u,
+                                  const double* a, const double* b, const double* c, double* ubar,
+                                  double* abar, double* bbar, double* cbar, double* rbar,
+                                  const int64_t* jtop, const uint8_t* mask, int32_t nthreads)
+{
+  if (nlevs > ORC_MAXL) return CLMGB_ERR_DIMS;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t col = 0; col < ncols; col++) {
+    if (!mask[col]) continue;
+    const int j0 = (int)jtop[col];
+    if (j0 < 1 || j0 > nlevs) continue;
+    double uc[ORC_MAXL], ac[ORC_MAXL], bc[ORC_MAXL], cc[ORC_MAXL], ub[ORC_MAXL];
+    double ab_[ORC_MAXL], bb_[ORC_MAXL], cb_[ORC_MAXL], rb_[ORC_MAXL];
+    for (int j = 1; j <= nlevs; j++) {
+      uc[j - 1] = IX(u, col, j, ld); ac[j - 1] = IX(a, col, j, ld); bc[j - 1] = IX(b, col, j, ld);
+      cc[j - 1] = IX(c, col, j, ld); ub[j - 1] = IX(ubar, col, j, ld);
+      ab_[j - 1] = abar ? IX(abar, col, j, ld) : 0.0;
+      bb_[j - 1] = bbar ? IX(bbar, col, j, ld) : 0.0;
+      cb_[j - 1] = cbar ? IX(cbar, col, j, ld) : 0.0;
+      rb_[j - 1] = rbar ? IX(rbar, col, j, ld) : 0.0;
+    }
+    orc_tridiagonal_adjoint(uc, ac, bc, cc, ub, abar ? ab_ : NULL, bbar ? bb_ : NULL, cbar ? cb_ : NULL,
+                            rbar ? rb_ : NULL, j0, nlevs);
+    for (int j = 1; j <= nlevs; j++) {
+      IX(ubar, col, j, ld) = ub[j - 1];
+      if (abar) IX(abar, col, j, ld) = ab_[j - 1];
+      if (bbar) IX(bbar, col, j, ld) = bb_[j - 1];
+      if (cbar) IX(cbar, col, j, ld) = cb_[j - 1];
+      if (rbar) IX(rbar, col, j, ld) = rb_[j - 1];
+    }
+  }
+  return 0;
+}
+
+/* band_solve! reverse rule (enzyme_rules.jl:80-107) on the batched layout of
+ * batched_band_solve! (band_diagonal.jl:179-189; A[i,j] = bmatrix[c, (i-j)+kl+1, jt+i-1]).
+ * The rule factorises A with LAPACK gbtrf and solves A^T lambda = xbar with
+ * gbtrs('T'); restated here on the dense matrix (entries outside the band are exact
+ * zeros, so the in-band arithmetic and its order are those of the banded factors):
+ *   factor: for k = 1..n-1 pick the largest |A(i,k)|, i >= k, swap rows k and piv(k),
+ *           f_ik = A(i,k)/A(k,k), A(i,j) -= f_ik*A(k,j) for j > k (multipliers of
+ *           earlier columns are not permuted: L in product form, as gbtrf keeps it);
+ *   U^T w = xbar:  w_i = (xbar_i - sum_{j<i} U(j,i) w_j) / U(i,i), j ascending;
+ *   L^T, P^T:      for k = n-1..1: w_k -= sum_{i>k} f_ik w_i (i ascending), swap(w_k, w_piv(k));
+ *   rbar += lambda; bmatrix_bar -= lambda_i * x_j on every band entry the forward reads;
+ *   xbar is consumed over the solved rows.  bbar and rbar may be NULL. */
+int orc_batched_band_solve_adjoint(int64_t nc, int64_t ld, int32_t nlev, const double* tvector,
+                                   double* tbar, const double* bmatrix, double* bbar, double* rbar,
+                                   const int64_t* jtop, const int64_t* jbot, const uint8_t* mask,
+                                   int32_t kl, int32_t ku, int32_t nlevsno_off, int32_t nthreads)
+{
+  if (nlev > ORC_MAXL) return CLMGB_ERR_DIMS;
+  const int nb = kl + ku + 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int64_t c = 0; c < nc; c++) {
+    if (!mask[c]) continue;
+    const int jt = (int)(jtop[c] + nlevsno_off + 1);
+    const int n = (int)(jbot[c] - jtop[c] + 1);
+    if (n <= 0) continue;
+    double A[ORC_MAXL * ORC_MAXL];
+    double w[ORC_MAXL], xs[ORC_MAXL];
+    int piv[ORC_MAXL];
+#define AA(i, j) A[((i) - 1) * n + ((j) - 1)]
+#define BM(bnd, lev) bmatrix[c + (int64_t)((bnd) - 1) * ld + (int64_t)((lev) - 1) * ld * nb]
+    for (int i = 1; i <= n; i++)
+      for (int j = 1; j <= n; j++) AA(i, j) = 0.0;
+    for (int j = 1; j <= n; j++) {
+      const int ilo = j - kl > 1 ? j - kl : 1;
+      const int ihi = j + ku < n ? j + ku : n;
+      for (int i = ilo; i <= ihi; i++) AA(i, j) = BM((i - j) + kl + 1, jt + i - 1);
+    }
+    for (int k = 1; k <= n - 1; k++) {
+      int p = k;
+      double maxv = fabs(AA(k, k));
+      for (int i = k + 1; i <= n; i++) {
+        const double v = fabs(AA(i, k));
+        if (v > maxv) { maxv = v; p = i; }
+      }
+      piv[k - 1] = p;
+      if (p != k)
+        for (int j = k; j <= n; j++) {
+          const double akj = AA(k, j), apj = AA(p, j);
+          AA(k, j) = apj; AA(p, j) = akj;
+        }
+      const double akk = AA(k, k);
+      for (int i = k + 1; i <= n; i++) {
+        const double f = AA(i, k) / akk;
+        for (int j = k + 1; j <= n; j++) AA(i, j) = AA(i, j) - f * AA(k, j);
+        AA(i, k) = f;
+      }
+    }
+    for (int i = 1; i <= n; i++) {
+      xs[i - 1] = tvector[c + (int64_t)(jt + i - 2) * ld];
+      double s = tbar[c + (int64_t)(jt + i - 2) * ld];
+      for (int j = 1; j < i; j++) s = s - AA(j, i) * w[j - 1];
+      w[i - 1] = s / AA(i, i);
+    }
+    for (int k = n - 1; k >= 1; k--) {
+      double s = w[k - 1];
+      for (int i = k + 1; i <= n; i++) s = s - AA(i, k) * w[i - 1];
+      w[k - 1] = s;
+      const int p = piv[k - 1];
+      if (p != k) { const double t = w[k - 1]; w[k - 1] = w[p - 1]; w[p - 1] = t; }
+    }
+    for (int i = 1; i <= n; i++) {
+      const int lev = jt + i - 1;
+      if (rbar) rbar[c + (int64_t)(lev - 1) * ld] += w[i - 1];
+      tbar[c + (int64_t)(lev - 1) * ld] = 0.0;
+    }
+    if (bbar)
+      for (int j = 1; j <= n; j++) {
+        const int ilo = j - kl > 1 ? j - kl : 1;
+        const int ihi = j + ku < n ? j + ku : n;
+        for (int i = ilo; i <= ihi; i++)
+          bbar[c + (int64_t)((i - j) + kl) * ld + (int64_t)(jt + i - 2) * ld * nb] -= w[i - 1] * xs[j - 1];
+      }
+#undef BM
+#undef AA
+  }
+  return 0;
+}
+
 /* ice_impedance (soil_water_movement.jl:722-724). */
 double orc_ice_impedance(double icefrac, double e_ice) { return cm_pow(10.0, -e_ice * icefrac); }
 

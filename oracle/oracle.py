@@ -47,6 +47,10 @@ def lib():
         L.orc_phase_change_h2osfc.argtypes = [P, P, P, C.c_double, P]
         L.orc_phase_change_beta.argtypes = [P, P, P, C.c_double, P]
         L.orc_init_soil_properties.argtypes = [C.c_int64] + [P] * 11
+        L.orc_tridiagonal_adjoint.argtypes = [P] * 9 + [C.c_int32, C.c_int32]
+        L.orc_tridiagonal_adjoint_multi.argtypes = [C.c_int64, C.c_int64, C.c_int32] + [P] * 11 + [C.c_int32]
+        L.orc_batched_band_solve_adjoint.argtypes = [C.c_int64, C.c_int64, C.c_int32] + [P] * 8 + \
+            [C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         _lib = L
     return _lib
 
@@ -140,6 +144,32 @@ def tridiagonal_col(a, b, c, r, jtop, lbj, ubj, u=None):
     arr = [np.ascontiguousarray(x, dtype=np.float64) for x in (a, b, c, r)]
     lib().orc_tridiagonal_col(_p(u), *[_p(x) for x in arr], jtop, lbj, ubj)
     return u
+
+
+def tridiagonal_adjoint(u, a, b, c, ubar, jtop, n):
+    """tridiagonal_solve! reverse rule for one system; returns (abar, bbar, cbar, rbar)
+    accumulated from zero, and consumes ubar (a float64 array, modified in place)."""
+    arr = [np.ascontiguousarray(x, dtype=np.float64) for x in (u, a, b, c)]
+    outs = [np.zeros(n) for _ in range(4)]
+    lib().orc_tridiagonal_adjoint(*[_p(x) for x in arr], _p(ubar), *[_p(x) for x in outs], jtop, n)
+    return tuple(outs)
+
+
+def tridiagonal_adjoint_multi(u, a, b, c, ubar, abar, bbar, cbar, rbar, jtop, mask, nthreads=None):
+    """Batched rule over (nlevs, ncols) arrays; the bar arrays accumulate in place (None = inactive)."""
+    nlevs, ncols = u.shape
+    _chk(lib().orc_tridiagonal_adjoint_multi(ncols, ncols, nlevs, _p(u), _p(a), _p(b), _p(c), _p(ubar),
+                                             _p(abar), _p(bbar), _p(cbar), _p(rbar), _p(jtop), _p(mask),
+                                             nthreads or default_threads()))
+
+
+def batched_band_solve_adjoint(tvector, tbar, bmatrix, bbar, rbar, jtop, jbot, mask, kl=2, ku=2,
+                               nlevsno_off=0, nthreads=None):
+    """band_solve! reverse rule on the batched layout; bbar/rbar accumulate (None = inactive)."""
+    nlev, nc = tvector.shape
+    _chk(lib().orc_batched_band_solve_adjoint(nc, nc, nlev, _p(tvector), _p(tbar), _p(bmatrix), _p(bbar),
+                                              _p(rbar), _p(jtop), _p(jbot), _p(mask), kl, ku, nlevsno_off,
+                                              nthreads or default_threads()))
 
 
 def ice_impedance(icefrac, e_ice):
