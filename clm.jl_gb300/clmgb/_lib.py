@@ -32,6 +32,8 @@ _SIGS = {
     "clmgb_batched_band_solve_factor": ([P, I64, I64, I32, P, P, P, P, P, P, I32, I32, I32, P, P, P], I32),
     "clmgb_batched_band_solve_adjoint": ([P, I64, I64, I32, P, P, P, P, P, P, P, P, P, I32, I32, I32, P], I32),
     "clmgb_tridiagonal_adjoint": ([P, I64, I64, I32] + [P] * 12, I32),
+    "clmgb_reserve_adjoint": ([P, I64, I64], I32),
+    "clmgb_column_step_vjp": ([P, P, P, P, P, F64, I32, P, P, P, P, P], I32),
     "clmgb_set_option": ([P, I32, I64], I32),
     "clmgb_reserve": ([P, I64], I32),
     "clmgb_get_option": ([P, I32, P], I32),

@@ -55,6 +55,13 @@ OPT_QUEUE_ORDER = 5
 OPT_RESERVED_COLUMNS = 6
 OPT_WAVES_BLOCKS_PER_SM = 7
 OPT_WAVES_OCCUPANCY = 8
+OPT_ADJ_TAPE_USED = 9
+OPT_ADJ_TAPE_SLOTS = 10
+OPT_ADJ_TAPE_ENTRIES = 11
+
+COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
+COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY = 32, 64, 128
+ADJ_MAX_SUBSTEPS = 128
 
 CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20
 
@@ -209,6 +216,14 @@ def _mk_struct(name, fields):
 
 
 SoilTempFields = _mk_struct("SoilTempFields", SOILTEMP_FIELDS)
+
+# clmgb_step_adjoint: (member, level kind or None for [nc]) in header order
+STEP_ADJOINT_MEMBERS = [("lam_t_soisno", "L"), ("lam_h2osoi_liq", "L"), ("lam_h2osoi_ice", "L"),
+                        ("lam_t_grnd", None), ("lam_t_h2osfc", None), ("lam_qcharge", None),
+                        ("grad_watsat", "SOI"), ("grad_bsw", "SOI"), ("grad_sucsat", "SOI"),
+                        ("grad_hksat", "SOI"), ("lam_forc_lwrad", None)]
+StepAdjoint = type("StepAdjoint", (C.Structure,),
+                   {"_fields_": [("struct_size", C.c_int64)] + [(n, c_double_p) for n, _ in STEP_ADJOINT_MEMBERS]})
 SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
 
 

@@ -64,6 +64,10 @@ class Handle:
         """Per-column scratch for up to max_nc columns (impedance pre-pass, queue order)."""
         check(self.lib.clmgb_reserve(self.h, int(max_nc)), "clmgb_reserve")
 
+    def reserve_adjoint(self, slots, entries):
+        """Tape of column_step_vjp: `slots` columns in flight x `entries` records (32 B each)."""
+        check(self.lib.clmgb_reserve_adjoint(self.h, int(slots), int(entries)), "clmgb_reserve_adjoint")
+
     def get_option(self, key):
         v = C.c_int64(0)
         check(self.lib.clmgb_get_option(self.h, key, C.byref(v)), "clmgb_get_option")
@@ -119,6 +123,23 @@ def column_step(handle, state, dtime, cfg=None, snow_method=abi.SNOW_JORDAN1991,
     check(handle.lib.clmgb_column_step(handle.h, C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg),
                                        float(dtime), snow_method, tss, thb, _dptr(col_status, "col_status"),
                                        _stream(stream)), "column_step")
+
+
+def column_step_vjp(handle, state, dtime, adj, cfg=None, snow_method=abi.SNOW_JORDAN1991, col_status=None,
+                    save_bef=True, stream=None):
+    """Reverse of column_step from the state it starts from (advances `state` like
+    column_step does).  `adj` is a clmgb.adjoint.StepAdjointBuffers: its lam_* hold the
+    adjoints of the step's outputs on entry and of its inputs on return; grad_*
+    accumulate."""
+    _require_device(state)
+    cfg = cfg or abi.SwmConfig.clm5_default()
+    ft, fw, b = state.soiltemp_fields(), state.soilwater_fields(), state.bounds()
+    tss = _dptr(state["t_ssbef"]) if save_bef else None
+    thb = _dptr(state["t_h2osfc_bef"]) if save_bef else None
+    a = adj.struct()
+    check(handle.lib.clmgb_column_step_vjp(handle.h, C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg),
+                                           float(dtime), snow_method, tss, thb, C.byref(a),
+                                           _dptr(col_status, "col_status"), _stream(stream)), "column_step_vjp")
 
 
 def phase_change_h2osfc(handle, state, dtime, dhsdT, stream=None):

@@ -48,43 +48,9 @@ k_band_factor_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const do
       ab[i * W + (j - i + KL)] = bmatrix[c + (int64_t)((i - j) + KL) * ldc + (lev - 1) * ldc * NB];
     x[i] = rvector[c + (lev - 1) * ldc];
   }
-#define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
-  for (int k = 0; k < n - 1; k++) {
-    int p = k;
-    double maxv = fabs(AB(k, k));
-    const int ilast = min(n - 1, k + KL);
-    for (int i = k + 1; i <= ilast; i++) {
-      const double v = fabs(AB(i, k));
-      if (v > maxv) { maxv = v; p = i; }
-    }
-    piv[c + (jt + k - 1) * ldc] = (uint8_t)(p - k);
-    const double akk = AB(p, k);
-    const int clast = min(n - 1, k + KL + KU);
-    if (p != k) {
-      for (int col = k; col <= clast; col++) {
-        const double akj = AB(k, col), apj = AB(p, col);
-        AB(k, col) = apj;
-        AB(p, col) = akj;
-      }
-      const double xk = x[k], xp = x[p];
-      x[k] = xp;
-      x[p] = xk;
-    }
-    for (int i = k + 1; i <= ilast; i++) {
-      const double f = AB(i, k) / akk;
-      for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
-      x[i] = x[i] - f * x[k];
-      AB(i, k) = f;
-    }
-  }
-  piv[c + (jt + n - 2) * ldc] = 0;   // the last row has no elimination step
-  for (int i = n - 1; i >= 0; i--) {
-    double s = x[i];
-    const int jl = min(n - 1, i + KL + KU);
-    for (int j = i + 1; j <= jl; j++) s = s - AB(i, j) * x[j];
-    x[i] = s / AB(i, i);
-  }
-#undef AB
+  uint8_t pv[MAXROWS + 1];
+  band_lu_factor_solve<KL, KU>(ab, x, pv, n);
+  for (int k = 0; k < n; k++) piv[c + (jt + k - 1) * ldc] = pv[k];
   for (int i = 0; i < n; i++) {
     tvector[c + (jt + i - 1) * ldc] = x[i];
     for (int d = 0; d < W; d++) lu[c + (int64_t)d * ldc + (jt + i - 1) * ldc * W] = ab[i * W + d];
@@ -112,25 +78,12 @@ k_band_solve_adjoint(int64_t nc, int64_t ldc, int nlev, const double* __restrict
   double w[MAXROWS + 1];
   for (int i = 0; i < n; i++)
     for (int d = 0; d < W; d++) ab[i * W + d] = lu[c + (int64_t)d * ldc + (jt + i - 1) * ldc * W];
-#define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
+  uint8_t pv[MAXROWS + 1];
   for (int i = 0; i < n; i++) {
-    double s = tbar[c + (jt + i - 1) * ldc];
-    for (int j = max(0, i - KL - KU); j < i; j++) s = s - AB(j, i) * w[j];
-    w[i] = s / AB(i, i);
+    w[i] = tbar[c + (jt + i - 1) * ldc];
+    pv[i] = piv[c + (jt + i - 1) * ldc];
   }
-  for (int k = n - 2; k >= 0; k--) {
-    double s = w[k];
-    const int ilast = min(n - 1, k + KL);
-    for (int i = k + 1; i <= ilast; i++) s = s - AB(i, k) * w[i];
-    w[k] = s;
-    const int p = k + (int)piv[c + (jt + k - 1) * ldc];
-    if (p != k) {
-      const double t = w[k];
-      w[k] = w[p];
-      w[p] = t;
-    }
-  }
-#undef AB
+  band_lu_transpose_solve<KL, KU>(ab, pv, w, n);
   for (int i = 0; i < n; i++) {
     const int64_t lev = jt + i;
     if (rbar) rbar[c + (lev - 1) * ldc] += w[i];

@@ -36,6 +36,9 @@ struct clmgb_handle_s {
   clmgb::WaveScratch ws;
   int waves_blocks;             // co-resident blocks per SM of the wave kernel (0 = cannot launch)
   int64_t waves_blocks_per_sm;  // CLMGB_OPT_WAVES_BLOCKS_PER_SM (0 = all co-resident)
+  // tape of the column-step adjoint (clmgb_reserve_adjoint, one allocation)
+  void* tape_block;
+  clmgb::AdjTape tape;
   cudaError_t last_error;
 };
 
@@ -204,6 +207,7 @@ int32_t clmgb_destroy(clmgb_handle h) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   cudaFree(h->scratch);
   if (h->reserve_block) cudaFree(h->reserve_block);
+  if (h->tape_block) cudaFree(h->tape_block);
   h->magic = 0;
   delete h;
   return CLMGB_OK;
@@ -446,6 +450,17 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_RESERVED_COLUMNS: *value = h->qs.capacity; return CLMGB_OK;
     case CLMGB_OPT_WAVES_BLOCKS_PER_SM: *value = h->waves_blocks_per_sm; return CLMGB_OK;
     case CLMGB_OPT_WAVES_OCCUPANCY: *value = h->waves_blocks; return CLMGB_OK;
+    case CLMGB_OPT_ADJ_TAPE_SLOTS: *value = h->tape.slots; return CLMGB_OK;
+    case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
+    case CLMGB_OPT_ADJ_TAPE_USED: {
+      unsigned int used = 0;
+      if (h->tape.max_used) {
+        cudaError_t ce = cudaMemcpy(&used, h->tape.max_used, sizeof(used), cudaMemcpyDeviceToHost);
+        if (ce != cudaSuccess) return cuda_fail(h, ce);
+      }
+      *value = used;
+      return CLMGB_OK;
+    }
     default: return CLMGB_ERR_CONFIG;
   }
 }
@@ -512,6 +527,67 @@ int32_t clmgb_tridiagonal_adjoint(clmgb_handle h, int64_t ncols, int64_t ldc, in
   if (!u || !a || !b || !c || !u_bar || !jtop || !mask) return CLMGB_ERR_NULL_ARG;
   cudaError_t ce = clmgb::launch_tridiagonal_adjoint(ncols, ldc, nlevs, u, a, b, c, u_bar, a_bar, b_bar, c_bar,
                                                      r_bar, jtop, mask, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_reserve_adjoint(clmgb_handle h, int64_t slots, int64_t entries) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (slots < 1 || slots > (1LL << 24) || entries < 256 || entries > (1LL << 30)) return CLMGB_ERR_DIMS;
+  slots = (slots + 63) / 64 * 64;
+  const size_t n = (size_t)slots * (size_t)entries;
+  const size_t nsub = (size_t)slots * CLMGB_ADJ_MAX_SUBSTEPS * (CLMGB_MAX_NLEVSOI + 2);
+  const size_t total = n * (sizeof(int2) + sizeof(double2) + sizeof(double)) + nsub * sizeof(double) + 256;
+  cudaError_t ce = cudaDeviceSynchronize();
+  if (ce != cudaSuccess) return cuda_fail(h, ce);
+  if (h->tape_block) {
+    cudaFree(h->tape_block);
+    h->tape_block = nullptr;
+    h->tape = clmgb::AdjTape{};
+  }
+  void* blk = nullptr;
+  ce = cudaMalloc(&blk, total);
+  if (ce != cudaSuccess) return cuda_fail(h, ce);
+  char* p = (char*)blk;
+  h->tape.par = (double2*)p;
+  p += n * sizeof(double2);
+  h->tape.adj = (double*)p;
+  p += n * sizeof(double);
+  h->tape.sub = (double*)p;
+  p += nsub * sizeof(double);
+  h->tape.idx = (int2*)p;
+  p += n * sizeof(int2);
+  h->tape.max_used = (unsigned int*)p;
+  h->tape.slots = slots;
+  h->tape.entries = entries;
+  h->tape.maxsub = CLMGB_ADJ_MAX_SUBSTEPS;
+  h->tape_block = blk;
+  ce = cudaMemset(h->tape.max_used, 0, sizeof(unsigned int));
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                              const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
+                              int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                              const clmgb_step_adjoint* adj, uint32_t* col_status, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_cfg(cfg);
+  if (e) return e;
+  if ((e = check_bounds(b, true))) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(ft))) return e;
+  if ((e = check_fields(fw))) return e;
+  if (!adj) return CLMGB_ERR_NULL_ARG;
+  if (adj->struct_size != (int64_t)sizeof(clmgb_step_adjoint)) return CLMGB_ERR_ABI;
+  if (!adj->lam_t_soisno || !adj->lam_h2osoi_liq || !adj->lam_h2osoi_ice || !adj->lam_t_grnd ||
+      !adj->lam_t_h2osfc)
+    return CLMGB_ERR_NULL_ARG;
+  if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  if (!h->tape_block) return CLMGB_ERR_CONFIG;
+  const Dims D = make_dims(h->vp, *b);
+  cudaError_t ce = clmgb::launch_column_step_vjp(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef,
+                                                 t_h2osfc_bef, *adj, h->tape, col_status, h->dev_status,
+                                                 (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 

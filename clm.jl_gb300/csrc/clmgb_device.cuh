@@ -103,6 +103,37 @@ __device__ __forceinline__ bool is_wallroof(int64_t it) {
   return it == ICOL_SUNWALL || it == ICOL_SHADEWALL || it == ICOL_ROOF;
 }
 
+// Value of a scalar: the identity for double.  The step adjoint's recording scalar
+// (adjoint_step.cu) overloads it.
+__device__ __forceinline__ double VAL(double x) { return x; }
+
+// Where a column's active state lives.  The production kernels read and write the
+// caller's fields in place (FieldState over clmgb_soiltemp_fields or
+// clmgb_soilwater_fields; only the members a kernel uses are instantiated).  The
+// step adjoint keeps the same quantities in per-thread storage with their tape
+// indices.  Every column function below takes its state through such an accessor
+// X, with X::S the scalar type of the active quantities.
+template <class F>
+struct FieldState {
+  typedef double S;
+  const F& f;
+  int64_t c, ld;
+  __device__ __forceinline__ FieldState(const F& ff, int64_t cc, int64_t l) : f(ff), c(cc), ld(l) {}
+  __device__ __forceinline__ decltype(auto) T(int jj) const { return LV(f.t_soisno, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Liq(int jj) const { return LV(f.h2osoi_liq, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Ice(int jj) const { return LV(f.h2osoi_ice, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Fact(int jj) const { return LV(f.fact, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Icefrac(int j) const { return LV(f.icefrac, c, j, ld); }
+  __device__ __forceinline__ decltype(auto) Tgrnd() const { return f.t_grnd[c]; }
+  __device__ __forceinline__ decltype(auto) Th2osfc() const { return f.t_h2osfc[c]; }
+  __device__ __forceinline__ decltype(auto) Qcharge() const { return f.qcharge[c]; }
+  __device__ __forceinline__ double ForcLwrad() const { return f.forc_lwrad[c]; }
+  __device__ __forceinline__ double Watsat(int j) const { return LVc(f.watsat, c, j, ld); }
+  __device__ __forceinline__ double Bsw(int j) const { return LVc(f.bsw, c, j, ld); }
+  __device__ __forceinline__ double Sucsat(int j) const { return LVc(f.sucsat, c, j, ld); }
+  __device__ __forceinline__ double Hksat(int j) const { return LVc(f.hksat, c, j, ld); }
+};
+
 // ===========================================================================
 // Banded pivoted LU for one column (band_diagonal.jl:87-170).
 //
@@ -114,36 +145,81 @@ __device__ __forceinline__ bool is_wallroof(int64_t it) {
 // upper factor widens to kl+ku, so each row keeps 2*kl+ku+1 entries:
 // ab[r*W + d] holds A[r, r-kl+d].
 // ===========================================================================
-template <int KL, int KU>
-__device__ __forceinline__ void band_lu_solve(double* ab, double* x, int n) {
+template <int KL, int KU, class S>
+__device__ __forceinline__ void band_lu_solve(S* ab, S* x, int n) {
   constexpr int W = 2 * KL + KU + 1;
 #define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
   for (int k = 0; k < n - 1; k++) {
     int piv = k;
-    double maxv = fabs(AB(k, k));
+    double maxv = fabs(VAL(AB(k, k)));
     const int ilast = min(n - 1, k + KL);
     for (int i = k + 1; i <= ilast; i++) {
-      double v = fabs(AB(i, k));
+      double v = fabs(VAL(AB(i, k)));
       if (v > maxv) { maxv = v; piv = i; }
     }
-    const double akk = AB(piv, k);
+    const S akk = AB(piv, k);
     const int clast = min(n - 1, k + KL + KU);
     if (piv != k) {
       for (int col = k; col <= clast; col++) {
-        double akj = AB(k, col), apj = AB(piv, col);
+        S akj = AB(k, col), apj = AB(piv, col);
         AB(k, col) = apj;
         AB(piv, col) = akj;
       }
-      double xk = x[k], xp = x[piv];
+      S xk = x[k], xp = x[piv];
       x[k] = xp;
       x[piv] = xk;
+    }
+    for (int i = k + 1; i <= ilast; i++) {
+      const S f = AB(i, k) / akk;
+      for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
+      x[i] = x[i] - f * x[k];
+    }
+  }
+  for (int i = n - 1; i >= 0; i--) {
+    S s = x[i];
+    const int jl = min(n - 1, i + KL + KU);
+    for (int j = i + 1; j <= jl; j++) s = s - AB(i, j) * x[j];
+    x[i] = s / AB(i, i);
+  }
+#undef AB
+}
+
+// The same elimination keeping its factorisation (LAPACK gbtrf's product form): each
+// multiplier f_ik stays in the slot of the entry it eliminated and piv[k] = p - k
+// records the row exchange of step k.  x is bit-identical to band_lu_solve's.
+template <int KL, int KU>
+__device__ __forceinline__ void band_lu_factor_solve(double* ab, double* x, uint8_t* piv, int n) {
+  constexpr int W = 2 * KL + KU + 1;
+#define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
+  for (int k = 0; k < n - 1; k++) {
+    int p = k;
+    double maxv = fabs(AB(k, k));
+    const int ilast = min(n - 1, k + KL);
+    for (int i = k + 1; i <= ilast; i++) {
+      const double v = fabs(AB(i, k));
+      if (v > maxv) { maxv = v; p = i; }
+    }
+    piv[k] = (uint8_t)(p - k);
+    const double akk = AB(p, k);
+    const int clast = min(n - 1, k + KL + KU);
+    if (p != k) {
+      for (int col = k; col <= clast; col++) {
+        const double akj = AB(k, col), apj = AB(p, col);
+        AB(k, col) = apj;
+        AB(p, col) = akj;
+      }
+      const double xk = x[k], xp = x[p];
+      x[k] = xp;
+      x[p] = xk;
     }
     for (int i = k + 1; i <= ilast; i++) {
       const double f = AB(i, k) / akk;
       for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
       x[i] = x[i] - f * x[k];
+      AB(i, k) = f;
     }
   }
+  if (n > 0) piv[n - 1] = 0;
   for (int i = n - 1; i >= 0; i--) {
     double s = x[i];
     const int jl = min(n - 1, i + KL + KU);
@@ -153,78 +229,111 @@ __device__ __forceinline__ void band_lu_solve(double* ab, double* x, int n) {
 #undef AB
 }
 
+// A^T w = b from the factors of band_lu_factor_solve (LAPACK gbtrs 'T' order):
+// U^T y = b by forward substitution, then for k = n-2..0: y_k -= sum_i f_ik y_i and
+// the row exchange of step k.  w holds b on entry.
+template <int KL, int KU>
+__device__ __forceinline__ void band_lu_transpose_solve(const double* ab, const uint8_t* piv, double* w, int n) {
+  constexpr int W = 2 * KL + KU + 1;
+#define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
+  for (int i = 0; i < n; i++) {
+    double s = w[i];
+    for (int j = max(0, i - KL - KU); j < i; j++) s = s - AB(j, i) * w[j];
+    w[i] = s / AB(i, i);
+  }
+  for (int k = n - 2; k >= 0; k--) {
+    double s = w[k];
+    const int ilast = min(n - 1, k + KL);
+    for (int i = k + 1; i <= ilast; i++) s = s - AB(i, k) * w[i];
+    w[k] = s;
+    const int p = k + (int)piv[k];
+    if (p != k) {
+      const double t = w[k];
+      w[k] = w[p];
+      w[p] = t;
+    }
+  }
+#undef AB
+}
+
 // ===========================================================================
 // phase_change_h2osfc! (soil_temperature.jl:1757-1855), column c.
 // ===========================================================================
-__device__ inline void phase_change_h2osfc_col(const Dims& D, const clmgb_soiltemp_fields& f,
-                                        int64_t c, double dtime, double dhsdT) {
-  const int64_t ld = D.ldc;
+template <class ST>
+__device__ inline void phase_change_h2osfc_col(const Dims& D, const clmgb_soiltemp_fields& f, int64_t c,
+                                               double dtime, typename ST::S dhsdT, ST& X) {
+  typedef typename ST::S S;
   const int joff = D.nlevsno;
   const int64_t snl = f.col_snl[c];
-  double* T = f.t_soisno;
   f.xmf_h2osfc[c] = 0.0;
   f.qflx_h2osfc_to_ice[c] = 0.0;
   f.eflx_h2osfc_to_snow[c] = 0.0;
   const double fh = f.frac_h2osfc[c];
-  if (fh > 0.0 && f.t_h2osfc[c] <= TFRZ) {
-    const double tinc = TFRZ - f.t_h2osfc[c];
-    f.t_h2osfc[c] = TFRZ;
+  if (fh > 0.0 && X.Th2osfc() <= TFRZ) {
+    const S tinc = TFRZ - X.Th2osfc();
+    X.Th2osfc() = TFRZ;
     const double ch = f.c_h2osfc[c];
-    const double hm = fh * (dhsdT * tinc - tinc * ch / dtime);
-    const double xm = hm * dtime / HFUS;
-    const double temp1 = f.h2osfc[c] + xm;
-    double h2osno_total = f.h2osno_no_layers[c];
+    const S hm = fh * (dhsdT * tinc - tinc * ch / dtime);
+    const S xm = hm * dtime / HFUS;
+    const S temp1 = f.h2osfc[c] + xm;
+    S h2osno_total = f.h2osno_no_layers[c];
     if (snl < 0)
-      for (int j = (int)snl + 1; j <= 0; j++)
-        h2osno_total += LV(f.h2osoi_ice, c, j + joff, ld) + LV(f.h2osoi_liq, c, j + joff, ld);
+      for (int j = (int)snl + 1; j <= 0; j++) h2osno_total += X.Ice(j + joff) + X.Liq(j + joff);
     const double fs = f.frac_sno_eff[c];
     const double z_avg = fs * f.snow_depth[c];
-    double rho_avg = z_avg > 0.0 ? jl_min(800.0, h2osno_total / z_avg) : 200.0;
+    S rho_avg = z_avg > 0.0 ? jl_min(800.0, h2osno_total / z_avg) : S(200.0);
     if (temp1 >= 0.0) {
-      f.int_snow[c] -= xm;
-      if (snl == 0) f.h2osno_no_layers[c] -= xm;
-      else LV(f.h2osoi_ice, c, joff, ld) -= xm;
+      f.int_snow[c] -= VAL(xm);
+      if (snl == 0) f.h2osno_no_layers[c] -= VAL(xm);
+      else X.Ice(joff) -= xm;
       h2osno_total -= xm;
-      f.h2osfc[c] += xm;
-      f.xmf_h2osfc[c] = hm;
-      f.qflx_h2osfc_to_ice[c] = -xm / dtime;
-      if (fs > 0.0 && snl < 0) f.snow_depth[c] = h2osno_total / (rho_avg * fs);
-      else f.snow_depth[c] = h2osno_total / DENICE;
+      f.h2osfc[c] += VAL(xm);
+      f.xmf_h2osfc[c] = VAL(hm);
+      f.qflx_h2osfc_to_ice[c] = -VAL(xm) / dtime;
+      if (fs > 0.0 && snl < 0) f.snow_depth[c] = VAL(h2osno_total / (rho_avg * fs));
+      else f.snow_depth[c] = VAL(h2osno_total) / DENICE;
       if (snl == 0) {
-        LV(T, c, joff, ld) = f.t_h2osfc[c];
+        X.T(joff) = X.Th2osfc();
         f.eflx_h2osfc_to_snow[c] = 0.0;
       } else {
-        double c1;
-        if (snl == -1) c1 = fs * (dtime / LV(f.fact, c, joff, ld) - dhsdT * dtime);
-        else c1 = fs / LV(f.fact, c, joff, ld) * dtime;
-        const double c2 = fh != 0.0 ? (-CPLIQ * xm - fh * dhsdT * dtime) : 0.0;
-        LV(T, c, joff, ld) = (c1 * LV(T, c, joff, ld) + c2 * f.t_h2osfc[c]) / (c1 + c2);
-        f.eflx_h2osfc_to_snow[c] = (f.t_h2osfc[c] - LV(T, c, joff, ld)) * c2 / dtime;
+        S c1;
+        if (snl == -1) c1 = fs * (dtime / X.Fact(joff) - dhsdT * dtime);
+        else c1 = fs / X.Fact(joff) * dtime;
+        const S c2 = fh != 0.0 ? (-CPLIQ * xm - fh * dhsdT * dtime) : S(0.0);
+        X.T(joff) = (c1 * X.T(joff) + c2 * X.Th2osfc()) / (c1 + c2);
+        f.eflx_h2osfc_to_snow[c] = VAL((X.Th2osfc() - X.T(joff)) * c2 / dtime);
       }
     } else {
-      rho_avg = (h2osno_total * rho_avg + f.h2osfc[c] * DENICE) / (h2osno_total + f.h2osfc[c]);
-      f.int_snow[c] += f.h2osfc[c];
-      if (snl == 0) f.h2osno_no_layers[c] += f.h2osfc[c];
-      else LV(f.h2osoi_ice, c, joff, ld) += f.h2osfc[c];
-      h2osno_total += f.h2osfc[c];
-      f.qflx_h2osfc_to_ice[c] = f.h2osfc[c] / dtime;
-      f.t_h2osfc[c] -= temp1 * HFUS / (dtime * dhsdT - ch);
-      f.xmf_h2osfc[c] = hm - fh * temp1 * HFUS / dtime;
+      const double h2osfc0 = f.h2osfc[c];
+      rho_avg = (h2osno_total * rho_avg + h2osfc0 * DENICE) / (h2osno_total + h2osfc0);
+      f.int_snow[c] += h2osfc0;
+      if (snl == 0) f.h2osno_no_layers[c] += h2osfc0;
+      else X.Ice(joff) += h2osfc0;
+      h2osno_total += h2osfc0;
+      f.qflx_h2osfc_to_ice[c] = h2osfc0 / dtime;
+      X.Th2osfc() -= temp1 * HFUS / (dtime * dhsdT - ch);
+      f.xmf_h2osfc[c] = VAL(hm - fh * temp1 * HFUS / dtime);
       if (snl == 0) {
-        LV(T, c, joff, ld) = f.t_h2osfc[c];
+        X.T(joff) = X.Th2osfc();
       } else {
-        double c1;
-        if (snl == -1) c1 = fs * (dtime / LV(f.fact, c, joff, ld) - dhsdT * dtime);
-        else c1 = fs / LV(f.fact, c, joff, ld) * dtime;
-        const double c2 = fh != 0.0 ? fh * (ch - dtime * dhsdT) : 0.0;
-        LV(T, c, joff, ld) = (c1 * LV(T, c, joff, ld) + c2 * f.t_h2osfc[c]) / (c1 + c2);
-        f.t_h2osfc[c] = LV(T, c, joff, ld);
+        S c1;
+        if (snl == -1) c1 = fs * (dtime / X.Fact(joff) - dhsdT * dtime);
+        else c1 = fs / X.Fact(joff) * dtime;
+        const S c2 = fh != 0.0 ? fh * (ch - dtime * dhsdT) : S(0.0);
+        X.T(joff) = (c1 * X.T(joff) + c2 * X.Th2osfc()) / (c1 + c2);
+        X.Th2osfc() = X.T(joff);
       }
       f.h2osfc[c] = 0.0;
-      if (fs > 0.0 && snl < 0) f.snow_depth[c] = h2osno_total / (rho_avg * fs);
-      else f.snow_depth[c] = h2osno_total / DENICE;
+      if (fs > 0.0 && snl < 0) f.snow_depth[c] = VAL(h2osno_total / (rho_avg * fs));
+      else f.snow_depth[c] = VAL(h2osno_total) / DENICE;
     }
   }
+}
+
+__device__ inline void phase_change_h2osfc_col(const Dims& D, const clmgb_soiltemp_fields& f, int64_t c,
+                                               double dtime, double dhsdT) {
+  FieldState<clmgb_soiltemp_fields> X(f, c, D.ldc);
+  phase_change_h2osfc_col(D, f, c, dtime, dhsdT, X);
 }
 
 // ===========================================================================
@@ -232,8 +341,10 @@ __device__ inline void phase_change_h2osfc_col(const Dims& D, const clmgb_soilte
 // The reference's four sequential level loops per thread are kept; the per-call
 // scratch rows (PcbTmp) become per-thread arrays.
 // ===========================================================================
-__device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp_fields& f,
-                                      int64_t c, double dtime, double dhsdT) {
+template <class ST>
+__device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp_fields& f, int64_t c,
+                                             double dtime, typename ST::S dhsdT, ST& X) {
+  typedef typename ST::S S;
   const int64_t ld = D.ldc;
   const int nlevsno = D.nlevsno, nlevgrnd = D.nlevgrnd, nlevmax = D.nlevmax;
   const int joff = nlevsno;
@@ -242,11 +353,9 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
   const int64_t it = f.col_itype[c];
   const int64_t lit = f.lun_itype[l];
   const bool wallroof = is_wallroof(it);
-  double hm[MAXL + 1], xm[MAXL + 1], wice0[MAXL + 1], wexice0[MAXL + 1], wmass0[MAXL + 1];
-  double tinc[MAXL + 1], supercool[MAXGRND + 1];
-  double* T = f.t_soisno;
-  double* ICE = f.h2osoi_ice;
-  double* LIQ = f.h2osoi_liq;
+  S hm[MAXL + 1], xm[MAXL + 1], wice0[MAXL + 1], wmass0[MAXL + 1];
+  S tinc[MAXL + 1], supercool[MAXGRND + 1];
+  double wexice0[MAXL + 1];
   double* EXI = f.excess_ice;
   const double fse = f.frac_sno_eff[c];
   const double fh = f.frac_h2osfc[c];
@@ -261,9 +370,9 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
       LV(f.imelt, c, jj, ld) = 0;
       hm[jj] = 0.0;
       xm[jj] = 0.0;
-      wice0[jj] = LV(ICE, c, jj, ld);
+      wice0[jj] = X.Ice(jj);
       wexice0[jj] = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
-      wmass0[jj] = LV(ICE, c, jj, ld) + LV(LIQ, c, jj, ld) + wexice0[jj];
+      wmass0[jj] = X.Ice(jj) + X.Liq(jj) + wexice0[jj];
       if (j >= 1) LV(f.exice_subs, c, j, ld) = 0.0;
     }
     if (j <= 0) {
@@ -273,15 +382,15 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
   }
   for (int j = (int)snl + 1; j <= 0; j++) {
     const int jj = j + joff;
-    if (LV(ICE, c, jj, ld) > 0.0 && LV(T, c, jj, ld) > TFRZ) {
+    if (X.Ice(jj) > 0.0 && X.T(jj) > TFRZ) {
       LV(f.imelt, c, jj, ld) = 1;
-      tinc[jj] = TFRZ - LV(T, c, jj, ld);
-      LV(T, c, jj, ld) = TFRZ;
+      tinc[jj] = TFRZ - X.T(jj);
+      X.T(jj) = TFRZ;
     }
-    if (LV(LIQ, c, jj, ld) > 0.0 && LV(T, c, jj, ld) < TFRZ) {
+    if (X.Liq(jj) > 0.0 && X.T(jj) < TFRZ) {
       LV(f.imelt, c, jj, ld) = 2;
-      tinc[jj] = TFRZ - LV(T, c, jj, ld);
-      LV(T, c, jj, ld) = TFRZ;
+      tinc[jj] = TFRZ - X.T(jj);
+      X.T(jj) = TFRZ;
     }
   }
   const bool supercool_type = (lit == ISTSOIL || lit == ISTCROP || it == ICOL_ROAD_PERV);
@@ -290,27 +399,27 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
     supercool[j] = 0.0;
     const bool active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= D.nlevurb);
     if (!active) continue;
-    if (LV(ICE, c, jj, ld) > 0.0 && LV(T, c, jj, ld) > TFRZ) {
-      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+    if (X.Ice(jj) > 0.0 && X.T(jj) > TFRZ) {
+      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
     }
-    if (LV(EXI, c, j, ld) > 0.0 && LV(T, c, jj, ld) > TFRZ) {
-      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+    if (LV(EXI, c, j, ld) > 0.0 && X.T(jj) > TFRZ) {
+      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
     }
     if (supercool_type) {
-      const double tt = LV(T, c, jj, ld);
+      const S tt = X.T(jj);
       if (tt < TFRZ) {
-        const double smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
-        double sc = LVc(f.watsat, c, j, ld) * cm_pow(smp / LVc(f.sucsat, c, j, ld), -1.0 / LVc(f.bsw, c, j, ld));
+        const S smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
+        S sc = X.Watsat(j) * cm_pow(smp / X.Sucsat(j), -1.0 / X.Bsw(j));
         sc *= LVc(f.dz, c, jj, ld) * 1000.0;
         supercool[j] = sc;
       }
     }
-    if (LV(LIQ, c, jj, ld) > supercool[j] && LV(T, c, jj, ld) < TFRZ) {
-      LV(f.imelt, c, jj, ld) = 2; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+    if (X.Liq(jj) > supercool[j] && X.T(jj) < TFRZ) {
+      LV(f.imelt, c, jj, ld) = 2; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
     }
     if (f.h2osno_no_layers[c] > 0.0 && j == 1) {
-      if (LV(T, c, jj, ld) > TFRZ) {
-        LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - LV(T, c, jj, ld); LV(T, c, jj, ld) = TFRZ;
+      if (X.T(jj) > TFRZ) {
+        LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
       }
     }
   }
@@ -319,7 +428,7 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
     const bool active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= D.nlevurb);
     if (!active) continue;
     int64_t im = LV(f.imelt, c, jj, ld);
-    const double fct = LV(f.fact, c, jj, ld);
+    const S fct = X.Fact(jj);
     if (im > 0) {
       if (j == snl + 1) {
         if (j > 0) hm[jj] = dhsdT * tinc[jj] - tinc[jj] / fct;
@@ -335,33 +444,35 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
     if (im == 1 && hm[jj] < 0.0) { hm[jj] = 0.0; im = 0; }
     if (im == 2 && hm[jj] > 0.0) { hm[jj] = 0.0; im = 0; }
     LV(f.imelt, c, jj, ld) = im;
-    if (im > 0 && fabs(hm[jj]) > 0.0) {
+    if (im > 0 && fabs(VAL(hm[jj])) > 0.0) {
       xm[jj] = hm[jj] * dtime / HFUS;
       if (j == 1) {
         if (f.h2osno_no_layers[c] > 0.0 && xm[jj] > 0.0) {
           const double temp1 = f.h2osno_no_layers[c];
-          f.h2osno_no_layers[c] = jl_max(0.0, temp1 - xm[jj]);
-          const double propor = f.h2osno_no_layers[c] / temp1;
-          f.snow_depth[c] = propor * f.snow_depth[c];
-          const double heatr0 = hm[jj] - HFUS * (temp1 - f.h2osno_no_layers[c]) / dtime;
+          const S h2n = jl_max(0.0, temp1 - xm[jj]);
+          f.h2osno_no_layers[c] = VAL(h2n);
+          const S propor = h2n / temp1;
+          f.snow_depth[c] = VAL(propor * f.snow_depth[c]);
+          const S heatr0 = hm[jj] - HFUS * (temp1 - h2n) / dtime;
           if (heatr0 > 0.0) { xm[jj] = heatr0 * dtime / HFUS; hm[jj] = heatr0; }
           else { xm[jj] = 0.0; hm[jj] = 0.0; }
-          f.qflx_snomelt[c] = jl_max(0.0, temp1 - f.h2osno_no_layers[c]) / dtime;
-          f.xmf[c] = HFUS * f.qflx_snomelt[c];
-          f.qflx_snow_drain[c] = f.qflx_snomelt[c];
+          const S qsm = jl_max(0.0, temp1 - h2n) / dtime;
+          f.qflx_snomelt[c] = VAL(qsm);
+          f.xmf[c] = HFUS * VAL(qsm);
+          f.qflx_snow_drain[c] = VAL(qsm);
         }
       }
-      double heatr = 0.0;
-      double ice = LV(ICE, c, jj, ld);
+      S heatr = 0.0;
+      S ice = X.Ice(jj);
       if (xm[jj] > 0.0) {
         ice = jl_max(0.0, wice0[jj] - xm[jj]);
-        LV(ICE, c, jj, ld) = ice;
+        X.Ice(jj) = ice;
         heatr = hm[jj] - HFUS * (wice0[jj] - ice) / dtime;
-        const double xm2 = xm[jj] - ice;
+        const S xm2 = xm[jj] - ice;
         if (ice == 0.0) {
           if (wexice0[jj] >= 0.0 && xm2 > 0.0 && j >= 2) {
-            const double ex = jl_max(0.0, wexice0[jj] - xm2);
-            LV(EXI, c, j, ld) = ex;
+            const S ex = jl_max(0.0, wexice0[jj] - xm2);
+            LV(EXI, c, j, ld) = VAL(ex);
             heatr = hm[jj] - HFUS * (wexice0[jj] - ex + wice0[jj] - ice) / dtime;
           }
         }
@@ -372,14 +483,14 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
           if (wmass0[jj] - wexice0[jj] < supercool[j]) ice = 0.0;
           else ice = jl_min(wmass0[jj] - wexice0[jj] - supercool[j], wice0[jj] - xm[jj]);
         }
-        LV(ICE, c, jj, ld) = ice;
+        X.Ice(jj) = ice;
         heatr = hm[jj] - HFUS * (wice0[jj] - ice) / dtime;
       }
       const double ei_val = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
-      const double liq = jl_max(0.0, wmass0[jj] - ice - ei_val);
-      LV(LIQ, c, jj, ld) = liq;
-      if (fabs(heatr) > 0.0) {
-        double tt = LV(T, c, jj, ld);
+      const S liq = jl_max(0.0, wmass0[jj] - ice - ei_val);
+      X.Liq(jj) = liq;
+      if (fabs(VAL(heatr)) > 0.0) {
+        S tt = X.T(jj);
         if (j == snl + 1) {
           if (j == 1) tt += fct * heatr / (1.0 - (1.0 - fh) * fct * dhsdT);
           else if (fse > 0.0) tt += (fct / fse) * heatr / (1.0 - fct * dhsdT);
@@ -390,24 +501,24 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
           else if (fse > 0.0) tt += (fct / fse) * heatr;
         }
         if (j <= 0)
-          if (liq * ice > 0.0) tt = TFRZ;
-        LV(T, c, jj, ld) = tt;
+          if (VAL(liq) * VAL(ice) > 0.0) tt = TFRZ;
+        X.T(jj) = tt;
       }
       if (j >= 1) {
         const double ex = LV(EXI, c, j, ld);
-        f.xmf[c] += HFUS * (wice0[jj] - ice) / dtime + HFUS * (wexice0[jj] - ex) / dtime;
+        f.xmf[c] += HFUS * (VAL(wice0[jj]) - VAL(ice)) / dtime + HFUS * (wexice0[jj] - ex) / dtime;
         LV(f.exice_subs, c, j, ld) = jl_max(0.0, (wexice0[jj] - ex) / DENICE);
       } else {
-        f.xmf[c] += HFUS * (wice0[jj] - ice) / dtime;
+        f.xmf[c] += HFUS * (VAL(wice0[jj]) - VAL(ice)) / dtime;
       }
       if (im == 1 && j < 1) {
-        const double q = jl_max(0.0, wice0[jj] - ice) / dtime;
+        const double q = jl_max(0.0, VAL(wice0[jj]) - VAL(ice)) / dtime;
         LV(f.qflx_snomelt_lyr, c, jj, ld) = q;
         f.qflx_snomelt[c] += q;
         f.snomelt_accum[c] += q * dtime * 1.0e-3;
       }
       if (im == 2 && j < 1) {
-        const double q = jl_max(0.0, ice - wice0[jj]) / dtime;
+        const double q = jl_max(0.0, VAL(ice) - VAL(wice0[jj])) / dtime;
         LV(f.qflx_snofrz_lyr, c, jj, ld) = q;
         f.qflx_snofrz[c] += q;
       }
@@ -418,12 +529,20 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
   else if (lit == ISTSOIL || lit == ISTCROP) f.eflx_snomelt_r[c] = f.eflx_snomelt[c];
 }
 
+__device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp_fields& f, int64_t c,
+                                             double dtime, double dhsdT) {
+  FieldState<clmgb_soiltemp_fields> X(f, c, D.ldc);
+  phase_change_beta_col(D, f, c, dtime, dhsdT, X);
+}
+
 // ===========================================================================
 // soil_temperature! (soil_temperature.jl:358-593) for one non-urban column,
 // all of its kernels fused in the reference's call order.
 // ===========================================================================
-__device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soiltemp_fields& f,
-                                         int64_t c, double dtime, int snow_method) {
+template <class ST>
+__device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soiltemp_fields& f, int64_t c,
+                                                double dtime, int snow_method, ST& X) {
+  typedef typename ST::S S;
   const int64_t ld = D.ldc, ldp = D.ldp;
   const int nlevsno = D.nlevsno, nlevgrnd = D.nlevgrnd, nlevsoi = D.nlevsoi;
   const int nlevmax = D.nlevmax;
@@ -442,44 +561,44 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   const int64_t nbedrock = f.col_nbedrock[c];
   const double fse = f.frac_sno_eff[c];
   const double fh = f.frac_h2osfc[c];
-  double* T = f.t_soisno;
   const double* DZ = f.dz;
   const double* Z = f.z;
   const double* ZI = f.zi;
-  const double* LIQ = f.h2osoi_liq;
-  const double* ICE = f.h2osoi_ice;
   const double* EXI = f.excess_ice;
 
   // per-column working rows (level index jj, 1-based; entries outside the active
   // range are never read)
-  double tk[MAXL + 2], fn[MAXL + 2], fct[MAXL + 2], tt[MAXL + 2], zz[MAXL + 2];
+  S tk[MAXL + 2], fn[MAXL + 2], fct[MAXL + 2], tt[MAXL + 2];
+  double zz[MAXL + 2];
 
   // ---- soil_therm_prop!: layer conductivity thk (_soil_snow_tk_kernel! :647-716) ----
   // thk kept in tk[] first, interface conductivity computed in place afterwards.
   for (int jj = jjtop; jj <= nlev; jj++) {
-    tt[jj] = LV(T, c, jj, ld);
+    tt[jj] = X.T(jj);
     zz[jj] = LVc(Z, c, jj, ld);
   }
   for (int jj = jjtop; jj <= nlevsno + nlevgrnd; jj++) {
     const int j = jj - nlevsno;
-    double thkv = 0.0;
+    S thkv = 0.0;
     if (j >= 1) {
       if (!is_special) {
         if (j > nbedrock) {
           thkv = THK_BEDROCK;             // bedrock overrides the soil value (:684-686)
         } else {
-          const double liq = LV(LIQ, c, jj, ld), ice = LV(ICE, c, jj, ld), exi = LV(EXI, c, j, ld);
-          const double dzv = LVc(DZ, c, jj, ld), ws = LVc(f.watsat, c, j, ld);
-          double satw = (liq / DENH2O + ice / DENICE + exi / DENICE) / (dzv * ws);
+          const S liq = X.Liq(jj), ice = X.Ice(jj);
+          const double exi = LV(EXI, c, j, ld);
+          const double dzv = LVc(DZ, c, jj, ld);
+          const S ws = X.Watsat(j);
+          S satw = (liq / DENH2O + ice / DENICE + exi / DENICE) / (dzv * ws);
           satw = jl_min(1.0, satw);
           if (satw > 1.0e-7) {
-            double dke;
+            S dke;
             if (tt[jj] >= TFRZ) dke = jl_max(0.0, cm_log10(satw) + 1.0);
             else dke = satw;
-            const double a1 = liq / (DENH2O * dzv);
-            const double fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
-            const double fl = a1 / fl_denom;
-            const double dksat = LVc(f.tkmg, c, j, ld) * cm_pow(TKWAT, fl * ws) * cm_pow(TKICE, (1.0 - fl) * ws);
+            const S a1 = liq / (DENH2O * dzv);
+            const S fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
+            const S fl = a1 / fl_denom;
+            const S dksat = LVc(f.tkmg, c, j, ld) * cm_pow(TKWAT, fl * ws) * cm_pow(TKICE, (1.0 - fl) * ws);
             thkv = dke * dksat + (1.0 - dke) * LVc(f.tkdry, c, j, ld);
           } else {
             thkv = LVc(f.tkdry, c, j, ld);
@@ -494,8 +613,8 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     } else {
       // snow layer (snl+1 <= j <= 0) — Jordan1991 or Sturm1997
       const double denom = jl_max(fse, 1.0e-6) * jl_max(LVc(DZ, c, jj, ld), 1.0e-6);
-      const double bwv = (LV(ICE, c, jj, ld) + LV(LIQ, c, jj, ld)) / denom;
-      LV(f.bw, c, jj, ld) = bwv;
+      const S bwv = (X.Ice(jj) + X.Liq(jj)) / denom;
+      LV(f.bw, c, jj, ld) = VAL(bwv);
       if (snow_method == CLMGB_SNOW_JORDAN1991) {
         thkv = TKAIR + (7.75e-5 * bwv + 1.105e-6 * (bwv * bwv)) * (TKICE - TKAIR);
       } else {
@@ -503,23 +622,25 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
         else thkv = 0.138 - 1.01 * (bwv / 1000.0) + 3.233 * ((bwv / 1000.0) * (bwv / 1000.0));
       }
     }
-    LV(f.thk, c, jj, ld) = thkv;
+    LV(f.thk, c, jj, ld) = VAL(thkv);
     tk[jj] = thkv;
   }
   // _tk_h2osfc_kernel! (:762-776): uses the soil-1 layer conductivity
-  double tk_h2osfc;
+  S tk_h2osfc;
   {
     const double zh2osfc = 1.0e-3 * (0.5 * f.h2osfc[c]);
-    const double z1 = zz[1 + joff], tk1 = tk[1 + joff];
-    const double denom = TKWAT * z1 + tk1 * zh2osfc;
-    tk_h2osfc = denom > 0.0 ? TKWAT * tk1 * (z1 + zh2osfc) / denom : tk1;
+    const double z1 = zz[1 + joff];
+    const S tk1 = tk[1 + joff];
+    const S denom = TKWAT * z1 + tk1 * zh2osfc;
+    if (denom > 0.0) tk_h2osfc = TKWAT * tk1 * (z1 + zh2osfc) / denom;
+    else tk_h2osfc = tk1;
   }
   // interface conductivity (_soil_tk_interface_kernel! :599-629), ascending so
   // tk[jj+1] still holds the layer value when tk[jj] is formed
   for (int jj = jjtop; jj <= nlev; jj++) {
     const int j = jj - nlevsno;
     if (j <= nlevgrnd - 1) {
-      const double tkj = tk[jj], tkj1 = tk[jj + 1];
+      const S tkj = tk[jj], tkj1 = tk[jj + 1];
       const double zj = zz[jj], zj1 = zz[jj + 1], zij1 = LVc(ZI, c, jj + 1, ld);
       tk[jj] = tkj * tkj1 * (zj1 - zj) / (tkj * (zj1 - zij1) + tkj1 * (zij1 - zj));
     } else if (j == nlevgrnd) {
@@ -532,23 +653,23 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   for (int jj = jjtop; jj <= nlevsno + nlevgrnd; jj++) {
     const int j = jj - nlevsno;
     const double dzv = LVc(DZ, c, jj, ld);
-    double cv;
+    S cv;
     if (j >= 1) {
       if (!is_special) {
-        cv = LVc(f.csol, c, j, ld) * (1.0 - LVc(f.watsat, c, j, ld)) * dzv +
-             (LV(ICE, c, jj, ld) * CPICE + LV(LIQ, c, jj, ld) * CPLIQ) + LV(EXI, c, j, ld) * CPICE;
+        cv = LVc(f.csol, c, j, ld) * (1.0 - X.Watsat(j)) * dzv + (X.Ice(jj) * CPICE + X.Liq(jj) * CPLIQ) +
+             LV(EXI, c, j, ld) * CPICE;
       } else {
-        cv = LV(ICE, c, jj, ld) * CPICE + LV(LIQ, c, jj, ld) * CPLIQ;
+        cv = X.Ice(jj) * CPICE + X.Liq(jj) * CPLIQ;
       }
       if (j > nbedrock) cv = CSOL_BEDROCK * dzv;
       if (j == 1 && f.h2osno_no_layers[c] > 0.0) cv += CPICE * f.h2osno_no_layers[c];
     } else {
       if (fse > 0.0)
-        cv = jl_max(THIN_SFCLAYER, (CPLIQ * LV(LIQ, c, jj, ld) + CPICE * LV(ICE, c, jj, ld)) / fse);
+        cv = jl_max(THIN_SFCLAYER, (CPLIQ * X.Liq(jj) + CPICE * X.Ice(jj)) / fse);
       else
         cv = THIN_SFCLAYER;
     }
-    double fc;
+    S fc;
     if (j == jtop) {
       fc = dtime / cv * dzv / (0.5 * (zz[jj] - LVc(ZI, c, jj, ld) + CAPR * (zz[jj + 1] - LVc(ZI, c, jj, ld))));
       fn[jj] = tk[jj] * (tt[jj + 1] - tt[jj]) / (zz[jj + 1] - zz[jj]);
@@ -560,49 +681,50 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
       fn[jj] = f.eflx_bot[c];
     }
     fct[jj] = fc;
-    LV(f.fact, c, jj, ld) = fc;
+    X.Fact(jj) = fc;
   }
 
   // ---- compute_ground_heat_flux_and_deriv! (:1200-1263) ----
   const double eg = f.emg[c];
-  const double tg = f.t_grnd[c];
-  const double lwrad_emit = eg * SB * jl_pow4(tg);
-  const double dlwrad_emit = 4.0 * eg * SB * (tg * tg * tg);
-  const double lwrad_emit_snow = eg * SB * jl_pow4(tt[jjtop]);
-  const double lwrad_emit_soil = eg * SB * jl_pow4(tt[1 + joff]);
-  const double lwrad_emit_h2osfc = eg * SB * jl_pow4(f.t_h2osfc[c]);
+  const S tg = X.Tgrnd();
+  const S lwrad_emit = eg * SB * jl_pow4(tg);
+  const S dlwrad_emit = 4.0 * eg * SB * (tg * tg * tg);
+  const S lwrad_emit_snow = eg * SB * jl_pow4(tt[jjtop]);
+  const S lwrad_emit_soil = eg * SB * jl_pow4(tt[1 + joff]);
+  const S lwrad_emit_h2osfc = eg * SB * jl_pow4(X.Th2osfc());
   const double htvp = f.htvp[c];
-  const double forc = f.forc_lwrad[c];
+  const S forc = X.ForcLwrad();
   const int64_t pi = f.col_patchi[c], pf = f.col_patchf[c];
   if (pi < 1 || pf > D.np || pf < pi - 1) return CLMGB_COL_PATCH_RANGE;
-  double dhsdT = 0.0, hs_soil = 0.0, hs_h2osfc = 0.0, hs_top_snow = 0.0;
+  S dhsdT = 0.0, hs_soil = 0.0, hs_h2osfc = 0.0, hs_top_snow = 0.0;
   double sabg_lyr_col[MAXSNO + 2];
   for (int k = 0; k <= nlevsno + 1; k++) sabg_lyr_col[k] = 0.0;
   for (int64_t p1 = pi; p1 <= pf; p1++) {
     const int64_t p = p1 - 1;
     if (f.patch_column[p] != c + 1) continue;
-    double dh_p = 0.0, hsoil_p = 0.0, hh_p = 0.0;
+    S dh_p = 0.0, hsoil_p = 0.0, hh_p = 0.0;
     const bool act = f.mask_nolakep[p] != 0;
-    const double base = f.dlrad[p] + (1.0 - (double)f.frac_veg_nosno[p]) * eg * forc;
+    const S base = f.dlrad[p] + (1.0 - (double)f.frac_veg_nosno[p]) * eg * forc;
     if (act && !f.lun_urbpoi[f.patch_landunit[p] - 1]) {
-      const double gnet = f.sabg[p] + base - lwrad_emit - (f.eflx_sh_grnd[p] + f.qflx_evap_soi[p] * htvp);
-      f.eflx_gnet[p] = gnet;
+      const S gnet = f.sabg[p] + base - lwrad_emit - (f.eflx_sh_grnd[p] + f.qflx_evap_soi[p] * htvp);
+      f.eflx_gnet[p] = VAL(gnet);
       f.sabg_chk[p] = fse * f.sabg_snow[p] + (1.0 - fse) * f.sabg_soil[p];
-      const double dg = -f.cgrnd[p] - dlwrad_emit;
-      f.dgnetdT[p] = dg;
+      const S dg = -f.cgrnd[p] - dlwrad_emit;
+      f.dgnetdT[p] = VAL(dg);
       const double wt = f.patch_wtcol[p];
-      const double gsoil = f.sabg_soil[p] + base - lwrad_emit_soil - (f.eflx_sh_soil[p] + f.qflx_ev_soil[p] * htvp);
-      const double gh2o = f.sabg_soil[p] + base - lwrad_emit_h2osfc - (f.eflx_sh_h2osfc[p] + f.qflx_ev_h2osfc[p] * htvp);
-      const bool wnz = wt != 0.0;
-      dh_p = wnz ? dg * wt : 0.0;
-      hsoil_p = wnz ? gsoil * wt : 0.0;
-      hh_p = wnz ? gh2o * wt : 0.0;
+      const S gsoil = f.sabg_soil[p] + base - lwrad_emit_soil - (f.eflx_sh_soil[p] + f.qflx_ev_soil[p] * htvp);
+      const S gh2o = f.sabg_soil[p] + base - lwrad_emit_h2osfc - (f.eflx_sh_h2osfc[p] + f.qflx_ev_h2osfc[p] * htvp);
+      if (wt != 0.0) {
+        dh_p = dg * wt;
+        hsoil_p = gsoil * wt;
+        hh_p = gh2o * wt;
+      }
     }
     dhsdT += dh_p; hs_soil += hsoil_p; hs_h2osfc += hh_p;
     if (act) {   // SNICAR top-layer flux + per-layer solar (:1139-1167)
       const double wt = f.patch_wtcol[p];
       const double sab = LVc(f.sabg_lyr, p, jtop + joff, ldp);
-      const double gsnow = sab + base - lwrad_emit_snow - (f.eflx_sh_snow[p] + f.qflx_ev_snow[p] * htvp);
+      const S gsnow = sab + base - lwrad_emit_snow - (f.eflx_sh_snow[p] + f.qflx_ev_snow[p] * htvp);
       hs_top_snow += gsnow * wt;
       for (int j = jtop; j <= 1; j++) sabg_lyr_col[j + nlevsno] += LVc(f.sabg_lyr, p, j + joff, ldp) * wt;
     }
@@ -623,8 +745,8 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   //      r = 0 is the top active layer; the surface-water row sits between the
   //      snow layers and soil layer 1), ab[r][d] = A[r, r-2+d] ----
   constexpr int W = 7;
-  double ab[MAXROWS * W];
-  double x[MAXROWS];
+  S ab[MAXROWS * W];
+  S x[MAXROWS];
   const int n = nlevgrnd - (int)snl + 1;
   const int rsw = -(int)snl;              // row of the surface-water equation
   const double omc = 1.0 - CNFAC;
@@ -633,7 +755,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   for (int j = jtop; j <= 0; j++) {
     const int jj = j + joff;
     const int r = j - jtop;
-    const double fc = fct[jj];
+    const S fc = fct[jj];
     const double dzp = zz[jj + 1] - zz[jj];
     if (j == jtop) {
       x[r] = tt[jj] + fc * (hs_top_snow - dhsdT * tt[jj] + CNFAC * fn[jj]);
@@ -649,11 +771,11 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     else ab[r * W + 4] = -omc * fc * tk[jj] / dzp;   // snow-soil coupling skips the h2osfc row
   }
   // surface-water row
-  double fn_h2osfc;
+  S fn_h2osfc;
   {
     const double dzm = 0.5 * dz_h2osfc + zz[1 + joff];
-    const double th = f.t_h2osfc[c];
-    const double fnh = tk_h2osfc * (tt[1 + joff] - th) / dzm;
+    const S th = X.Th2osfc();
+    const S fnh = tk_h2osfc * (tt[1 + joff] - th) / dzm;
     fn_h2osfc = fnh;
     x[rsw] = th + (dtime / ch) * (hs_h2osfc - dhsdT * th + CNFAC * fnh);
     ab[rsw * W + 2] = 1.0 + omc * (dtime / ch) * tk_h2osfc / dzm - (dtime / ch) * dhsdT;
@@ -663,8 +785,8 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   for (int j = 1; j <= nlevgrnd; j++) {
     const int jj = j + joff;
     const int r = rsw + j;
-    const double fc = fct[jj];
-    const double t0 = tt[jj];
+    const S fc = fct[jj];
+    const S t0 = tt[jj];
     if (j == jtop) {   // snl == 0
       const double dzp = zz[jj + 1] - zz[jj];
       x[r] = t0 + fc * (hs_top_snow - dhsdT * t0 + CNFAC * fn[jj]);
@@ -695,7 +817,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   if (fh != 0.0) {   // surface-water corrections to soil layer 1 (:1480-1494, :1689-1707)
     const int jj = 1 + joff;
     const int r = rsw + 1;
-    const double fc = fct[jj];
+    const S fc = fct[jj];
     x[r] -= fh * fc * ((hs_soil - dhsdT * tt[jj]) + CNFAC * fn_h2osfc);
     const double dzm = 0.5 * dz_h2osfc + zz[1 + joff];
     ab[r * W + 2] += fh * (omc * fc * tk_h2osfc / dzm + fc * dhsdT);
@@ -711,9 +833,9 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   // ---- _tvector_extract_kernel! (:149-167) ----
   for (int j = jtop; j <= 0; j++) tt[j + joff] = x[j - jtop];
   for (int j = 1; j <= nlevgrnd; j++) tt[j + joff] = x[rsw + j];
-  for (int jj = jjtop; jj <= nlev; jj++) LV(T, c, jj, ld) = tt[jj];
-  if (fh == 0.0) f.t_h2osfc[c] = tt[1 + joff];
-  else f.t_h2osfc[c] = x[rsw];
+  for (int jj = jjtop; jj <= nlev; jj++) X.T(jj) = tt[jj];
+  if (fh == 0.0) X.Th2osfc() = tt[1 + joff];
+  else X.Th2osfc() = x[rsw];
 
   // ---- _fn1_kernel! (:170-206) and _eflx_fgr_kernel! (:250-269) ----
   const bool issoilcrop = (lit == ISTSOIL || lit == ISTCROP);
@@ -722,52 +844,66 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     for (int jj = jjtop; jj <= nlev; jj++) {
       const int j = jj - nlevsno;
       double fn1v;
-      if (j <= nlevgrnd - 1) fn1v = tk[jj] * (tt[jj + 1] - tt[jj]) / (zz[jj + 1] - zz[jj]);
+      if (j <= nlevgrnd - 1) fn1v = VAL(tk[jj]) * (VAL(tt[jj + 1]) - VAL(tt[jj])) / (zz[jj + 1] - zz[jj]);
       else fn1v = 0.0;
-      if (j == 1) f.eflx_fgr12[c] = -CNFAC * fn[jj] - (1.0 - CNFAC) * fn1v;
-      if (j >= 1 && j < nlevgrnd && issoilcrop) LV(f.eflx_fgr, c, j, ld) = -CNFAC * fn[jj] - (1.0 - CNFAC) * fn1v;
+      if (j == 1) f.eflx_fgr12[c] = -CNFAC * VAL(fn[jj]) - (1.0 - CNFAC) * fn1v;
+      if (j >= 1 && j < nlevgrnd && issoilcrop) LV(f.eflx_fgr, c, j, ld) = -CNFAC * VAL(fn[jj]) - (1.0 - CNFAC) * fn1v;
       else if (j == nlevgrnd && issoilcrop) LV(f.eflx_fgr, c, j, ld) = 0.0;
     }
   }
 
   // ---- phase change (:552-561) ----
-  phase_change_h2osfc_col(D, f, c, dtime, dhsdT);
-  phase_change_beta_col(D, f, c, dtime, dhsdT);
+  phase_change_h2osfc_col(D, f, c, dtime, dhsdT, X);
+  phase_change_beta_col(D, f, c, dtime, dhsdT, X);
 
   // ---- _tgrnd_kernel! (:224-247) ----
   {
-    const double t1 = LV(T, c, 1 + joff, ld), th = f.t_h2osfc[c];
-    double tgn;
+    const S t1 = X.T(1 + joff), th = X.Th2osfc();
+    S tgn;
     if (snl < 0) {
-      const double ts = LV(T, c, jjtop, ld);
+      const S ts = X.T(jjtop);
       if (fh != 0.0) tgn = fse * ts + (1.0 - fse - fh) * t1 + fh * th;
       else tgn = fse * ts + (1.0 - fse) * t1;
     } else {
       if (fh != 0.0) tgn = (1.0 - fh) * t1 + fh * th;
       else tgn = t1;
     }
-    f.t_grnd[c] = tgn;
+    X.Tgrnd() = tgn;
   }
   uint32_t status = 0;
   for (int jj = jjtop; jj <= nlev; jj++)
-    if (!isfinite(LV(T, c, jj, ld))) status |= CLMGB_COL_NONFINITE;
+    if (!isfinite(VAL(X.T(jj)))) status |= CLMGB_COL_NONFINITE;
   return status;
+}
+
+__device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soiltemp_fields& f, int64_t c,
+                                                double dtime, int snow_method) {
+  FieldState<clmgb_soiltemp_fields> X(f, c, D.ldc);
+  return soil_temperature_col(D, f, c, dtime, snow_method, X);
 }
 
 // ===========================================================================
 // set_soil_water_fractions! kernel (soil_hydrology.jl:110-130), column c.
 // ===========================================================================
-__device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_soilwater_fields& f, int64_t c) {
+template <class ST>
+__device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_soilwater_fields& f, int64_t c,
+                                                    ST& X) {
+  typedef typename ST::S S;
   const int64_t ld = D.ldc;
   const int joff = D.nlevsno;
   for (int j = 1; j <= D.nlevsoi; j++) {
     const double exi = LV(f.excess_ice, c, j, ld);
     const double dz_ext = LVc(f.dz, c, j + joff, ld) + exi / DENICE;
-    const double ws = LVc(f.watsat, c, j, ld);
-    const double vol_ice = jl_min(ws, (LV(f.h2osoi_ice, c, j + joff, ld) + exi) / (dz_ext * DENICE));
-    LV(f.eff_porosity, c, j, ld) = jl_max(0.01, ws - vol_ice);
-    LV(f.icefrac, c, j, ld) = jl_min(1.0, vol_ice / ws);
+    const S ws = X.Watsat(j);
+    const S vol_ice = jl_min(ws, (X.Ice(j + joff) + exi) / (dz_ext * DENICE));
+    LV(f.eff_porosity, c, j, ld) = jl_max(0.01, VAL(ws) - VAL(vol_ice));
+    X.Icefrac(j) = jl_min(1.0, vol_ice / ws);
   }
+}
+
+__device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_soilwater_fields& f, int64_t c) {
+  FieldState<clmgb_soilwater_fields> X(f, c, D.ldc);
+  water_fractions_col(D, f, c, X);
 }
 
 // ===========================================================================
@@ -785,34 +921,45 @@ __device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_s
 //  * dt_dz = dtsub/(1000*dz): when dtsub is halved or doubled the quotient scales
 //    by exactly the same power of two, so it is rescaled through its exponent bits
 //    instead of divided again; any other change of dtsub divides afresh.
+// The accept/reject test and the error estimate only decide the substep schedule,
+// so they are formed from the values of the active quantities.
 // ===========================================================================
-struct MfLane {
+template <class S>
+struct MfLaneT {
   int64_t c;
   int nlayers;
   int nsub;
   bool fresh;
   uint32_t status;
-  double dtsub, dtdone, qc, dt_cur;
-  double liq[MAXSOI + 1], dzv[MAXSOI + 1], imp[MAXSOI + 1];
-  double hk[MAXSOI + 1], dhkdw[MAXSOI + 1];
-  double qin[MAXSOI + 1], qout[MAXSOI + 1], dqidw0[MAXSOI + 1], dqidw1[MAXSOI + 1];
-  double dqodw1[MAXSOI + 1], dqodw2[MAXSOI + 1], fnet1[MAXSOI + 1];
-  double gam[MAXSOI + 1], dwat[MAXSOI + 1], dt_dz[MAXSOI + 1];
+  double dtsub, dtdone, dt_cur;
+  S qc;
+  double dzv[MAXSOI + 1], dt_dz[MAXSOI + 1];
+  S liq[MAXSOI + 1], imp[MAXSOI + 1];
+  S hk[MAXSOI + 1], dhkdw[MAXSOI + 1];
+  S qin[MAXSOI + 1], qout[MAXSOI + 1], dqidw0[MAXSOI + 1], dqidw1[MAXSOI + 1];
+  S dqodw1[MAXSOI + 1], dqodw2[MAXSOI + 1], fnet1[MAXSOI + 1];
+  S gam[MAXSOI + 1], dwat[MAXSOI + 1];
 };
+typedef MfLaneT<double> MfLane;
 
 // Ice impedance 10^(-e_ice*icefrac) of layer j (interface mean above the bottom
 // layer), as formed at soil_water_movement.jl:1287-1293.
+template <class ST>
+__device__ __forceinline__ typename ST::S mf_impedance(double e_ice, int j, int nlayers, ST& X) {
+  if (j == nlayers) return cm_pow(10.0, -e_ice * X.Icefrac(j));
+  return cm_pow(10.0, -e_ice * (0.5 * (X.Icefrac(j) + X.Icefrac(j + 1))));
+}
 __device__ __forceinline__ double mf_impedance(const Dims& D, const clmgb_soilwater_fields& f, double e_ice,
                                                int64_t c, int j, int nlayers) {
-  const int64_t ld = D.ldc;
-  if (j == nlayers) return cm_pow(10.0, -e_ice * LV(f.icefrac, c, j, ld));
-  return cm_pow(10.0, -e_ice * (0.5 * (LV(f.icefrac, c, j, ld) + LV(f.icefrac, c, j + 1, ld))));
+  FieldState<clmgb_soilwater_fields> X(f, c, D.ldc);
+  return mf_impedance(e_ice, j, nlayers, X);
 }
 
 // returns false (and sets L.status) when the column cannot be solved.  imp_cache,
 // when given, holds the impedances formed by k_impedance ([nlevsoi, ld_imp]).
-__device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
-                                         const clmgb_swm_config& cfg, double dtime, int64_t c,
+template <class ST>
+__device__ __forceinline__ bool mf_begin(MfLaneT<typename ST::S>& L, const Dims& D, const clmgb_soilwater_fields& f,
+                                         const clmgb_swm_config& cfg, double dtime, int64_t c, ST& X,
                                          const double* imp_cache = nullptr, int64_t ld_imp = 0) {
   const int64_t ld = D.ldc;
   const int joff = D.nlevsno;
@@ -826,13 +973,13 @@ __device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_s
   const int nlayers = (int)nl;
   L.nlayers = nlayers;
   for (int j = 1; j <= nlayers; j++) {
-    L.liq[j] = LV(f.h2osoi_liq, c, joff + j, ld);
+    L.liq[j] = X.Liq(joff + j);
     L.dzv[j] = LVc(f.dz, c, joff + j, ld);
   }
   if (imp_cache) {
     for (int j = 1; j <= nlayers; j++) L.imp[j] = imp_cache[(int64_t)(j - 1) * ld_imp + c];
   } else {
-    for (int j = 1; j <= nlayers; j++) L.imp[j] = mf_impedance(D, f, cfg.e_ice, c, j, nlayers);
+    for (int j = 1; j <= nlayers; j++) L.imp[j] = mf_impedance(cfg.e_ice, j, nlayers, X);
   }
   L.nsub = 0;
   L.dtsub = dtime;
@@ -844,8 +991,11 @@ __device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_s
 }
 
 // one attempt; returns true when the column's substep loop has finished
-__device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
-                                           const clmgb_swm_config& cfg, double dtime) {
+template <class ST>
+__device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dims& D,
+                                           const clmgb_soilwater_fields& f, const clmgb_swm_config& cfg,
+                                           double dtime, ST& X) {
+  typedef typename ST::S S;
   const int64_t ld = D.ldc;
   const int64_t c = L.c;
   const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
@@ -879,30 +1029,30 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
   }
   if (L.fresh) {
     // ---- hydraulic properties (Clapp-Hornberger inlined, :1280-1308) ----
-    double s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
+    S s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
     for (int j = 1; j <= nlayers; j++) {
-      const double vwc = jl_max(L.liq[j], 1.0e-6) / (L.dzv[j] * DENH2O);
-      double s = vwc / LVc(f.watsat, c, j, ld);
+      const S vwc = jl_max(L.liq[j], 1.0e-6) / (L.dzv[j] * DENH2O);
+      S s = vwc / X.Watsat(j);
       s = jl_min(s, 1.0);
       s = jl_max(0.01, s);
       s2[j] = s;
     }
     for (int j = 1; j <= nlayers; j++) {
-      double s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
+      S s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
       s1 = jl_min(s1, 1.0);
       s1 = jl_max(0.01, s1);
-      const double b = LVc(f.bsw, c, j, ld);
-      const double hkv = L.imp[j] * LVc(f.hksat, c, j, ld) * cm_pow(s1, 2.0 * b + 3.0);
-      const double dhkds = (2.0 * b + 3.0) * hkv / s1;
-      const double sn = s2[j];
-      const double smpv = -LVc(f.sucsat, c, j, ld) * cm_pow(sn, -b);
-      const double dsmpds = -b * smpv / sn;
+      const S b = X.Bsw(j);
+      const S hkv = L.imp[j] * X.Hksat(j) * cm_pow(s1, 2.0 * b + 3.0);
+      const S dhkds = (2.0 * b + 3.0) * hkv / s1;
+      const S sn = s2[j];
+      const S smpv = -X.Sucsat(j) * cm_pow(sn, -b);
+      const S dsmpds = -b * smpv / sn;
       L.hk[j] = hkv;
       smp[j] = smpv;
       L.dhkdw[j] = dhkds;
-      dsmpdw[j] = dsmpds / LVc(f.watsat, c, j, ld);
-      LV(f.smp_l, c, j, ld) = smpv;
-      LV(f.hk_l, c, j, ld) = hkv;
+      dsmpdw[j] = dsmpds / X.Watsat(j);
+      LV(f.smp_l, c, j, ld) = VAL(smpv);
+      LV(f.hk_l, c, j, ld) = VAL(hkv);
     }
     // ---- fluxes and derivatives (:1310-1378) ----
     for (int j = 1; j <= nlayers; j++) {
@@ -910,9 +1060,9 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
       L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
     }
     for (int j = 1; j <= nlayers - 1; j++) {
-      const double dhkds1 = 0.5 * L.dhkdw[j] / LVc(f.watsat, c, j, ld);
-      const double dhkds2 = 0.5 * L.dhkdw[j] / LVc(f.watsat, c, j + 1, ld);
-      const double num = smp[j + 1] - smp[j];
+      const S dhkds1 = 0.5 * L.dhkdw[j] / X.Watsat(j);
+      const S dhkds2 = 0.5 * L.dhkdw[j] / X.Watsat(j + 1);
+      const S num = smp[j + 1] - smp[j];
       const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
       L.qout[j] = -L.hk[j] * num / den + L.hk[j];
       L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1 * num) / den + dhkds1;
@@ -928,8 +1078,8 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
         if (j > jwt) {
           L.qout[j] = 0.0; L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
         } else {
-          const double dhkds1l = L.dhkdw[j] / LVc(f.watsat, c, j, ld);
-          const double num = -smp[j];
+          const S dhkds1l = L.dhkdw[j] / X.Watsat(j);
+          const S num = -smp[j];
           const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
           L.qout[j] = -L.hk[j] * num / den + L.hk[j];
           L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1l * num) / den + dhkds1l;
@@ -937,7 +1087,7 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
         }
       } else if (lower_bc == CLMGB_BC_FLUX) {
         L.qout[j] = L.hk[j];
-        L.dqodw1[j] = L.dhkdw[j] / LVc(f.watsat, c, j, ld);
+        L.dqodw1[j] = L.dhkdw[j] / X.Watsat(j);
       } else {
         L.qout[j] = 0.0;
         L.dqodw1[j] = 0.0;
@@ -954,30 +1104,31 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
     L.fresh = false;
   }
   // ---- RHS / LHS (:1380-1397) fused into the Thomas forward sweep (:1421-1438) ----
-  double bet, dwat_prev;
+  S bet, dwat_prev;
   {
-    const double rmx = -L.fnet1[1] * L.dt_dz[1];
-    const double bmx = -1.0 - (-L.dqidw1[1] + L.dqodw1[1]) * L.dt_dz[1];
+    const S rmx = -L.fnet1[1] * L.dt_dz[1];
+    const S bmx = -1.0 - (-L.dqidw1[1] + L.dqodw1[1]) * L.dt_dz[1];
     bet = bmx;
-    if (abs_lt(bet, 1.0e-30)) bet = 1.0e-30;
+    if (abs_lt(VAL(bet), 1.0e-30)) bet = 1.0e-30;
     dwat_prev = rmx / bet;
     L.dwat[1] = dwat_prev;
   }
-  double cmx_prev = -L.dqodw2[1] * L.dt_dz[1];
+  S cmx_prev = -L.dqodw2[1] * L.dt_dz[1];
   for (int j = 2; j <= nlayers; j++) {
-    const double amx = L.dqidw0[j] * L.dt_dz[j];
-    const double bmx = -1.0 - (-L.dqidw1[j] + L.dqodw1[j]) * L.dt_dz[j];
-    const double cmx = (j == nlayers) ? 0.0 : -L.dqodw2[j] * L.dt_dz[j];
-    const double rmx = -L.fnet1[j] * L.dt_dz[j];
+    const S amx = L.dqidw0[j] * L.dt_dz[j];
+    const S bmx = -1.0 - (-L.dqidw1[j] + L.dqodw1[j]) * L.dt_dz[j];
+    S cmx = 0.0;
+    if (j != nlayers) cmx = -L.dqodw2[j] * L.dt_dz[j];
+    const S rmx = -L.fnet1[j] * L.dt_dz[j];
     L.gam[j] = cmx_prev / bet;
     bet = bmx - amx * L.gam[j];
-    if (abs_lt(bet, 1.0e-30)) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
+    if (abs_lt(VAL(bet), 1.0e-30)) bet = copysign(1.0e-30, VAL(bet) == 0.0 ? 1.0 : VAL(bet));
     dwat_prev = (rmx - amx * dwat_prev) / bet;
     L.dwat[j] = dwat_prev;
     cmx_prev = cmx;
   }
   {
-    double dwat_next = dwat_prev;
+    S dwat_next = dwat_prev;
     for (int j = nlayers - 1; j >= 1; j--) {
       dwat_next = L.dwat[j] - L.gam[j + 1] * dwat_next;
       L.dwat[j] = dwat_next;
@@ -989,15 +1140,17 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
   for (int j = 1; j <= nlayers; j++) {
     double fnet0;
     if (expensive) {
-      const double qin_test = j == 1 ? L.qin[j] + L.dqidw1[j] * L.dwat[j]
-                                     : L.qin[j] + L.dqidw0[j] * L.dwat[j - 1] + L.dqidw1[j] * L.dwat[j];
-      const double qout_test = j == nlayers ? L.qout[j] + L.dqodw1[j] * L.dwat[j]
-                                            : L.qout[j] + L.dqodw1[j] * L.dwat[j] + L.dqodw2[j] * L.dwat[j + 1];
+      const double qin_test = j == 1 ? VAL(L.qin[j]) + VAL(L.dqidw1[j]) * VAL(L.dwat[j])
+                                     : VAL(L.qin[j]) + VAL(L.dqidw0[j]) * VAL(L.dwat[j - 1]) +
+                                           VAL(L.dqidw1[j]) * VAL(L.dwat[j]);
+      const double qout_test = j == nlayers ? VAL(L.qout[j]) + VAL(L.dqodw1[j]) * VAL(L.dwat[j])
+                                            : VAL(L.qout[j]) + VAL(L.dqodw1[j]) * VAL(L.dwat[j]) +
+                                                  VAL(L.dqodw2[j]) * VAL(L.dwat[j + 1]);
       fnet0 = qin_test - qout_test - LVc(f.qflx_rootsoi, c, j, ld);
     } else {
-      fnet0 = L.dwat[j] / L.dt_dz[j];
+      fnet0 = VAL(L.dwat[j]) / L.dt_dz[j];
     }
-    const double ev = fabs(L.fnet1[j] - fnet0) * dtsub * 0.5;
+    const double ev = fabs(VAL(L.fnet1[j]) - fnet0) * dtsub * 0.5;
     errorMax = jl_max(errorMax, ev);
   }
   // ---- reject (:1460-1463) ----
@@ -1008,7 +1161,7 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
   // ---- accept (:1466-1483) ----
   for (int j = 1; j <= nlayers; j++) L.liq[j] = L.liq[j] + L.dwat[j] * (M_TO_MM * L.dzv[j]);
   L.fresh = true;
-  double qcTemp;
+  S qcTemp;
   if (lower_bc == CLMGB_BC_FLUX) qcTemp = L.hk[nlayers] + L.dhkdw[nlayers] * L.dwat[nlayers];
   else if (lower_bc == CLMGB_BC_ZERO_FLUX) qcTemp = 0.0;
   else qcTemp = L.qout[nlayers] + L.dqodw1[nlayers] * L.dwat[nlayers];
@@ -1021,28 +1174,52 @@ __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb
   return false;
 }
 
-__device__ __forceinline__ uint32_t mf_end(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f) {
-  const int64_t ld = D.ldc;
+template <class ST>
+__device__ __forceinline__ uint32_t mf_end(MfLaneT<typename ST::S>& L, const Dims& D,
+                                           const clmgb_soilwater_fields& f, ST& X) {
   const int64_t c = L.c;
   const int joff = D.nlevsno;
   uint32_t status = L.status;
   for (int j = 1; j <= L.nlayers; j++) {
-    LV(f.h2osoi_liq, c, joff + j, ld) = L.liq[j];
-    if (!isfinite(L.liq[j])) status |= CLMGB_COL_NONFINITE;
+    X.Liq(joff + j) = L.liq[j];
+    if (!isfinite(VAL(L.liq[j]))) status |= CLMGB_COL_NONFINITE;
   }
-  f.qcharge[c] = L.qc;
+  X.Qcharge() = L.qc;
   f.num_substeps[c] = (double)L.nsub;
   return status;
 }
 
+// production forms: the column's state in the caller's fields
+__device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
+                                         const clmgb_swm_config& cfg, double dtime, int64_t c,
+                                         const double* imp_cache = nullptr, int64_t ld_imp = 0) {
+  FieldState<clmgb_soilwater_fields> X(f, c, D.ldc);
+  return mf_begin(L, D, f, cfg, dtime, c, X, imp_cache, ld_imp);
+}
+__device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
+                                           const clmgb_swm_config& cfg, double dtime) {
+  FieldState<clmgb_soilwater_fields> X(f, L.c, D.ldc);
+  return mf_attempt(L, D, f, cfg, dtime, X);
+}
+__device__ __forceinline__ uint32_t mf_end(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f) {
+  FieldState<clmgb_soilwater_fields> X(f, L.c, D.ldc);
+  return mf_end(L, D, f, X);
+}
+
 // The whole substep loop for one column (one thread, one column).
+template <class ST>
+__device__ inline uint32_t moisture_form_col(const Dims& D, const clmgb_soilwater_fields& f,
+                                             const clmgb_swm_config& cfg, double dtime, int64_t c, ST& X) {
+  MfLaneT<typename ST::S> L;
+  if (!mf_begin(L, D, f, cfg, dtime, c, X)) return L.status;
+  while (!mf_attempt(L, D, f, cfg, dtime, X)) {
+  }
+  return mf_end(L, D, f, X);
+}
 __device__ inline uint32_t moisture_form_col(const Dims& D, const clmgb_soilwater_fields& f,
                                              const clmgb_swm_config& cfg, double dtime, int64_t c) {
-  MfLane L;
-  if (!mf_begin(L, D, f, cfg, dtime, c)) return L.status;
-  while (!mf_attempt(L, D, f, cfg, dtime)) {
-  }
-  return mf_end(L, D, f);
+  FieldState<clmgb_soilwater_fields> X(f, c, D.ldc);
+  return moisture_form_col(D, f, cfg, dtime, c, X);
 }
 
 }  // namespace clmgb

@@ -33,6 +33,16 @@ struct WaveScratch {
   unsigned int* counters;
 };
 
+// Tape of the column-step adjoint (adjoint_step.cu): slots x entries records.
+struct AdjTape {
+  int2* idx;
+  double2* par;
+  double* adj;
+  double* sub;
+  int64_t slots, entries, maxsub;
+  unsigned int* max_used;
+};
+
 // All launchers return the cudaError_t of the launch (cudaGetLastError()).
 cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
                                     int snow_method, uint32_t* col_status, uint32_t* dev_status,
@@ -75,6 +85,11 @@ cudaError_t launch_moisture_form_waves(const Dims& D, int64_t nc, const clmgb_so
                                        int or_status, uint32_t* dev_status, const WaveScratch& w, int grid_blocks,
                                        cudaStream_t s);
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s);
+cudaError_t launch_column_step_vjp(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                                   const clmgb_soilwater_fields& fw, const clmgb_swm_config& cfg, double dtime,
+                                   int snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                                   const clmgb_step_adjoint& adj, const AdjTape& tp, uint32_t* col_status,
+                                   uint32_t* dev_status, cudaStream_t s);
 cudaError_t launch_band_factor_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const double* bmatrix,
                                      const double* rvector, const int64_t* jtop, const int64_t* jbot,
                                      const uint8_t* mask, int kl, int ku, int nlevsno_off, double* lu, uint8_t* piv,

@@ -56,6 +56,13 @@ extern "C" {
 #define CLMGB_COL_NONFINITE      4u  /* a non-finite temperature / water value was produced */
 #define CLMGB_COL_LEVEL_RANGE    8u  /* snl / nbedrock outside the level range */
 #define CLMGB_COL_PATCH_RANGE   16u  /* patchi/patchf outside 1..np */
+#define CLMGB_COL_ADJ_UNSUPPORTED 32u /* step adjoint: the column holds state the adjoint treats as
+                                        constant (frac_h2osfc > 0, excess ice, snow without layers) */
+#define CLMGB_COL_TAPE_FULL     64u  /* step adjoint: the column's tape (or its substep checkpoints)
+                                        overflowed; its adjoints are not computed (raise the entries
+                                        of clmgb_reserve_adjoint) */
+#define CLMGB_COL_ADJ_REPLAY   128u  /* step adjoint: a replayed substep was not accepted again
+                                        (its adjoint is not valid) */
 
 /* ---- compile-time limits of this build ---- */
 #define CLMGB_MAX_NLEVSNO   12
@@ -262,6 +269,10 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
 #define CLMGB_OPT_RESERVED_COLUMNS     6  /* read-only: columns covered by clmgb_reserve */
 #define CLMGB_OPT_WAVES_BLOCKS_PER_SM  7  /* co-resident blocks per SM of the wave kernel (0 = occupancy limit) */
 #define CLMGB_OPT_WAVES_OCCUPANCY      8  /* read-only: occupancy limit of the wave kernel (0 = unavailable) */
+#define CLMGB_OPT_ADJ_TAPE_USED        9  /* read-only (synchronises): most tape entries one column used in
+                                             clmgb_column_step_vjp since clmgb_reserve_adjoint */
+#define CLMGB_OPT_ADJ_TAPE_SLOTS      10  /* read-only: tape slots (concurrent columns) reserved */
+#define CLMGB_OPT_ADJ_TAPE_ENTRIES    11  /* read-only: tape entries per slot reserved */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
 /* Gives the handle per-column scratch for up to max_nc columns (about 48*nlevsoi + 80
  * bytes per column): the Richards solve then forms the ice impedances in a uniform
@@ -399,6 +410,54 @@ int32_t clmgb_tridiagonal_adjoint(clmgb_handle h, int64_t ncols, int64_t ldc, in
                                   const double* u, const double* a, const double* b, const double* c,
                                   double* u_bar, double* a_bar, double* b_bar, double* c_bar,
                                   double* r_bar, const int64_t* jtop, const uint8_t* mask, void* stream);
+
+/* ---- reverse mode through a whole column step ---- */
+
+/* Adjoints of one column step (clmgb_column_step), all device pointers in the
+ * layouts of the fields they belong to.  lam_* hold, on entry, the adjoints of the
+ * step's OUTPUTS (the state after the step) and, on return, the adjoints of its
+ * INPUTS (the state before it): the adjoint threaded backwards through a trajectory
+ * as _reverse_step_into! (canopy_fluxes_reverse.jl:447-465) threads Enzyme's shadow.
+ * lam_qcharge (may be NULL) is the adjoint of the step's qcharge output.  grad_*
+ * ([ldc, nlevsoi], may be NULL) accumulate (+=) the adjoints of the hydraulic
+ * parameters watsat, bsw, sucsat, hksat of levels 1..nlevsoi.  Levels above the top
+ * active snow layer are left unchanged (the step does not touch them). */
+typedef struct clmgb_step_adjoint {
+  int64_t struct_size;               /* sizeof(clmgb_step_adjoint) */
+  double* lam_t_soisno;              /* [ldc, nlevsno+nlevmaxurbgrnd] */
+  double* lam_h2osoi_liq;            /* [ldc, nlevsno+nlevmaxurbgrnd] */
+  double* lam_h2osoi_ice;            /* [ldc, nlevsno+nlevmaxurbgrnd] */
+  double* lam_t_grnd;                /* [nc] */
+  double* lam_t_h2osfc;              /* [nc] */
+  const double* lam_qcharge;         /* [nc] */
+  double* grad_watsat;               /* [ldc, nlevsoi] */
+  double* grad_bsw;
+  double* grad_sucsat;
+  double* grad_hksat;
+  double* lam_forc_lwrad;            /* [nc] out (may be NULL): adjoint of the step's forc_lwrad input,
+                                        for callers whose forcing depends on the state */
+} clmgb_step_adjoint;
+
+/* Reserves the tape of clmgb_column_step_vjp: `slots` columns in flight (rounded up
+ * to a multiple of 64) with room for `entries` recorded operations each, plus the
+ * liquid-water checkpoints of up to CLMGB_ADJ_MAX_SUBSTEPS accepted Richards substeps
+ * per column: slots*(entries*32 + CLMGB_ADJ_MAX_SUBSTEPS*(CLMGB_MAX_NLEVSOI+2)*8) bytes.
+ * The tape holds soil_temperature! and one substep at a time (a few thousand entries
+ * per column).  Synchronises the device.  A column needing more is flagged
+ * CLMGB_COL_TAPE_FULL. */
+#define CLMGB_ADJ_MAX_SUBSTEPS 128
+int32_t clmgb_reserve_adjoint(clmgb_handle h, int64_t slots, int64_t entries);
+
+/* Reverse of one clmgb_column_step from the state it starts from (the fields hold
+ * the step's input state): replays the step (the state is left holding the step's
+ * output, as the forward call leaves it, bit for bit) and propagates adj (see
+ * clmgb_step_adjoint).  Needs clmgb_reserve_adjoint.  col_status gets the step's
+ * status bits plus CLMGB_COL_ADJ_UNSUPPORTED / CLMGB_COL_TAPE_FULL. */
+int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                              const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg,
+                              double dtime, int32_t snow_method, double* t_ssbef,
+                              double* t_h2osfc_bef, const clmgb_step_adjoint* adj,
+                              uint32_t* col_status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -38,6 +38,15 @@ def test_header_structs_match_ctypes():
     assert abi.header_struct_members(txt, "clmgb_varpar") == [f[0] for f in abi.Varpar._fields_]
     assert abi.header_struct_members(txt, "clmgb_bounds") == [f[0] for f in abi.Bounds._fields_]
     assert abi.header_struct_members(txt, "clmgb_swm_config") == [f[0] for f in abi.SwmConfig._fields_]
+    assert abi.header_struct_members(txt, "clmgb_step_adjoint") == [f[0] for f in abi.StepAdjoint._fields_]
+
+
+def test_header_constants_match_python():
+    txt = header_text()
+    consts = dict(re.findall(r"#define\s+CLMGB_(\w+)\s+(\d+)u?\b", txt))
+    for name in ("COL_ADJ_UNSUPPORTED", "COL_TAPE_FULL", "OPT_ADJ_TAPE_USED", "OPT_ADJ_TAPE_SLOTS",
+                 "OPT_ADJ_TAPE_ENTRIES", "OPT_STEP_SCHEDULE", "OPT_WAVES_OCCUPANCY"):
+        assert int(consts[name]) == getattr(abi, name), name
 
 
 def test_abi_version_and_errors():

@@ -199,3 +199,33 @@ def test_band_adjoint_vs_complex_step(pivot):
         for lv, bd in flat:
             touched[lv, bd] = True
         assert np.all(bbar[:, :, col][~touched] == 0.0)
+
+
+def test_complex_step_moisture_form_matches_oracle():
+    """The complex-step restatement used as the exact derivative reference reproduces
+    the oracle's moisture-form solve (real part) on the no-frost workload, where the
+    soil-temperature step leaves the water alone."""
+    from adjoint_reference import moisture_form
+    from clmgb import abi, synth
+    wl = synth.make_workload(0, nc=48, seed=31, nsteps=1)
+    st = wl.state
+    G, I = wl.forcing(0)
+    synth.apply_forcing_host(st, G, I)
+    cfg = abi.SwmConfig.clm5_default()
+    cfg.lower_boundary_condition = abi.BC_FLUX
+    ref = st.copy()
+    oracle.soil_water_fractions(ref)
+    oracle.soil_water(ref, wl.dtime, cfg)
+    joff = st.vp.nlevsno
+    worst = 0.0
+    for c in range(st.nc):
+        nl = int(st["col_nbedrock"][c])
+        lv = slice(joff, joff + nl)
+        liq, qc, _ = moisture_form(st["h2osoi_liq"][lv, c], st["dz"][lv, c], st["z"][lv, c],
+                                   st["watsat"][:nl, c], st["bsw"][:nl, c], st["sucsat"][:nl, c],
+                                   st["hksat"][:nl, c], np.ones(nl), st["qflx_infl"][c],
+                                   st["qflx_rootsoi"][:nl, c], wl.dtime, cfg, "flux")
+        worst = max(worst, np.max(np.abs(liq.real - ref["h2osoi_liq"][lv, c]) / np.abs(ref["h2osoi_liq"][lv, c])))
+        assert abs(qc.real - ref["qcharge"][c]) <= 1e-9 * max(abs(ref["qcharge"][c]), 1e-12)
+        assert np.all(liq.imag == 0.0)
+    assert worst < 1e-9, worst

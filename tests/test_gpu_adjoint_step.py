@@ -1,0 +1,306 @@
+"""GPU tests of the reverse mode through the column step (clmgb_column_step_vjp) and
+the checkpointed trajectory reverse (clmgb.adjoint).
+
+* The replay inside the adjoint is the production step: it leaves every field bit
+  for bit as clmgb_column_step does.
+* Gradients are checked against FP64 central finite differences with h = 1e-6
+  relative (the reference's own adjoint check, test_enzyme_smoke.jl:216-231, uses
+  central FD with the error measure max|g - fd| / max|fd| < 1e-6, per column here).
+  A difference quotient is only a derivative where it resolves one: a perturbation
+  can move a discrete decision (a substep accepted instead of rejected, a doubled
+  substep, a layer that starts to freeze), and a loss that hardly depends on a
+  parameter changes by less than its own rounding.  Entries whose quotients at
+  h and 2h disagree, or whose substep counts / phase flags change, are left out;
+  the tests require that the entries carrying the gradient are resolved and bound
+  the share left out.  A column whose loss residual y - target sits at the rounding
+  level of y is left out whole: its gradient is 2 (y - target) dy/dtheta with a
+  factor that each run rounds differently.
+* The moisture-form part is also checked against complex-step derivatives (exact
+  to rounding) of a numpy restatement.
+* The flat, every-k and bisection checkpoint schedules give the same bits.
+"""
+import numpy as np
+import pytest
+
+from clmgb import abi, adjoint, api, synth
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _cfg_flux():
+    cfg = abi.SwmConfig.clm5_default()
+    cfg.lower_boundary_condition = abi.BC_FLUX
+    return cfg
+
+
+@pytest.fixture(scope="module")
+def handle():
+    assert torch.cuda.is_available()
+    h = api.Handle(synth.clm5_varpar())
+    h.reserve_adjoint(4096, 8192)
+    yield h
+    h.close()
+
+
+def _workload_cfg(cfg_id, nc, nsteps, seed):
+    wl = synth.make_workload(cfg_id, nc=nc, seed=seed, nsteps=nsteps)
+    G, I = wl.forcing_block(range(nsteps))
+    return wl, torch.from_numpy(G).cuda(), torch.from_numpy(I).cuda()
+
+
+def _workload(nc, nsteps, seed=20241):
+    return _workload_cfg(1, nc, nsteps, seed)
+
+
+def _traj(h, wl, G, I, nsteps, cfg):
+    def forcing(t, st):
+        api.synth_forcing(h, st, G[t], I[t])
+    return adjoint.Trajectory(h, nsteps, wl.dtime, forcing, cfg, forcing_reverse=adjoint.synth_forcing_reverse)
+
+
+def test_replay_is_the_production_step(handle):
+    cfg = _cfg_flux()
+    wl, G, I = _workload(700, 6)
+    a = wl.state.to_device()
+    b = a.copy()
+    adj = adjoint.StepAdjointBuffers(a)
+    status = torch.zeros(a.nc, dtype=torch.int32, device="cuda")
+    for t in range(6):
+        api.synth_forcing(handle, a, G[t], I[t])
+        api.column_step(handle, a, wl.dtime, cfg)
+        api.synth_forcing(handle, b, G[t], I[t])
+        adj.zero_()
+        api.column_step_vjp(handle, b, wl.dtime, adj, cfg, col_status=status)
+        torch.cuda.synchronize()
+        for k in a.arrays:
+            assert torch.equal(a[k], b[k]), "step %d field %s" % (t, k)
+    st = status.cpu().numpy()
+    assert np.all((st & abi.COL_TAPE_FULL) == 0)
+    assert handle.get_option(abi.OPT_ADJ_TAPE_USED) > 1000
+
+
+def _params_and_decisions(traj, st0, loss, steps):
+    """Forward run: per-column loss plus the discrete record (substeps, imelt)."""
+    st = st0.copy()
+    loss.y = []
+    nsub, imelt = [], []
+    for t in range(steps):
+        traj.step(t, st)
+        loss.observe(t, st)
+        nsub.append(st["num_substeps"].clone())
+        imelt.append(st["imelt"].clone())
+    return loss.per_column(), torch.stack(nsub), torch.stack(imelt)
+
+
+def _fd_check(traj, st0, loss, steps, grads, params, tol):
+    """Central differences at h = 1e-6 and 1.37e-6 relative (steps that are not
+    commensurate, so a difference quantised to a few ulps of the loss cannot agree
+    with itself by accident).  An entry is resolved when the discrete record matches
+    the base run, the change of the loss is at least ~2e8 ulps of it, and the two
+    quotients agree to 1e-7.  Every resolved entry must satisfy
+    max|g - fd| <= tol * max|fd| over the resolved entries of its column."""
+    base_L, base_n, base_m = _params_and_decisions(traj, st0, loss, steps)
+    L0 = base_L.cpu().numpy()
+    # dL/dtheta = sum 2 (y - target) dy/dtheta: where |y - target| is at the rounding
+    # level of y, every run rounds it differently and no quotient can resolve it
+    Y = torch.stack(loss.y).cpu().numpy()
+    resid = np.abs(Y - loss.target.cpu().numpy()).max(0)
+    conditioned = resid >= 1e-6 * np.abs(Y).max(0)
+    nc = st0.nc
+    nsoi = st0.vp.nlevsoi
+    G, F1, F2, OK = [], [], [], []
+    for p in params:
+        for j in range(nsoi):
+            theta = st0[p][j].clone()
+            fds, same = [], torch.ones(nc, dtype=torch.bool, device="cuda")
+            dl = None
+            for rel in (1e-6, 1.37e-6):
+                h = rel * theta.abs()
+                res = []
+                for sgn in (1.0, -1.0):
+                    st = st0.copy()
+                    st[p][j] = theta + sgn * h
+                    res.append(_params_and_decisions(traj, st, loss, steps))
+                (Lp, np_, mp), (Lm, nm, mm) = res
+                same &= ((np_ == nm).all(0) & (np_ == base_n).all(0) &
+                         (mp == mm).all(0).all(0) & (mp == base_m).all(0).all(0))
+                fds.append(((Lp - Lm) / (2.0 * h)).cpu().numpy())
+                if dl is None:
+                    dl = (Lp - Lm).abs().cpu().numpy()
+            G.append(grads[p][j].cpu().numpy())
+            F1.append(fds[0])
+            F2.append(fds[1])
+            OK.append(same.cpu().numpy() & (dl >= 4e-8 * np.abs(L0)))
+    G, F1, F2, OK = (np.array(x) for x in (G, F1, F2, OK))     # [nparam, nc]
+    resolved = OK & (np.abs(F1 - F2) <= 1e-7 * np.abs(F1)) & conditioned[None, :]
+    scale = np.max(np.where(resolved, np.abs(F1), 0.0), axis=0)
+    err = np.where(resolved, np.abs(G - F1), 0.0) / np.maximum(scale, 1e-300)
+    rel = err.max(axis=0)
+    bad = np.where(rel > tol)[0]
+    if len(bad):
+        lines = []
+        for c in bad[:10]:
+            k = int(np.argmax(err[:, c]))
+            p, j = params[k // nsoi], k % nsoi + 1
+            lines.append("col %d %s[%d]: adj %.10e fd(h) %.10e fd(1.37h) %.10e scale %.3e" %
+                         (c, p, j, G[k, c], F1[k, c], F2[k, c], scale[c]))
+        raise AssertionError("%d columns above tol:\n" % len(bad) + "\n".join(lines))
+    # a quotient with h = 1e-6 resolves an entry only where the loss moves by enough
+    # ulps (relative sensitivity (theta/L) dL/dtheta above ~1e-2): require that the
+    # largest entry is checked in a good share of the columns
+    gbig = np.argmax(np.abs(G), axis=0)
+    top_resolved = resolved[gbig, np.arange(nc)][conditioned].mean()
+    assert top_resolved >= 0.4, top_resolved
+    return rel, resolved.mean(), top_resolved
+
+
+def test_one_step_gradient_vs_finite_differences(handle):
+    cfg = _cfg_flux()
+    wl, G, I = _workload(64, 1, seed=777)
+    traj = _traj(handle, wl, G, I, 1, cfg)
+    st0 = wl.state.to_device()
+    loss = adjoint.CalibrationLoss(st0, wl.dtime)
+    # target: the same model with perturbed parameters
+    pert = wl.state.copy()
+    adjoint.perturb_parameters(pert, np.random.default_rng(5))
+    tl = adjoint.CalibrationLoss(st0, wl.dtime)
+    _params_and_decisions(traj, pert.to_device(), tl, 1)
+    loss.target = torch.stack(tl.y)
+    st = st0.copy()
+    adj = adjoint.multistep_reverse(traj, st, loss.seed, loss.observe, checkpoint_every=1)
+    rel, frac, top = _fd_check(traj, st0, loss, 1, adj.grad, adjoint.PARAMS, 1e-6)
+    print("one step: max rel err %.3g over resolved entries (%.1f%% resolved, largest entry resolved in "
+          "%.0f%% of columns)" % (rel.max(), 100 * frac, 100 * top))
+
+
+def test_calibration_gradient_48_steps_vs_finite_differences(handle):
+    cfg = _cfg_flux()
+    nsteps = 48
+    wl, G, I = _workload(64, nsteps, seed=4242)
+    traj = _traj(handle, wl, G, I, nsteps, cfg)
+    st0 = wl.state.to_device()
+    pert = wl.state.copy()
+    adjoint.perturb_parameters(pert, np.random.default_rng(9))
+    tl = adjoint.CalibrationLoss(st0, wl.dtime)
+    _params_and_decisions(traj, pert.to_device(), tl, nsteps)
+    loss = adjoint.CalibrationLoss(st0, wl.dtime, torch.stack(tl.y))
+    st = st0.copy()
+    status = torch.zeros(st.nc, dtype=torch.int32, device="cuda")
+    adj = adjoint.multistep_reverse(traj, st, loss.seed, loss.observe, checkpoint_every=8, col_status=status)
+    assert int((status.cpu().numpy() & (abi.COL_TAPE_FULL | abi.COL_ADJ_UNSUPPORTED)).sum()) == 0
+    for p in adjoint.PARAMS:
+        assert torch.isfinite(adj.grad[p]).all()
+    rel, frac, top = _fd_check(traj, st0, loss, nsteps, adj.grad, adjoint.PARAMS, 1e-6)
+    print("48 steps: max rel err %.3g over resolved entries (%.1f%% resolved, largest entry resolved in "
+          "%.0f%% of columns)" % (rel.max(), 100 * frac, 100 * top))
+
+
+def test_richards_gradient_vs_complex_step(handle):
+    """Exact reference: the moisture-form solve restated in complex arithmetic
+    (tests/adjoint_reference.py, pinned to the oracle), differentiated by complex step
+    for every parameter of every level.  On the no-frost workload the soil-temperature
+    step leaves the water alone, so this is the whole step's gradient of the
+    calibration loss."""
+    from adjoint_reference import moisture_form
+    cfg = _cfg_flux()
+    nc = 16
+    wl, G, I = _workload_cfg(0, nc, 1, seed=1234)
+    traj = _traj(handle, wl, G, I, 1, cfg)
+    st0 = wl.state.to_device()
+    loss = adjoint.CalibrationLoss(st0, wl.dtime, torch.zeros((1, nc), dtype=torch.float64, device="cuda"))
+    st = st0.copy()
+    status = torch.zeros(nc, dtype=torch.int32, device="cuda")
+    adj = adjoint.multistep_reverse(traj, st, loss.seed, loss.observe, checkpoint_every=1, col_status=status)
+    assert int(status.cpu().numpy().sum()) == 0
+    h0 = wl.state
+    w = loss.w.cpu().numpy()
+    Ih = I.cpu().numpy()[0]
+    joff = h0.vp.nlevsno
+    nsoi = h0.vp.nlevsoi
+    worst = 0.0
+    for c in range(nc):
+        nl = int(h0["col_nbedrock"][c])
+        lv = slice(joff, joff + nl)
+        base = {p: h0[p][:nl, c].astype(complex) for p in adjoint.PARAMS}
+
+        def y_of(theta):
+            liq, qc, _ = moisture_form(h0["h2osoi_liq"][lv, c], h0["dz"][lv, c], h0["z"][lv, c],
+                                       theta["watsat"], theta["bsw"], theta["sucsat"], theta["hksat"],
+                                       np.ones(nl), Ih[c], h0["qflx_rootsoi"][:nl, c], wl.dtime, cfg, "flux")
+            y = qc * wl.dtime + np.sum(w[:nl, c] * (liq + h0["h2osoi_ice"][lv, c]))
+            return y * y
+        ref = np.zeros((len(adjoint.PARAMS), nsoi))
+        for k, p in enumerate(adjoint.PARAMS):
+            for j in range(nl):
+                th = {q: v.copy() for q, v in base.items()}
+                th[p][j] += 1e-30j
+                ref[k, j] = y_of(th).imag / 1e-30
+        got = np.array([adj.grad[p][:, c].cpu().numpy() for p in adjoint.PARAMS])
+        e = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        worst = max(worst, e)
+    print("complex-step: max rel err %.3g" % worst)
+    assert worst < 1e-9
+
+
+def test_checkpoint_schedules_give_the_same_bits(handle):
+    cfg = _cfg_flux()
+    nsteps = 13
+    wl, G, I = _workload(300, nsteps, seed=99)
+    traj = _traj(handle, wl, G, I, nsteps, cfg)
+    st0 = wl.state.to_device()
+    tgt = torch.zeros((nsteps, st0.nc), dtype=torch.float64, device="cuda")
+    outs = []
+    for sched in ("k1", "k8", "k5", "binomial"):
+        loss = adjoint.CalibrationLoss(st0, wl.dtime, tgt)
+        st = st0.copy()
+        if sched == "binomial":
+            peak = [0]
+            adj = adjoint.multistep_reverse_binomial(traj, st, loss.seed, loss.observe, peak=peak)
+            assert peak[0] <= 1 + int(np.ceil(np.log2(nsteps)))
+        else:
+            adj = adjoint.multistep_reverse(traj, st, loss.seed, loss.observe, checkpoint_every=int(sched[1:]))
+        outs.append((adj, st))
+    ref, ref_st = outs[0]
+    for adj, st in outs[1:]:
+        for p in adjoint.PARAMS:
+            assert torch.equal(adj.grad[p], ref.grad[p])
+        assert torch.equal(adj.lam_t_soisno, ref.lam_t_soisno)
+        assert torch.equal(adj.lam_h2osoi_liq, ref.lam_h2osoi_liq)
+        assert torch.equal(st["t_soisno"], ref_st["t_soisno"])
+
+
+def test_tape_overflow_and_unsupported_state_are_flagged():
+    h = api.Handle(synth.clm5_varpar())
+    try:
+        cfg = _cfg_flux()
+        wl, G, I = _workload(128, 1, seed=5)
+        st = wl.state.to_device()
+        st["frac_h2osfc"][3] = 0.2
+        st["h2osfc"][3] = 5.0
+        api.synth_forcing(h, st, G[0], I[0])
+        adj = adjoint.StepAdjointBuffers(st)
+        status = torch.zeros(st.nc, dtype=torch.int32, device="cuda")
+        h.reserve_adjoint(128, 256)
+        api.column_step_vjp(h, st.copy(), wl.dtime, adj, cfg, col_status=status)
+        s = status.cpu().numpy()
+        assert np.all(s & abi.COL_TAPE_FULL)
+        h.reserve_adjoint(128, 8192)
+        api.column_step_vjp(h, st.copy(), wl.dtime, adj, cfg, col_status=status)
+        s = status.cpu().numpy()
+        assert s[3] & abi.COL_ADJ_UNSUPPORTED
+        assert np.all((np.delete(s, 3) & (abi.COL_ADJ_UNSUPPORTED | abi.COL_TAPE_FULL)) == 0)
+    finally:
+        h.close()
+
+
+def test_vjp_requires_reserved_tape():
+    h = api.Handle(synth.clm5_varpar())
+    try:
+        wl, G, I = _workload(32, 1)
+        st = wl.state.to_device()
+        adj = adjoint.StepAdjointBuffers(st)
+        with pytest.raises(api.CLMGBError):
+            api.column_step_vjp(h, st, wl.dtime, adj)
+    finally:
+        h.close()
