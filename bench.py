@@ -54,6 +54,12 @@ def parse():
     ap.add_argument("--no-reserve", action="store_true", help="run without clmgb_reserve scratch")
     ap.add_argument("--queue-order", type=int, default=None)
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration leg")
+    ap.add_argument("--adj-nc", type=int, default=65536)
+    ap.add_argument("--adj-steps", type=int, default=48)
+    ap.add_argument("--adj-k", type=int, default=8, help="checkpoint every k steps")
+    ap.add_argument("--adj-slots", type=int, default=65536)
+    ap.add_argument("--adj-entries", type=int, default=8192)
     return ap.parse_args()
 
 
@@ -179,6 +185,84 @@ def run_reference(args):
                              "sample": "%d columns per step of the same workload" % nsample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def adjoint_leg(args):
+    """Calibration gradient: 65,536 columns of the snow / frozen-soil workload, 48 steps
+    of 1800 s, free-drainage lower boundary; loss sum_t (drainage + top-10 cm water -
+    target)^2 with the target from the same model with bsw, hksat, watsat, sucsat
+    perturbed by lognormal(0.2); gradient w.r.t. those 4 x 20 parameters per column,
+    checkpoints every k steps.  Times the plain forward (48 production steps) and the
+    gradient pass (forward with checkpoints, then reverse)."""
+    import torch
+    from clmgb import abi, adjoint, api, synth
+    nc, nsteps = args.adj_nc, args.adj_steps
+    wl = synth.make_workload(1, nc=nc, seed=synth.CONFIGS[1]["seed"] + 4000, nsteps=nsteps)
+    cfg = abi.SwmConfig.clm5_default()
+    cfg.lower_boundary_condition = abi.BC_FLUX
+    h = api.Handle(wl.state.vp)
+    h.reserve(nc)
+    h.reserve_adjoint(min(nc, args.adj_slots), args.adj_entries)
+    G, I = wl.forcing_block(range(nsteps))
+    Gd, Id = torch.from_numpy(G).cuda(), torch.from_numpy(I).cuda()
+
+    def forcing(t, st):
+        api.synth_forcing(h, st, Gd[t], Id[t])
+    traj = adjoint.Trajectory(h, nsteps, wl.dtime, forcing, cfg, forcing_reverse=adjoint.synth_forcing_reverse)
+    st0 = wl.state.to_device()
+    pert = wl.state.copy()
+    adjoint.perturb_parameters(pert, np.random.default_rng(4242))
+    tl = adjoint.CalibrationLoss(st0, wl.dtime)
+    s = pert.to_device()
+    for t in range(nsteps):
+        traj.step(t, s)
+        tl.observe(t, s)
+    target = torch.stack(tl.y)
+    del s, pert
+    # warm-up: two steps forward and back
+    warm = adjoint.Trajectory(h, 2, wl.dtime, forcing, cfg, forcing_reverse=adjoint.synth_forcing_reverse)
+    wloss = adjoint.CalibrationLoss(st0, wl.dtime, target[:2])
+    adjoint.multistep_reverse(warm, st0.copy(), wloss.seed, wloss.observe, checkpoint_every=args.adj_k)
+    torch.cuda.synchronize()
+    # the plain forward
+    st = st0.copy()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for t in range(nsteps):
+        traj.step(t, st)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1)
+    del st
+    # the gradient pass
+    loss = adjoint.CalibrationLoss(st0, wl.dtime, target)
+    st = st0.copy()
+    status = torch.zeros(nc, dtype=torch.int32, device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    adj = adjoint.multistep_reverse(traj, st, loss.seed, loss.observe, checkpoint_every=args.adj_k,
+                                    col_status=status, events=ev)
+    torch.cuda.synchronize()
+    fwd_ckpt_ms = ev[0].elapsed_time(ev[1])
+    rev_ms = ev[1].elapsed_time(ev[2])
+    sts = status.cpu().numpy()
+    finite = all(bool(torch.isfinite(adj.grad[p]).all()) for p in adjoint.PARAMS)
+    out = {"workload": "adjoint calibration: %d columns, snow + frozen soil, %d steps x %g s, free drainage, "
+                       "checkpoints every %d steps" % (nc, nsteps, wl.dtime, args.adj_k),
+           "forward_ms": fwd_ms, "forward_with_checkpoints_ms": fwd_ckpt_ms, "reverse_ms": rev_ms,
+           "adjoint_over_forward": rev_ms / fwd_ms,
+           "gradient_over_forward": (fwd_ckpt_ms + rev_ms) / fwd_ms,
+           "loss": float(loss.per_column().sum()),
+           "gradients_finite": finite,
+           "tape_entries_max": h.get_option(abi.OPT_ADJ_TAPE_USED),
+           "tape": {"slots": h.get_option(abi.OPT_ADJ_TAPE_SLOTS), "entries": h.get_option(abi.OPT_ADJ_TAPE_ENTRIES)},
+           "columns_flagged": int(np.count_nonzero(sts & (abi.COL_TAPE_FULL | abi.COL_ADJ_UNSUPPORTED |
+                                                          abi.COL_ADJ_REPLAY))),
+           "note": "adjoint_over_forward = reverse pass / plain forward; gradients checked against "
+                   "complex-step and central differences in tests/test_gpu_adjoint_step.py"}
+    h.close()
+    return out
 
 
 def run_ours(args):
@@ -330,13 +414,19 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(wl, cfg, args.cpu_sample, 1)
 
+    state_gb = sum(v.numel() * v.element_size() for v in d.arrays.values()) / 1e9
+    adj_line = None
+    if rank == 0 and not args.no_adjoint:
+        del d, Gd, Id
+        torch.cuda.empty_cache()
+        adj_line = adjoint_leg(args)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "nc_per_gpu": nc, "dtime": wl.dtime, "variant": "plain FP64",
-                           "l2": "inputs larger than L2 (state %.2f GB per GPU)" % (sum(
-                               v.numel() * v.element_size() for v in d.arrays.values()) / 1e9),
+                           "l2": "inputs larger than L2 (state %.2f GB per GPU)" % state_gb,
                            "device_status": status, "parallelism": "replicas over disjoint column shards",
                            "schedule": h.get_option(abi.OPT_STEP_SCHEDULE),
                            "queue_blocks_per_sm": h.get_option(abi.OPT_QUEUE_BLOCKS_PER_SM),
@@ -344,6 +434,7 @@ def run_ours(args):
                            "reserved_columns": h.get_option(abi.OPT_RESERVED_COLUMNS),
                            "queue_order": h.get_option(abi.OPT_QUEUE_ORDER)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "graph": graph, "autotune": tune,
+                "adjoint": adj_line,
                 "gpu_launches": 4 * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)
     h.close()

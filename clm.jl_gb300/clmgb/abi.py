@@ -58,6 +58,8 @@ OPT_WAVES_OCCUPANCY = 8
 OPT_ADJ_TAPE_USED = 9
 OPT_ADJ_TAPE_SLOTS = 10
 OPT_ADJ_TAPE_ENTRIES = 11
+OPT_ADJ_RICHARDS = 12
+ADJ_RICHARDS_CLOSED_FORM, ADJ_RICHARDS_RECORDED = 0, 1
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
 COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY = 32, 64, 128

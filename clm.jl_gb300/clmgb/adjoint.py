@@ -114,12 +114,16 @@ def synth_forcing_reverse(t, before, adj):
     adj.lam_t_grnd += 4.0 * SB * tg * tg * tg * adj.lam_forc_lwrad
 
 
-def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_status=None):
+def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_status=None, events=None):
     """Forward through traj from `state` (left holding the final state), keeping a
     checkpoint every `checkpoint_every` steps; then reverse, recomputing each segment's
     step-entry states from its checkpoint.  observe(t, state_after_t) runs after every
-    forward step (the loss's forward half).  Returns the adjoint buffers."""
+    forward step (the loss's forward half).  `events`, three CUDA events, are recorded
+    at the start, between the forward and the reverse pass, and at the end.  Returns
+    the adjoint buffers."""
     k = max(1, int(checkpoint_every))
+    if events is not None:
+        events[0].record()
     ckpt = []
     for t in range(traj.nsteps):
         if t % k == 0:
@@ -127,6 +131,8 @@ def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_s
         traj.step(t, state)
         if observe is not None:
             observe(t, state)
+    if events is not None:
+        events[1].record()
     adj = StepAdjointBuffers(state)
     seg_states = [state.copy() for _ in range(min(k, traj.nsteps))]
     for s in range(len(ckpt) - 1, -1, -1):
@@ -138,6 +144,8 @@ def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_s
         for t in range(t1 - 1, t0 - 1, -1):
             seed(t, adj)
             traj.reverse_step(t, seg_states[t - t0], adj, col_status)
+    if events is not None:
+        events[2].record()
     return adj
 
 

@@ -433,6 +433,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value < 0) return CLMGB_ERR_CONFIG;
       h->waves_blocks_per_sm = value;
       return CLMGB_OK;
+    case CLMGB_OPT_ADJ_RICHARDS:
+      if (value != CLMGB_ADJ_RICHARDS_CLOSED_FORM && value != CLMGB_ADJ_RICHARDS_RECORDED) return CLMGB_ERR_CONFIG;
+      h->tape.richards_mode = (int)value;
+      return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
   }
@@ -451,6 +455,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_WAVES_BLOCKS_PER_SM: *value = h->waves_blocks_per_sm; return CLMGB_OK;
     case CLMGB_OPT_WAVES_OCCUPANCY: *value = h->waves_blocks; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_SLOTS: *value = h->tape.slots; return CLMGB_OK;
+    case CLMGB_OPT_ADJ_RICHARDS: *value = h->tape.richards_mode; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_USED: {
       unsigned int used = 0;
@@ -542,7 +547,9 @@ int32_t clmgb_reserve_adjoint(clmgb_handle h, int64_t slots, int64_t entries) {
   if (h->tape_block) {
     cudaFree(h->tape_block);
     h->tape_block = nullptr;
+    const int mode = h->tape.richards_mode;
     h->tape = clmgb::AdjTape{};
+    h->tape.richards_mode = mode;
   }
   void* blk = nullptr;
   ce = cudaMalloc(&blk, total);

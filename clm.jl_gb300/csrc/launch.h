@@ -41,6 +41,7 @@ struct AdjTape {
   double* sub;
   int64_t slots, entries, maxsub;
   unsigned int* max_used;
+  int richards_mode;
 };
 
 // All launchers return the cudaError_t of the launch (cudaGetLastError()).

@@ -273,6 +273,9 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                              clmgb_column_step_vjp since clmgb_reserve_adjoint */
 #define CLMGB_OPT_ADJ_TAPE_SLOTS      10  /* read-only: tape slots (concurrent columns) reserved */
 #define CLMGB_OPT_ADJ_TAPE_ENTRIES    11  /* read-only: tape entries per slot reserved */
+#define CLMGB_OPT_ADJ_RICHARDS        12  /* how clmgb_column_step_vjp reverses the Richards substeps: */
+#define   CLMGB_ADJ_RICHARDS_CLOSED_FORM 0 /*   hand-written reverse of each accepted substep (default) */
+#define   CLMGB_ADJ_RICHARDS_RECORDED    1 /*   each substep replayed through the recording scalar */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
 /* Gives the handle per-column scratch for up to max_nc columns (about 48*nlevsoi + 80
  * bytes per column): the Richards solve then forms the ice impedances in a uniform

@@ -45,7 +45,8 @@ def test_header_constants_match_python():
     txt = header_text()
     consts = dict(re.findall(r"#define\s+CLMGB_(\w+)\s+(\d+)u?\b", txt))
     for name in ("COL_ADJ_UNSUPPORTED", "COL_TAPE_FULL", "OPT_ADJ_TAPE_USED", "OPT_ADJ_TAPE_SLOTS",
-                 "OPT_ADJ_TAPE_ENTRIES", "OPT_STEP_SCHEDULE", "OPT_WAVES_OCCUPANCY"):
+                 "OPT_ADJ_TAPE_ENTRIES", "OPT_STEP_SCHEDULE", "OPT_WAVES_OCCUPANCY", "OPT_ADJ_RICHARDS",
+                 "ADJ_RICHARDS_CLOSED_FORM", "ADJ_RICHARDS_RECORDED", "COL_ADJ_REPLAY", "ADJ_MAX_SUBSTEPS"):
         assert int(consts[name]) == getattr(abi, name), name
 
 

@@ -243,6 +243,35 @@ def test_richards_gradient_vs_complex_step(handle):
     assert worst < 1e-9
 
 
+def test_closed_form_substep_reverse_matches_recorded_replay(handle):
+    """The hand-written reverse of a Richards substep and the recorded replay of the
+    same substep differentiate the same arithmetic: they agree to rounding."""
+    cfg = _cfg_flux()
+    nsteps = 4
+    wl, G, I = _workload(256, nsteps, seed=555)
+    traj = _traj(handle, wl, G, I, nsteps, cfg)
+    st0 = wl.state.to_device()
+    tgt = torch.zeros((nsteps, st0.nc), dtype=torch.float64, device="cuda")
+    out = {}
+    try:
+        for mode in (abi.ADJ_RICHARDS_CLOSED_FORM, abi.ADJ_RICHARDS_RECORDED):
+            handle.set_option(abi.OPT_ADJ_RICHARDS, mode)
+            loss = adjoint.CalibrationLoss(st0, wl.dtime, tgt)
+            status = torch.zeros(st0.nc, dtype=torch.int32, device="cuda")
+            adj = adjoint.multistep_reverse(traj, st0.copy(), loss.seed, loss.observe, checkpoint_every=2,
+                                            col_status=status)
+            assert int(status.cpu().numpy().sum()) == 0
+            out[mode] = np.array([adj.grad[p].cpu().numpy() for p in adjoint.PARAMS] +
+                                 [adj.lam_h2osoi_liq.cpu().numpy()[st0.vp.nlevsno:st0.vp.nlevsno + 20]])
+    finally:
+        handle.set_option(abi.OPT_ADJ_RICHARDS, abi.ADJ_RICHARDS_CLOSED_FORM)
+    a, b = out[abi.ADJ_RICHARDS_CLOSED_FORM], out[abi.ADJ_RICHARDS_RECORDED]
+    scale = np.max(np.abs(b), axis=(0, 1))
+    rel = np.max(np.abs(a - b), axis=(0, 1)) / np.maximum(scale, 1e-300)
+    print("closed form vs recorded: max rel diff %.3g" % rel.max())
+    assert rel.max() < 1e-11
+
+
 def test_checkpoint_schedules_give_the_same_bits(handle):
     cfg = _cfg_flux()
     nsteps = 13
