@@ -28,9 +28,8 @@
 // frac_h2osfc > 0, excess ice, snow without layers) would carry sensitivity into
 // the next step; columns holding any of it are flagged CLMGB_COL_ADJ_UNSUPPORTED.
 //
-// Tape layout: entry k of the thread in slot s sits at [k * nslots + s] (int2 parent
-// indices, double2 partials, double adjoint), so the lanes of a warp recording the
-// same entry index write 32 consecutive elements.
+// Tape layout: [warp][entry][lane] (int2 parent indices, double2 partials, double
+// adjoint), see tape_off.
 #include "clmgb_device.cuh"
 #include "launch.h"
 
@@ -55,6 +54,15 @@ __shared__ int s_ovf[VJP_BLOCK];
 
 __device__ __forceinline__ int64_t vjp_slot() { return (int64_t)blockIdx.x * VJP_BLOCK + threadIdx.x; }
 
+// Offset of record k of this thread: [warp][k][lane].  A warp's tape is one
+// contiguous range (few pages, so address translation stays cached while the lanes
+// walk their tapes at different positions), and lanes at the same position share
+// one 256-byte line.
+__device__ __forceinline__ int64_t tape_off(int64_t k) {
+  const int64_t slot = vjp_slot();
+  return ((slot >> 5) * s_tape.cap + k) * 32 + (slot & 31);
+}
+
 // append one entry; returns its index, or -1 once the tape is full
 __device__ __forceinline__ int ad_rec(int a, double pa, int b, double pb) {
   const int k = s_cur[threadIdx.x];
@@ -63,7 +71,7 @@ __device__ __forceinline__ int ad_rec(int a, double pa, int b, double pb) {
     return -1;
   }
   s_cur[threadIdx.x] = k + 1;
-  const int64_t o = (int64_t)k * s_tape.ld + vjp_slot();
+  const int64_t o = tape_off(k);
   s_tape.idx[o] = make_int2(a, b);
   s_tape.par[o] = make_double2(pa, pb);
   s_tape.adj[o] = 0.0;
@@ -179,10 +187,10 @@ __device__ __forceinline__ AD ad_input(double v) { return AD(v, ad_rec(-1, 0.0, 
 
 // adjoint accumulate into the tape's adjoint of variable k
 __device__ __forceinline__ void adj_add(int k, double g) {
-  if (k >= 0) s_tape.adj[(int64_t)k * s_tape.ld + vjp_slot()] += g;
+  if (k >= 0) s_tape.adj[tape_off(k)] += g;
 }
 __device__ __forceinline__ double adj_get(int k) {
-  return k >= 0 ? s_tape.adj[(int64_t)k * s_tape.ld + vjp_slot()] : 0.0;
+  return k >= 0 ? s_tape.adj[tape_off(k)] : 0.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -223,35 +231,87 @@ __device__ __forceinline__ void band_lu_solve(AD* ab, AD* x, int n) {
   for (int r = 0; r < n; r++) x[r] = ad_input(B.x[r]);
 }
 
-__device__ __forceinline__ void band_node_reverse(const BandNode& B) {
+// Reverse sweep over entries hi..lo (descending).  Most operations read values
+// computed a few entries earlier, so the adjoints of the newest SWEEP_WIN entries
+// below the current one live in shared memory (s_win, one column per thread) and
+// only contributions to older entries go to the tape's adjoint array in global
+// memory.  An entry's global part is final SWEEP_WIN iterations before the sweep
+// reaches it, so the records and global parts of the next entries are loaded ahead
+// of the dependent work.  Each entry's total adjoint is written back to the tape
+// (tape nodes read their outputs' adjoints from there), and on return the window's
+// partial sums below `lo` are added to the tape, so adj_get sees complete values.
+constexpr int SWEEP_WIN = 32;
+__shared__ double s_win[SWEEP_WIN * VJP_BLOCK];
+
+__device__ __forceinline__ double& win_at(int k) { return s_win[(k & (SWEEP_WIN - 1)) * VJP_BLOCK + threadIdx.x]; }
+
+// adds v to the adjoint of entry p while the sweep is at entry k (p < k)
+__device__ __forceinline__ void sweep_add(int p, int k, double v) {
+  if (p < 0) return;
+  if (p > k - SWEEP_WIN) win_at(p) += v;
+  else s_tape.adj[tape_off(p)] += v;
+}
+
+// the band node's reverse, at its marker entry k: the solution rows' adjoints are
+// complete on the tape (they sit above the marker)
+__device__ __forceinline__ void band_node_reverse(const BandNode& B, int k) {
   double w[MAXROWS];
   const int n = B.n;
   for (int r = 0; r < n; r++) w[r] = adj_get(B.first + r);
   band_lu_transpose_solve<2, 2>(B.lu, B.piv, w, n);
   for (int r = 0; r < n; r++) {
-    adj_add(B.ridx[r], w[r]);
+    sweep_add(B.ridx[r], k, w[r]);
     for (int d = 0; d < 5; d++) {
       const int col = r - 2 + d;
-      if (col >= 0 && col < n) adj_add(B.aidx[r * 5 + d], -w[r] * B.x[col]);
+      if (col >= 0 && col < n) sweep_add(B.aidx[r * 5 + d], k, -w[r] * B.x[col]);
     }
   }
 }
 
-// reverse sweep over entries hi..lo (descending)
-__device__ __forceinline__ void sweep(int hi, int lo) {
-  const int64_t s = vjp_slot(), L = s_tape.ld;
-  for (int k = hi; k >= lo; k--) {
-    const int64_t o = (int64_t)k * L + s;
-    const int2 e = s_tape.idx[o];
-    if (e.x == MARK_BAND) {
-      band_node_reverse(*s_band[threadIdx.x]);
-      continue;
+__device__ void sweep(int hi, int lo) {
+  if (hi < lo) return;
+  for (int m = hi; m > hi - SWEEP_WIN; m--) win_at(m) = 0.0;
+  // two-deep prefetch of the records and the global adjoint parts
+  int64_t o = tape_off(hi);
+  int2 e0 = s_tape.idx[o];
+  double2 p0 = s_tape.par[o];
+  double g0 = s_tape.adj[o];
+  int2 e1 = make_int2(-1, -1);
+  double2 p1 = make_double2(0.0, 0.0);
+  double g1 = 0.0;
+  if (hi - 1 >= lo) {
+    const int64_t o1 = o - 32;
+    e1 = s_tape.idx[o1];
+    p1 = s_tape.par[o1];
+    g1 = s_tape.adj[o1];
+  }
+  for (int k = hi; k >= lo; k--, o -= 32) {
+    int2 e2 = make_int2(-1, -1);
+    double2 p2 = make_double2(0.0, 0.0);
+    double g2 = 0.0;
+    if (k - 2 >= lo) {
+      const int64_t o2 = o - 64;
+      e2 = s_tape.idx[o2];
+      p2 = s_tape.par[o2];
+      g2 = s_tape.adj[o2];
     }
-    const double g = s_tape.adj[o];
-    if (g == 0.0) continue;
-    const double2 p = s_tape.par[o];
-    if (e.x >= 0) s_tape.adj[(int64_t)e.x * L + s] += p.x * g;
-    if (e.y >= 0) s_tape.adj[(int64_t)e.y * L + s] += p.y * g;
+    double& wk = win_at(k);
+    const double g = wk + g0;
+    wk = 0.0;                                  // the slot now holds entry k - SWEEP_WIN
+    s_tape.adj[o] = g;
+    if (e0.x == MARK_BAND) {
+      band_node_reverse(*s_band[threadIdx.x], k);
+    } else if (g != 0.0) {
+      if (e0.x >= 0) sweep_add(e0.x, k, p0.x * g);
+      if (e0.y >= 0) sweep_add(e0.y, k, p0.y * g);
+    }
+    e0 = e1; p0 = p1; g0 = g1;
+    e1 = e2; p1 = p2; g1 = g2;
+  }
+  for (int m = lo - 1; m > lo - SWEEP_WIN && m >= 0; m--) {
+    double& wm = win_at(m);
+    s_tape.adj[tape_off(m)] += wm;
+    wm = 0.0;
   }
 }
 
@@ -499,7 +559,9 @@ __device__ __noinline__ void mf_substep_reverse(const Dims& D, const clmgb_soilw
 // per-substep checkpoint record: nlevsoi liquid water values, dtsub, dtdone
 constexpr int SUB_REC = MAXSOI + 2;
 __device__ __forceinline__ double& sub_at(int sidx, int j) {
-  return s_tape.sub[((int64_t)sidx * SUB_REC + j) * s_tape.ld + vjp_slot()];
+  const int64_t slot = vjp_slot();
+  return s_tape.sub[((slot >> 5) * ((int64_t)s_tape.maxsub * SUB_REC) + (int64_t)sidx * SUB_REC + j) * 32 +
+                    (slot & 31)];
 }
 
 __global__ void __launch_bounds__(VJP_BLOCK)
