@@ -60,6 +60,11 @@ def parse():
     ap.add_argument("--adj-k", type=int, default=8, help="checkpoint every k steps")
     ap.add_argument("--adj-slots", type=int, default=65536)
     ap.add_argument("--adj-entries", type=int, default=8192)
+    ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start leg")
+    ap.add_argument("--warm-train-nc", type=int, default=262144)
+    ap.add_argument("--warm-train-steps", type=int, default=8)
+    ap.add_argument("--warm-eval-steps", type=int, default=20)
+    ap.add_argument("--warm-epochs", type=int, default=3)
     return ap.parse_args()
 
 
@@ -265,6 +270,110 @@ def adjoint_leg(args):
     return out
 
 
+def warm_leg(args, wl_eval):
+    """Learned warm start: training pairs from the plain solver on the scale workload's
+    column distribution with another seed, GPU training, then the plain and the
+    warm-started step timed on the scale workload itself."""
+    import torch
+    from clmgb import abi, api, mlp, synth
+    cfg = abi.SwmConfig.clm5_default()
+    h = api.Handle(wl_eval.state.vp)
+    h.reserve(max(args.warm_train_nc, wl_eval.state.nc))
+    t0 = time.time()
+    # ---- training pairs (first substep of every column-step) ----
+    wt = synth.make_workload(2, nc=args.warm_train_nc, seed=synth.CONFIGS[2]["seed"] + 777,
+                             nsteps=args.warm_train_steps + 4)
+    Gt, It = wt.forcing_block(range(args.warm_train_steps + 4))
+    Gt, It = torch.from_numpy(Gt).cuda(), torch.from_numpy(It).cuda()
+    st = wt.state.to_device()
+    F, T = mlp.generate_samples(h, st, Gt, It, args.warm_train_steps, wt.dtime, per_column=1)
+    gen_s = time.time() - t0
+    n_pairs = int(F.shape[0])
+    model = mlp.WarmStartMLP(h, seed=0)
+    t1 = time.time()
+    hist = model.train(F, T, epochs=args.warm_epochs, batch=4096, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.time() - t1
+    del F, T
+
+    def run(state, G, I, steps, warm, t_first=0, timed=True):
+        dt = torch.empty(state.nc, dtype=torch.float64, device="cuda")
+        nsub = torch.zeros(state.nc, dtype=torch.float64, device="cuda")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for k in range(steps):
+            t = t_first + k
+            api.synth_forcing(h, state, G[t], I[t])
+            api.soil_temperature(h, state, wl_eval.dtime)
+            api.set_soil_water_fractions(h, state)
+            if warm:
+                model.propose_first_dt(state, wl_eval.dtime, cfg, out=dt)
+                mlp.soil_water_warm(h, state, wl_eval.dtime, dt, cfg)
+            else:
+                api.soil_water(h, state, wl_eval.dtime, cfg)
+            nsub += state["num_substeps"]
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), float(nsub.sum()) / (steps * state.nc)
+
+    # ---- decision margin, chosen on the training workload ----
+    tune = {}
+    for m in (0.0, 0.5, 1.0):
+        model.margin = m
+        s2 = wt.state.to_device()
+        ms, att = run(s2, Gt, It, 4, True, t_first=args.warm_train_steps)
+        tune[m] = {"ms": ms, "attempts": att}
+    model.margin = min(tune, key=lambda m: tune[m]["ms"])
+    del st
+    # ---- evaluation on the scale workload ----
+    ne = args.warm_eval_steps
+    G, I = wl_eval.forcing_block(range(ne + 2))
+    G, I = torch.from_numpy(G).cuda(), torch.from_numpy(I).cuda()
+    res = {}
+    for mode in ("plain", "warm"):
+        s2 = wl_eval.state.to_device()
+        run(s2, G, I, 2, mode == "warm")               # warm-up
+        ms, att = run(s2, G, I, ne, mode == "warm", t_first=2)
+        res[mode] = {"ms_per_step": ms / ne, "value": ne * s2.nc / (ms / 1000.0), "attempts_per_column_step": att}
+        del s2
+    # ---- error against the FP64 oracle on a sample of columns ----
+    from oracle import oracle as orc
+    cols = np.linspace(0, wl_eval.state.nc - 1, 256).astype(np.int64)
+    sub = wl_eval.state.subset(cols)
+    ref = sub.copy()
+    Gh, Ih = G.cpu().numpy()[:, cols], I.cpu().numpy()[:, cols]
+    orc.run_steps(ref, wl_eval.dtime, Gh[:ne + 2], Ih[:ne + 2], cfg)
+    errs = {}
+    for mode in ("plain", "warm"):
+        d = sub.to_device()
+        Gs, Is = torch.from_numpy(np.ascontiguousarray(Gh)).cuda(), torch.from_numpy(np.ascontiguousarray(Ih)).cuda()
+        dtv = torch.empty(d.nc, dtype=torch.float64, device="cuda")
+        for t in range(ne + 2):
+            api.synth_forcing(h, d, Gs[t], Is[t])
+            api.column_step(h, d, wl_eval.dtime, cfg) if mode == "plain" else None
+            if mode == "warm":
+                api.soil_temperature(h, d, wl_eval.dtime)
+                api.set_soil_water_fractions(h, d)
+                model.propose_first_dt(d, wl_eval.dtime, cfg, out=dtv)
+                mlp.soil_water_warm(h, d, wl_eval.dtime, dtv, cfg)
+        liq = d["h2osoi_liq"].cpu().numpy()
+        errs[mode] = float(np.max(np.abs(liq - ref["h2osoi_liq"])))
+    out = {"workload": "learned warm start: MLP 64-128-128-21 (SiLU, bf16/fp32), trained on %d pairs from the "
+                       "plain solver (%d columns x %d steps, other seed); evaluated on the scale workload, %d steps"
+                       % (n_pairs, args.warm_train_nc, args.warm_train_steps, ne),
+           "plain": res["plain"], "warm": res["warm"],
+           "speedup": res["warm"]["value"] / res["plain"]["value"],
+           "attempt_ratio": res["warm"]["attempts_per_column_step"] / res["plain"]["attempts_per_column_step"],
+           "max_abs_liq_error_vs_oracle_mm": errs, "error_sample_columns": 256,
+           "margin": model.margin, "margin_tuning": tune, "train_loss": hist,
+           "sample_generation_s": gen_s, "training_s": train_s,
+           "note": "both paths meet the same accept tolerance (xTolerUpper); the warm path only changes the "
+                   "first substep each column tries"}
+    h.close()
+    return out
+
+
 def run_ours(args):
     import torch
     from clmgb import abi, api, bytes_model, synth
@@ -416,10 +525,15 @@ def run_ours(args):
 
     state_gb = sum(v.numel() * v.element_size() for v in d.arrays.values()) / 1e9
     adj_line = None
-    if rank == 0 and not args.no_adjoint:
+    warm_line = None
+    if rank == 0 and (not args.no_adjoint or not args.no_warm):
         del d, Gd, Id
         torch.cuda.empty_cache()
-        adj_line = adjoint_leg(args)
+        if not args.no_warm:
+            warm_line = warm_leg(args, wl)
+            torch.cuda.empty_cache()
+        if not args.no_adjoint:
+            adj_line = adjoint_leg(args)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -434,7 +548,7 @@ def run_ours(args):
                            "reserved_columns": h.get_option(abi.OPT_RESERVED_COLUMNS),
                            "queue_order": h.get_option(abi.OPT_QUEUE_ORDER)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "graph": graph, "autotune": tune,
-                "adjoint": adj_line,
+                "adjoint": adj_line, "warm_start": warm_line,
                 "gpu_launches": 4 * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)
     h.close()

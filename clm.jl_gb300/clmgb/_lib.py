@@ -33,6 +33,15 @@ _SIGS = {
     "clmgb_batched_band_solve_adjoint": ([P, I64, I64, I32, P, P, P, P, P, P, P, P, P, I32, I32, I32, P], I32),
     "clmgb_tridiagonal_adjoint": ([P, I64, I64, I32] + [P] * 12, I32),
     "clmgb_reserve_adjoint": ([P, I64, I64], I32),
+    "clmgb_soil_water_warm": ([P, P, P, P, F64, P, P, P], I32),
+    "clmgb_mlp_samples": ([P, P, P, P, F64, I32, P, P, P, I64, P, P], I32),
+    "clmgb_mlp_linear": ([P, I64, I32, I32, P, I64, P, P, I32, P, I64, P, I64, P], I32),
+    "clmgb_mlp_linear_dw": ([P, I64, I32, I32, P, I64, P, I64, P, P, P], I32),
+    "clmgb_mlp_silu_backward": ([P, I64, P, P, P, P], I32),
+    "clmgb_mlp_loss": ([P, I64, P, P, C.c_float, C.c_float, P, P, P], I32),
+    "clmgb_mlp_adam": ([P, I64, I64, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, I32, P, P, P], I32),
+    "clmgb_mlp_features": ([P, P, P, P, F64, P, P, P, P], I32),
+    "clmgb_mlp_first_dt": ([P, I64, P, F64, C.c_float, I32, P, P], I32),
     "clmgb_column_step_vjp": ([P, P, P, P, P, F64, I32, P, P, P, P, P], I32),
     "clmgb_set_option": ([P, I32, I64], I32),
     "clmgb_reserve": ([P, I64], I32),

@@ -598,4 +598,110 @@ int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_soil_water_warm(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                              const clmgb_swm_config* cfg, double dtime, const double* dt_first,
+                              uint32_t* col_status, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_cfg(cfg);
+  if (e) return e;
+  if ((e = check_bounds(b, false))) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  cudaError_t ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
+                                                     h->dev_status, h->queue, queue_grid(h), queue_scratch(h),
+                                                     (cudaStream_t)stream, dt_first);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_samples(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                          const clmgb_swm_config* cfg, double dtime, int32_t per_column, float* features,
+                          float* targets, uint32_t* count, int64_t capacity, uint32_t* col_status, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_cfg(cfg);
+  if (e) return e;
+  if ((e = check_bounds(b, false))) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (!(dtime > 0.0) || per_column < 0) return CLMGB_ERR_CONFIG;
+  if (!features || !targets || !count || capacity < 0) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_richards_samples(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, per_column, features,
+                                                  targets, count, capacity, col_status, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_linear(clmgb_handle h, int64_t M, int32_t N, int32_t K, const uint16_t* X, int64_t ldx,
+                         const uint16_t* W, const float* bias, int32_t act, float* Z, int64_t ldz, uint16_t* Y,
+                         int64_t ldy, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (M < 0 || ldx < K || (Z && ldz < N) || (Y && ldy < N)) return CLMGB_ERR_DIMS;
+  if (!X || !W) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_mlp_linear(M, N, K, X, ldx, W, bias, act, Z, ldz, Y, ldy, (cudaStream_t)stream);
+  if (ce == cudaErrorInvalidValue) return CLMGB_ERR_UNSUPPORTED;
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_linear_dw(clmgb_handle h, int64_t M, int32_t N, int32_t K, const uint16_t* dZ, int64_t lddz,
+                            const uint16_t* X, int64_t ldx, float* dW, float* db, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (M < 0 || lddz < N || ldx < K) return CLMGB_ERR_DIMS;
+  if (!dZ || !X || !dW) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_mlp_linear_dw(M, N, K, dZ, lddz, X, ldx, dW, db, (cudaStream_t)stream);
+  if (ce == cudaErrorInvalidValue) return CLMGB_ERR_UNSUPPORTED;
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_silu_backward(clmgb_handle h, int64_t n, const float* Z, const uint16_t* dY, uint16_t* dZ,
+                                void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (n < 0) return CLMGB_ERR_DIMS;
+  if (n && (!Z || !dY || !dZ)) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_mlp_silu_backward(n, Z, dY, dZ, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_loss(clmgb_handle h, int64_t M, const float* Y, const float* T, float w_dt, float w_incr,
+                       float* loss, uint16_t* dY, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (M < 0) return CLMGB_ERR_DIMS;
+  if (M && (!Y || !T || !loss || !dY)) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_mlp_loss(M, Y, T, w_dt, w_incr, loss, dY, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_adam(clmgb_handle h, int64_t rows, int64_t cols, float* w, const float* grad, float* m, float* v,
+                       float lr, float beta1, float beta2, float eps, int32_t step, uint16_t* w_bf16,
+                       uint16_t* wt_bf16, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (rows < 0 || cols < 0 || step < 1) return CLMGB_ERR_DIMS;
+  if (rows * cols && (!w || !grad || !m || !v)) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_mlp_adam(rows, cols, w, grad, m, v, lr, beta1, beta2, eps, step, w_bf16, wt_bf16,
+                                          (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_features(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                           const clmgb_swm_config* cfg, double dtime, const float* mean, const float* istd,
+                           uint16_t* X, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_cfg(cfg);
+  if (e) return e;
+  if ((e = check_bounds(b, false))) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (!mean || !istd || !X) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_mlp_features(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, mean, istd, X,
+                                              (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_mlp_first_dt(clmgb_handle h, int64_t nc, const float* Y, double dtime, float margin, int32_t kmax,
+                           double* dt_first, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (nc < 0 || kmax < 0) return CLMGB_ERR_DIMS;
+  if (nc && (!Y || !dt_first)) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_mlp_first_dt(nc, Y, dtime, margin, kmax, dt_first, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 }  // extern "C"

@@ -957,10 +957,14 @@ __device__ __forceinline__ double mf_impedance(const Dims& D, const clmgb_soilwa
 
 // returns false (and sets L.status) when the column cannot be solved.  imp_cache,
 // when given, holds the impedances formed by k_impedance ([nlevsoi, ld_imp]).
+// dt_init, when given, is a proposed size of the first substep per column (the
+// warm start); it is clamped to [dtmin, dtime] and the solver's own error test
+// accepts or halves it like any other substep.
 template <class ST>
 __device__ __forceinline__ bool mf_begin(MfLaneT<typename ST::S>& L, const Dims& D, const clmgb_soilwater_fields& f,
                                          const clmgb_swm_config& cfg, double dtime, int64_t c, ST& X,
-                                         const double* imp_cache = nullptr, int64_t ld_imp = 0) {
+                                         const double* imp_cache = nullptr, int64_t ld_imp = 0,
+                                         const double* dt_init = nullptr) {
   const int64_t ld = D.ldc;
   const int joff = D.nlevsno;
   L.c = c;
@@ -983,6 +987,10 @@ __device__ __forceinline__ bool mf_begin(MfLaneT<typename ST::S>& L, const Dims&
   }
   L.nsub = 0;
   L.dtsub = dtime;
+  if (dt_init) {
+    const double d = dt_init[c];
+    if (d == d) L.dtsub = jl_min(jl_max(d, cfg.dtmin), dtime);   // NaN keeps dtime
+  }
   L.dtdone = 0.0;
   L.qc = 0.0;
   L.fresh = true;
@@ -1192,9 +1200,10 @@ __device__ __forceinline__ uint32_t mf_end(MfLaneT<typename ST::S>& L, const Dim
 // production forms: the column's state in the caller's fields
 __device__ __forceinline__ bool mf_begin(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
                                          const clmgb_swm_config& cfg, double dtime, int64_t c,
-                                         const double* imp_cache = nullptr, int64_t ld_imp = 0) {
+                                         const double* imp_cache = nullptr, int64_t ld_imp = 0,
+                                         const double* dt_init = nullptr) {
   FieldState<clmgb_soilwater_fields> X(f, c, D.ldc);
-  return mf_begin(L, D, f, cfg, dtime, c, X, imp_cache, ld_imp);
+  return mf_begin(L, D, f, cfg, dtime, c, X, imp_cache, ld_imp, dt_init);
 }
 __device__ __forceinline__ bool mf_attempt(MfLane& L, const Dims& D, const clmgb_soilwater_fields& f,
                                            const clmgb_swm_config& cfg, double dtime) {

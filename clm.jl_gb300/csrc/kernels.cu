@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(BLOCK)
 k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                       uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
                       const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
-                      int64_t ld_imp) {
+                      int64_t ld_imp, const double* dt_init) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned long long nq = order ? (unsigned long long)(*(volatile const unsigned int*)nlisted_ptr)
@@ -119,7 +119,7 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
         } else {
           const int64_t c = order ? (int64_t)order[k] : (int64_t)k;
           if (order || f.mask_hydrology[c]) {
-            if (mf_begin(L, D, f, cfg, dtime, c, imp_cache, ld_imp)) {
+            if (mf_begin(L, D, f, cfg, dtime, c, imp_cache, ld_imp, dt_init)) {
               active = true;
             } else {
               const uint32_t st = L.status;
@@ -351,7 +351,8 @@ int queue_blocks_per_sm() {
 cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
-                                       int grid_blocks, const QueueScratch& qs, cudaStream_t s) {
+                                       int grid_blocks, const QueueScratch& qs, cudaStream_t s,
+                                       const double* dt_init) {
   cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   const bool use = qs.capacity >= nc && qs.order && qs.bins && qs.imp;
@@ -373,7 +374,8 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   k_moisture_form_queue<<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status,
                                                               queue, listed ? qs.order : nullptr,
                                                               listed ? qs.bins + 2 * ORDER_BINS : nullptr,
-                                                              use ? qs.imp : nullptr, use ? qs.capacity : 0);
+                                                              use ? qs.imp : nullptr, use ? qs.capacity : 0,
+                                                              dt_init);
   return cudaGetLastError();
 }
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {

@@ -76,7 +76,8 @@ int queue_blocks_per_sm();
 cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
-                                       int grid_blocks, const QueueScratch& qs, cudaStream_t s);
+                                       int grid_blocks, const QueueScratch& qs, cudaStream_t s,
+                                       const double* dt_init = nullptr);
 cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                       cudaStream_t s);
@@ -103,5 +104,23 @@ cudaError_t launch_tridiagonal_adjoint(int64_t ncols, int64_t ldc, int nlevs, co
                                        const double* b, const double* c, double* ubar, double* abar, double* bbar,
                                        double* cbar, double* rbar, const int64_t* jtop, const uint8_t* mask,
                                        cudaStream_t s);
+
+cudaError_t launch_mlp_linear(int64_t M, int N, int K, const void* X, int64_t ldx, const void* W, const float* b,
+                              int act, float* Z, int64_t ldz, void* Y, int64_t ldy, cudaStream_t s);
+cudaError_t launch_mlp_linear_dw(int64_t M, int N, int K, const void* dZ, int64_t lddz, const void* X, int64_t ldx,
+                                 float* dW, float* db, cudaStream_t s);
+cudaError_t launch_mlp_silu_backward(int64_t n, const float* Z, const void* dY, void* dZ, cudaStream_t s);
+cudaError_t launch_mlp_loss(int64_t M, const float* Y, const float* T, float w0, float w1, float* loss, void* dY,
+                            cudaStream_t s);
+cudaError_t launch_mlp_adam(int64_t rows, int64_t cols, float* w, const float* g, float* m, float* v, float lr,
+                            float b1, float b2, float eps, int step, void* wb, void* wbt, cudaStream_t s);
+cudaError_t launch_richards_samples(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                    const clmgb_swm_config& cfg, double dtime, int rmax, float* feat, float* targ,
+                                    unsigned int* count, int64_t capacity, uint32_t* col_status, cudaStream_t s);
+cudaError_t launch_mlp_features(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                const clmgb_swm_config& cfg, double dtime, const float* mean, const float* istd,
+                                void* X, cudaStream_t s);
+cudaError_t launch_mlp_first_dt(int64_t nc, const float* Y, double dtime, float margin, int kmax, double* dt_first,
+                                cudaStream_t s);
 
 }  // namespace clmgb

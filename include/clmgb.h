@@ -462,6 +462,71 @@ int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb
                               double* t_h2osfc_bef, const clmgb_step_adjoint* adj,
                               uint32_t* col_status, void* stream);
 
+/* ---- learned warm start of the moisture-form solve ----
+ * A 64 -> 128 -> 128 -> 21 perceptron (SiLU hidden layers, BF16 weights and
+ * activations, FP32 accumulation) proposes the size of the first substep of every
+ * column: output 0 is the number k of halvings of the remaining time the solver's
+ * error test needs, outputs 1..20 the saturation increment of that substep per
+ * level.  Weights of a layer are [out x in] row-major BF16 (uint16_t), the last
+ * layer padded to 32 outputs; feature rows are 64 BF16 values. */
+
+/* soil_water! (moisture form) starting every column with the proposed first
+ * substep dt_first[c] (clamped to [dtmin, dtime]; NaN = dtime) instead of dtime.
+ * The error test accepts or halves it as any substep, so results meet the same
+ * tolerance; they differ from clmgb_soil_water's by the changed substep sequence.
+ * Always uses the work-queue schedule. */
+int32_t clmgb_soil_water_warm(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                              const clmgb_swm_config* cfg, double dtime, const double* dt_first,
+                              uint32_t* col_status, void* stream);
+
+/* The plain solve (advances the state like clmgb_soil_water) that also records
+ * training pairs at the first `per_column` substep starts of every column: 64 fp32
+ * features and 32 fp32 targets per pair (target 0 = smallest k for which an attempt
+ * at remaining/2^k is accepted, 1..20 = that attempt's saturation increment, the
+ * rest 0), appended at rows atomically counted in *count (capacity rows at most). */
+int32_t clmgb_mlp_samples(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                          const clmgb_swm_config* cfg, double dtime, int32_t per_column, float* features,
+                          float* targets, uint32_t* count, int64_t capacity, uint32_t* col_status,
+                          void* stream);
+
+/* Y = act(X W^T + bias) on the tensor cores (mma.sync bf16 -> fp32): X [M x K] BF16,
+ * W [N x K] BF16, bias [N] fp32 (may be NULL), act 1 = SiLU; Z [M x N] fp32
+ * pre-activation and Y [M x N] BF16 are each optional.  (K, N) in {(64,128),
+ * (128,128), (128,32), (32,128)}. */
+int32_t clmgb_mlp_linear(clmgb_handle h, int64_t M, int32_t N, int32_t K, const uint16_t* X, int64_t ldx,
+                         const uint16_t* W, const float* bias, int32_t act, float* Z, int64_t ldz,
+                         uint16_t* Y, int64_t ldy, void* stream);
+
+/* dW [N x K] += dZ^T X and db [N] += column sums of dZ (fp32 accumulation); dZ
+ * [M x N] and X [M x K] BF16.  (N, K) in {(128,64), (128,128), (32,128)}. */
+int32_t clmgb_mlp_linear_dw(clmgb_handle h, int64_t M, int32_t N, int32_t K, const uint16_t* dZ, int64_t lddz,
+                            const uint16_t* X, int64_t ldx, float* dW, float* db, void* stream);
+
+/* dZ = dY * silu'(Z) elementwise (n values; Z fp32, dY and dZ BF16). */
+int32_t clmgb_mlp_silu_backward(clmgb_handle h, int64_t n, const float* Z, const uint16_t* dY, uint16_t* dZ,
+                                void* stream);
+
+/* loss += sum_m [w_dt (y0-t0)^2 + w_incr/20 sum_{j=1..20} (yj-tj)^2] / M over rows of
+ * 32 fp32 outputs Y and targets T; dY [M x 32] BF16 its gradient. */
+int32_t clmgb_mlp_loss(clmgb_handle h, int64_t M, const float* Y, const float* T, float w_dt, float w_incr,
+                       float* loss, uint16_t* dY, void* stream);
+
+/* One Adam step (bias-corrected, step >= 1) on fp32 master weights [rows x cols];
+ * also writes their BF16 copy and its transpose (each may be NULL). */
+int32_t clmgb_mlp_adam(clmgb_handle h, int64_t rows, int64_t cols, float* w, const float* grad, float* m,
+                       float* v, float lr, float beta1, float beta2, float eps, int32_t step,
+                       uint16_t* w_bf16, uint16_t* wt_bf16, void* stream);
+
+/* Normalised BF16 features [nc x 64] of every column at the start of a solve
+ * ((x - mean) * istd per feature). */
+int32_t clmgb_mlp_features(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
+                           const clmgb_swm_config* cfg, double dtime, const float* mean, const float* istd,
+                           uint16_t* X, void* stream);
+
+/* dt_first[c] = dtime / 2^k with k = clamp(ceil(Y[c*32] - margin), 0, kmax). */
+int32_t clmgb_mlp_first_dt(clmgb_handle h, int64_t nc, const float* Y, double dtime, float margin, int32_t kmax,
+                           double* dt_first, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
