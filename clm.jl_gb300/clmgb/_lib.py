@@ -34,6 +34,8 @@ _SIGS = {
     "clmgb_tridiagonal_adjoint": ([P, I64, I64, I32] + [P] * 12, I32),
     "clmgb_reserve_adjoint": ([P, I64, I64], I32),
     "clmgb_soil_water_warm": ([P, P, P, P, F64, P, P, P], I32),
+    "clmgb_balance_begin": ([P, P, P, P, P, P], I32),
+    "clmgb_balance_residuals": ([P, P, P, P, F64, P, P, P, P, P, P, P], I32),
     "clmgb_mlp_samples": ([P, P, P, P, F64, I32, P, P, P, I64, P, P], I32),
     "clmgb_mlp_linear": ([P, I64, I32, I32, P, I64, P, P, I32, P, I64, P, I64, P], I32),
     "clmgb_mlp_linear_dw": ([P, I64, I32, I32, P, I64, P, I64, P, P, P], I32),

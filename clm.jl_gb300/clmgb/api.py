@@ -210,6 +210,29 @@ def tridiagonal_adjoint(handle, u, a, b, c, u_bar, a_bar, b_bar, c_bar, r_bar, j
           "tridiagonal_adjoint")
 
 
+def balance_begin(handle, state, stream=None):
+    """(t_grnd0, begwb) recorded before a step (clmgb_balance_begin)."""
+    import torch
+    t0 = torch.empty(state.nc, dtype=torch.float64, device="cuda")
+    w0 = torch.empty(state.nc, dtype=torch.float64, device="cuda")
+    check(handle.lib.clmgb_balance_begin(handle.h, C.byref(state.bounds()), C.byref(state.soiltemp_fields()),
+                                         _dptr(t0), _dptr(w0), _stream(stream)), "balance_begin")
+    return t0, w0
+
+
+def balance_residuals(handle, state, dtime, t_grnd0, begwb, stream=None):
+    """(errsoi W/m2, errh2o mm) of the step just taken (clmgb_balance_residuals)."""
+    import torch
+    es = torch.empty(state.nc, dtype=torch.float64, device="cuda")
+    eh = torch.empty(state.nc, dtype=torch.float64, device="cuda")
+    check(handle.lib.clmgb_balance_residuals(handle.h, C.byref(state.bounds()), C.byref(state.soiltemp_fields()),
+                                             C.byref(state.soilwater_fields()), float(dtime),
+                                             _dptr(state["t_ssbef"]), _dptr(state["t_h2osfc_bef"]), _dptr(t_grnd0),
+                                             _dptr(begwb), _dptr(es), _dptr(eh), _stream(stream)),
+          "balance_residuals")
+    return es, eh
+
+
 MATH_OPS = {"log": 0, "exp": 1, "pow": 2, "log10": 3}
 
 

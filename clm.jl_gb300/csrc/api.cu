@@ -704,4 +704,33 @@ int32_t clmgb_mlp_first_dt(clmgb_handle h, int64_t nc, const float* Y, double dt
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_balance_begin(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft, double* t_grnd0,
+                            double* begwb, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, true);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(ft))) return e;
+  if (!t_grnd0 || !begwb) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_balance_begin(make_dims(h->vp, *b), b->nc, *ft, t_grnd0, begwb, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_balance_residuals(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                                const clmgb_soilwater_fields* fw, double dtime, const double* t_ssbef,
+                                const double* t_h2osfc_bef, const double* t_grnd0, const double* begwb,
+                                double* errsoi, double* errh2o, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, true);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(ft))) return e;
+  if ((e = check_fields(fw))) return e;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  if (!t_ssbef || !t_h2osfc_bef || !t_grnd0 || !begwb || !errsoi || !errh2o) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_balance_residuals(make_dims(h->vp, *b), b->nc, *ft, *fw, dtime, t_ssbef, t_h2osfc_bef,
+                                                   t_grnd0, begwb, errsoi, errh2o, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 }  // extern "C"

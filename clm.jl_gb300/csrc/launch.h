@@ -123,4 +123,11 @@ cudaError_t launch_mlp_features(const Dims& D, int64_t nc, const clmgb_soilwater
 cudaError_t launch_mlp_first_dt(int64_t nc, const float* Y, double dtime, float margin, int kmax, double* dt_first,
                                 cudaStream_t s);
 
+cudaError_t launch_balance_begin(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double* t_grnd0,
+                                 double* begwb, cudaStream_t s);
+cudaError_t launch_balance_residuals(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                                     const clmgb_soilwater_fields& fw, double dtime, const double* t_ssbef,
+                                     const double* t_h2osfc_bef, const double* t_grnd0, const double* begwb,
+                                     double* errsoi, double* errh2o, cudaStream_t s);
+
 }  // namespace clmgb

@@ -527,6 +527,22 @@ int32_t clmgb_mlp_features(clmgb_handle h, const clmgb_bounds* b, const clmgb_so
 int32_t clmgb_mlp_first_dt(clmgb_handle h, int64_t nc, const float* Y, double dtime, float margin, int32_t kmax,
                            double* dt_first, void* stream);
 
+/* ---- balance residuals (soil_fluxes.jl:321-447, balance_check.jl:741-768) ----
+ * Before a step: t_grnd0[c] = t_grnd[c] and begwb[c] = the column's water (liquid +
+ * ice of the active snow and ground levels, h2osfc, h2osno_no_layers). */
+int32_t clmgb_balance_begin(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                            double* t_grnd0, double* begwb, void* stream);
+
+/* After a step (t_ssbef / t_h2osfc_bef as the step saved them): the soil energy
+ * residual errsoi[c] (W/m2: the ground heat flux linearised around t_grnd0 minus the
+ * latent heat and the storage change of the snow and soil levels) and the water
+ * residual errh2o[c] (mm: storage change minus (qflx_infl - sum qflx_rootsoi -
+ * qcharge) dtime).  Urban and lake columns get 0. */
+int32_t clmgb_balance_residuals(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                                const clmgb_soilwater_fields* fw, double dtime, const double* t_ssbef,
+                                const double* t_h2osfc_bef, const double* t_grnd0, const double* begwb,
+                                double* errsoi, double* errh2o, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
