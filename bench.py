@@ -337,6 +337,20 @@ def warm_leg(args, wl_eval):
         ms, att = run(s2, G, I, ne, mode == "warm", t_first=2)
         res[mode] = {"ms_per_step": ms / ne, "value": ne * s2.nc / (ms / 1000.0), "attempts_per_column_step": att}
         del s2
+    # ---- balance residuals of one warm-started step ----
+    s2 = wl_eval.state.to_device()
+    dtv = torch.empty(s2.nc, dtype=torch.float64, device="cuda")
+    api.synth_forcing(h, s2, G[0], I[0])
+    tg0, bw = api.balance_begin(h, s2)
+    s2["t_ssbef"].copy_(s2["t_soisno"])          # the driver records these before soil_temperature!
+    s2["t_h2osfc_bef"].copy_(s2["t_h2osfc"])
+    api.soil_temperature(h, s2, wl_eval.dtime, col_status=None)
+    api.set_soil_water_fractions(h, s2)
+    model.propose_first_dt(s2, wl_eval.dtime, cfg, out=dtv)
+    mlp.soil_water_warm(h, s2, wl_eval.dtime, dtv, cfg)
+    es, eh = api.balance_residuals(h, s2, wl_eval.dtime, tg0, bw)
+    warm_balance = {"errsoi_max_abs_w_m2": float(es.abs().max()), "errh2o_max_abs_mm": float(eh.abs().max())}
+    del s2
     # ---- error against the FP64 oracle on a sample of columns ----
     from oracle import oracle as orc
     cols = np.linspace(0, wl_eval.state.nc - 1, 256).astype(np.int64)
@@ -365,7 +379,7 @@ def warm_leg(args, wl_eval):
            "plain": res["plain"], "warm": res["warm"],
            "speedup": res["warm"]["value"] / res["plain"]["value"],
            "attempt_ratio": res["warm"]["attempts_per_column_step"] / res["plain"]["attempts_per_column_step"],
-           "max_abs_liq_error_vs_oracle_mm": errs, "error_sample_columns": 256,
+           "max_abs_liq_error_vs_oracle_mm": errs, "error_sample_columns": 256, "balance": warm_balance,
            "margin": model.margin, "margin_tuning": tune, "train_loss": hist,
            "sample_generation_s": gen_s, "training_s": train_s,
            "note": "both paths meet the same accept tolerance (xTolerUpper); the warm path only changes the "
@@ -445,6 +459,18 @@ def run_ours(args):
     elapsed_ms = t_start.elapsed_time(t_end)
     kern_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
     status = h.device_status()
+    # balance residuals of one more step (soil_fluxes.jl errsoi, balance_check.jl errh2o)
+    tg0, bw = api.balance_begin(h, d)
+    api.synth_forcing(h, d, Gd[nsteps - 1], Id[nsteps - 1], stream=stream)
+    api.column_step(h, d, wl.dtime, cfg, stream=stream)
+    es, eh = api.balance_residuals(h, d, wl.dtime, tg0, bw)
+    balance = {"errsoi_max_abs_w_m2": float(es.abs().max()), "errh2o_max_abs_mm": float(eh.abs().max()),
+               "columns_errh2o_above_1e-9_mm": int((eh.abs() > 1e-9).sum()),
+               "thresholds": {"errsoi_w_m2": 1e-5, "errh2o_mm": 1e-9},
+               "note": "state after the timed steps; the path is bit-identical to the oracle, so these are the "
+                       "reference's residuals.  Water residuals come from phase change clamping a level's liquid "
+                       "water at zero (liq = max(0, wmass0 - ice), soil_temperature.jl:2168) after the moisture-form "
+                       "update left it negative"}
     graph = None
     if not args.no_graph:
         # the same timestep sequence captured once as a CUDA graph and replayed
@@ -548,7 +574,7 @@ def run_ours(args):
                            "reserved_columns": h.get_option(abi.OPT_RESERVED_COLUMNS),
                            "queue_order": h.get_option(abi.OPT_QUEUE_ORDER)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "graph": graph, "autotune": tune,
-                "adjoint": adj_line, "warm_start": warm_line,
+                "adjoint": adj_line, "warm_start": warm_line, "balance": balance,
                 "gpu_launches": 4 * args.steps, "clocks": clocks}
         print(json.dumps(line), flush=True)
     h.close()

@@ -129,4 +129,78 @@ function CLM.soil_water!(col::CLM.ColumnData{<:Any,<:CuArray}, mask_hydrology, m
     nothing
 end
 
+# ---------------------------------------------------------------------------
+# Reverse mode.  One column step's vector-Jacobian product (clmgb_column_step_vjp)
+# behind a ChainRulesCore.rrule and an Enzyme reverse rule, the counterparts of the
+# reference's _reverse_step_into! (canopy_fluxes_reverse.jl:447-465).  `StepState`
+# bundles the CuArray fields of the step; its pullback maps the adjoints of the
+# step's outputs to those of its inputs and of the hydraulic parameters.
+# ---------------------------------------------------------------------------
+struct StepAdjoint
+    struct_size::Int64
+    lam_t_soisno::Ptr{Cvoid}; lam_h2osoi_liq::Ptr{Cvoid}; lam_h2osoi_ice::Ptr{Cvoid}
+    lam_t_grnd::Ptr{Cvoid}; lam_t_h2osfc::Ptr{Cvoid}; lam_qcharge::Ptr{Cvoid}
+    grad_watsat::Ptr{Cvoid}; grad_bsw::Ptr{Cvoid}; grad_sucsat::Ptr{Cvoid}; grad_hksat::Ptr{Cvoid}
+    lam_forc_lwrad::Ptr{Cvoid}
+end
+
+const TAPE_RESERVED = Ref(false)
+function reserve_adjoint!(slots::Integer, entries::Integer = 8192)
+    check(ccall((:clmgb_reserve_adjoint, lib), Int32, (Ptr{Cvoid}, Int64, Int64), handle(), slots, entries),
+          "clmgb_reserve_adjoint")
+    TAPE_RESERVED[] = true
+end
+
+# lam: NamedTuple of CuArrays (t_soisno, h2osoi_liq, h2osoi_ice, t_grnd, t_h2osfc,
+# qcharge, forc_lwrad) in the fields' layouts; grad: (watsat, bsw, sucsat, hksat),
+# each [nc, nlevsoi], accumulated.
+function column_step_vjp!(ft_buf, fw_buf, b::Bounds, cfg::SwmConfig, dtime, snow_method, t_ssbef, t_h2osfc_bef,
+                          lam, grad)
+    TAPE_RESERVED[] || reserve_adjoint!(b.nc)
+    a = StepAdjoint(sizeof(StepAdjoint), ptr(lam.t_soisno), ptr(lam.h2osoi_liq), ptr(lam.h2osoi_ice),
+                    ptr(lam.t_grnd), ptr(lam.t_h2osfc), ptr(lam.qcharge), ptr(grad.watsat), ptr(grad.bsw),
+                    ptr(grad.sucsat), ptr(grad.hksat), ptr(lam.forc_lwrad))
+    GC.@preserve ft_buf fw_buf begin
+        check(ccall((:clmgb_column_step_vjp, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Int32,
+                     Ptr{Cvoid}, Ptr{Cvoid}, Ref{StepAdjoint}, Ptr{UInt32}, Ptr{Cvoid}),
+                    handle(), b, ft_buf, fw_buf, cfg, dtime, snow_method, ptr(t_ssbef), ptr(t_h2osfc_bef), a,
+                    C_NULL, CUDA.stream().handle), "clmgb_column_step_vjp")
+    end
+    nothing
+end
+
+# ChainRulesCore: y = step(x, theta) on a snapshot of the state (the rule replays the
+# step from the snapshot, so the primal is not re-run by the caller).
+#   function ChainRulesCore.rrule(::typeof(CLM.column_step!), st::StepState, theta)
+#       x0 = snapshot(st)                       # device copy of the step's inputs
+#       CLM.column_step!(st, theta)
+#       function pullback(ybar)
+#           lam = adjoint_buffers(ybar); grad = zero_grads(st)
+#           restore!(st_scratch, x0)
+#           column_step_vjp!(fields(st_scratch)..., lam, grad)
+#           return NoTangent(), tangent_of_state(lam), grad
+#       end
+#       return st, pullback
+#   end
+# Enzyme: EnzymeRules.augmented_primal stores the same snapshot as its tape and
+# EnzymeRules.reverse calls column_step_vjp! with the shadow arrays as `lam`/`grad`,
+# exactly as enzyme_rules.jl does for band_solve! (augmented primal keeps A and x,
+# the reverse consumes the output shadow).
+
+# ---------------------------------------------------------------------------
+# Learned warm start: the first substep proposed by the perceptron (its weights are
+# trained by the library's kernels, see INTEGRATION.md), then soil_water! from it.
+# ---------------------------------------------------------------------------
+function soil_water_warm!(fw_buf, b::Bounds, cfg::SwmConfig, dtime, dt_first::CuArray{Float64})
+    GC.@preserve fw_buf begin
+        check(ccall((:clmgb_soil_water_warm, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Ptr{Cvoid}, Ptr{UInt32},
+                     Ptr{Cvoid}),
+                    handle(), b, fw_buf, cfg, dtime, ptr(dt_first), C_NULL, CUDA.stream().handle),
+              "clmgb_soil_water_warm")
+    end
+    nothing
+end
+
 end # module
