@@ -60,6 +60,8 @@ OPT_ADJ_TAPE_SLOTS = 10
 OPT_ADJ_TAPE_ENTRIES = 11
 OPT_ADJ_RICHARDS = 12
 ADJ_RICHARDS_CLOSED_FORM, ADJ_RICHARDS_RECORDED = 0, 1
+OPT_ADJ_SOIL_TEMPERATURE = 13
+ADJ_ST_CLOSED_FORM, ADJ_ST_RECORDED = 0, 1
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
 COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY = 32, 64, 128
@@ -70,6 +72,13 @@ CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20
 MAX_NLEVSNO = 12
 MAX_NLEVGRND = 25
 MAX_NLEVSOI = 25
+LOG_REC = MAX_NLEVSOI + 2
+LOG_FIN = 3 * MAX_NLEVSOI + 3
+
+
+def log_stride(cap):
+    """Doubles per column of a substep log with `cap` records (CLMGB_LOG_STRIDE)."""
+    return cap * LOG_REC + LOG_FIN
 
 
 class Varpar(C.Structure):
@@ -227,6 +236,12 @@ STEP_ADJOINT_MEMBERS = [("lam_t_soisno", "L"), ("lam_h2osoi_liq", "L"), ("lam_h2
 StepAdjoint = type("StepAdjoint", (C.Structure,),
                    {"_fields_": [("struct_size", C.c_int64)] + [(n, c_double_p) for n, _ in STEP_ADJOINT_MEMBERS]})
 SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
+
+
+class SubstepLog(C.Structure):
+    """clmgb_substep_log."""
+    _fields_ = [("struct_size", C.c_int64), ("rec", c_double_p), ("count", C.POINTER(C.c_int32)),
+                ("cap", C.c_int32)]
 
 
 def all_fields():

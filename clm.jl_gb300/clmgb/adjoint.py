@@ -90,17 +90,24 @@ class Trajectory:
         self.snow_method = snow_method
         self.forcing_reverse = forcing_reverse
 
-    def step(self, t, state):
+    def step(self, t, state, log=None):
+        """Step t in place; with `log` (an api.SubstepLog) the Richards solve also
+        writes the substep log the step's reverse can read."""
         self.forcing(t, state)
-        api.column_step(self.handle, state, self.dtime, self.cfg, self.snow_method)
+        if log is None:
+            api.column_step(self.handle, state, self.dtime, self.cfg, self.snow_method)
+        else:
+            api.column_step_logged(self.handle, state, self.dtime, log, self.cfg, self.snow_method)
 
-    def reverse_step(self, t, state_in, adj, col_status=None):
-        """_reverse_step_into!: state_in is the state entering step t (before its forcing)."""
+    def reverse_step(self, t, state_in, adj, col_status=None, log=None):
+        """_reverse_step_into!: state_in is the state entering step t (before its forcing);
+        `log`: the substep log of step t from the same state, or None."""
         before = None
         if self.forcing_reverse is not None:
             before = {"t_grnd": state_in["t_grnd"].clone()}
         self.forcing(t, state_in)
-        api.column_step_vjp(self.handle, state_in, self.dtime, adj, self.cfg, self.snow_method, col_status)
+        api.column_step_vjp(self.handle, state_in, self.dtime, adj, self.cfg, self.snow_method, col_status,
+                            log=log)
         if self.forcing_reverse is not None:
             self.forcing_reverse(t, before, adj)
 
@@ -114,13 +121,17 @@ def synth_forcing_reverse(t, before, adj):
     adj.lam_t_grnd += 4.0 * SB * tg * tg * tg * adj.lam_forc_lwrad
 
 
-def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_status=None, events=None):
+def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_status=None, events=None,
+                      log_cap=24):
     """Forward through traj from `state` (left holding the final state), keeping a
     checkpoint every `checkpoint_every` steps; then reverse, recomputing each segment's
     step-entry states from its checkpoint.  observe(t, state_after_t) runs after every
     forward step (the loss's forward half).  `events`, three CUDA events, are recorded
-    at the start, between the forward and the reverse pass, and at the end.  Returns
-    the adjoint buffers."""
+    at the start, between the forward and the reverse pass, and at the end.  The
+    recomputed steps write substep logs (`log_cap` records per column; 0: no logs) so
+    that their reverses do not run the Richards substep loop again; the last step of a
+    segment is not recomputed and its reverse runs the loop itself.  Returns the
+    adjoint buffers."""
     k = max(1, int(checkpoint_every))
     if events is not None:
         events[0].record()
@@ -135,15 +146,17 @@ def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_s
         events[1].record()
     adj = StepAdjointBuffers(state)
     seg_states = [state.copy() for _ in range(min(k, traj.nsteps))]
+    logs = [api.SubstepLog(state.nc, log_cap) for _ in range(min(k, traj.nsteps) - 1)] if log_cap > 0 else []
     for s in range(len(ckpt) - 1, -1, -1):
         t0, t1 = s * k, min((s + 1) * k, traj.nsteps)
         copy_state_(seg_states[0], ckpt[s])
         for t in range(t0, t1 - 1):
             copy_state_(seg_states[t - t0 + 1], seg_states[t - t0])
-            traj.step(t, seg_states[t - t0 + 1])
+            traj.step(t, seg_states[t - t0 + 1], logs[t - t0] if logs else None)
         for t in range(t1 - 1, t0 - 1, -1):
             seed(t, adj)
-            traj.reverse_step(t, seg_states[t - t0], adj, col_status)
+            lg = logs[t - t0] if (logs and t < t1 - 1) else None
+            traj.reverse_step(t, seg_states[t - t0], adj, col_status, log=lg)
     if events is not None:
         events[2].record()
     return adj

@@ -125,21 +125,57 @@ def column_step(handle, state, dtime, cfg=None, snow_method=abi.SNOW_JORDAN1991,
                                        _stream(stream)), "column_step")
 
 
+class SubstepLog:
+    """Device buffers of a clmgb_substep_log for `nc` columns, `cap` records each."""
+
+    def __init__(self, nc, cap=24, device="cuda"):
+        import torch
+        self.nc, self.cap = int(nc), int(cap)
+        self.rec = torch.empty(self.nc * abi.log_stride(self.cap), dtype=torch.float64, device=device)
+        self.count = torch.full((self.nc,), -1, dtype=torch.int32, device=device)
+
+    def struct(self):
+        s = abi.SubstepLog()
+        s.struct_size = C.sizeof(abi.SubstepLog)
+        s.rec = C.cast(C.c_void_p(self.rec.data_ptr()), abi.c_double_p)
+        s.count = C.cast(C.c_void_p(self.count.data_ptr()), C.POINTER(C.c_int32))
+        s.cap = self.cap
+        return s
+
+
+def column_step_logged(handle, state, dtime, log, cfg=None, snow_method=abi.SNOW_JORDAN1991, col_status=None,
+                       save_bef=True, stream=None):
+    """column_step that also writes the substep log `log` (a SubstepLog) for the reverse."""
+    _require_device(state)
+    cfg = cfg or abi.SwmConfig.clm5_default()
+    ft, fw, b = state.soiltemp_fields(), state.soilwater_fields(), state.bounds()
+    tss = _dptr(state["t_ssbef"]) if save_bef else None
+    thb = _dptr(state["t_h2osfc_bef"]) if save_bef else None
+    lg = log.struct()
+    check(handle.lib.clmgb_column_step_logged(handle.h, C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg),
+                                              float(dtime), snow_method, tss, thb, C.byref(lg),
+                                              _dptr(col_status, "col_status"), _stream(stream)),
+          "column_step_logged")
+
+
 def column_step_vjp(handle, state, dtime, adj, cfg=None, snow_method=abi.SNOW_JORDAN1991, col_status=None,
-                    save_bef=True, stream=None):
+                    save_bef=True, stream=None, log=None):
     """Reverse of column_step from the state it starts from (advances `state` like
     column_step does).  `adj` is a clmgb.adjoint.StepAdjointBuffers: its lam_* hold the
     adjoints of the step's outputs on entry and of its inputs on return; grad_*
-    accumulate."""
+    accumulate.  `log`: the SubstepLog column_step_logged wrote from the same state,
+    or None."""
     _require_device(state)
     cfg = cfg or abi.SwmConfig.clm5_default()
     ft, fw, b = state.soiltemp_fields(), state.soilwater_fields(), state.bounds()
     tss = _dptr(state["t_ssbef"]) if save_bef else None
     thb = _dptr(state["t_h2osfc_bef"]) if save_bef else None
     a = adj.struct()
-    check(handle.lib.clmgb_column_step_vjp(handle.h, C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg),
-                                           float(dtime), snow_method, tss, thb, C.byref(a),
-                                           _dptr(col_status, "col_status"), _stream(stream)), "column_step_vjp")
+    lg = C.byref(log.struct()) if log is not None else None
+    check(handle.lib.clmgb_column_step_vjp_logged(handle.h, C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg),
+                                                  float(dtime), snow_method, tss, thb, C.byref(a), lg,
+                                                  _dptr(col_status, "col_status"), _stream(stream)),
+          "column_step_vjp")
 
 
 def phase_change_h2osfc(handle, state, dtime, dhsdT, stream=None):

@@ -39,6 +39,7 @@ struct clmgb_handle_s {
   // tape of the column-step adjoint (clmgb_reserve_adjoint, one allocation)
   void* tape_block;
   clmgb::AdjTape tape;
+  int64_t adj_st_mode;          // CLMGB_OPT_ADJ_SOIL_TEMPERATURE
   cudaError_t last_error;
 };
 
@@ -137,6 +138,9 @@ static int queue_grid(clmgb_handle h) {
   if (per_sm > h->occupancy_blocks) per_sm = h->occupancy_blocks;
   return per_sm * h->num_sms;
 }
+
+// resident blocks of the hand-written step adjoint over the device
+static int vjp_grid(clmgb_handle h) { return clmgb::vjp_cf_blocks_per_sm() * h->num_sms; }
 
 extern "C" {
 
@@ -437,6 +441,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value != CLMGB_ADJ_RICHARDS_CLOSED_FORM && value != CLMGB_ADJ_RICHARDS_RECORDED) return CLMGB_ERR_CONFIG;
       h->tape.richards_mode = (int)value;
       return CLMGB_OK;
+    case CLMGB_OPT_ADJ_SOIL_TEMPERATURE:
+      if (value != CLMGB_ADJ_ST_CLOSED_FORM && value != CLMGB_ADJ_ST_RECORDED) return CLMGB_ERR_CONFIG;
+      h->adj_st_mode = value;
+      return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
   }
@@ -456,6 +464,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_WAVES_OCCUPANCY: *value = h->waves_blocks; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_SLOTS: *value = h->tape.slots; return CLMGB_OK;
     case CLMGB_OPT_ADJ_RICHARDS: *value = h->tape.richards_mode; return CLMGB_OK;
+    case CLMGB_OPT_ADJ_SOIL_TEMPERATURE: *value = h->adj_st_mode; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_USED: {
       unsigned int used = 0;
@@ -572,10 +581,59 @@ int32_t clmgb_reserve_adjoint(clmgb_handle h, int64_t slots, int64_t entries) {
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+static int32_t check_log(const clmgb_substep_log* log) {
+  if (!log) return CLMGB_OK;
+  if (log->struct_size != (int64_t)sizeof(clmgb_substep_log)) return CLMGB_ERR_ABI;
+  if (!log->rec || !log->count) return CLMGB_ERR_NULL_ARG;
+  if (log->cap < 1 || log->cap > CLMGB_ADJ_MAX_SUBSTEPS) return CLMGB_ERR_CONFIG;
+  return CLMGB_OK;
+}
+
+static clmgb::SubstepLogView log_view(const clmgb_substep_log* log) {
+  if (!log) return clmgb::SubstepLogView{nullptr, nullptr, 0, 0};
+  return clmgb::SubstepLogView{log->rec, log->count, (int)log->cap, CLMGB_LOG_STRIDE(log->cap)};
+}
+
+int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                                 const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
+                                 int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                                 const clmgb_substep_log* log, uint32_t* col_status, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_cfg(cfg);
+  if (e) return e;
+  if ((e = check_bounds(b, true))) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(ft))) return e;
+  if ((e = check_fields(fw))) return e;
+  if (!log) return CLMGB_ERR_NULL_ARG;
+  if ((e = check_log(log))) return e;
+  if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  const Dims D = make_dims(h->vp, *b);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t ce = clmgb::launch_soiltemp_fractions(D, b->nc, *ft, *fw, dtime, snow_method, t_ssbef, t_h2osfc_bef,
+                                                    col_status, h->dev_status, s);
+  if (ce == cudaSuccess) {
+    const clmgb::SubstepLogView lv = log_view(log);
+    ce = clmgb::launch_moisture_form_queue(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->queue,
+                                           queue_grid(h), queue_scratch(h), s, nullptr, &lv);
+  }
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
                               const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
                               int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
                               const clmgb_step_adjoint* adj, uint32_t* col_status, void* stream) {
+  return clmgb_column_step_vjp_logged(h, b, ft, fw, cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef, adj, nullptr,
+                                      col_status, stream);
+}
+
+int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                                     const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
+                                     int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                                     const clmgb_step_adjoint* adj, const clmgb_substep_log* log,
+                                     uint32_t* col_status, void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_cfg(cfg);
   if (e) return e;
@@ -592,9 +650,15 @@ int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!h->tape_block) return CLMGB_ERR_CONFIG;
   const Dims D = make_dims(h->vp, *b);
-  cudaError_t ce = clmgb::launch_column_step_vjp(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef,
-                                                 t_h2osfc_bef, *adj, h->tape, col_status, h->dev_status,
-                                                 (cudaStream_t)stream);
+  if ((e = check_log(log))) return e;
+  cudaError_t ce;
+  if (h->adj_st_mode == CLMGB_ADJ_ST_CLOSED_FORM && h->tape.richards_mode == CLMGB_ADJ_RICHARDS_CLOSED_FORM)
+    ce = clmgb::launch_column_step_vjp_cf(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef, *adj,
+                                          h->tape, log_view(log), h->queue, vjp_grid(h), col_status, h->dev_status,
+                                          (cudaStream_t)stream);
+  else
+    ce = clmgb::launch_column_step_vjp(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef, *adj,
+                                       h->tape, col_status, h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 

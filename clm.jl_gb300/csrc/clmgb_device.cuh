@@ -107,33 +107,6 @@ __device__ __forceinline__ bool is_wallroof(int64_t it) {
 // (adjoint_step.cu) overloads it.
 __device__ __forceinline__ double VAL(double x) { return x; }
 
-// Where a column's active state lives.  The production kernels read and write the
-// caller's fields in place (FieldState over clmgb_soiltemp_fields or
-// clmgb_soilwater_fields; only the members a kernel uses are instantiated).  The
-// step adjoint keeps the same quantities in per-thread storage with their tape
-// indices.  Every column function below takes its state through such an accessor
-// X, with X::S the scalar type of the active quantities.
-template <class F>
-struct FieldState {
-  typedef double S;
-  const F& f;
-  int64_t c, ld;
-  __device__ __forceinline__ FieldState(const F& ff, int64_t cc, int64_t l) : f(ff), c(cc), ld(l) {}
-  __device__ __forceinline__ decltype(auto) T(int jj) const { return LV(f.t_soisno, c, jj, ld); }
-  __device__ __forceinline__ decltype(auto) Liq(int jj) const { return LV(f.h2osoi_liq, c, jj, ld); }
-  __device__ __forceinline__ decltype(auto) Ice(int jj) const { return LV(f.h2osoi_ice, c, jj, ld); }
-  __device__ __forceinline__ decltype(auto) Fact(int jj) const { return LV(f.fact, c, jj, ld); }
-  __device__ __forceinline__ decltype(auto) Icefrac(int j) const { return LV(f.icefrac, c, j, ld); }
-  __device__ __forceinline__ decltype(auto) Tgrnd() const { return f.t_grnd[c]; }
-  __device__ __forceinline__ decltype(auto) Th2osfc() const { return f.t_h2osfc[c]; }
-  __device__ __forceinline__ decltype(auto) Qcharge() const { return f.qcharge[c]; }
-  __device__ __forceinline__ double ForcLwrad() const { return f.forc_lwrad[c]; }
-  __device__ __forceinline__ double Watsat(int j) const { return LVc(f.watsat, c, j, ld); }
-  __device__ __forceinline__ double Bsw(int j) const { return LVc(f.bsw, c, j, ld); }
-  __device__ __forceinline__ double Sucsat(int j) const { return LVc(f.sucsat, c, j, ld); }
-  __device__ __forceinline__ double Hksat(int j) const { return LVc(f.hksat, c, j, ld); }
-};
-
 // ===========================================================================
 // Banded pivoted LU for one column (band_diagonal.jl:87-170).
 //
@@ -255,6 +228,36 @@ __device__ __forceinline__ void band_lu_transpose_solve(const double* ab, const 
   }
 #undef AB
 }
+
+// Where a column's active state lives.  The production kernels read and write the
+// caller's fields in place (FieldState over clmgb_soiltemp_fields or
+// clmgb_soilwater_fields; only the members a kernel uses are instantiated).  The
+// step adjoint keeps the same quantities in per-thread storage with their tape
+// indices.  Every column function below takes its state through such an accessor
+// X, with X::S the scalar type of the active quantities, and the banded solve of
+// soil_temperature! goes through X.band_solve.
+template <class F>
+struct FieldState {
+  typedef double S;
+  const F& f;
+  int64_t c, ld;
+  __device__ __forceinline__ FieldState(const F& ff, int64_t cc, int64_t l) : f(ff), c(cc), ld(l) {}
+  __device__ __forceinline__ decltype(auto) T(int jj) const { return LV(f.t_soisno, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Liq(int jj) const { return LV(f.h2osoi_liq, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Ice(int jj) const { return LV(f.h2osoi_ice, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Fact(int jj) const { return LV(f.fact, c, jj, ld); }
+  __device__ __forceinline__ decltype(auto) Icefrac(int j) const { return LV(f.icefrac, c, j, ld); }
+  __device__ __forceinline__ decltype(auto) Tgrnd() const { return f.t_grnd[c]; }
+  __device__ __forceinline__ decltype(auto) Th2osfc() const { return f.t_h2osfc[c]; }
+  __device__ __forceinline__ decltype(auto) Qcharge() const { return f.qcharge[c]; }
+  __device__ __forceinline__ double ForcLwrad() const { return f.forc_lwrad[c]; }
+  __device__ __forceinline__ double Watsat(int j) const { return LVc(f.watsat, c, j, ld); }
+  __device__ __forceinline__ double Bsw(int j) const { return LVc(f.bsw, c, j, ld); }
+  __device__ __forceinline__ double Sucsat(int j) const { return LVc(f.sucsat, c, j, ld); }
+  __device__ __forceinline__ double Hksat(int j) const { return LVc(f.hksat, c, j, ld); }
+  // the banded solve of soil_temperature! (ab, x: the column's band rows and right-hand side)
+  __device__ __forceinline__ void band_solve(double* ab, double* x, int n) const { band_lu_solve<2, 2>(ab, x, n); }
+};
 
 // ===========================================================================
 // phase_change_h2osfc! (soil_temperature.jl:1757-1855), column c.
@@ -828,7 +831,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   if (n > 1) ab[1 * W + 0] = 0.0;
 
   // ---- batched_band_solve! (band_diagonal.jl:87-170), banded form ----
-  band_lu_solve<2, 2>(ab, x, n);
+  X.band_solve(ab, x, n);
 
   // ---- _tvector_extract_kernel! (:149-167) ----
   for (int j = jtop; j <= 0; j++) tt[j + joff] = x[j - jtop];
@@ -941,6 +944,13 @@ struct MfLaneT {
   S gam[MAXSOI + 1], dwat[MAXSOI + 1];
 };
 typedef MfLaneT<double> MfLane;
+
+// Substep log record (clmgb_substep_log): the liquid water of levels 1..nlevsoi at
+// the start of an accepted substep, its dtsub, the time done before it.  After a
+// column's cap records: its final liquid water, smp_l, hk_l (nlevsoi each),
+// qcharge, attempts and status.
+constexpr int SUB_REC = MAXSOI + 2;
+constexpr int LOG_FIN = 3 * MAXSOI + 3;
 
 // Ice impedance 10^(-e_ice*icefrac) of layer j (interface mean above the bottom
 // layer), as formed at soil_water_movement.jl:1287-1293.

@@ -93,16 +93,21 @@ k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb
 // expected first) and the impedances come precomputed in imp_cache.  The
 // per-column arithmetic is unchanged, so results do not depend on the schedule.
 // `queue` must be zero at launch.
+// With LOG the kernel also writes the substep log of every column it solves (the
+// starting water of each accepted substep and the solve's outputs), for the step
+// adjoint; the solve itself is unchanged.
+template <bool LOG>
 __global__ void __launch_bounds__(BLOCK)
 k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                       uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
                       const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
-                      int64_t ld_imp, const double* dt_init) {
+                      int64_t ld_imp, const double* dt_init, SubstepLogView lg) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned long long nq = order ? (unsigned long long)(*(volatile const unsigned int*)nlisted_ptr)
                                       : (unsigned long long)nc;
   MfLane L;
+  int nacc = 0;
   bool active = false, exhausted = false;
   for (;;) {
     const bool need = !active && !exhausted;
@@ -121,6 +126,7 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
           if (order || f.mask_hydrology[c]) {
             if (mf_begin(L, D, f, cfg, dtime, c, imp_cache, ld_imp, dt_init)) {
               active = true;
+              nacc = 0;
             } else {
               const uint32_t st = L.status;
               if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
@@ -136,8 +142,38 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
       if (__all_sync(FULL, exhausted)) break;
       continue;
     }
-    if (active && mf_attempt(L, D, f, cfg, dtime)) {
+    if (!active) continue;
+    double* rec = nullptr;
+    double dts = 0.0, dtd = 0.0;
+    if (LOG) {
+      rec = lg.rec + L.c * lg.stride;
+      if (L.fresh && nacc < lg.cap)
+        for (int j = 1; j <= L.nlayers; j++) rec[(int64_t)nacc * SUB_REC + j - 1] = L.liq[j];
+      dts = L.dtsub;
+      dtd = L.dtdone;
+    }
+    const bool fin = mf_attempt(L, D, f, cfg, dtime);
+    if (LOG && L.dtdone != dtd) {
+      if (nacc < lg.cap) {
+        rec[(int64_t)nacc * SUB_REC + MAXSOI] = dts;
+        rec[(int64_t)nacc * SUB_REC + MAXSOI + 1] = dtd;
+      }
+      nacc++;
+    }
+    if (fin) {
       const uint32_t st = mf_end(L, D, f);
+      if (LOG) {
+        double* out = rec + (int64_t)lg.cap * SUB_REC;
+        for (int j = 1; j <= L.nlayers; j++) {
+          out[j - 1] = L.liq[j];
+          out[MAXSOI + j - 1] = LV(f.smp_l, L.c, j, D.ldc);
+          out[2 * MAXSOI + j - 1] = LV(f.hk_l, L.c, j, D.ldc);
+        }
+        out[3 * MAXSOI] = L.qc;
+        out[3 * MAXSOI + 1] = (double)L.nsub;
+        out[3 * MAXSOI + 2] = (double)st;
+        lg.count[L.c] = nacc;
+      }
       if (col_status) col_status[L.c] = or_status ? (col_status[L.c] | st) : st;
       if (st && dev_status) atomicOr(dev_status, st);
       active = false;
@@ -345,16 +381,18 @@ cudaError_t launch_soiltemp_fractions(const Dims& D, int64_t nc, const clmgb_soi
 }
 int queue_blocks_per_sm() {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_moisture_form_queue, BLOCK, 0) != cudaSuccess) nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_moisture_form_queue<false>, BLOCK, 0) != cudaSuccess)
+    nb = 1;
   return nb > 0 ? nb : 1;
 }
 cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
                                        int grid_blocks, const QueueScratch& qs, cudaStream_t s,
-                                       const double* dt_init) {
+                                       const double* dt_init, const SubstepLogView* log) {
   cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
+  if (log && (e = cudaMemsetAsync(log->count, 0xff, (size_t)nc * sizeof(int32_t), s)) != cudaSuccess) return e;
   const bool use = qs.capacity >= nc && qs.order && qs.bins && qs.imp;
   if (use) {
     k_impedance<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg.e_ice, qs.imp, qs.capacity);
@@ -371,11 +409,18 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   const int64_t need = (nc + BLOCK - 1) / BLOCK;
   const int grid = (int)(need < grid_blocks ? need : grid_blocks);
   const bool listed = use && qs.longest_first;
-  k_moisture_form_queue<<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status,
-                                                              queue, listed ? qs.order : nullptr,
-                                                              listed ? qs.bins + 2 * ORDER_BINS : nullptr,
-                                                              use ? qs.imp : nullptr, use ? qs.capacity : 0,
-                                                              dt_init);
+  const uint32_t* ord = listed ? qs.order : nullptr;
+  const unsigned int* nl = listed ? qs.bins + 2 * ORDER_BINS : nullptr;
+  const double* imp = use ? qs.imp : nullptr;
+  const int64_t ldi = use ? qs.capacity : 0;
+  if (log)
+    k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
+                                                                      dev_status, queue, ord, nl, imp, ldi, dt_init,
+                                                                      *log);
+  else
+    k_moisture_form_queue<false><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
+                                                                       dev_status, queue, ord, nl, imp, ldi, dt_init,
+                                                                       SubstepLogView{nullptr, nullptr, 0, 0});
   return cudaGetLastError();
 }
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {

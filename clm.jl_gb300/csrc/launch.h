@@ -44,6 +44,18 @@ struct AdjTape {
   int richards_mode;
 };
 
+// A substep log of the moisture-form solve (clmgb_substep_log): per column a region
+// of `stride` doubles at rec + c*stride holding up to `cap` records of SUB_REC
+// doubles (the liquid water at the start of an accepted substep, its dtsub and the
+// time done before it) followed by the solve's outputs; count[c] = accepted
+// substeps (-1: the column was not solved).  rec == nullptr: no log.
+struct SubstepLogView {
+  double* rec;
+  int32_t* count;
+  int cap;
+  int64_t stride;
+};
+
 // All launchers return the cudaError_t of the launch (cudaGetLastError()).
 cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
                                     int snow_method, uint32_t* col_status, uint32_t* dev_status,
@@ -77,7 +89,7 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
                                        int grid_blocks, const QueueScratch& qs, cudaStream_t s,
-                                       const double* dt_init = nullptr);
+                                       const double* dt_init = nullptr, const SubstepLogView* log = nullptr);
 cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                       cudaStream_t s);
@@ -92,6 +104,13 @@ cudaError_t launch_column_step_vjp(const Dims& D, int64_t nc, const clmgb_soilte
                                    int snow_method, double* t_ssbef, double* t_h2osfc_bef,
                                    const clmgb_step_adjoint& adj, const AdjTape& tp, uint32_t* col_status,
                                    uint32_t* dev_status, cudaStream_t s);
+int vjp_cf_blocks_per_sm();
+cudaError_t launch_column_step_vjp_cf(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
+                                      const clmgb_soilwater_fields& fw, const clmgb_swm_config& cfg, double dtime,
+                                      int snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                                      const clmgb_step_adjoint& adj, const AdjTape& tp, const SubstepLogView& lg,
+                                      unsigned long long* queue, int grid_blocks, uint32_t* col_status,
+                                      uint32_t* dev_status, cudaStream_t s);
 cudaError_t launch_band_factor_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const double* bmatrix,
                                      const double* rvector, const int64_t* jtop, const int64_t* jbot,
                                      const uint8_t* mask, int kl, int ku, int nlevsno_off, double* lu, uint8_t* piv,

@@ -276,6 +276,10 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
 #define CLMGB_OPT_ADJ_RICHARDS        12  /* how clmgb_column_step_vjp reverses the Richards substeps: */
 #define   CLMGB_ADJ_RICHARDS_CLOSED_FORM 0 /*   hand-written reverse of each accepted substep (default) */
 #define   CLMGB_ADJ_RICHARDS_RECORDED    1 /*   each substep replayed through the recording scalar */
+#define CLMGB_OPT_ADJ_SOIL_TEMPERATURE 13 /* how clmgb_column_step_vjp reverses soil_temperature!: */
+#define   CLMGB_ADJ_ST_CLOSED_FORM       0 /*   hand-written reverse of every stage, no tape (default;
+                                                 used when CLMGB_OPT_ADJ_RICHARDS is closed form too) */
+#define   CLMGB_ADJ_ST_RECORDED          1 /*   replayed through the recording scalar and swept */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
 /* Gives the handle per-column scratch for up to max_nc columns (about 48*nlevsoi + 80
  * bytes per column): the Richards solve then forms the ice impedances in a uniform
@@ -461,6 +465,44 @@ int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb
                               double dtime, int32_t snow_method, double* t_ssbef,
                               double* t_h2osfc_bef, const clmgb_step_adjoint* adj,
                               uint32_t* col_status, void* stream);
+
+/* Substep log of the moisture-form solve: what the reverse of a step needs from its
+ * forward Richards solve, written by clmgb_column_step_logged and read by
+ * clmgb_column_step_vjp_logged, so that the reverse does not run the substep loop
+ * again.  rec holds, per column c, CLMGB_LOG_STRIDE(cap) doubles at
+ * rec + c*CLMGB_LOG_STRIDE(cap): up to cap records of CLMGB_LOG_REC doubles (the
+ * liquid water of levels 1..CLMGB_MAX_NLEVSOI at the start of an accepted substep,
+ * its dtsub, the time done before it), then CLMGB_LOG_FIN doubles of the solve's
+ * outputs (final liquid water, smp_l, hk_l, qcharge, attempts, status).  count[c]
+ * (int32, [nc]) gets the accepted substeps, -1 for a column that was not solved; a
+ * column with more than cap is reversed by running its substep loop again.  No
+ * counterpart in the reference (Enzyme keeps its own tape). */
+#define CLMGB_LOG_REC (CLMGB_MAX_NLEVSOI + 2)
+#define CLMGB_LOG_FIN (3 * CLMGB_MAX_NLEVSOI + 3)
+#define CLMGB_LOG_STRIDE(cap) ((int64_t)(cap) * CLMGB_LOG_REC + CLMGB_LOG_FIN)
+typedef struct clmgb_substep_log {
+  int64_t struct_size;               /* sizeof(clmgb_substep_log) */
+  double* rec;                       /* [nc * CLMGB_LOG_STRIDE(cap)] */
+  int32_t* count;                    /* [nc] */
+  int32_t cap;                       /* records per column, 1..CLMGB_ADJ_MAX_SUBSTEPS */
+} clmgb_substep_log;
+
+/* clmgb_column_step that also writes the substep log (the Richards solve runs on the
+ * work-queue schedule whatever CLMGB_OPT_STEP_SCHEDULE says; results are the same
+ * bits). */
+int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                                 const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
+                                 int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                                 const clmgb_substep_log* log, uint32_t* col_status, void* stream);
+
+/* clmgb_column_step_vjp taking the substep log the forward step wrote from the same
+ * input state (log may be NULL: the same as clmgb_column_step_vjp).  The
+ * recording kernels (CLMGB_ADJ_*_RECORDED) do not read the log. */
+int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
+                                     const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
+                                     int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
+                                     const clmgb_step_adjoint* adj, const clmgb_substep_log* log,
+                                     uint32_t* col_status, void* stream);
 
 /* ---- learned warm start of the moisture-form solve ----
  * A 64 -> 128 -> 128 -> 21 perceptron (SiLU hidden layers, BF16 weights and

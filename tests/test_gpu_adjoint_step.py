@@ -245,7 +245,8 @@ def test_richards_gradient_vs_complex_step(handle):
 
 def test_closed_form_substep_reverse_matches_recorded_replay(handle):
     """The hand-written reverse of a Richards substep and the recorded replay of the
-    same substep differentiate the same arithmetic: they agree to rounding."""
+    same substep differentiate the same arithmetic: they agree to rounding (both with
+    soil_temperature! recorded, so only the substep reverse differs)."""
     cfg = _cfg_flux()
     nsteps = 4
     wl, G, I = _workload(256, nsteps, seed=555)
@@ -253,6 +254,7 @@ def test_closed_form_substep_reverse_matches_recorded_replay(handle):
     st0 = wl.state.to_device()
     tgt = torch.zeros((nsteps, st0.nc), dtype=torch.float64, device="cuda")
     out = {}
+    handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_RECORDED)
     try:
         for mode in (abi.ADJ_RICHARDS_CLOSED_FORM, abi.ADJ_RICHARDS_RECORDED):
             handle.set_option(abi.OPT_ADJ_RICHARDS, mode)
@@ -265,6 +267,7 @@ def test_closed_form_substep_reverse_matches_recorded_replay(handle):
                                  [adj.lam_h2osoi_liq.cpu().numpy()[st0.vp.nlevsno:st0.vp.nlevsno + 20]])
     finally:
         handle.set_option(abi.OPT_ADJ_RICHARDS, abi.ADJ_RICHARDS_CLOSED_FORM)
+        handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_CLOSED_FORM)
     a, b = out[abi.ADJ_RICHARDS_CLOSED_FORM], out[abi.ADJ_RICHARDS_RECORDED]
     scale = np.max(np.abs(b), axis=(0, 1))
     rel = np.max(np.abs(a - b), axis=(0, 1)) / np.maximum(scale, 1e-300)
@@ -311,9 +314,16 @@ def test_tape_overflow_and_unsupported_state_are_flagged():
         adj = adjoint.StepAdjointBuffers(st)
         status = torch.zeros(st.nc, dtype=torch.int32, device="cuda")
         h.reserve_adjoint(128, 256)
+        h.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_RECORDED)   # only the recording kernel has a tape
         api.column_step_vjp(h, st.copy(), wl.dtime, adj, cfg, col_status=status)
         s = status.cpu().numpy()
         assert np.all(s & abi.COL_TAPE_FULL)
+        h.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_CLOSED_FORM)
+        api.column_step_vjp(h, st.copy(), wl.dtime, adj, cfg, col_status=status)
+        s = status.cpu().numpy()
+        assert s[3] & abi.COL_ADJ_UNSUPPORTED
+        assert np.all((np.delete(s, 3) & (abi.COL_ADJ_UNSUPPORTED | abi.COL_TAPE_FULL)) == 0)
+        h.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_RECORDED)
         h.reserve_adjoint(128, 8192)
         api.column_step_vjp(h, st.copy(), wl.dtime, adj, cfg, col_status=status)
         s = status.cpu().numpy()
@@ -333,3 +343,128 @@ def test_vjp_requires_reserved_tape():
             api.column_step_vjp(h, st, wl.dtime, adj)
     finally:
         h.close()
+
+
+class _LinearSeed:
+    """A fixed random linear functional of every step's outputs: temperatures, liquid
+    water, ice, t_grnd, t_h2osfc and qcharge all carry adjoint."""
+
+    def __init__(self, st0, nsteps, seed):
+        rng = np.random.default_rng(seed)
+        shp = tuple(st0["t_soisno"].shape)
+        nc = st0.nc
+        t = lambda *s: torch.from_numpy(rng.normal(size=s)).cuda()  # noqa: E731
+        self.w = [dict(t=t(*shp), l=t(*shp), i=t(*shp), g=t(nc), h=t(nc), q=t(nc)) for _ in range(nsteps)]
+
+    def seed(self, t, adj):
+        w = self.w[t]
+        adj.lam_t_soisno += w["t"]
+        adj.lam_h2osoi_liq += w["l"]
+        adj.lam_h2osoi_ice += w["i"]
+        adj.lam_t_grnd += w["g"]
+        adj.lam_t_h2osfc += w["h"]
+        adj.lam_qcharge.copy_(w["q"])
+
+
+def _adjoint_arrays(adj):
+    out = {k: getattr(adj, k).clone() for k in ("lam_t_soisno", "lam_h2osoi_liq", "lam_h2osoi_ice", "lam_t_grnd",
+                                                 "lam_t_h2osfc")}
+    out.update({"grad_" + p: adj.grad[p].clone() for p in adjoint.PARAMS})
+    return out
+
+
+def _traj_method(h, wl, G, I, nsteps, cfg, method):
+    def forcing(t, st):
+        api.synth_forcing(h, st, G[t], I[t])
+    return adjoint.Trajectory(h, nsteps, wl.dtime, forcing, cfg, snow_method=method,
+                              forcing_reverse=adjoint.synth_forcing_reverse)
+
+
+@pytest.mark.parametrize("cfg_id,method", [(1, abi.SNOW_JORDAN1991), (1, abi.SNOW_STURM1997),
+                                           (2, abi.SNOW_JORDAN1991)])
+def test_closed_form_step_adjoint_matches_recorded(handle, cfg_id, method):
+    """The hand-written reverse of the whole step (soil_temperature! stage by stage,
+    fractions, impedance, substeps) and the recording kernel differentiate the same
+    arithmetic: every input adjoint and parameter gradient agrees to rounding, per
+    column relative to the column's largest entry of that quantity."""
+    cfg = _cfg_flux()
+    nsteps = 4
+    wl, G, I = _workload_cfg(cfg_id, 512, nsteps, seed=31 + cfg_id)
+    traj = _traj_method(handle, wl, G, I, nsteps, cfg, method)
+    st0 = wl.state.to_device()
+    lin = _LinearSeed(st0, nsteps, 7 + cfg_id)
+    out, stat = {}, {}
+    try:
+        for mode in (abi.ADJ_ST_CLOSED_FORM, abi.ADJ_ST_RECORDED):
+            handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, mode)
+            status = torch.zeros(st0.nc, dtype=torch.int32, device="cuda")
+            adj = adjoint.multistep_reverse(traj, st0.copy(), lin.seed, None, checkpoint_every=2, col_status=status)
+            out[mode] = _adjoint_arrays(adj)
+            stat[mode] = status.cpu().numpy()
+    finally:
+        handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_CLOSED_FORM)
+    assert np.all((stat[abi.ADJ_ST_CLOSED_FORM] & abi.COL_TAPE_FULL) == 0)
+    assert np.all((stat[abi.ADJ_ST_RECORDED] & abi.COL_TAPE_FULL) == 0)
+    ok = (stat[abi.ADJ_ST_CLOSED_FORM] & abi.COL_ADJ_UNSUPPORTED) == 0
+    assert ok.mean() > 0.5
+    worst = 0.0
+    for k in out[abi.ADJ_ST_CLOSED_FORM]:
+        a = out[abi.ADJ_ST_CLOSED_FORM][k].cpu().numpy()
+        b = out[abi.ADJ_ST_RECORDED][k].cpu().numpy()
+        assert np.isfinite(a).all(), k
+        if a.ndim == 1:
+            a, b = a[None, :], b[None, :]
+        scale = np.max(np.abs(b), axis=0)
+        rel = np.max(np.abs(a - b), axis=0) / np.maximum(scale, 1e-300)
+        rel = rel[ok & (scale > 0)]
+        if rel.size:
+            print("%s: max rel diff %.3g" % (k, rel.max()))
+            worst = max(worst, rel.max())
+    assert worst < 1e-9, worst
+
+
+def test_substep_log_gives_the_same_bits(handle):
+    """The reverse reading the substep log of the recomputed forward, running the
+    substep loop itself (no log), or mixing both (a log too small for some columns)
+    gives the same bits."""
+    cfg = _cfg_flux()
+    nsteps = 6
+    wl, G, I = _workload(384, nsteps, seed=808)
+    traj = _traj(handle, wl, G, I, nsteps, cfg)
+    st0 = wl.state.to_device()
+    lin = _LinearSeed(st0, nsteps, 3)
+    res = {}
+    for cap in (0, 24, 2):
+        adj = adjoint.multistep_reverse(traj, st0.copy(), lin.seed, None, checkpoint_every=3, log_cap=cap)
+        res[cap] = _adjoint_arrays(adj)
+    for cap in (24, 2):
+        for k in res[0]:
+            assert torch.equal(res[0][k], res[cap][k]), (cap, k)
+
+
+def test_logged_step_is_the_production_step(handle):
+    cfg = _cfg_flux()
+    wl, G, I = _workload(600, 3, seed=99)
+    a = wl.state.to_device()
+    b = a.copy()
+    log = api.SubstepLog(a.nc, 16)
+    for t in range(3):
+        api.synth_forcing(handle, a, G[t], I[t])
+        api.column_step(handle, a, wl.dtime, cfg)
+        api.synth_forcing(handle, b, G[t], I[t])
+        api.column_step_logged(handle, b, wl.dtime, log, cfg)
+        torch.cuda.synchronize()
+        for k in a.arrays:
+            assert torch.equal(a[k], b[k]), "step %d field %s" % (t, k)
+        cnt = log.count.cpu().numpy()
+        hyd = b["mask_hydrology"].cpu().numpy() != 0
+        assert np.all(cnt[hyd] >= 1) and np.all(cnt[~hyd] == -1)
+        # the log's final block holds the solve's outputs
+        stride = abi.log_stride(log.cap)
+        rec = log.rec.view(a.nc, stride)
+        fin = rec[:, log.cap * abi.LOG_REC:]
+        nl = int(b["col_nbedrock"].min())
+        j0 = a.vp.nlevsno
+        hydt = torch.from_numpy(hyd).cuda()
+        assert torch.equal(fin[hydt, :nl].T.contiguous(), b["h2osoi_liq"][j0:j0 + nl][:, hydt])
+        assert torch.equal(fin[hydt, 3 * abi.MAX_NLEVSOI], b["qcharge"][hydt])
