@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--queue-order", type=int, default=None)
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration leg")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the adjoint calibration leg and print its JSON (profiling)")
     ap.add_argument("--adj-nc", type=int, default=65536)
     ap.add_argument("--adj-steps", type=int, default=48)
     ap.add_argument("--adj-k", type=int, default=8, help="checkpoint every k steps")
@@ -584,6 +586,9 @@ def run_ours(args):
 
 def main():
     args = parse()
+    if args.adjoint_only:
+        print(json.dumps(adjoint_leg(args)))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

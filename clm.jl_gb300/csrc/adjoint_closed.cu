@@ -804,8 +804,8 @@ __device__ __forceinline__ double& cf_sub(const CfSub& S, int64_t slot, int sidx
 __global__ void __launch_bounds__(CF_BLOCK)
 k_column_step_vjp_cf(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw, clmgb_swm_config cfg,
                      double dtime, int snow_method, double* t_ssbef, double* t_h2osfc_bef, clmgb_step_adjoint adj,
-                     CfSub S, SubstepLogView lg, unsigned long long* queue, uint32_t* col_status,
-                     uint32_t* dev_status) {
+                     CfSub S, SubstepLogView lg, unsigned long long* queue, const uint32_t* order,
+                     uint32_t* col_status, uint32_t* dev_status) {
   const int64_t ld = D.ldc;
   const int nlevsno = D.nlevsno, nlevgrnd = D.nlevgrnd, nlevsoi = D.nlevsoi;
   const int nlev = nlevsno + D.nlevmax;
@@ -815,8 +815,9 @@ k_column_step_vjp_cf(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwat
   const double LN10 = cm_log(10.0);
   CfBand band;
   for (;;) {
-    const int64_t c = (int64_t)atomicAdd(queue, 1ULL);
-    if (c >= nc) break;
+    const int64_t k = (int64_t)atomicAdd(queue, 1ULL);
+    if (k >= nc) break;
+    const int64_t c = order ? (int64_t)order[k] : k;
     const bool do_t = ft.mask_nolakec[c] != 0, do_w = fw.mask_hydrology[c] != 0;
     if (!do_t && !do_w) {     // the step leaves the column alone: identity
       if (col_status) col_status[c] = 0;
@@ -1031,6 +1032,56 @@ k_column_step_vjp_cf(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwat
   }
 }
 
+// Work order of the adjoint: the 32 columns a warp runs side by side should take
+// the same paths, so columns are handed out sorted (counting sort, descending) on
+// a key of the Richards work (accepted substeps from the log, else the previous
+// call's attempt count) and the number of snow layers.  Columns the step leaves
+// alone sort last.  The order does not change any result.
+constexpr int VJP_BINS = 64;
+__device__ __forceinline__ int vjp_key(const clmgb_soiltemp_fields& ft, const clmgb_soilwater_fields& fw,
+                                       const SubstepLogView& lg, int64_t c) {
+  if (!ft.mask_nolakec[c] && !fw.mask_hydrology[c]) return 0;
+  int a;
+  if (lg.rec) {
+    const int32_t n = lg.count[c];
+    a = n < 0 ? 0 : (n > lg.cap ? 15 : n);
+  } else {
+    const double ns = fw.num_substeps[c];
+    a = ns > 0.0 ? (ns >= 15.0 ? 15 : (int)ns) : 0;
+  }
+  if (a > 15) a = 15;
+  const int64_t snl = ft.col_snl[c];
+  int sb = (int)((-snl + 3) / 4);
+  sb = sb < 0 ? 0 : (sb > 3 ? 3 : sb);
+  return a * 4 + sb;
+}
+__global__ void k_vjp_hist(int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw, SubstepLogView lg,
+                           unsigned int* bins) {
+  __shared__ unsigned int sh[VJP_BINS];
+  for (int i = threadIdx.x; i < VJP_BINS; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nc) atomicAdd(&sh[vjp_key(ft, fw, lg, c)], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < VJP_BINS; i += blockDim.x)
+    if (sh[i]) atomicAdd(&bins[i], sh[i]);
+}
+__global__ void k_vjp_scan(unsigned int* bins) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned int run = 0;
+  for (int b = VJP_BINS - 1; b >= 0; b--) {
+    bins[VJP_BINS + b] = run;
+    run += bins[b];
+  }
+}
+__global__ void k_vjp_scatter(int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw, SubstepLogView lg,
+                              unsigned int* bins, uint32_t* order) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const unsigned int pos = atomicAdd(&bins[VJP_BINS + vjp_key(ft, fw, lg, c)], 1u);
+  order[pos] = (uint32_t)c;
+}
+
 int vjp_cf_blocks_per_sm() {
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_column_step_vjp_cf, CF_BLOCK, 0) != cudaSuccess) nb = 1;
@@ -1041,10 +1092,20 @@ cudaError_t launch_column_step_vjp_cf(const Dims& D, int64_t nc, const clmgb_soi
                                       const clmgb_soilwater_fields& fw, const clmgb_swm_config& cfg, double dtime,
                                       int snow_method, double* t_ssbef, double* t_h2osfc_bef,
                                       const clmgb_step_adjoint& adj, const AdjTape& tp, const SubstepLogView& lg,
-                                      unsigned long long* queue, int grid_blocks, uint32_t* col_status,
-                                      uint32_t* dev_status, cudaStream_t s) {
+                                      const QueueScratch& qs, unsigned long long* queue, int grid_blocks,
+                                      uint32_t* col_status, uint32_t* dev_status, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
+  const uint32_t* order = nullptr;
+  if (qs.capacity >= nc && qs.order && qs.bins && nc < (int64_t)0xffffffffLL) {
+    const unsigned g = (unsigned)((nc + 127) / 128);
+    if ((e = cudaMemsetAsync(qs.bins, 0, 2 * VJP_BINS * sizeof(unsigned int), s)) != cudaSuccess) return e;
+    k_vjp_hist<<<g, 128, 0, s>>>(nc, ft, fw, lg, qs.bins);
+    k_vjp_scan<<<1, 32, 0, s>>>(qs.bins);
+    k_vjp_scatter<<<g, 128, 0, s>>>(nc, ft, fw, lg, qs.bins, qs.order);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    order = qs.order;
+  }
   int64_t blocks = grid_blocks;
   const int64_t max_blocks = tp.slots / CF_BLOCK;
   if (blocks > max_blocks) blocks = max_blocks;
@@ -1053,8 +1114,8 @@ cudaError_t launch_column_step_vjp_cf(const Dims& D, int64_t nc, const clmgb_soi
   if (blocks < 1) return cudaErrorInvalidValue;
   CfSub S{tp.sub, (int)tp.maxsub, tp.slots};
   k_column_step_vjp_cf<<<(unsigned int)blocks, CF_BLOCK, 0, s>>>(D, nc, ft, fw, cfg, dtime, snow_method, t_ssbef,
-                                                                 t_h2osfc_bef, adj, S, lg, queue, col_status,
-                                                                 dev_status);
+                                                                 t_h2osfc_bef, adj, S, lg, queue, order,
+                                                                 col_status, dev_status);
   return cudaGetLastError();
 }
 

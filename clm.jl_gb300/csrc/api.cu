@@ -654,8 +654,8 @@ int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, cons
   cudaError_t ce;
   if (h->adj_st_mode == CLMGB_ADJ_ST_CLOSED_FORM && h->tape.richards_mode == CLMGB_ADJ_RICHARDS_CLOSED_FORM)
     ce = clmgb::launch_column_step_vjp_cf(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef, *adj,
-                                          h->tape, log_view(log), h->queue, vjp_grid(h), col_status, h->dev_status,
-                                          (cudaStream_t)stream);
+                                          h->tape, log_view(log), h->qs, h->queue, vjp_grid(h), col_status,
+                                          h->dev_status, (cudaStream_t)stream);
   else
     ce = clmgb::launch_column_step_vjp(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef, *adj,
                                        h->tape, col_status, h->dev_status, (cudaStream_t)stream);

@@ -109,8 +109,8 @@ cudaError_t launch_column_step_vjp_cf(const Dims& D, int64_t nc, const clmgb_soi
                                       const clmgb_soilwater_fields& fw, const clmgb_swm_config& cfg, double dtime,
                                       int snow_method, double* t_ssbef, double* t_h2osfc_bef,
                                       const clmgb_step_adjoint& adj, const AdjTape& tp, const SubstepLogView& lg,
-                                      unsigned long long* queue, int grid_blocks, uint32_t* col_status,
-                                      uint32_t* dev_status, cudaStream_t s);
+                                      const QueueScratch& qs, unsigned long long* queue, int grid_blocks,
+                                      uint32_t* col_status, uint32_t* dev_status, cudaStream_t s);
 cudaError_t launch_band_factor_solve(int64_t nc, int64_t ldc, int nlev, double* tvector, const double* bmatrix,
                                      const double* rvector, const int64_t* jtop, const int64_t* jbot,
                                      const uint8_t* mask, int kl, int ku, int nlevsno_off, double* lu, uint8_t* piv,

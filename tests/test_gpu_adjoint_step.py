@@ -59,25 +59,31 @@ def _traj(h, wl, G, I, nsteps, cfg):
     return adjoint.Trajectory(h, nsteps, wl.dtime, forcing, cfg, forcing_reverse=adjoint.synth_forcing_reverse)
 
 
-def test_replay_is_the_production_step(handle):
+@pytest.mark.parametrize("st_mode", [abi.ADJ_ST_CLOSED_FORM, abi.ADJ_ST_RECORDED])
+def test_replay_is_the_production_step(handle, st_mode):
     cfg = _cfg_flux()
     wl, G, I = _workload(700, 6)
     a = wl.state.to_device()
     b = a.copy()
     adj = adjoint.StepAdjointBuffers(a)
     status = torch.zeros(a.nc, dtype=torch.int32, device="cuda")
-    for t in range(6):
-        api.synth_forcing(handle, a, G[t], I[t])
-        api.column_step(handle, a, wl.dtime, cfg)
-        api.synth_forcing(handle, b, G[t], I[t])
-        adj.zero_()
-        api.column_step_vjp(handle, b, wl.dtime, adj, cfg, col_status=status)
-        torch.cuda.synchronize()
-        for k in a.arrays:
-            assert torch.equal(a[k], b[k]), "step %d field %s" % (t, k)
+    handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, st_mode)
+    try:
+        for t in range(6):
+            api.synth_forcing(handle, a, G[t], I[t])
+            api.column_step(handle, a, wl.dtime, cfg)
+            api.synth_forcing(handle, b, G[t], I[t])
+            adj.zero_()
+            api.column_step_vjp(handle, b, wl.dtime, adj, cfg, col_status=status)
+            torch.cuda.synchronize()
+            for k in a.arrays:
+                assert torch.equal(a[k], b[k]), "step %d field %s" % (t, k)
+    finally:
+        handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_CLOSED_FORM)
     st = status.cpu().numpy()
     assert np.all((st & abi.COL_TAPE_FULL) == 0)
-    assert handle.get_option(abi.OPT_ADJ_TAPE_USED) > 1000
+    if st_mode == abi.ADJ_ST_RECORDED:
+        assert handle.get_option(abi.OPT_ADJ_TAPE_USED) > 1000
 
 
 def _params_and_decisions(traj, st0, loss, steps):
