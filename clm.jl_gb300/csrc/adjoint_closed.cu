@@ -202,34 +202,37 @@ __device__ __noinline__ void phase_change_level_reverse(const PcLevelIn& in, dou
   const double liqv = wmass0 - ice - 0.0;
   const double liq = jl_max(0.0, liqv);
   const bool liq_pass = !same_bits(liq, 0.0);
-  // ---- reverse ----
+  // ---- reverse (derivative coefficients with reciprocals) ----
   double heatr_b = 0.0, hm_b = 0.0, xm_b = 0.0, ice_b = icepc_b, wmass0_b = 0.0, wice0_b = 0.0, sc_b = 0.0;
   double tinc_b = 0.0;
+  const double rf = 1.0 / fct;
   if (fabs(heatr) > 0.0 && !(j <= 0 && liq * ice > 0.0)) {
     // temperature correction (:2145-2165); the level starts from freezing
-    if ((j == jtop && j == 1) || (j != jtop && j == 1)) {
+    if (j == 1) {
       const double k = (j == jtop) ? (1.0 - fh) : (1.0 - fse - fh);
-      const double den = 1.0 - k * fct * dhsdT;
-      const double incr = fct * heatr / den;
-      const double N_b = Tpc_b / den, den_b = -Tpc_b * incr / den;
+      const double rden = 1.0 / (1.0 - k * fct * dhsdT);
+      const double incr = fct * heatr * rden;
+      const double N_b = Tpc_b * rden, den_b = -Tpc_b * incr * rden;
       fct_b += N_b * heatr - den_b * k * dhsdT;
       heatr_b += N_b * fct;
       dhsdT_b += -den_b * k * fct;
     } else if (j == jtop) {      // top snow layer
       if (fse > 0.0) {
-        const double den = 1.0 - fct * dhsdT;
-        const double incr = (fct / fse) * heatr / den;
-        const double N_b = Tpc_b / den, den_b = -Tpc_b * incr / den;
-        fct_b += N_b * heatr / fse - den_b * dhsdT;
-        heatr_b += N_b * (fct / fse);
+        const double rfse = 1.0 / fse;
+        const double rden = 1.0 / (1.0 - fct * dhsdT);
+        const double incr = fct * rfse * heatr * rden;
+        const double N_b = Tpc_b * rden, den_b = -Tpc_b * incr * rden;
+        fct_b += N_b * heatr * rfse - den_b * dhsdT;
+        heatr_b += N_b * fct * rfse;
         dhsdT_b += -den_b * fct;
       }
     } else if (j > 0) {
       fct_b += Tpc_b * heatr;
       heatr_b += Tpc_b * fct;
     } else if (fse > 0.0) {
-      fct_b += Tpc_b * heatr / fse;
-      heatr_b += Tpc_b * (fct / fse);
+      const double rfse = 1.0 / fse;
+      fct_b += Tpc_b * heatr * rfse;
+      heatr_b += Tpc_b * fct * rfse;
     }
   }
   if (liq_pass) {
@@ -238,7 +241,7 @@ __device__ __noinline__ void phase_change_level_reverse(const PcLevelIn& in, dou
   }
   if (xm != 0.0) {
     hm_b += heatr_b;
-    const double d_b = -heatr_b * HFUS / dtime;
+    const double d_b = -heatr_b * HFUS * (1.0 / dtime);
     wice0_b += d_b;
     ice_b -= d_b;
   }
@@ -249,13 +252,13 @@ __device__ __noinline__ void phase_change_level_reverse(const PcLevelIn& in, dou
     case 4: wmass0_b += ice_b; sc_b -= ice_b; break;
     default: break;
   }
-  hm_b += xm_b * dtime / HFUS;
+  hm_b += xm_b * dtime * (1.0 / HFUS);
   // hm
   if (j == jtop) {
     const double hb = (j > 0) ? hm_b : hm_b * fse;
     dhsdT_b += hb * tinc;
-    tinc_b += hb * dhsdT - hb / fct;
-    fct_b += hb * (tinc / fct) / fct;
+    tinc_b += hb * dhsdT - hb * rf;
+    fct_b += hb * tinc * rf * rf;
     if (j == 1 && fh != 0.0) {
       dhsdT_b -= hm_b * fh * tinc;
       tinc_b -= hm_b * fh * dhsdT;
@@ -263,12 +266,12 @@ __device__ __noinline__ void phase_change_level_reverse(const PcLevelIn& in, dou
   } else if (j == 1) {
     const double k = 1.0 - fse - fh;
     dhsdT_b += hm_b * k * tinc;
-    tinc_b += hm_b * k * dhsdT - hm_b / fct;
-    fct_b += hm_b * (tinc / fct) / fct;
+    tinc_b += hm_b * k * dhsdT - hm_b * rf;
+    fct_b += hm_b * tinc * rf * rf;
   } else {
     const double a = (j < 1) ? fse : 1.0;     // hm = -a tinc / fct
-    tinc_b -= hm_b * a / fct;
-    fct_b += hm_b * (a * tinc / fct) / fct;
+    tinc_b -= hm_b * a * rf;
+    fct_b += hm_b * a * tinc * rf * rf;
   }
   T0_b -= tinc_b;
   // supercooled water sc = watsat (smp/sucsat)^(-1/bsw) dz 1000, smp = HFUS (TFRZ-T)/(GRAV T) 1000
@@ -276,14 +279,15 @@ __device__ __noinline__ void phase_change_level_reverse(const PcLevelIn& in, dou
     const double sc0_b = sc_b * (in.dz * 1000.0);
     ws_b += sc0_b * P;
     const double P_b = sc0_b * in.ws;
-    const double r_b = r != 0.0 ? P_b * (e * P / r) : 0.0;
+    const double rr = 1.0 / r, rsuc = 1.0 / in.suc, rg = 1.0 / g;
+    const double r_b = r != 0.0 ? P_b * e * P * rr : 0.0;
     const double e_b = r > 0.0 ? P_b * P * cm_log(r) : 0.0;
-    bs_b += e_b * (-e / in.bs);
-    const double smp_b = r_b / in.suc;
-    suc_b += r_b * (-r / in.suc);
+    bs_b += e_b * (-e) * (1.0 / in.bs);
+    const double smp_b = r_b * rsuc;
+    suc_b += r_b * (-r) * rsuc;
     const double q_b = smp_b * 1000.0;
-    const double a_b = q_b / g;
-    const double g_b = -q_b * q / g;
+    const double a_b = q_b * rg;
+    const double g_b = -q_b * q * rg;
     T0_b += -a_b * HFUS + g_b * GRAV;
   }
   ice0_b += wice0_b + wmass0_b;
@@ -319,8 +323,9 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
   const double omc = 1.0 - CNFAC;
   const double LN_TKWAT = cm_log(TKWAT), LN_TKICE = cm_log(TKICE);
 
-  double zz[MAXL + 2];
+  double zz[MAXL + 2], rdzp[MAXL + 2];     // rdzp[jj] = 1 / (z[jj+1] - z[jj])
   for (int jj = jjtop; jj <= nw; jj++) zz[jj] = LVc(f.z, c, jj, ld);
+  for (int jj = jjtop; jj < nw; jj++) rdzp[jj] = 1.0 / (zz[jj + 1] - zz[jj]);
 
   // ---- forward values with local partials ----
   // layer conductivity thk and its partials in liquid water, ice and watsat
@@ -346,27 +351,30 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
             if (tin[jj] >= TFRZ) {
               const double L = cm_log10(satw) + 1.0;
               dke = jl_max(0.0, L);
-              ddke = same_bits(dke, 0.0) ? 0.0 : 0.43429448190325182765 / satw;
+              ddke = same_bits(dke, 0.0) ? 0.0 : 0.43429448190325182765 * (1.0 / satw);
             } else {
               dke = satw;
               ddke = 1.0;
             }
-            const double a1 = liq / (DENH2O * dzv);
-            const double fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
-            const double fl = a1 / fl_denom;
-            const double P1 = cm_pow(TKWAT, fl * ws), P2 = cm_pow(TKICE, (1.0 - fl) * ws);
+            // derivative coefficients (reciprocals instead of divisions; TKWAT^a TKICE^b
+            // as one exponential)
+            const double rm = 1.0 / m, rdz = 1.0 / dzv;
+            const double a1 = liq * (1.0 / DENH2O) * rdz;
+            const double fl_denom = a1 + (ice + exi) * (1.0 / DENICE) * rdz;
+            const double rfd = 1.0 / fl_denom;
+            const double fl = a1 * rfd;
             const double tkmg = LVc(f.tkmg, c, j, ld), tkdry = LVc(f.tkdry, c, j, ld);
-            const double dksat = tkmg * P1 * P2;
+            const double dksat = tkmg * cm_exp(ws * (fl * LN_TKWAT + (1.0 - fl) * LN_TKICE));
             v = dke * dksat + (1.0 - dke) * tkdry;
             // d satw
-            const double sl = spass ? (1.0 / DENH2O) / m : 0.0;
-            const double si = spass ? (1.0 / DENICE) / m : 0.0;
-            const double sw = spass ? -(satw0 / m) * dzv : 0.0;
+            const double sl = spass ? (1.0 / DENH2O) * rm : 0.0;
+            const double si = spass ? (1.0 / DENICE) * rm : 0.0;
+            const double sw = spass ? -(satw0 * rm) * dzv : 0.0;
             // d dksat / d fl, d ws
             const double kfl = dksat * (LN_TKWAT * ws - LN_TKICE * ws);
             const double kws = dksat * (LN_TKWAT * fl + LN_TKICE * (1.0 - fl));
-            const double fll = (1.0 - fl) / fl_denom / (DENH2O * dzv);
-            const double fli = -fl / fl_denom / (DENICE * dzv);
+            const double fll = (1.0 - fl) * rfd * (1.0 / DENH2O) * rdz;
+            const double fli = -fl * rfd * (1.0 / DENICE) * rdz;
             const double cdke = (dksat - tkdry) * ddke;
             dl = cdke * sl + dke * kfl * fll;
             di = cdke * si + dke * kfl * fli;
@@ -426,11 +434,11 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
       const double tkj = thk[jj], tkj1 = thk[jj + 1];
       const double zj = zz[jj], zj1 = zz[jj + 1], zij1 = LVc(f.zi, c, jj + 1, ld);
       const double A = zj1 - zj, Bz = zj1 - zij1, Cz = zij1 - zj;
-      const double den = tkj * Bz + tkj1 * Cz;
-      const double v = tkj * tkj1 * A / den;
+      const double rden = 1.0 / (tkj * Bz + tkj1 * Cz);
+      const double v = tkj * tkj1 * A * rden;
       tkif[jj] = v;
-      da[jj] = (tkj1 * A - v * Bz) / den;
-      db[jj] = (tkj * A - v * Cz) / den;
+      da[jj] = (tkj1 * A - v * Bz) * rden;
+      db[jj] = (tkj * A - v * Cz) * rden;
     } else {
       tkif[jj] = 0.0;
       da[jj] = 0.0;
@@ -478,7 +486,7 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
     cl[jj] = dfdcv * dl;
     ci[jj] = dfdcv * di;
     cw[jj] = dfdcv * dw;
-    if (j <= nlevgrnd - 1) fn[jj] = tkif[jj] * (tin[jj + 1] - tin[jj]) / (zz[jj + 1] - zz[jj]);
+    if (j <= nlevgrnd - 1) fn[jj] = tkif[jj] * (tin[jj + 1] - tin[jj]) * rdzp[jj];
     else fn[jj] = f.eflx_bot[c];
   }
   // ground heat flux sums and their derivative weights
@@ -604,7 +612,7 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
     const int jj = j + joff;
     const int r = j - jtop;
     const double fc = fact[jj];
-    const double dzp = zz[jj + 1] - zz[jj];
+    const double rp = rdzp[jj];
     const double lam = w[r];
     tin_b[jj] += lam;
     if (j == jtop) {
@@ -616,28 +624,28 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
       tin_b[jj] -= ib * dhsdT;
       fn_b[jj] += ib * CNFAC;
       const double g2 = ABAR(r, 2);
-      fct_b[jj] += g2 * (omc * tkif[jj] / dzp - dhsdT);
-      tkif_b[jj] += g2 * omc * fc / dzp;
+      fct_b[jj] += g2 * (omc * tkif[jj] * rp - dhsdT);
+      tkif_b[jj] += g2 * omc * fc * rp;
       dhsdT_b -= g2 * fc;
     } else {
       fct_b[jj] += lam * (CNFAC * (fn[jj] - fn[jj - 1]) + sabg_col[jj]);
       fn_b[jj] += lam * CNFAC * fc;
       fn_b[jj - 1] -= lam * CNFAC * fc;
-      const double dzm = zz[jj] - zz[jj - 1];
+      const double rmn = rdzp[jj - 1];
       const double g1 = ABAR(r, 1), g2 = ABAR(r, 2);
-      fct_b[jj] += -g1 * omc * tkif[jj - 1] / dzm + g2 * omc * (tkif[jj] / dzp + tkif[jj - 1] / dzm);
-      tkif_b[jj - 1] += -g1 * omc * fc / dzm + g2 * omc * fc / dzm;
-      tkif_b[jj] += g2 * omc * fc / dzp;
+      fct_b[jj] += -g1 * omc * tkif[jj - 1] * rmn + g2 * omc * (tkif[jj] * rp + tkif[jj - 1] * rmn);
+      tkif_b[jj - 1] += -g1 * omc * fc * rmn + g2 * omc * fc * rmn;
+      tkif_b[jj] += g2 * omc * fc * rp;
     }
     const double g = (j != 0) ? ABAR(r, 3) : ABAR(r, 4);
-    fct_b[jj] += -g * omc * tkif[jj] / dzp;
-    tkif_b[jj] += -g * omc * fc / dzp;
+    fct_b[jj] += -g * omc * tkif[jj] * rp;
+    tkif_b[jj] += -g * omc * fc * rp;
   }
   {   // surface-water row
-    const double dzm = 0.5 * dz_h2osfc + zz[1 + joff];
+    const double rdh = 1.0 / (0.5 * dz_h2osfc + zz[1 + joff]);
     const double dtc = dtime / ch;
     const double t1 = tin[1 + joff];
-    const double fnh = tkh * (t1 - th0) / dzm;
+    const double fnh = tkh * (t1 - th0) * rdh;
     const double lam = w[rsw];
     th_b += lam;
     const double ib = lam * dtc;
@@ -646,10 +654,10 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
     th_b -= ib * dhsdT;
     const double fnh_b = ib * CNFAC;
     const double g2 = ABAR(rsw, 2), g3 = ABAR(rsw, 3);
-    tkh_b += g2 * omc * dtc / dzm - g3 * omc * dtc / dzm;
+    tkh_b += g2 * omc * dtc * rdh - g3 * omc * dtc * rdh;
     dhsdT_b -= g2 * dtc;
-    tkh_b += fnh_b * (t1 - th0) / dzm;
-    const double d_b = fnh_b * tkh / dzm;
+    tkh_b += fnh_b * (t1 - th0) * rdh;
+    const double d_b = fnh_b * tkh * rdh;
     tin_b[1 + joff] += d_b;
     th_b -= d_b;
     (void)fnh;
@@ -662,7 +670,7 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
     const double lam = w[r];
     tin_b[jj] += lam;
     if (j == jtop) {
-      const double dzp = zz[jj + 1] - zz[jj];
+      const double rp = rdzp[jj];
       const double inner = hs_top - dhsdT * t0 + CNFAC * fn[jj];
       fct_b[jj] += lam * inner;
       const double ib = lam * fc;
@@ -671,12 +679,12 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
       tin_b[jj] -= ib * dhsdT;
       fn_b[jj] += ib * CNFAC;
       const double g2 = ABAR(r, 2), g3 = ABAR(r, 3);
-      fct_b[jj] += g2 * (omc * tkif[jj] / dzp - dhsdT) - g3 * omc * tkif[jj] / dzp;
-      tkif_b[jj] += g2 * omc * fc / dzp - g3 * omc * fc / dzp;
+      fct_b[jj] += g2 * (omc * tkif[jj] * rp - dhsdT) - g3 * omc * tkif[jj] * rp;
+      tkif_b[jj] += g2 * omc * fc * rp - g3 * omc * fc * rp;
       dhsdT_b -= g2 * fc;
     } else if (j == 1) {
-      const double dzm = zz[jj] - zz[jj - 1];
-      const double dzp = zz[jj + 1] - zz[jj];
+      const double rmn = rdzp[jj - 1];
+      const double rp = rdzp[jj];
       const double inner = (1.0 - fse) * (hs_soil - dhsdT * t0) + CNFAC * (fn[jj] - fse * fn[jj - 1]);
       fct_b[jj] += lam * (inner + fse * sabg_col[j + nlevsno]);
       const double ib = lam * fc;
@@ -687,38 +695,38 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
       fn_b[jj] += ib * CNFAC;
       fn_b[jj - 1] -= ib * CNFAC * fse;
       const double g0 = ABAR(r, 0), g2 = ABAR(r, 2), g3 = ABAR(r, 3);
-      fct_b[jj] += -g3 * omc * tkif[jj] / dzp +
-                   g2 * (omc * (tkif[jj] / dzp + fse * tkif[jj - 1] / dzm) - (1.0 - fse) * dhsdT) -
-                   g0 * fse * omc * tkif[jj - 1] / dzm;
-      tkif_b[jj] += -g3 * omc * fc / dzp + g2 * omc * fc / dzp;
-      tkif_b[jj - 1] += g2 * omc * fc * fse / dzm - g0 * fse * omc * fc / dzm;
+      fct_b[jj] += -g3 * omc * tkif[jj] * rp +
+                   g2 * (omc * (tkif[jj] * rp + fse * tkif[jj - 1] * rmn) - (1.0 - fse) * dhsdT) -
+                   g0 * fse * omc * tkif[jj - 1] * rmn;
+      tkif_b[jj] += -g3 * omc * fc * rp + g2 * omc * fc * rp;
+      tkif_b[jj - 1] += g2 * omc * fc * fse * rmn - g0 * fse * omc * fc * rmn;
       dhsdT_b -= g2 * (1.0 - fse) * fc;
     } else if (j <= nlevgrnd - 1) {
-      const double dzm = zz[jj] - zz[jj - 1];
-      const double dzp = zz[jj + 1] - zz[jj];
+      const double rmn = rdzp[jj - 1];
+      const double rp = rdzp[jj];
       fct_b[jj] += lam * CNFAC * (fn[jj] - fn[jj - 1]);
       fn_b[jj] += lam * CNFAC * fc;
       fn_b[jj - 1] -= lam * CNFAC * fc;
       const double g1 = ABAR(r, 1), g2 = ABAR(r, 2), g3 = ABAR(r, 3);
-      fct_b[jj] += -g3 * omc * tkif[jj] / dzp + g2 * omc * (tkif[jj] / dzp + tkif[jj - 1] / dzm) -
-                   g1 * omc * tkif[jj - 1] / dzm;
-      tkif_b[jj] += -g3 * omc * fc / dzp + g2 * omc * fc / dzp;
-      tkif_b[jj - 1] += g2 * omc * fc / dzm - g1 * omc * fc / dzm;
+      fct_b[jj] += -g3 * omc * tkif[jj] * rp + g2 * omc * (tkif[jj] * rp + tkif[jj - 1] * rmn) -
+                   g1 * omc * tkif[jj - 1] * rmn;
+      tkif_b[jj] += -g3 * omc * fc * rp + g2 * omc * fc * rp;
+      tkif_b[jj - 1] += g2 * omc * fc * rmn - g1 * omc * fc * rmn;
     } else {
-      const double dzm = zz[jj] - zz[jj - 1];
+      const double rmn = rdzp[jj - 1];
       fct_b[jj] += lam * (-CNFAC * fn[jj - 1] + fn[jj]);
       fn_b[jj - 1] -= lam * CNFAC * fc;
       const double g1 = ABAR(r, 1), g2 = ABAR(r, 2);
-      fct_b[jj] += g2 * omc * tkif[jj - 1] / dzm - g1 * omc * tkif[jj - 1] / dzm;
-      tkif_b[jj - 1] += g2 * omc * fc / dzm - g1 * omc * fc / dzm;
+      fct_b[jj] += g2 * omc * tkif[jj - 1] * rmn - g1 * omc * tkif[jj - 1] * rmn;
+      tkif_b[jj - 1] += g2 * omc * fc * rmn - g1 * omc * fc * rmn;
     }
   }
   if (fh != 0.0) {   // surface-water corrections to soil layer 1
     const int jj = 1 + joff;
     const int r = rsw + 1;
     const double fc = fact[jj];
-    const double dzm = 0.5 * dz_h2osfc + zz[1 + joff];
-    const double fnh = tkh * (tin[jj] - th0) / dzm;
+    const double rdh = 1.0 / (0.5 * dz_h2osfc + zz[1 + joff]);
+    const double fnh = tkh * (tin[jj] - th0) * rdh;
     const double lam = w[r];
     // x[r] -= fh fc ((hs_soil - dhsdT t1) + CNFAC fnh)
     const double ib = -lam * fh;
@@ -727,13 +735,13 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
     dhsdT_b -= ib * fc * tin[jj];
     tin_b[jj] -= ib * fc * dhsdT;
     const double fnh_b = ib * fc * CNFAC;
-    tkh_b += fnh_b * (tin[jj] - th0) / dzm;
-    tin_b[jj] += fnh_b * tkh / dzm;
-    th_b -= fnh_b * tkh / dzm;
+    tkh_b += fnh_b * (tin[jj] - th0) * rdh;
+    tin_b[jj] += fnh_b * tkh * rdh;
+    th_b -= fnh_b * tkh * rdh;
     // ab[r][2] += fh (omc fc tkh / dzm + fc dhsdT); ab[r][1] = -fh omc fc tkh / dzm
     const double g2 = ABAR(r, 2), g1 = ABAR(r, 1);
-    fct_b[jj] += g2 * fh * (omc * tkh / dzm + dhsdT) - g1 * fh * omc * tkh / dzm;
-    tkh_b += g2 * fh * omc * fc / dzm - g1 * fh * omc * fc / dzm;
+    fct_b[jj] += g2 * fh * (omc * tkh * rdh + dhsdT) - g1 * fh * omc * tkh * rdh;
+    tkh_b += g2 * fh * omc * fc * rdh - g1 * fh * omc * fc * rdh;
     dhsdT_b += g2 * fh * fc;
   }
 #undef ABAR
@@ -741,9 +749,9 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
   for (int jj = jjtop; jj <= nw; jj++) {
     const int j = jj - nlevsno;
     if (j <= nlevgrnd - 1 && fn_b[jj] != 0.0) {
-      const double dz = zz[jj + 1] - zz[jj];
-      tkif_b[jj] += fn_b[jj] * (tin[jj + 1] - tin[jj]) / dz;
-      const double d_b = fn_b[jj] * tkif[jj] / dz;
+      const double rz = rdzp[jj];
+      tkif_b[jj] += fn_b[jj] * (tin[jj + 1] - tin[jj]) * rz;
+      const double d_b = fn_b[jj] * tkif[jj] * rz;
       tin_b[jj + 1] += d_b;
       tin_b[jj] -= d_b;
     }

@@ -243,7 +243,9 @@ def test_richards_gradient_vs_complex_step(handle):
                 th[p][j] += 1e-30j
                 ref[k, j] = y_of(th).imag / 1e-30
         got = np.array([adj.grad[p][:, c].cpu().numpy() for p in adjoint.PARAMS])
+        assert np.isfinite(got).all(), c
         e = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+        assert np.isfinite(e), c
         worst = max(worst, e)
     print("complex-step: max rel err %.3g" % worst)
     assert worst < 1e-9
@@ -275,6 +277,7 @@ def test_closed_form_substep_reverse_matches_recorded_replay(handle):
         handle.set_option(abi.OPT_ADJ_RICHARDS, abi.ADJ_RICHARDS_CLOSED_FORM)
         handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_CLOSED_FORM)
     a, b = out[abi.ADJ_RICHARDS_CLOSED_FORM], out[abi.ADJ_RICHARDS_RECORDED]
+    assert np.isfinite(a).all() and np.isfinite(b).all()
     scale = np.max(np.abs(b), axis=(0, 1))
     rel = np.max(np.abs(a - b), axis=(0, 1)) / np.maximum(scale, 1e-300)
     print("closed form vs recorded: max rel diff %.3g" % rel.max())
