@@ -128,18 +128,21 @@ def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_s
     step-entry states from its checkpoint.  observe(t, state_after_t) runs after every
     forward step (the loss's forward half).  `events`, three CUDA events, are recorded
     at the start, between the forward and the reverse pass, and at the end.  The
-    recomputed steps write substep logs (`log_cap` records per column; 0: no logs) so
-    that their reverses do not run the Richards substep loop again; the last step of a
-    segment is not recomputed and its reverse runs the loop itself.  Returns the
-    adjoint buffers."""
+    recomputed steps, and the last step of every segment in the forward pass, write
+    substep logs (`log_cap` records per column; 0: no logs) so that no reverse runs the
+    Richards substep loop again.  Returns the adjoint buffers."""
     k = max(1, int(checkpoint_every))
     if events is not None:
         events[0].record()
     ckpt = []
+    nseg = (traj.nsteps + k - 1) // k
+    # the last step of a segment is not recomputed: the forward pass logs it
+    last_logs = [api.SubstepLog(state.nc, log_cap) for _ in range(nseg)] if log_cap > 0 else []
     for t in range(traj.nsteps):
         if t % k == 0:
             ckpt.append(state.copy())
-        traj.step(t, state)
+        last = t % k == k - 1 or t == traj.nsteps - 1
+        traj.step(t, state, last_logs[t // k] if (last_logs and last) else None)
         if observe is not None:
             observe(t, state)
     if events is not None:
@@ -155,7 +158,9 @@ def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_s
             traj.step(t, seg_states[t - t0 + 1], logs[t - t0] if logs else None)
         for t in range(t1 - 1, t0 - 1, -1):
             seed(t, adj)
-            lg = logs[t - t0] if (logs and t < t1 - 1) else None
+            lg = None
+            if logs:
+                lg = logs[t - t0] if t < t1 - 1 else last_logs[s]
             traj.reverse_step(t, seg_states[t - t0], adj, col_status, log=lg)
     if events is not None:
         events[2].record()
