@@ -251,15 +251,20 @@ def test_richards_gradient_vs_complex_step(handle):
     assert worst < 1e-9
 
 
-def test_closed_form_substep_reverse_matches_recorded_replay(handle):
+@pytest.mark.parametrize("bc", [abi.BC_FLUX, abi.BC_WATERTABLE, abi.BC_ZERO_FLUX])
+def test_closed_form_substep_reverse_matches_recorded_replay(handle, bc):
     """The hand-written reverse of a Richards substep and the recorded replay of the
     same substep differentiate the same arithmetic: they agree to rounding (both with
-    soil_temperature! recorded, so only the substep reverse differs)."""
-    cfg = _cfg_flux()
+    soil_temperature! recorded, so only the substep reverse differs), for each lower
+    boundary condition."""
+    cfg = abi.SwmConfig.clm5_default()
+    cfg.lower_boundary_condition = bc
     nsteps = 4
     wl, G, I = _workload(256, nsteps, seed=555)
     traj = _traj(handle, wl, G, I, nsteps, cfg)
     st0 = wl.state.to_device()
+    if bc == abi.BC_WATERTABLE:
+        st0["zwt"][::2] += 1.5     # water table below the soil column: drainage to it is active
     tgt = torch.zeros((nsteps, st0.nc), dtype=torch.float64, device="cuda")
     out = {}
     handle.set_option(abi.OPT_ADJ_SOIL_TEMPERATURE, abi.ADJ_ST_RECORDED)
@@ -389,18 +394,26 @@ def _traj_method(h, wl, G, I, nsteps, cfg, method):
                               forcing_reverse=adjoint.synth_forcing_reverse)
 
 
-@pytest.mark.parametrize("cfg_id,method", [(1, abi.SNOW_JORDAN1991), (1, abi.SNOW_STURM1997),
-                                           (2, abi.SNOW_JORDAN1991)])
-def test_closed_form_step_adjoint_matches_recorded(handle, cfg_id, method):
+@pytest.mark.parametrize("cfg_id,method,bc", [(1, abi.SNOW_JORDAN1991, abi.BC_FLUX),
+                                              (1, abi.SNOW_STURM1997, abi.BC_FLUX),
+                                              (2, abi.SNOW_JORDAN1991, abi.BC_FLUX),
+                                              (1, abi.SNOW_JORDAN1991, abi.BC_WATERTABLE),
+                                              (2, abi.SNOW_JORDAN1991, abi.BC_ZERO_FLUX)])
+def test_closed_form_step_adjoint_matches_recorded(handle, cfg_id, method, bc):
     """The hand-written reverse of the whole step (soil_temperature! stage by stage,
     fractions, impedance, substeps) and the recording kernel differentiate the same
     arithmetic: every input adjoint and parameter gradient agrees to rounding, per
-    column relative to the column's largest entry of that quantity."""
-    cfg = _cfg_flux()
+    column relative to the column's largest entry of that quantity; for both snow
+    conductivity methods and the free-drainage, water-table and zero-flux lower
+    boundaries."""
+    cfg = abi.SwmConfig.clm5_default()
+    cfg.lower_boundary_condition = bc
     nsteps = 4
     wl, G, I = _workload_cfg(cfg_id, 512, nsteps, seed=31 + cfg_id)
     traj = _traj_method(handle, wl, G, I, nsteps, cfg, method)
     st0 = wl.state.to_device()
+    if bc == abi.BC_WATERTABLE:
+        st0["zwt"][::2] += 1.5     # water table below the soil column: drainage to it is active
     lin = _LinearSeed(st0, nsteps, 7 + cfg_id)
     out, stat = {}, {}
     try:
