@@ -170,6 +170,50 @@ function column_step_vjp!(ft_buf, fw_buf, b::Bounds, cfg::SwmConfig, dtime, snow
     nothing
 end
 
+# Substep log (clmgb_substep_log): the forward step writes it, the reverse reads it,
+# so the reverse does not run the Richards substep loop again.  rec holds
+# LOG_STRIDE(cap) Float64 per column, count one Int32 per column.
+struct SubstepLog
+    struct_size::Int64
+    rec::Ptr{Cvoid}
+    count::Ptr{Cvoid}
+    cap::Int32
+end
+const LOG_REC = 25 + 2                  # CLMGB_MAX_NLEVSOI + 2
+const LOG_FIN = 3 * 25 + 3
+log_stride(cap) = cap * LOG_REC + LOG_FIN
+new_substep_log(nc::Integer, cap::Integer = 24) =
+    (rec = CUDA.zeros(Float64, nc * log_stride(cap)), count = CUDA.fill(Int32(-1), nc), cap = Int32(cap))
+log_struct(lg) = SubstepLog(sizeof(SubstepLog), ptr(lg.rec), ptr(lg.count), lg.cap)
+
+function column_step_logged!(ft_buf, fw_buf, b::Bounds, cfg::SwmConfig, dtime, snow_method, t_ssbef,
+                             t_h2osfc_bef, lg)
+    GC.@preserve ft_buf fw_buf lg begin
+        check(ccall((:clmgb_column_step_logged, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Int32,
+                     Ptr{Cvoid}, Ptr{Cvoid}, Ref{SubstepLog}, Ptr{UInt32}, Ptr{Cvoid}),
+                    handle(), b, ft_buf, fw_buf, cfg, dtime, snow_method, ptr(t_ssbef), ptr(t_h2osfc_bef),
+                    log_struct(lg), C_NULL, CUDA.stream().handle), "clmgb_column_step_logged")
+    end
+    nothing
+end
+
+function column_step_vjp_logged!(ft_buf, fw_buf, b::Bounds, cfg::SwmConfig, dtime, snow_method, t_ssbef,
+                                 t_h2osfc_bef, lam, grad, lg)
+    TAPE_RESERVED[] || reserve_adjoint!(b.nc, 256)
+    a = StepAdjoint(sizeof(StepAdjoint), ptr(lam.t_soisno), ptr(lam.h2osoi_liq), ptr(lam.h2osoi_ice),
+                    ptr(lam.t_grnd), ptr(lam.t_h2osfc), ptr(lam.qcharge), ptr(grad.watsat), ptr(grad.bsw),
+                    ptr(grad.sucsat), ptr(grad.hksat), ptr(lam.forc_lwrad))
+    GC.@preserve ft_buf fw_buf lg begin
+        check(ccall((:clmgb_column_step_vjp_logged, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Int32,
+                     Ptr{Cvoid}, Ptr{Cvoid}, Ref{StepAdjoint}, Ref{SubstepLog}, Ptr{UInt32}, Ptr{Cvoid}),
+                    handle(), b, ft_buf, fw_buf, cfg, dtime, snow_method, ptr(t_ssbef), ptr(t_h2osfc_bef), a,
+                    log_struct(lg), C_NULL, CUDA.stream().handle), "clmgb_column_step_vjp_logged")
+    end
+    nothing
+end
+
 # ChainRulesCore: y = step(x, theta) on a snapshot of the state (the rule replays the
 # step from the snapshot, so the primal is not re-run by the caller).
 #   function ChainRulesCore.rrule(::typeof(CLM.column_step!), st::StepState, theta)
