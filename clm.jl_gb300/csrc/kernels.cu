@@ -13,11 +13,46 @@ __device__ __forceinline__ void report(uint32_t st, uint32_t* col_status, uint32
   if (st && dev_status) atomicOr(dev_status, st);
 }
 
+// The column of this thread in the soil-temperature kernels: the block's BLOCK
+// consecutive columns, reordered by snow-layer count (a counting sort in shared
+// memory), so the lanes of a warp run level loops and band solves of about the same
+// length.  Accesses stay inside the block's columns; each column's arithmetic is
+// unchanged, so results do not depend on the order.  Every thread of the block must
+// call it; returns -1 past the last column.
+__device__ __forceinline__ int64_t snl_sorted_column(int64_t nc, const int64_t* col_snl, int nlevsno) {
+  __shared__ unsigned int s_cnt[16];
+  __shared__ unsigned short s_perm[BLOCK];
+  const int64_t base = (int64_t)blockIdx.x * BLOCK;
+  if (threadIdx.x < 16) s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t c0 = base + threadIdx.x;
+  int key = 15;
+  if (c0 < nc) {
+    const int64_t s = -col_snl[c0];
+    key = (s < 0 || s > nlevsno || s > 13) ? 14 : (int)s;
+  }
+  const unsigned int r = atomicAdd(&s_cnt[key], 1u);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int run = 0;
+    for (int k = 0; k < 16; k++) {
+      const unsigned int t = s_cnt[k];
+      s_cnt[k] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+  s_perm[s_cnt[key] + r] = (unsigned short)threadIdx.x;
+  __syncthreads();
+  const int64_t c = base + s_perm[threadIdx.x];
+  return c < nc ? c : -1;
+}
+
 __global__ void __launch_bounds__(BLOCK)
 k_soil_temperature(Dims D, int64_t nc, clmgb_soiltemp_fields f, double dtime, int snow_method,
                    uint32_t* col_status, uint32_t* dev_status) {
-  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-  if (c >= nc) return;
+  const int64_t c = snl_sorted_column(nc, f.col_snl, D.nlevsno);
+  if (c < 0) return;
   uint32_t st = 0;
   if (f.mask_nolakec[c]) st = soil_temperature_col(D, f, c, dtime, snow_method);
   report(st, col_status, dev_status, c);
@@ -69,8 +104,8 @@ __global__ void __launch_bounds__(BLOCK)
 k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw,
                              double dtime, int snow_method, double* t_ssbef, double* t_h2osfc_bef,
                              uint32_t* col_status, uint32_t* dev_status) {
-  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-  if (c >= nc) return;
+  const int64_t c = snl_sorted_column(nc, ft.col_snl, D.nlevsno);
+  if (c < 0) return;
   uint32_t st = 0;
   if (ft.mask_nolakec[c]) {
     if (t_ssbef) {
