@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-reserve", action="store_true", help="run without clmgb_reserve scratch")
     ap.add_argument("--queue-order", type=int, default=None)
+    ap.add_argument("--fresh-batch", type=int, default=None, help="CLMGB_OPT_QUEUE_FRESH_BATCH override")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration leg")
     ap.add_argument("--adjoint-only", action="store_true",
@@ -414,6 +415,8 @@ def run_ours(args):
         h.set_option(abi.OPT_QUEUE_BLOCKS_PER_SM, args.queue_bps)
     if args.queue_order is not None:
         h.set_option(abi.OPT_QUEUE_ORDER, args.queue_order)
+    if args.fresh_batch is not None:
+        h.set_option(abi.OPT_QUEUE_FRESH_BATCH, args.fresh_batch)
     d = st.to_device()
     # per-step forcing, resident in HBM before the timed region
     Gd = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")

@@ -62,6 +62,7 @@ OPT_ADJ_RICHARDS = 12
 ADJ_RICHARDS_CLOSED_FORM, ADJ_RICHARDS_RECORDED = 0, 1
 OPT_ADJ_SOIL_TEMPERATURE = 13
 ADJ_ST_CLOSED_FORM, ADJ_ST_RECORDED = 0, 1
+OPT_QUEUE_FRESH_BATCH = 14
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
 COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY = 32, 64, 128

@@ -40,6 +40,7 @@ struct clmgb_handle_s {
   void* tape_block;
   clmgb::AdjTape tape;
   int64_t adj_st_mode;          // CLMGB_OPT_ADJ_SOIL_TEMPERATURE
+  int64_t fresh_batch;          // CLMGB_OPT_QUEUE_FRESH_BATCH
   cudaError_t last_error;
 };
 
@@ -50,6 +51,10 @@ static const uint32_t HANDLE_MAGIC = 0xC1A9B300u;
 // 262,144 columns: 1 -> 6.8, 2 -> 7.9, 3 -> 7.5, 4 -> 7.2, occupancy limit -> 5.2
 // M column-steps/s.
 static const int64_t CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM = 2;
+// Lanes of the work-queue kernel that batch the hydraulic block (CLMGB_OPT_QUEUE_FRESH_BATCH).
+// Measured on GB300 at 262,144 columns (2 blocks/SM): 0 -> 10.16, 8 -> 10.36, 16 -> 10.47,
+// 20 -> 10.54, 24 -> 10.51 M column-steps/s.
+static const int64_t CLMGB_DEFAULT_FRESH_BATCH = 20;
 
 using clmgb::Dims;
 
@@ -121,6 +126,7 @@ static int32_t check_cfg(const clmgb_swm_config* cfg) {
 static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
   clmgb::QueueScratch q = h->qs;
   q.longest_first = h->queue_order == 1 ? 1 : 0;
+  q.fresh_batch = (int)h->fresh_batch;
   return q;
 }
 
@@ -183,6 +189,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->qs.order = nullptr;
   h->qs.bins = nullptr;
   h->qs.longest_first = 1;
+  h->fresh_batch = CLMGB_DEFAULT_FRESH_BATCH;
   memset(&h->ws, 0, sizeof(h->ws));
   h->waves_blocks = 0;
   h->waves_blocks_per_sm = 0;
@@ -445,6 +452,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value != CLMGB_ADJ_ST_CLOSED_FORM && value != CLMGB_ADJ_ST_RECORDED) return CLMGB_ERR_CONFIG;
       h->adj_st_mode = value;
       return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_FRESH_BATCH:
+      if (value < 0 || value > 32) return CLMGB_ERR_CONFIG;
+      h->fresh_batch = value;
+      return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
   }
@@ -465,6 +476,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_ADJ_TAPE_SLOTS: *value = h->tape.slots; return CLMGB_OK;
     case CLMGB_OPT_ADJ_RICHARDS: *value = h->tape.richards_mode; return CLMGB_OK;
     case CLMGB_OPT_ADJ_SOIL_TEMPERATURE: *value = h->adj_st_mode; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_FRESH_BATCH: *value = h->fresh_batch; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_USED: {
       unsigned int used = 0;

@@ -1008,6 +1008,96 @@ __device__ __forceinline__ bool mf_begin(MfLaneT<typename ST::S>& L, const Dims&
   return true;
 }
 
+// The hydraulic properties, fluxes and flux derivatives of an accepted substep's
+// starting water (the `fresh` part of an attempt, soil_water_movement.jl:1280-1378).
+// mf_attempt calls it at the first attempt after an accepted substep; the
+// work-queue kernel may also call it on its own, before that attempt, when it
+// batches this block across the lanes of a warp (same operations, same order).
+template <class ST>
+__device__ __forceinline__ void mf_refresh(MfLaneT<typename ST::S>& L, const Dims& D,
+                                           const clmgb_soilwater_fields& f, const clmgb_swm_config& cfg, ST& X) {
+  typedef typename ST::S S;
+  const int64_t ld = D.ldc;
+  const int64_t c = L.c;
+  const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
+  const int nlayers = L.nlayers;
+  const int lower_bc = cfg.lower_boundary_condition;
+  // ---- hydraulic properties (Clapp-Hornberger inlined, :1280-1308) ----
+  S s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
+  for (int j = 1; j <= nlayers; j++) {
+    const S vwc = jl_max(L.liq[j], 1.0e-6) / (L.dzv[j] * DENH2O);
+    S s = vwc / X.Watsat(j);
+    s = jl_min(s, 1.0);
+    s = jl_max(0.01, s);
+    s2[j] = s;
+  }
+  for (int j = 1; j <= nlayers; j++) {
+    S s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
+    s1 = jl_min(s1, 1.0);
+    s1 = jl_max(0.01, s1);
+    const S b = X.Bsw(j);
+    const S hkv = L.imp[j] * X.Hksat(j) * cm_pow(s1, 2.0 * b + 3.0);
+    const S dhkds = (2.0 * b + 3.0) * hkv / s1;
+    const S sn = s2[j];
+    const S smpv = -X.Sucsat(j) * cm_pow(sn, -b);
+    const S dsmpds = -b * smpv / sn;
+    L.hk[j] = hkv;
+    smp[j] = smpv;
+    L.dhkdw[j] = dhkds;
+    dsmpdw[j] = dsmpds / X.Watsat(j);
+    LV(f.smp_l, c, j, ld) = VAL(smpv);
+    LV(f.hk_l, c, j, ld) = VAL(hkv);
+  }
+  // ---- fluxes and derivatives (:1310-1378) ----
+  for (int j = 1; j <= nlayers; j++) {
+    L.qin[j] = 0.0; L.qout[j] = 0.0; L.dqidw0[j] = 0.0; L.dqidw1[j] = 0.0;
+    L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
+  }
+  for (int j = 1; j <= nlayers - 1; j++) {
+    const S dhkds1 = 0.5 * L.dhkdw[j] / X.Watsat(j);
+    const S dhkds2 = 0.5 * L.dhkdw[j] / X.Watsat(j + 1);
+    const S num = smp[j + 1] - smp[j];
+    const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
+    L.qout[j] = -L.hk[j] * num / den + L.hk[j];
+    L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1 * num) / den + dhkds1;
+    L.dqodw2[j] = (-L.hk[j] * dsmpdw[j + 1] - dhkds2 * num) / den + dhkds2;
+  }
+  {
+    const int j = nlayers;
+    if (lower_bc == CLMGB_BC_WATERTABLE) {
+      int jwt = nlevsoi;
+      for (int jj = 1; jj <= nlevsoi; jj++) {
+        if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
+      }
+      if (j > jwt) {
+        L.qout[j] = 0.0; L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
+      } else {
+        const S dhkds1l = L.dhkdw[j] / X.Watsat(j);
+        const S num = -smp[j];
+        const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
+        L.qout[j] = -L.hk[j] * num / den + L.hk[j];
+        L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1l * num) / den + dhkds1l;
+        L.dqodw2[j] = 0.0;
+      }
+    } else if (lower_bc == CLMGB_BC_FLUX) {
+      L.qout[j] = L.hk[j];
+      L.dqodw1[j] = L.dhkdw[j] / X.Watsat(j);
+    } else {
+      L.qout[j] = 0.0;
+      L.dqodw1[j] = 0.0;
+    }
+  }
+  for (int j = 2; j <= nlayers; j++) {
+    L.qin[j] = L.qout[j - 1];
+    L.dqidw0[j] = L.dqodw1[j - 1];
+    L.dqidw1[j] = L.dqodw2[j - 1];
+  }
+  L.qin[1] = f.qflx_infl[c];
+  L.dqidw1[1] = 0.0;
+  for (int j = 1; j <= nlayers; j++) L.fnet1[j] = L.qin[j] - L.qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
+  L.fresh = false;
+}
+
 // one attempt; returns true when the column's substep loop has finished
 template <class ST>
 __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dims& D,
@@ -1045,82 +1135,7 @@ __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dim
     }
     L.dt_cur = dtsub;
   }
-  if (L.fresh) {
-    // ---- hydraulic properties (Clapp-Hornberger inlined, :1280-1308) ----
-    S s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
-    for (int j = 1; j <= nlayers; j++) {
-      const S vwc = jl_max(L.liq[j], 1.0e-6) / (L.dzv[j] * DENH2O);
-      S s = vwc / X.Watsat(j);
-      s = jl_min(s, 1.0);
-      s = jl_max(0.01, s);
-      s2[j] = s;
-    }
-    for (int j = 1; j <= nlayers; j++) {
-      S s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
-      s1 = jl_min(s1, 1.0);
-      s1 = jl_max(0.01, s1);
-      const S b = X.Bsw(j);
-      const S hkv = L.imp[j] * X.Hksat(j) * cm_pow(s1, 2.0 * b + 3.0);
-      const S dhkds = (2.0 * b + 3.0) * hkv / s1;
-      const S sn = s2[j];
-      const S smpv = -X.Sucsat(j) * cm_pow(sn, -b);
-      const S dsmpds = -b * smpv / sn;
-      L.hk[j] = hkv;
-      smp[j] = smpv;
-      L.dhkdw[j] = dhkds;
-      dsmpdw[j] = dsmpds / X.Watsat(j);
-      LV(f.smp_l, c, j, ld) = VAL(smpv);
-      LV(f.hk_l, c, j, ld) = VAL(hkv);
-    }
-    // ---- fluxes and derivatives (:1310-1378) ----
-    for (int j = 1; j <= nlayers; j++) {
-      L.qin[j] = 0.0; L.qout[j] = 0.0; L.dqidw0[j] = 0.0; L.dqidw1[j] = 0.0;
-      L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
-    }
-    for (int j = 1; j <= nlayers - 1; j++) {
-      const S dhkds1 = 0.5 * L.dhkdw[j] / X.Watsat(j);
-      const S dhkds2 = 0.5 * L.dhkdw[j] / X.Watsat(j + 1);
-      const S num = smp[j + 1] - smp[j];
-      const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
-      L.qout[j] = -L.hk[j] * num / den + L.hk[j];
-      L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1 * num) / den + dhkds1;
-      L.dqodw2[j] = (-L.hk[j] * dsmpdw[j + 1] - dhkds2 * num) / den + dhkds2;
-    }
-    {
-      const int j = nlayers;
-      if (lower_bc == CLMGB_BC_WATERTABLE) {
-        int jwt = nlevsoi;
-        for (int jj = 1; jj <= nlevsoi; jj++) {
-          if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
-        }
-        if (j > jwt) {
-          L.qout[j] = 0.0; L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
-        } else {
-          const S dhkds1l = L.dhkdw[j] / X.Watsat(j);
-          const S num = -smp[j];
-          const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
-          L.qout[j] = -L.hk[j] * num / den + L.hk[j];
-          L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1l * num) / den + dhkds1l;
-          L.dqodw2[j] = 0.0;
-        }
-      } else if (lower_bc == CLMGB_BC_FLUX) {
-        L.qout[j] = L.hk[j];
-        L.dqodw1[j] = L.dhkdw[j] / X.Watsat(j);
-      } else {
-        L.qout[j] = 0.0;
-        L.dqodw1[j] = 0.0;
-      }
-    }
-    for (int j = 2; j <= nlayers; j++) {
-      L.qin[j] = L.qout[j - 1];
-      L.dqidw0[j] = L.dqodw1[j - 1];
-      L.dqidw1[j] = L.dqodw2[j - 1];
-    }
-    L.qin[1] = f.qflx_infl[c];
-    L.dqidw1[1] = 0.0;
-    for (int j = 1; j <= nlayers; j++) L.fnet1[j] = L.qin[j] - L.qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
-    L.fresh = false;
-  }
+  if (L.fresh) mf_refresh(L, D, f, cfg, X);
   // ---- RHS / LHS (:1380-1397) fused into the Thomas forward sweep (:1421-1438) ----
   S bet, dwat_prev;
   {

@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(BLOCK)
 k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                       uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
                       const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
-                      int64_t ld_imp, const double* dt_init, SubstepLogView lg) {
+                      int64_t ld_imp, const double* dt_init, SubstepLogView lg, int fresh_batch) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned long long nq = order ? (unsigned long long)(*(volatile const unsigned int*)nlisted_ptr)
@@ -177,7 +177,28 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
       if (__all_sync(FULL, exhausted)) break;
       continue;
     }
-    if (!active) continue;
+    // Batched refresh.  A lane whose substep was just accepted needs the hydraulic
+    // block (mf_refresh, about 2.7 attempts' worth of FP64 work) before its next
+    // attempt.  Run at once, it idles the other lanes of the warp; with
+    // fresh_batch > 0 such lanes wait while the others attempt, until fresh_batch of
+    // them need it or no lane can attempt, and then run it together.  Each column's
+    // operations and their order are unchanged.
+    bool can_try = active;
+    if (fresh_batch > 0) {
+      const bool want = active && L.fresh && L.nsub < MF_ATTEMPT_CAP;
+      const unsigned wm = __ballot_sync(FULL, want);
+      const unsigned tm = __ballot_sync(FULL, active && !want);
+      if (wm && (__popc(wm) >= fresh_batch || tm == 0) && want) {
+        if (LOG && nacc < lg.cap) {
+          double* r0 = lg.rec + L.c * lg.stride + (int64_t)nacc * SUB_REC;
+          for (int j = 1; j <= L.nlayers; j++) r0[j - 1] = L.liq[j];
+        }
+        FieldState<clmgb_soilwater_fields> X(f, L.c, D.ldc);
+        mf_refresh(L, D, f, cfg, X);
+      }
+      can_try = active && !(L.fresh && L.nsub < MF_ATTEMPT_CAP);
+    }
+    if (!can_try) continue;
     double* rec = nullptr;
     double dts = 0.0, dtd = 0.0;
     if (LOG) {
@@ -451,11 +472,12 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   if (log)
     k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                       dev_status, queue, ord, nl, imp, ldi, dt_init,
-                                                                      *log);
+                                                                      *log, qs.fresh_batch);
   else
     k_moisture_form_queue<false><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                        dev_status, queue, ord, nl, imp, ldi, dt_init,
-                                                                       SubstepLogView{nullptr, nullptr, 0, 0});
+                                                                       SubstepLogView{nullptr, nullptr, 0, 0},
+                                                                       qs.fresh_batch);
   return cudaGetLastError();
 }
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {

@@ -18,6 +18,7 @@ struct QueueScratch {
   uint32_t* order;
   unsigned int* bins;
   int longest_first;
+  int fresh_batch;   // CLMGB_OPT_QUEUE_FRESH_BATCH (0: refresh at once)
 };
 
 // Per-column state of the wave-synchronous Richards solve (richards_waves.cu), from

@@ -280,6 +280,10 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
 #define   CLMGB_ADJ_ST_CLOSED_FORM       0 /*   hand-written reverse of every stage, no tape (default;
                                                  used when CLMGB_OPT_ADJ_RICHARDS is closed form too) */
 #define   CLMGB_ADJ_ST_RECORDED          1 /*   replayed through the recording scalar and swept */
+#define CLMGB_OPT_QUEUE_FRESH_BATCH   14 /* work-queue Richards kernel: lanes whose substep was accepted wait
+                                            for the hydraulic block until this many lanes of the warp need it
+                                            (or no lane can attempt), then run it together; 0 = at once.
+                                            Results do not depend on it. */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
 /* Gives the handle per-column scratch for up to max_nc columns (about 48*nlevsoi + 80
  * bytes per column): the Richards solve then forms the ice impedances in a uniform
