@@ -65,7 +65,7 @@ ADJ_ST_CLOSED_FORM, ADJ_ST_RECORDED = 0, 1
 OPT_QUEUE_FRESH_BATCH = 14
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
-COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY = 32, 64, 128
+COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY, COL_FILTER = 32, 64, 128, 256
 ADJ_MAX_SUBSTEPS = 128
 
 CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20
@@ -213,6 +213,33 @@ SOILWATER_FIELDS = [
     ("num_substeps", _f64, "c", None),
 ]
 
+# clmgb_rootsink_fields (compute_effec_rootfrac_and_vert_tran_sink!), header order;
+# HYDRSTRESS_ONLY may be NULL for the default method
+ROOTSINK_FIELDS = [
+    ("mask_hydrology", _u8, "c", None),
+    ("col_itype", _i64, "c", None),
+    ("col_landunit", _i64, "c", None),
+    ("lun_itype", _i64, "l", None),
+    ("col_patchi", _i64, "c", None),
+    ("col_npatches", _i64, "c", None),
+    ("patch_active", _u8, "p", None),
+    ("patch_wtcol", _f64, "p", None),
+    ("rootr_patch", _f64, "p", "G"),
+    ("qflx_tran_veg_patch", _f64, "p", None),
+    ("qflx_tran_veg_col", _f64, "c", None),
+    ("rootr_col", _f64, "c", "G"),
+    ("qflx_rootsoi_col", _f64, "c", "SOI"),
+    ("k_soil_root_patch", _f64, "p", "SOI"),
+    ("smp_l", _f64, "c", "G"),
+    ("vegwp_patch", _f64, "p", "V4"),
+    ("frac_veg_nosno", _i64, "p", None),
+    ("z", _f64, "c", "L"),
+    ("qflx_phs_neg_col", _f64, "c", None),
+    ("qflx_hydr_redist_patch", _f64, "p", None),
+]
+HYDRSTRESS_ONLY = ("k_soil_root_patch", "smp_l", "vegwp_patch", "frac_veg_nosno", "z", "qflx_phs_neg_col",
+                   "qflx_hydr_redist_patch")
+
 # Fields of the synthetic step harness that are not in either struct.
 EXTRA_FIELDS = [
     ("t_ssbef", _f64, "c", "L"),
@@ -237,6 +264,7 @@ STEP_ADJOINT_MEMBERS = [("lam_t_soisno", "L"), ("lam_h2osoi_liq", "L"), ("lam_h2
 StepAdjoint = type("StepAdjoint", (C.Structure,),
                    {"_fields_": [("struct_size", C.c_int64)] + [(n, c_double_p) for n, _ in STEP_ADJOINT_MEMBERS]})
 SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
+RootSinkFields = _mk_struct("RootSinkFields", ROOTSINK_FIELDS)
 
 
 class SubstepLog(C.Structure):
@@ -260,7 +288,7 @@ def level_count(kind, vp):
     """Number of levels of a field kind for a Varpar-like object."""
     L = vp.nlevsno + vp.nlevmaxurbgrnd
     return {"L": L, "LZ": L + 1, "G": vp.nlevgrnd, "S": vp.nlevsno,
-            "S1": vp.nlevsno + 1, "SOI": vp.nlevsoi}[kind]
+            "S1": vp.nlevsno + 1, "SOI": vp.nlevsoi, "V4": 4}[kind]
 
 
 def header_struct_members(header_text, struct_name):

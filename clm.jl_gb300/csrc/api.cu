@@ -258,6 +258,32 @@ int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_effec_rootfrac_vert_tran_sink(clmgb_handle h, const clmgb_bounds* b,
+                                            const clmgb_rootsink_fields* f, int32_t use_hydrstress,
+                                            uint32_t* col_status, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, true);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if (!f) return CLMGB_ERR_NULL_ARG;
+  if (f->struct_size != (int64_t)sizeof(clmgb_rootsink_fields)) return CLMGB_ERR_ABI;
+  // the default method's 13 pointers always, the hydraulic-stress method's 7 with it
+  const void* need[] = {f->mask_hydrology, f->col_itype, f->col_landunit, f->lun_itype, f->col_patchi,
+                        f->col_npatches, f->patch_active, f->patch_wtcol, f->rootr_patch, f->qflx_tran_veg_patch,
+                        f->qflx_tran_veg_col, f->rootr_col, f->qflx_rootsoi_col};
+  for (const void* p : need)
+    if (!p) return CLMGB_ERR_NULL_ARG;
+  if (use_hydrstress) {
+    const void* hs[] = {f->k_soil_root_patch, f->smp_l, f->vegwp_patch, f->frac_veg_nosno, f->z,
+                        f->qflx_phs_neg_col, f->qflx_hydr_redist_patch};
+    for (const void* p : hs)
+      if (!p) return CLMGB_ERR_NULL_ARG;
+  }
+  cudaError_t ce = clmgb::launch_rootsink(make_dims(h->vp, *b), b->nc, b->nl, *f, use_hydrstress ? 1 : 0,
+                                          col_status, h->dev_status, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
                                    void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;

@@ -63,6 +63,8 @@ extern "C" {
                                         of clmgb_reserve_adjoint) */
 #define CLMGB_COL_ADJ_REPLAY   128u  /* step adjoint: a replayed substep was not accepted again
                                         (its adjoint is not valid) */
+#define CLMGB_COL_FILTER       256u  /* root sink: the column is in two of the reference's filters
+                                        (a pervious road on a natural-vegetation landunit) */
 
 /* ---- compile-time limits of this build ---- */
 #define CLMGB_MAX_NLEVSNO   12
@@ -240,6 +242,34 @@ typedef struct clmgb_soilwater_fields {
   double* num_substeps;              /* [nc]  W (Float64 as in the reference) */
 } clmgb_soilwater_fields;
 
+/* compute_effec_rootfrac_and_vert_tran_sink! (soil_water_plant_sink.jl:341-451): the
+ * column root fraction and the transpiration sink qflx_rootsoi that soil_water! reads.
+ * Patch-level level arrays are [ldp, levels] (element (p, j) at p + (j-1)*ldp). */
+typedef struct clmgb_rootsink_fields {
+  int64_t struct_size;               /* sizeof(clmgb_rootsink_fields) */
+  const uint8_t* mask_hydrology;     /* [nc]  filt.hydrologyc */
+  const int64_t* col_itype;          /* [nc] */
+  const int64_t* col_landunit;       /* [nc]  1-based */
+  const int64_t* lun_itype;          /* [nl] */
+  const int64_t* col_patchi;         /* [nc]  1-based first patch */
+  const int64_t* col_npatches;       /* [nc] */
+  const uint8_t* patch_active;       /* [np] */
+  const double* patch_wtcol;         /* [np] */
+  const double* rootr_patch;         /* [ldp, G]  levels 1..nlevsoi read */
+  const double* qflx_tran_veg_patch; /* [np] */
+  const double* qflx_tran_veg_col;   /* [nc] */
+  double* rootr_col;                 /* [ldc, G]  W, levels 1..nlevsoi (default method) */
+  double* qflx_rootsoi_col;          /* [ldc, nlevsoi]  W */
+  /* the hydraulic-stress method only (use_hydrstress != 0; may be NULL otherwise): */
+  const double* k_soil_root_patch;   /* [ldp, nlevsoi] */
+  const double* smp_l;               /* [ldc, G] */
+  const double* vegwp_patch;         /* [ldp, 4]  segment 4 = root */
+  const int64_t* frac_veg_nosno;     /* [np] */
+  const double* z;                   /* [ldc, L] */
+  double* qflx_phs_neg_col;          /* [nc]  W */
+  double* qflx_hydr_redist_patch;    /* [np]  W */
+} clmgb_rootsink_fields;
+
 typedef struct clmgb_handle_s* clmgb_handle;
 
 /* ---- library / handle ---- */
@@ -322,6 +352,18 @@ int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b,
 int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b,
                          const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
                          double dtime, uint32_t* col_status, void* stream);
+
+/* compute_effec_rootfrac_and_vert_tran_sink! (soil_water_plant_sink.jl:341-451) over the
+ * hydrology columns: pervious roads take the transpiration-weighted root fractions
+ * (the default method, which is also the roads' hydraulic-stress method, :48-78 and
+ * :160-180); other columns take the default method, or with use_hydrstress the
+ * soil-root conductance method (:210-245).  A column that is a pervious road on a
+ * natural-vegetation landunit falls in two of the reference's filters, which then
+ * raises an error: it is computed as the reference computes it and flagged
+ * CLMGB_COL_FILTER. */
+int32_t clmgb_effec_rootfrac_vert_tran_sink(clmgb_handle h, const clmgb_bounds* b,
+                                            const clmgb_rootsink_fields* f, int32_t use_hydrstress,
+                                            uint32_t* col_status, void* stream);
 
 /* One whole column step in a single launch: t_ssbef/t_h2osfc_bef copies, soil_temperature!,
  * set_soil_water_fractions!, soil_water! (moisture form) — the driver's order

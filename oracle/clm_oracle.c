@@ -21,6 +21,8 @@
  *     _phase_change_beta_kernel! :1929-2230    _tgrnd_kernel!             :224-247
  *     _eflx_fgr_kernel!          :250-269
  *   _soilhyd_water_fractions_kernel!  src/biogeophys/soil_hydrology.jl:110-130
+ *   compute_effec_rootfrac_and_vert_tran_sink!  src/biogeophys/soil_water_plant_sink.jl:48-78,
+ *                                     :210-245, :341-451
  *   _soilwm_moisture_form_kernel!     src/biogeophys/soil_water_movement.jl:1250-1489
  *   tridiagonal_solve! / _tridiag_multi_kernel!  src/infrastructure/tridiagonal.jl:35-127
  *   tridiagonal_col!                  src/biogeophys/soil_water_movement.jl:736-773
@@ -1169,6 +1171,93 @@ int orc_soil_water_fractions(const clmgb_varpar* vp, const clmgb_bounds* b,
 #endif
   for (int64_t c = 0; c < b->nc; c++) fractions_col(vp, b, f, c);
   return 0;
+}
+
+/* ===================================================================== */
+/* compute_effec_rootfrac_and_vert_tran_sink! (soil_water_plant_sink.jl)  */
+/* ===================================================================== */
+/* _plantsink_default_kernel! (:48-78) over one filter */
+static void rootsink_default_filter(const clmgb_varpar* vp, const clmgb_bounds* b,
+                                    const clmgb_rootsink_fields* f, const int64_t* filt, int64_t n)
+{
+  for (int64_t i = 0; i < n; i++) {
+    const int64_t c = filt[i];
+    const int64_t p_lo = f->col_patchi[c] - 1, p_hi = f->col_patchi[c] + f->col_npatches[c] - 2;
+    double temp_c = 0.0;
+    for (int64_t p = p_lo; p <= p_hi; p++)
+      if (f->patch_active[p]) temp_c += f->qflx_tran_veg_patch[p] * f->patch_wtcol[p];
+    for (int j = 1; j <= vp->nlevsoi; j++) {
+      double acc = 0.0;
+      for (int64_t p = p_lo; p <= p_hi; p++)
+        if (f->patch_active[p]) acc += IX(f->rootr_patch, p, j, b->ldp) * f->qflx_tran_veg_patch[p] * f->patch_wtcol[p];
+      if (temp_c != 0.0) acc /= temp_c;
+      IX(f->rootr_col, c, j, b->ldc) = acc;
+      IX(f->qflx_rootsoi_col, c, j, b->ldc) = acc * f->qflx_tran_veg_col[c];
+    }
+  }
+}
+
+/* _plantsink_hydstress_kernel! (:210-245) over one filter, root_idx = 4 */
+static void rootsink_hydstress_filter(const clmgb_varpar* vp, const clmgb_bounds* b,
+                                      const clmgb_rootsink_fields* f, const int64_t* filt, int64_t n)
+{
+  for (int64_t i = 0; i < n; i++) {
+    const int64_t c = filt[i];
+    const int64_t p_lo = f->col_patchi[c] - 1, p_hi = f->col_patchi[c] + f->col_npatches[c] - 2;
+    f->qflx_phs_neg_col[c] = 0.0;
+    for (int j = 1; j <= vp->nlevsoi; j++) {
+      const double grav2 = IX(f->z, c, j + vp->nlevsno, b->ldc) * 1000.0;
+      double temp_c = 0.0;
+      for (int64_t p = p_lo; p <= p_hi; p++) {
+        if (j == 1) f->qflx_hydr_redist_patch[p] = 0.0;
+        if (f->patch_active[p] && f->frac_veg_nosno[p] > 0) {
+          if (f->patch_wtcol[p] > 0.0) {
+            const double patchflux = IX(f->k_soil_root_patch, p, j, b->ldp) *
+                (IX(f->smp_l, c, j, b->ldc) - IX(f->vegwp_patch, p, 4, b->ldp) - grav2);
+            if (patchflux < 0.0) f->qflx_hydr_redist_patch[p] += patchflux;
+            temp_c += patchflux * f->patch_wtcol[p];
+          }
+        }
+      }
+      IX(f->qflx_rootsoi_col, c, j, b->ldc) = temp_c;
+      if (temp_c < 0.0) f->qflx_phs_neg_col[c] += temp_c;
+    }
+  }
+}
+
+/* the wrapper (:341-451): three filters in order; returns 1 when the filter counts do
+ * not add up to the hydrology columns (the reference's error) */
+int orc_rootsink(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_rootsink_fields* f,
+                 int32_t use_hydrstress)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  int64_t* filt = (int64_t*)calloc((size_t)(b->nc > 0 ? b->nc : 1), sizeof(int64_t));
+  int64_t n, total = 0, nhyd = 0;
+  for (int64_t c = 0; c < b->nc; c++) nhyd += f->mask_hydrology[c] ? 1 : 0;
+  /* 1) pervious roads */
+  n = 0;
+  for (int64_t c = 0; c < b->nc; c++)
+    if (f->mask_hydrology[c] && f->col_itype[c] == ICOL_ROAD_PERV) filt[n++] = c;
+  total += n;
+  rootsink_default_filter(vp, b, f, filt, n);   /* hydstress_roads is the same algorithm */
+  /* 2) neither pervious road nor natural vegetation */
+  n = 0;
+  for (int64_t c = 0; c < b->nc; c++)
+    if (f->mask_hydrology[c] && f->col_itype[c] != ICOL_ROAD_PERV &&
+        f->lun_itype[f->col_landunit[c] - 1] != ISTSOIL) filt[n++] = c;
+  total += n;
+  if (use_hydrstress) rootsink_hydstress_filter(vp, b, f, filt, n);
+  else rootsink_default_filter(vp, b, f, filt, n);
+  /* 3) natural vegetation */
+  n = 0;
+  for (int64_t c = 0; c < b->nc; c++)
+    if (f->mask_hydrology[c] && f->lun_itype[f->col_landunit[c] - 1] == ISTSOIL) filt[n++] = c;
+  total += n;
+  if (use_hydrstress) rootsink_hydstress_filter(vp, b, f, filt, n);
+  else rootsink_default_filter(vp, b, f, filt, n);
+  free(filt);
+  return total != nhyd ? 1 : 0;
 }
 
 /* ===================================================================== */

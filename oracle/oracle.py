@@ -34,6 +34,7 @@ def lib():
         P = C.c_void_p
         L.orc_soil_temperature.argtypes = [P, P, P, C.c_double, C.c_int32, P, C.c_int32]
         L.orc_soil_water_fractions.argtypes = [P, P, P, C.c_int32]
+        L.orc_rootsink.argtypes = [P, P, P, C.c_int32]
         L.orc_soil_water.argtypes = [P, P, P, P, C.c_double, P, P, P, C.c_int32]
         L.orc_run_steps.argtypes = [P, P, P, P, P, C.c_double, C.c_int32, C.c_int32, P, P,
                                     C.c_int64, P, P, P, C.c_int32]
@@ -80,6 +81,16 @@ def soil_temperature(st, dtime, snow_method=abi.SNOW_JORDAN1991, nthreads=None):
 def soil_water_fractions(st, nthreads=None):
     vp, b, f = st.vp, st.bounds(), st.soilwater_fields()
     _chk(lib().orc_soil_water_fractions(C.byref(vp), C.byref(b), C.byref(f), nthreads or default_threads()))
+
+
+def rootsink(rs, use_hydrstress=False):
+    """compute_effec_rootfrac_and_vert_tran_sink! in place on a host RootSinkState;
+    returns 1 where the reference would raise its filter-count error, else 0."""
+    vp, b, f = rs.vp, rs.bounds(), rs.fields(with_hydrstress=True)
+    rc = lib().orc_rootsink(C.byref(vp), C.byref(b), C.byref(f), 1 if use_hydrstress else 0)
+    if rc < 0:
+        _chk(rc)
+    return rc
 
 
 def soil_water(st, dtime, cfg=None, capture=False, nthreads=None):

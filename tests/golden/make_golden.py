@@ -40,6 +40,81 @@ def band_case(A, x, jtop, nlevs, kl, ku, tol, src):
                 jbot=jtop + n - 1, nlevs=nlevs, kl=kl, ku=ku, atol=tol, source=src)
 
 
+def rootsink_cases():
+    """test/test_soil_water_plant_sink.jl: varpar nlevsno 5, nlevgrnd 10, nlevsoi 4 (:8-21);
+    z[c, j + nlevsno] = 0.1 j (:57-61); the expected values are the test's own formulas."""
+    ISTSOIL, ISTCROP, ISTURB_MD, ROAD = 1, 2, 9, 75
+    nsoi = 4
+    zs = [0.1 * j for j in range(1, nsoi + 1)]
+    out = []
+
+    def case(name, src, method, col_itype, col_landunit, lun_itype, ppc, rootr, tran_p, tran_c, wt, active,
+             expect, mask=None, fvn=None, k=None, smp=None, vegwp4=None, use_hydrstress=False):
+        nc = len(col_itype)
+        out.append(dict(name=name, source=src, method=method, use_hydrstress=use_hydrstress,
+                        nc=nc, np=len(wt), nl=len(lun_itype), col_itype=col_itype, col_landunit=col_landunit,
+                        lun_itype=lun_itype, patches_per_col=ppc, rootr=rootr, tran_patch=tran_p,
+                        tran_col=tran_c, wtcol=wt, active=active, mask=mask or [True] * nc,
+                        fvn=fvn or [0] * len(wt), k=k or [[0.0] * nsoi for _ in wt],
+                        smp=smp or [0.0] * nc, vegwp4=vegwp4 or [0.0] * len(wt), expect=expect))
+
+    r = [0.4, 0.3, 0.2, 0.1]
+    case("default_single", "test/test_soil_water_plant_sink.jl:131-163", "default", [ISTSOIL], [1], [ISTSOIL], [1],
+         [r], [0.002], [0.002], [1.0], [True],
+         dict(rootr_col=[r], rootsoi=[[x * 0.002 for x in r]], atol_rootr=1e-12, atol_rootsoi=1e-14))
+    r1, r2 = [0.1, 0.2, 0.3, 0.4], [0.5, 0.3, 0.15, 0.05]
+    tp, wt = [0.001, 0.003], [0.4, 0.6]
+    temp = tp[0] * wt[0] + tp[1] * wt[1]
+    ex = [(r1[j] * tp[0] * wt[0] + r2[j] * tp[1] * wt[1]) / temp for j in range(nsoi)]
+    case("default_two_patches", "test/test_soil_water_plant_sink.jl:165-207", "default", [ISTSOIL], [1], [ISTSOIL],
+         [2], [r1, r2], tp, [temp], wt, [True, True],
+         dict(rootr_col=[ex], rootsoi=[[x * temp for x in ex]], atol_rootr=1e-12, atol_rootsoi=1e-14))
+    case("default_zero_transpiration", "test/test_soil_water_plant_sink.jl:209-238", "default", [ISTSOIL], [1],
+         [ISTSOIL], [1], [[0.25] * 4], [0.0], [0.0], [1.0], [True],
+         dict(rootr_col=[[0.0] * 4], rootsoi=[[0.0] * 4], atol_rootr=1e-14, atol_rootsoi=1e-14))
+    case("default_inactive_patch", "test/test_soil_water_plant_sink.jl:240-270", "default", [ISTSOIL], [1],
+         [ISTSOIL], [2], [[0.4, 0.3, 0.2, 0.1], [0.1, 0.1, 0.1, 0.7]], [0.002, 0.005], [0.001], [0.5, 0.5],
+         [True, False], dict(rootr_col=[[0.4, 0.3, 0.2, 0.1]], atol_rootr=1e-12))
+    rr = [0.3, 0.3, 0.2, 0.2]
+    case("hydstress_roads", "test/test_soil_water_plant_sink.jl:272-304", "hydstress_roads", [ROAD], [1],
+         [ISTURB_MD], [1], [rr], [0.001], [0.001], [1.0], [True],
+         dict(rootr_col=[rr], rootsoi=[[x * 0.001 for x in rr]], atol_rootr=1e-12, atol_rootsoi=1e-14),
+         use_hydrstress=True)
+    fl = [0.01 * (-500.0 - (-1000.0) - z * 1000.0) for z in zs]
+    case("hydstress_single", "test/test_soil_water_plant_sink.jl:306-346", "hydstress", [ISTSOIL], [1], [ISTSOIL],
+         [1], [[0.0] * 4], [0.002], [0.002], [1.0], [True],
+         dict(rootsoi=[fl], atol_rootsoi=1e-10), fvn=[1], k=[[0.01] * 4], smp=[-500.0], vegwp4=[-1000.0],
+         use_hydrstress=True)
+    fl = [0.01 * (-5000.0 - (-500.0) - z * 1000.0) for z in zs]
+    case("hydstress_negative", "test/test_soil_water_plant_sink.jl:348-389", "hydstress", [ISTSOIL], [1],
+         [ISTSOIL], [1], [[0.0] * 4], [0.002], [0.002], [1.0], [True],
+         dict(rootsoi=[fl], phs_neg=[sum(fl)], hydr_redist_negative=[True], atol_rootsoi=1e-10),
+         fvn=[1], k=[[0.01] * 4], smp=[-5000.0], vegwp4=[-500.0], use_hydrstress=True)
+    fl = [0.01 * (-500.0 - (-1000.0) - z * 1000.0) * 0.6 for z in zs]
+    case("hydstress_noveg_patch", "test/test_soil_water_plant_sink.jl:391-434", "hydstress",
+         [ISTSOIL], [1], [ISTSOIL], [2], [[0.0] * 4, [0.0] * 4], [0.002, 0.003], [0.002], [0.6, 0.4],
+         [True, True], dict(rootsoi=[fl], atol_rootsoi=1e-10), fvn=[1, 0], k=[[0.01] * 4, [0.01] * 4],
+         smp=[-500.0], vegwp4=[-1000.0, -200.0], use_hydrstress=True)
+    rw = [[0.25] * 4, [0.4, 0.3, 0.2, 0.1], [0.1, 0.2, 0.3, 0.4]]
+    tc = [0.001, 0.002, 0.003]
+    case("wrapper_default_types", "test/test_soil_water_plant_sink.jl:436-482", "wrapper", [ROAD, ISTCROP, ISTSOIL],
+         [1, 2, 3], [ISTURB_MD, ISTCROP, ISTSOIL], [1, 1, 1], rw, tc, tc, [1.0, 1.0, 1.0], [True] * 3,
+         dict(rootr_col=rw, rootsoi=[[x * tc[c] for x in rw[c]] for c in range(3)], atol_rootr=1e-12,
+              atol_rootsoi=1e-14))
+    case("wrapper_hydstress_dispatch", "test/test_soil_water_plant_sink.jl:520-572", "wrapper", [ROAD, ISTSOIL],
+         [1, 2], [ISTURB_MD, ISTSOIL], [1, 1], [[0.25] * 4, [0.0] * 4], [0.001, 0.002], [0.001, 0.002],
+         [1.0, 1.0], [True, True],
+         dict(rootr_col=[[0.25] * 4, None], rootsoi=[None, [0.005 * (-300.0 - (-600.0) - z * 1000.0) for z in zs]],
+              atol_rootr=1e-12, atol_rootsoi=1e-10),
+         fvn=[1, 1], k=[[0.005] * 4, [0.005] * 4], smp=[-300.0, -300.0], vegwp4=[-800.0, -600.0],
+         use_hydrstress=True)
+    case("wrapper_mask", "test/test_soil_water_plant_sink.jl:612-652", "wrapper", [ISTSOIL, ISTSOIL], [1, 1],
+         [ISTSOIL], [1, 1], [[0.4, 0.3, 0.2, 0.1], [0.1, 0.2, 0.3, 0.4]], [0.001, 0.002], [0.001, 0.002],
+         [1.0, 1.0], [True, True], dict(rootr_col=[[0.4, 0.3, 0.2, 0.1], [0.0] * 4], atol_rootr=1e-12),
+         mask=[True, False])
+    return dict(nlevsno=5, nlevgrnd=10, nlevsoi=nsoi, nlevurb=5, nlevmaxurbgrnd=10, z_soil=zs, cases=out)
+
+
 def main():
     cases = {}
     cases["band_penta5"] = band_case(penta(5), np.arange(1.0, 6.0), 1, 5, 2, 2, 1e-10,
@@ -106,6 +181,7 @@ def main():
                                               frac_h2osfc=0.5, h2osfc=20.0, dT=-1.0, fact0=1.0, c_h2osfc=0.0,
                                               dtime=1800.0, dhsdT=-1000.0,
                                               source="test/test_soil_temperature.jl:498-532")
+    cases["rootsink"] = rootsink_cases()
     with open(os.path.join(HERE, "reference_cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1, sort_keys=True)
 

@@ -31,7 +31,8 @@ def test_library_exports_every_declared_symbol():
 def test_header_structs_match_ctypes():
     txt = header_text()
     for sname, fields in (("clmgb_soiltemp_fields", abi.SOILTEMP_FIELDS),
-                          ("clmgb_soilwater_fields", abi.SOILWATER_FIELDS)):
+                          ("clmgb_soilwater_fields", abi.SOILWATER_FIELDS),
+                          ("clmgb_rootsink_fields", abi.ROOTSINK_FIELDS)):
         members = abi.header_struct_members(txt, sname)
         assert members[0] == "struct_size"
         assert members[1:] == [f[0] for f in fields], sname
@@ -39,6 +40,7 @@ def test_header_structs_match_ctypes():
     assert abi.header_struct_members(txt, "clmgb_bounds") == [f[0] for f in abi.Bounds._fields_]
     assert abi.header_struct_members(txt, "clmgb_swm_config") == [f[0] for f in abi.SwmConfig._fields_]
     assert abi.header_struct_members(txt, "clmgb_step_adjoint") == [f[0] for f in abi.StepAdjoint._fields_]
+    assert abi.header_struct_members(txt, "clmgb_substep_log") == [f[0] for f in abi.SubstepLog._fields_]
 
 
 def test_header_constants_match_python():
@@ -46,7 +48,9 @@ def test_header_constants_match_python():
     consts = dict(re.findall(r"#define\s+CLMGB_(\w+)\s+(\d+)u?\b", txt))
     for name in ("COL_ADJ_UNSUPPORTED", "COL_TAPE_FULL", "OPT_ADJ_TAPE_USED", "OPT_ADJ_TAPE_SLOTS",
                  "OPT_ADJ_TAPE_ENTRIES", "OPT_STEP_SCHEDULE", "OPT_WAVES_OCCUPANCY", "OPT_ADJ_RICHARDS",
-                 "ADJ_RICHARDS_CLOSED_FORM", "ADJ_RICHARDS_RECORDED", "COL_ADJ_REPLAY", "ADJ_MAX_SUBSTEPS"):
+                 "ADJ_RICHARDS_CLOSED_FORM", "ADJ_RICHARDS_RECORDED", "COL_ADJ_REPLAY", "ADJ_MAX_SUBSTEPS",
+                 "OPT_ADJ_SOIL_TEMPERATURE", "ADJ_ST_CLOSED_FORM", "ADJ_ST_RECORDED", "OPT_QUEUE_FRESH_BATCH",
+                 "COL_FILTER"):
         assert int(consts[name]) == getattr(abi, name), name
 
 

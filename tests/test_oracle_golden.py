@@ -271,3 +271,27 @@ def test_workload_water_balance_closes():
     w1 = st["h2osoi_liq"].sum(0) + st["h2osoi_ice"].sum(0) + st["h2osno_no_layers"] + st["h2osfc"]
     expect = I_.sum(0) * wl.dtime - st["qflx_rootsoi"].sum(0) * wl.dtime * 6
     np.testing.assert_allclose(w1 - w0, expect, atol=1e-9)
+
+
+def test_oracle_root_sink_known_answers():
+    """compute_effec_rootfrac_and_vert_tran_sink! known answers of
+    test_soil_water_plant_sink.jl, through the oracle's wrapper restatement."""
+    import rootsink_cases as RC
+    from oracle import oracle as O
+    g = RC.load()
+    for case in g["cases"]:
+        rs = RC.build(g, case)
+        assert O.rootsink(rs, case["use_hydrstress"]) == 0
+        RC.check(g, case, rs)
+
+
+def test_oracle_root_sink_filter_error():
+    """A pervious road on a natural-vegetation landunit sits in two of the wrapper's
+    filters: the counts disagree, where the reference raises its error."""
+    import rootsink_cases as RC
+    from oracle import oracle as O
+    g = RC.load()
+    case = dict(g["cases"][0])
+    case["col_itype"] = [75]
+    rs = RC.build(g, case)
+    assert O.rootsink(rs, False) == 1
