@@ -237,6 +237,30 @@ ROOTSINK_FIELDS = [
     ("qflx_phs_neg_col", _f64, "c", None),
     ("qflx_hydr_redist_patch", _f64, "p", None),
 ]
+# clmgb_zd09_fields (soilwater_zengdecker2009!), header order
+ZD09_FIELDS = [
+    ("mask_hydrology", _u8, "c", None),
+    ("dz", _f64, "c", "L"),
+    ("z", _f64, "c", "L"),
+    ("zi", _f64, "c", "LZ"),
+    ("t_soisno", _f64, "c", "L"),
+    ("h2osoi_liq", _f64, "c", "L"),
+    ("h2osoi_ice", _f64, "c", "L"),
+    ("h2osoi_vol", _f64, "c", "G"),
+    ("watsat", _f64, "c", "G"),
+    ("hksat", _f64, "c", "G"),
+    ("bsw", _f64, "c", "G"),
+    ("sucsat", _f64, "c", "G"),
+    ("smpmin", _f64, "c", None),
+    ("icefrac", _f64, "c", "G"),
+    ("smp_l", _f64, "c", "G"),
+    ("hk_l", _f64, "c", "G"),
+    ("qflx_rootsoi", _f64, "c", "SOI"),
+    ("qflx_infl", _f64, "c", None),
+    ("zwt", _f64, "c", None),
+    ("qcharge", _f64, "c", None),
+    ("qflx_deficit", _f64, "c", None),
+]
 HYDRSTRESS_ONLY = ("k_soil_root_patch", "smp_l", "vegwp_patch", "frac_veg_nosno", "z", "qflx_phs_neg_col",
                    "qflx_hydr_redist_patch")
 
@@ -265,6 +289,7 @@ StepAdjoint = type("StepAdjoint", (C.Structure,),
                    {"_fields_": [("struct_size", C.c_int64)] + [(n, c_double_p) for n, _ in STEP_ADJOINT_MEMBERS]})
 SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
 RootSinkFields = _mk_struct("RootSinkFields", ROOTSINK_FIELDS)
+Zd09Fields = _mk_struct("Zd09Fields", ZD09_FIELDS)
 
 
 class SubstepLog(C.Structure):

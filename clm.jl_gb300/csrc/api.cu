@@ -258,6 +258,23 @@ int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_soil_water_zd09(clmgb_handle h, const clmgb_bounds* b, const clmgb_zd09_fields* f,
+                              const clmgb_swm_config* cfg, double dtime, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (!cfg) return CLMGB_ERR_NULL_ARG;
+  // init_soilwater_movement (soil_water_movement.jl:681-698): ZD09 with the aquifer
+  // lower boundary only
+  if (cfg->soilwater_movement_method != CLMGB_ZENGDECKER_2009) return CLMGB_ERR_CONFIG;
+  if (cfg->lower_boundary_condition != CLMGB_BC_AQUIFER) return CLMGB_ERR_CONFIG;
+  int32_t e = check_bounds(b, false);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  cudaError_t ce = clmgb::launch_zd09(make_dims(h->vp, *b), b->nc, *f, cfg->e_ice, dtime, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 int32_t clmgb_effec_rootfrac_vert_tran_sink(clmgb_handle h, const clmgb_bounds* b,
                                             const clmgb_rootsink_fields* f, int32_t use_hydrstress,
                                             uint32_t* col_status, void* stream) {

@@ -113,14 +113,62 @@ function soilwater_fields(col, mask_hydrology, sh, ss, wfb, wsb)
     buf
 end
 
+# a fields struct: its size, then one device pointer per member
+function fields_buffer(p::Vector{Ptr{Cvoid}})
+    buf = Vector{UInt8}(undef, 8 * (1 + length(p)))
+    GC.@preserve buf begin
+        unsafe_store!(Ptr{Int64}(pointer(buf)), Int64(length(buf)))
+        for (i, q) in enumerate(p)
+            unsafe_store!(Ptr{Ptr{Cvoid}}(pointer(buf) + 8i), q)
+        end
+    end
+    buf
+end
+
+# compute_effec_rootfrac_and_vert_tran_sink! (soil_water_plant_sink.jl:341) on CuArrays
+function CLM.compute_effec_rootfrac_and_vert_tran_sink!(bounds_col, nlevsoi, mask_hydrology::CuArray,
+        ss, cs, wfb, ef, col, lun, patch_data; use_hydrstress::Bool = false)
+    f = fields_buffer(Ptr{Cvoid}[ptr(mask_hydrology), ptr(col.itype), ptr(col.landunit), ptr(lun.itype),
+                                 ptr(col.patchi), ptr(col.npatches), ptr(patch_data.active), ptr(patch_data.wtcol),
+                                 ptr(ss.rootr_patch), ptr(wfb.wf.qflx_tran_veg_patch), ptr(wfb.wf.qflx_tran_veg_col),
+                                 ptr(ss.rootr_col), ptr(wfb.qflx_rootsoi_col), ptr(ss.k_soil_root_patch),
+                                 ptr(ss.smp_l_col), ptr(cs.vegwp_patch), ptr(cs.frac_veg_nosno_patch), ptr(col.z),
+                                 ptr(wfb.qflx_phs_neg_col), ptr(wfb.qflx_hydr_redist_patch)])
+    b = Bounds(length(mask_hydrology), length(patch_data.wtcol), length(lun.itype), size(col.z, 1),
+               length(patch_data.wtcol))
+    GC.@preserve f begin
+        check(ccall((:clmgb_effec_rootfrac_vert_tran_sink, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Int32, Ptr{UInt32}, Ptr{Cvoid}),
+                    handle(), b, f, Int32(use_hydrstress), C_NULL, CUDA.stream().handle),
+              "clmgb_effec_rootfrac_vert_tran_sink")
+    end
+    nothing
+end
+
 function CLM.soil_water!(col::CLM.ColumnData{<:Any,<:CuArray}, mask_hydrology, mask_urban, sh, ss, wfb,
                          wsb, temp, cs, ef, swrc, cfg::CLM.SoilWaterMovementConfig, dtime;
                          use_flexibleCN::Bool = false)
     use_flexibleCN && error("use_flexibleCN is not implemented by the GB300 path")
     c = SwmConfig(cfg.soilwater_movement_method, cfg.upper_boundary_condition, cfg.lower_boundary_condition,
                   cfg.flux_calculation, cfg.dtmin, cfg.verySmall, cfg.xTolerUpper, cfg.xTolerLower, cfg.e_ice)
-    f = soilwater_fields(col, mask_hydrology, sh, ss, wfb, wsb)
     b = Bounds(length(mask_hydrology), 0, 0, size(col.dz, 1), 0)
+    if cfg.soilwater_movement_method == CLM.ZENGDECKER_2009
+        # soilwater_zengdecker2009! has its own field set (clmgb_zd09_fields)
+        z = fields_buffer(Ptr{Cvoid}[ptr(mask_hydrology), ptr(col.dz), ptr(col.z), ptr(col.zi),
+                                     ptr(temp.t_soisno_col), ptr(wsb.ws.h2osoi_liq_col),
+                                     ptr(wsb.ws.h2osoi_ice_col), ptr(wsb.ws.h2osoi_vol_col), ptr(ss.watsat_col),
+                                     ptr(ss.hksat_col), ptr(ss.bsw_col), ptr(ss.sucsat_col), ptr(ss.smpmin_col),
+                                     ptr(sh.icefrac_col), ptr(ss.smp_l_col), ptr(ss.hk_l_col),
+                                     ptr(wfb.qflx_rootsoi_col), ptr(wfb.wf.qflx_infl_col), ptr(sh.zwt_col),
+                                     ptr(sh.qcharge_col), ptr(wfb.qflx_deficit_col)])
+        GC.@preserve z begin
+            check(ccall((:clmgb_soil_water_zd09, lib), Int32,
+                        (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Ptr{Cvoid}),
+                        handle(), b, z, c, dtime, CUDA.stream().handle), "clmgb_soil_water_zd09")
+        end
+        return nothing
+    end
+    f = soilwater_fields(col, mask_hydrology, sh, ss, wfb, wsb)
     GC.@preserve f begin
         check(ccall((:clmgb_soil_water, lib), Int32,
                     (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Ptr{UInt32}, Ptr{Cvoid}),

@@ -270,6 +270,33 @@ typedef struct clmgb_rootsink_fields {
   double* qflx_hydr_redist_patch;    /* [np]  W */
 } clmgb_rootsink_fields;
 
+/* soilwater_zengdecker2009! (soil_water_movement.jl:1616-1764): the fields of the
+ * Zeng & Decker (2009) method, which soil_water! selects with use_aquifer_layer. */
+typedef struct clmgb_zd09_fields {
+  int64_t struct_size;               /* sizeof(clmgb_zd09_fields) */
+  const uint8_t* mask_hydrology;     /* [nc] */
+  const double* dz;                  /* [ldc, L] */
+  const double* z;                   /* [ldc, L] */
+  const double* zi;                  /* [ldc, LZ] */
+  const double* t_soisno;            /* [ldc, L] */
+  double* h2osoi_liq;                /* [ldc, L]  RW (soil part) */
+  const double* h2osoi_ice;          /* [ldc, L] */
+  const double* h2osoi_vol;          /* [ldc, G] */
+  const double* watsat;              /* [ldc, G] */
+  const double* hksat;               /* [ldc, G] */
+  const double* bsw;                 /* [ldc, G] */
+  const double* sucsat;              /* [ldc, G] */
+  const double* smpmin;              /* [nc] */
+  double* icefrac;                   /* [ldc, G]  W */
+  double* smp_l;                     /* [ldc, G]  W */
+  double* hk_l;                      /* [ldc, G]  W */
+  const double* qflx_rootsoi;        /* [ldc, nlevsoi] */
+  const double* qflx_infl;           /* [nc] */
+  const double* zwt;                 /* [nc] */
+  double* qcharge;                   /* [nc]  W */
+  double* qflx_deficit;              /* [nc]  W */
+} clmgb_zd09_fields;
+
 typedef struct clmgb_handle_s* clmgb_handle;
 
 /* ---- library / handle ---- */
@@ -352,6 +379,16 @@ int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b,
 int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b,
                          const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
                          double dtime, uint32_t* col_status, void* stream);
+
+/* soil_water! with the Zeng-Decker 2009 method (soilwater_zengdecker2009!,
+ * soil_water_movement.jl:1616-1764): equilibrium matric potential from the water
+ * table, one implicit tridiagonal solve over the soil layers plus the aquifer layer,
+ * aquifer recharge qcharge and the water deficit.  cfg must select
+ * CLMGB_ZENGDECKER_2009 with the CLMGB_BC_AQUIFER lower boundary (the reference's
+ * init_soilwater_movement rejects any other pair, :681-705).  clmgb_soil_water returns
+ * CLMGB_ERR_UNSUPPORTED for this method: its fields are these. */
+int32_t clmgb_soil_water_zd09(clmgb_handle h, const clmgb_bounds* b, const clmgb_zd09_fields* f,
+                              const clmgb_swm_config* cfg, double dtime, void* stream);
 
 /* compute_effec_rootfrac_and_vert_tran_sink! (soil_water_plant_sink.jl:341-451) over the
  * hydrology columns: pervious roads take the transpiration-weighted root fractions

@@ -21,6 +21,7 @@
  *     _phase_change_beta_kernel! :1929-2230    _tgrnd_kernel!             :224-247
  *     _eflx_fgr_kernel!          :250-269
  *   _soilhyd_water_fractions_kernel!  src/biogeophys/soil_hydrology.jl:110-130
+ *   soilwater_zengdecker2009!         src/biogeophys/soil_water_movement.jl:97-635,1616-1764
  *   compute_effec_rootfrac_and_vert_tran_sink!  src/biogeophys/soil_water_plant_sink.jl:48-78,
  *                                     :210-245, :341-451
  *   _soilwm_moisture_form_kernel!     src/biogeophys/soil_water_movement.jl:1250-1489
@@ -1172,6 +1173,293 @@ int orc_soil_water_fractions(const clmgb_varpar* vp, const clmgb_bounds* b,
   for (int64_t c = 0; c < b->nc; c++) fractions_col(vp, b, f, c);
   return 0;
 }
+
+/* ===================================================================== */
+/* soilwater_zengdecker2009! (soil_water_movement.jl:1616-1764): the ten  */
+/* stages as the reference runs them, each over every column, with       */
+/* [nc, nlevsoi+1] scratch matrices (SC(a, c, j) = a[c*n1 + j], j 1-based) */
+/* ===================================================================== */
+#define SC(a, c, j) ((a)[(int64_t)(c) * n1 + (j)])
+
+int orc_soil_water_zd09(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_zd09_fields* f,
+                        double e_ice, double dtime)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  const int64_t nc = b->nc, ld = b->ldc;
+  const int nlevsoi = vp->nlevsoi, nlevgrnd = vp->nlevgrnd, joff = vp->nlevsno, joff_zi = vp->nlevsno + 1;
+  const int64_t n1 = nlevsoi + 3;
+  const double sdamp = 0.0;
+  enum { ZMM, DZMM, ZIMM, ICEF, VWC, VOLEQ, ZQ, HK, DHKDW, SMP, DSMPDW, IMPED, QIN, QOUT, DQIDW0, DQIDW1,
+         DQODW1, DQODW2, AMX, BMX, CMX, RMX, DWAT2, CP, NMAT };
+  double* M[NMAT];
+  for (int k = 0; k < NMAT; k++) M[k] = (double*)calloc((size_t)(nc > 0 ? nc : 1) * n1, sizeof(double));
+  double* zwtmm = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+  double* vwc_zwt = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+  int* jwt = (int*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(int));
+  /* _soilwm_mm_icefrac_kernel! (:97-127) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    for (int j = 1; j <= nlevsoi; j++) {
+      SC(M[ZMM], c, j) = IX(f->z, c, joff + j, ld) * 1.0e3;
+      SC(M[DZMM], c, j) = IX(f->dz, c, joff + j, ld) * 1.0e3;
+      SC(M[ZIMM], c, j + 1) = IX(f->zi, c, joff_zi + j, ld) * 1.0e3;
+      double vol_ice = jl_min(IX(f->watsat, c, j, ld), IX(f->h2osoi_ice, c, joff + j, ld) / (IX(f->dz, c, joff + j, ld) * DENICE));
+      SC(M[ICEF], c, j) = jl_min(1.0, vol_ice / IX(f->watsat, c, j, ld));
+      IX(f->icefrac, c, j, ld) = SC(M[ICEF], c, j);
+      SC(M[VWC], c, j) = jl_max(IX(f->h2osoi_liq, c, joff + j, ld), 1.0e-6) / (IX(f->dz, c, joff + j, ld) * DENH2O);
+    }
+  }
+  /* _soilwm_zwtmm_kernel! (:143-150) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    SC(M[ZIMM], c, 1) = 0.0;
+    zwtmm[c] = f->zwt[c] * 1.0e3;
+  }
+  /* _soilwm_jwt_vwczwt_kernel! (:289-327) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    int jw = nlevsoi;
+    for (int j = 1; j <= nlevsoi; j++)
+      if (f->zwt[c] <= IX(f->zi, c, joff_zi + j, ld)) { jw = j - 1; break; }
+    jwt[c] = jw;
+    vwc_zwt[c] = IX(f->watsat, c, nlevsoi, ld);
+    if (IX(f->t_soisno, c, joff + jw + 1, ld) < TFRZ) {
+      double v = SC(M[VWC], c, nlevsoi);
+      for (int j = nlevsoi; j <= nlevgrnd; j++) {
+        if (f->zwt[c] <= IX(f->zi, c, joff_zi + j, ld)) {
+          double t = IX(f->t_soisno, c, joff + j, ld);
+          double smp1 = HFUS * (TFRZ - t) / (GRAV * t) * 1000.0;
+          smp1 = jl_max(IX(f->sucsat, c, nlevsoi, ld), smp1);
+          v = IX(f->watsat, c, nlevsoi, ld) * cm_pow(smp1 / IX(f->sucsat, c, nlevsoi, ld), -1.0 / IX(f->bsw, c, nlevsoi, ld));
+          v = jl_min(v, 0.5 * (IX(f->watsat, c, nlevsoi, ld) + IX(f->h2osoi_vol, c, nlevsoi, ld)));
+          break;
+        }
+      }
+      vwc_zwt[c] = v;
+    }
+  }
+  /* _soilwm_voleq_zq_kernel! (:171-205) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    for (int j = 1; j <= nlevsoi; j++) {
+      double zm1 = SC(M[ZIMM], c, j), zj = SC(M[ZIMM], c, j + 1);
+      double ws = IX(f->watsat, c, j, ld), suc = IX(f->sucsat, c, j, ld), bb = IX(f->bsw, c, j, ld);
+      double zwt = zwtmm[c], onem1b = 1.0 - 1.0 / bb, v;
+      if (zwt <= zm1) {
+        SC(M[VOLEQ], c, j) = ws;
+      } else if (zwt < zj && zwt > zm1) {
+        double temp0 = cm_pow((suc + zwt - zm1) / suc, onem1b);
+        double voleq1 = -suc * ws / onem1b / (zwt - zm1) * (1.0 - temp0);
+        v = (voleq1 * (zwt - zm1) + ws * (zj - zwt)) / (zj - zm1);
+        v = jl_min(ws, v);
+        SC(M[VOLEQ], c, j) = jl_max(v, 0.0);
+      } else {
+        double tempi = cm_pow((suc + zwt - zj) / suc, onem1b);
+        double temp0 = cm_pow((suc + zwt - zm1) / suc, onem1b);
+        v = -suc * ws / onem1b / (zj - zm1) * (tempi - temp0);
+        v = jl_max(v, 0.0);
+        SC(M[VOLEQ], c, j) = jl_min(ws, v);
+      }
+      double zqv = -suc * cm_pow(jl_max(SC(M[VOLEQ], c, j) / ws, 0.01), -bb);
+      SC(M[ZQ], c, j) = jl_max(f->smpmin[c], zqv);
+    }
+  }
+  /* _soilwm_voleq_zq_aqu_kernel! (:346-366) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c] || jwt[c] != nlevsoi) continue;
+    int j = nlevsoi;
+    double suc = IX(f->sucsat, c, j, ld), ws = IX(f->watsat, c, j, ld), bb = IX(f->bsw, c, j, ld);
+    double zwt = zwtmm[c], zj = SC(M[ZIMM], c, j + 1), onem1b = 1.0 - 1.0 / bb;
+    double temp0 = cm_pow((suc + zwt - zj) / suc, onem1b);
+    double v = -suc * ws / onem1b / (zwt - zj) * (1.0 - temp0);
+    v = jl_max(v, 0.0);
+    v = jl_min(ws, v);
+    SC(M[VOLEQ], c, j + 1) = v;
+    double zqv = -suc * cm_pow(jl_max(v / ws, 0.01), -bb);
+    SC(M[ZQ], c, j + 1) = jl_max(f->smpmin[c], zqv);
+  }
+  /* _soilwm_hk_smp_kernel! (:223-270) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    for (int j = 1; j <= nlevsoi; j++) {
+      int jp1 = j + 1 < nlevsoi ? j + 1 : nlevsoi;
+      double bb = IX(f->bsw, c, j, ld);
+      double s1 = 0.5 * (SC(M[VWC], c, j) + SC(M[VWC], c, jp1)) / (0.5 * (IX(f->watsat, c, j, ld) + IX(f->watsat, c, jp1, ld)));
+      s1 = jl_min(1.0, s1);
+      double s2 = IX(f->hksat, c, j, ld) * cm_pow(s1, 2.0 * bb + 2.0);
+      double imp = cm_pow(10.0, -e_ice * (0.5 * (SC(M[ICEF], c, j) + SC(M[ICEF], c, jp1))));
+      SC(M[IMPED], c, j) = imp;
+      SC(M[HK], c, j) = imp * s1 * s2;
+      SC(M[DHKDW], c, j) = imp * (2.0 * bb + 3.0) * s2 * (1.0 / (IX(f->watsat, c, j, ld) + IX(f->watsat, c, jp1, ld)));
+      double s_node = jl_max(SC(M[VWC], c, j) / IX(f->watsat, c, j, ld), 0.01);
+      s_node = jl_min(1.0, s_node);
+      double smpv = -IX(f->sucsat, c, j, ld) * cm_pow(s_node, -bb);
+      smpv = jl_max(f->smpmin[c], smpv);
+      SC(M[SMP], c, j) = smpv;
+      SC(M[DSMPDW], c, j) = -bb * smpv / SC(M[VWC], c, j);
+      IX(f->smp_l, c, j, ld) = smpv;
+      IX(f->hk_l, c, j, ld) = SC(M[HK], c, j);
+    }
+  }
+  /* _soilwm_aqu_zmm_kernel! (:385-397) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    SC(M[ZMM], c, nlevsoi + 1) = 0.5 * (1.0e3 * f->zwt[c] + SC(M[ZMM], c, nlevsoi));
+    if (jwt[c] < nlevsoi) SC(M[DZMM], c, nlevsoi + 1) = SC(M[DZMM], c, nlevsoi);
+    else SC(M[DZMM], c, nlevsoi + 1) = 1.0e3 * f->zwt[c] - SC(M[ZMM], c, nlevsoi);
+  }
+  /* _soilwm_tridiag_assemble_kernel! (:430-539) */
+#define A_(k, j) SC(M[k], c, j)
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    double den, dzq, num;
+    int j = 1;
+    A_(QIN, j) = f->qflx_infl[c];
+    den = A_(ZMM, j + 1) - A_(ZMM, j);
+    dzq = A_(ZQ, j + 1) - A_(ZQ, j);
+    num = (A_(SMP, j + 1) - A_(SMP, j)) - dzq;
+    A_(QOUT, j) = -A_(HK, j) * num / den;
+    A_(DQODW1, j) = -(-A_(HK, j) * A_(DSMPDW, j) + num * A_(DHKDW, j)) / den;
+    A_(DQODW2, j) = -(A_(HK, j) * A_(DSMPDW, j + 1) + num * A_(DHKDW, j)) / den;
+    A_(RMX, j) = A_(QIN, j) - A_(QOUT, j) - IX(f->qflx_rootsoi, c, j, ld);
+    A_(AMX, j) = 0.0;
+    A_(BMX, j) = A_(DZMM, j) * (sdamp + 1.0 / dtime) + A_(DQODW1, j);
+    A_(CMX, j) = A_(DQODW2, j);
+    for (j = 2; j <= nlevsoi - 1; j++) {
+      den = A_(ZMM, j) - A_(ZMM, j - 1);
+      dzq = A_(ZQ, j) - A_(ZQ, j - 1);
+      num = (A_(SMP, j) - A_(SMP, j - 1)) - dzq;
+      A_(QIN, j) = -A_(HK, j - 1) * num / den;
+      A_(DQIDW0, j) = -(-A_(HK, j - 1) * A_(DSMPDW, j - 1) + num * A_(DHKDW, j - 1)) / den;
+      A_(DQIDW1, j) = -(A_(HK, j - 1) * A_(DSMPDW, j) + num * A_(DHKDW, j - 1)) / den;
+      den = A_(ZMM, j + 1) - A_(ZMM, j);
+      dzq = A_(ZQ, j + 1) - A_(ZQ, j);
+      num = (A_(SMP, j + 1) - A_(SMP, j)) - dzq;
+      A_(QOUT, j) = -A_(HK, j) * num / den;
+      A_(DQODW1, j) = -(-A_(HK, j) * A_(DSMPDW, j) + num * A_(DHKDW, j)) / den;
+      A_(DQODW2, j) = -(A_(HK, j) * A_(DSMPDW, j + 1) + num * A_(DHKDW, j)) / den;
+      A_(RMX, j) = A_(QIN, j) - A_(QOUT, j) - IX(f->qflx_rootsoi, c, j, ld);
+      A_(AMX, j) = -A_(DQIDW0, j);
+      A_(BMX, j) = A_(DZMM, j) / dtime - A_(DQIDW1, j) + A_(DQODW1, j);
+      A_(CMX, j) = A_(DQODW2, j);
+    }
+    j = nlevsoi;
+    if (j > jwt[c]) {
+      den = A_(ZMM, j) - A_(ZMM, j - 1);
+      dzq = A_(ZQ, j) - A_(ZQ, j - 1);
+      num = (A_(SMP, j) - A_(SMP, j - 1)) - dzq;
+      A_(QIN, j) = -A_(HK, j - 1) * num / den;
+      A_(DQIDW0, j) = -(-A_(HK, j - 1) * A_(DSMPDW, j - 1) + num * A_(DHKDW, j - 1)) / den;
+      A_(DQIDW1, j) = -(A_(HK, j - 1) * A_(DSMPDW, j) + num * A_(DHKDW, j - 1)) / den;
+      A_(QOUT, j) = 0.0;
+      A_(DQODW1, j) = 0.0;
+      A_(RMX, j) = A_(QIN, j) - A_(QOUT, j) - IX(f->qflx_rootsoi, c, j, ld);
+      A_(AMX, j) = -A_(DQIDW0, j);
+      A_(BMX, j) = A_(DZMM, j) / dtime - A_(DQIDW1, j) + A_(DQODW1, j);
+      A_(CMX, j) = 0.0;
+      A_(RMX, j + 1) = 0.0;
+      A_(AMX, j + 1) = 0.0;
+      A_(BMX, j + 1) = A_(DZMM, j + 1) / dtime;
+      A_(CMX, j + 1) = 0.0;
+    } else {
+      double ws = IX(f->watsat, c, j, ld);
+      double s_node = jl_max(0.5 * ((vwc_zwt[c] + A_(VWC, j)) / ws), 0.01);
+      s_node = jl_min(1.0, s_node);
+      double smp1 = -IX(f->sucsat, c, j, ld) * cm_pow(s_node, -IX(f->bsw, c, j, ld));
+      smp1 = jl_max(f->smpmin[c], smp1);
+      double dsmpdw1 = -IX(f->bsw, c, j, ld) * smp1 / (s_node * ws);
+      den = A_(ZMM, j) - A_(ZMM, j - 1);
+      dzq = A_(ZQ, j) - A_(ZQ, j - 1);
+      num = (A_(SMP, j) - A_(SMP, j - 1)) - dzq;
+      A_(QIN, j) = -A_(HK, j - 1) * num / den;
+      A_(DQIDW0, j) = -(-A_(HK, j - 1) * A_(DSMPDW, j - 1) + num * A_(DHKDW, j - 1)) / den;
+      A_(DQIDW1, j) = -(A_(HK, j - 1) * A_(DSMPDW, j) + num * A_(DHKDW, j - 1)) / den;
+      den = A_(ZMM, j + 1) - A_(ZMM, j);
+      dzq = A_(ZQ, j + 1) - A_(ZQ, j);
+      num = (smp1 - A_(SMP, j)) - dzq;
+      A_(QOUT, j) = -A_(HK, j) * num / den;
+      A_(DQODW1, j) = -(-A_(HK, j) * A_(DSMPDW, j) + num * A_(DHKDW, j)) / den;
+      A_(DQODW2, j) = -(A_(HK, j) * dsmpdw1 + num * A_(DHKDW, j)) / den;
+      A_(RMX, j) = A_(QIN, j) - A_(QOUT, j) - IX(f->qflx_rootsoi, c, j, ld);
+      A_(AMX, j) = -A_(DQIDW0, j);
+      A_(BMX, j) = A_(DZMM, j) / dtime - A_(DQIDW1, j) + A_(DQODW1, j);
+      A_(CMX, j) = A_(DQODW2, j);
+      A_(QIN, j + 1) = A_(QOUT, j);
+      A_(DQIDW0, j + 1) = -(-A_(HK, j) * A_(DSMPDW, j) + num * A_(DHKDW, j)) / den;
+      A_(DQIDW1, j + 1) = -(A_(HK, j) * dsmpdw1 + num * A_(DHKDW, j)) / den;
+      A_(QOUT, j + 1) = 0.0;
+      A_(DQODW1, j + 1) = 0.0;
+      A_(RMX, j + 1) = A_(QIN, j + 1) - A_(QOUT, j + 1);
+      A_(AMX, j + 1) = -A_(DQIDW0, j + 1);
+      A_(BMX, j + 1) = A_(DZMM, j + 1) / dtime - A_(DQIDW1, j + 1) + A_(DQODW1, j + 1);
+      A_(CMX, j + 1) = 0.0;
+    }
+  }
+  /* tridiagonal_multi! (tridiagonal.jl:86-127), jtop = 1, nlevs = nlevsoi + 1 */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    int n = nlevsoi + 1;
+    double bet = A_(BMX, 1);
+    if (fabs(bet) < 1.0e-30) bet = 1.0e-30;
+    double cp_prev = A_(CMX, 1) / bet, dp_prev = A_(RMX, 1) / bet;
+    A_(CP, 1) = cp_prev;
+    A_(DWAT2, 1) = dp_prev;
+    for (int jj = 2; jj <= n; jj++) {
+      double denom = A_(BMX, jj) - A_(AMX, jj) * cp_prev;
+      if (fabs(denom) < 1.0e-30) denom = copysign(1.0e-30, denom == 0.0 ? 1.0 : denom);
+      cp_prev = A_(CMX, jj) / denom;
+      dp_prev = (A_(RMX, jj) - A_(AMX, jj) * dp_prev) / denom;
+      A_(CP, jj) = cp_prev;
+      A_(DWAT2, jj) = dp_prev;
+    }
+    double u_next = dp_prev;
+    A_(DWAT2, n) = u_next;
+    for (int jj = n - 1; jj >= 1; jj--) {
+      u_next = A_(DWAT2, jj) - A_(CP, jj) * u_next;
+      A_(DWAT2, jj) = u_next;
+    }
+  }
+  /* _soilwm_renew_qcharge_kernel! (:561-605) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    for (int j = 1; j <= nlevsoi; j++)
+      IX(f->h2osoi_liq, c, joff + j, ld) = IX(f->h2osoi_liq, c, joff + j, ld) + A_(DWAT2, j) * A_(DZMM, j);
+    int jw = jwt[c];
+    if (jw < nlevsoi) {
+      double wh_zwt = 0.0;
+      double s_node = jl_max(IX(f->h2osoi_vol, c, jw + 1, ld) / IX(f->watsat, c, jw + 1, ld), 0.01);
+      double s1 = jl_min(1.0, s_node);
+      double ka = A_(IMPED, jw + 1) * IX(f->hksat, c, jw + 1, ld) * cm_pow(s1, 2.0 * IX(f->bsw, c, jw + 1, ld) + 3.0);
+      int jm = jw > 1 ? jw : 1;
+      double smp1 = jl_max(f->smpmin[c], A_(SMP, jm));
+      double wh = smp1 - A_(ZQ, jm);
+      if (jw == 0) f->qcharge[c] = -ka * (wh_zwt - wh) / ((f->zwt[c] + 1.0e-3) * 1000.0);
+      else f->qcharge[c] = -ka * (wh_zwt - wh) / ((f->zwt[c] - IX(f->z, c, joff + jw, ld)) * 1000.0 * 2.0);
+      f->qcharge[c] = jl_max(-10.0 / dtime, f->qcharge[c]);
+      f->qcharge[c] = jl_min(10.0 / dtime, f->qcharge[c]);
+    } else {
+      f->qcharge[c] = A_(DWAT2, nlevsoi + 1) * A_(DZMM, nlevsoi + 1) / dtime;
+    }
+  }
+#undef A_
+  /* _soilwm_deficit_kernel! (:621-635) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    double acc = 0.0;
+    for (int j = 1; j <= nlevsoi; j++) {
+      double l = IX(f->h2osoi_liq, c, joff + j, ld);
+      acc = acc + (l >= 0.0 ? 0.0 : -l);
+    }
+    f->qflx_deficit[c] = acc;
+  }
+  for (int k = 0; k < NMAT; k++) free(M[k]);
+  free(zwtmm);
+  free(vwc_zwt);
+  free(jwt);
+  return 0;
+}
+#undef SC
 
 /* ===================================================================== */
 /* compute_effec_rootfrac_and_vert_tran_sink! (soil_water_plant_sink.jl)  */

@@ -35,6 +35,7 @@ def lib():
         L.orc_soil_temperature.argtypes = [P, P, P, C.c_double, C.c_int32, P, C.c_int32]
         L.orc_soil_water_fractions.argtypes = [P, P, P, C.c_int32]
         L.orc_rootsink.argtypes = [P, P, P, C.c_int32]
+        L.orc_soil_water_zd09.argtypes = [P, P, P, C.c_double, C.c_double]
         L.orc_soil_water.argtypes = [P, P, P, P, C.c_double, P, P, P, C.c_int32]
         L.orc_run_steps.argtypes = [P, P, P, P, P, C.c_double, C.c_int32, C.c_int32, P, P,
                                     C.c_int64, P, P, P, C.c_int32]
@@ -91,6 +92,12 @@ def rootsink(rs, use_hydrstress=False):
     if rc < 0:
         _chk(rc)
     return rc
+
+
+def soil_water_zd09(zs, dtime, e_ice=6.0):
+    """soilwater_zengdecker2009! in place on a host Zd09State."""
+    _chk(lib().orc_soil_water_zd09(C.byref(zs.vp), C.byref(zs.bounds()), C.byref(zs.fields()), float(e_ice),
+                                   float(dtime)))
 
 
 def soil_water(st, dtime, cfg=None, capture=False, nthreads=None):
