@@ -237,6 +237,88 @@ ROOTSINK_FIELDS = [
     ("qflx_phs_neg_col", _f64, "c", None),
     ("qflx_hydr_redist_patch", _f64, "p", None),
 ]
+# clmgb_soilflux_fields (soil_fluxes!), header order
+SOILFLUX_FIELDS = [
+    ("mask_nolakec", _u8, "c", None),
+    ("mask_nolakep", _u8, "p", None),
+    ("mask_urbanp", _u8, "p", None),
+    ("col_snl", _i64, "c", None),
+    ("col_itype", _i64, "c", None),
+    ("col_patchi", _i64, "c", None),
+    ("col_patchf", _i64, "c", None),
+    ("lun_itype", _i64, "l", None),
+    ("lun_urbpoi", _u8, "l", None),
+    ("patch_column", _i64, "p", None),
+    ("patch_landunit", _i64, "p", None),
+    ("patch_wtcol", _f64, "p", None),
+    ("frac_veg_nosno", _i64, "p", None),
+    ("frac_sno_eff", _f64, "c", None),
+    ("frac_h2osfc", _f64, "c", None),
+    ("t_ssbef", _f64, "c", "L"),
+    ("t_h2osfc_bef", _f64, "c", None),
+    ("t_grnd", _f64, "c", None),
+    ("t_h2osfc", _f64, "c", None),
+    ("emg", _f64, "c", None),
+    ("t_soisno", _f64, "c", "L"),
+    ("fact", _f64, "c", "L"),
+    ("h2osoi_liq", _f64, "c", "L"),
+    ("h2osoi_ice", _f64, "c", "L"),
+    ("htvp", _f64, "c", None),
+    ("xmf", _f64, "c", None),
+    ("xmf_h2osfc", _f64, "c", None),
+    ("c_h2osfc", _f64, "c", None),
+    ("eflx_h2osfc_to_snow", _f64, "c", None),
+    ("eflx_building_heat_errsoi", _f64, "c", None),
+    ("forc_lwrad", _f64, "c", None),
+    ("errsoi_col", _f64, "c", None),
+    ("cgrnds", _f64, "p", None),
+    ("cgrndl", _f64, "p", None),
+    ("sabg", _f64, "p", None),
+    ("sabg_soil", _f64, "p", None),
+    ("sabg_snow", _f64, "p", None),
+    ("dlrad", _f64, "p", None),
+    ("ulrad", _f64, "p", None),
+    ("eflx_sh_veg", _f64, "p", None),
+    ("eflx_sh_stem", _f64, "p", None),
+    ("eflx_wasteheat", _f64, "p", None),
+    ("eflx_heat_from_ac", _f64, "p", None),
+    ("eflx_traffic", _f64, "p", None),
+    ("eflx_ventilation", _f64, "p", None),
+    ("qflx_evap_veg", _f64, "p", None),
+    ("qflx_tran_veg", _f64, "p", None),
+    ("eflx_sh_grnd", _f64, "p", None),
+    ("qflx_evap_soi", _f64, "p", None),
+    ("qflx_ev_soil", _f64, "p", None),
+    ("qflx_ev_h2osfc", _f64, "p", None),
+    ("qflx_ev_snow", _f64, "p", None),
+    ("eflx_lwrad_net", _f64, "p", None),
+    ("eflx_lwrad_out", _f64, "p", None),
+    ("eflx_lwrad_net_u", _f64, "p", None),
+    ("eflx_sh_tot", _f64, "p", None),
+    ("eflx_sh_tot_r", _f64, "p", None),
+    ("eflx_sh_tot_u", _f64, "p", None),
+    ("eflx_lh_tot", _f64, "p", None),
+    ("eflx_lh_tot_r", _f64, "p", None),
+    ("eflx_lh_tot_u", _f64, "p", None),
+    ("eflx_lh_vege", _f64, "p", None),
+    ("eflx_lh_vegt", _f64, "p", None),
+    ("eflx_lh_grnd", _f64, "p", None),
+    ("eflx_soil_grnd", _f64, "p", None),
+    ("eflx_soil_grnd_r", _f64, "p", None),
+    ("eflx_soil_grnd_u", _f64, "p", None),
+    ("eflx_lwrad_net_r", _f64, "p", None),
+    ("eflx_lwrad_out_r", _f64, "p", None),
+    ("eflx_lwrad_out_u", _f64, "p", None),
+    ("errsoi_patch", _f64, "p", None),
+    ("t_skin", _f64, "p", None),
+    ("qflx_evap_tot", _f64, "p", None),
+    ("qflx_evap_can", _f64, "p", None),
+    ("qflx_liqevap_from_top_layer", _f64, "p", None),
+    ("qflx_solidevap_from_top_layer", _f64, "p", None),
+    ("qflx_soliddew_to_top_layer", _f64, "p", None),
+    ("qflx_liqdew_to_top_layer", _f64, "p", None),
+]
+
 # clmgb_zd09_fields (soilwater_zengdecker2009!), header order
 ZD09_FIELDS = [
     ("mask_hydrology", _u8, "c", None),
@@ -290,6 +372,7 @@ StepAdjoint = type("StepAdjoint", (C.Structure,),
 SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
 RootSinkFields = _mk_struct("RootSinkFields", ROOTSINK_FIELDS)
 Zd09Fields = _mk_struct("Zd09Fields", ZD09_FIELDS)
+SoilFluxFields = _mk_struct("SoilFluxFields", SOILFLUX_FIELDS)
 
 
 class SubstepLog(C.Structure):

@@ -9,63 +9,19 @@ import ctypes as C
 import numpy as np
 
 from . import abi, api
+from .fieldset import FieldSet
 
 ISTSOIL, ISTCROP, ISTURB_MD = 1, 2, 9
 ICOL_ROAD_PERV = 75
-_NP = {"u8": np.uint8, "i64": np.int64, "f64": np.float64}
 
 
-class RootSinkState:
+class RootSinkState(FieldSet):
     """Arrays of clmgb_rootsink_fields for nc columns, npch patches, nl landunits."""
-
-    def __init__(self, vp, nc, npch, nl, arrays=None):
-        self.vp, self.nc, self.np, self.nl = vp, int(nc), int(npch), int(nl)
-        if arrays is None:
-            arrays = {}
-            for (n, t, kind, dims) in abi.ROOTSINK_FIELDS:
-                m = {"c": self.nc, "p": self.np, "l": self.nl}[kind]
-                shape = (m,) if dims is None else (abi.level_count(dims, vp), m)
-                arrays[n] = np.zeros(shape, dtype=_NP[t])
-        self.arrays = arrays
-
-    def __getitem__(self, k):
-        return self.arrays[k]
-
-    def __setitem__(self, k, v):
-        self.arrays[k] = v
-
-    def bounds(self):
-        return abi.Bounds(self.nc, self.np, self.nl, self.nc, self.np)
-
-    def to_device(self, device="cuda"):
-        import torch
-        arrs = {k: torch.from_numpy(np.ascontiguousarray(v)).to(device) for k, v in self.arrays.items()}
-        return RootSinkState(self.vp, self.nc, self.np, self.nl, arrs)
-
-    def to_host(self):
-        arrs = {k: (v if isinstance(v, np.ndarray) else v.detach().cpu().numpy()).copy()
-                for k, v in self.arrays.items()}
-        return RootSinkState(self.vp, self.nc, self.np, self.nl, arrs)
-
-    def copy(self):
-        arrs = {k: (v.copy() if isinstance(v, np.ndarray) else v.clone()) for k, v in self.arrays.items()}
-        return RootSinkState(self.vp, self.nc, self.np, self.nl, arrs)
+    SPEC = abi.ROOTSINK_FIELDS
+    STRUCT = abi.RootSinkFields
 
     def fields(self, with_hydrstress=True):
-        s = abi.RootSinkFields()
-        s.struct_size = C.sizeof(abi.RootSinkFields)
-        for (n, t, _, _) in abi.ROOTSINK_FIELDS:
-            if not with_hydrstress and n in abi.HYDRSTRESS_ONLY:
-                continue
-            a = self.arrays[n]
-            if isinstance(a, np.ndarray):
-                assert a.flags.c_contiguous, n
-                p = a.ctypes.data_as(abi._CT[t])
-            else:
-                assert a.is_contiguous(), n
-                p = C.cast(C.c_void_p(a.data_ptr()), abi._CT[t])
-            setattr(s, n, p)
-        return s
+        return super().fields(skip=() if with_hydrstress else abi.HYDRSTRESS_ONLY)
 
 
 def effec_rootfrac_vert_tran_sink(handle, rs, use_hydrstress=False, col_status=None, stream=None):

@@ -258,6 +258,19 @@ int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilflux_fields* f, double dtime,
+                          void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, false);
+  if (e) return e;
+  if (b->nc == 0 && b->np == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  cudaError_t ce = clmgb::launch_soil_fluxes(make_dims(h->vp, *b), b->nc, b->nl, *f, dtime, h->dev_status,
+                                             (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 int32_t clmgb_soil_water_zd09(clmgb_handle h, const clmgb_bounds* b, const clmgb_zd09_fields* f,
                               const clmgb_swm_config* cfg, double dtime, void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;

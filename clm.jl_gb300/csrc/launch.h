@@ -109,6 +109,8 @@ cudaError_t launch_rootsink(const Dims& D, int64_t nc, int64_t nl, const clmgb_r
                             uint32_t* col_status, uint32_t* dev_status, cudaStream_t s);
 cudaError_t launch_zd09(const Dims& D, int64_t nc, const clmgb_zd09_fields& f, double e_ice, double dtime,
                         cudaStream_t s);
+cudaError_t launch_soil_fluxes(const Dims& D, int64_t nc, int64_t nl, const clmgb_soilflux_fields& f, double dtime,
+                               uint32_t* dev_status, cudaStream_t s);
 int vjp_cf_blocks_per_sm();
 cudaError_t launch_column_step_vjp_cf(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
                                       const clmgb_soilwater_fields& fw, const clmgb_swm_config& cfg, double dtime,

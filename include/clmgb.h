@@ -297,6 +297,91 @@ typedef struct clmgb_zd09_fields {
   double* qflx_deficit;              /* [nc]  W */
 } clmgb_zd09_fields;
 
+/* soil_fluxes! (soil_fluxes.jl:553-697): the surface fluxes corrected to the new ground
+ * temperature, the evaporation partition, totals, outgoing longwave and the soil
+ * energy balance error.  [np] patch vectors, [nc] column vectors, [nl] landunits. */
+typedef struct clmgb_soilflux_fields {
+  int64_t struct_size;               /* sizeof(clmgb_soilflux_fields) */
+  const uint8_t* mask_nolakec;       /* [nc] */
+  const uint8_t* mask_nolakep;       /* [np] */
+  const uint8_t* mask_urbanp;        /* [np] */
+  const int64_t* col_snl;            /* [nc] */
+  const int64_t* col_itype;          /* [nc] */
+  const int64_t* col_patchi;         /* [nc]  1-based */
+  const int64_t* col_patchf;         /* [nc]  1-based */
+  const int64_t* lun_itype;          /* [nl] */
+  const uint8_t* lun_urbpoi;         /* [nl] */
+  const int64_t* patch_column;       /* [np]  1-based */
+  const int64_t* patch_landunit;     /* [np]  1-based */
+  const double* patch_wtcol;         /* [np] */
+  const int64_t* frac_veg_nosno;     /* [np] */
+  const double* frac_sno_eff;        /* [nc] */
+  const double* frac_h2osfc;         /* [nc] */
+  const double* t_ssbef;             /* [ldc, L] */
+  const double* t_h2osfc_bef;        /* [nc] */
+  const double* t_grnd;              /* [nc] */
+  const double* t_h2osfc;            /* [nc] */
+  const double* emg;                 /* [nc] */
+  const double* t_soisno;            /* [ldc, L] */
+  const double* fact;                /* [ldc, L] */
+  const double* h2osoi_liq;          /* [ldc, L] */
+  const double* h2osoi_ice;          /* [ldc, L] */
+  const double* htvp;                /* [nc] */
+  const double* xmf;                 /* [nc] */
+  const double* xmf_h2osfc;          /* [nc] */
+  const double* c_h2osfc;            /* [nc] */
+  const double* eflx_h2osfc_to_snow; /* [nc] */
+  const double* eflx_building_heat_errsoi; /* [nc] */
+  const double* forc_lwrad;          /* [nc] */
+  double* errsoi_col;                /* [nc]  W */
+  const double* cgrnds;              /* [np] */
+  const double* cgrndl;              /* [np] */
+  const double* sabg;                /* [np] */
+  const double* sabg_soil;           /* [np] */
+  const double* sabg_snow;           /* [np] */
+  const double* dlrad;               /* [np] */
+  const double* ulrad;               /* [np] */
+  const double* eflx_sh_veg;         /* [np] */
+  const double* eflx_sh_stem;        /* [np] */
+  const double* eflx_wasteheat;      /* [np] */
+  const double* eflx_heat_from_ac;   /* [np] */
+  const double* eflx_traffic;        /* [np] */
+  const double* eflx_ventilation;    /* [np] */
+  const double* qflx_evap_veg;       /* [np] */
+  const double* qflx_tran_veg;       /* [np] */
+  double* eflx_sh_grnd;              /* [np]  RW */
+  double* qflx_evap_soi;             /* [np]  RW */
+  double* qflx_ev_soil;              /* [np]  RW */
+  double* qflx_ev_h2osfc;            /* [np]  RW */
+  double* qflx_ev_snow;              /* [np]  RW */
+  double* eflx_lwrad_net;            /* [np]  RW (read by urban patches) */
+  double* eflx_lwrad_out;            /* [np]  RW */
+  double* eflx_lwrad_net_u;          /* [np]  RW */
+  double* eflx_sh_tot;               /* [np]  W */
+  double* eflx_sh_tot_r;             /* [np]  W */
+  double* eflx_sh_tot_u;             /* [np]  W */
+  double* eflx_lh_tot;               /* [np]  W */
+  double* eflx_lh_tot_r;             /* [np]  W */
+  double* eflx_lh_tot_u;             /* [np]  W */
+  double* eflx_lh_vege;              /* [np]  W */
+  double* eflx_lh_vegt;              /* [np]  W */
+  double* eflx_lh_grnd;              /* [np]  W */
+  double* eflx_soil_grnd;            /* [np]  W */
+  double* eflx_soil_grnd_r;          /* [np]  W */
+  double* eflx_soil_grnd_u;          /* [np]  W */
+  double* eflx_lwrad_net_r;          /* [np]  W */
+  double* eflx_lwrad_out_r;          /* [np]  W */
+  double* eflx_lwrad_out_u;          /* [np]  W */
+  double* errsoi_patch;              /* [np]  W */
+  double* t_skin;                    /* [np]  W */
+  double* qflx_evap_tot;             /* [np]  W */
+  double* qflx_evap_can;             /* [np]  W */
+  double* qflx_liqevap_from_top_layer;   /* [np]  W */
+  double* qflx_solidevap_from_top_layer; /* [np]  W */
+  double* qflx_soliddew_to_top_layer;    /* [np]  W */
+  double* qflx_liqdew_to_top_layer;      /* [np]  W */
+} clmgb_soilflux_fields;
+
 typedef struct clmgb_handle_s* clmgb_handle;
 
 /* ---- library / handle ---- */
@@ -379,6 +464,13 @@ int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b,
 int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b,
                          const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
                          double dtime, uint32_t* col_status, void* stream);
+
+/* soil_fluxes! (soil_fluxes.jl:553-697) in its loop order: the ground temperature
+ * change tinc (per column), the flux correction, evaporation partition and limit,
+ * totals, errsoi and outgoing longwave (per patch), then errsoi_col as the wtcol-weighted
+ * patch sum in ascending patch order (the reference's p2c), and urban t_skin. */
+int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilflux_fields* f, double dtime,
+                          void* stream);
 
 /* soil_water! with the Zeng-Decker 2009 method (soilwater_zengdecker2009!,
  * soil_water_movement.jl:1616-1764): equilibrium matric potential from the water

@@ -21,6 +21,7 @@
  *     _phase_change_beta_kernel! :1929-2230    _tgrnd_kernel!             :224-247
  *     _eflx_fgr_kernel!          :250-269
  *   _soilhyd_water_fractions_kernel!  src/biogeophys/soil_hydrology.jl:110-130
+ *   soil_fluxes!                      src/biogeophys/soil_fluxes.jl:19-697
  *   soilwater_zengdecker2009!         src/biogeophys/soil_water_movement.jl:97-635,1616-1764
  *   compute_effec_rootfrac_and_vert_tran_sink!  src/biogeophys/soil_water_plant_sink.jl:48-78,
  *                                     :210-245, :341-451
@@ -1171,6 +1172,214 @@ int orc_soil_water_fractions(const clmgb_varpar* vp, const clmgb_bounds* b,
 #pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
 #endif
   for (int64_t c = 0; c < b->nc; c++) fractions_col(vp, b, f, c);
+  return 0;
+}
+
+/* ===================================================================== */
+/* soil_fluxes! (soil_fluxes.jl:553-697), loop by loop                    */
+/* ===================================================================== */
+int orc_soil_fluxes(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_soilflux_fields* f, double dtime)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  const int64_t nc = b->nc, np = b->np, ld = b->ldc;
+  const int nlevsno = vp->nlevsno;
+  const double hvap = 2.501e6, sb = 5.67e-8;
+  double* tinc = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+  double* t_grnd0 = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+  double* lwrad_del = (double*)calloc((size_t)(np > 0 ? np : 1), sizeof(double));
+  /* _soilflux_tinc_kernel! (:19-41) */
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_nolakec[c]) continue;
+    int64_t snl = f->col_snl[c];
+    if (snl < 0)
+      t_grnd0[c] = f->frac_sno_eff[c] * IX(f->t_ssbef, c, snl + 1 + nlevsno, ld) +
+                   (1.0 - f->frac_sno_eff[c] - f->frac_h2osfc[c]) * IX(f->t_ssbef, c, 1 + nlevsno, ld) +
+                   f->frac_h2osfc[c] * f->t_h2osfc_bef[c];
+    else
+      t_grnd0[c] = (1.0 - f->frac_h2osfc[c]) * IX(f->t_ssbef, c, 1 + nlevsno, ld) + f->frac_h2osfc[c] * f->t_h2osfc_bef[c];
+    tinc[c] = f->t_grnd[c] - t_grnd0[c];
+  }
+  /* _soilflux_correct_kernel! (:51-76) */
+  for (int64_t p = 0; p < np; p++) {
+    if (!f->mask_nolakep[p]) continue;
+    int64_t c = f->patch_column[p] - 1, l = f->patch_landunit[p] - 1;
+    f->eflx_sh_grnd[p] += tinc[c] * f->cgrnds[p];
+    f->qflx_evap_soi[p] += tinc[c] * f->cgrndl[p];
+    if (f->lun_urbpoi[l]) {
+      f->qflx_ev_soil[p] = 0.0;
+      f->qflx_ev_h2osfc[p] = 0.0;
+      f->qflx_ev_snow[p] = f->qflx_evap_soi[p];
+    } else {
+      f->qflx_ev_snow[p] += tinc[c] * f->cgrndl[p];
+      f->qflx_ev_soil[p] += tinc[c] * f->cgrndl[p];
+      f->qflx_ev_h2osfc[p] += tinc[c] * f->cgrndl[p];
+    }
+  }
+  /* _soilflux_partition_kernel! (:181-240) */
+  for (int64_t p = 0; p < np; p++) {
+    if (!f->mask_nolakep[p]) continue;
+    int64_t c = f->patch_column[p] - 1, l = f->patch_landunit[p] - 1;
+    int64_t jj = f->col_snl[c] + 1 + nlevsno;
+    f->qflx_liqevap_from_top_layer[p] = 0.0;
+    f->qflx_solidevap_from_top_layer[p] = 0.0;
+    f->qflx_soliddew_to_top_layer[p] = 0.0;
+    f->qflx_liqdew_to_top_layer[p] = 0.0;
+    double liq = IX(f->h2osoi_liq, c, jj, ld), ice = IX(f->h2osoi_ice, c, jj, ld);
+    double ev = f->lun_urbpoi[l] ? f->qflx_evap_soi[p] : f->qflx_ev_snow[p];
+    if (ev >= 0.0) {
+      if ((liq + ice) > 0.0) f->qflx_liqevap_from_top_layer[p] = jl_max(ev * (liq / (liq + ice)), 0.0);
+      else f->qflx_liqevap_from_top_layer[p] = 0.0;
+      f->qflx_solidevap_from_top_layer[p] = ev - f->qflx_liqevap_from_top_layer[p];
+    } else {
+      if (f->t_grnd[c] < TFRZ) f->qflx_soliddew_to_top_layer[p] = fabs(ev);
+      else f->qflx_liqdew_to_top_layer[p] = fabs(ev);
+    }
+  }
+  /* _soilflux_evaplimit_kernel! (:242-300) */
+  for (int64_t p = 0; p < np; p++) {
+    if (!f->mask_nolakep[p]) continue;
+    int64_t c = f->patch_column[p] - 1, l = f->patch_landunit[p] - 1;
+    int64_t j = f->col_snl[c] + 1, jj = j + nlevsno;
+    double liq = IX(f->h2osoi_liq, c, jj, ld), ice = IX(f->h2osoi_ice, c, jj, ld);
+    double fse = f->frac_sno_eff[c];
+    if (j < 1) {
+      double lim = (ice + liq) / (fse * dtime);
+      if (f->qflx_ev_snow[p] > lim) {
+        double dem = f->qflx_ev_snow[p];
+        f->qflx_ev_snow[p] = lim;
+        f->qflx_evap_soi[p] -= fse * (dem - lim);
+        f->qflx_liqevap_from_top_layer[p] = jl_max(liq / (fse * dtime), 0.0);
+        f->qflx_solidevap_from_top_layer[p] = jl_max(ice / (fse * dtime), 0.0);
+        f->eflx_sh_grnd[p] += fse * (dem - lim) * f->htvp[c];
+      }
+    }
+    if (f->lun_urbpoi[l] && f->col_itype[c] != ICOL_ROAD_PERV && j == 1) {
+      double lim = (ice + liq) / dtime;
+      if (f->qflx_evap_soi[p] > lim) {
+        double dem = f->qflx_evap_soi[p];
+        f->qflx_evap_soi[p] = lim;
+        f->qflx_ev_snow[p] = f->qflx_evap_soi[p];
+        f->qflx_liqevap_from_top_layer[p] = jl_max(liq / dtime, 0.0);
+        f->qflx_solidevap_from_top_layer[p] = jl_max(ice / dtime, 0.0);
+        f->eflx_sh_grnd[p] += (dem - lim) * f->htvp[c];
+      }
+    }
+    if (j == 1 && f->frac_h2osfc[c] < 1.0) {
+      double lim = ice / (dtime * (1.0 - f->frac_h2osfc[c]));
+      if (f->qflx_solidevap_from_top_layer[p] >= lim) {
+        double dem = f->qflx_solidevap_from_top_layer[p];
+        f->qflx_solidevap_from_top_layer[p] = lim;
+        f->qflx_liqevap_from_top_layer[p] += (dem - lim);
+      }
+    }
+  }
+  /* _soilflux_totals_kernel! (:303-378) */
+  for (int64_t p = 0; p < np; p++) {
+    if (!f->mask_nolakep[p]) continue;
+    int64_t c = f->patch_column[p] - 1, l = f->patch_landunit[p] - 1;
+    int64_t lit = f->lun_itype[l];
+    double fse = f->frac_sno_eff[c], fh = f->frac_h2osfc[c], emg = f->emg[c], tg0 = t_grnd0[c];
+    if (!f->lun_urbpoi[l]) {
+      double lw = fse * jl_pow4(IX(f->t_ssbef, c, f->col_snl[c] + 1 + nlevsno, ld)) +
+                  (1.0 - fse - fh) * jl_pow4(IX(f->t_ssbef, c, 1 + nlevsno, ld)) + fh * jl_pow4(f->t_h2osfc_bef[c]);
+      f->eflx_soil_grnd[p] = ((1.0 - fse) * f->sabg_soil[p] + fse * f->sabg_snow[p]) + f->dlrad[p] +
+                             (1.0 - (double)f->frac_veg_nosno[p]) * emg * f->forc_lwrad[c] - emg * sb * lw -
+                             emg * sb * (tg0 * tg0 * tg0) * (4.0 * tinc[c]) -
+                             (f->eflx_sh_grnd[p] + f->qflx_evap_soi[p] * f->htvp[c]);
+      if (lit == ISTSOIL || lit == ISTCROP) f->eflx_soil_grnd_r[p] = f->eflx_soil_grnd[p];
+    } else {
+      lwrad_del[p] = 4.0 * emg * sb * (tg0 * tg0 * tg0) * tinc[c];
+      f->eflx_soil_grnd[p] = f->sabg[p] + f->dlrad[p] - f->eflx_lwrad_net[p] - lwrad_del[p] -
+                             (f->eflx_sh_grnd[p] + f->qflx_evap_soi[p] * f->htvp[c] + f->qflx_tran_veg[p] * hvap) +
+                             f->eflx_wasteheat[p] + f->eflx_heat_from_ac[p] + f->eflx_traffic[p] + f->eflx_ventilation[p];
+      f->eflx_soil_grnd_u[p] = f->eflx_soil_grnd[p];
+    }
+    f->eflx_sh_tot[p] = f->eflx_sh_veg[p] + f->eflx_sh_grnd[p];
+    if (!f->lun_urbpoi[l]) f->eflx_sh_tot[p] += f->eflx_sh_stem[p];
+    f->qflx_evap_tot[p] = f->qflx_evap_veg[p] + f->qflx_evap_soi[p];
+    f->eflx_lh_tot[p] = hvap * f->qflx_evap_veg[p] + f->htvp[c] * f->qflx_evap_soi[p];
+    if (lit == ISTSOIL || lit == ISTCROP) {
+      f->eflx_lh_tot_r[p] = f->eflx_lh_tot[p];
+      f->eflx_sh_tot_r[p] = f->eflx_sh_tot[p];
+    } else if (f->lun_urbpoi[l]) {
+      f->eflx_lh_tot_u[p] = f->eflx_lh_tot[p];
+      f->eflx_sh_tot_u[p] = f->eflx_sh_tot[p];
+    }
+    f->qflx_evap_can[p] = f->qflx_evap_veg[p] - f->qflx_tran_veg[p];
+    f->eflx_lh_vege[p] = (f->qflx_evap_veg[p] - f->qflx_tran_veg[p]) * hvap;
+    f->eflx_lh_vegt[p] = f->qflx_tran_veg[p] * hvap;
+    f->eflx_lh_grnd[p] = f->qflx_evap_soi[p] * f->htvp[c];
+  }
+  /* _soilflux_errsoi_base_kernel! (:380-407) */
+  for (int64_t p = 0; p < np; p++) {
+    if (!f->mask_nolakep[p]) continue;
+    int64_t c = f->patch_column[p] - 1;
+    f->errsoi_patch[p] = f->eflx_soil_grnd[p] - f->xmf[c] - f->xmf_h2osfc[c] -
+                         f->frac_h2osfc[c] * (f->t_h2osfc[c] - f->t_h2osfc_bef[c]) * (f->c_h2osfc[c] / dtime);
+    f->errsoi_patch[p] += f->eflx_h2osfc_to_snow[c];
+    if (col_is_wallroof(f->col_itype[c])) f->errsoi_patch[p] += f->eflx_building_heat_errsoi[c];
+  }
+  /* _soilflux_errsoi_layers_kernel! (:425-453): non-urban then urban */
+  for (int pass = 0; pass < 2; pass++) {
+    const uint8_t* mask = pass == 0 ? f->mask_nolakep : f->mask_urbanp;
+    int jmax = pass == 0 ? vp->nlevgrnd : vp->nlevurb;
+    for (int64_t p = 0; p < np; p++) {
+      if (!mask[p]) continue;
+      int64_t c = f->patch_column[p] - 1;
+      int wr = col_is_wallroof(f->col_itype[c]);
+      if ((pass == 1) != (wr != 0)) continue;
+      for (int jf = -nlevsno + 1; jf <= jmax; jf++) {
+        int jl = jf + nlevsno;
+        if (jf >= f->col_snl[c] + 1 && jf < 1)
+          f->errsoi_patch[p] -= f->frac_sno_eff[c] * (IX(f->t_soisno, c, jl, ld) - IX(f->t_ssbef, c, jl, ld)) / IX(f->fact, c, jl, ld);
+        if (jf >= 1)
+          f->errsoi_patch[p] -= (IX(f->t_soisno, c, jl, ld) - IX(f->t_ssbef, c, jl, ld)) / IX(f->fact, c, jl, ld);
+      }
+    }
+  }
+  /* _soilflux_lwrad_kernel! (:455-497) */
+  for (int64_t p = 0; p < np; p++) {
+    if (!f->mask_nolakep[p]) continue;
+    int64_t c = f->patch_column[p] - 1, l = f->patch_landunit[p] - 1;
+    int64_t lit = f->lun_itype[l];
+    double fse = f->frac_sno_eff[c], fh = f->frac_h2osfc[c], emg = f->emg[c], tg0 = t_grnd0[c];
+    double fvn = (double)f->frac_veg_nosno[p];
+    if (!f->lun_urbpoi[l]) {
+      double lw = fse * jl_pow4(IX(f->t_ssbef, c, f->col_snl[c] + 1 + nlevsno, ld)) +
+                  (1.0 - fse - fh) * jl_pow4(IX(f->t_ssbef, c, 1 + nlevsno, ld)) + fh * jl_pow4(f->t_h2osfc_bef[c]);
+      f->eflx_lwrad_out[p] = f->ulrad[p] + (1.0 - fvn) * (1.0 - emg) * f->forc_lwrad[c] + (1.0 - fvn) * emg * sb * lw +
+                             4.0 * emg * sb * (tg0 * tg0 * tg0) * tinc[c];
+      if (fvn == 0.0) f->t_skin[p] = sqrt(sqrt(lw));
+      f->eflx_lwrad_net[p] = f->eflx_lwrad_out[p] - f->forc_lwrad[c];
+      if (lit == ISTSOIL || lit == ISTCROP) {
+        f->eflx_lwrad_net_r[p] = f->eflx_lwrad_out[p] - f->forc_lwrad[c];
+        f->eflx_lwrad_out_r[p] = f->eflx_lwrad_out[p];
+      }
+    } else {
+      f->eflx_lwrad_out[p] += lwrad_del[p];
+      f->eflx_lwrad_net[p] += lwrad_del[p];
+      f->eflx_lwrad_net_u[p] += lwrad_del[p];
+      f->eflx_lwrad_out_u[p] = f->eflx_lwrad_out[p];
+    }
+  }
+  /* _soilflux_errsoi_zero_kernel! and _p2c_kernel! (:499-524), in patch order */
+  for (int64_t c = 0; c < nc; c++)
+    if (f->mask_nolakec[c]) f->errsoi_col[c] = 0.0;
+  for (int64_t p = 0; p < np; p++) {
+    int64_t c = f->patch_column[p] - 1;
+    if (c >= 0 && f->mask_nolakec[c] && f->col_patchi[c] <= p + 1 && p + 1 <= f->col_patchf[c])
+      f->errsoi_col[c] += f->errsoi_patch[p] * f->patch_wtcol[p];
+  }
+  /* _soilflux_urban_tskin_kernel! (:526-534) */
+  for (int64_t p = 0; p < np; p++) {
+    if (!f->mask_urbanp[p]) continue;
+    int64_t c = f->patch_column[p] - 1;
+    f->t_skin[p] = IX(f->t_soisno, c, f->col_snl[c] + 1 + nlevsno, ld);
+  }
+  free(tinc);
+  free(t_grnd0);
+  free(lwrad_del);
   return 0;
 }
 

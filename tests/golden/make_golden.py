@@ -40,6 +40,36 @@ def band_case(A, x, jtop, nlevs, kl, ku, tol, src):
                 jbot=jtop + n - 1, nlevs=nlevs, kl=kl, ku=ku, atol=tol, source=src)
 
 
+def soil_fluxes_cases():
+    """test/test_soil_fluxes.jl: one soil patch on one column, the inputs of its three
+    scenarios (level values are the same on every level) and the properties it checks."""
+    HVAP, HSUB = 2.501e6, 2.501e6 + 3.337e5
+    base = dict(snl=0, t_grnd=280.0, t_h2osfc=280.0, t_h2osfc_bef=279.5, emg=0.96, xmf=0.0, xmf_h2osfc=0.0,
+                c_h2osfc=4.188e6, t_skin=280.0, t_ssbef=279.5, t_soisno=280.0, fact=1.0e7, liq=20.0, ice=5.0,
+                frac_sno_eff=0.0, frac_h2osfc=0.0, cgrnds=10.0, cgrndl=0.001, htvp=HVAP, eflx_sh_grnd=50.0,
+                eflx_sh_veg=10.0, eflx_sh_stem=2.0, dlrad=300.0, ulrad=350.0, qflx_evap_soi=1.0e-5,
+                qflx_evap_veg=2.0e-5, qflx_tran_veg=1.0e-5, qflx_ev_snow=5.0e-6, qflx_ev_soil=5.0e-6,
+                qflx_ev_h2osfc=0.0, frac_veg_nosno=0, sabg_soil=100.0, sabg_snow=0.0, sabg=100.0,
+                forc_lwrad=300.0)
+    dew = dict(base, t_grnd=265.0, t_h2osfc=265.0, t_h2osfc_bef=265.0, t_skin=265.0, t_ssbef=265.0,
+               t_soisno=265.0, liq=10.0, ice=10.0, htvp=HSUB, eflx_sh_grnd=30.0, eflx_sh_veg=5.0,
+               eflx_sh_stem=1.0, dlrad=250.0, ulrad=280.0, qflx_evap_soi=-1.0e-5, qflx_evap_veg=0.0,
+               qflx_tran_veg=0.0, qflx_ev_snow=-1.0e-5, qflx_ev_soil=-1.0e-5, sabg_soil=50.0, sabg=50.0,
+               forc_lwrad=250.0)
+    snow = dict(base, snl=-3, t_grnd=270.0, t_h2osfc=270.0, t_h2osfc_bef=269.5, emg=0.97, t_skin=270.0,
+                t_ssbef=269.5, t_soisno=270.0, liq=5.0, ice=50.0, frac_sno_eff=0.8, cgrnds=8.0, cgrndl=0.0005,
+                htvp=HSUB, eflx_sh_grnd=20.0, eflx_sh_veg=3.0, eflx_sh_stem=0.5, dlrad=220.0, ulrad=240.0,
+                qflx_evap_soi=5.0e-6, qflx_evap_veg=0.0, qflx_tran_veg=0.0, qflx_ev_snow=5.0e-6,
+                qflx_ev_soil=0.0, sabg_soil=30.0, sabg_snow=80.0)
+    return dict(hvap=HVAP, dtime=1800.0, scenarios=[
+        dict(name="smoke", source="test/test_soil_fluxes.jl:3-210", inputs=base,
+             checks=["finite", "identities", "t_skin_range", "errsoi_col", "evap_partition"]),
+        dict(name="dew_below_freezing", source="test/test_soil_fluxes.jl:257-368", inputs=dew,
+             checks=["finite", "frost"]),
+        dict(name="snow_layers", source="test/test_soil_fluxes.jl:370-485", inputs=snow,
+             checks=["finite", "ev_snow_nonnegative"])])
+
+
 def rootsink_cases():
     """test/test_soil_water_plant_sink.jl: varpar nlevsno 5, nlevgrnd 10, nlevsoi 4 (:8-21);
     z[c, j + nlevsno] = 0.1 j (:57-61); the expected values are the test's own formulas."""
@@ -182,6 +212,7 @@ def main():
                                               dtime=1800.0, dhsdT=-1000.0,
                                               source="test/test_soil_temperature.jl:498-532")
     cases["rootsink"] = rootsink_cases()
+    cases["soil_fluxes"] = soil_fluxes_cases()
     with open(os.path.join(HERE, "reference_cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1, sort_keys=True)
 

@@ -33,7 +33,8 @@ def test_header_structs_match_ctypes():
     for sname, fields in (("clmgb_soiltemp_fields", abi.SOILTEMP_FIELDS),
                           ("clmgb_soilwater_fields", abi.SOILWATER_FIELDS),
                           ("clmgb_rootsink_fields", abi.ROOTSINK_FIELDS),
-                          ("clmgb_zd09_fields", abi.ZD09_FIELDS)):
+                          ("clmgb_zd09_fields", abi.ZD09_FIELDS),
+                          ("clmgb_soilflux_fields", abi.SOILFLUX_FIELDS)):
         members = abi.header_struct_members(txt, sname)
         assert members[0] == "struct_size"
         assert members[1:] == [f[0] for f in fields], sname
