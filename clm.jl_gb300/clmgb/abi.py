@@ -105,6 +105,32 @@ class SwmConfig(C.Structure):
         return cls(MOISTURE_FORM, BC_FLUX, BC_ZERO_FLUX, 1, 60.0, 1.0e-8, 1.0e-1, 1.0e-2, 6.0)
 
 
+# clmgb_surface_hydrology stages (CLMGB_SH_*), in the driver's order
+SH_FLOODC, SH_SAT_EXCESS, SH_QFLX_INPUTS, SH_INFL_EXCESS, SH_ROUTE = 1, 2, 4, 8, 16
+SH_UPDATE_H2OSFC, SH_INFILTRATION, SH_TOTAL_RUNOFF, SH_URBAN_PONDING = 32, 64, 128, 256
+SH_ALL = 511
+FSAT_TOPMODEL, FSAT_VIC = 1, 2
+QINMAX_NONE, QINMAX_HKSAT = 0, 1
+
+
+class SurfHydConfig(C.Structure):
+    """clmgb_surfhyd_config: the parameters, method flags and keyword arguments of the
+    surface-hydrology routines."""
+    _fields_ = [("struct_size", C.c_int64), ("ng", C.c_int64), ("fsat_method", C.c_int32),
+                ("crop_fsat_equals_zero", C.c_int32), ("hillslope_fsat_equals_zero", C.c_int32),
+                ("qinmax_method", C.c_int32), ("h2osfcflag", C.c_int32), ("update_h2osfcflag", C.c_int32),
+                ("fff", C.c_double), ("e_ice", C.c_double), ("pc", C.c_double), ("mu", C.c_double),
+                ("pondmx_urban", C.c_double)]
+
+    @classmethod
+    def default(cls, ng=1, fff=0.5):
+        """TOPModel fsat, hksat qinmax, h2osfcflag 1 (clm_initialize.jl:132-134), e_ice 6
+        (infilt_excess_runoff.jl:26), pc 0.4 and mu 0.13889 (surface_water.jl:20-21),
+        pondmx_urban 1 mm (varcon.jl:68); fff is read from the parameter file by the
+        reference (read_params.jl:23) and is the caller's."""
+        return cls(C.sizeof(cls), ng, FSAT_TOPMODEL, 0, 0, QINMAX_HKSAT, 1, 1, fff, 6.0, 0.4, 0.13889, 1.0)
+
+
 # (name, ctype, kind, dims) ; kind: 'c' column, 'p' patch, 'l' landunit
 # dims: None = vector, else level-kind string
 _u8, _i64, _f64 = "u8", "i64", "f64"
@@ -319,6 +345,62 @@ SOILFLUX_FIELDS = [
     ("qflx_liqdew_to_top_layer", _f64, "p", None),
 ]
 
+# clmgb_surfhyd_fields (the surface hydrology before soil_water!), header order;
+# kind 'g' = gridcell
+SURFHYD_FIELDS = [
+    ("mask_nolakec", _u8, "c", None),
+    ("mask_hydrology", _u8, "c", None),
+    ("mask_urban", _u8, "c", None),
+    ("col_snl", _i64, "c", None),
+    ("col_itype", _i64, "c", None),
+    ("col_landunit", _i64, "c", None),
+    ("col_gridcell", _i64, "c", None),
+    ("col_urbpoi", _u8, "c", None),
+    ("col_is_hillslope", _u8, "c", None),
+    ("col_active", _u8, "c", None),
+    ("col_cold", _i64, "c", None),
+    ("lun_itype", _i64, "l", None),
+    ("qflx_floodg", _f64, "g", None),
+    ("frost_table", _f64, "c", None),
+    ("zwt", _f64, "c", None),
+    ("zwt_perched", _f64, "c", None),
+    ("wtfact", _f64, "c", None),
+    ("b_infil", _f64, "c", None),
+    ("top_max_moist", _f64, "c", None),
+    ("top_moist_limited", _f64, "c", None),
+    ("icefrac", _f64, "c", "G"),
+    ("hksat", _f64, "c", "G"),
+    ("frac_sno_eff", _f64, "c", None),
+    ("frac_h2osfc", _f64, "c", None),
+    ("frac_h2osfc_nosnow", _f64, "c", None),
+    ("h2osfc_thresh", _f64, "c", None),
+    ("topo_slope", _f64, "c", None),
+    ("qflx_rain_plus_snomelt", _f64, "c", None),
+    ("qflx_snow_h2osfc", _f64, "c", None),
+    ("qflx_liqevap_from_top_layer", _f64, "c", None),
+    ("qflx_ev_soil", _f64, "c", None),
+    ("qflx_ev_h2osfc", _f64, "c", None),
+    ("qflx_floodc", _f64, "c", None),
+    ("fsat", _f64, "c", None),
+    ("fcov", _f64, "c", None),
+    ("qflx_sat_excess_surf", _f64, "c", None),
+    ("qflx_top_soil", _f64, "c", None),
+    ("qflx_in_soil", _f64, "c", None),
+    ("qflx_top_soil_to_h2osfc", _f64, "c", None),
+    ("qinmax", _f64, "c", None),
+    ("qflx_infl_excess", _f64, "c", None),
+    ("qflx_in_soil_limited", _f64, "c", None),
+    ("qflx_in_h2osfc", _f64, "c", None),
+    ("qflx_infl_excess_surf", _f64, "c", None),
+    ("h2osfc", _f64, "c", None),
+    ("qflx_h2osfc_surf", _f64, "c", None),
+    ("qflx_h2osfc_drain", _f64, "c", None),
+    ("qflx_infl", _f64, "c", None),
+    ("qflx_surf", _f64, "c", None),
+    ("xs_urban", _f64, "c", None),
+    ("h2osoi_liq", _f64, "c", "L"),
+]
+
 # clmgb_zd09_fields (soilwater_zengdecker2009!), header order
 ZD09_FIELDS = [
     ("mask_hydrology", _u8, "c", None),
@@ -372,6 +454,7 @@ StepAdjoint = type("StepAdjoint", (C.Structure,),
 SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
 RootSinkFields = _mk_struct("RootSinkFields", ROOTSINK_FIELDS)
 Zd09Fields = _mk_struct("Zd09Fields", ZD09_FIELDS)
+SurfHydFields = _mk_struct("SurfHydFields", SURFHYD_FIELDS)
 SoilFluxFields = _mk_struct("SoilFluxFields", SOILFLUX_FIELDS)
 
 

@@ -1,7 +1,7 @@
 """A set of CLM fields described by an (name, type, kind, levels) spec, host (numpy)
 or device (torch), with the matching ABI struct of pointers.  Column level arrays
 are (levels, ldc) as CLM.jl's column-major [nc, levels] matrices; patch ones
-(levels, ldp)."""
+(levels, ldp).  Kinds: 'c' column, 'p' patch, 'l' landunit, 'g' gridcell."""
 import ctypes as C
 
 import numpy as np
@@ -15,14 +15,14 @@ class FieldSet:
     SPEC = ()
     STRUCT = None
 
-    def __init__(self, vp, nc, npch=None, nl=1, arrays=None):
+    def __init__(self, vp, nc, npch=None, nl=1, arrays=None, ng=1):
         self.vp, self.nc = vp, int(nc)
         self.np = int(nc if npch is None else npch)
-        self.nl = int(nl)
+        self.nl, self.ng = int(nl), int(ng)
         if arrays is None:
             arrays = {}
             for (n, t, kind, dims) in self.SPEC:
-                m = {"c": self.nc, "p": self.np, "l": self.nl}[kind]
+                m = {"c": self.nc, "p": self.np, "l": self.nl, "g": self.ng}[kind]
                 shape = (m,) if dims is None else (abi.level_count(dims, vp), m)
                 arrays[n] = np.zeros(shape, dtype=_NP[t])
         self.arrays = arrays
@@ -34,7 +34,7 @@ class FieldSet:
         self.arrays[k] = v
 
     def _like(self, arrays):
-        return type(self)(self.vp, self.nc, self.np, self.nl, arrays)
+        return type(self)(self.vp, self.nc, self.np, self.nl, arrays, ng=self.ng)
 
     def bounds(self):
         return abi.Bounds(self.nc, self.np, self.nl, self.nc, self.np)

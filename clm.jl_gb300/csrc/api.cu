@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
+#include <initializer_list>
 #include "clmgb_device.cuh"
 #include "launch.h"
 
@@ -314,6 +315,84 @@ int32_t clmgb_effec_rootfrac_vert_tran_sink(clmgb_handle h, const clmgb_bounds* 
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+// the pointers the selected stages read or write (clmgb_surface_hydrology)
+static bool surfhyd_pointers_ok(const clmgb_surfhyd_fields* f, const clmgb_surfhyd_config* cfg, uint32_t st) {
+  auto all = [](std::initializer_list<const void*> ps) {
+    for (const void* p : ps)
+      if (!p) return false;
+    return true;
+  };
+  if ((st & CLMGB_SH_FLOODC) && !all({f->mask_nolakec, f->col_gridcell, f->col_itype, f->qflx_floodg, f->qflx_floodc}))
+    return false;
+  if (st & CLMGB_SH_SAT_EXCESS) {
+    if (!all({f->mask_hydrology, f->col_urbpoi, f->qflx_floodc, f->qflx_rain_plus_snomelt, f->fsat, f->fcov,
+              f->qflx_sat_excess_surf}))
+      return false;
+    if (cfg->fsat_method == CLMGB_FSAT_TOPMODEL ? !all({f->frost_table, f->zwt, f->zwt_perched, f->wtfact})
+                                                : !all({f->b_infil, f->top_max_moist, f->top_moist_limited}))
+      return false;
+    if (cfg->crop_fsat_equals_zero && !all({f->col_landunit, f->lun_itype})) return false;
+    if (cfg->hillslope_fsat_equals_zero && !all({f->col_is_hillslope, f->col_active, f->col_cold})) return false;
+  }
+  if ((st & CLMGB_SH_QFLX_INPUTS) &&
+      !all({f->mask_hydrology, f->col_snl, f->qflx_rain_plus_snomelt, f->qflx_snow_h2osfc, f->qflx_floodc,
+            f->qflx_liqevap_from_top_layer, f->qflx_ev_soil, f->qflx_ev_h2osfc, f->qflx_sat_excess_surf,
+            f->frac_sno_eff, f->frac_h2osfc, f->qflx_top_soil, f->qflx_in_soil, f->qflx_top_soil_to_h2osfc}))
+    return false;
+  if (st & CLMGB_SH_INFL_EXCESS) {
+    if (!all({f->mask_hydrology, f->fsat, f->qflx_in_soil, f->frac_h2osfc, f->qinmax, f->qflx_infl_excess}))
+      return false;
+    if (cfg->qinmax_method == CLMGB_QINMAX_HKSAT && !all({f->icefrac, f->hksat})) return false;
+  }
+  if ((st & CLMGB_SH_ROUTE) &&
+      !all({f->mask_hydrology, f->col_landunit, f->lun_itype, f->qflx_in_soil, f->qflx_top_soil_to_h2osfc,
+            f->qflx_infl_excess, f->qflx_in_soil_limited, f->qflx_in_h2osfc, f->qflx_infl_excess_surf}))
+    return false;
+  if ((st & CLMGB_SH_UPDATE_H2OSFC) &&
+      !all({f->mask_hydrology, f->h2osfc, f->h2osfc_thresh, f->frac_h2osfc_nosnow, f->topo_slope, f->qflx_in_h2osfc,
+            f->frac_h2osfc, f->qinmax, f->qflx_h2osfc_surf, f->qflx_h2osfc_drain}))
+    return false;
+  if ((st & CLMGB_SH_INFILTRATION) &&
+      !all({f->mask_hydrology, f->qflx_in_soil_limited, f->qflx_h2osfc_drain, f->qflx_infl}))
+    return false;
+  if ((st & CLMGB_SH_TOTAL_RUNOFF) &&
+      !all({f->mask_hydrology, f->qflx_sat_excess_surf, f->qflx_infl_excess_surf, f->qflx_h2osfc_surf, f->qflx_surf,
+            f->mask_urban, f->col_itype, f->col_snl, f->qflx_rain_plus_snomelt, f->h2osoi_liq,
+            f->qflx_liqevap_from_top_layer, f->qflx_floodc, f->xs_urban}))
+    return false;
+  if ((st & CLMGB_SH_URBAN_PONDING) &&
+      !all({f->mask_urban, f->col_itype, f->col_snl, f->xs_urban, f->qflx_rain_plus_snomelt,
+            f->qflx_liqevap_from_top_layer, f->h2osoi_liq}))
+    return false;
+  return true;
+}
+
+int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clmgb_surfhyd_fields* f,
+                                const clmgb_surfhyd_config* cfg, uint32_t stages, double dtime, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (!f || !cfg) return CLMGB_ERR_NULL_ARG;
+  if (f->struct_size != (int64_t)sizeof(clmgb_surfhyd_fields) ||
+      cfg->struct_size != (int64_t)sizeof(clmgb_surfhyd_config))
+    return CLMGB_ERR_ABI;
+  if (stages & ~CLMGB_SH_ALL) return CLMGB_ERR_CONFIG;
+  // the reference's error() on an unknown method (sat_excess_runoff.jl:347-349,
+  // infilt_excess_runoff.jl:185-187), raised whenever that routine is called
+  if ((stages & CLMGB_SH_SAT_EXCESS) && cfg->fsat_method != CLMGB_FSAT_TOPMODEL && cfg->fsat_method != CLMGB_FSAT_VIC)
+    return CLMGB_ERR_CONFIG;
+  if ((stages & CLMGB_SH_INFL_EXCESS) && cfg->qinmax_method != CLMGB_QINMAX_NONE &&
+      cfg->qinmax_method != CLMGB_QINMAX_HKSAT)
+    return CLMGB_ERR_CONFIG;
+  if ((stages & CLMGB_SH_FLOODC) && cfg->ng < 0) return CLMGB_ERR_CONFIG;
+  int32_t e = check_bounds(b, false);
+  if (e) return e;
+  if (b->nc == 0 || stages == 0) return CLMGB_OK;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  if (!surfhyd_pointers_ok(f, cfg, stages)) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_surface_hydrology(make_dims(h->vp, *b), b->nc, b->nl, *f, *cfg, stages, dtime,
+                                                   h->dev_status, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
                                    void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
@@ -550,7 +629,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
 int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y, double* out,
                         void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
-  if (op < 0 || op > 3 || n < 0) return CLMGB_ERR_CONFIG;
+  if (op < 0 || op > 4 || n < 0) return CLMGB_ERR_CONFIG;
   if (n == 0) return CLMGB_OK;
   if (!x || !out || (op == 2 && !y)) return CLMGB_ERR_NULL_ARG;
   cudaError_t ce = clmgb::launch_math_eval(op, n, x, y, out, (cudaStream_t)stream);

@@ -1,4 +1,4 @@
-// clm_math.h — table-driven log/exp/pow/log10 in binary64 for C and CUDA alike.
+// clm_math.h — table-driven log/exp/pow/log10, and sin, in binary64 for C and CUDA alike.
 //
 // Method: P. T. P. Tang's table-driven algorithms ("Table-driven implementation of
 // the exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2),
@@ -18,6 +18,8 @@
 //   cm_exp:           relative error below 2 ulp
 //   cm_pow(x, y):     relative error below (3 + |y| + |y*log(x)|) ulp (the product y*log(x)
 //                     is formed in binary64; at most ~3e-14 over the ranges the solve uses)
+//   cm_sin:           error below 1 ulp of max(|result|, 2^-53 |x|) for |x| < 2^20 pi/2
+//                     (Cody-Waite reduction; the 2^-53 |x| term covers x near multiples of pi)
 #pragma once
 #include <stdint.h>
 
@@ -144,3 +146,57 @@ CM_FN double cm_pow(double x, double y) {
 
 // Base-10 logarithm.
 CM_FN double cm_log10(double x) { return CM_MUL(cm_log(x), CM_INVLN10); }
+
+// sin and cos of a reduced argument r + lo, |r| <= pi/4, |lo| <= ulp(r) (Taylor
+// polynomials in r^2; lo enters to first order: sin' = cos ~ 1 - r^2/2, cos' = -sin ~ -r).
+CM_FN double cm_sin_poly(double r, double lo) {
+  const double z = CM_MUL(r, r);
+  double p = CM_FMA(z, CM_SIN_S8, CM_SIN_S7);
+  p = CM_FMA(z, p, CM_SIN_S6);
+  p = CM_FMA(z, p, CM_SIN_S5);
+  p = CM_FMA(z, p, CM_SIN_S4);
+  p = CM_FMA(z, p, CM_SIN_S3);
+  p = CM_FMA(z, p, CM_SIN_S2);
+  p = CM_FMA(z, p, CM_SIN_S1);
+  const double lo1 = CM_FMA(CM_MUL(-0.5, z), lo, lo);       // lo (1 - r^2/2)
+  return CM_ADD(r, CM_FMA(CM_MUL(r, z), p, lo1));            // r + (r^3 p + lo1)
+}
+CM_FN double cm_cos_poly(double r, double lo) {
+  const double z = CM_MUL(r, r);
+  double q = CM_FMA(z, CM_COS_C8, CM_COS_C7);
+  q = CM_FMA(z, q, CM_COS_C6);
+  q = CM_FMA(z, q, CM_COS_C5);
+  q = CM_FMA(z, q, CM_COS_C4);
+  q = CM_FMA(z, q, CM_COS_C3);
+  q = CM_FMA(z, q, CM_COS_C2);
+  // 1 - z/2 + z^2 q - r lo, with the rounding error of w = 1 - z/2 carried into the tail
+  const double hz = CM_MUL(0.5, z);
+  const double w = CM_SUB(1.0, hz);
+  const double c = CM_FMA(-r, lo, CM_SUB(CM_SUB(1.0, w), hz));
+  return CM_ADD(w, CM_FMA(CM_MUL(z, z), q, c));
+}
+
+// Sine for |x| < 2^20 * pi/2 (NaN beyond, and for NaN or infinite x): the reduced
+// argument x - k pi/2 = r + lo with pi/2 in three parts (k*hi and k*mid exact, the
+// subtraction of k*mid error-free by Knuth's two-sum), then sin or cos by k mod 4.
+CM_FN double cm_sin(double x) {
+  const double ax = x < 0.0 ? -x : x;
+  if (!(ax < 1647099.0)) return CM_NAN;                     // 2^20 * pi/2, NaN, Inf
+  if (ax < 0x1p-27) return x;                               // sin(x) = x in binary64
+  if (ax <= CM_PIO4) return cm_sin_poly(x, 0.0);
+  const double shift = 0x1.8p52;
+  double kd = CM_FMA(x, CM_INVPIO2, shift);
+  const int64_t k = (int64_t)(CM_AS_U64(kd) - 0x4338000000000000ULL);   // round(x*2/pi)
+  kd = CM_SUB(kd, shift);
+  const double a = CM_FMA(-kd, CM_PIO2_HI, x);              // exact
+  const double b = CM_MUL(-kd, CM_PIO2_MID);                // exact
+  const double r0 = CM_ADD(a, b);
+  const double bv = CM_SUB(r0, a);
+  const double err = CM_ADD(CM_SUB(a, CM_SUB(r0, bv)), CM_SUB(b, bv));   // a + b - r0
+  const double lo0 = CM_FMA(-kd, CM_PIO2_LO, err);
+  const double r = CM_ADD(r0, lo0);
+  const double lo = CM_SUB(lo0, CM_SUB(r, r0));
+  const int q = (int)(k & 3);
+  const double v = (q & 1) ? cm_cos_poly(r, lo) : cm_sin_poly(r, lo);
+  return (q & 2) ? -v : v;
+}

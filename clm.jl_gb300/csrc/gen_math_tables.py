@@ -15,6 +15,12 @@ logc_i = RN(-log(invc_i)), so log(z) = logc_i + log1p(z*invc_i - 1) with
 exp table (Tang's table-driven exponential, N = 64): T_j = RN(2^(j/64)), j = 0..63.
 Also the split constants ln2/N = hi + lo with hi holding 36 significant bits (k*hi
 exact for |k| < 2^17) and ln2 = hi + lo with 42-bit hi (k*hi exact for |k| < 2^11).
+
+sin: Cody and Waite's reduction by pi/2 in three parts (pi/2 = hi + mid + lo, hi and
+mid with 33 significant bits, so k*hi and k*mid are exact for |k| < 2^20), then the
+Taylor polynomials of sin (to r^17) and cos (to r^16) on |r| <= pi/4, whose
+truncation errors are below 2^-60 relative.  DEG2RAD is RN(RN(pi) / 180), the binary64
+quotient that pi/180.0 gives.
 """
 import mpmath as mp
 
@@ -73,6 +79,18 @@ def main():
         lines.append("#define CM_LOG_C%d (%s)" % (n, hexd(mp.mpf((-1) ** (n + 1)) / n)))
     for n in range(2, 7):
         lines.append("#define CM_EXP_C%d (%s)" % (n, hexd(1 / mp.factorial(n))))
+    pio2 = mp.pi / 2
+    p_hi = round_bits(pio2, 33)
+    p_mid = round_bits(pio2 - mp.mpf(p_hi), 33)
+    p_lo = float(pio2 - mp.mpf(p_hi) - mp.mpf(p_mid))
+    for k, v in (("CM_PIO2_HI", p_hi), ("CM_PIO2_MID", p_mid), ("CM_PIO2_LO", p_lo),
+                 ("CM_INVPIO2", float(2 / mp.pi)), ("CM_PIO4", float(mp.pi / 4)),
+                 ("CM_DEG2RAD", float(mp.mpf(float(mp.pi)) / 180))):
+        lines.append("#define %s (%s)" % (k, hexd(v)))
+    for k in range(1, 9):        # sin: (-1)^k / (2k+1)!
+        lines.append("#define CM_SIN_S%d (%s)" % (k, hexd(mp.mpf((-1) ** k) / mp.factorial(2 * k + 1))))
+    for k in range(2, 9):        # cos: (-1)^k / (2k)!
+        lines.append("#define CM_COS_C%d (%s)" % (k, hexd(mp.mpf((-1) ** k) / mp.factorial(2 * k))))
     print("\n".join(lines))
 
 

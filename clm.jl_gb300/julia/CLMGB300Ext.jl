@@ -178,6 +178,143 @@ function CLM.soil_water!(col::CLM.ColumnData{<:Any,<:CuArray}, mask_hydrology, m
 end
 
 # ---------------------------------------------------------------------------
+# Surface hydrology before soil_water! (clm_driver.jl:1938-2007): each routine is one
+# stage of clmgb_surface_hydrology; the whole sequence is one call with every bit.
+# Members a stage does not read stay NULL (the library checks only the selected ones).
+# ---------------------------------------------------------------------------
+struct SurfHydConfig
+    struct_size::Int64; ng::Int64
+    fsat_method::Int32; crop_fsat_equals_zero::Int32; hillslope_fsat_equals_zero::Int32
+    qinmax_method::Int32; h2osfcflag::Int32; update_h2osfcflag::Int32
+    fff::Float64; e_ice::Float64; pc::Float64; mu::Float64; pondmx_urban::Float64
+end
+const SH = (floodc = 0x1, sat_excess = 0x2, qflx_inputs = 0x4, infl_excess = 0x8, route = 0x10,
+            update_h2osfc = 0x20, infiltration = 0x40, total_runoff = 0x80, urban_ponding = 0x100)
+const SURFHYD_MEMBERS = (
+    :mask_nolakec, :mask_hydrology, :mask_urban, :col_snl, :col_itype, :col_landunit, :col_gridcell,
+    :col_urbpoi, :col_is_hillslope, :col_active, :col_cold, :lun_itype, :qflx_floodg, :frost_table, :zwt,
+    :zwt_perched, :wtfact, :b_infil, :top_max_moist, :top_moist_limited, :icefrac, :hksat, :frac_sno_eff,
+    :frac_h2osfc, :frac_h2osfc_nosnow, :h2osfc_thresh, :topo_slope, :qflx_rain_plus_snomelt, :qflx_snow_h2osfc,
+    :qflx_liqevap_from_top_layer, :qflx_ev_soil, :qflx_ev_h2osfc, :qflx_floodc, :fsat, :fcov,
+    :qflx_sat_excess_surf, :qflx_top_soil, :qflx_in_soil, :qflx_top_soil_to_h2osfc, :qinmax, :qflx_infl_excess,
+    :qflx_in_soil_limited, :qflx_in_h2osfc, :qflx_infl_excess_surf, :h2osfc, :qflx_h2osfc_surf,
+    :qflx_h2osfc_drain, :qflx_infl, :qflx_surf, :xs_urban, :h2osoi_liq)
+
+
+surfhyd_config(; ng = 1, fsat_method = CLM.FSAT_METHOD_TOPMODEL, crop = false, hillslope = false,
+               qinmax_method = CLM.QINMAX_METHOD_HKSAT, h2osfcflag = 1, update_h2osfcflag = 1) =
+    SurfHydConfig(sizeof(SurfHydConfig), ng, fsat_method, crop, hillslope, qinmax_method, h2osfcflag,
+                  update_h2osfcflag, CLM.sat_excess_runoff_params.fff, CLM.infilt_excess_params.e_ice,
+                  CLM.SURFACE_WATER_PC[], CLM.SURFACE_WATER_MU[], CLM.PONDMX_URBAN)
+
+function surface_hydrology!(stages, cfg::SurfHydConfig, nc, ldc, nl, dtime; arrays...)
+    p = Ptr{Cvoid}[haskey(arrays, m) ? ptr(arrays[m]) : C_NULL for m in SURFHYD_MEMBERS]
+    f = fields_buffer(p)
+    GC.@preserve f begin
+        check(ccall((:clmgb_surface_hydrology, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{SurfHydConfig}, UInt32, Float64, Ptr{Cvoid}),
+                    handle(), Bounds(nc, 0, nl, ldc, 0), f, cfg, UInt32(stages), Float64(dtime),
+                    CUDA.stream().handle), "clmgb_surface_hydrology")
+    end
+    nothing
+end
+
+CLM.set_floodc!(qflx_floodc, qflx_floodg, col_gridcell, col_itype, mask_nolake::CuArray, bounds) =
+    surface_hydrology!(SH.floodc, surfhyd_config(ng = length(qflx_floodg)), length(mask_nolake),
+                       length(mask_nolake), 1, 1.0; mask_nolakec = mask_nolake, qflx_floodg, col_gridcell,
+                       col_itype, qflx_floodc)
+
+function CLM.saturated_excess_runoff!(ser, mask_hydrology::CuArray, bounds_col, col, lun, sh, ss, wfb;
+                                      crop_fsat_equals_zero::Bool = false, hillslope_fsat_equals_zero::Bool = false)
+    nc = length(mask_hydrology)
+    surface_hydrology!(SH.sat_excess, surfhyd_config(fsat_method = ser.fsat_method, crop = crop_fsat_equals_zero,
+                                                     hillslope = hillslope_fsat_equals_zero),
+                       nc, nc, length(lun.itype), 1.0; mask_hydrology, frost_table = sh.frost_table_col,
+                       zwt = sh.zwt_col, zwt_perched = sh.zwt_perched_col, wtfact = ss.wtfact_col,
+                       b_infil = sh.b_infil_col, top_max_moist = sh.top_max_moist_col,
+                       top_moist_limited = sh.top_moist_limited_col, col_landunit = col.landunit,
+                       lun_itype = lun.itype, col_is_hillslope = col.is_hillslope_column, col_active = col.active,
+                       col_cold = col.cold, col_urbpoi = col.urbpoi, qflx_floodc = wfb.wf.qflx_floodc_col,
+                       qflx_rain_plus_snomelt = wfb.wf.qflx_rain_plus_snomelt_col, fsat = ser.fsat_col,
+                       fcov = ser.fcov_col, qflx_sat_excess_surf = wfb.qflx_sat_excess_surf_col)
+end
+
+function CLM.set_qflx_inputs!(wfb, wdb, col_snl, mask_hydrology::CuArray, bounds)
+    nc = length(mask_hydrology)
+    surface_hydrology!(SH.qflx_inputs, surfhyd_config(), nc, nc, 1, 1.0; mask_hydrology, col_snl,
+                       qflx_rain_plus_snomelt = wfb.wf.qflx_rain_plus_snomelt_col,
+                       qflx_snow_h2osfc = wfb.wf.qflx_snow_h2osfc_col, qflx_floodc = wfb.wf.qflx_floodc_col,
+                       qflx_liqevap_from_top_layer = wfb.wf.qflx_liqevap_from_top_layer_col,
+                       qflx_ev_soil = wfb.qflx_ev_soil_col, qflx_ev_h2osfc = wfb.qflx_ev_h2osfc_col,
+                       qflx_sat_excess_surf = wfb.qflx_sat_excess_surf_col, frac_sno_eff = wdb.frac_sno_eff_col,
+                       frac_h2osfc = wdb.frac_h2osfc_col, qflx_top_soil = wfb.wf.qflx_top_soil_col,
+                       qflx_in_soil = wfb.qflx_in_soil_col, qflx_top_soil_to_h2osfc = wfb.qflx_top_soil_to_h2osfc_col)
+end
+
+function CLM.infiltration_excess_runoff!(ier, sh, ss, fsat_col, wfb, wdb, mask_hydrology::CuArray, bounds;
+                                         params = CLM.infilt_excess_params)
+    nc = length(mask_hydrology)
+    cfg = surfhyd_config(qinmax_method = ier.qinmax_method)
+    cfg = SurfHydConfig(cfg.struct_size, cfg.ng, cfg.fsat_method, cfg.crop_fsat_equals_zero,
+                        cfg.hillslope_fsat_equals_zero, cfg.qinmax_method, cfg.h2osfcflag, cfg.update_h2osfcflag,
+                        cfg.fff, params.e_ice, cfg.pc, cfg.mu, cfg.pondmx_urban)
+    surface_hydrology!(SH.infl_excess, cfg, nc, size(sh.icefrac_col, 1), 1, 1.0; mask_hydrology,
+                       icefrac = sh.icefrac_col, hksat = ss.hksat_col, fsat = fsat_col,
+                       qflx_in_soil = wfb.qflx_in_soil_col, frac_h2osfc = wdb.frac_h2osfc_col,
+                       qinmax = ier.qinmax_col, qflx_infl_excess = wfb.qflx_infl_excess_col)
+end
+
+function CLM.route_infiltration_excess!(wfb, sh, col_landunit, lun_itype, mask_hydrology::CuArray, bounds)
+    nc = length(mask_hydrology)
+    surface_hydrology!(SH.route, surfhyd_config(h2osfcflag = sh.h2osfcflag), nc, nc, length(lun_itype), 1.0;
+                       mask_hydrology, col_landunit, lun_itype, qflx_in_soil = wfb.qflx_in_soil_col,
+                       qflx_top_soil_to_h2osfc = wfb.qflx_top_soil_to_h2osfc_col,
+                       qflx_infl_excess = wfb.qflx_infl_excess_col, qflx_in_soil_limited = wfb.qflx_in_soil_limited_col,
+                       qflx_in_h2osfc = wfb.qflx_in_h2osfc_col, qflx_infl_excess_surf = wfb.qflx_infl_excess_surf_col)
+end
+
+function CLM.update_h2osfc!(col_data, sh, ef, wfb, wsb, wdb, mask_hydrologyc::CuArray, bounds_col;
+                            dtime::Real = 1800.0, h2osfcflag::Int = 1, qinmax = nothing)
+    nc = length(mask_hydrologyc)
+    q = qinmax === nothing ? CUDA.zeros(Float64, nc) : qinmax
+    surface_hydrology!(SH.update_h2osfc, surfhyd_config(update_h2osfcflag = h2osfcflag), nc, nc, 1, dtime;
+                       mask_hydrology = mask_hydrologyc, h2osfc = wsb.ws.h2osfc_col,
+                       h2osfc_thresh = sh.h2osfc_thresh_col, frac_h2osfc_nosnow = wdb.frac_h2osfc_nosnow_col,
+                       topo_slope = col_data.topo_slope, qflx_in_h2osfc = wfb.qflx_in_h2osfc_col,
+                       frac_h2osfc = wdb.frac_h2osfc_col, qinmax = q, qflx_h2osfc_surf = wfb.qflx_h2osfc_surf_col,
+                       qflx_h2osfc_drain = wfb.qflx_h2osfc_drain_col)
+end
+
+function CLM.infiltration!(wfb, mask_hydrology::CuArray, bounds)
+    nc = length(mask_hydrology)
+    surface_hydrology!(SH.infiltration, surfhyd_config(), nc, nc, 1, 1.0; mask_hydrology,
+                       qflx_in_soil_limited = wfb.qflx_in_soil_limited_col,
+                       qflx_h2osfc_drain = wfb.qflx_h2osfc_drain_col, qflx_infl = wfb.wf.qflx_infl_col)
+end
+
+function CLM.total_surface_runoff!(wfb, sh, ws, col_snl, col_itype, col_landunit, lun_urbpoi,
+                                   mask_hydrology::CuArray, mask_urban, bounds, dtime)
+    nc = length(mask_hydrology)
+    surface_hydrology!(SH.total_runoff, surfhyd_config(), nc, size(ws.h2osoi_liq_col, 1), 1, dtime;
+                       mask_hydrology, mask_urban, col_snl, col_itype,
+                       qflx_sat_excess_surf = wfb.qflx_sat_excess_surf_col,
+                       qflx_infl_excess_surf = wfb.qflx_infl_excess_surf_col,
+                       qflx_h2osfc_surf = wfb.qflx_h2osfc_surf_col, qflx_surf = wfb.wf.qflx_surf_col,
+                       qflx_rain_plus_snomelt = wfb.wf.qflx_rain_plus_snomelt_col, h2osoi_liq = ws.h2osoi_liq_col,
+                       qflx_liqevap_from_top_layer = wfb.wf.qflx_liqevap_from_top_layer_col,
+                       qflx_floodc = wfb.wf.qflx_floodc_col, xs_urban = sh.xs_urban_col)
+end
+
+function CLM.update_urban_ponding!(ws, sh, wfb, col_snl, col_itype, mask_urban::CuArray, bounds, dtime)
+    nc = length(mask_urban)
+    surface_hydrology!(SH.urban_ponding, surfhyd_config(), nc, size(ws.h2osoi_liq_col, 1), 1, dtime;
+                       mask_urban, col_snl, col_itype, xs_urban = sh.xs_urban_col,
+                       qflx_rain_plus_snomelt = wfb.wf.qflx_rain_plus_snomelt_col,
+                       qflx_liqevap_from_top_layer = wfb.wf.qflx_liqevap_from_top_layer_col,
+                       h2osoi_liq = ws.h2osoi_liq_col)
+end
+
+# ---------------------------------------------------------------------------
 # Reverse mode.  One column step's vector-Jacobian product (clmgb_column_step_vjp)
 # behind a ChainRulesCore.rrule and an Enzyme reverse rule, the counterparts of the
 # reference's _reverse_step_into! (canopy_fluxes_reverse.jl:447-465).  `StepState`

@@ -382,6 +382,103 @@ typedef struct clmgb_soilflux_fields {
   double* qflx_liqdew_to_top_layer;      /* [np]  W */
 } clmgb_soilflux_fields;
 
+/* ---- surface hydrology before the soil solve (clm_driver.jl:1938-2007) ----
+ * The steps of the driver between set_soil_water_fractions! and the root sink, each a
+ * per-column update, run by clmgb_surface_hydrology in the driver's order for the
+ * stages selected by a mask of these bits:                                          */
+#define CLMGB_SH_FLOODC          1u   /* set_floodc! (soil_hydrology.jl:430-442; kernel :139-152) */
+#define CLMGB_SH_SAT_EXCESS      2u   /* saturated_excess_runoff! (sat_excess_runoff.jl:329-365; kernel :246-300) */
+#define CLMGB_SH_QFLX_INPUTS     4u   /* set_qflx_inputs! (soil_hydrology.jl:456-485; kernel :160-187) */
+#define CLMGB_SH_INFL_EXCESS     8u   /* infiltration_excess_runoff! (infilt_excess_runoff.jl:142-211, :241-274) */
+#define CLMGB_SH_ROUTE          16u   /* route_infiltration_excess! (soil_hydrology.jl:500-525; kernel :199-225) */
+#define CLMGB_SH_UPDATE_H2OSFC  32u   /* update_h2osfc! (surface_water.jl:462-520; kernels :279-450) */
+#define CLMGB_SH_INFILTRATION   64u   /* infiltration! (soil_hydrology.jl:538-552; kernel :236-243) */
+#define CLMGB_SH_TOTAL_RUNOFF  128u   /* total_surface_runoff! (soil_hydrology.jl:567-604; kernels :250-301) */
+#define CLMGB_SH_URBAN_PONDING 256u   /* update_urban_ponding! (soil_hydrology.jl:618-640; kernel :316-338) */
+#define CLMGB_SH_ALL           511u
+
+/* saturated_excess_runoff! fsat methods (sat_excess_runoff.jl:31-32) and
+ * infiltration_excess_runoff! qinmax methods (infilt_excess_runoff.jl:40-41). */
+#define CLMGB_FSAT_TOPMODEL 1
+#define CLMGB_FSAT_VIC      2
+#define CLMGB_QINMAX_NONE   0
+#define CLMGB_QINMAX_HKSAT  1
+
+/* The scalars of those routines: parameters, method flags and keyword arguments. */
+typedef struct clmgb_surfhyd_config {
+  int64_t struct_size;                /* sizeof(clmgb_surfhyd_config) */
+  int64_t ng;                         /* gridcells: length of qflx_floodg */
+  int32_t fsat_method;                /* SaturatedExcessRunoffData.fsat_method */
+  int32_t crop_fsat_equals_zero;      /* keyword of saturated_excess_runoff! (default 0) */
+  int32_t hillslope_fsat_equals_zero; /* keyword of saturated_excess_runoff! (default 0) */
+  int32_t qinmax_method;              /* InfiltrationExcessRunoffData.qinmax_method */
+  int32_t h2osfcflag;                 /* SoilHydrologyData.h2osfcflag, read by route_infiltration_excess! */
+  int32_t update_h2osfcflag;          /* the h2osfcflag keyword of update_h2osfc! (the driver leaves it 1) */
+  double  fff;                        /* sat_excess_runoff_params.fff, TOPModel decay factor (1/m) */
+  double  e_ice;                      /* infilt_excess_params.e_ice (6.0) */
+  double  pc;                         /* SURFACE_WATER_PC (0.4) */
+  double  mu;                         /* SURFACE_WATER_MU (0.13889) */
+  double  pondmx_urban;               /* PONDMX_URBAN (1.0 mm) */
+} clmgb_surfhyd_config;
+
+/* Every field those routines read or write.  [nc] column vectors, [nl] landunits,
+ * [ng] gridcells; icefrac/hksat [ldc, G] soil levels; h2osoi_liq [ldc, L] (the top
+ * soil level is row nlevsno). */
+typedef struct clmgb_surfhyd_fields {
+  int64_t struct_size;                /* sizeof(clmgb_surfhyd_fields) */
+  const uint8_t* mask_nolakec;        /* [nc]  filt.nolakec (set_floodc!) */
+  const uint8_t* mask_hydrology;      /* [nc]  filt.hydrologyc */
+  const uint8_t* mask_urban;          /* [nc]  filt.urbanc (total_surface_runoff!, update_urban_ponding!) */
+  const int64_t* col_snl;             /* [nc] */
+  const int64_t* col_itype;           /* [nc] */
+  const int64_t* col_landunit;        /* [nc]  1-based */
+  const int64_t* col_gridcell;        /* [nc]  1-based */
+  const uint8_t* col_urbpoi;          /* [nc] */
+  const uint8_t* col_is_hillslope;    /* [nc] */
+  const uint8_t* col_active;          /* [nc] */
+  const int64_t* col_cold;            /* [nc]  ISPVAL (-9999) when none */
+  const int64_t* lun_itype;           /* [nl] */
+  const double* qflx_floodg;          /* [ng] */
+  const double* frost_table;          /* [nc] */
+  const double* zwt;                  /* [nc] */
+  const double* zwt_perched;          /* [nc] */
+  const double* wtfact;               /* [nc] */
+  const double* b_infil;              /* [nc]  VIC */
+  const double* top_max_moist;        /* [nc]  VIC */
+  const double* top_moist_limited;    /* [nc]  VIC */
+  const double* icefrac;              /* [ldc, G] */
+  const double* hksat;                /* [ldc, G] */
+  const double* frac_sno_eff;         /* [nc] */
+  const double* frac_h2osfc;          /* [nc] */
+  const double* frac_h2osfc_nosnow;   /* [nc] */
+  const double* h2osfc_thresh;        /* [nc] */
+  const double* topo_slope;           /* [nc]  degrees */
+  const double* qflx_rain_plus_snomelt; /* [nc] */
+  const double* qflx_snow_h2osfc;     /* [nc] */
+  const double* qflx_liqevap_from_top_layer; /* [nc] */
+  const double* qflx_ev_soil;         /* [nc] */
+  const double* qflx_ev_h2osfc;       /* [nc] */
+  double* qflx_floodc;                /* [nc]  W (set_floodc!), R after */
+  double* fsat;                       /* [nc]  W */
+  double* fcov;                       /* [nc]  W */
+  double* qflx_sat_excess_surf;       /* [nc]  W */
+  double* qflx_top_soil;              /* [nc]  W */
+  double* qflx_in_soil;               /* [nc]  W */
+  double* qflx_top_soil_to_h2osfc;    /* [nc]  W */
+  double* qinmax;                     /* [nc]  W */
+  double* qflx_infl_excess;           /* [nc]  W */
+  double* qflx_in_soil_limited;       /* [nc]  W */
+  double* qflx_in_h2osfc;             /* [nc]  W */
+  double* qflx_infl_excess_surf;      /* [nc]  W */
+  double* h2osfc;                     /* [nc]  RW */
+  double* qflx_h2osfc_surf;           /* [nc]  W */
+  double* qflx_h2osfc_drain;          /* [nc]  W */
+  double* qflx_infl;                  /* [nc]  W */
+  double* qflx_surf;                  /* [nc]  W */
+  double* xs_urban;                   /* [nc]  RW */
+  double* h2osoi_liq;                 /* [ldc, L]  RW (top soil level of urban columns) */
+} clmgb_surfhyd_fields;
+
 typedef struct clmgb_handle_s* clmgb_handle;
 
 /* ---- library / handle ---- */
@@ -436,7 +533,7 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
 int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc);
 int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value);
 
-/* Evaluates the library's binary64 log (op 0), exp (1), pow (2) or log10 (3)
+/* Evaluates the library's binary64 log (op 0), exp (1), pow (2), log10 (3) or sin (4)
  * elementwise on device arrays; y is read for pow only.  The oracle and the tests
  * use it to check that the GPU rounds exactly as the CPU build does. */
 int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y,
@@ -471,6 +568,19 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b,
  * patch sum in ascending patch order (the reference's p2c), and urban t_skin. */
 int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilflux_fields* f, double dtime,
                           void* stream);
+
+/* The surface hydrology of clm_drv_core! before the root sink and soil_water!
+ * (clm_driver.jl:1938-2007), one thread per column: the CLMGB_SH_* stages in `stages`
+ * run in the driver's order, each over its own filter (nolakec for set_floodc!, urbanc
+ * for the urban part of total_surface_runoff! and update_urban_ponding!, hydrologyc for
+ * the rest), with the results of the reference's calls one by one.  A stage reads what
+ * an earlier selected stage wrote from registers and what no selected stage wrote from
+ * memory, so any subset is the same sequence of reference calls.  Only the pointers of
+ * the selected stages are required.  fsat_method and qinmax_method outside their sets
+ * -> CLMGB_ERR_CONFIG, as the reference's error().  Gridcell and landunit indices out of
+ * range set CLMGB_COL_PATCH_RANGE in the device status and skip the column. */
+int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clmgb_surfhyd_fields* f,
+                                const clmgb_surfhyd_config* cfg, uint32_t stages, double dtime, void* stream);
 
 /* soil_water! with the Zeng-Decker 2009 method (soilwater_zengdecker2009!,
  * soil_water_movement.jl:1616-1764): equilibrium matric potential from the water

@@ -16,9 +16,11 @@ LIB = os.path.join(OUT_DIR, "libclmoracle.so")
 
 def build(force=False, verbose=False):
     src = os.path.join(HERE, "clm_oracle.c")
-    hdr = os.path.join(HERE, "..", "include", "clmgb.h")
+    csrc = os.path.join(HERE, "..", "clm.jl_gb300", "csrc")
+    deps = [src, os.path.join(HERE, "..", "include", "clmgb.h"), os.path.join(csrc, "clm_math.h"),
+            os.path.join(csrc, "clm_math_tables.h")]
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) > max(os.path.getmtime(src), os.path.getmtime(hdr))):
+            and os.path.getmtime(LIB) > max(os.path.getmtime(d) for d in deps)):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()

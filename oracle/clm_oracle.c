@@ -30,9 +30,21 @@
  *   tridiagonal_col!                  src/biogeophys/soil_water_movement.jl:736-773
  *   init_soil_properties!             src/infrastructure/cold_start.jl:225-391
  *
- * Transcendentals: the reference uses Julia Base's pow/log10 (openlibm for log10);
- * this file uses the C library's.  Both are within ~1 ulp, so parity at the 1e-10
- * level is unaffected; decisions that sit within an ulp of a threshold can flip.
+ *   surface hydrology (clm_driver.jl:1938-2007), routine by routine:
+ *     set_floodc!                     src/biogeophys/soil_hydrology.jl:139-152
+ *     saturated_excess_runoff!        src/biogeophys/sat_excess_runoff.jl:246-300,329-365
+ *     set_qflx_inputs!                src/biogeophys/soil_hydrology.jl:160-187
+ *     infiltration_excess_runoff!     src/biogeophys/infilt_excess_runoff.jl:142-211,241-274
+ *     route_infiltration_excess!      src/biogeophys/soil_hydrology.jl:199-225
+ *     update_h2osfc!                  src/biogeophys/surface_water.jl:279-520
+ *     infiltration!                   src/biogeophys/soil_hydrology.jl:236-243
+ *     total_surface_runoff!           src/biogeophys/soil_hydrology.jl:250-301,567-604
+ *     update_urban_ponding!           src/biogeophys/soil_hydrology.jl:316-338
+ *
+ * Transcendentals: the reference uses Julia Base's exp/log/pow/sin (openlibm for
+ * log10); this file and the CUDA kernels share clm_math.h's binary64 versions, which
+ * are within ~1 ulp of those, so parity at the 1e-10 level is unaffected; decisions
+ * that sit within an ulp of a threshold can flip.
  * Integer powers follow Julia's literal_pow: x^2 = x*x, x^3 = x*x*x, and x^4 uses
  * Base.Math.pow_body's compensated squaring (Julia >= 1.10, Project.toml compat).
  * smooth_min/smooth_max are exact min/max for Float64 (smooth_ad.jl:91-149), with
@@ -1176,6 +1188,207 @@ int orc_soil_water_fractions(const clmgb_varpar* vp, const clmgb_bounds* b,
 }
 
 /* ===================================================================== */
+/* surface hydrology (clm_driver.jl:1938-2007), one loop per routine      */
+/* ===================================================================== */
+int orc_surface_hydrology(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_surfhyd_fields* f,
+                          const clmgb_surfhyd_config* cfg, uint32_t stages, double dtime)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  const int64_t nc = b->nc, ld = b->ldc;
+  const int top = vp->nlevsno + 1;
+  if ((stages & CLMGB_SH_SAT_EXCESS) && cfg->fsat_method != CLMGB_FSAT_TOPMODEL && cfg->fsat_method != CLMGB_FSAT_VIC)
+    return -1;
+  if ((stages & CLMGB_SH_INFL_EXCESS) && cfg->qinmax_method != CLMGB_QINMAX_NONE &&
+      cfg->qinmax_method != CLMGB_QINMAX_HKSAT)
+    return -1;
+  /* set_floodc! (soil_hydrology.jl:139-152) */
+  if (stages & CLMGB_SH_FLOODC)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_nolakec[c]) continue;
+      if (f->col_itype[c] != ICOL_SUNWALL && f->col_itype[c] != ICOL_SHADEWALL)
+        f->qflx_floodc[c] = f->qflx_floodg[f->col_gridcell[c] - 1];
+      else
+        f->qflx_floodc[c] = 0.0;
+    }
+  /* saturated_excess_runoff! (sat_excess_runoff.jl:246-300) */
+  if (stages & CLMGB_SH_SAT_EXCESS)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_hydrology[c]) continue;
+      double fs;
+      if (cfg->fsat_method == CLMGB_FSAT_TOPMODEL) {
+        if (f->frost_table[c] > f->zwt_perched[c] && f->frost_table[c] <= f->zwt[c])
+          fs = f->wtfact[c] * cm_exp(-0.5 * cfg->fff * f->zwt_perched[c]);
+        else
+          fs = f->wtfact[c] * cm_exp(-0.5 * cfg->fff * f->zwt[c]);
+      } else {
+        double ex = f->b_infil[c] / (1.0 + f->b_infil[c]);
+        fs = 1.0 - cm_pow(1.0 - f->top_moist_limited[c] / f->top_max_moist[c], ex);
+      }
+      if (cfg->crop_fsat_equals_zero && f->lun_itype[f->col_landunit[c] - 1] == ISTCROP) fs = 0.0;
+      if (cfg->hillslope_fsat_equals_zero && f->col_is_hillslope[c] && f->col_active[c] && f->col_cold[c] != -9999)
+        fs = 0.0;
+      f->fsat[c] = fs;
+      double q = fs * f->qflx_rain_plus_snomelt[c];
+      f->fcov[c] = fs;
+      if (f->col_urbpoi[c]) q = q + f->qflx_floodc[c];
+      f->qflx_sat_excess_surf[c] = q;
+    }
+  /* set_qflx_inputs! (soil_hydrology.jl:160-187) */
+  if (stages & CLMGB_SH_QFLX_INPUTS)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_hydrology[c]) continue;
+      f->qflx_top_soil[c] = f->qflx_rain_plus_snomelt[c] + f->qflx_snow_h2osfc[c] + f->qflx_floodc[c];
+      double fsno, qflx_evap;
+      if (f->col_snl[c] >= 0) {
+        fsno = 0.0;
+        qflx_evap = f->qflx_liqevap_from_top_layer[c];
+      } else {
+        fsno = f->frac_sno_eff[c];
+        qflx_evap = f->qflx_ev_soil[c];
+      }
+      f->qflx_in_soil[c] = (1.0 - f->frac_h2osfc[c]) * (f->qflx_top_soil[c] - f->qflx_sat_excess_surf[c]);
+      f->qflx_top_soil_to_h2osfc[c] = f->frac_h2osfc[c] * (f->qflx_top_soil[c] - f->qflx_sat_excess_surf[c]);
+      f->qflx_in_soil[c] = f->qflx_in_soil[c] - (1.0 - fsno - f->frac_h2osfc[c]) * qflx_evap;
+      f->qflx_top_soil_to_h2osfc[c] = f->qflx_top_soil_to_h2osfc[c] - f->frac_h2osfc[c] * f->qflx_ev_h2osfc[c];
+    }
+  /* infiltration_excess_runoff! (infilt_excess_runoff.jl:142-211, 241-274) */
+  if (stages & CLMGB_SH_INFL_EXCESS) {
+    double* qinmax_unsat = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_hydrology[c]) continue;
+      if (cfg->qinmax_method == CLMGB_QINMAX_NONE) {
+        qinmax_unsat[c] = 1.0e200;
+      } else {
+        double qmin = INFINITY;
+        for (int j = 1; j <= 3; j++) {
+          double val = cm_pow(10.0, -cfg->e_ice * IX(f->icefrac, c, j, ld)) * IX(f->hksat, c, j, ld);
+          if (val < qmin) qmin = val;
+        }
+        qinmax_unsat[c] = qmin;
+      }
+    }
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_hydrology[c]) continue;
+      f->qinmax[c] = (1.0 - f->fsat[c]) * qinmax_unsat[c];
+      f->qflx_infl_excess[c] = jl_max(0.0, f->qflx_in_soil[c] - (1.0 - f->frac_h2osfc[c]) * f->qinmax[c]);
+    }
+    free(qinmax_unsat);
+  }
+  /* route_infiltration_excess! (soil_hydrology.jl:199-225) */
+  if (stages & CLMGB_SH_ROUTE)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_hydrology[c]) continue;
+      int64_t lt = f->lun_itype[f->col_landunit[c] - 1];
+      if (lt == ISTSOIL || lt == ISTCROP) {
+        f->qflx_in_soil_limited[c] = f->qflx_in_soil[c] - f->qflx_infl_excess[c];
+        if (cfg->h2osfcflag != 0) {
+          f->qflx_in_h2osfc[c] = f->qflx_top_soil_to_h2osfc[c] + f->qflx_infl_excess[c];
+          f->qflx_infl_excess_surf[c] = 0.0;
+        } else {
+          f->qflx_in_h2osfc[c] = f->qflx_top_soil_to_h2osfc[c];
+          f->qflx_infl_excess_surf[c] = f->qflx_infl_excess[c];
+        }
+      } else {
+        f->qflx_in_soil_limited[c] = f->qflx_in_soil[c];
+        f->qflx_in_h2osfc[c] = 0.0;
+        f->qflx_infl_excess_surf[c] = 0.0;
+      }
+    }
+  /* update_h2osfc! (surface_water.jl:462-520): its four kernels in turn, with the
+   * two scratch vectors it allocates */
+  if (stages & CLMGB_SH_UPDATE_H2OSFC) {
+    const int flag = cfg->update_h2osfcflag;
+    double* qsurf = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+    double* qdrain = (double*)calloc((size_t)(nc > 0 ? nc : 1), sizeof(double));
+    for (int64_t c = 0; c < nc; c++) {       /* _surfwat_qflx_surf_kernel! (:279-316) */
+      if (!f->mask_hydrology[c]) continue;
+      if (flag != 1) {
+        qsurf[c] = 0.0;
+      } else {
+        double frac_infclust;
+        if (f->frac_h2osfc_nosnow[c] <= cfg->pc) frac_infclust = 0.0;
+        else frac_infclust = cm_pow(f->frac_h2osfc_nosnow[c] - cfg->pc, cfg->mu);
+        double q = 0.0;
+        if (f->h2osfc[c] > f->h2osfc_thresh[c] && flag != 0) {
+          double k_wet = 1.0e-4 * cm_sin(CM_DEG2RAD * f->topo_slope[c]);
+          q = k_wet * frac_infclust * (f->h2osfc[c] - f->h2osfc_thresh[c]);
+          q = jl_min(q, (f->h2osfc[c] - f->h2osfc_thresh[c]) / dtime);
+        }
+        if (q < 1.0e-8) q = 0.0;
+        qsurf[c] = q;
+      }
+    }
+    for (int64_t c = 0; c < nc; c++) {       /* _surfwat_partial_update_kernel! (:400-414) */
+      if (!f->mask_hydrology[c]) continue;
+      double h = f->h2osfc[c] + (f->qflx_in_h2osfc[c] - qsurf[c]) * dtime;
+      if (fabs(h) < 1.0e-13 * fabs(f->h2osfc[c])) h = 0.0;
+      f->h2osfc[c] = h;
+    }
+    for (int64_t c = 0; c < nc; c++) {       /* _surfwat_qflx_drain_kernel! (:357-374) */
+      if (!f->mask_hydrology[c]) continue;
+      if (f->h2osfc[c] < 0.0) {
+        qdrain[c] = f->h2osfc[c] / dtime;
+      } else {
+        double q = jl_min(f->frac_h2osfc[c] * f->qinmax[c], f->h2osfc[c] / dtime);
+        if (flag == 0) q = jl_max(0.0, f->h2osfc[c] / dtime);
+        qdrain[c] = q;
+      }
+    }
+    for (int64_t c = 0; c < nc; c++) {       /* _surfwat_final_update_kernel! (:426-443) */
+      if (!f->mask_hydrology[c]) continue;
+      double h = f->h2osfc[c] - qdrain[c] * dtime;
+      if (fabs(h) < 1.0e-13 * fabs(f->h2osfc[c])) h = 0.0;
+      f->h2osfc[c] = h;
+      f->qflx_h2osfc_surf[c] = qsurf[c];
+      f->qflx_h2osfc_drain[c] = qdrain[c];
+    }
+    free(qsurf);
+    free(qdrain);
+  }
+  /* infiltration! (soil_hydrology.jl:236-243) */
+  if (stages & CLMGB_SH_INFILTRATION)
+    for (int64_t c = 0; c < nc; c++)
+      if (f->mask_hydrology[c]) f->qflx_infl[c] = f->qflx_in_soil_limited[c] + f->qflx_h2osfc_drain[c];
+  /* total_surface_runoff! (soil_hydrology.jl:250-301) */
+  if (stages & CLMGB_SH_TOTAL_RUNOFF) {
+    for (int64_t c = 0; c < nc; c++)
+      if (f->mask_hydrology[c])
+        f->qflx_surf[c] = f->qflx_sat_excess_surf[c] + f->qflx_infl_excess_surf[c] + f->qflx_h2osfc_surf[c];
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_urban[c]) continue;
+      int64_t it = f->col_itype[c];
+      if (it == ICOL_ROOF || it == ICOL_ROAD_IMPERV) {
+        if (f->col_snl[c] < 0) {
+          f->qflx_surf[c] = jl_max(0.0, f->qflx_rain_plus_snomelt[c]);
+        } else {
+          f->xs_urban[c] = jl_max(0.0, IX(f->h2osoi_liq, c, top, ld) / dtime + f->qflx_rain_plus_snomelt[c] -
+                                           f->qflx_liqevap_from_top_layer[c] - cfg->pondmx_urban / dtime);
+          f->qflx_surf[c] = f->xs_urban[c];
+        }
+        f->qflx_surf[c] = f->qflx_surf[c] + f->qflx_floodc[c];
+      } else if (it == ICOL_SUNWALL || it == ICOL_SHADEWALL) {
+        f->qflx_surf[c] = 0.0;
+      }
+    }
+  }
+  /* update_urban_ponding! (soil_hydrology.jl:316-338) */
+  if (stages & CLMGB_SH_URBAN_PONDING)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_urban[c]) continue;
+      int64_t it = f->col_itype[c];
+      if ((it == ICOL_ROOF || it == ICOL_ROAD_IMPERV) && f->col_snl[c] >= 0) {
+        if (f->xs_urban[c] > 0.0)
+          IX(f->h2osoi_liq, c, top, ld) = cfg->pondmx_urban;
+        else
+          IX(f->h2osoi_liq, c, top, ld) = jl_max(0.0, IX(f->h2osoi_liq, c, top, ld) +
+                                                          (f->qflx_rain_plus_snomelt[c] - f->qflx_liqevap_from_top_layer[c]) * dtime);
+      }
+    }
+  return 0;
+}
+
+/* ===================================================================== */
 /* soil_fluxes! (soil_fluxes.jl:553-697), loop by loop                    */
 /* ===================================================================== */
 int orc_soil_fluxes(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_soilflux_fields* f, double dtime)
@@ -2100,3 +2313,4 @@ double orc_cm_log(double x) { return cm_log(x); }
 double orc_cm_exp(double x) { return cm_exp(x); }
 double orc_cm_pow(double x, double y) { return cm_pow(x, y); }
 double orc_cm_log10(double x) { return cm_log10(x); }
+double orc_cm_sin(double x) { return cm_sin(x); }

@@ -37,6 +37,7 @@ def lib():
         L.orc_rootsink.argtypes = [P, P, P, C.c_int32]
         L.orc_soil_water_zd09.argtypes = [P, P, P, C.c_double, C.c_double]
         L.orc_soil_fluxes.argtypes = [P, P, P, C.c_double]
+        L.orc_surface_hydrology.argtypes = [P, P, P, P, C.c_uint32, C.c_double]
         L.orc_soil_water.argtypes = [P, P, P, P, C.c_double, P, P, P, C.c_int32]
         L.orc_run_steps.argtypes = [P, P, P, P, P, C.c_double, C.c_int32, C.c_int32, P, P,
                                     C.c_int64, P, P, P, C.c_int32]
@@ -98,6 +99,12 @@ def rootsink(rs, use_hydrstress=False):
 def soil_fluxes(fs, dtime):
     """soil_fluxes! in place on a host SoilFluxState."""
     _chk(lib().orc_soil_fluxes(C.byref(fs.vp), C.byref(fs.bounds()), C.byref(fs.fields()), float(dtime)))
+
+
+def surface_hydrology(sh, dtime, cfg, stages):
+    """The surface-hydrology routines selected by `stages`, in place on a host SurfHydState."""
+    _chk(lib().orc_surface_hydrology(C.byref(sh.vp), C.byref(sh.bounds()), C.byref(sh.fields()), C.byref(cfg),
+                                     int(stages), float(dtime)))
 
 
 def soil_water_zd09(zs, dtime, e_ice=6.0):

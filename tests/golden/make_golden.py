@@ -6,6 +6,7 @@ and analytic answers (x = 1:n solutions, [1,1,1], impedance powers, conservation
 identities), not outputs captured from a run.  Run:  python tests/golden/make_golden.py
 """
 import json
+import math
 import os
 
 import numpy as np
@@ -38,6 +39,163 @@ def band_case(A, x, jtop, nlevs, kl, ku, tol, src):
             bm[band, lev] = A[i, j]
     return dict(bmatrix=bm.tolist(), rvector=r.tolist(), x_exact=x.tolist(), jtop=jtop,
                 jbot=jtop + n - 1, nlevs=nlevs, kl=kl, ku=ku, atol=tol, source=src)
+
+
+def surface_hydrology_cases():
+    """The known answers of the surface-hydrology routines' tests, one case per call:
+    test/test_sat_excess_runoff.jl, test/test_infilt_excess_runoff.jl and
+    test/test_soil_hydrology_mod.jl.  Column vectors are per column; "icefrac3" and
+    "hksat3" give soil levels 1-3 per column; "liq_top" the top soil level's liquid.
+    Expected values are the tests' own formulas with their tolerances (isapprox's
+    default rtol is sqrt(eps) = 1.49e-8)."""
+    RT = 2.0 ** -26
+    ISTSOIL, ISTCROP, SUNWALL, SHADEWALL, ROOF, ROAD_IMPERV, ISPVAL = 1, 2, 72, 73, 71, 74, -9999
+    out = []
+
+    def case(name, src, stages, nc, inputs, expect, cfg=None, nl=1, ng=1, dtime=1800.0, masks=None, nan=None,
+             error=False):
+        out.append(dict(name=name, source=src, stages=stages, nc=nc, nl=nl, ng=ng, dtime=dtime, cfg=cfg or {},
+                        inputs=inputs, masks=masks or {}, expect=expect, expect_nan=nan or {}, error=error))
+
+    def ex(field, values, rtol=RT, atol=0.0):
+        return dict(field=field, values=values, rtol=rtol, atol=atol)
+
+    sat = ["saturated_excess_runoff!"]
+
+    def sat_inputs(nc, **kw):
+        d = dict(col_landunit=[1] * nc, col_urbpoi=[0] * nc, col_active=[1] * nc, col_is_hillslope=[0] * nc,
+                 col_cold=[ISPVAL] * nc, qflx_floodc=[0.0] * nc)
+        d.update(kw)
+        return d
+
+    e = [0.4 * math.exp(-0.5 * 0.5 * 2.0), 0.4 * math.exp(-0.5 * 0.5 * 1.0), 0.4 * math.exp(-0.5 * 0.5 * 2.0)]
+    case("sat_topmodel", "test/test_sat_excess_runoff.jl:182-245", sat, 3,
+         sat_inputs(3, frost_table=[5.0, 1.5, 0.5], zwt=[2.0] * 3, zwt_perched=[1.0] * 3, wtfact=[0.4] * 3,
+                    qflx_rain_plus_snomelt=[5.0, 10.0, 2.0]),
+         [ex("fsat", e), ex("qflx_sat_excess_surf", [e[0] * 5.0, e[1] * 10.0, e[2] * 2.0]), ex("fcov", e)],
+         cfg=dict(fff=0.5), nl=1)
+    f1, f2 = 1.0 - (1.0 - 50.0 / 100.0) ** 0.5, 1.0 - (1.0 - 150.0 / 200.0) ** (2.0 / 3.0)
+    case("sat_vic", "test/test_sat_excess_runoff.jl:250-305", sat, 2,
+         sat_inputs(2, b_infil=[1.0, 2.0], top_max_moist=[100.0, 200.0], top_moist_limited=[50.0, 150.0],
+                    qflx_rain_plus_snomelt=[8.0, 4.0]),
+         [ex("fsat", [f1, f2]), ex("qflx_sat_excess_surf", [f1 * 8.0, f2 * 4.0])], cfg=dict(fsat_method=2))
+    e1 = 0.4 * math.exp(-0.5 * 0.5 * 1.0)
+    case("sat_crop_fsat_zero", "test/test_sat_excess_runoff.jl:310-364", sat, 2,
+         sat_inputs(2, col_landunit=[1, 2], lun_itype=[ISTSOIL, ISTCROP], frost_table=[5.0] * 2, zwt=[1.0] * 2,
+                    zwt_perched=[10.0] * 2, wtfact=[0.4] * 2, qflx_rain_plus_snomelt=[10.0] * 2),
+         [ex("fsat", [e1, 0.0]), ex("qflx_sat_excess_surf", [e1 * 10.0, 0.0])],
+         cfg=dict(fff=0.5, crop_fsat_equals_zero=1), nl=2)
+    case("sat_hillslope_fsat_zero", "test/test_sat_excess_runoff.jl:369-428", sat, 3,
+         sat_inputs(3, col_is_hillslope=[0, 1, 1], col_cold=[ISPVAL, 3, ISPVAL], frost_table=[5.0] * 3,
+                    zwt=[1.0] * 3, zwt_perched=[10.0] * 3, wtfact=[0.4] * 3, qflx_rain_plus_snomelt=[10.0] * 3),
+         [ex("fsat", [e1, 0.0, e1]), ex("qflx_sat_excess_surf", [None, 0.0, e1 * 10.0])],
+         cfg=dict(fff=0.5, hillslope_fsat_equals_zero=1))
+    e3 = 0.3 * math.exp(-0.5 * 0.5 * 1.0)
+    case("sat_urban_flood", "test/test_sat_excess_runoff.jl:433-478", sat, 2,
+         sat_inputs(2, col_urbpoi=[1, 0], frost_table=[5.0] * 2, zwt=[1.0] * 2, zwt_perched=[10.0] * 2,
+                    wtfact=[0.3] * 2, qflx_rain_plus_snomelt=[5.0] * 2, qflx_floodc=[2.0] * 2),
+         [ex("qflx_sat_excess_surf", [e3 * 5.0 + 2.0, e3 * 5.0])], cfg=dict(fff=0.5))
+    e5 = 0.5 * math.exp(-0.5 * 1.0 * 1.0)
+    case("sat_mask", "test/test_sat_excess_runoff.jl:483-530", sat, 4,
+         sat_inputs(4, frost_table=[5.0] * 4, zwt=[1.0] * 4, zwt_perched=[10.0] * 4, wtfact=[0.5] * 4,
+                    qflx_rain_plus_snomelt=[3.0] * 4, fsat=[float("nan")] * 4),
+         [ex("fsat", [e5, None, e5, None]), ex("qflx_sat_excess_surf", [e5 * 3.0, None, e5 * 3.0, None])],
+         cfg=dict(fff=1.0), masks=dict(mask_hydrology=[1, 0, 1, 0]), nan=dict(fsat=[1, 3]))
+    case("sat_invalid_method", "test/test_sat_excess_runoff.jl:535-570", sat, 1, sat_inputs(1), [],
+         cfg=dict(fsat_method=99), error=True)
+    case("sat_crop_and_hillslope", "test/test_sat_excess_runoff.jl:575-630", sat, 3,
+         sat_inputs(3, col_landunit=[1, 2, 2], lun_itype=[ISTCROP, ISTSOIL], col_is_hillslope=[0, 1, 0],
+                    col_cold=[ISPVAL, 3, ISPVAL], frost_table=[5.0] * 3, zwt=[1.0] * 3, zwt_perched=[10.0] * 3,
+                    wtfact=[0.4] * 3, qflx_rain_plus_snomelt=[10.0] * 3),
+         [ex("fsat", [0.0, 0.0, e1], atol=0.0), ex("qflx_sat_excess_surf", [0.0, 0.0, e1 * 10.0])],
+         cfg=dict(fff=0.5, crop_fsat_equals_zero=1, hillslope_fsat_equals_zero=1), nl=2)
+
+    inf = ["infiltration_excess_runoff!"]
+
+    def inf_inputs(nc, ice, hk, fsat, qin, fh):
+        return dict(icefrac3=ice, hksat3=hk, fsat=fsat, qflx_in_soil=qin, frac_h2osfc=fh)
+
+    v = [10.0 ** (-6.0 * 0.1) * 0.01, 10.0 ** (-6.0 * 0.2) * 0.02, 10.0 ** (-6.0 * 0.3) * 0.03]
+    case("qinmax_hksat", "test/test_infilt_excess_runoff.jl:71-124 (qinmax with fsat = 0 is qinmax_on_unsaturated_area)",
+         inf, 3, inf_inputs(3, [[0.1, 0.2, 0.3], [0.0] * 3, [0.5] * 3], [[0.01, 0.02, 0.03], [0.05] * 3, [0.01] * 3],
+                            [0.0] * 3, [0.0] * 3, [0.0] * 3),
+         [ex("qinmax", [min(v), 0.05, 10.0 ** (-6.0 * 0.5) * 0.01], rtol=0.0, atol=1e-15)])
+    case("infl_excess_hksat", "test/test_infilt_excess_runoff.jl:128-170", inf, 2,
+         inf_inputs(2, [[0.0] * 3] * 2, [[0.01] * 3] * 2, [0.1, 0.2], [0.02, 0.005], [0.0, 0.0]),
+         [ex("qinmax", [0.9 * 0.01, 0.8 * 0.01], rtol=0.0, atol=1e-15),
+          ex("qflx_infl_excess", [max(0.0, 0.02 - 0.009), 0.0], rtol=0.0, atol=1e-15)])
+    case("infl_excess_none", "test/test_infilt_excess_runoff.jl:175-210", inf, 2,
+         inf_inputs(2, [[0.0] * 3] * 2, [[0.01] * 3] * 2, [0.0, 0.0], [100.0, 200.0], [0.0, 0.0]),
+         [ex("qinmax", [1.0e200, 1.0e200], rtol=0.0, atol=1e190), ex("qflx_infl_excess", [0.0, 0.0], rtol=0.0)],
+         cfg=dict(qinmax_method=0))
+    case("infl_excess_mask", "test/test_infilt_excess_runoff.jl:215-252", inf, 3,
+         dict(inf_inputs(3, [[0.0] * 3] * 3, [[0.01] * 3] * 3, [0.0] * 3, [0.02] * 3, [0.0] * 3),
+              qinmax=[float("nan")] * 3),
+         [ex("qinmax", [None, 0.01, None], rtol=0.0, atol=1e-15)], masks=dict(mask_hydrology=[0, 1, 0]),
+         nan=dict(qinmax=[0, 2]))
+    case("qinmax_zero_ice", "test/test_infilt_excess_runoff.jl:257-280", inf, 1,
+         inf_inputs(1, [[0.0] * 3], [[0.05, 0.03, 0.04]], [0.0], [0.0], [0.0]),
+         [ex("qinmax", [0.03], rtol=0.0, atol=1e-15)])
+    fz = 10.0 ** (-6.0) * 0.01
+    case("infl_excess_fully_frozen", "test/test_infilt_excess_runoff.jl:284-330", inf, 1,
+         inf_inputs(1, [[1.0] * 3], [[0.01] * 3], [0.0], [0.001], [0.0]),
+         [ex("qinmax", [fz], rtol=0.0, atol=1e-20), ex("qflx_infl_excess", [max(0.0, 0.001 - fz)], rtol=0.0, atol=1e-12)])
+    for fs, qm, exv in ((0.5, 0.5 * 0.02, 0.0), (0.9, 0.1 * 0.02, 0.003)):
+        case("infl_excess_fsat_%g" % fs, "test/test_infilt_excess_runoff.jl:335-378", inf, 1,
+             inf_inputs(1, [[0.0] * 3], [[0.02] * 3], [fs], [0.005], [0.0]),
+             [ex("qinmax", [qm], rtol=0.0, atol=1e-15), ex("qflx_infl_excess", [exv], rtol=0.0, atol=1e-15)])
+    for fh, exv in ((0.0, 0.005), (0.5, max(0.0, 0.015 - 0.5 * 0.01)), (1.0, 0.015)):
+        case("infl_excess_frac_h2osfc_%g" % fh, "test/test_infilt_excess_runoff.jl:383-428", inf, 1,
+             inf_inputs(1, [[0.0] * 3], [[0.01] * 3], [0.0], [0.015], [fh]),
+             [ex("qflx_infl_excess", [exv], rtol=0.0, atol=1e-15)])
+    q3 = 10.0 ** (-6.0 * 0.8) * 0.01
+    case("infl_excess_heterogeneous", "test/test_infilt_excess_runoff.jl:433-488", inf, 4,
+         inf_inputs(4, [[0.0] * 3, [0.0] * 3, [0.8] * 3, [0.0] * 3], [[0.01] * 3, [0.1] * 3, [0.01] * 3, [0.01] * 3],
+                    [0.0, 0.0, 0.0, 0.5], [0.005] * 4, [0.0] * 4),
+         [ex("qflx_infl_excess", [0.0, 0.0, None, 0.0], rtol=0.0, atol=1e-15),
+          ex("qflx_infl_excess", [None, None, max(0.0, 0.005 - q3), None], rtol=0.0, atol=1e-12),
+          ex("qinmax", [None, None, q3, 0.005], rtol=0.0, atol=1e-15)])
+    case("infl_invalid_method", "test/test_infilt_excess_runoff.jl:493-520", inf, 1,
+         inf_inputs(1, [[0.0] * 3], [[0.01] * 3], [0.0], [0.01], [0.0]), [], cfg=dict(qinmax_method=99), error=True)
+    for ei in (3.0, 9.0):
+        case("qinmax_e_ice_%g" % ei, "test/test_infilt_excess_runoff.jl:525-555", inf, 1,
+             inf_inputs(1, [[0.5] * 3], [[0.01] * 3], [0.0], [0.0], [0.0]),
+             [ex("qinmax", [10.0 ** (-ei * 0.5) * 0.01], rtol=0.0, atol=1e-15)], cfg=dict(e_ice=ei))
+
+    case("set_floodc", "test/test_soil_hydrology_mod.jl:117-131", ["set_floodc!"], 4,
+         dict(qflx_floodg=[0.5, 0.3], col_gridcell=[1, 1, 2, 2], col_itype=[1, SUNWALL, 1, SHADEWALL]),
+         [ex("qflx_floodc", [0.5, 0.0, 0.3, 0.0])], ng=2)
+    case("infiltration", "test/test_soil_hydrology_mod.jl:136-150", ["infiltration!"], 3,
+         dict(qflx_in_soil_limited=[0.1, 0.2, 0.3], qflx_h2osfc_drain=[0.01, 0.02, 0.03]),
+         [ex("qflx_infl", [0.11, 0.22, 0.33])])
+    # The truncation test calls the partial-update kernel alone with an outflow; through
+    # update_h2osfc! the same arithmetic is an inflow of the opposite sign, the store
+    # below its spill threshold (no runoff) and no drainage (frac_h2osfc = 0).
+    for rel, res in ((5.0e-11, 5.0e-11), (5.0e-14, 0.0)):
+        case("h2osfc_truncation_%g" % rel, "test/test_soil_hydrology_mod.jl:152-173", ["update_h2osfc!"], 1,
+             dict(h2osfc=[1.0], qflx_in_h2osfc=[-(1.0 - rel) / 1800.0], h2osfc_thresh=[10.0], frac_h2osfc=[0.0],
+                  frac_h2osfc_nosnow=[0.0], qinmax=[0.0], topo_slope=[5.0]),
+             [ex("h2osfc", [res], rtol=0.0, atol=1e-15 if res else 0.0)])
+    urb = ["total_surface_runoff!", "update_urban_ponding!"]
+
+    def urb_inputs(rain, evap, pond0):
+        return dict(col_snl=[0, 0], col_itype=[ROOF, ROAD_IMPERV], qflx_rain_plus_snomelt=[rain] * 2,
+                    qflx_liqevap_from_top_layer=[evap] * 2, qflx_floodc=[0.0] * 2, xs_urban=[0.0] * 2,
+                    qflx_surf=[0.0] * 2, liq_top=pond0, qflx_sat_excess_surf=[0.0] * 2,
+                    qflx_infl_excess_surf=[0.0] * 2, qflx_h2osfc_surf=[0.0] * 2)
+
+    um = dict(mask_hydrology=[0, 0], mask_urban=[1, 1])
+    case("urban_pond_light_rain", "test/test_soil_hydrology_mod.jl:495-534", urb, 2, urb_inputs(1.0e-4, 0.0, [0.0, 0.0]),
+         [ex("xs_urban", [0.0, 0.0], rtol=0.0, atol=1e-12), ex("qflx_surf", [0.0, 0.0], rtol=0.0, atol=1e-12),
+          ex("liq_top", [1.0e-4 * 3600.0] * 2)], dtime=3600.0, masks=um)
+    xs = 1.0e-2 - 1.0 / 3600.0
+    case("urban_pond_heavy_rain", "test/test_soil_hydrology_mod.jl:536-556", urb, 2, urb_inputs(1.0e-2, 0.0, [0.0, 0.0]),
+         [ex("xs_urban", [xs] * 2, rtol=1e-10), ex("qflx_surf", [xs] * 2, rtol=1e-10), ex("liq_top", [1.0, 1.0])],
+         dtime=3600.0, masks=um)
+    case("urban_pond_balance", "test/test_soil_hydrology_mod.jl:558-582", urb, 2, urb_inputs(5.0e-4, 1.0e-4, [0.2, 0.5]),
+         [dict(field="pond_balance", rain=5.0e-4, evap=1.0e-4, pond0=[0.2, 0.5], atol=1e-10)],
+         dtime=3600.0, masks=um)
+    return dict(cases=out)
 
 
 def soil_fluxes_cases():
@@ -213,6 +371,7 @@ def main():
                                               source="test/test_soil_temperature.jl:498-532")
     cases["rootsink"] = rootsink_cases()
     cases["soil_fluxes"] = soil_fluxes_cases()
+    cases["surface_hydrology"] = surface_hydrology_cases()
     with open(os.path.join(HERE, "reference_cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1, sort_keys=True)
 

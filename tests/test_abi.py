@@ -34,7 +34,8 @@ def test_header_structs_match_ctypes():
                           ("clmgb_soilwater_fields", abi.SOILWATER_FIELDS),
                           ("clmgb_rootsink_fields", abi.ROOTSINK_FIELDS),
                           ("clmgb_zd09_fields", abi.ZD09_FIELDS),
-                          ("clmgb_soilflux_fields", abi.SOILFLUX_FIELDS)):
+                          ("clmgb_soilflux_fields", abi.SOILFLUX_FIELDS),
+                          ("clmgb_surfhyd_fields", abi.SURFHYD_FIELDS)):
         members = abi.header_struct_members(txt, sname)
         assert members[0] == "struct_size"
         assert members[1:] == [f[0] for f in fields], sname
@@ -43,6 +44,7 @@ def test_header_structs_match_ctypes():
     assert abi.header_struct_members(txt, "clmgb_swm_config") == [f[0] for f in abi.SwmConfig._fields_]
     assert abi.header_struct_members(txt, "clmgb_step_adjoint") == [f[0] for f in abi.StepAdjoint._fields_]
     assert abi.header_struct_members(txt, "clmgb_substep_log") == [f[0] for f in abi.SubstepLog._fields_]
+    assert abi.header_struct_members(txt, "clmgb_surfhyd_config") == [f[0] for f in abi.SurfHydConfig._fields_]
 
 
 def test_header_constants_match_python():
@@ -53,6 +55,10 @@ def test_header_constants_match_python():
                  "ADJ_RICHARDS_CLOSED_FORM", "ADJ_RICHARDS_RECORDED", "COL_ADJ_REPLAY", "ADJ_MAX_SUBSTEPS",
                  "OPT_ADJ_SOIL_TEMPERATURE", "ADJ_ST_CLOSED_FORM", "ADJ_ST_RECORDED", "OPT_QUEUE_FRESH_BATCH",
                  "COL_FILTER"):
+        assert int(consts[name]) == getattr(abi, name), name
+    for name in ("SH_FLOODC", "SH_SAT_EXCESS", "SH_QFLX_INPUTS", "SH_INFL_EXCESS", "SH_ROUTE", "SH_UPDATE_H2OSFC",
+                 "SH_INFILTRATION", "SH_TOTAL_RUNOFF", "SH_URBAN_PONDING", "SH_ALL", "FSAT_TOPMODEL", "FSAT_VIC",
+                 "QINMAX_NONE", "QINMAX_HKSAT"):
         assert int(consts[name]) == getattr(abi, name), name
 
 

@@ -316,7 +316,7 @@ def test_empty_bounds_is_noop(handle_factory):
 
 
 # ---------------------------------------------------------------- shared math
-@pytest.mark.parametrize("op", ["log", "exp", "pow", "log10"])
+@pytest.mark.parametrize("op", ["log", "exp", "pow", "log10", "sin"])
 def test_math_bit_identical_to_cpu_build(handle_factory, op):
     import ctypes as C
     h = handle_factory(synth.clm5_varpar())
@@ -324,6 +324,8 @@ def test_math_bit_identical_to_cpu_build(handle_factory, op):
     n = 200000
     if op == "exp":
         x = rng.uniform(-745, 709, n)
+    elif op == "sin":
+        x = np.concatenate([rng.uniform(-1e5, 1e5, n // 2), rng.uniform(-4.0, 4.0, n - n // 2)])
     else:
         x = np.concatenate([10 ** rng.uniform(-300, 300, n // 2), rng.uniform(0.0, 3.0, n - n // 2)])
     y = rng.uniform(-50, 50, n)

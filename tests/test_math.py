@@ -89,3 +89,22 @@ def test_pow_special_values():
     assert fpow(0.0, 2.0) == 0.0 and fpow(0.0, -1.0) == math.inf
     assert math.isnan(fpow(-2.0, 0.5)) and fpow(-2.0, 3.0) == pytest.approx(-8.0, rel=1e-15)
     assert fpow(math.inf, 2.0) == math.inf and fpow(math.inf, -2.0) == 0.0
+
+
+def test_sin_accuracy():
+    rng = np.random.default_rng(3)
+    xs = np.concatenate([rng.uniform(-math.pi, math.pi, 4000), rng.uniform(-1e5, 1e5, 2000),
+                         rng.uniform(0.0, 90.0, 2000) * float.fromhex("0x1.1df46a2529d39p-6"),
+                         10 ** rng.uniform(-12, 0, 500),
+                         [0.0, -0.0, 1e-300, math.pi / 4, math.pi / 2, math.pi, 3 * math.pi / 4, 1.6e6]])
+    fsin = _fn("orc_cm_sin", 1)
+    worst = 0.0
+    for x in xs:
+        x = float(x)
+        ref = mp.sin(mp.mpf(x))
+        got = fsin(x)
+        scale = max(abs(float(ref)), 2.0 ** -53 * abs(x), 5e-324)
+        worst = max(worst, float(abs(mp.mpf(got) - ref)) / ulp(scale))
+    assert worst < 1.0, worst
+    assert fsin(0.0) == 0.0 and math.copysign(1.0, fsin(-0.0)) == -1.0
+    assert math.isnan(fsin(math.inf)) and math.isnan(fsin(math.nan)) and math.isnan(fsin(2e6))
