@@ -131,6 +131,28 @@ class SurfHydConfig(C.Structure):
         return cls(C.sizeof(cls), ng, FSAT_TOPMODEL, 0, 0, QINMAX_HKSAT, 1, 1, fff, 6.0, 0.4, 0.13889, 1.0)
 
 
+# clmgb_snow_layers stages (CLMGB_SL_*), in the driver's order
+SL_COMPACTION, SL_COMBINE, SL_DIVIDE, SL_ZERO_EMPTY, SL_FILTER, SL_ALL = 1, 2, 4, 8, 16, 31
+OVERBURDEN_ANDERSON1976, OVERBURDEN_VIONNET2012 = 1, 2
+
+
+class SnowLayerConfig(C.Structure):
+    """clmgb_snowlayer_config: SnowHydrologyParams and the snow module switches."""
+    _fields_ = [("struct_size", C.c_int64), ("ng", C.c_int64), ("use_subgrid_fluxes", C.c_int32),
+                ("overburden_method", C.c_int32), ("wind_dependent_snow_density", C.c_int32),
+                ("is_lake", C.c_int32)] + [(n, C.c_double) for n in (
+                    "int_snow_max", "overburden_compress_tfactor", "upplim_destruct_metamorph", "eta0_anderson",
+                    "eta0_vionnet", "ceta", "drift_gs", "rho_min", "rho_max", "tau_ref", "snw_rds_min",
+                    "snw_rds_max", "dzmin_1", "dzmin_2", "dzmax_l_1", "dzmax_l_2", "dzmax_u_1", "dzmax_u_2")]
+
+    @classmethod
+    def default(cls, ng=1):
+        """The reference's defaults (snow_hydrology.jl:43-63, 90-101; varctl.jl:79;
+        SNW_RDS_MAX, snow_snicar.jl:35; int_snow_max 2000 mm, clm_driver.jl:2154)."""
+        return cls(C.sizeof(cls), ng, 1, OVERBURDEN_ANDERSON1976, 0, 0, 2000.0, 0.08, 100.0, 9.0e5, 7.62237e6, 250.0,
+                   0.35, 50.0, 350.0, 172800.0, 54.526, 1500.0, 0.010, 0.015, 0.03, 0.07, 0.02, 0.05)
+
+
 # (name, ctype, kind, dims) ; kind: 'c' column, 'p' patch, 'l' landunit
 # dims: None = vector, else level-kind string
 _u8, _i64, _f64 = "u8", "i64", "f64"
@@ -401,6 +423,46 @@ SURFHYD_FIELDS = [
     ("h2osoi_liq", _f64, "c", "L"),
 ]
 
+# clmgb_snowlayer_fields (snow layer dynamics after the soil solve), header order
+SNOWLAYER_FIELDS = [
+    ("mask_snow", _u8, "c", None),
+    ("mask_nosnow", _u8, "c", None),
+    ("mask_nolakec", _u8, "c", None),
+    ("col_snl", _i64, "c", None),
+    ("col_landunit", _i64, "c", None),
+    ("col_gridcell", _i64, "c", None),
+    ("lun_itype", _i64, "l", None),
+    ("lun_lakpoi", _u8, "l", None),
+    ("lun_urbpoi", _u8, "l", None),
+    ("forc_wind", _f64, "g", None),
+    ("n_melt", _f64, "c", None),
+    ("frac_h2osfc", _f64, "c", None),
+    ("frac_sno", _f64, "c", None),
+    ("frac_sno_eff", _f64, "c", None),
+    ("int_snow", _f64, "c", None),
+    ("h2osno_no_layers", _f64, "c", None),
+    ("snow_depth", _f64, "c", None),
+    ("qflx_sl_top_soil", _f64, "c", None),
+    ("dz", _f64, "c", "L"),
+    ("z", _f64, "c", "L"),
+    ("zi", _f64, "c", "LZ"),
+    ("t_soisno", _f64, "c", "L"),
+    ("h2osoi_ice", _f64, "c", "L"),
+    ("h2osoi_liq", _f64, "c", "L"),
+    ("imelt", _i64, "c", "S"),
+    ("swe_old", _f64, "c", "S"),
+    ("frac_iceold", _f64, "c", "S"),
+    ("snw_rds", _f64, "c", "S"),
+    ("mss_bcphi", _f64, "c", "S"),
+    ("mss_bcpho", _f64, "c", "S"),
+    ("mss_ocphi", _f64, "c", "S"),
+    ("mss_ocpho", _f64, "c", "S"),
+    ("mss_dst1", _f64, "c", "S"),
+    ("mss_dst2", _f64, "c", "S"),
+    ("mss_dst3", _f64, "c", "S"),
+    ("mss_dst4", _f64, "c", "S"),
+]
+
 # clmgb_zd09_fields (soilwater_zengdecker2009!), header order
 ZD09_FIELDS = [
     ("mask_hydrology", _u8, "c", None),
@@ -455,6 +517,7 @@ SoilWaterFields = _mk_struct("SoilWaterFields", SOILWATER_FIELDS)
 RootSinkFields = _mk_struct("RootSinkFields", ROOTSINK_FIELDS)
 Zd09Fields = _mk_struct("Zd09Fields", ZD09_FIELDS)
 SurfHydFields = _mk_struct("SurfHydFields", SURFHYD_FIELDS)
+SnowLayerFields = _mk_struct("SnowLayerFields", SNOWLAYER_FIELDS)
 SoilFluxFields = _mk_struct("SoilFluxFields", SOILFLUX_FIELDS)
 
 

@@ -269,7 +269,7 @@ def balance_residuals(handle, state, dtime, t_grnd0, begwb, stream=None):
     return es, eh
 
 
-MATH_OPS = {"log": 0, "exp": 1, "pow": 2, "log10": 3, "sin": 4}
+MATH_OPS = {"log": 0, "exp": 1, "pow": 2, "log10": 3, "sin": 4, "acos": 5}
 
 
 def math_eval(handle, op, x, y=None, out=None, stream=None):

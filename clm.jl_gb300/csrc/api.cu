@@ -393,6 +393,57 @@ int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clm
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+// the pointers the selected stages read or write (clmgb_snow_layers)
+static bool snowlayer_pointers_ok(const clmgb_snowlayer_fields* f, const clmgb_snowlayer_config* cfg, uint32_t st) {
+  auto all = [](std::initializer_list<const void*> ps) {
+    for (const void* p : ps)
+      if (!p) return false;
+    return true;
+  };
+  const bool layers = st & (CLMGB_SL_COMPACTION | CLMGB_SL_COMBINE | CLMGB_SL_DIVIDE | CLMGB_SL_ZERO_EMPTY);
+  if (layers && !all({f->mask_snow, f->col_snl, f->dz, f->t_soisno, f->h2osoi_ice, f->h2osoi_liq})) return false;
+  if ((st & CLMGB_SL_COMPACTION) &&
+      !all({f->col_landunit, f->lun_lakpoi, f->lun_urbpoi, f->n_melt, f->frac_h2osfc, f->frac_sno, f->int_snow,
+            f->imelt, f->swe_old, f->frac_iceold}))
+    return false;
+  if ((st & CLMGB_SL_COMPACTION) && cfg->wind_dependent_snow_density && !all({f->col_gridcell, f->forc_wind}))
+    return false;
+  if ((st & (CLMGB_SL_COMBINE | CLMGB_SL_DIVIDE | CLMGB_SL_ZERO_EMPTY)) && !all({f->z, f->zi})) return false;
+  if ((st & (CLMGB_SL_COMBINE | CLMGB_SL_DIVIDE)) &&
+      !all({f->frac_sno, f->snw_rds, f->mss_bcphi, f->mss_bcpho, f->mss_ocphi, f->mss_ocpho, f->mss_dst1, f->mss_dst2,
+            f->mss_dst3, f->mss_dst4}))
+    return false;
+  if ((st & CLMGB_SL_COMBINE) &&
+      !all({f->col_landunit, f->lun_itype, f->lun_urbpoi, f->frac_sno_eff, f->int_snow, f->h2osno_no_layers,
+            f->snow_depth, f->qflx_sl_top_soil}))
+    return false;
+  if ((st & CLMGB_SL_FILTER) && !all({f->mask_snow, f->mask_nosnow, f->mask_nolakec, f->col_snl})) return false;
+  return true;
+}
+
+int32_t clmgb_snow_layers(clmgb_handle h, const clmgb_bounds* b, const clmgb_snowlayer_fields* f,
+                          const clmgb_snowlayer_config* cfg, uint32_t stages, double dtime, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (!cfg) return CLMGB_ERR_NULL_ARG;
+  if (cfg->struct_size != (int64_t)sizeof(clmgb_snowlayer_config)) return CLMGB_ERR_ABI;
+  if (stages & ~CLMGB_SL_ALL) return CLMGB_ERR_CONFIG;
+  // snow_compaction!'s error() on an unknown overburden method (snow_hydrology.jl:1373-1377)
+  if ((stages & CLMGB_SL_COMPACTION) && cfg->overburden_method != CLMGB_OVERBURDEN_ANDERSON1976 &&
+      cfg->overburden_method != CLMGB_OVERBURDEN_VIONNET2012)
+    return CLMGB_ERR_CONFIG;
+  if (cfg->ng < 0) return CLMGB_ERR_CONFIG;
+  int32_t e = check_bounds(b, false);
+  if (e) return e;
+  if (b->nc == 0 || stages == 0) return CLMGB_OK;
+  if (!f) return CLMGB_ERR_NULL_ARG;
+  if (f->struct_size != (int64_t)sizeof(clmgb_snowlayer_fields)) return CLMGB_ERR_ABI;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  if (!snowlayer_pointers_ok(f, cfg, stages)) return CLMGB_ERR_NULL_ARG;
+  cudaError_t ce = clmgb::launch_snow_layers(make_dims(h->vp, *b), b->nc, b->nl, *f, *cfg, stages, dtime,
+                                             h->dev_status, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
                                    void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
@@ -629,7 +680,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
 int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y, double* out,
                         void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
-  if (op < 0 || op > 4 || n < 0) return CLMGB_ERR_CONFIG;
+  if (op < 0 || op > 5 || n < 0) return CLMGB_ERR_CONFIG;
   if (n == 0) return CLMGB_OK;
   if (!x || !out || (op == 2 && !y)) return CLMGB_ERR_NULL_ARG;
   cudaError_t ce = clmgb::launch_math_eval(op, n, x, y, out, (cudaStream_t)stream);

@@ -1,4 +1,4 @@
-// clm_math.h — table-driven log/exp/pow/log10, and sin, in binary64 for C and CUDA alike.
+// clm_math.h — table-driven log/exp/pow/log10, and sin and acos, in binary64 for C and CUDA alike.
 //
 // Method: P. T. P. Tang's table-driven algorithms ("Table-driven implementation of
 // the exponential function in IEEE floating-point arithmetic", ACM TOMS 15(2),
@@ -19,6 +19,7 @@
 //   cm_pow(x, y):     relative error below (3 + |y| + |y*log(x)|) ulp (the product y*log(x)
 //                     is formed in binary64; at most ~3e-14 over the ranges the solve uses)
 //   cm_sin:           error below 1 ulp of max(|result|, 2^-53 |x|) for |x| < 2^20 pi/2
+//   cm_acos:          error below 1.5 ulp on [-1, 1]
 //                     (Cody-Waite reduction; the 2^-53 |x| term covers x near multiples of pi)
 #pragma once
 #include <stdint.h>
@@ -31,6 +32,7 @@
 #define CM_MUL(a, b) __dmul_rn((a), (b))
 #define CM_ADD(a, b) __dadd_rn((a), (b))
 #define CM_SUB(a, b) __dsub_rn((a), (b))
+#define CM_SQRT(a) __dsqrt_rn(a)
 #define CM_AS_U64(x) ((uint64_t)__double_as_longlong(x))
 #define CM_AS_F64(u) __longlong_as_double((long long)(u))
 #define CM_INF __longlong_as_double(0x7ff0000000000000LL)
@@ -46,6 +48,7 @@
 #define CM_MUL(a, b) ((a) * (b))
 #define CM_ADD(a, b) ((a) + (b))
 #define CM_SUB(a, b) ((a) - (b))
+#define CM_SQRT(a) sqrt(a)
 static inline uint64_t cm_as_u64_(double x) { uint64_t u; memcpy(&u, &x, 8); return u; }
 static inline double cm_as_f64_(uint64_t u) { double x; memcpy(&x, &u, 8); return x; }
 #define CM_AS_U64(x) cm_as_u64_(x)
@@ -199,4 +202,48 @@ CM_FN double cm_sin(double x) {
   const int q = (int)(k & 3);
   const double v = (q & 1) ? cm_cos_poly(r, lo) : cm_sin_poly(r, lo);
   return (q & 2) ? -v : v;
+}
+
+// asin(t) for |t| <= 1/2: t + t^3 P(t^2) (Taylor series, 27 terms).
+CM_FN double cm_asin_small(double t) {
+  const double z = CM_MUL(t, t);
+  double p = CM_ASIN_A27;
+  p = CM_FMA(z, p, CM_ASIN_A26);
+  p = CM_FMA(z, p, CM_ASIN_A25);
+  p = CM_FMA(z, p, CM_ASIN_A24);
+  p = CM_FMA(z, p, CM_ASIN_A23);
+  p = CM_FMA(z, p, CM_ASIN_A22);
+  p = CM_FMA(z, p, CM_ASIN_A21);
+  p = CM_FMA(z, p, CM_ASIN_A20);
+  p = CM_FMA(z, p, CM_ASIN_A19);
+  p = CM_FMA(z, p, CM_ASIN_A18);
+  p = CM_FMA(z, p, CM_ASIN_A17);
+  p = CM_FMA(z, p, CM_ASIN_A16);
+  p = CM_FMA(z, p, CM_ASIN_A15);
+  p = CM_FMA(z, p, CM_ASIN_A14);
+  p = CM_FMA(z, p, CM_ASIN_A13);
+  p = CM_FMA(z, p, CM_ASIN_A12);
+  p = CM_FMA(z, p, CM_ASIN_A11);
+  p = CM_FMA(z, p, CM_ASIN_A10);
+  p = CM_FMA(z, p, CM_ASIN_A9);
+  p = CM_FMA(z, p, CM_ASIN_A8);
+  p = CM_FMA(z, p, CM_ASIN_A7);
+  p = CM_FMA(z, p, CM_ASIN_A6);
+  p = CM_FMA(z, p, CM_ASIN_A5);
+  p = CM_FMA(z, p, CM_ASIN_A4);
+  p = CM_FMA(z, p, CM_ASIN_A3);
+  p = CM_FMA(z, p, CM_ASIN_A2);
+  p = CM_FMA(z, p, CM_ASIN_A1);
+  return CM_FMA(CM_MUL(t, z), p, t);
+}
+
+// Arc cosine for |x| <= 1 (NaN outside): pi/2 - asin(x) on |x| <= 1/2, else through
+// asin(sqrt((1 -+ x)/2)), whose argument is formed exactly ((1 -+ x) by Sterbenz, the
+// halving) and rounded once by the square root.
+CM_FN double cm_acos(double x) {
+  if (!(x >= -1.0 && x <= 1.0)) return CM_NAN;
+  if (x <= 0.5 && x >= -0.5) return CM_ADD(CM_PIO2_H, CM_SUB(CM_PIO2_L, cm_asin_small(x)));
+  if (x > 0.5) return CM_MUL(2.0, cm_asin_small(CM_SQRT(CM_MUL(0.5, CM_SUB(1.0, x)))));
+  const double a = CM_MUL(2.0, cm_asin_small(CM_SQRT(CM_MUL(0.5, CM_ADD(1.0, x)))));
+  return CM_ADD(CM_PI_HI, CM_SUB(CM_PI_LO, a));
 }

@@ -366,3 +366,34 @@ CM_TABLE(CM_EXP_T, 64) = {
 #define CM_COS_C6 (0x1.1eed8eff8d898p-29)
 #define CM_COS_C7 (-0x1.93974a8c07c9dp-37)
 #define CM_COS_C8 (0x1.ae7f3e733b81fp-45)
+#define CM_ASIN_A1 (0x1.5555555555555p-3)
+#define CM_ASIN_A2 (0x1.3333333333333p-4)
+#define CM_ASIN_A3 (0x1.6db6db6db6db7p-5)
+#define CM_ASIN_A4 (0x1.f1c71c71c71c7p-6)
+#define CM_ASIN_A5 (0x1.6e8ba2e8ba2e9p-6)
+#define CM_ASIN_A6 (0x1.1c4ec4ec4ec4fp-6)
+#define CM_ASIN_A7 (0x1.c99999999999ap-7)
+#define CM_ASIN_A8 (0x1.7a87878787878p-7)
+#define CM_ASIN_A9 (0x1.3fde50d79435ep-7)
+#define CM_ASIN_A10 (0x1.12ef3cf3cf3cfp-7)
+#define CM_ASIN_A11 (0x1.df3bd37a6f4dfp-8)
+#define CM_ASIN_A12 (0x1.a6863d70a3d71p-8)
+#define CM_ASIN_A13 (0x1.782dda12f684cp-8)
+#define CM_ASIN_A14 (0x1.51ba308d3dcb1p-8)
+#define CM_ASIN_A15 (0x1.31683bdef7bdfp-8)
+#define CM_ASIN_A16 (0x1.15ee9d45d1746p-8)
+#define CM_ASIN_A17 (0x1.fcaf8fb6db6dbp-9)
+#define CM_ASIN_A18 (0x1.d3d2a8e0dd67dp-9)
+#define CM_ASIN_A19 (0x1.b026f57b13b14p-9)
+#define CM_ASIN_A20 (0x1.90cb77f60c7cep-9)
+#define CM_ASIN_A21 (0x1.750de64d7d05fp-9)
+#define CM_ASIN_A22 (0x1.5c5f56efaaaabp-9)
+#define CM_ASIN_A23 (0x1.464c0950f7d47p-9)
+#define CM_ASIN_A24 (0x1.3275586c5f2f0p-9)
+#define CM_ASIN_A25 (0x1.208d3570ae5a6p-9)
+#define CM_ASIN_A26 (0x1.1052bc5fa960ap-9)
+#define CM_ASIN_A27 (0x1.018f963c229bfp-9)
+#define CM_PI_HI (0x1.921fb54442d18p+1)
+#define CM_PI_LO (0x1.1a62633145c07p-53)
+#define CM_PIO2_H (0x1.921fb54442d18p+0)
+#define CM_PIO2_L (0x1.1a62633145c07p-54)

@@ -21,6 +21,10 @@ mid with 33 significant bits, so k*hi and k*mid are exact for |k| < 2^20), then 
 Taylor polynomials of sin (to r^17) and cos (to r^16) on |r| <= pi/4, whose
 truncation errors are below 2^-60 relative.  DEG2RAD is RN(RN(pi) / 180), the binary64
 quotient that pi/180.0 gives.
+
+acos: asin's Taylor series on [0, 1/2] (27 terms), with acos(x) = pi/2 - asin(x) for
+|x| <= 1/2 and acos(x) = 2 asin(sqrt((1-x)/2)), pi - 2 asin(sqrt((1+x)/2)) beyond;
+pi and pi/2 in two parts.
 """
 import mpmath as mp
 
@@ -91,6 +95,17 @@ def main():
         lines.append("#define CM_SIN_S%d (%s)" % (k, hexd(mp.mpf((-1) ** k) / mp.factorial(2 * k + 1))))
     for k in range(2, 9):        # cos: (-1)^k / (2k)!
         lines.append("#define CM_COS_C%d (%s)" % (k, hexd(mp.mpf((-1) ** k) / mp.factorial(2 * k))))
+    # asin(t) = t + t^3 sum_k A_k t^(2k-2), A_k = (2k)! / (4^k (k!)^2 (2k+1)), k = 1..27:
+    # on |t| <= 1/2 the first omitted term is below 2^-58 relative
+    for k in range(1, 28):
+        a = mp.factorial(2 * k) / (mp.mpf(4) ** k * mp.factorial(k) ** 2 * (2 * k + 1))
+        lines.append("#define CM_ASIN_A%d (%s)" % (k, hexd(a)))
+    pi_hi = float(mp.pi)
+    lines.append("#define CM_PI_HI (%s)" % hexd(pi_hi))
+    lines.append("#define CM_PI_LO (%s)" % hexd(mp.pi - mp.mpf(pi_hi)))
+    p2 = float(mp.pi / 2)
+    lines.append("#define CM_PIO2_H (%s)" % hexd(p2))
+    lines.append("#define CM_PIO2_L (%s)" % hexd(mp.pi / 2 - mp.mpf(p2)))
     print("\n".join(lines))
 
 

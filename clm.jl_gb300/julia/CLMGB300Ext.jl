@@ -315,6 +315,88 @@ function CLM.update_urban_ponding!(ws, sh, wfb, col_snl, col_itype, mask_urban::
 end
 
 # ---------------------------------------------------------------------------
+# Snow layer dynamics after the soil solve (clm_driver.jl:2146-2200): each routine is one
+# stage of clmgb_snow_layers (the arrays a routine does not take stay NULL).
+# ---------------------------------------------------------------------------
+struct SnowLayerConfig
+    struct_size::Int64; ng::Int64
+    use_subgrid_fluxes::Int32; overburden_method::Int32; wind_dependent_snow_density::Int32; is_lake::Int32
+    int_snow_max::Float64; overburden_compress_tfactor::Float64; upplim_destruct_metamorph::Float64
+    eta0_anderson::Float64; eta0_vionnet::Float64; ceta::Float64; drift_gs::Float64; rho_min::Float64
+    rho_max::Float64; tau_ref::Float64; snw_rds_min::Float64; snw_rds_max::Float64
+    dzmin_1::Float64; dzmin_2::Float64; dzmax_l_1::Float64; dzmax_l_2::Float64; dzmax_u_1::Float64
+    dzmax_u_2::Float64
+end
+const SL = (compaction = 0x1, combine = 0x2, divide = 0x4, zero_empty = 0x8, filter = 0x10)
+const SNOWLAYER_MEMBERS = (
+    :mask_snow, :mask_nosnow, :mask_nolakec, :col_snl, :col_landunit, :col_gridcell, :lun_itype, :lun_lakpoi,
+    :lun_urbpoi, :forc_wind, :n_melt, :frac_h2osfc, :frac_sno, :frac_sno_eff, :int_snow, :h2osno_no_layers,
+    :snow_depth, :qflx_sl_top_soil, :dz, :z, :zi, :t_soisno, :h2osoi_ice, :h2osoi_liq, :imelt, :swe_old,
+    :frac_iceold, :snw_rds, :mss_bcphi, :mss_bcpho, :mss_ocphi, :mss_ocpho, :mss_dst1, :mss_dst2, :mss_dst3,
+    :mss_dst4)
+
+
+function snowlayer_config(; ng = 1, is_lake = false, use_subgrid_fluxes = CLM.varctl.use_subgrid_fluxes,
+                          int_snow_max = 2000.0)
+    p = CLM.snowhydrology_params
+    SnowLayerConfig(sizeof(SnowLayerConfig), ng, use_subgrid_fluxes, CLM.OVERBURDEN_COMPACTION_METHOD[],
+                    CLM.WIND_DEPENDENT_SNOW_DENSITY[], is_lake, int_snow_max, CLM.OVERBURDEN_COMPRESS_TFACTOR[],
+                    p.upplim_destruct_metamorph, p.eta0_anderson, p.eta0_vionnet, p.ceta, p.drift_gs, p.rho_min,
+                    p.rho_max, p.tau_ref, p.snw_rds_min, CLM.SNW_RDS_MAX, CLM.SNOW_DZMIN_1[], CLM.SNOW_DZMIN_2[],
+                    CLM.SNOW_DZMAX_L_1[], CLM.SNOW_DZMAX_L_2[], CLM.SNOW_DZMAX_U_1[], CLM.SNOW_DZMAX_U_2[])
+end
+
+function snow_layers!(stages, cfg::SnowLayerConfig, nc, ldc, nl, dtime; arrays...)
+    p = Ptr{Cvoid}[haskey(arrays, m) ? ptr(arrays[m]) : C_NULL for m in SNOWLAYER_MEMBERS]
+    f = fields_buffer(p)
+    GC.@preserve f begin
+        check(ccall((:clmgb_snow_layers, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{SnowLayerConfig}, UInt32, Float64, Ptr{Cvoid}),
+                    handle(), Bounds(nc, 0, nl, ldc, 0), f, cfg, UInt32(stages), Float64(dtime),
+                    CUDA.stream().handle), "clmgb_snow_layers")
+    end
+    nothing
+end
+
+aerosol_arrays(aer) = (mss_bcphi = aer.mss_bcphi_col, mss_bcpho = aer.mss_bcpho_col, mss_ocphi = aer.mss_ocphi_col,
+                       mss_ocpho = aer.mss_ocpho_col, mss_dst1 = aer.mss_dst1_col, mss_dst2 = aer.mss_dst2_col,
+                       mss_dst3 = aer.mss_dst3_col, mss_dst4 = aer.mss_dst4_col)
+
+function CLM.snow_compaction!(dz::CuArray, dtime, snl, t_soisno, h2osoi_ice, h2osoi_liq, imelt, frac_sno,
+                              frac_h2osfc, swe_old, int_snow, frac_iceold, forc_wind, col_gridcell, col_landunit,
+                              lakpoi, urbpoi, mask_snow, bounds, nlevsno; use_subgrid_fluxes::Bool = true,
+                              n_melt = CUDA.fill(20.0, length(snl)), int_snow_max::Real = 2000.0)
+    nc = length(snl)
+    snow_layers!(SL.compaction, snowlayer_config(ng = length(forc_wind); use_subgrid_fluxes, int_snow_max), nc,
+                 size(dz, 1), length(lakpoi), dtime; mask_snow, col_snl = snl, col_landunit, col_gridcell,
+                 lun_lakpoi = lakpoi, lun_urbpoi = urbpoi, forc_wind, n_melt = CuArray(Float64.(n_melt)),
+                 frac_h2osfc, frac_sno, int_snow, dz, t_soisno, h2osoi_ice, h2osoi_liq, imelt, swe_old, frac_iceold)
+end
+
+function CLM.combine_snow_layers!(snl::CuArray, dz, zi, z, t_soisno, h2osoi_ice, h2osoi_liq, h2osno_no_layers,
+                                  snow_depth, frac_sno, frac_sno_eff, int_snow, snw_rds, aerosol, lun_itype, urbpoi,
+                                  col_landunit, mask_snow, bounds, nlevsno, qflx_sl_top_soil, dtime)
+    snow_layers!(SL.combine, snowlayer_config(), length(snl), size(dz, 1), length(lun_itype), dtime;
+                 mask_snow, col_snl = snl, col_landunit, lun_itype, lun_urbpoi = urbpoi, frac_sno, frac_sno_eff,
+                 int_snow, h2osno_no_layers, snow_depth, qflx_sl_top_soil, dz, z, zi, t_soisno, h2osoi_ice,
+                 h2osoi_liq, snw_rds, aerosol_arrays(aerosol)...)
+end
+
+function CLM.divide_snow_layers!(snl::CuArray, dz, zi, z, t_soisno, h2osoi_ice, h2osoi_liq, frac_sno, snw_rds,
+                                 aerosol, is_lake::Bool, mask_snow, bounds, nlevsno)
+    snow_layers!(SL.divide, snowlayer_config(; is_lake), length(snl), size(dz, 1), 1, 1.0; mask_snow, col_snl = snl,
+                 frac_sno, dz, z, zi, t_soisno, h2osoi_ice, h2osoi_liq, snw_rds, aerosol_arrays(aerosol)...)
+end
+
+CLM.zero_empty_snow_layers!(snl::CuArray, dz, z, zi, t_soisno, h2osoi_ice, h2osoi_liq, mask_snow, bounds, nlevsno) =
+    snow_layers!(SL.zero_empty, snowlayer_config(), length(snl), size(dz, 1), 1, 1.0; mask_snow, col_snl = snl,
+                 dz, z, zi, t_soisno, h2osoi_ice, h2osoi_liq)
+
+CLM.build_snow_filter!(mask_snow::CuArray, mask_nosnow, snl, mask_nolake, bounds) =
+    snow_layers!(SL.filter, snowlayer_config(), length(snl), length(snl), 1, 1.0; mask_snow, mask_nosnow,
+                 mask_nolakec = mask_nolake, col_snl = snl)
+
+# ---------------------------------------------------------------------------
 # Reverse mode.  One column step's vector-Jacobian product (clmgb_column_step_vjp)
 # behind a ChainRulesCore.rrule and an Enzyme reverse rule, the counterparts of the
 # reference's _reverse_step_into! (canopy_fluxes_reverse.jl:447-465).  `StepState`

@@ -479,6 +479,91 @@ typedef struct clmgb_surfhyd_fields {
   double* h2osoi_liq;                 /* [ldc, L]  RW (top soil level of urban columns) */
 } clmgb_surfhyd_fields;
 
+/* ---- snow layer dynamics (clm_driver.jl:2146-2200) ----
+ * The snow-layer steps of clm_drv_core! after the soil solve, per column over the snow
+ * filter, selected by a mask of these bits and run in this order:                  */
+#define CLMGB_SL_COMPACTION  1u   /* snow_compaction! (snow_hydrology.jl:1203-1398, 1412-1500) */
+#define CLMGB_SL_COMBINE     2u   /* combine_snow_layers! (:1584-1926) with combo_scalar (:1960-2000) */
+#define CLMGB_SL_DIVIDE      4u   /* divide_snow_layers! (:2057-2286), mass_weighted_snow_radius (:2021-2031) */
+#define CLMGB_SL_ZERO_EMPTY  8u   /* zero_empty_snow_layers! (:2298-2329) */
+#define CLMGB_SL_FILTER     16u   /* build_snow_filter! (:2488-2510): snow/no-snow filters from snl */
+#define CLMGB_SL_ALL        31u
+
+#define CLMGB_OVERBURDEN_ANDERSON1976 1   /* snow_hydrology.jl:78-79 */
+#define CLMGB_OVERBURDEN_VIONNET2012  2
+
+/* The parameters and switches of those routines (SnowHydrologyParams, snow_hydrology.jl:43-63;
+ * the module switches :90-101; varctl.use_subgrid_fluxes). */
+typedef struct clmgb_snowlayer_config {
+  int64_t struct_size;                /* sizeof(clmgb_snowlayer_config) */
+  int64_t ng;                         /* gridcells: length of forc_wind */
+  int32_t use_subgrid_fluxes;         /* varctl.use_subgrid_fluxes (1) */
+  int32_t overburden_method;          /* OVERBURDEN_COMPACTION_METHOD (Anderson 1976) */
+  int32_t wind_dependent_snow_density;/* WIND_DEPENDENT_SNOW_DENSITY (0) */
+  int32_t is_lake;                    /* divide_snow_layers!'s is_lake (0 in clm_drv_core!) */
+  double  int_snow_max;               /* SCF int_snow_max (2000 mm) */
+  double  overburden_compress_tfactor;/* 0.08 1/K */
+  double  upplim_destruct_metamorph;  /* 100 kg/m3 */
+  double  eta0_anderson;              /* 9.0e5 kg s/m2 */
+  double  eta0_vionnet;               /* 7.62237e6 kg s/m2 */
+  double  ceta;                       /* 250 kg/m3 */
+  double  drift_gs;                   /* 0.35 */
+  double  rho_min;                    /* 50 kg/m3 */
+  double  rho_max;                    /* 350 kg/m3 */
+  double  tau_ref;                    /* 172800 s */
+  double  snw_rds_min;                /* 54.526 microns */
+  double  snw_rds_max;                /* SNW_RDS_MAX, 1500 microns */
+  double  dzmin_1;                    /* SNOW_DZMIN_1 (0.010 m) */
+  double  dzmin_2;                    /* SNOW_DZMIN_2 (0.015 m) */
+  double  dzmax_l_1;                  /* SNOW_DZMAX_L_1 (0.03 m) */
+  double  dzmax_l_2;                  /* SNOW_DZMAX_L_2 (0.07 m) */
+  double  dzmax_u_1;                  /* SNOW_DZMAX_U_1 (0.02 m) */
+  double  dzmax_u_2;                  /* SNOW_DZMAX_U_2 (0.05 m); deeper levels follow init_snow_layers! (:2357-2377) */
+} clmgb_snowlayer_config;
+
+/* Every field those routines read or write.  [ldc, S] arrays hold the nlevsno snow
+ * levels (CLM.jl's [nc, nlevsno] snow matrices, or the snow part of a longer one);
+ * [ldc, L] and [ldc, LZ] are the combined snow+soil arrays. */
+typedef struct clmgb_snowlayer_fields {
+  int64_t struct_size;                /* sizeof(clmgb_snowlayer_fields) */
+  uint8_t* mask_snow;                 /* [nc]  RW: filt.snowc (rebuilt by CLMGB_SL_FILTER) */
+  uint8_t* mask_nosnow;               /* [nc]  W: filt.nosnowc */
+  const uint8_t* mask_nolakec;        /* [nc]  filt.nolakec (CLMGB_SL_FILTER) */
+  int64_t* col_snl;                   /* [nc]  RW */
+  const int64_t* col_landunit;        /* [nc]  1-based */
+  const int64_t* col_gridcell;        /* [nc]  1-based */
+  const int64_t* lun_itype;           /* [nl] */
+  const uint8_t* lun_lakpoi;          /* [nl] */
+  const uint8_t* lun_urbpoi;          /* [nl] */
+  const double* forc_wind;            /* [ng] */
+  const double* n_melt;               /* [nc]  SCF melt shape parameter */
+  const double* frac_h2osfc;          /* [nc] */
+  double* frac_sno;                   /* [nc]  RW */
+  double* frac_sno_eff;               /* [nc]  RW */
+  double* int_snow;                   /* [nc]  RW */
+  double* h2osno_no_layers;           /* [nc]  W */
+  double* snow_depth;                 /* [nc]  W */
+  double* qflx_sl_top_soil;           /* [nc]  W */
+  double* dz;                         /* [ldc, L]  RW */
+  double* z;                          /* [ldc, L]  RW */
+  double* zi;                         /* [ldc, LZ] RW */
+  double* t_soisno;                   /* [ldc, L]  RW */
+  double* h2osoi_ice;                 /* [ldc, L]  RW (snow levels and soil level 1) */
+  double* h2osoi_liq;                 /* [ldc, L]  RW (snow levels and soil level 1) */
+  const int64_t* imelt;               /* [ldc, S] */
+  const double* swe_old;              /* [ldc, S] */
+  const double* frac_iceold;          /* [ldc, S] */
+  double* snw_rds;                    /* [ldc, S]  RW */
+  double* mss_bcphi;                  /* [ldc, S]  RW */
+  double* mss_bcpho;                  /* [ldc, S]  RW */
+  double* mss_ocphi;                  /* [ldc, S]  RW */
+  double* mss_ocpho;                  /* [ldc, S]  RW */
+  double* mss_dst1;                   /* [ldc, S]  RW */
+  double* mss_dst2;                   /* [ldc, S]  RW */
+  double* mss_dst3;                   /* [ldc, S]  RW */
+  double* mss_dst4;                   /* [ldc, S]  RW */
+} clmgb_snowlayer_fields;
+
 typedef struct clmgb_handle_s* clmgb_handle;
 
 /* ---- library / handle ---- */
@@ -533,7 +618,7 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
 int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc);
 int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value);
 
-/* Evaluates the library's binary64 log (op 0), exp (1), pow (2), log10 (3) or sin (4)
+/* Evaluates the library's binary64 log (op 0), exp (1), pow (2), log10 (3), sin (4) or acos (5)
  * elementwise on device arrays; y is read for pow only.  The oracle and the tests
  * use it to check that the GPU rounds exactly as the CPU build does. */
 int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y,
@@ -581,6 +666,18 @@ int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
  * range set CLMGB_COL_PATCH_RANGE in the device status and skip the column. */
 int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clmgb_surfhyd_fields* f,
                                 const clmgb_surfhyd_config* cfg, uint32_t stages, double dtime, void* stream);
+
+/* The snow layer dynamics of clm_drv_core! after the soil solve (clm_driver.jl:2146-2200),
+ * one thread per snow-filter column: the CLMGB_SL_* stages in `stages` run in order on
+ * the column's snow levels held on chip, with the results of the reference's calls one
+ * after another (the layer thresholds dzmin/dzmax_l/dzmax_u are built from the config
+ * as init_snow_layers! builds them).  Only the pointers of the selected stages are
+ * required (the arrays each reference routine takes).  An unknown overburden
+ * method -> CLMGB_ERR_CONFIG (the reference's error()); gridcell or landunit indices out
+ * of range, or snl outside -nlevsno..0, set CLMGB_COL_PATCH_RANGE / CLMGB_COL_LEVEL_RANGE
+ * in the device status and skip the column. */
+int32_t clmgb_snow_layers(clmgb_handle h, const clmgb_bounds* b, const clmgb_snowlayer_fields* f,
+                          const clmgb_snowlayer_config* cfg, uint32_t stages, double dtime, void* stream);
 
 /* soil_water! with the Zeng-Decker 2009 method (soilwater_zengdecker2009!,
  * soil_water_movement.jl:1616-1764): equilibrium matric potential from the water

@@ -40,6 +40,12 @@
  *     infiltration!                   src/biogeophys/soil_hydrology.jl:236-243
  *     total_surface_runoff!           src/biogeophys/soil_hydrology.jl:250-301,567-604
  *     update_urban_ponding!           src/biogeophys/soil_hydrology.jl:316-338
+ *   snow layer dynamics (clm_driver.jl:2146-2200), routine by routine:
+ *     snow_compaction!                src/biogeophys/snow_hydrology.jl:1203-1326,1412-1500
+ *     combine_snow_layers!, combo     :1584-1874, :1960-2000
+ *     divide_snow_layers!             :2021-2031, :2057-2237
+ *     zero_empty_snow_layers!         :2314-2329
+ *     build_snow_filter!              :2488-2510
  *
  * Transcendentals: the reference uses Julia Base's exp/log/pow/sin (openlibm for
  * log10); this file and the CUDA kernels share clm_math.h's binary64 versions, which
@@ -1389,6 +1395,404 @@ int orc_surface_hydrology(const clmgb_varpar* vp, const clmgb_bounds* b, const c
 }
 
 /* ===================================================================== */
+/* snow layer dynamics (clm_driver.jl:2146-2200), one loop per routine    */
+/* ===================================================================== */
+#define SNW_LSADZ 0.03
+#define SNW_ISTDLAK 5
+
+static void snw_combo(double* dz, double* wliq, double* wice, double* t, double dz2, double wliq2, double wice2,
+                      double t2)
+{
+  double dzc = *dz + dz2, wicec = *wice + wice2, wliqc = *wliq + wliq2;
+  double h = (CPICE * *wice + CPLIQ * *wliq) * (*t - TFRZ) + HFUS * *wliq;
+  double h2 = (CPICE * wice2 + CPLIQ * wliq2) * (t2 - TFRZ) + HFUS * wliq2;
+  double hc = h + h2;
+  double denom = CPICE * wicec + CPLIQ * wliqc;
+  double tc;
+  if (denom > 0.0) tc = TFRZ + (hc - HFUS * wliqc) / denom;
+  else tc = TFRZ;
+  *dz = dzc;
+  *wice = wicec;
+  *wliq = wliqc;
+  *t = tc;
+}
+
+static double snw_radius(double rds1, double rds2, double swtot, double zwtot, double rmin, double rmax)
+{
+  double total_wt = swtot + zwtot;
+  double r = total_wt > 0.0 ? (rds2 * swtot + rds1 * zwtot) / total_wt : 0.5 * (rds1 + rds2);
+  return r > rmax ? rmax : (r < rmin ? rmin : r);           /* Julia clamp */
+}
+
+int orc_snow_layers(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_snowlayer_fields* f,
+                    const clmgb_snowlayer_config* cfg, uint32_t stages, double dtime)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  const int64_t nc = b->nc, ld = b->ldc;
+  const int ns = vp->nlevsno;
+  if ((stages & CLMGB_SL_COMPACTION) && cfg->overburden_method != CLMGB_OVERBURDEN_ANDERSON1976 &&
+      cfg->overburden_method != CLMGB_OVERBURDEN_VIONNET2012)
+    return -1;
+  /* init_snow_layers! thresholds (snow_hydrology.jl:2357-2377), 1-based like the reference */
+  double dzmin[ORC_MAXL + 1], dzmax_l[ORC_MAXL + 1], dzmax_u[ORC_MAXL + 1];
+  memset(dzmin, 0, sizeof dzmin);
+  memset(dzmax_l, 0, sizeof dzmax_l);
+  memset(dzmax_u, 0, sizeof dzmax_u);
+  dzmin[1] = cfg->dzmin_1; dzmax_l[1] = cfg->dzmax_l_1; dzmax_u[1] = cfg->dzmax_u_1;
+  dzmin[2] = cfg->dzmin_2; dzmax_l[2] = cfg->dzmax_l_2; dzmax_u[2] = cfg->dzmax_u_2;
+  for (int j = 3; j <= ns; j++) {
+    dzmin[j] = dzmax_u[j - 1] * 0.5;
+    dzmax_u[j] = 2.0 * dzmax_u[j - 1] + 0.01;
+    dzmax_l[j] = dzmax_u[j] + dzmax_l[j - 1];
+    if (j == ns) { dzmax_u[j] = 1.7976931348623157e308; dzmax_l[j] = 1.7976931348623157e308; }
+  }
+  double* aer[8] = {f->mss_bcphi, f->mss_bcpho, f->mss_ocphi, f->mss_ocpho,
+                    f->mss_dst1, f->mss_dst2, f->mss_dst3, f->mss_dst4};
+
+  /* snow_compaction! (_snowhyd_compaction_kernel!, :1203-1326) */
+  if (stages & CLMGB_SL_COMPACTION)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_snow[c]) continue;
+      const double c3 = 2.777e-6, c4 = 0.04, c5 = 2.0;
+      double burden = 0.0, zpseudo = 0.0;
+      int mobile = 1;
+      for (int j = -ns + 1; j <= 0; j++) {
+        if (!(j >= f->col_snl[c] + 1)) continue;
+        int jj = j + ns;
+        double wx = IX(f->h2osoi_ice, c, jj, ld) + IX(f->h2osoi_liq, c, jj, ld);
+        double voidv = 1.0 - (IX(f->h2osoi_ice, c, jj, ld) / DENICE + IX(f->h2osoi_liq, c, jj, ld) / DENH2O) /
+                                 (f->frac_sno[c] * IX(f->dz, c, jj, ld));
+        if (voidv > 0.001 && IX(f->h2osoi_ice, c, jj, ld) > 0.1) {
+          double bi = IX(f->h2osoi_ice, c, jj, ld) / (f->frac_sno[c] * IX(f->dz, c, jj, ld));
+          double fi = IX(f->h2osoi_ice, c, jj, ld) / wx;
+          double td = TFRZ - IX(f->t_soisno, c, jj, ld);
+          double dexpf = cm_exp(-c4 * td);
+          double ddz1 = -c3 * dexpf;
+          if (bi > cfg->upplim_destruct_metamorph)
+            ddz1 = ddz1 * cm_exp(-46.0e-3 * (bi - cfg->upplim_destruct_metamorph));
+          if (IX(f->h2osoi_liq, c, jj, ld) > 0.01 * IX(f->dz, c, jj, ld) * f->frac_sno[c]) ddz1 = ddz1 * c5;
+          double ddz2;
+          if (cfg->overburden_method == CLMGB_OVERBURDEN_ANDERSON1976) {
+            double c2 = 23.0e-3;
+            ddz2 = -(burden + wx / 2.0) * cm_exp(-cfg->overburden_compress_tfactor * td - c2 * bi) /
+                   cfg->eta0_anderson;
+          } else {
+            double f1 = 1.0 / (1.0 + 60.0 * IX(f->h2osoi_liq, c, jj, ld) / (DENH2O * IX(f->dz, c, jj, ld)));
+            double f2 = 4.0;
+            double eta = f1 * f2 * (bi / cfg->ceta) * cm_exp(0.1 * td + 0.023 * bi) * cfg->eta0_vionnet;
+            ddz2 = -(burden + wx / 2.0) / eta;
+          }
+          double ddz3;
+          if (IX(f->imelt, c, jj, ld) == 1) {
+            int64_t l = f->col_landunit[c] - 1;
+            if (cfg->use_subgrid_fluxes && !f->lun_lakpoi[l] && !f->lun_urbpoi[l]) {
+              ddz3 = jl_max(0.0, jl_min(1.0, (IX(f->swe_old, c, jj, ld) - wx) / wx));
+              if ((IX(f->swe_old, c, jj, ld) - wx) > 0.0) {
+                double wsum = 0.0;
+                for (int64_t jj2 = f->col_snl[c] + 1; jj2 <= 0; jj2++)
+                  wsum += IX(f->h2osoi_liq, c, jj2 + ns, ld) + IX(f->h2osoi_ice, c, jj2 + ns, ld);
+                double int_snow_lim = jl_min(f->int_snow[c], cfg->int_snow_max);
+                double fsno_melt;
+                if (int_snow_lim > 0.0) {
+                  double smr = jl_min(1.0, wsum / int_snow_lim);
+                  fsno_melt = 1.0 - cm_pow(cm_acos(jl_min(1.0, 2.0 * smr - 1.0)) / 3.14159265358979323846,
+                                           f->n_melt[c]);
+                } else {
+                  fsno_melt = 1.0;
+                }
+                if ((fsno_melt + f->frac_h2osfc[c]) > 1.0) fsno_melt = 1.0 - f->frac_h2osfc[c];
+                ddz3 = ddz3 - jl_max(0.0, (fsno_melt - f->frac_sno[c]) / f->frac_sno[c]);
+              }
+              ddz3 = -1.0 / dtime * ddz3;
+            } else {
+              ddz3 = -1.0 / dtime * jl_max(0.0, (IX(f->frac_iceold, c, jj, ld) - fi) / IX(f->frac_iceold, c, jj, ld));
+            }
+          } else {
+            ddz3 = 0.0;
+          }
+          double ddz4_val = 0.0;
+          if (cfg->wind_dependent_snow_density) {
+            /* _wind_drift_compaction_dev (:1466-1500) */
+            if (mobile) {
+              double forc_wind = f->forc_wind[f->col_gridcell[c] - 1], dzj = IX(f->dz, c, jj, ld);
+              double Frho = 1.25 - 0.0042 * (jl_max(cfg->rho_min, bi) - cfg->rho_min);
+              double MO = 0.34 * (-0.583 * cfg->drift_gs - 0.833 * 1.0 + 0.833) + 0.66 * Frho;
+              double SI = -2.868 * cm_exp(-0.085 * forc_wind) + 1.0 + MO;
+              if (SI > 0.0) {
+                SI = jl_min(SI, 3.25);
+                double zp = zpseudo + 0.5 * dzj * (3.25 - SI);
+                double gamma_drift = SI * cm_exp(-zp / 0.1);
+                double tau_inverse = gamma_drift / cfg->tau_ref;
+                ddz4_val = -jl_max(0.0, cfg->rho_max - bi) * tau_inverse;
+                zp = zp + 0.5 * dzj * (3.25 - SI);
+                zpseudo = zp;
+                mobile = 1;
+              } else {
+                ddz4_val = 0.0;
+                mobile = 0;
+              }
+            } else {
+              ddz4_val = 0.0;
+              mobile = 0;
+            }
+          }
+          double pdzdtc = ddz1 + ddz2 + ddz3 + ddz4_val;
+          IX(f->dz, c, jj, ld) = jl_max(IX(f->dz, c, jj, ld) * (1.0 + pdzdtc * dtime),
+                                        (IX(f->h2osoi_ice, c, jj, ld) / DENICE + IX(f->h2osoi_liq, c, jj, ld) / DENH2O) /
+                                            f->frac_sno[c]);
+        } else {
+          mobile = 0;
+        }
+        burden = burden + wx;
+      }
+    }
+
+  /* combine_snow_layers! (_snowhyd_combine_kernel!, :1584-1874) */
+  if (stages & CLMGB_SL_COMBINE)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_snow[c]) continue;
+      int64_t* snl = (int64_t*)&f->col_snl[c];
+      f->qflx_sl_top_soil[c] = 0.0;
+      int64_t msn_old = *snl;
+      int64_t j = msn_old + 1;
+      while (j <= 0) {
+        int64_t jj = j + ns;
+        if (IX(f->h2osoi_ice, c, jj, ld) <= 0.01) {
+          int64_t l = f->col_landunit[c] - 1;
+          int64_t ltype = f->lun_itype[l];
+          if (j < 0 || (ltype == ISTSOIL || f->lun_urbpoi[l] || ltype == ISTCROP)) {
+            IX(f->h2osoi_liq, c, jj + 1, ld) += IX(f->h2osoi_liq, c, jj, ld);
+            IX(f->h2osoi_ice, c, jj + 1, ld) += IX(f->h2osoi_ice, c, jj, ld);
+          }
+          if (j == 0) f->qflx_sl_top_soil[c] = (IX(f->h2osoi_liq, c, jj, ld) + IX(f->h2osoi_ice, c, jj, ld)) / dtime;
+          if (j < 0) {
+            IX(f->dz, c, jj + 1, ld) += IX(f->dz, c, jj, ld);
+            for (int a = 0; a < 8; a++) IX(aer[a], c, jj + 1, ld) += IX(aer[a], c, jj, ld);
+          }
+          if (j > *snl + 1 && *snl < -1)
+            for (int64_t i = j; i >= *snl + 2; i--) {
+              int64_t ii = i + ns, ia = i - 1 + ns;
+              IX(f->h2osoi_liq, c, ii, ld) = IX(f->h2osoi_liq, c, ia, ld);
+              IX(f->h2osoi_ice, c, ii, ld) = IX(f->h2osoi_ice, c, ia, ld);
+              IX(f->t_soisno, c, ii, ld) = IX(f->t_soisno, c, ia, ld);
+              IX(f->dz, c, ii, ld) = IX(f->dz, c, ia, ld);
+              for (int a = 0; a < 8; a++) IX(aer[a], c, ii, ld) = IX(aer[a], c, ia, ld);
+              IX(f->snw_rds, c, ii, ld) = IX(f->snw_rds, c, ia, ld);
+            }
+          *snl = *snl + 1;
+        }
+        j += 1;
+      }
+      double snow_depth_acc = 0.0, h2osno_total = 0.0;
+      for (int64_t jl = *snl + 1; jl <= 0; jl++) {
+        snow_depth_acc += IX(f->dz, c, jl + ns, ld);
+        h2osno_total += IX(f->h2osoi_ice, c, jl + ns, ld) + IX(f->h2osoi_liq, c, jl + ns, ld);
+      }
+      f->snow_depth[c] = snow_depth_acc;
+      if (f->snow_depth[c] > 0.0) {
+        int64_t l = f->col_landunit[c] - 1;
+        int64_t ltype = f->lun_itype[l];
+        int all_gone = (ltype == SNW_ISTDLAK && f->snow_depth[c] < dzmin[1] + SNW_LSADZ) ||
+                       (ltype != SNW_ISTDLAK && (f->frac_sno_eff[c] * f->snow_depth[c] < dzmin[1] ||
+                                                 h2osno_total / (f->frac_sno_eff[c] * f->snow_depth[c]) < 50.0));
+        if (all_gone) {
+          double zwice = 0.0, zwliq = 0.0;
+          for (int64_t jl = *snl + 1; jl <= 0; jl++) {
+            zwice += IX(f->h2osoi_ice, c, jl + ns, ld);
+            zwliq += IX(f->h2osoi_liq, c, jl + ns, ld);
+          }
+          f->h2osno_no_layers[c] = zwice;
+          if (ltype == ISTSOIL || f->lun_urbpoi[l] || ltype == ISTCROP) IX(f->h2osoi_liq, c, ns + 1, ld) += zwliq;
+          *snl = 0;
+          h2osno_total = f->h2osno_no_layers[c];
+          for (int jj = 1; jj <= ns; jj++)
+            for (int a = 0; a < 8; a++) IX(aer[a], c, jj, ld) = 0.0;
+          if (f->h2osno_no_layers[c] <= 0.0) f->snow_depth[c] = 0.0;
+        }
+      }
+      if (h2osno_total <= 0.0) {
+        f->snow_depth[c] = 0.0;
+        f->frac_sno[c] = 0.0;
+        f->frac_sno_eff[c] = 0.0;
+        f->int_snow[c] = 0.0;
+      }
+      if (*snl < -1) {
+        int mssi = 1;
+        int64_t i = *snl + 1;
+        while (i <= 0) {
+          int64_t ji = i + ns;
+          int thin = (f->frac_sno_eff[c] * IX(f->dz, c, ji, ld) < dzmin[mssi]) ||
+                     ((IX(f->h2osoi_ice, c, ji, ld) + IX(f->h2osoi_liq, c, ji, ld)) /
+                          (f->frac_sno_eff[c] * IX(f->dz, c, ji, ld)) < 50.0);
+          if (thin) {
+            int64_t neibor;
+            if (i == *snl + 1) neibor = i + 1;
+            else if (i == 0) neibor = i - 1;
+            else {
+              neibor = i + 1;
+              if ((IX(f->dz, c, ji - 1, ld) + IX(f->dz, c, ji, ld)) < (IX(f->dz, c, ji + 1, ld) + IX(f->dz, c, ji, ld)))
+                neibor = i - 1;
+            }
+            int64_t j_keep, l_remove;
+            if (neibor > i) { j_keep = neibor; l_remove = i; }
+            else { j_keep = i; l_remove = neibor; }
+            int64_t jk = j_keep + ns, jr = l_remove + ns;
+            for (int a = 0; a < 8; a++) IX(aer[a], c, jk, ld) += IX(aer[a], c, jr, ld);
+            double total_mass = IX(f->h2osoi_liq, c, jk, ld) + IX(f->h2osoi_ice, c, jk, ld) +
+                                IX(f->h2osoi_liq, c, jr, ld) + IX(f->h2osoi_ice, c, jr, ld);
+            if (total_mass > 0.0)
+              IX(f->snw_rds, c, jk, ld) =
+                  (IX(f->snw_rds, c, jk, ld) * (IX(f->h2osoi_liq, c, jk, ld) + IX(f->h2osoi_ice, c, jk, ld)) +
+                   IX(f->snw_rds, c, jr, ld) * (IX(f->h2osoi_liq, c, jr, ld) + IX(f->h2osoi_ice, c, jr, ld))) /
+                  total_mass;
+            snw_combo(&IX(f->dz, c, jk, ld), &IX(f->h2osoi_liq, c, jk, ld), &IX(f->h2osoi_ice, c, jk, ld),
+                      &IX(f->t_soisno, c, jk, ld), IX(f->dz, c, jr, ld), IX(f->h2osoi_liq, c, jr, ld),
+                      IX(f->h2osoi_ice, c, jr, ld), IX(f->t_soisno, c, jr, ld));
+            if (j_keep - 1 > *snl + 1)
+              for (int64_t k = j_keep - 1; k >= *snl + 2; k--) {
+                int64_t kk = k + ns, ka = k - 1 + ns;
+                IX(f->h2osoi_ice, c, kk, ld) = IX(f->h2osoi_ice, c, ka, ld);
+                IX(f->h2osoi_liq, c, kk, ld) = IX(f->h2osoi_liq, c, ka, ld);
+                IX(f->t_soisno, c, kk, ld) = IX(f->t_soisno, c, ka, ld);
+                IX(f->dz, c, kk, ld) = IX(f->dz, c, ka, ld);
+                for (int a = 0; a < 8; a++) IX(aer[a], c, kk, ld) = IX(aer[a], c, ka, ld);
+                IX(f->snw_rds, c, kk, ld) = IX(f->snw_rds, c, ka, ld);
+              }
+            *snl = *snl + 1;
+            if (*snl >= -1) break;
+          } else {
+            mssi = mssi + 1;
+          }
+          i += 1;
+        }
+      }
+      for (int64_t jl = 0; jl >= -ns + 1; jl--) {
+        int64_t jj = jl + ns;
+        if (jl >= *snl + 1) {
+          IX(f->z, c, jj, ld) = IX(f->zi, c, jj + 1, ld) - 0.5 * IX(f->dz, c, jj, ld);
+          IX(f->zi, c, jj, ld) = IX(f->zi, c, jj + 1, ld) - IX(f->dz, c, jj, ld);
+        }
+      }
+    }
+
+  /* divide_snow_layers! (_snowhyd_divide_kernel!, :2057-2237) */
+  if (stages & CLMGB_SL_DIVIDE)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_snow[c]) continue;
+      double dzsno[ORC_MAXL + 2], swice[ORC_MAXL + 2], swliq[ORC_MAXL + 2], tsno[ORC_MAXL + 2], rds[ORC_MAXL + 2];
+      double ma[8][ORC_MAXL + 2];
+      memset(dzsno, 0, sizeof dzsno); memset(swice, 0, sizeof swice); memset(swliq, 0, sizeof swliq);
+      memset(tsno, 0, sizeof tsno); memset(rds, 0, sizeof rds); memset(ma, 0, sizeof ma);
+      const int is_lake = cfg->is_lake != 0;
+      int64_t snl = f->col_snl[c];
+      int64_t msno = snl < 0 ? -snl : snl;
+      for (int64_t k = 1; k <= msno; k++) {
+        int64_t jj = (k + snl) + ns;
+        dzsno[k] = is_lake ? IX(f->dz, c, jj, ld) : f->frac_sno[c] * IX(f->dz, c, jj, ld);
+        swice[k] = IX(f->h2osoi_ice, c, jj, ld);
+        swliq[k] = IX(f->h2osoi_liq, c, jj, ld);
+        tsno[k] = IX(f->t_soisno, c, jj, ld);
+        for (int a = 0; a < 8; a++) ma[a][k] = IX(aer[a], c, jj, ld);
+        rds[k] = IX(f->snw_rds, c, jj, ld);
+      }
+      int64_t k = 1;
+      while (k <= msno && k < ns) {
+        if (k == msno) {
+          double offset = is_lake ? 2.0 * SNW_LSADZ : 0.0;
+          if (dzsno[k] > dzmax_l[k] + offset) {
+            msno += 1;
+            dzsno[k] /= 2.0; dzsno[k + 1] = dzsno[k];
+            swice[k] /= 2.0; swice[k + 1] = swice[k];
+            swliq[k] /= 2.0; swliq[k + 1] = swliq[k];
+            if (k == 1) {
+              tsno[k + 1] = tsno[k];
+            } else {
+              double dtdz = (tsno[k - 1] - tsno[k]) / ((dzsno[k - 1] + 2.0 * dzsno[k]) / 2.0);
+              double tsno_kp1_candidate = tsno[k] - dtdz * dzsno[k] / 2.0;
+              double tsno_k_candidate = tsno[k] + dtdz * dzsno[k] / 2.0;
+              double w_frozen = (TFRZ - tsno_kp1_candidate) >= 0.0 ? 1.0 : 0.0;
+              tsno[k + 1] = w_frozen * tsno_kp1_candidate + (1.0 - w_frozen) * tsno[k];
+              tsno[k] = w_frozen * tsno_k_candidate + (1.0 - w_frozen) * tsno[k];
+            }
+            for (int a = 0; a < 8; a++) { ma[a][k] /= 2.0; ma[a][k + 1] = ma[a][k]; }
+            rds[k + 1] = rds[k];
+          }
+        }
+        if (k < msno) {
+          double offset = is_lake ? SNW_LSADZ : 0.0;
+          if (dzsno[k] > dzmax_u[k] + offset) {
+            double drr = dzsno[k] - dzmax_u[k] - offset;
+            double propor = drr / dzsno[k];
+            double zwice = propor * swice[k], zwliq = propor * swliq[k], zm[8];
+            for (int a = 0; a < 8; a++) zm[a] = propor * ma[a][k];
+            double propor_keep = (dzmax_u[k] + offset) / dzsno[k];
+            swice[k] *= propor_keep;
+            swliq[k] *= propor_keep;
+            for (int a = 0; a < 8; a++) ma[a][k] *= propor_keep;
+            dzsno[k] = dzmax_u[k] + offset;
+            for (int a = 0; a < 8; a++) ma[a][k + 1] += zm[a];
+            rds[k + 1] = snw_radius(rds[k], rds[k + 1], swliq[k + 1] + swice[k + 1], zwliq + zwice,
+                                    cfg->snw_rds_min, cfg->snw_rds_max);
+            snw_combo(&dzsno[k + 1], &swliq[k + 1], &swice[k + 1], &tsno[k + 1], drr, zwliq, zwice, tsno[k]);
+          }
+        }
+        k += 1;
+      }
+      f->col_snl[c] = -msno;
+      snl = f->col_snl[c];
+      for (int64_t jl = -ns + 1; jl <= 0; jl++) {
+        int64_t jj = jl + ns;
+        if (jl >= snl + 1) {
+          int64_t ki = jl - snl;
+          IX(f->dz, c, jj, ld) = is_lake ? dzsno[ki] : dzsno[ki] / f->frac_sno[c];
+          IX(f->h2osoi_ice, c, jj, ld) = swice[ki];
+          IX(f->h2osoi_liq, c, jj, ld) = swliq[ki];
+          IX(f->t_soisno, c, jj, ld) = tsno[ki];
+          for (int a = 0; a < 8; a++) IX(aer[a], c, jj, ld) = ma[a][ki];
+          IX(f->snw_rds, c, jj, ld) = rds[ki];
+        }
+      }
+      for (int64_t jl = 0; jl >= -ns + 1; jl--) {
+        int64_t jj = jl + ns;
+        if (jl >= snl + 1) {
+          IX(f->z, c, jj, ld) = IX(f->zi, c, jj + 1, ld) - 0.5 * IX(f->dz, c, jj, ld);
+          IX(f->zi, c, jj, ld) = IX(f->zi, c, jj + 1, ld) - IX(f->dz, c, jj, ld);
+        }
+      }
+    }
+
+  /* zero_empty_snow_layers! (:2314-2329) */
+  if (stages & CLMGB_SL_ZERO_EMPTY)
+    for (int64_t c = 0; c < nc; c++) {
+      if (!f->mask_snow[c]) continue;
+      for (int jj = 1; jj <= ns; jj++) {
+        int64_t j = jj - ns;
+        if (j <= f->col_snl[c] && f->col_snl[c] > -ns) {
+          IX(f->h2osoi_ice, c, jj, ld) = 0.0;
+          IX(f->h2osoi_liq, c, jj, ld) = 0.0;
+          IX(f->t_soisno, c, jj, ld) = 0.0;
+          IX(f->dz, c, jj, ld) = 0.0;
+          IX(f->z, c, jj, ld) = 0.0;
+          IX(f->zi, c, jj, ld) = 0.0;
+        }
+      }
+    }
+
+  /* build_snow_filter! (:2488-2510) */
+  if (stages & CLMGB_SL_FILTER)
+    for (int64_t c = 0; c < nc; c++) {
+      f->mask_snow[c] = 0;
+      f->mask_nosnow[c] = 0;
+      if (f->mask_nolakec[c]) {
+        if (f->col_snl[c] < 0) f->mask_snow[c] = 1;
+        else f->mask_nosnow[c] = 1;
+      }
+    }
+  return 0;
+}
+
+/* ===================================================================== */
 /* soil_fluxes! (soil_fluxes.jl:553-697), loop by loop                    */
 /* ===================================================================== */
 int orc_soil_fluxes(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_soilflux_fields* f, double dtime)
@@ -2314,3 +2718,4 @@ double orc_cm_exp(double x) { return cm_exp(x); }
 double orc_cm_pow(double x, double y) { return cm_pow(x, y); }
 double orc_cm_log10(double x) { return cm_log10(x); }
 double orc_cm_sin(double x) { return cm_sin(x); }
+double orc_cm_acos(double x) { return cm_acos(x); }

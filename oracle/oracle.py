@@ -38,6 +38,7 @@ def lib():
         L.orc_soil_water_zd09.argtypes = [P, P, P, C.c_double, C.c_double]
         L.orc_soil_fluxes.argtypes = [P, P, P, C.c_double]
         L.orc_surface_hydrology.argtypes = [P, P, P, P, C.c_uint32, C.c_double]
+        L.orc_snow_layers.argtypes = [P, P, P, P, C.c_uint32, C.c_double]
         L.orc_soil_water.argtypes = [P, P, P, P, C.c_double, P, P, P, C.c_int32]
         L.orc_run_steps.argtypes = [P, P, P, P, P, C.c_double, C.c_int32, C.c_int32, P, P,
                                     C.c_int64, P, P, P, C.c_int32]
@@ -99,6 +100,12 @@ def rootsink(rs, use_hydrstress=False):
 def soil_fluxes(fs, dtime):
     """soil_fluxes! in place on a host SoilFluxState."""
     _chk(lib().orc_soil_fluxes(C.byref(fs.vp), C.byref(fs.bounds()), C.byref(fs.fields()), float(dtime)))
+
+
+def snow_layers(sl, dtime, cfg, stages):
+    """The snow-layer routines selected by `stages`, in place on a host SnowLayerState."""
+    _chk(lib().orc_snow_layers(C.byref(sl.vp), C.byref(sl.bounds()), C.byref(sl.fields()), C.byref(cfg),
+                               int(stages), float(dtime)))
 
 
 def surface_hydrology(sh, dtime, cfg, stages):

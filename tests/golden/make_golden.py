@@ -198,6 +198,42 @@ def surface_hydrology_cases():
     return dict(cases=out)
 
 
+def snow_layer_cases():
+    """Known answers of test/test_snow_hydrology.jl for the snow-layer routines, each
+    through the public routine that uses it.  "snow" level values are listed from the
+    bottom snow level up (j = 0, -1, ...); every column has the same values."""
+    TFRZ = 273.15
+    out = []
+
+    def case(name, src, stages, nc, snl, snow, col, expect):
+        out.append(dict(name=name, source=src, stages=stages, nc=nc, snl=snl, snow=snow, col=col, expect=expect))
+
+    case("zero_empty_interface_regression", "test/test_snow_hydrology.jl:264-286", ["zero_empty_snow_layers!"], 1,
+         [-1], dict(all_levels=dict(dz=0.1, z=-0.05, zi=-0.1, t_soisno=TFRZ - 2.0, h2osoi_ice=1.0, h2osoi_liq=0.5)),
+         {}, [dict(what="top_level_zero", fields=["h2osoi_ice", "h2osoi_liq", "zi"])])
+    # combo_scalar's answer (:421-433) through combine_snow_layers!: the top layer is
+    # thinner than dzmin (frac_sno_eff * dz = 0.009 < 0.01) and merges into the one below
+    t1, t2 = TFRZ - 5.0, TFRZ - 10.0
+    case("combine_merges_thin_top_layer", "test/test_snow_hydrology.jl:421-433", ["combine_snow_layers!"], 1, [-2],
+         dict(dz=[0.05, 0.03], h2osoi_liq=[2.0, 1.0], h2osoi_ice=[8.0, 5.0], t_soisno=[t2, t1]),
+         dict(frac_sno=0.3, frac_sno_eff=0.3, int_snow=100.0),
+         [dict(what="snl", value=-1), dict(what="bottom", field="dz", value=0.08),
+          dict(what="bottom", field="h2osoi_liq", value=3.0), dict(what="bottom", field="h2osoi_ice", value=13.0),
+          dict(what="bottom_below", field="t_soisno", value=TFRZ)])
+    # mass_weighted_snow_radius's answers (:435-447) through divide_snow_layers!: the top
+    # layer (0.04 m > dzmax_u 0.02 m) hands half its 10 kg/m2 to the layer below (5 kg/m2)
+    for name, r1, r2, want in (("radius_weighted", 100.0, 200.0, 150.0), ("radius_clamped_min", 10.0, 20.0, 54.526),
+                               ("radius_clamped_max", 2000.0, 2000.0, 1500.0)):
+        case("divide_" + name, "test/test_snow_hydrology.jl:435-447", ["divide_snow_layers!"], 1, [-2],
+             dict(dz=[0.03, 0.04], h2osoi_liq=[0.0, 0.0], h2osoi_ice=[5.0, 10.0], t_soisno=[TFRZ - 3.0] * 2,
+                  snw_rds=[r2, r1]),
+             dict(frac_sno=1.0, frac_sno_eff=1.0, int_snow=100.0),
+             [dict(what="snl", value=-2), dict(what="bottom", field="snw_rds", value=want, exact=name != "radius_weighted")])
+    case("build_snow_filter", "test/test_snow_hydrology.jl:451-465", ["build_snow_filter!"], 4, [-2, 0, -1, 0], {}, {},
+         [dict(what="masks", mask_snow=[1, 0, 1, 0], mask_nosnow=[0, 1, 0, 1])])
+    return dict(cases=out)
+
+
 def soil_fluxes_cases():
     """test/test_soil_fluxes.jl: one soil patch on one column, the inputs of its three
     scenarios (level values are the same on every level) and the properties it checks."""
@@ -372,6 +408,7 @@ def main():
     cases["rootsink"] = rootsink_cases()
     cases["soil_fluxes"] = soil_fluxes_cases()
     cases["surface_hydrology"] = surface_hydrology_cases()
+    cases["snow_layers"] = snow_layer_cases()
     with open(os.path.join(HERE, "reference_cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1, sort_keys=True)
 

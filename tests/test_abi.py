@@ -35,7 +35,8 @@ def test_header_structs_match_ctypes():
                           ("clmgb_rootsink_fields", abi.ROOTSINK_FIELDS),
                           ("clmgb_zd09_fields", abi.ZD09_FIELDS),
                           ("clmgb_soilflux_fields", abi.SOILFLUX_FIELDS),
-                          ("clmgb_surfhyd_fields", abi.SURFHYD_FIELDS)):
+                          ("clmgb_surfhyd_fields", abi.SURFHYD_FIELDS),
+                          ("clmgb_snowlayer_fields", abi.SNOWLAYER_FIELDS)):
         members = abi.header_struct_members(txt, sname)
         assert members[0] == "struct_size"
         assert members[1:] == [f[0] for f in fields], sname
@@ -45,6 +46,7 @@ def test_header_structs_match_ctypes():
     assert abi.header_struct_members(txt, "clmgb_step_adjoint") == [f[0] for f in abi.StepAdjoint._fields_]
     assert abi.header_struct_members(txt, "clmgb_substep_log") == [f[0] for f in abi.SubstepLog._fields_]
     assert abi.header_struct_members(txt, "clmgb_surfhyd_config") == [f[0] for f in abi.SurfHydConfig._fields_]
+    assert abi.header_struct_members(txt, "clmgb_snowlayer_config") == [f[0] for f in abi.SnowLayerConfig._fields_]
 
 
 def test_header_constants_match_python():
@@ -58,7 +60,8 @@ def test_header_constants_match_python():
         assert int(consts[name]) == getattr(abi, name), name
     for name in ("SH_FLOODC", "SH_SAT_EXCESS", "SH_QFLX_INPUTS", "SH_INFL_EXCESS", "SH_ROUTE", "SH_UPDATE_H2OSFC",
                  "SH_INFILTRATION", "SH_TOTAL_RUNOFF", "SH_URBAN_PONDING", "SH_ALL", "FSAT_TOPMODEL", "FSAT_VIC",
-                 "QINMAX_NONE", "QINMAX_HKSAT"):
+                 "QINMAX_NONE", "QINMAX_HKSAT", "SL_COMPACTION", "SL_COMBINE", "SL_DIVIDE", "SL_ZERO_EMPTY",
+                 "SL_FILTER", "SL_ALL", "OVERBURDEN_ANDERSON1976", "OVERBURDEN_VIONNET2012"):
         assert int(consts[name]) == getattr(abi, name), name
 
 

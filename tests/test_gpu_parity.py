@@ -316,7 +316,7 @@ def test_empty_bounds_is_noop(handle_factory):
 
 
 # ---------------------------------------------------------------- shared math
-@pytest.mark.parametrize("op", ["log", "exp", "pow", "log10", "sin"])
+@pytest.mark.parametrize("op", ["log", "exp", "pow", "log10", "sin", "acos"])
 def test_math_bit_identical_to_cpu_build(handle_factory, op):
     import ctypes as C
     h = handle_factory(synth.clm5_varpar())
@@ -326,6 +326,8 @@ def test_math_bit_identical_to_cpu_build(handle_factory, op):
         x = rng.uniform(-745, 709, n)
     elif op == "sin":
         x = np.concatenate([rng.uniform(-1e5, 1e5, n // 2), rng.uniform(-4.0, 4.0, n - n // 2)])
+    elif op == "acos":
+        x = rng.uniform(-1.0, 1.0, n)
     else:
         x = np.concatenate([10 ** rng.uniform(-300, 300, n // 2), rng.uniform(0.0, 3.0, n - n // 2)])
     y = rng.uniform(-50, 50, n)

@@ -108,3 +108,21 @@ def test_sin_accuracy():
     assert worst < 1.0, worst
     assert fsin(0.0) == 0.0 and math.copysign(1.0, fsin(-0.0)) == -1.0
     assert math.isnan(fsin(math.inf)) and math.isnan(fsin(math.nan)) and math.isnan(fsin(2e6))
+
+
+def test_acos_accuracy():
+    rng = np.random.default_rng(5)
+    xs = np.concatenate([rng.uniform(-1, 1, 6000), 1 - 10 ** rng.uniform(-16, 0, 1000),
+                         -1 + 10 ** rng.uniform(-16, 0, 1000), [1.0, -1.0, 0.5, -0.5, 0.0, -0.0]])
+    facos = _fn("orc_cm_acos", 1)
+    worst = 0.0
+    for x in xs:
+        x = float(x)
+        ref = mp.acos(mp.mpf(x))
+        got = facos(x)
+        if ref == 0:
+            assert got == 0.0
+            continue
+        worst = max(worst, float(abs(mp.mpf(got) - ref) / ref) / (2.0 ** -52))
+    assert worst < 1.5, worst
+    assert facos(1.0) == 0.0 and math.isnan(facos(1.0000000000000002)) and math.isnan(facos(math.nan))
