@@ -153,6 +153,22 @@ class SnowLayerConfig(C.Structure):
                    0.35, 50.0, 350.0, 172800.0, 54.526, 1500.0, 0.010, 0.015, 0.03, 0.07, 0.02, 0.05)
 
 
+NLEVLAK = 10                      # varpar.nlevlak
+MAX_NLEVLAK = 16
+
+
+class LakeConfig(C.Structure):
+    """clmgb_lake_config: varpar.nlevlak and the lake_con sub-options."""
+    _fields_ = [("struct_size", C.c_int64), ("nlevlak", C.c_int32), ("use_lch4", C.c_int32),
+                ("lakepuddling", C.c_int32), ("lake_no_ed", C.c_int32), ("deepmixing_depthcrit", C.c_double),
+                ("deepmixing_mixfact", C.c_double), ("lake_puddle_thick", C.c_double)]
+
+    @classmethod
+    def default(cls):
+        """nlevlak 10, no CH4, lake_con defaults (lake_temperature.jl:15-23)."""
+        return cls(C.sizeof(cls), NLEVLAK, 0, 0, 0, 25.0, 10.0, 0.2)
+
+
 # (name, ctype, kind, dims) ; kind: 'c' column, 'p' patch, 'l' landunit
 # dims: None = vector, else level-kind string
 _u8, _i64, _f64 = "u8", "i64", "f64"
@@ -463,6 +479,63 @@ SNOWLAYER_FIELDS = [
     ("mss_dst4", _f64, "c", "S"),
 ]
 
+# clmgb_lake_fields (lake_temperature!), header order; level kind "K" = nlevlak
+LAKE_FIELDS = [
+    ("mask_lakec", _u8, "c", None),
+    ("mask_lakep", _u8, "p", None),
+    ("col_patchi", _i64, "c", None),
+    ("patch_column", _i64, "p", None),
+    ("col_snl", _i64, "c", None),
+    ("dz", _f64, "c", "L"),
+    ("z", _f64, "c", "L"),
+    ("zi", _f64, "c", "LZ"),
+    ("dz_lake", _f64, "c", "K"),
+    ("z_lake", _f64, "c", "K"),
+    ("lakedepth", _f64, "c", None),
+    ("watsat", _f64, "c", "G"),
+    ("tksatu", _f64, "c", "G"),
+    ("tkmg", _f64, "c", "G"),
+    ("tkdry", _f64, "c", "G"),
+    ("csol", _f64, "c", "G"),
+    ("t_grnd", _f64, "c", None),
+    ("etal", _f64, "c", None),
+    ("ks", _f64, "c", None),
+    ("ws", _f64, "c", None),
+    ("lake_raw", _f64, "c", None),
+    ("t_soisno", _f64, "c", "L"),
+    ("t_lake", _f64, "c", "K"),
+    ("h2osoi_liq", _f64, "c", "L"),
+    ("h2osoi_ice", _f64, "c", "L"),
+    ("h2osno_no_layers", _f64, "c", None),
+    ("snow_depth", _f64, "c", None),
+    ("frac_iceold", _f64, "c", "S"),
+    ("betaprime", _f64, "c", None),
+    ("lake_icefrac", _f64, "c", "K"),
+    ("lake_icefracsurf", _f64, "c", None),
+    ("lake_icethick", _f64, "c", None),
+    ("savedtke1", _f64, "c", None),
+    ("lakeresist", _f64, "c", None),
+    ("grnd_ch4_cond", _f64, "c", None),
+    ("qflx_snomelt", _f64, "c", None),
+    ("qflx_snofrz", _f64, "c", None),
+    ("qflx_snow_drain", _f64, "c", None),
+    ("qflx_snomelt_lyr", _f64, "c", "S"),
+    ("qflx_snofrz_lyr", _f64, "c", "S"),
+    ("imelt", _i64, "c", "S"),
+    ("eflx_snomelt", _f64, "c", None),
+    ("errsoi_col", _f64, "c", None),
+    ("sabg", _f64, "p", None),
+    ("sabg_lyr", _f64, "p", "S1"),
+    ("fsds_nir_d", _f64, "p", None),
+    ("fsds_nir_i", _f64, "p", None),
+    ("fsr_nir_d", _f64, "p", None),
+    ("fsr_nir_i", _f64, "p", None),
+    ("eflx_gnet", _f64, "p", None),
+    ("eflx_sh_tot", _f64, "p", None),
+    ("eflx_sh_grnd", _f64, "p", None),
+    ("eflx_soil_grnd", _f64, "p", None),
+]
+
 # clmgb_zd09_fields (soilwater_zengdecker2009!), header order
 ZD09_FIELDS = [
     ("mask_hydrology", _u8, "c", None),
@@ -518,6 +591,7 @@ RootSinkFields = _mk_struct("RootSinkFields", ROOTSINK_FIELDS)
 Zd09Fields = _mk_struct("Zd09Fields", ZD09_FIELDS)
 SurfHydFields = _mk_struct("SurfHydFields", SURFHYD_FIELDS)
 SnowLayerFields = _mk_struct("SnowLayerFields", SNOWLAYER_FIELDS)
+LakeFields = _mk_struct("LakeFields", LAKE_FIELDS)
 SoilFluxFields = _mk_struct("SoilFluxFields", SOILFLUX_FIELDS)
 
 
@@ -542,7 +616,7 @@ def level_count(kind, vp):
     """Number of levels of a field kind for a Varpar-like object."""
     L = vp.nlevsno + vp.nlevmaxurbgrnd
     return {"L": L, "LZ": L + 1, "G": vp.nlevgrnd, "S": vp.nlevsno,
-            "S1": vp.nlevsno + 1, "SOI": vp.nlevsoi, "V4": 4}[kind]
+            "S1": vp.nlevsno + 1, "SOI": vp.nlevsoi, "V4": 4, "K": NLEVLAK}[kind]
 
 
 def header_struct_members(header_text, struct_name):

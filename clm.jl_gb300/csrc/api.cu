@@ -393,6 +393,32 @@ int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clm
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_lake_temperature(clmgb_handle h, const clmgb_bounds* b, const clmgb_lake_fields* f,
+                               const clmgb_lake_config* cfg, double dtime, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (!f || !cfg) return CLMGB_ERR_NULL_ARG;
+  if (f->struct_size != (int64_t)sizeof(clmgb_lake_fields) || cfg->struct_size != (int64_t)sizeof(clmgb_lake_config))
+    return CLMGB_ERR_ABI;
+  if (cfg->nlevlak < 2 || cfg->nlevlak > CLMGB_MAX_NLEVLAK) return CLMGB_ERR_DIMS;
+  int32_t e = check_bounds(b, true);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  // every member but the two CH4 outputs, which only use_lch4 writes
+  const char* base = reinterpret_cast<const char*>(f) + sizeof(int64_t);
+  const size_t nptr = (sizeof(clmgb_lake_fields) - sizeof(int64_t)) / sizeof(void*);
+  for (size_t i = 0; i < nptr; i++) {
+    const void* q;
+    memcpy(&q, base + i * sizeof(void*), sizeof(void*));
+    const void* member = base + i * sizeof(void*);
+    const bool ch4 = member == (const void*)&f->lakeresist || member == (const void*)&f->grnd_ch4_cond;
+    if (!q && !(ch4 && !cfg->use_lch4)) return CLMGB_ERR_NULL_ARG;
+  }
+  cudaError_t ce = clmgb::launch_lake_temperature(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, h->dev_status,
+                                                  (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 // the pointers the selected stages read or write (clmgb_snow_layers)
 static bool snowlayer_pointers_ok(const clmgb_snowlayer_fields* f, const clmgb_snowlayer_config* cfg, uint32_t st) {
   auto all = [](std::initializer_list<const void*> ps) {

@@ -397,6 +397,47 @@ CLM.build_snow_filter!(mask_snow::CuArray, mask_nosnow, snl, mask_nolake, bounds
                  mask_nolakec = mask_nolake, col_snl = snl)
 
 # ---------------------------------------------------------------------------
+# lake_temperature! (lake_temperature.jl:1016) on CuArrays: clmgb_lake_temperature.
+# ---------------------------------------------------------------------------
+struct LakeConfig
+    struct_size::Int64
+    nlevlak::Int32; use_lch4::Int32; lakepuddling::Int32; lake_no_ed::Int32
+    deepmixing_depthcrit::Float64; deepmixing_mixfact::Float64; lake_puddle_thick::Float64
+end
+
+function CLM.lake_temperature!(col::CLM.ColumnData{<:Any,<:CuArray}, patch_data, solarabs, soilstate,
+                               waterstatebulk, waterdiagbulk, waterfluxbulk, energyflux, temperature, lakestate,
+                               grnd_ch4_cond, mask_lakec, mask_lakep, bounds_col, bounds_patch, dtime)
+    lc = CLM.lake_con
+    cfg = LakeConfig(sizeof(LakeConfig), CLM.varpar.nlevlak, CLM.varctl.use_lch4, lc.lakepuddling, lc.lake_no_ed,
+                     lc.deepmixing_depthcrit, lc.deepmixing_mixfact, lc.lake_puddle_thick)
+    ws, wf = waterstatebulk.ws, waterfluxbulk.wf
+    f = fields_buffer(Ptr{Cvoid}[
+        ptr(mask_lakec), ptr(mask_lakep), ptr(col.patchi), ptr(patch_data.column), ptr(col.snl), ptr(col.dz),
+        ptr(col.z), ptr(col.zi), ptr(col.dz_lake), ptr(col.z_lake), ptr(col.lakedepth), ptr(soilstate.watsat_col),
+        ptr(soilstate.tksatu_col), ptr(soilstate.tkmg_col), ptr(soilstate.tkdry_col), ptr(soilstate.csol_col),
+        ptr(temperature.t_grnd_col), ptr(lakestate.etal_col), ptr(lakestate.ks_col), ptr(lakestate.ws_col),
+        ptr(lakestate.lake_raw_col), ptr(temperature.t_soisno_col), ptr(temperature.t_lake_col),
+        ptr(ws.h2osoi_liq_col), ptr(ws.h2osoi_ice_col), ptr(ws.h2osno_no_layers_col),
+        ptr(waterdiagbulk.snow_depth_col), ptr(waterdiagbulk.frac_iceold_col), ptr(lakestate.betaprime_col),
+        ptr(lakestate.lake_icefrac_col), ptr(lakestate.lake_icefracsurf_col), ptr(lakestate.lake_icethick_col),
+        ptr(lakestate.savedtke1_col), ptr(lakestate.lakeresist_col), ptr(grnd_ch4_cond), ptr(wf.qflx_snomelt_col),
+        ptr(wf.qflx_snofrz_col), ptr(wf.qflx_snow_drain_col), ptr(wf.qflx_snomelt_lyr_col),
+        ptr(wf.qflx_snofrz_lyr_col), ptr(temperature.imelt_col), ptr(energyflux.eflx_snomelt_col),
+        ptr(energyflux.errsoi_col), ptr(solarabs.sabg_patch), ptr(solarabs.sabg_lyr_patch),
+        ptr(solarabs.fsds_nir_d_patch), ptr(solarabs.fsds_nir_i_patch), ptr(solarabs.fsr_nir_d_patch),
+        ptr(solarabs.fsr_nir_i_patch), ptr(energyflux.eflx_gnet_patch), ptr(energyflux.eflx_sh_tot_patch),
+        ptr(energyflux.eflx_sh_grnd_patch), ptr(energyflux.eflx_soil_grnd_patch)])
+    b = Bounds(length(mask_lakec), length(mask_lakep), 1, size(col.dz, 1), size(solarabs.sabg_lyr_patch, 1))
+    GC.@preserve f begin
+        check(ccall((:clmgb_lake_temperature, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{LakeConfig}, Float64, Ptr{Cvoid}),
+                    handle(), b, f, cfg, dtime, CUDA.stream().handle), "clmgb_lake_temperature")
+    end
+    nothing
+end
+
+# ---------------------------------------------------------------------------
 # Reverse mode.  One column step's vector-Jacobian product (clmgb_column_step_vjp)
 # behind a ChainRulesCore.rrule and an Enzyme reverse rule, the counterparts of the
 # reference's _reverse_step_into! (canopy_fluxes_reverse.jl:447-465).  `StepState`

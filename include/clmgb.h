@@ -564,6 +564,79 @@ typedef struct clmgb_snowlayer_fields {
   double* mss_dst4;                   /* [ldc, S]  RW */
 } clmgb_snowlayer_fields;
 
+/* ---- lake temperature (lake_temperature.jl:1016-1295) ---- */
+/* The lake configuration: varpar.nlevlak and the lake_con sub-options. */
+typedef struct clmgb_lake_config {
+  int64_t struct_size;                /* sizeof(clmgb_lake_config) */
+  int32_t nlevlak;                    /* varpar.nlevlak (10), at most CLMGB_MAX_NLEVLAK */
+  int32_t use_lch4;                   /* varctl.use_lch4: lake resistance and CH4 conductance */
+  int32_t lakepuddling;               /* lake_con.lakepuddling (0) */
+  int32_t lake_no_ed;                 /* lake_con.lake_no_ed (0) */
+  double  deepmixing_depthcrit;       /* lake_con.deepmixing_depthcrit (25 m) */
+  double  deepmixing_mixfact;         /* lake_con.deepmixing_mixfact (10) */
+  double  lake_puddle_thick;          /* lake_con.lake_puddle_thick (0.2 m) */
+} clmgb_lake_config;
+#define CLMGB_MAX_NLEVLAK 16
+
+/* Every field lake_temperature! reads or writes.  K = nlevlak lake levels; each lake
+ * column has one patch, col_patchi (CLM's col.patchi). */
+typedef struct clmgb_lake_fields {
+  int64_t struct_size;                /* sizeof(clmgb_lake_fields) */
+  const uint8_t* mask_lakec;          /* [nc]  filt.lakec */
+  const uint8_t* mask_lakep;          /* [np]  filt.lakep */
+  const int64_t* col_patchi;          /* [nc]  1-based */
+  const int64_t* patch_column;        /* [np]  1-based */
+  const int64_t* col_snl;             /* [nc] */
+  const double* dz;                   /* [ldc, L] */
+  const double* z;                    /* [ldc, L] */
+  const double* zi;                   /* [ldc, LZ] */
+  const double* dz_lake;              /* [ldc, K] */
+  const double* z_lake;               /* [ldc, K] */
+  const double* lakedepth;            /* [nc] */
+  const double* watsat;               /* [ldc, G] */
+  const double* tksatu;               /* [ldc, G] */
+  const double* tkmg;                 /* [ldc, G] */
+  const double* tkdry;                /* [ldc, G] */
+  const double* csol;                 /* [ldc, G] */
+  const double* t_grnd;               /* [nc] */
+  const double* etal;                 /* [nc] */
+  const double* ks;                   /* [nc] */
+  const double* ws;                   /* [nc] */
+  const double* lake_raw;             /* [nc] */
+  double* t_soisno;                   /* [ldc, L]  RW */
+  double* t_lake;                     /* [ldc, K]  RW */
+  double* h2osoi_liq;                 /* [ldc, L]  RW */
+  double* h2osoi_ice;                 /* [ldc, L]  RW */
+  double* h2osno_no_layers;           /* [nc]  RW */
+  double* snow_depth;                 /* [nc]  RW */
+  double* frac_iceold;                /* [ldc, S]  W */
+  double* betaprime;                  /* [nc]  W */
+  double* lake_icefrac;               /* [ldc, K]  RW */
+  double* lake_icefracsurf;           /* [nc]  W */
+  double* lake_icethick;              /* [nc]  W */
+  double* savedtke1;                  /* [nc]  W */
+  double* lakeresist;                 /* [nc]  W (use_lch4) */
+  double* grnd_ch4_cond;              /* [nc]  W (use_lch4) */
+  double* qflx_snomelt;               /* [nc]  W */
+  double* qflx_snofrz;                /* [nc]  W */
+  double* qflx_snow_drain;            /* [nc]  W */
+  double* qflx_snomelt_lyr;           /* [ldc, S]  W */
+  double* qflx_snofrz_lyr;            /* [ldc, S]  W */
+  int64_t* imelt;                     /* [ldc, S]  W */
+  double* eflx_snomelt;               /* [nc]  W */
+  double* errsoi_col;                 /* [nc]  W */
+  const double* sabg;                 /* [np] */
+  const double* sabg_lyr;             /* [ldp, S1] */
+  const double* fsds_nir_d;           /* [np] */
+  const double* fsds_nir_i;           /* [np] */
+  const double* fsr_nir_d;            /* [np] */
+  const double* fsr_nir_i;            /* [np] */
+  double* eflx_gnet;                  /* [np]  RW */
+  double* eflx_sh_tot;                /* [np]  RW */
+  double* eflx_sh_grnd;               /* [np]  RW */
+  double* eflx_soil_grnd;             /* [np]  RW */
+} clmgb_lake_fields;
+
 typedef struct clmgb_handle_s* clmgb_handle;
 
 /* ---- library / handle ---- */
@@ -678,6 +751,17 @@ int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clm
  * in the device status and skip the column. */
 int32_t clmgb_snow_layers(clmgb_handle h, const clmgb_bounds* b, const clmgb_snowlayer_fields* f,
                           const clmgb_snowlayer_config* cfg, uint32_t stages, double dtime, void* stream);
+
+/* lake_temperature! (lake_temperature.jl:1016-1295) for the lake columns, one thread per
+ * column through the whole sequence: thermal properties, eddy diffusivity, solar source,
+ * the Crank-Nicolson system over snow, lake and soil levels and its tridiagonal solve,
+ * phase change (phase_change_lake!), convective mixing, and the energy check that
+ * moves a residual below 0.1 W/m2 into the patch's sensible heat.  Results are the
+ * reference's bits.  Every pointer is required, lakeresist and grnd_ch4_cond only with
+ * use_lch4.  A patch index that does not map back to its column sets
+ * CLMGB_COL_PATCH_RANGE, snl outside -nlevsno..0 CLMGB_COL_LEVEL_RANGE (column skipped). */
+int32_t clmgb_lake_temperature(clmgb_handle h, const clmgb_bounds* b, const clmgb_lake_fields* f,
+                               const clmgb_lake_config* cfg, double dtime, void* stream);
 
 /* soil_water! with the Zeng-Decker 2009 method (soilwater_zengdecker2009!,
  * soil_water_movement.jl:1616-1764): equilibrium matric potential from the water

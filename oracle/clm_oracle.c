@@ -46,6 +46,7 @@
  *     divide_snow_layers!             :2021-2031, :2057-2237
  *     zero_empty_snow_layers!         :2314-2329
  *     build_snow_filter!              :2488-2510
+ *   lake_temperature!                 src/biogeophys/lake_temperature.jl:39-1295, kernel by kernel
  *
  * Transcendentals: the reference uses Julia Base's exp/log/pow/sin (openlibm for
  * log10); this file and the CUDA kernels share clm_math.h's binary64 versions, which
@@ -1789,6 +1790,543 @@ int orc_snow_layers(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_s
         else f->mask_nosnow[c] = 1;
       }
     }
+  return 0;
+}
+
+/* ===================================================================== */
+/* lake_temperature! (lake_temperature.jl:1016-1295), kernel by kernel    */
+/* ===================================================================== */
+#define LK_MAXX (ORC_MAXL + 2 * CLMGB_MAX_NLEVLAK)
+#define LK_BETAVIS 0.0
+#define LK_ZA 0.6
+#define LK_TDMAX 277.0
+#define LK_VKC 0.4
+
+/* soil_therm_prop_lake! (:39-192) for column c: tk, cv [1..ns+nlevgrnd] and tktopsoillay */
+static void lake_therm_prop(const clmgb_varpar* vp, const clmgb_lake_fields* f, int64_t c, int64_t ld, double* tk,
+                            double* cv, double* tktopsoillay)
+{
+  const int ns = vp->nlevsno, ng = vp->nlevgrnd, nsoi = vp->nlevsoi;
+  const int64_t snl = f->col_snl[c];
+  double thk[ORC_MAXL + 2];
+  memset(thk, 0, sizeof thk);
+  for (int jj = 1; jj <= ns + ng; jj++) {           /* _lake_soil_tk_kernel! */
+    int j = jj - ns;
+    if (j >= 1 && j <= nsoi) {
+      double satw = 1.0;
+      double fl = IX(f->h2osoi_liq, c, jj, ld) / (IX(f->h2osoi_ice, c, jj, ld) + IX(f->h2osoi_liq, c, jj, ld));
+      double dke, dksat;
+      if (IX(f->t_soisno, c, jj, ld) >= TFRZ) {
+        dke = jl_max(0.0, cm_log10(satw) + 1.0);
+        dksat = IX(f->tksatu, c, j, ld);
+      } else {
+        dke = satw;
+        dksat = IX(f->tkmg, c, j, ld) * cm_pow(0.249, fl * IX(f->watsat, c, j, ld)) * cm_pow(2.29, IX(f->watsat, c, j, ld));
+      }
+      thk[jj] = dke * dksat + (1.0 - dke) * IX(f->tkdry, c, j, ld);
+      satw = (IX(f->h2osoi_liq, c, jj, ld) / DENH2O + IX(f->h2osoi_ice, c, jj, ld) / DENICE) /
+             (IX(f->dz, c, jj, ld) * IX(f->watsat, c, j, ld));
+      if (satw > 1.0) {
+        double xicevol = (satw - 1.0) * IX(f->watsat, c, j, ld);
+        thk[jj] = (thk[jj] + xicevol * TKICE) / (1.0 + xicevol) / (1.0 + xicevol);
+      }
+    } else if (j > nsoi) {
+      thk[jj] = THK_BEDROCK;
+    }
+    if (snl + 1 < 1 && j >= snl + 1 && j <= 0) {
+      double bw = (IX(f->h2osoi_ice, c, jj, ld) + IX(f->h2osoi_liq, c, jj, ld)) / IX(f->dz, c, jj, ld);
+      thk[jj] = TKAIR + (7.75e-5 * bw + 1.105e-6 * bw * bw) * (TKICE - TKAIR);
+    }
+  }
+  for (int jj = 1; jj <= ns + ng; jj++) {           /* _lake_tk_interface_kernel! */
+    int j = jj - ns;
+    if (j >= snl + 1 && j <= ng - 1 && j != 0) {
+      int jj1 = jj + 1;
+      tk[jj] = thk[jj] * thk[jj1] * (IX(f->z, c, jj1, ld) - IX(f->z, c, jj, ld)) /
+               (thk[jj] * (IX(f->z, c, jj1, ld) - IX(f->zi, c, jj + 1, ld)) +
+                thk[jj1] * (IX(f->zi, c, jj + 1, ld) - IX(f->z, c, jj, ld)));
+    } else if (j == 0 && j >= snl + 1) {
+      tk[jj] = thk[jj];
+    } else if (j == ng) {
+      tk[jj] = 0.0;
+    }
+    if (j == 1) *tktopsoillay = thk[jj];
+  }
+  for (int j = 1; j <= ng; j++) {                   /* _lake_soil_cv_kernel! */
+    int jj = j + ns;
+    cv[jj] = IX(f->csol, c, j, ld) * (1.0 - IX(f->watsat, c, j, ld)) * IX(f->dz, c, jj, ld) +
+             (IX(f->h2osoi_ice, c, jj, ld) * CPICE + IX(f->h2osoi_liq, c, jj, ld) * CPLIQ);
+    if (j > nsoi) cv[jj] = CSOL_BEDROCK * IX(f->dz, c, jj, ld);
+  }
+  for (int jj = 1; jj <= ns; jj++) {                /* _lake_snow_cv_kernel! */
+    int j = jj - ns;
+    if (snl + 1 < 1 && j >= snl + 1)
+      cv[jj] = CPLIQ * IX(f->h2osoi_liq, c, jj, ld) + CPICE * IX(f->h2osoi_ice, c, jj, ld);
+  }
+}
+
+static double lake_rhow(double icefrac, double t)
+{
+  return (1.0 - icefrac) * 1000.0 * (1.0 - 1.9549e-05 * cm_pow(fabs(t - LK_TDMAX), 1.68)) + icefrac * DENICE;
+}
+
+static double lake_h2osno_total(const clmgb_varpar* vp, const clmgb_lake_fields* f, int64_t c, int64_t ld)
+{
+  double tot = f->h2osno_no_layers[c];
+  for (int jj = 1; jj <= vp->nlevsno; jj++)
+    if (jj - vp->nlevsno >= f->col_snl[c] + 1) tot += IX(f->h2osoi_ice, c, jj, ld) + IX(f->h2osoi_liq, c, jj, ld);
+  return tot;
+}
+
+/* convective mixing of lake levels lo..hi (_lake_top/_bottom_convection_kernel!, :787-894) */
+static void lake_mix(const clmgb_lake_fields* f, int64_t c, int64_t ld, int lo, int hi, double* rhow, double cwat,
+                     double cice_eff)
+{
+  double qav = 0.0, nav = 0.0, iceav = 0.0;
+  for (int i = lo; i <= hi; i++) {
+    qav += IX(f->dz_lake, c, i, ld) * (IX(f->t_lake, c, i, ld) - TFRZ) *
+           ((1.0 - IX(f->lake_icefrac, c, i, ld)) * cwat + IX(f->lake_icefrac, c, i, ld) * cice_eff);
+    iceav += IX(f->lake_icefrac, c, i, ld) * IX(f->dz_lake, c, i, ld);
+    nav += IX(f->dz_lake, c, i, ld);
+  }
+  qav /= nav;
+  iceav /= nav;
+  double tav_froz = 0.0, tav_unfr = 0.0;
+  if (qav > 0.0) tav_unfr = qav / ((1.0 - iceav) * cwat);
+  else if (qav < 0.0) tav_froz = qav / (iceav * cice_eff);
+  double zsum = 0.0;
+  for (int i = lo; i <= hi; i++) {
+    double dzl = IX(f->dz_lake, c, i, ld);
+    if ((zsum + dzl) / nav <= iceav) {
+      IX(f->lake_icefrac, c, i, ld) = 1.0;
+      IX(f->t_lake, c, i, ld) = tav_froz + TFRZ;
+    } else if (zsum / nav < iceav) {
+      IX(f->lake_icefrac, c, i, ld) = (iceav * nav - zsum) / dzl;
+      double fi = IX(f->lake_icefrac, c, i, ld);
+      IX(f->t_lake, c, i, ld) = (fi * tav_froz * cice_eff + (1.0 - fi) * tav_unfr * cwat) /
+                                    (fi * cice_eff + (1.0 - fi) * cwat) + TFRZ;
+    } else {
+      IX(f->lake_icefrac, c, i, ld) = 0.0;
+      IX(f->t_lake, c, i, ld) = tav_unfr + TFRZ;
+    }
+    zsum += dzl;
+    rhow[i] = lake_rhow(IX(f->lake_icefrac, c, i, ld), IX(f->t_lake, c, i, ld));
+  }
+}
+
+int orc_lake_temperature(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_lake_fields* f,
+                         const clmgb_lake_config* cfg, double dtime)
+{
+  int e = check_varpar(vp);
+  if (e) return e;
+  if (cfg->nlevlak < 2 || cfg->nlevlak > CLMGB_MAX_NLEVLAK) return -1;
+  const int64_t nc = b->nc, ld = b->ldc, ldp = b->ldp;
+  const int ns = vp->nlevsno, ngr = vp->nlevgrnd, nlak = cfg->nlevlak;
+  const int ntot = ns + nlak + ngr;
+  const double p0 = 1.0, cwat = CPLIQ * DENH2O, cice_eff = CPICE * DENH2O, cfus = HFUS * DENH2O;
+  const double tkice_eff = TKICE * DENICE / DENH2O, km = TKWAT / cwat;
+  const int puddling = cfg->lakepuddling != 0, no_ed = cfg->lake_no_ed != 0, lch4 = cfg->use_lch4 != 0;
+  const double pudz = puddling ? cfg->lake_puddle_thick : 0.0;
+  for (int64_t c = 0; c < nc; c++) {
+    if (!f->mask_lakec[c]) continue;
+    const int64_t p = f->col_patchi[c] - 1;
+    const int pact = f->mask_lakep[p] != 0;
+    const int64_t snl = f->col_snl[c];
+    double rhow[CLMGB_MAX_NLEVLAK + 1] = {0}, phi[CLMGB_MAX_NLEVLAK + 1] = {0}, kme[CLMGB_MAX_NLEVLAK + 1] = {0};
+    double cv_lake[CLMGB_MAX_NLEVLAK + 1] = {0}, tk_lake[CLMGB_MAX_NLEVLAK + 1] = {0};
+    double tk[ORC_MAXL + 2] = {0}, cv[ORC_MAXL + 2] = {0}, sabg_lyr_col[ORC_MAXL + 2] = {0};
+    double cvx[LK_MAXX] = {0}, tkix[LK_MAXX] = {0}, tx[LK_MAXX] = {0}, phix[LK_MAXX] = {0}, zx[LK_MAXX] = {0};
+    double fnx[LK_MAXX] = {0}, factx[LK_MAXX] = {0}, a[LK_MAXX] = {0}, bb[LK_MAXX] = {0}, c1[LK_MAXX] = {0};
+    double r[LK_MAXX] = {0};
+    double phi_soil = 0.0, fin = 0.0, ocvts = 0.0, ncvts = 0.0, tktopsoillay = 0.0, lhabs = 0.0;
+    int jconvect = 0, jconvectbot = nlak + 1, bottomconvect = 0, puddle = 0, frzn = 0;
+    /* _lake_init_kernel! */
+    if (lch4) f->lakeresist[c] = 0.0;
+    /* _lake_prior_ice_kernel! */
+    for (int jj = 1; jj <= ns; jj++)
+      if (jj - ns >= snl + 1)
+        IX(f->frac_iceold, c, jj, ld) =
+            IX(f->h2osoi_ice, c, jj, ld) / (IX(f->h2osoi_liq, c, jj, ld) + IX(f->h2osoi_ice, c, jj, ld));
+    /* _lake_solar_nir_kernel! */
+    if (pact) {
+      fin = f->eflx_gnet[p];
+      double sabg_nir = f->fsds_nir_d[p] + f->fsds_nir_i[p] - f->fsr_nir_d[p] - f->fsr_nir_i[p];
+      sabg_nir = jl_min(sabg_nir, f->sabg[p]);
+      f->betaprime[c] = sabg_nir / jl_max(1.0e-5, f->sabg[p]);
+      f->betaprime[c] = f->betaprime[c] + (1.0 - f->betaprime[c]) * LK_BETAVIS;
+    }
+    const double beta = f->betaprime[c];
+    /* _lake_density_kernel! */
+    for (int j = 1; j <= nlak; j++) rhow[j] = lake_rhow(IX(f->lake_icefrac, c, j, ld), IX(f->t_lake, c, j, ld));
+    /* _lake_diffusivity_kernel! (j = 1 .. nlevlak-1, in order) */
+    const int warm = f->t_grnd[c] > TFRZ && IX(f->t_lake, c, 1, ld) > TFRZ && snl == 0;
+    for (int j = 1; j <= nlak - 1; j++) {
+      double zl = IX(f->z_lake, c, j, ld);
+      double drhodz = (rhow[j + 1] - rhow[j]) / (IX(f->z_lake, c, j + 1, ld) - zl);
+      double n2 = GRAV / rhow[j] * drhodz;
+      double vz = LK_VKC * zl;
+      double num = 40.0 * n2 * (vz * vz);
+      double wsc = f->ws[c];
+      double den = jl_max((wsc * wsc) * cm_exp(-2.0 * f->ks[c] * zl), 1.0e-10);
+      double ri = (-1.0 + sqrt(jl_max(1.0 + num / den, 0.0))) / 20.0;
+      if (puddling && j == 1) frzn = 0;
+      double fi = IX(f->lake_icefrac, c, j, ld);
+      if (warm && (!puddling || (fi == 0.0 && !frzn))) {
+        double ke = LK_VKC * wsc * zl / p0 * cm_exp(-f->ks[c] * zl) / (1.0 + 37.0 * ri * ri);
+        kme[j] = km + ke;
+        if (!no_ed) {
+          double fangkm = 1.039e-8 * cm_pow(jl_max(n2, 7.5e-5), -0.43);
+          kme[j] = kme[j] + fangkm;
+        }
+        if (f->lakedepth[c] >= cfg->deepmixing_depthcrit) kme[j] = kme[j] * cfg->deepmixing_mixfact;
+        tk_lake[j] = kme[j] * cwat;
+      } else {
+        kme[j] = km;
+        if (!no_ed) {
+          double fangkm = 1.039e-8 * cm_pow(jl_max(n2, 7.5e-5), -0.43);
+          kme[j] = kme[j] + fangkm;
+          if (f->lakedepth[c] >= cfg->deepmixing_depthcrit) kme[j] = kme[j] * cfg->deepmixing_mixfact;
+          tk_lake[j] = kme[j] * cwat * tkice_eff / ((1.0 - fi) * tkice_eff + kme[j] * cwat * fi);
+        } else {
+          tk_lake[j] = TKWAT * tkice_eff / ((1.0 - fi) * tkice_eff + TKWAT * fi);
+        }
+        if (puddling) frzn = 1;
+      }
+    }
+    /* _lake_diffusivity_bottom_kernel! */
+    {
+      int j = nlak;
+      double fi = IX(f->lake_icefrac, c, j, ld);
+      kme[nlak] = kme[nlak - 1];
+      if (warm && (!puddling || (fi == 0.0 && !frzn))) {
+        tk_lake[j] = tk_lake[j - 1];
+      } else if (!no_ed) {
+        tk_lake[j] = kme[j] * cwat * tkice_eff / ((1.0 - fi) * tkice_eff + kme[j] * cwat * fi);
+      } else {
+        tk_lake[j] = TKWAT * tkice_eff / ((1.0 - fi) * tkice_eff + TKWAT * fi);
+      }
+      f->savedtke1[c] = kme[1] * cwat;
+    }
+    const int64_t jtop = snl + 1;
+    /* _lake_heat_source_kernel! (the reference reads sabg_lyr[p, 1] for layer 1 under snow) */
+    if (pact)
+      for (int j = 1; j <= nlak; j++) {
+        double eta = f->etal[c] > 0.0 ? f->etal[c] : 1.1925 * cm_pow(jl_max(f->lakedepth[c], 1.0), -0.424);
+        double zin = IX(f->z_lake, c, j, ld) - 0.5 * IX(f->dz_lake, c, j, ld);
+        double zout = IX(f->z_lake, c, j, ld) + 0.5 * IX(f->dz_lake, c, j, ld);
+        double rsfin = cm_exp(-eta * jl_max(zin - LK_ZA, 0.0));
+        double rsfout = cm_exp(-eta * jl_max(zout - LK_ZA, 0.0));
+        double phidum;
+        if (warm) {
+          phidum = (rsfin - rsfout) * f->sabg[p] * (1.0 - beta);
+          if (j == nlak) phi_soil = rsfout * f->sabg[p] * (1.0 - beta);
+        } else if (j == 1 && snl == 0) {
+          phidum = f->sabg[p] * (1.0 - beta);
+        } else if (j == 1) {
+          phidum = IX(f->sabg_lyr, p, j, ldp);
+        } else {
+          phidum = 0.0;
+          if (j == nlak) phi_soil = 0.0;
+        }
+        phi[j] = phidum;
+      }
+    /* _lake_cv_lake_kernel!, soil_therm_prop_lake! */
+    for (int j = 1; j <= nlak; j++) {
+      double fi = IX(f->lake_icefrac, c, j, ld);
+      cv_lake[j] = IX(f->dz_lake, c, j, ld) * (cwat * (1.0 - fi) + cice_eff * fi);
+    }
+    lake_therm_prop(vp, f, c, ld, tk, cv, &tktopsoillay);
+    /* _lake_energy_sum_lake_kernel!, _lake_energy_sum_soil_kernel! */
+    for (int j = 1; j <= nlak; j++)
+      ocvts += cv_lake[j] * (IX(f->t_lake, c, j, ld) - TFRZ) +
+               cfus * IX(f->dz_lake, c, j, ld) * (1.0 - IX(f->lake_icefrac, c, j, ld));
+    double h2osno_total = lake_h2osno_total(vp, f, c, ld);
+    for (int j = -ns + 1; j <= ngr; j++) {
+      int jj = j + ns;
+      if (j >= jtop) {
+        ocvts += cv[jj] * (IX(f->t_soisno, c, jj, ld) - TFRZ) + HFUS * IX(f->h2osoi_liq, c, jj, ld);
+        if (j == 1 && h2osno_total > 0.0 && j == jtop) ocvts -= h2osno_total * HFUS;
+      }
+    }
+    /* _lake_solar_transfer_kernel! */
+    if (pact)
+      for (int jidx = 1; jidx <= ns + 1; jidx++)
+        if (jidx - ns >= jtop) sabg_lyr_col[jidx] = IX(f->sabg_lyr, p, jidx, ldp);
+    /* _lake_extcol_setup_kernel! */
+    for (int je = -ns + 1; je <= nlak + ngr; je++) {
+      int ji = je + ns, jj = je + ns;
+      if (je < jtop) continue;
+      if (je < 1) {
+        zx[ji] = IX(f->z, c, jj, ld);
+        cvx[ji] = cv[jj];
+        phix[ji] = je == jtop ? 0.0 : sabg_lyr_col[je + ns];
+        tx[ji] = IX(f->t_soisno, c, jj, ld);
+      } else if (je <= nlak) {
+        zx[ji] = IX(f->z_lake, c, je, ld);
+        cvx[ji] = cv_lake[je];
+        phix[ji] = phi[je];
+        tx[ji] = IX(f->t_lake, c, je, ld);
+      } else {
+        int jpjj = je - nlak + ns;
+        zx[ji] = zx[nlak + ns] + IX(f->dz_lake, c, nlak, ld) / 2.0 + IX(f->z, c, jpjj, ld);
+        cvx[ji] = cv[jpjj];
+        phix[ji] = je == nlak + 1 ? phi_soil : 0.0;
+        tx[ji] = IX(f->t_soisno, c, jpjj, ld);
+      }
+    }
+    /* _lake_tkix_kernel! */
+    for (int ji = 1; ji <= ntot; ji++) {
+      int je = ji - ns, jj = je + ns;
+      if (je < jtop) continue;
+      if (je < 0) {
+        tkix[ji] = tk[jj];
+      } else if (je == 0) {
+        double dzp = zx[ji + 1] - zx[ji];
+        tkix[ji] = tk_lake[1] * tk[jj] * dzp / (tk[jj] * IX(f->z_lake, c, 1, ld) + tk_lake[1] * (-IX(f->z, c, jj, ld)));
+      } else if (je < nlak) {
+        tkix[ji] = (tk_lake[je] * tk_lake[je + 1] * (IX(f->dz_lake, c, je + 1, ld) + IX(f->dz_lake, c, je, ld))) /
+                   (tk_lake[je] * IX(f->dz_lake, c, je + 1, ld) + tk_lake[je + 1] * IX(f->dz_lake, c, je, ld));
+      } else if (je == nlak) {
+        double dzp = zx[ji + 1] - zx[ji];
+        tkix[ji] = tktopsoillay * tk_lake[je] * dzp /
+                   (tktopsoillay * IX(f->dz_lake, c, je, ld) / 2.0 + tk_lake[je] * IX(f->z, c, 1 + ns, ld));
+      } else {
+        tkix[ji] = tk[je - nlak + ns];
+      }
+    }
+    /* _lake_tridiag_factors_kernel!, _lake_tridiag_coeffs_kernel! */
+    for (int ji = 1; ji <= ntot; ji++) {
+      int je = ji - ns;
+      if (je < jtop) continue;
+      factx[ji] = dtime / cvx[ji];
+      fnx[ji] = je < nlak + ngr ? tkix[ji] * (tx[ji + 1] - tx[ji]) / (zx[ji + 1] - zx[ji]) : 0.0;
+    }
+    const double omc = 1.0 - CNFAC;
+    for (int ji = 1; ji <= ntot; ji++) {
+      int je = ji - ns;
+      if (je < jtop) continue;
+      if (je == jtop) {
+        double dzp = zx[ji + 1] - zx[ji];
+        a[ji] = 0.0;
+        bb[ji] = 1.0 + omc * factx[ji] * tkix[ji] / dzp;
+        c1[ji] = -omc * factx[ji] * tkix[ji] / dzp;
+        r[ji] = tx[ji] + factx[ji] * (fin + phix[ji] + CNFAC * fnx[ji]);
+      } else if (je < nlak + ngr) {
+        double dzm = zx[ji] - zx[ji - 1], dzp = zx[ji + 1] - zx[ji];
+        a[ji] = -omc * factx[ji] * tkix[ji - 1] / dzm;
+        bb[ji] = 1.0 + omc * factx[ji] * (tkix[ji] / dzp + tkix[ji - 1] / dzm);
+        c1[ji] = -omc * factx[ji] * tkix[ji] / dzp;
+        r[ji] = tx[ji] + CNFAC * factx[ji] * (fnx[ji] - fnx[ji - 1]) + factx[ji] * phix[ji];
+      } else {
+        double dzm = zx[ji] - zx[ji - 1];
+        a[ji] = -omc * factx[ji] * tkix[ji - 1] / dzm;
+        bb[ji] = 1.0 + omc * factx[ji] * tkix[ji - 1] / dzm;
+        c1[ji] = 0.0;
+        r[ji] = tx[ji] - CNFAC * factx[ji] * fnx[ji - 1];
+      }
+    }
+    /* tridiagonal_multi! (tridiagonal.jl:86-127) from jtop + nlevsno */
+    {
+      int j0 = (int)jtop + ns;
+      double cp[LK_MAXX], dp[LK_MAXX];
+      const double tiny = 1e-30;
+      double bet = bb[j0];
+      if (fabs(bet) < tiny) bet = tiny;
+      double cpp = c1[j0] / bet, dpp = r[j0] / bet;
+      cp[j0] = cpp;
+      dp[j0] = dpp;
+      for (int jj = j0 + 1; jj <= ntot; jj++) {
+        double denom = bb[jj] - a[jj] * cpp;
+        if (fabs(denom) < tiny) denom = copysign(tiny, denom == 0.0 ? 1.0 : denom);
+        cpp = c1[jj] / denom;
+        dpp = (r[jj] - a[jj] * dpp) / denom;
+        cp[jj] = cpp;
+        dp[jj] = dpp;
+      }
+      double un = dpp;
+      tx[ntot] = un;
+      for (int jj = ntot - 1; jj >= j0; jj--) {
+        un = dp[jj] - cp[jj] * un;
+        tx[jj] = un;
+      }
+    }
+    /* _lake_unpack_kernel! */
+    for (int ji = 1; ji <= ntot; ji++) {
+      int je = ji - ns;
+      if (je < jtop) continue;
+      if (je < 1) IX(f->t_soisno, c, je + ns, ld) = tx[ji];
+      else if (je <= nlak) IX(f->t_lake, c, je, ld) = tx[ji];
+      else IX(f->t_soisno, c, je - nlak + ns, ld) = tx[ji];
+    }
+    /* phase_change_lake! (_phase_change_lake_water_kernel!, _soil_kernel!, :204-314) */
+    {
+      const double small = 1.0e-12;
+      double qsm = 0.0, qsd = 0.0, lh = 0.0, qsf = 0.0;
+      for (int jj = 1; jj <= ns; jj++) {
+        IX(f->qflx_snomelt_lyr, c, jj, ld) = 0.0;
+        IX(f->qflx_snofrz_lyr, c, jj, ld) = 0.0;
+        IX(f->imelt, c, jj, ld) = 0;
+      }
+      if (f->h2osno_no_layers[c] > 0.0 && IX(f->t_lake, c, 1, ld) > TFRZ) {
+        double heatavail = (IX(f->t_lake, c, 1, ld) - TFRZ) * cv_lake[1];
+        double melt = jl_min(f->h2osno_no_layers[c], heatavail / HFUS);
+        double heatrem = jl_max(heatavail - melt * HFUS, 0.0);
+        IX(f->t_lake, c, 1, ld) = TFRZ + heatrem / cv_lake[1];
+        f->snow_depth[c] = f->snow_depth[c] * (1.0 - melt / f->h2osno_no_layers[c]);
+        f->h2osno_no_layers[c] = f->h2osno_no_layers[c] - melt;
+        lh += melt * HFUS;
+        qsm += melt / dtime;
+        qsd += melt / dtime;
+        if (f->h2osno_no_layers[c] < small) f->h2osno_no_layers[c] = 0.0;
+        if (f->snow_depth[c] < small) f->snow_depth[c] = 0.0;
+      }
+      for (int j = 1; j <= nlak; j++) {
+        int dophase = 0;
+        double heatavail = 0.0, melt = 0.0, heatrem = 0.0;
+        double tl = IX(f->t_lake, c, j, ld), fi = IX(f->lake_icefrac, c, j, ld), dzl = IX(f->dz_lake, c, j, ld);
+        if (tl > TFRZ && fi > 0.0) {
+          dophase = 1;
+          heatavail = (tl - TFRZ) * cv_lake[j];
+          melt = jl_min(fi * DENH2O * dzl, heatavail / HFUS);
+          heatrem = jl_max(heatavail - melt * HFUS, 0.0);
+        } else if (tl < TFRZ && fi < 1.0) {
+          dophase = 1;
+          heatavail = (tl - TFRZ) * cv_lake[j];
+          melt = jl_max(-(1.0 - fi) * DENH2O * dzl, heatavail / HFUS);
+          heatrem = jl_min(heatavail - melt * HFUS, 0.0);
+        }
+        if (dophase) {
+          IX(f->lake_icefrac, c, j, ld) = fi - melt / (DENH2O * dzl);
+          lh += melt * HFUS;
+          cv_lake[j] = cv_lake[j] + melt * (CPLIQ - CPICE);
+          IX(f->t_lake, c, j, ld) = TFRZ + heatrem / cv_lake[j];
+          if (IX(f->lake_icefrac, c, j, ld) > 1.0 - small) IX(f->lake_icefrac, c, j, ld) = 1.0;
+          if (IX(f->lake_icefrac, c, j, ld) < small) IX(f->lake_icefrac, c, j, ld) = 0.0;
+        }
+      }
+      for (int j = -ns + 1; j <= ngr; j++) {
+        int jj = j + ns;
+        if (j < snl + 1) continue;
+        int dophase = 0;
+        double heatavail = 0.0, melt = 0.0, heatrem = 0.0;
+        double t = IX(f->t_soisno, c, jj, ld);
+        if (t > TFRZ && IX(f->h2osoi_ice, c, jj, ld) > 0.0) {
+          dophase = 1;
+          heatavail = (t - TFRZ) * cv[jj];
+          melt = jl_min(IX(f->h2osoi_ice, c, jj, ld), heatavail / HFUS);
+          heatrem = jl_max(heatavail - melt * HFUS, 0.0);
+          if (j <= 0) {
+            IX(f->imelt, c, jj, ld) = 1;
+            IX(f->qflx_snomelt_lyr, c, jj, ld) = melt / dtime;
+            qsm += IX(f->qflx_snomelt_lyr, c, jj, ld);
+          }
+        } else if (t < TFRZ && IX(f->h2osoi_liq, c, jj, ld) > 0.0) {
+          dophase = 1;
+          heatavail = (t - TFRZ) * cv[jj];
+          melt = jl_max(-IX(f->h2osoi_liq, c, jj, ld), heatavail / HFUS);
+          heatrem = jl_min(heatavail - melt * HFUS, 0.0);
+          if (j <= 0) {
+            IX(f->imelt, c, jj, ld) = 2;
+            IX(f->qflx_snofrz_lyr, c, jj, ld) = -melt / dtime;
+            qsf += IX(f->qflx_snofrz_lyr, c, jj, ld);
+          }
+        }
+        if (dophase) {
+          IX(f->h2osoi_ice, c, jj, ld) = IX(f->h2osoi_ice, c, jj, ld) - melt;
+          IX(f->h2osoi_liq, c, jj, ld) = IX(f->h2osoi_liq, c, jj, ld) + melt;
+          lh += melt * HFUS;
+          cv[jj] = cv[jj] + melt * (CPLIQ - CPICE);
+          IX(f->t_soisno, c, jj, ld) = TFRZ + heatrem / cv[jj];
+          if (IX(f->h2osoi_ice, c, jj, ld) < small) IX(f->h2osoi_ice, c, jj, ld) = 0.0;
+          if (IX(f->h2osoi_liq, c, jj, ld) < small) IX(f->h2osoi_liq, c, jj, ld) = 0.0;
+        }
+      }
+      lhabs = lh;
+      f->qflx_snomelt[c] = qsm;
+      f->qflx_snofrz[c] = qsf;
+      f->qflx_snow_drain[c] = qsd;
+      f->eflx_snomelt[c] = qsm * HFUS;
+    }
+    (void)lhabs;
+    /* convective mixing: density, puddling, top-down then bottom-up (:1204-1241) */
+    for (int j = 1; j <= nlak; j++) rhow[j] = lake_rhow(IX(f->lake_icefrac, c, j, ld), IX(f->t_lake, c, j, ld));
+    if (puddling) {
+      double icesum = 0.0;
+      for (int j = 1; j <= nlak; j++) icesum = icesum + IX(f->lake_icefrac, c, j, ld) * IX(f->dz, c, j + ns, ld);
+      puddle = icesum >= pudz;
+    }
+    for (int j = 1; j <= nlak - 2; j++) {
+      int doconv = (!puddling || !puddle) &&
+                   (rhow[j] > rhow[j + 1] ||
+                    (IX(f->lake_icefrac, c, j, ld) < 1.0 && IX(f->lake_icefrac, c, j + 1, ld) > 0.0));
+      if (!doconv) continue;
+      if (lch4) jconvect = j + 1;
+      lake_mix(f, c, ld, 1, j + 1, rhow, cwat, cice_eff);
+    }
+    {
+      int jb = nlak - 1;
+      if ((!puddling || !puddle) &&
+          (rhow[jb] > rhow[jb + 1] || (IX(f->lake_icefrac, c, jb, ld) < 1.0 && IX(f->lake_icefrac, c, jb + 1, ld) > 0.0)))
+        bottomconvect = 1;
+    }
+    for (int j = nlak - 1; j >= 1; j--) {
+      int doconv = bottomconvect && (!puddling || !puddle) &&
+                   (rhow[j] > rhow[j + 1] ||
+                    (IX(f->lake_icefrac, c, j, ld) < 1.0 && IX(f->lake_icefrac, c, j + 1, ld) > 0.0));
+      if (!doconv) continue;
+      if (lch4) jconvectbot = j;
+      lake_mix(f, c, ld, j, nlak, rhow, cwat, cice_eff);
+    }
+    /* _lake_ch4_kernel! */
+    if (lch4) {
+      double lr = f->lakeresist[c];
+      for (int j = 1; j <= nlak; j++)
+        if (j > jconvect && j < jconvectbot) lr += IX(f->dz_lake, c, j, ld) / kme[j];
+      f->lakeresist[c] = lr;
+      double gc = 1.0 / (lr + f->lake_raw[c]);
+      if (IX(f->lake_icefrac, c, 1, ld) > 0.1) gc = 0.0;
+      f->grnd_ch4_cond[c] = gc;
+    }
+    /* re-evaluated properties and the energy after (:1250-1267) */
+    for (int j = 1; j <= nlak; j++) {
+      double fi = IX(f->lake_icefrac, c, j, ld);
+      cv_lake[j] = IX(f->dz_lake, c, j, ld) * (cwat * (1.0 - fi) + cice_eff * fi);
+    }
+    lake_therm_prop(vp, f, c, ld, tk, cv, &tktopsoillay);
+    for (int j = 1; j <= nlak; j++) {
+      ncvts += cv_lake[j] * (IX(f->t_lake, c, j, ld) - TFRZ) +
+               cfus * IX(f->dz_lake, c, j, ld) * (1.0 - IX(f->lake_icefrac, c, j, ld));
+      fin += phi[j];
+    }
+    h2osno_total = lake_h2osno_total(vp, f, c, ld);
+    for (int j = -ns + 1; j <= ngr; j++) {
+      int jj = j + ns;
+      if (j >= jtop) {
+        ncvts += cv[jj] * (IX(f->t_soisno, c, jj, ld) - TFRZ) + HFUS * IX(f->h2osoi_liq, c, jj, ld);
+        if (j < 1) fin += phix[j + ns];
+        if (j == 1 && h2osno_total > 0.0 && j == jtop) ncvts -= h2osno_total * HFUS;
+      }
+      if (j == 1) fin += phi_soil;
+    }
+    /* _lake_energy_conservation_kernel!, _lake_icethick_kernel! */
+    if (pact) {
+      double err = (ncvts - ocvts) / dtime - fin;
+      if (fabs(err) < 0.10) {
+        f->eflx_sh_tot[p] -= err;
+        f->eflx_sh_grnd[p] -= err;
+        f->eflx_soil_grnd[p] += err;
+        f->eflx_gnet[p] += err;
+        err = 0.0;
+      }
+      f->errsoi_col[c] = err;
+    }
+    double thick = 0.0;
+    for (int j = 1; j <= nlak; j++) {
+      if (j == 1) f->lake_icefracsurf[c] = IX(f->lake_icefrac, c, 1, ld);
+      thick += IX(f->lake_icefrac, c, j, ld) * IX(f->dz_lake, c, j, ld) * DENH2O / DENICE;
+    }
+    f->lake_icethick[c] = thick;
+  }
   return 0;
 }
 

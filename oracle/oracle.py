@@ -39,6 +39,7 @@ def lib():
         L.orc_soil_fluxes.argtypes = [P, P, P, C.c_double]
         L.orc_surface_hydrology.argtypes = [P, P, P, P, C.c_uint32, C.c_double]
         L.orc_snow_layers.argtypes = [P, P, P, P, C.c_uint32, C.c_double]
+        L.orc_lake_temperature.argtypes = [P, P, P, P, C.c_double]
         L.orc_soil_water.argtypes = [P, P, P, P, C.c_double, P, P, P, C.c_int32]
         L.orc_run_steps.argtypes = [P, P, P, P, P, C.c_double, C.c_int32, C.c_int32, P, P,
                                     C.c_int64, P, P, P, C.c_int32]
@@ -100,6 +101,12 @@ def rootsink(rs, use_hydrstress=False):
 def soil_fluxes(fs, dtime):
     """soil_fluxes! in place on a host SoilFluxState."""
     _chk(lib().orc_soil_fluxes(C.byref(fs.vp), C.byref(fs.bounds()), C.byref(fs.fields()), float(dtime)))
+
+
+def lake_temperature(lk, dtime, cfg):
+    """lake_temperature! in place on a host LakeState."""
+    _chk(lib().orc_lake_temperature(C.byref(lk.vp), C.byref(lk.bounds()), C.byref(lk.fields()), C.byref(cfg),
+                                    float(dtime)))
 
 
 def snow_layers(sl, dtime, cfg, stages):

@@ -409,6 +409,13 @@ def main():
     cases["soil_fluxes"] = soil_fluxes_cases()
     cases["surface_hydrology"] = surface_hydrology_cases()
     cases["snow_layers"] = snow_layer_cases()
+    cases["lake_temperature"] = dict(
+        varpar=dict(nlevsno=5, nlevsoi=10, nlevgrnd=15, nlevlak=10, nlevurb=5, nlevmaxurbgrnd=15),
+        source="test/test_lake_temperature.jl:9-17 (setup_lake_params!), :24-170 (create_test_data)",
+        cases=[dict(name="runs_finite", source="test/test_lake_temperature.jl:285-311", nc=2, zero_flux=False,
+                    checks=["t_lake_finite", "icethick_nonnegative", "errsoi_finite"]),
+               dict(name="energy_conservation_zero_input", source="test/test_lake_temperature.jl:314-337", nc=1,
+                    zero_flux=True, checks=["errsoi_below_0.2"])])
     with open(os.path.join(HERE, "reference_cases.json"), "w") as fh:
         json.dump(cases, fh, indent=1, sort_keys=True)
 
