@@ -153,6 +153,16 @@ class SnowLayerConfig(C.Structure):
                    0.35, 50.0, 350.0, 172800.0, 54.526, 1500.0, 0.010, 0.015, 0.03, 0.07, 0.02, 0.05)
 
 
+BAL_H2O_WARN, BAL_H2O_ERROR, BAL_H2O_NONFINITE, BAL_SOI_WARN, BAL_SOI_ERROR = 1, 2, 4, 8, 16
+
+
+class BalanceReport(C.Structure):
+    """clmgb_balance_report."""
+    _fields_ = [("errh2o_max", C.c_double), ("errh2o_index", C.c_int64), ("errh2o_nonfinite", C.c_int64),
+                ("errsoi_max", C.c_double), ("errsoi_index", C.c_int64), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
 NLEVLAK = 10                      # varpar.nlevlak
 MAX_NLEVLAK = 16
 
@@ -536,6 +546,29 @@ LAKE_FIELDS = [
     ("eflx_soil_grnd", _f64, "p", None),
 ]
 
+# clmgb_colbalance_fields (balance_check!'s column checks), header order
+COLBALANCE_FIELDS = [
+    ("col_itype", _i64, "c", None),
+    ("col_active", _u8, "c", None),
+    ("forc_rain", _f64, "c", None),
+    ("forc_snow", _f64, "c", None),
+    ("begwb", _f64, "c", None),
+    ("endwb", _f64, "c", None),
+    ("qflx_flood", _f64, "c", None),
+    ("qflx_sfc_irrig", _f64, "c", None),
+    ("qflx_glcice_dyn_water_flux", _f64, "c", None),
+    ("qflx_evap_tot", _f64, "c", None),
+    ("qflx_surf", _f64, "c", None),
+    ("qflx_qrgwl", _f64, "c", None),
+    ("qflx_drain", _f64, "c", None),
+    ("qflx_drain_perched", _f64, "c", None),
+    ("qflx_ice_runoff", _f64, "c", None),
+    ("qflx_snwcp_discarded_liq", _f64, "c", None),
+    ("qflx_snwcp_discarded_ice", _f64, "c", None),
+    ("errsoi", _f64, "c", None),
+    ("errh2o", _f64, "c", None),
+]
+
 # clmgb_zd09_fields (soilwater_zengdecker2009!), header order
 ZD09_FIELDS = [
     ("mask_hydrology", _u8, "c", None),
@@ -592,6 +625,7 @@ Zd09Fields = _mk_struct("Zd09Fields", ZD09_FIELDS)
 SurfHydFields = _mk_struct("SurfHydFields", SURFHYD_FIELDS)
 SnowLayerFields = _mk_struct("SnowLayerFields", SNOWLAYER_FIELDS)
 LakeFields = _mk_struct("LakeFields", LAKE_FIELDS)
+ColBalanceFields = _mk_struct("ColBalanceFields", COLBALANCE_FIELDS)
 SoilFluxFields = _mk_struct("SoilFluxFields", SOILFLUX_FIELDS)
 
 

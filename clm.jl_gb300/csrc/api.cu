@@ -22,8 +22,9 @@ struct clmgb_handle_s {
   int device;
   int num_sms;
   clmgb_varpar vp;
-  // device scratch owned by the handle (one allocation): the status word (OR of
-  // CLMGB_COL_* bits) and the Richards work-queue counter
+  // device scratch owned by the handle (one allocation of 8 words): the status word
+  // (OR of CLMGB_COL_* bits), the Richards work-queue counter, and 5 words for the
+  // reductions of clmgb_balance_check_columns
   unsigned long long* scratch;
   uint32_t* dev_status;
   unsigned long long* queue;
@@ -196,8 +197,8 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->waves_blocks_per_sm = 0;
   cudaError_t ce = cudaGetDevice(&h->device);
   if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
-  if (ce == cudaSuccess) ce = cudaMalloc(&h->scratch, 2 * sizeof(unsigned long long));
-  if (ce == cudaSuccess) ce = cudaMemset(h->scratch, 0, 2 * sizeof(unsigned long long));
+  if (ce == cudaSuccess) ce = cudaMalloc(&h->scratch, 8 * sizeof(unsigned long long));
+  if (ce == cudaSuccess) ce = cudaMemset(h->scratch, 0, 8 * sizeof(unsigned long long));
   if (ce == cudaSuccess) {
     h->dev_status = reinterpret_cast<uint32_t*>(h->scratch);
     h->queue = h->scratch + 1;
@@ -391,6 +392,47 @@ int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clm
   cudaError_t ce = clmgb::launch_surface_hydrology(make_dims(h->vp, *b), b->nc, b->nl, *f, *cfg, stages, dtime,
                                                    h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_balance_check_columns(clmgb_handle h, const clmgb_bounds* b, const clmgb_colbalance_fields* f,
+                                    double dtime, clmgb_balance_report* report, void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  if (!f || !report) return CLMGB_ERR_NULL_ARG;
+  if (f->struct_size != (int64_t)sizeof(clmgb_colbalance_fields)) return CLMGB_ERR_ABI;
+  int32_t e = check_bounds(b, false);
+  if (e) return e;
+  memset(report, 0, sizeof(*report));
+  if (b->nc == 0) return CLMGB_OK;
+  if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
+  // every member but errsoi (NULL: no soil energy scan)
+  const void* need[] = {f->col_itype, f->col_active, f->forc_rain, f->forc_snow, f->begwb, f->endwb, f->qflx_flood,
+                        f->qflx_sfc_irrig, f->qflx_glcice_dyn_water_flux, f->qflx_evap_tot, f->qflx_surf,
+                        f->qflx_qrgwl, f->qflx_drain, f->qflx_drain_perched, f->qflx_ice_runoff,
+                        f->qflx_snwcp_discarded_liq, f->qflx_snwcp_discarded_ice, f->errh2o};
+  for (const void* p : need)
+    if (!p) return CLMGB_ERR_NULL_ARG;
+  const cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* r = h->scratch + 2;
+  cudaError_t ce = clmgb::launch_colbalance(b->nc, *f, dtime, r, s);
+  unsigned long long v[5];
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(v, r, sizeof(v), cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (ce != cudaSuccess) return cuda_fail(h, ce);
+  double m, ms;
+  memcpy(&m, &v[0], sizeof(double));
+  memcpy(&ms, &v[3], sizeof(double));
+  report->errh2o_max = m;
+  report->errh2o_index = (int64_t)v[1];
+  report->errh2o_nonfinite = v[2] == ~0ULL ? 0 : (int64_t)v[2];
+  report->errsoi_max = f->errsoi ? ms : 0.0;
+  report->errsoi_index = f->errsoi ? (int64_t)v[4] : 0;
+  // the scans' thresholds (balance_check.jl:711-713, 1352, 1356); NaN compares false
+  if (m > 1.0e-9) report->flags |= CLMGB_BAL_H2O_WARN;
+  if (m > 1.0e-5) report->flags |= CLMGB_BAL_H2O_ERROR;
+  if (report->errh2o_nonfinite) report->flags |= CLMGB_BAL_H2O_NONFINITE;
+  if (f->errsoi && ms > 1.0e-5) report->flags |= CLMGB_BAL_SOI_WARN;
+  if (f->errsoi && ms > 1.0e-4) report->flags |= CLMGB_BAL_SOI_ERROR;
+  return CLMGB_OK;
 }
 
 int32_t clmgb_lake_temperature(clmgb_handle h, const clmgb_bounds* b, const clmgb_lake_fields* f,

@@ -109,4 +109,62 @@ cudaError_t launch_balance_residuals(const Dims& D, int64_t nc, const clmgb_soil
   return cudaGetLastError();
 }
 
+// ---- balance_check!'s column checks (balance_check.jl:723-770, 1124-1160, 1347-1365) ----
+// Maxima of |x| are reduced with integer atomics on the bits of |x| (non-negative doubles
+// order as their bit patterns; NaN is canonicalised above +Inf, as Julia's findmax ranks
+// it), then a second pass takes the first column holding the maximum.
+namespace {
+
+constexpr int CB_BLOCK = 256;
+constexpr int64_t ICOL_SUNWALL_ = 72, ICOL_SHADEWALL_ = 73;
+
+__device__ __forceinline__ unsigned long long abs_key(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+  return b > 0x7ff0000000000000ULL ? 0x7ff8000000000000ULL : b;
+}
+
+__global__ void k_colbalance_init(unsigned long long* r) {
+  if (threadIdx.x < 5) r[threadIdx.x] = (threadIdx.x == 0 || threadIdx.x == 3) ? 0ULL : ~0ULL;
+}
+
+__global__ void __launch_bounds__(CB_BLOCK)
+k_colbalance(int64_t nc, clmgb_colbalance_fields f, double dtime, unsigned long long* r) {
+  const int64_t c = (int64_t)blockIdx.x * CB_BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  double e = 0.0;
+  if (f.col_active[c]) {
+    const bool wall = f.col_itype[c] == ICOL_SUNWALL_ || f.col_itype[c] == ICOL_SHADEWALL_;
+    const double rain = wall ? 0.0 : f.forc_rain[c], snow = wall ? 0.0 : f.forc_snow[c];
+    e = f.endwb[c] - f.begwb[c] -
+        (rain + snow + f.qflx_flood[c] + f.qflx_sfc_irrig[c] + f.qflx_glcice_dyn_water_flux[c] -
+         f.qflx_evap_tot[c] - f.qflx_surf[c] - f.qflx_qrgwl[c] - f.qflx_drain[c] - f.qflx_drain_perched[c] -
+         f.qflx_ice_runoff[c] - f.qflx_snwcp_discarded_liq[c] - f.qflx_snwcp_discarded_ice[c]) *
+            dtime;
+  }
+  f.errh2o[c] = e;
+  atomicMax(&r[0], abs_key(e));
+  if (!isfinite(e)) atomicMin(&r[2], (unsigned long long)(c + 1));
+  if (f.errsoi) atomicMax(&r[3], f.col_active[c] ? abs_key(f.errsoi[c]) : 0ULL);
+}
+
+__global__ void __launch_bounds__(CB_BLOCK)
+k_colbalance_index(int64_t nc, clmgb_colbalance_fields f, unsigned long long* r) {
+  const int64_t c = (int64_t)blockIdx.x * CB_BLOCK + threadIdx.x;
+  if (c >= nc) return;
+  if (abs_key(f.errh2o[c]) == r[0]) atomicMin(&r[1], (unsigned long long)(c + 1));
+  if (f.errsoi && (f.col_active[c] ? abs_key(f.errsoi[c]) : 0ULL) == r[3]) atomicMin(&r[4], (unsigned long long)(c + 1));
+}
+
+}  // namespace
+
+cudaError_t launch_colbalance(int64_t nc, const clmgb_colbalance_fields& f, double dtime, unsigned long long* r,
+                              cudaStream_t s) {
+  // r: max key, first index, first non-finite index, errsoi max key, errsoi first index
+  k_colbalance_init<<<1, 32, 0, s>>>(r);
+  const unsigned int grid = (unsigned int)((nc + CB_BLOCK - 1) / CB_BLOCK);
+  k_colbalance<<<grid, CB_BLOCK, 0, s>>>(nc, f, dtime, r);
+  k_colbalance_index<<<grid, CB_BLOCK, 0, s>>>(nc, f, r);
+  return cudaGetLastError();
+}
+
 }  // namespace clmgb

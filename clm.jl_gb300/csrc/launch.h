@@ -117,6 +117,8 @@ cudaError_t launch_snow_layers(const Dims& D, int64_t nc, int64_t nl, const clmg
                                cudaStream_t s);
 cudaError_t launch_lake_temperature(const Dims& D, int64_t nc, const clmgb_lake_fields& f, const clmgb_lake_config& P,
                                     double dtime, uint32_t* dev_status, cudaStream_t s);
+cudaError_t launch_colbalance(int64_t nc, const clmgb_colbalance_fields& f, double dtime, unsigned long long* r,
+                              cudaStream_t s);
 cudaError_t launch_soil_fluxes(const Dims& D, int64_t nc, int64_t nl, const clmgb_soilflux_fields& f, double dtime,
                                uint32_t* dev_status, cudaStream_t s);
 int vjp_cf_blocks_per_sm();

@@ -438,6 +438,34 @@ function CLM.lake_temperature!(col::CLM.ColumnData{<:Any,<:CuArray}, patch_data,
 end
 
 # ---------------------------------------------------------------------------
+# balance_check!'s column part on CuArrays (balance_check.jl:1099-1160, 1347-1365): errh2o
+# and the scans' maxima computed on the device; the stop decision stays in balance_check!
+# (hard_error, skip_steps), which calls this for its CuArray columns and applies it.
+# ---------------------------------------------------------------------------
+struct BalanceReport
+    errh2o_max::Float64; errh2o_index::Int64; errh2o_nonfinite::Int64
+    errsoi_max::Float64; errsoi_index::Int64; flags::UInt32; reserved::UInt32
+end
+
+function column_balance_check!(errh2o::CuArray, col, wb, wf, wfb, forc_rain_col, forc_snow_col, qflx_ice_runoff_col,
+                               errsoi_col, dtime)
+    f = fields_buffer(Ptr{Cvoid}[
+        ptr(col.itype), ptr(col.active), ptr(forc_rain_col), ptr(forc_snow_col), ptr(wb.begwb_col), ptr(wb.endwb_col),
+        ptr(wf.qflx_floodc_col), ptr(wf.qflx_sfc_irrig_col), ptr(wf.qflx_glcice_dyn_water_flux_col),
+        ptr(wf.qflx_evap_tot_col), ptr(wf.qflx_surf_col), ptr(wf.qflx_qrgwl_col), ptr(wf.qflx_drain_col),
+        ptr(wf.qflx_drain_perched_col), ptr(qflx_ice_runoff_col), ptr(wf.qflx_snwcp_discarded_liq_col),
+        ptr(wf.qflx_snwcp_discarded_ice_col), ptr(errsoi_col), ptr(errh2o)])
+    rep = Ref{BalanceReport}()
+    GC.@preserve f begin
+        check(ccall((:clmgb_balance_check_columns, lib), Int32,
+                    (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Float64, Ref{BalanceReport}, Ptr{Cvoid}),
+                    handle(), Bounds(length(errh2o), 0, 0, length(errh2o), 0), f, dtime, rep,
+                    CUDA.stream().handle), "clmgb_balance_check_columns")
+    end
+    rep[]
+end
+
+# ---------------------------------------------------------------------------
 # Reverse mode.  One column step's vector-Jacobian product (clmgb_column_step_vjp)
 # behind a ChainRulesCore.rrule and an Enzyme reverse rule, the counterparts of the
 # reference's _reverse_step_into! (canopy_fluxes_reverse.jl:447-465).  `StepState`

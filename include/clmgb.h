@@ -1051,6 +1051,55 @@ int32_t clmgb_balance_residuals(clmgb_handle h, const clmgb_bounds* b, const clm
                                 const double* t_h2osfc_bef, const double* t_grnd0, const double* begwb,
                                 double* errsoi, double* errh2o, void* stream);
 
+/* ---- balance_check!'s column checks (balance_check.jl:707-768, 1099-1160, 1347-1365) ---- */
+/* Every field of the column water-balance check, and the soil energy residual. */
+typedef struct clmgb_colbalance_fields {
+  int64_t struct_size;                /* sizeof(clmgb_colbalance_fields) */
+  const int64_t* col_itype;           /* [nc]  walls take no precipitation */
+  const uint8_t* col_active;          /* [nc] */
+  const double* forc_rain;            /* [nc]  column rain (mm/s) */
+  const double* forc_snow;            /* [nc]  column snow (mm/s) */
+  const double* begwb;                /* [nc]  water at the start of the step (mm) */
+  const double* endwb;                /* [nc]  water at its end (mm) */
+  const double* qflx_flood;           /* [nc]  mm/s, like every flux below */
+  const double* qflx_sfc_irrig;       /* [nc] */
+  const double* qflx_glcice_dyn_water_flux; /* [nc] */
+  const double* qflx_evap_tot;        /* [nc] */
+  const double* qflx_surf;            /* [nc] */
+  const double* qflx_qrgwl;           /* [nc] */
+  const double* qflx_drain;           /* [nc] */
+  const double* qflx_drain_perched;   /* [nc] */
+  const double* qflx_ice_runoff;      /* [nc] */
+  const double* qflx_snwcp_discarded_liq; /* [nc] */
+  const double* qflx_snwcp_discarded_ice; /* [nc] */
+  const double* errsoi;               /* [nc]  soil energy residual (W/m2), e.g. from clmgb_soil_fluxes */
+  double* errh2o;                     /* [nc]  W: column water residual (mm) */
+} clmgb_colbalance_fields;
+
+/* What the reference's host-side scans look at, computed on the device. */
+typedef struct clmgb_balance_report {
+  double  errh2o_max;                 /* maximum |errh2o| over the columns (NaN if any is NaN) */
+  int64_t errh2o_index;               /* 1-based column of its first occurrence (0: no columns) */
+  int64_t errh2o_nonfinite;           /* 1-based first column with a NaN/Inf errh2o (0: none) */
+  double  errsoi_max;                 /* maximum |errsoi| over the active columns (0 for inactive) */
+  int64_t errsoi_index;               /* 1-based column of its first occurrence */
+  uint32_t flags;                     /* CLMGB_BAL_* */
+  uint32_t reserved;
+} clmgb_balance_report;
+#define CLMGB_BAL_H2O_WARN       1u   /* errh2o_max > H2O_WARNING_THRESH (1e-9 mm), :711 */
+#define CLMGB_BAL_H2O_ERROR      2u   /* errh2o_max > BALANCE_ERROR_THRESH (1e-5 mm), :713 */
+#define CLMGB_BAL_H2O_NONFINITE  4u   /* some errh2o is NaN/Inf (a failure, not a pass) */
+#define CLMGB_BAL_SOI_WARN       8u   /* errsoi_max > 1e-5 W/m2, :1352 */
+#define CLMGB_BAL_SOI_ERROR     16u   /* errsoi_max > 1e-4 W/m2, :1356 */
+
+/* The column part of balance_check!: errh2o (_bc_forc_rainsnow_kernel! and
+ * _bc_errh2o_col_kernel!, :723-770) and the maxima and first indices its warn/error scans
+ * read (:1124-1160, :1347-1365), reduced on the device.  The report is written to host
+ * memory, so the call waits for `stream`.  Whether a flagged error stops the model
+ * (hard_error, skip_steps, DAnstep) stays with the caller, as in the reference. */
+int32_t clmgb_balance_check_columns(clmgb_handle h, const clmgb_bounds* b, const clmgb_colbalance_fields* f,
+                                    double dtime, clmgb_balance_report* report, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

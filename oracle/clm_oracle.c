@@ -47,6 +47,7 @@
  *     zero_empty_snow_layers!         :2314-2329
  *     build_snow_filter!              :2488-2510
  *   lake_temperature!                 src/biogeophys/lake_temperature.jl:39-1295, kernel by kernel
+ *   balance_check! column checks      src/biogeophys/balance_check.jl:723-770, 1124-1160, 1347-1365
  *
  * Transcendentals: the reference uses Julia Base's exp/log/pow/sin (openlibm for
  * log10); this file and the CUDA kernels share clm_math.h's binary64 versions, which
@@ -2326,6 +2327,59 @@ int orc_lake_temperature(const clmgb_varpar* vp, const clmgb_bounds* b, const cl
       thick += IX(f->lake_icefrac, c, j, ld) * IX(f->dz_lake, c, j, ld) * DENH2O / DENICE;
     }
     f->lake_icethick[c] = thick;
+  }
+  return 0;
+}
+
+/* ===================================================================== */
+/* balance_check!'s column checks (balance_check.jl:723-770, 1124-1365)  */
+/* ===================================================================== */
+int orc_balance_check_columns(const clmgb_bounds* b, const clmgb_colbalance_fields* f, double dtime,
+                              clmgb_balance_report* rep)
+{
+  const int64_t nc = b->nc;
+  memset(rep, 0, sizeof(*rep));
+  /* _bc_forc_rainsnow_kernel!, _bc_errh2o_col_kernel! */
+  for (int64_t c = 0; c < nc; c++) {
+    double rain = f->forc_rain[c], snow = f->forc_snow[c];
+    if (f->col_itype[c] == ICOL_SUNWALL || f->col_itype[c] == ICOL_SHADEWALL) rain = snow = 0.0;
+    if (f->col_active[c])
+      f->errh2o[c] = f->endwb[c] - f->begwb[c] -
+                     (rain + snow + f->qflx_flood[c] + f->qflx_sfc_irrig[c] + f->qflx_glcice_dyn_water_flux[c] -
+                      f->qflx_evap_tot[c] - f->qflx_surf[c] - f->qflx_qrgwl[c] - f->qflx_drain[c] -
+                      f->qflx_drain_perched[c] - f->qflx_ice_runoff[c] - f->qflx_snwcp_discarded_liq[c] -
+                      f->qflx_snwcp_discarded_ice[c]) * dtime;
+    else
+      f->errh2o[c] = 0.0;
+  }
+  if (nc == 0) return 0;
+  /* the scans: first non-finite, then maximum(abs.(...)) and its first index, where a
+   * NaN is the maximum (Julia's findmax) */
+  double m = -1.0;
+  int64_t im = 0;
+  for (int64_t c = 0; c < nc; c++) {
+    double a = fabs(f->errh2o[c]);
+    if (!isfinite(f->errh2o[c]) && !rep->errh2o_nonfinite) rep->errh2o_nonfinite = c + 1;
+    if (isnan(m)) continue;
+    if (isnan(a) || a > m) { m = a; im = c + 1; }
+  }
+  rep->errh2o_max = m;
+  rep->errh2o_index = im;
+  if (m > 1.0e-9) rep->flags |= CLMGB_BAL_H2O_WARN;
+  if (m > 1.0e-5) rep->flags |= CLMGB_BAL_H2O_ERROR;
+  if (rep->errh2o_nonfinite) rep->flags |= CLMGB_BAL_H2O_NONFINITE;
+  if (f->errsoi) {
+    double ms = -1.0;
+    int64_t is = 0;
+    for (int64_t c = 0; c < nc; c++) {
+      double a = f->col_active[c] ? fabs(f->errsoi[c]) : 0.0;
+      if (isnan(ms)) continue;
+      if (isnan(a) || a > ms) { ms = a; is = c + 1; }
+    }
+    rep->errsoi_max = ms;
+    rep->errsoi_index = is;
+    if (ms > 1.0e-5) rep->flags |= CLMGB_BAL_SOI_WARN;
+    if (ms > 1.0e-4) rep->flags |= CLMGB_BAL_SOI_ERROR;
   }
   return 0;
 }

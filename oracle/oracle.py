@@ -40,6 +40,7 @@ def lib():
         L.orc_surface_hydrology.argtypes = [P, P, P, P, C.c_uint32, C.c_double]
         L.orc_snow_layers.argtypes = [P, P, P, P, C.c_uint32, C.c_double]
         L.orc_lake_temperature.argtypes = [P, P, P, P, C.c_double]
+        L.orc_balance_check_columns.argtypes = [P, P, C.c_double, P]
         L.orc_soil_water.argtypes = [P, P, P, P, C.c_double, P, P, P, C.c_int32]
         L.orc_run_steps.argtypes = [P, P, P, P, P, C.c_double, C.c_int32, C.c_int32, P, P,
                                     C.c_int64, P, P, P, C.c_int32]
@@ -101,6 +102,13 @@ def rootsink(rs, use_hydrstress=False):
 def soil_fluxes(fs, dtime):
     """soil_fluxes! in place on a host SoilFluxState."""
     _chk(lib().orc_soil_fluxes(C.byref(fs.vp), C.byref(fs.bounds()), C.byref(fs.fields()), float(dtime)))
+
+
+def balance_check_columns(cb, dtime):
+    """balance_check!'s column checks on a host ColBalanceState; returns the report."""
+    rep = abi.BalanceReport()
+    _chk(lib().orc_balance_check_columns(C.byref(cb.bounds()), C.byref(cb.fields()), float(dtime), C.byref(rep)))
+    return rep
 
 
 def lake_temperature(lk, dtime, cfg):

@@ -198,6 +198,45 @@ def surface_hydrology_cases():
     return dict(cases=out)
 
 
+def balance_check_cases():
+    """Column water-balance cases of test/test_balance_check.jl (make_bc_test_data: 4
+    soil columns, begwb = endwb = 100 mm, zero fluxes, dtime 1800 s, errsoi 0); each
+    sets the inputs it changes and the answers and stop decisions the test asserts.
+    The stop rule is _bc_should_error: hard_error and DAnstep > skip_steps (3)."""
+    out = []
+    dt = 1800.0
+
+    def case(name, src, inputs, expect, stops=()):
+        out.append(dict(name=name, source=src, nc=4, dtime=dt, inputs=inputs, expect=expect, stops=list(stops)))
+
+    case("perfect_balance", "test/test_balance_check.jl:309-378", {}, [dict(field="errh2o", exact=[0.0] * 4)],
+         stops=[dict(dastep=100, hard_error=True, stop=False)])
+    case("water_error_detection", "test/test_balance_check.jl:381-429", dict(endwb=[200.0] * 4),
+         [dict(field="errh2o", exact=[100.0] * 4)], stops=[dict(dastep=100, hard_error=True, stop=True)])
+    case("urban_walls_take_no_precipitation", "test/test_balance_check.jl:432-477",
+         dict(col_itype=[1, 72, 73, 1], forc_rain=[5.0] * 4, forc_snow=[2.0] * 4),
+         [dict(field="errh2o", index=[1, 2], atol=1e-15, value=0.0), dict(field="errh2o", index=[0], nonzero=True)],
+         stops=[dict(dastep=1, hard_error=True, stop=False)])
+    q = 5.7e-1
+    case("ice_runoff_closes_the_balance", "test/test_balance_check.jl:533-592 (a)",
+         dict(begwb=[12000.0] * 4, endwb=[12000.0 - q * dt] * 4, qflx_ice_runoff=[q] * 4),
+         [dict(field="errh2o", index=[0, 1, 2, 3], atol=1e-10, value=0.0)])
+    case("ice_runoff_missing", "test/test_balance_check.jl:533-592 (b)",
+         dict(begwb=[12000.0] * 4, endwb=[12000.0 - q * dt] * 4),
+         [dict(field="errh2o", index=[0, 1, 2, 3], rtol=1e-12, value=-q * dt), dict(flag="H2O_ERROR")],
+         stops=[dict(dastep=2, hard_error=True, stop=False)])
+    case("unbalanced_column_stops_past_skip", "test/test_balance_check.jl:639-700", dict(endwb=[150.0] * 4),
+         [dict(field="errh2o", index=[0], rtol=1e-12, value=50.0), dict(flag="H2O_ERROR")],
+         stops=[dict(dastep=4, hard_error=True, stop=True), dict(dastep=500, hard_error=True, stop=True),
+                dict(dastep=2, hard_error=True, stop=False), dict(dastep=500, hard_error=False, stop=False)])
+    for field, val in (("endwb", "nan"), ("begwb", "nan"), ("endwb", "inf")):
+        case("nonfinite_%s_%s" % (field, val), "test/test_balance_check.jl:709-765",
+             {field: [float(val), 100.0, 100.0, 100.0]},
+             [dict(field="errh2o", index=[0], nonfinite=True), dict(flag="H2O_NONFINITE")],
+             stops=[dict(dastep=4, hard_error=True, stop=True)])
+    return dict(cases=out)
+
+
 def snow_layer_cases():
     """Known answers of test/test_snow_hydrology.jl for the snow-layer routines, each
     through the public routine that uses it.  "snow" level values are listed from the
@@ -409,6 +448,7 @@ def main():
     cases["soil_fluxes"] = soil_fluxes_cases()
     cases["surface_hydrology"] = surface_hydrology_cases()
     cases["snow_layers"] = snow_layer_cases()
+    cases["balance_check_columns"] = balance_check_cases()
     cases["lake_temperature"] = dict(
         varpar=dict(nlevsno=5, nlevsoi=10, nlevgrnd=15, nlevlak=10, nlevurb=5, nlevmaxurbgrnd=15),
         source="test/test_lake_temperature.jl:9-17 (setup_lake_params!), :24-170 (create_test_data)",

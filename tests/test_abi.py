@@ -37,7 +37,8 @@ def test_header_structs_match_ctypes():
                           ("clmgb_soilflux_fields", abi.SOILFLUX_FIELDS),
                           ("clmgb_surfhyd_fields", abi.SURFHYD_FIELDS),
                           ("clmgb_snowlayer_fields", abi.SNOWLAYER_FIELDS),
-                          ("clmgb_lake_fields", abi.LAKE_FIELDS)):
+                          ("clmgb_lake_fields", abi.LAKE_FIELDS),
+                          ("clmgb_colbalance_fields", abi.COLBALANCE_FIELDS)):
         members = abi.header_struct_members(txt, sname)
         assert members[0] == "struct_size"
         assert members[1:] == [f[0] for f in fields], sname
@@ -49,6 +50,7 @@ def test_header_structs_match_ctypes():
     assert abi.header_struct_members(txt, "clmgb_surfhyd_config") == [f[0] for f in abi.SurfHydConfig._fields_]
     assert abi.header_struct_members(txt, "clmgb_snowlayer_config") == [f[0] for f in abi.SnowLayerConfig._fields_]
     assert abi.header_struct_members(txt, "clmgb_lake_config") == [f[0] for f in abi.LakeConfig._fields_]
+    assert abi.header_struct_members(txt, "clmgb_balance_report") == [f[0] for f in abi.BalanceReport._fields_]
 
 
 def test_header_constants_match_python():
