@@ -503,7 +503,7 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
     const double lwe_h2osfc = eg * SB * jl_pow4(th0);
     for (int64_t p1 = f.col_patchi[c]; p1 <= f.col_patchf[c]; p1++) {
       const int64_t p = p1 - 1;
-      if (f.patch_column[p] != c + 1) continue;
+      if (f.patch_column[p] != c + 1 + D.c0) continue;
       double dh_p = 0.0, hsoil_p = 0.0, hh_p = 0.0;
       const bool act = f.mask_nolakep[p] != 0;
       const double cb = (1.0 - (double)f.frac_veg_nosno[p]) * eg;

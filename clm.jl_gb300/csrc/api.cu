@@ -28,6 +28,8 @@ struct clmgb_handle_s {
   unsigned long long* scratch;
   uint32_t* dev_status;
   unsigned long long* queue;
+  int64_t column_base;          // CLMGB_OPT_COLUMN_BASE
+  int64_t defer;                // CLMGB_OPT_QUEUE_DEFER
   int64_t step_schedule;        // CLMGB_OPT_STEP_SCHEDULE
   int64_t queue_blocks_per_sm;  // CLMGB_OPT_QUEUE_BLOCKS_PER_SM (0 = occupancy limit)
   int occupancy_blocks;         // occupancy limit of the queue kernel
@@ -57,6 +59,11 @@ static const int64_t CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM = 2;
 // Measured on GB300 at 262,144 columns (2 blocks/SM): 0 -> 10.16, 8 -> 10.36, 16 -> 10.47,
 // 20 -> 10.54, 24 -> 10.51 M column-steps/s.
 static const int64_t CLMGB_DEFAULT_FRESH_BATCH = 20;
+// Attempts after which the work-queue kernel hands a column to the warp-per-column
+// finish (CLMGB_OPT_QUEUE_DEFER).  Measured on GB300, 262,144 columns of the scale
+// workload, ms per column step: off 27.1, 8 -> 32.8, 12 -> 27.7, 16 -> 25.5,
+// 20 -> 24.6, 24 -> 24.4, 28 -> 24.8, 32 -> 25.2, 40 -> 25.8, 56 -> 26.8.
+static const int64_t CLMGB_DEFAULT_QUEUE_DEFER = 24;
 
 using clmgb::Dims;
 
@@ -84,8 +91,9 @@ static int32_t check_bounds(const clmgb_bounds* b, bool need_patches) {
   return CLMGB_OK;
 }
 
-static Dims make_dims(const clmgb_varpar& vp, const clmgb_bounds& b) {
+static Dims make_dims(const clmgb_varpar& vp, const clmgb_bounds& b, int64_t c0 = 0) {
   Dims D;
+  D.c0 = c0;
   D.nlevsno = vp.nlevsno;
   D.nlevgrnd = vp.nlevgrnd;
   D.nlevsoi = vp.nlevsoi;
@@ -129,6 +137,17 @@ static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
   clmgb::QueueScratch q = h->qs;
   q.longest_first = h->queue_order == 1 ? 1 : 0;
   q.fresh_batch = (int)h->fresh_batch;
+  // deferred columns keep their state in the wave scratch of the same reservation
+  const bool have = h->ws.cap == h->qs.capacity && h->ws.cap > 0;
+  q.defer = have ? (int)h->defer : 0;
+  q.d_liq = have ? h->ws.qout : nullptr;
+  q.d_dtsub = have ? h->ws.dtsub : nullptr;
+  q.d_dtdone = have ? h->ws.dtdone : nullptr;
+  q.d_qc = have ? h->ws.qc : nullptr;
+  q.d_nsub = have ? h->ws.nsub : nullptr;
+  q.d_status = have ? h->ws.status : nullptr;
+  q.d_list = have ? h->ws.listA[0] : nullptr;
+  q.d_count = have ? h->scratch + 7 : nullptr;
   return q;
 }
 
@@ -181,6 +200,8 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->magic = HANDLE_MAGIC;
   h->vp = *vp;
   h->last_error = cudaSuccess;
+  h->column_base = 0;
+  h->defer = CLMGB_DEFAULT_QUEUE_DEFER;
   h->step_schedule = CLMGB_SCHEDULE_QUEUE;
   h->queue_blocks_per_sm = CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM;
   h->scratch = nullptr;
@@ -255,7 +276,7 @@ int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (use_excess_ice) return CLMGB_ERR_UNSUPPORTED;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_soil_temperature(make_dims(h->vp, *b), b->nc, *f, dtime, snow_method, col_status,
+  cudaError_t ce = clmgb::launch_soil_temperature(make_dims(h->vp, *b, h->column_base), b->nc, *f, dtime, snow_method, col_status,
                                                   h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -268,7 +289,7 @@ int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   if (b->nc == 0 && b->np == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_soil_fluxes(make_dims(h->vp, *b), b->nc, b->nl, *f, dtime, h->dev_status,
+  cudaError_t ce = clmgb::launch_soil_fluxes(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, dtime, h->dev_status,
                                              (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -286,7 +307,7 @@ int32_t clmgb_soil_water_zd09(clmgb_handle h, const clmgb_bounds* b, const clmgb
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_zd09(make_dims(h->vp, *b), b->nc, *f, cfg->e_ice, dtime, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_zd09(make_dims(h->vp, *b, h->column_base), b->nc, *f, cfg->e_ice, dtime, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -311,7 +332,7 @@ int32_t clmgb_effec_rootfrac_vert_tran_sink(clmgb_handle h, const clmgb_bounds* 
     for (const void* p : hs)
       if (!p) return CLMGB_ERR_NULL_ARG;
   }
-  cudaError_t ce = clmgb::launch_rootsink(make_dims(h->vp, *b), b->nc, b->nl, *f, use_hydrstress ? 1 : 0,
+  cudaError_t ce = clmgb::launch_rootsink(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, use_hydrstress ? 1 : 0,
                                           col_status, h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -389,9 +410,19 @@ int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clm
   if (b->nc == 0 || stages == 0) return CLMGB_OK;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!surfhyd_pointers_ok(f, cfg, stages)) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_surface_hydrology(make_dims(h->vp, *b), b->nc, b->nl, *f, *cfg, stages, dtime,
+  cudaError_t ce = clmgb::launch_surface_hydrology(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, *cfg, stages, dtime,
                                                    h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
+int32_t clmgb_copy_columns(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch, int64_t width,
+                           int64_t rows, void* stream) {
+  if (!dst || !src) return CLMGB_ERR_NULL_ARG;
+  if (width < 0 || rows < 0 || dst_pitch < width || src_pitch < width) return CLMGB_ERR_DIMS;
+  if (width == 0 || rows == 0) return CLMGB_OK;
+  const cudaError_t ce = cudaMemcpy2DAsync(dst, (size_t)dst_pitch, src, (size_t)src_pitch, (size_t)width,
+                                           (size_t)rows, cudaMemcpyDefault, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : CLMGB_ERR_CUDA;
 }
 
 int32_t clmgb_balance_check_columns(clmgb_handle h, const clmgb_bounds* b, const clmgb_colbalance_fields* f,
@@ -456,7 +487,7 @@ int32_t clmgb_lake_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
     const bool ch4 = member == (const void*)&f->lakeresist || member == (const void*)&f->grnd_ch4_cond;
     if (!q && !(ch4 && !cfg->use_lch4)) return CLMGB_ERR_NULL_ARG;
   }
-  cudaError_t ce = clmgb::launch_lake_temperature(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, h->dev_status,
+  cudaError_t ce = clmgb::launch_lake_temperature(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, h->dev_status,
                                                   (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -507,7 +538,7 @@ int32_t clmgb_snow_layers(clmgb_handle h, const clmgb_bounds* b, const clmgb_sno
   if (f->struct_size != (int64_t)sizeof(clmgb_snowlayer_fields)) return CLMGB_ERR_ABI;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!snowlayer_pointers_ok(f, cfg, stages)) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_snow_layers(make_dims(h->vp, *b), b->nc, b->nl, *f, *cfg, stages, dtime,
+  cudaError_t ce = clmgb::launch_snow_layers(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, *cfg, stages, dtime,
                                              h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -519,7 +550,7 @@ int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const 
   if (e) return e;
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
-  cudaError_t ce = clmgb::launch_water_fractions(make_dims(h->vp, *b), b->nc, *f, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_water_fractions(make_dims(h->vp, *b, h->column_base), b->nc, *f, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -534,13 +565,13 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soil
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   cudaError_t ce;
   if (h->step_schedule == CLMGB_SCHEDULE_FUSED)
-    ce = clmgb::launch_moisture_form(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, h->dev_status,
+    ce = clmgb::launch_moisture_form(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, h->dev_status,
                                      (cudaStream_t)stream);
   else if (use_waves(h, b->nc))
-    ce = clmgb::launch_moisture_form_waves(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
+    ce = clmgb::launch_moisture_form_waves(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, 0,
                                            h->dev_status, h->ws, waves_grid(h), (cudaStream_t)stream);
   else
-    ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
+    ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, 0,
                                            h->dev_status, h->queue, queue_grid(h), queue_scratch(h),
                                            (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
@@ -559,7 +590,7 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   if ((e = check_fields(fw))) return e;
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  const Dims D = make_dims(h->vp, *b);
+  const Dims D = make_dims(h->vp, *b, h->column_base);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce;
   if (h->step_schedule == CLMGB_SCHEDULE_FUSED) {
@@ -589,7 +620,7 @@ static int32_t phase_change_common(clmgb_handle h, const clmgb_bounds* b, const 
   if ((e = check_fields(f))) return e;
   if (!dhsdT) return CLMGB_ERR_NULL_ARG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_phase_change(make_dims(h->vp, *b), b->nc, *f, dtime, dhsdT, which,
+  cudaError_t ce = clmgb::launch_phase_change(make_dims(h->vp, *b, h->column_base), b->nc, *f, dtime, dhsdT, which,
                                               (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -613,7 +644,7 @@ int32_t clmgb_synth_forcing(clmgb_handle h, const clmgb_bounds* b, const clmgb_s
   if ((e = check_fields(ft))) return e;
   if ((e = check_fields(fw))) return e;
   if (!G || !I) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_synth_forcing(make_dims(h->vp, *b), b->nc, *ft, *fw, G, I, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_synth_forcing(make_dims(h->vp, *b, h->column_base), b->nc, *ft, *fw, G, I, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -710,6 +741,14 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value < 0 || value > 32) return CLMGB_ERR_CONFIG;
       h->fresh_batch = value;
       return CLMGB_OK;
+    case CLMGB_OPT_COLUMN_BASE:
+      if (value < 0) return CLMGB_ERR_CONFIG;
+      h->column_base = value;
+      return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_DEFER:
+      if (value < 0 || value > clmgb::MF_ATTEMPT_CAP) return CLMGB_ERR_CONFIG;
+      h->defer = value;
+      return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
   }
@@ -731,6 +770,8 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_ADJ_RICHARDS: *value = h->tape.richards_mode; return CLMGB_OK;
     case CLMGB_OPT_ADJ_SOIL_TEMPERATURE: *value = h->adj_st_mode; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_FRESH_BATCH: *value = h->fresh_batch; return CLMGB_OK;
+    case CLMGB_OPT_COLUMN_BASE: *value = h->column_base; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_DEFER: *value = h->defer; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_USED: {
       unsigned int used = 0;
@@ -875,7 +916,7 @@ int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const cl
   if ((e = check_log(log))) return e;
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  const Dims D = make_dims(h->vp, *b);
+  const Dims D = make_dims(h->vp, *b, h->column_base);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce = clmgb::launch_soiltemp_fractions(D, b->nc, *ft, *fw, dtime, snow_method, t_ssbef, t_h2osfc_bef,
                                                     col_status, h->dev_status, s);
@@ -915,7 +956,7 @@ int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, cons
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!h->tape_block) return CLMGB_ERR_CONFIG;
-  const Dims D = make_dims(h->vp, *b);
+  const Dims D = make_dims(h->vp, *b, h->column_base);
   if ((e = check_log(log))) return e;
   cudaError_t ce;
   if (h->adj_st_mode == CLMGB_ADJ_ST_CLOSED_FORM && h->tape.richards_mode == CLMGB_ADJ_RICHARDS_CLOSED_FORM)
@@ -938,7 +979,7 @@ int32_t clmgb_soil_water_warm(clmgb_handle h, const clmgb_bounds* b, const clmgb
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, col_status, 0,
+  cudaError_t ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, 0,
                                                      h->dev_status, h->queue, queue_grid(h), queue_scratch(h),
                                                      (cudaStream_t)stream, dt_first);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
@@ -955,7 +996,7 @@ int32_t clmgb_mlp_samples(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0) || per_column < 0) return CLMGB_ERR_CONFIG;
   if (!features || !targets || !count || capacity < 0) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_richards_samples(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, per_column, features,
+  cudaError_t ce = clmgb::launch_richards_samples(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, per_column, features,
                                                   targets, count, capacity, col_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -1020,7 +1061,7 @@ int32_t clmgb_mlp_features(clmgb_handle h, const clmgb_bounds* b, const clmgb_so
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!mean || !istd || !X) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_mlp_features(make_dims(h->vp, *b), b->nc, *f, *cfg, dtime, mean, istd, X,
+  cudaError_t ce = clmgb::launch_mlp_features(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, mean, istd, X,
                                               (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -1042,7 +1083,7 @@ int32_t clmgb_balance_begin(clmgb_handle h, const clmgb_bounds* b, const clmgb_s
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(ft))) return e;
   if (!t_grnd0 || !begwb) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_balance_begin(make_dims(h->vp, *b), b->nc, *ft, t_grnd0, begwb, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_balance_begin(make_dims(h->vp, *b, h->column_base), b->nc, *ft, t_grnd0, begwb, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -1058,7 +1099,7 @@ int32_t clmgb_balance_residuals(clmgb_handle h, const clmgb_bounds* b, const clm
   if ((e = check_fields(fw))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!t_ssbef || !t_h2osfc_bef || !t_grnd0 || !begwb || !errsoi || !errh2o) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_balance_residuals(make_dims(h->vp, *b), b->nc, *ft, *fw, dtime, t_ssbef, t_h2osfc_bef,
+  cudaError_t ce = clmgb::launch_balance_residuals(make_dims(h->vp, *b, h->column_base), b->nc, *ft, *fw, dtime, t_ssbef, t_h2osfc_bef,
                                                    t_grnd0, begwb, errsoi, errh2o, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }

@@ -66,7 +66,7 @@ __global__ void k_balance_residuals(Dims D, int64_t nc, clmgb_soiltemp_fields ft
                              fh * jl_pow4(t_h2osfc_bef[c]);
       for (int64_t p1 = ft.col_patchi[c]; p1 <= ft.col_patchf[c]; p1++) {
         const int64_t p = p1 - 1;
-        if (p < 0 || p >= D.np || ft.patch_column[p] != c + 1 || !ft.mask_nolakep[p]) continue;
+        if (p < 0 || p >= D.np || ft.patch_column[p] != c + 1 + D.c0 || !ft.mask_nolakep[p]) continue;
         const double gs = ((1.0 - fsno) * ft.sabg_soil[p] + fsno * ft.sabg_snow[p]) + ft.dlrad[p] +
                           (1.0 - (double)ft.frac_veg_nosno[p]) * eg * ft.forc_lwrad[c] - eg * SB * lw_grnd -
                           eg * SB * (tg0 * tg0 * tg0) * (4.0 * tinc) -

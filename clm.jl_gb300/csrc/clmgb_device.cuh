@@ -51,6 +51,7 @@ constexpr int MF_ATTEMPT_CAP = 4096;         // safety cap on Richards substep a
 struct Dims {
   int nlevsno, nlevgrnd, nlevsoi, nlevurb, nlevmax;
   int64_t ldc, ldp, np;
+  int64_t c0 = 0;    // global index of the call's first column (patch_column holds global indices)
 };
 
 // Julia Base.max / Base.min on Float64 (NaN propagates, -0.0 < 0.0).  They only
@@ -704,7 +705,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   for (int k = 0; k <= nlevsno + 1; k++) sabg_lyr_col[k] = 0.0;
   for (int64_t p1 = pi; p1 <= pf; p1++) {
     const int64_t p = p1 - 1;
-    if (f.patch_column[p] != c + 1) continue;
+    if (f.patch_column[p] != c + 1 + D.c0) continue;
     S dh_p = 0.0, hsoil_p = 0.0, hh_p = 0.0;
     const bool act = f.mask_nolakep[p] != 0;
     const S base = f.dlrad[p] + (1.0 - (double)f.frac_veg_nosno[p]) * eg * forc;

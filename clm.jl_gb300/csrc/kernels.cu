@@ -131,12 +131,17 @@ k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb
 // With LOG the kernel also writes the substep log of every column it solves (the
 // starting water of each accepted substep and the solve's outputs), for the step
 // adjoint; the solve itself is unchanged.
+// With qs.defer > 0 (never with LOG) a column that has made qs.defer attempts and
+// is not done leaves the lane at its next accepted substep: the lane stores the
+// column's state for the warp-per-column finish (k_moisture_form_coop) and takes
+// new work, so the few columns that need several times the mean number of attempts
+// no longer hold the kernel's end.
 template <bool LOG>
 __global__ void __launch_bounds__(BLOCK)
 k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                       uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
                       const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
-                      int64_t ld_imp, const double* dt_init, SubstepLogView lg, int fresh_batch) {
+                      int64_t ld_imp, const double* dt_init, SubstepLogView lg, int fresh_batch, QueueScratch qs) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned long long nq = order ? (unsigned long long)(*(volatile const unsigned int*)nlisted_ptr)
@@ -215,6 +220,18 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
         rec[(int64_t)nacc * SUB_REC + MAXSOI + 1] = dtd;
       }
       nacc++;
+    }
+    if (!LOG && !fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer) {
+      const int64_t c = L.c, cap = qs.capacity;
+      for (int j = 1; j <= L.nlayers; j++) qs.d_liq[(int64_t)(j - 1) * cap + c] = L.liq[j];
+      qs.d_dtsub[c] = L.dtsub;
+      qs.d_dtdone[c] = L.dtdone;
+      qs.d_qc[c] = L.qc;
+      qs.d_nsub[c] = L.nsub;
+      qs.d_status[c] = L.status;
+      qs.d_list[atomicAdd(qs.d_count, 1ULL)] = (uint32_t)c;
+      active = false;
+      continue;
     }
     if (fin) {
       const uint32_t st = mf_end(L, D, f);
@@ -471,16 +488,21 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   const unsigned int* nl = listed ? qs.bins + 2 * ORDER_BINS : nullptr;
   const double* imp = use ? qs.imp : nullptr;
   const int64_t ldi = use ? qs.capacity : 0;
+  QueueScratch q = qs;
+  if (!use || log || !q.d_count) q.defer = 0;              // deferral needs the reserved scratch
+  if (q.defer > 0 && (e = cudaMemsetAsync(q.d_count, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
   if (log)
     k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                       dev_status, queue, ord, nl, imp, ldi, dt_init,
-                                                                      *log, qs.fresh_batch);
+                                                                      *log, qs.fresh_batch, q);
   else
     k_moisture_form_queue<false><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                        dev_status, queue, ord, nl, imp, ldi, dt_init,
                                                                        SubstepLogView{nullptr, nullptr, 0, 0},
-                                                                       qs.fresh_batch);
-  return cudaGetLastError();
+                                                                       qs.fresh_batch, q);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (q.defer > 0) return launch_moisture_form_coop(D, nc, f, cfg, dtime, col_status, or_status, dev_status, q, grid, s);
+  return cudaSuccess;
 }
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {
   k_math_eval<<<grid_for(n), BLOCK, 0, s>>>(op, n, x, y, out);

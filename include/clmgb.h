@@ -681,6 +681,15 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             for the hydraulic block until this many lanes of the warp need it
                                             (or no lane can attempt), then run it together; 0 = at once.
                                             Results do not depend on it. */
+#define CLMGB_OPT_QUEUE_DEFER         16 /* work-queue Richards kernel with reserved scratch: a column not done
+                                            after this many attempts leaves the queue at its next accepted
+                                            substep and is finished by one warp (one level per lane); 0 = off.
+                                            Results do not depend on it. */
+#define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls
+                                            receive (default 0).  A caller that runs a column range [c0, c1)
+                                            passes column arrays advanced by c0 (same ldc) and the patch
+                                            arrays whole, since col_patchi/col_patchf and patch_column
+                                            hold global indices, and sets this to c0. */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
 /* Gives the handle per-column scratch for up to max_nc columns (about 48*nlevsoi + 80
  * bytes per column): the Richards solve then forms the ice impedances in a uniform
@@ -1097,6 +1106,13 @@ typedef struct clmgb_balance_report {
  * read (:1124-1160, :1347-1365), reduced on the device.  The report is written to host
  * memory, so the call waits for `stream`.  Whether a flagged error stops the model
  * (hard_error, skip_steps, DAnstep) stays with the caller, as in the reference. */
+/* Copies `rows` rows of `width` bytes between host and device memory (either direction),
+ * stride dst_pitch / src_pitch bytes, asynchronously on `stream`: the columns [c0, c1)
+ * of a [ldc, levels] field are rows = levels, width = (c1 - c0) * 8, pitch = ldc * 8.
+ * Host memory should be page-locked for the copy to overlap kernels. */
+int32_t clmgb_copy_columns(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch, int64_t width,
+                           int64_t rows, void* stream);
+
 int32_t clmgb_balance_check_columns(clmgb_handle h, const clmgb_bounds* b, const clmgb_colbalance_fields* f,
                                     double dtime, clmgb_balance_report* report, void* stream);
 

@@ -59,7 +59,7 @@ def test_header_constants_match_python():
     for name in ("COL_ADJ_UNSUPPORTED", "COL_TAPE_FULL", "OPT_ADJ_TAPE_USED", "OPT_ADJ_TAPE_SLOTS",
                  "OPT_ADJ_TAPE_ENTRIES", "OPT_STEP_SCHEDULE", "OPT_WAVES_OCCUPANCY", "OPT_ADJ_RICHARDS",
                  "ADJ_RICHARDS_CLOSED_FORM", "ADJ_RICHARDS_RECORDED", "COL_ADJ_REPLAY", "ADJ_MAX_SUBSTEPS",
-                 "OPT_ADJ_SOIL_TEMPERATURE", "ADJ_ST_CLOSED_FORM", "ADJ_ST_RECORDED", "OPT_QUEUE_FRESH_BATCH",
+                 "OPT_ADJ_SOIL_TEMPERATURE", "ADJ_ST_CLOSED_FORM", "ADJ_ST_RECORDED", "OPT_QUEUE_FRESH_BATCH", "OPT_COLUMN_BASE", "OPT_QUEUE_DEFER",
                  "COL_FILTER"):
         assert int(consts[name]) == getattr(abi, name), name
     for name in ("SH_FLOODC", "SH_SAT_EXCESS", "SH_QFLX_INPUTS", "SH_INFL_EXCESS", "SH_ROUTE", "SH_UPDATE_H2OSFC",

@@ -37,3 +37,34 @@ def test_host_stepper_matches_device_steps():
         assert hs.h2d_bytes < 0.4 * hoststep.nbytes(host, list(host))
     finally:
         h.close()
+
+
+@pytest.mark.parametrize("chunks", [2, 3, 7])
+def test_chunked_host_stepper_matches_device_steps(chunks):
+    nsteps = 4
+    wl = synth.make_workload(2, nc=3001, seed=12, nsteps=nsteps)
+    cfg = abi.SwmConfig.clm5_default()
+    h = api.Handle(wl.state.vp)
+    try:
+        h.reserve(wl.state.nc)
+        G, I = wl.forcing_block(range(nsteps))
+        Gd, Id = torch.from_numpy(G).cuda(), torch.from_numpy(I).cuda()
+        d = wl.state.to_device()
+        for t in range(nsteps):
+            api.synth_forcing(h, d, Gd[t], Id[t])
+            api.soil_temperature(h, d, wl.dtime)
+            api.set_soil_water_fractions(h, d)
+            api.soil_water(h, d, wl.dtime, cfg)
+        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in wl.state.arrays.items()}
+        hs = hoststep.HostStepper(h, host, wl.state.to_device(), wl.dtime, cfg, chunks=chunks)
+        assert len(hs.ranges) == chunks
+        for t in range(nsteps):
+            hs.step_chunked(forcing=lambda v, t=t: api.synth_forcing(h, v, Gd[t][v.c0:v.c1], Id[t][v.c0:v.c1]))
+        torch.cuda.synchronize()
+        written = set(hoststep.WRITTEN_TEMPERATURE) | set(hoststep.WRITTEN_WATER)
+        for k in written:
+            assert torch.equal(host[k], d[k].cpu()), k
+        assert h.get_option(abi.OPT_COLUMN_BASE) == 0
+        assert h.device_status() == 0
+    finally:
+        h.close()
