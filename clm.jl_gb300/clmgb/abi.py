@@ -67,7 +67,7 @@ OPT_COLUMN_BASE = 15
 OPT_QUEUE_DEFER = 16
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
-COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY, COL_FILTER = 32, 64, 128, 256
+COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY, COL_FILTER, COL_QUEUE_WAIT = 32, 64, 128, 256, 512
 ADJ_MAX_SUBSTEPS = 128
 
 CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20

@@ -22,9 +22,9 @@ struct clmgb_handle_s {
   int device;
   int num_sms;
   clmgb_varpar vp;
-  // device scratch owned by the handle (one allocation of 8 words): the status word
-  // (OR of CLMGB_COL_* bits), the Richards work-queue counter, and 5 words for the
-  // reductions of clmgb_balance_check_columns
+  // device scratch owned by the handle (one allocation of 12 words): the status word
+  // (OR of CLMGB_COL_* bits), the Richards work-queue counter, 5 words for the
+  // reductions of clmgb_balance_check_columns, 3 counters of deferred columns
   unsigned long long* scratch;
   uint32_t* dev_status;
   unsigned long long* queue;
@@ -61,8 +61,10 @@ static const int64_t CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM = 2;
 static const int64_t CLMGB_DEFAULT_FRESH_BATCH = 20;
 // Attempts after which the work-queue kernel hands a column to the warp-per-column
 // finish (CLMGB_OPT_QUEUE_DEFER).  Measured on GB300, 262,144 columns of the scale
-// workload, ms per column step: off 27.1, 8 -> 32.8, 12 -> 27.7, 16 -> 25.5,
-// 20 -> 24.6, 24 -> 24.4, 28 -> 24.8, 32 -> 25.2, 40 -> 25.8, 56 -> 26.8.
+// workload, 2 blocks/SM, ms per column step: off 27.1, 12 -> 40.3, 16 -> 29.9,
+// 18 -> 30.2, 20 -> 25.2, 22 -> 23.8, 24 -> 23.6, 26 -> 23.9, 30 -> 24.4, 36 -> 25.0
+// (3 blocks/SM: 24 -> 23.4).  Below ~20 the deferred backlog, finished at a few
+// times the cost per attempt, outweighs the shorter end of the queue.
 static const int64_t CLMGB_DEFAULT_QUEUE_DEFER = 24;
 
 using clmgb::Dims;
@@ -218,8 +220,8 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->waves_blocks_per_sm = 0;
   cudaError_t ce = cudaGetDevice(&h->device);
   if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
-  if (ce == cudaSuccess) ce = cudaMalloc(&h->scratch, 8 * sizeof(unsigned long long));
-  if (ce == cudaSuccess) ce = cudaMemset(h->scratch, 0, 8 * sizeof(unsigned long long));
+  if (ce == cudaSuccess) ce = cudaMalloc(&h->scratch, 12 * sizeof(unsigned long long));
+  if (ce == cudaSuccess) ce = cudaMemset(h->scratch, 0, 12 * sizeof(unsigned long long));
   if (ce == cudaSuccess) {
     h->dev_status = reinterpret_cast<uint32_t*>(h->scratch);
     h->queue = h->scratch + 1;

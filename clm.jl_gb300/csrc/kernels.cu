@@ -1,6 +1,7 @@
 // kernels.cu — CUDA kernels of the soil/snow column solve (one thread per column).
 #include "clmgb_device.cuh"
 #include "launch.h"
+#include "richards_coop.cuh"
 
 namespace clmgb {
 
@@ -133,9 +134,10 @@ k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb
 // adjoint; the solve itself is unchanged.
 // With qs.defer > 0 (never with LOG) a column that has made qs.defer attempts and
 // is not done leaves the lane at its next accepted substep: the lane stores the
-// column's state for the warp-per-column finish (k_moisture_form_coop) and takes
-// new work, so the few columns that need several times the mean number of attempts
-// no longer hold the kernel's end.
+// column's state and takes new work, and warps that run out of queued columns
+// finish the deferred ones one warp per column (coop_drain, richards_coop.cuh), so
+// the few columns that need several times the mean number of attempts no longer
+// hold the kernel's end with one useful lane per warp.
 template <bool LOG>
 __global__ void __launch_bounds__(BLOCK)
 k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
@@ -179,7 +181,11 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
       }
     }
     if (!__any_sync(FULL, active)) {
-      if (__all_sync(FULL, exhausted)) break;
+      if (__all_sync(FULL, exhausted)) {
+        // no queued column left for this warp: finish deferred ones, one warp each
+        if (!LOG && qs.defer > 0) coop_drain(D, f, cfg, dtime, col_status, or_status, dev_status, qs);
+        break;
+      }
       continue;
     }
     // Batched refresh.  A lane whose substep was just accepted needs the hydraulic
@@ -222,14 +228,19 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
       nacc++;
     }
     if (!LOG && !fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer) {
+      // hand the column over: claim a list slot, store the state, then publish
       const int64_t c = L.c, cap = qs.capacity;
+      const unsigned long long slot = atomicAdd(qs.d_count, 1ULL);
       for (int j = 1; j <= L.nlayers; j++) qs.d_liq[(int64_t)(j - 1) * cap + c] = L.liq[j];
       qs.d_dtsub[c] = L.dtsub;
       qs.d_dtdone[c] = L.dtdone;
       qs.d_qc[c] = L.qc;
       qs.d_nsub[c] = L.nsub;
       qs.d_status[c] = L.status;
-      qs.d_list[atomicAdd(qs.d_count, 1ULL)] = (uint32_t)c;
+      __threadfence();
+      *(volatile uint32_t*)(qs.d_list + slot) = (uint32_t)c;
+      __threadfence();
+      atomicAdd(qs.d_count + 1, 1ULL);
       active = false;
       continue;
     }
@@ -490,7 +501,10 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   const int64_t ldi = use ? qs.capacity : 0;
   QueueScratch q = qs;
   if (!use || log || !q.d_count) q.defer = 0;              // deferral needs the reserved scratch
-  if (q.defer > 0 && (e = cudaMemsetAsync(q.d_count, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
+  if (q.defer > 0) {                                       // empty list, zero claim/publish/consume counts
+    if ((e = cudaMemsetAsync(q.d_count, 0, 3 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(q.d_list, 0xff, (size_t)nc * sizeof(uint32_t), s)) != cudaSuccess) return e;
+  }
   if (log)
     k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                       dev_status, queue, ord, nl, imp, ldi, dt_init,
@@ -500,9 +514,7 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
                                                                        dev_status, queue, ord, nl, imp, ldi, dt_init,
                                                                        SubstepLogView{nullptr, nullptr, 0, 0},
                                                                        qs.fresh_batch, q);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (q.defer > 0) return launch_moisture_form_coop(D, nc, f, cfg, dtime, col_status, or_status, dev_status, q, grid, s);
-  return cudaSuccess;
+  return cudaGetLastError();
 }
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {
   k_math_eval<<<grid_for(n), BLOCK, 0, s>>>(op, n, x, y, out);

@@ -21,8 +21,9 @@ struct QueueScratch {
   int fresh_batch;   // CLMGB_OPT_QUEUE_FRESH_BATCH (0: refresh at once)
   // CLMGB_OPT_QUEUE_DEFER: a column still unfinished after `defer` attempts leaves the
   // work queue at its next accepted substep; its state (water [nlevsoi][capacity],
-  // dtsub, dtdone, qcharge so far, attempts, status at index c) and its index (list,
-  // count) are kept for the warp-per-column finish (richards_coop.cu).  0: off.
+  // dtsub, dtdone, qcharge so far, attempts, status at index c) and its index (list)
+  // are kept for the warp-per-column finish (richards_coop.cuh).  d_count: the
+  // claimed, published and consumed list slots.  0: off.
   int defer;
   double *d_liq, *d_dtsub, *d_dtdone, *d_qc;
   int* d_nsub;
@@ -129,11 +130,6 @@ cudaError_t launch_lake_temperature(const Dims& D, int64_t nc, const clmgb_lake_
                                     double dtime, uint32_t* dev_status, cudaStream_t s);
 cudaError_t launch_colbalance(int64_t nc, const clmgb_colbalance_fields& f, double dtime, unsigned long long* r,
                               cudaStream_t s);
-// finishes the columns the work-queue kernel deferred (QueueScratch::defer), one warp
-// per column; reads the deferred count on the device
-cudaError_t launch_moisture_form_coop(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
-                                      const clmgb_swm_config& cfg, double dtime, uint32_t* col_status, int or_status,
-                                      uint32_t* dev_status, const QueueScratch& qs, int grid_blocks, cudaStream_t s);
 cudaError_t launch_soil_fluxes(const Dims& D, int64_t nc, int64_t nl, const clmgb_soilflux_fields& f, double dtime,
                                uint32_t* dev_status, cudaStream_t s);
 int vjp_cf_blocks_per_sm();

@@ -63,6 +63,8 @@ extern "C" {
                                         of clmgb_reserve_adjoint) */
 #define CLMGB_COL_ADJ_REPLAY   128u  /* step adjoint: a replayed substep was not accepted again
                                         (its adjoint is not valid) */
+#define CLMGB_COL_QUEUE_WAIT   512u  /* Richards work queue: a bounded wait for a deferred column's
+                                        index gave up; the column was left unfinished (not expected) */
 #define CLMGB_COL_FILTER       256u  /* root sink: the column is in two of the reference's filters
                                         (a pervious road on a natural-vegetation landunit) */
 
