@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--nc", type=int, default=262144)
     ap.add_argument("--cfg", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=8)
-    ap.add_argument("--e2e-chunks", type=int, default=4,
+    ap.add_argument("--e2e-chunks", type=int, default=1,
                     help="column ranges of the end-to-end step (uploads and read-backs overlap the other ranges)")
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -556,8 +556,9 @@ def run_ours(args):
                "h2d_bytes_per_step": hs.h2d_bytes, "d2h_bytes_per_step": hs.d2h_bytes,
                "chunks": len(hs.ranges),
                "note": "host-resident state: per step H2D of the inputs other modules change, D2H of every "
-                       "written field; the step runs over column ranges so each range's upload and read-back "
-                       "overlap the other ranges' compute; parameters/geometry/topology uploaded once"}
+                       "written field, the soil-temperature outputs read back during the Richards solve "
+                       "(with --e2e-chunks > 1 the step runs over column ranges); "
+                       "parameters/geometry/topology uploaded once"}
         del host, hs
 
     cpu = None
