@@ -122,12 +122,14 @@ CM_FN double cm_exp(double x) {
   return CM_MUL(CM_AS_F64(CM_AS_U64(res) + ((uint64_t)(n + 1000) << 52)), 0x1p-1000);
 }
 
-// x^y (Julia Base ^ for Float64 arguments).
+// x^y (Julia Base ^ for Float64 arguments).  The tests of the common case look at
+// the bit patterns (integer pipes): y == +-0, x == 1, x or y NaN, 0 < x < Inf.
 CM_FN double cm_pow(double x, double y) {
-  if (y == 0.0) return 1.0;
-  if (x == 1.0) return 1.0;
-  if (x != x || y != y) return CM_ADD(x, y);
-  if (x > 0.0 && x < CM_INF) return cm_exp(CM_MUL(y, cm_log(x)));
+  const uint64_t ux = CM_AS_U64(x), uy = CM_AS_U64(y);
+  if ((uy << 1) == 0) return 1.0;
+  if (ux == 0x3ff0000000000000ULL) return 1.0;
+  if ((ux << 1) > 0xffe0000000000000ULL || (uy << 1) > 0xffe0000000000000ULL) return CM_ADD(x, y);
+  if (ux - 1 < 0x7fefffffffffffffULL) return cm_exp(CM_MUL(y, cm_log(x)));
   const double ay = y < 0.0 ? -y : y;
   const bool yint = (ay < 0x1p53) ? ((double)(int64_t)ay == ay) : true;
   const bool yodd = yint && ay < 0x1p53 && (((int64_t)ay) & 1);
@@ -145,6 +147,15 @@ CM_FN double cm_pow(double x, double y) {
   if (!yint) return CM_NAN;
   const double v = cm_exp(CM_MUL(y, cm_log(-x)));
   return yodd ? -v : v;
+}
+
+// x^y for a positive finite x other than 1 whose logarithm lx = cm_log(x) the caller
+// formed once: the value of cm_pow(x, y) for every y, without forming cm_log(x) again.
+CM_FN double cm_pow_lx(double x, double lx, double y) {
+  const uint64_t uy = CM_AS_U64(y);
+  if ((uy << 1) == 0) return 1.0;
+  if ((uy << 1) > 0xffe0000000000000ULL) return CM_ADD(x, y);
+  return cm_exp(CM_MUL(y, lx));
 }
 
 // Base-10 logarithm.

@@ -576,6 +576,8 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
   double zz[MAXL + 2];
 
   // ---- soil_therm_prop!: layer conductivity thk (_soil_snow_tk_kernel! :647-716) ----
+  // the logarithms of the two constant bases of tkwat^x and tkice^x, formed once
+  const double ln_tkwat = cm_log(TKWAT), ln_tkice = cm_log(TKICE);
   // thk kept in tk[] first, interface conductivity computed in place afterwards.
   for (int jj = jjtop; jj <= nlev; jj++) {
     tt[jj] = X.T(jj);
@@ -602,7 +604,8 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
             const S a1 = liq / (DENH2O * dzv);
             const S fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
             const S fl = a1 / fl_denom;
-            const S dksat = LVc(f.tkmg, c, j, ld) * cm_pow(TKWAT, fl * ws) * cm_pow(TKICE, (1.0 - fl) * ws);
+            const S dksat =
+                LVc(f.tkmg, c, j, ld) * cm_pow_lx(TKWAT, ln_tkwat, fl * ws) * cm_pow_lx(TKICE, ln_tkice, (1.0 - fl) * ws);
             thkv = dke * dksat + (1.0 - dke) * LVc(f.tkdry, c, j, ld);
           } else {
             thkv = LVc(f.tkdry, c, j, ld);
@@ -937,11 +940,15 @@ struct MfLaneT {
   uint32_t status;
   double dtsub, dtdone, dt_cur;
   S qc;
+  // the refresh's values the attempts read: the inflow of level 1, the bottom
+  // level's conductivity and its derivative (the flux lower boundary's recharge)
+  S qin1, hk_bot, dhkdw_bot;
   double dzv[MAXSOI + 1], dt_dz[MAXSOI + 1];
   S liq[MAXSOI + 1], imp[MAXSOI + 1];
-  S hk[MAXSOI + 1], dhkdw[MAXSOI + 1];
-  S qin[MAXSOI + 1], qout[MAXSOI + 1], dqidw0[MAXSOI + 1], dqidw1[MAXSOI + 1];
-  S dqodw1[MAXSOI + 1], dqodw2[MAXSOI + 1], fnet1[MAXSOI + 1];
+  // outflow of each level and its derivatives; the inflow of level j > 1 and its
+  // derivatives are the outflow ones of level j-1 (qin[j] = qout[j-1],
+  // dqidw0[j] = dqodw1[j-1], dqidw1[j] = dqodw2[j-1], :1372-1376)
+  S qout[MAXSOI + 1], dqodw1[MAXSOI + 1], dqodw2[MAXSOI + 1], fnet1[MAXSOI + 1];
   S gam[MAXSOI + 1], dwat[MAXSOI + 1];
 };
 typedef MfLaneT<double> MfLane;
@@ -957,8 +964,9 @@ constexpr int LOG_FIN = 3 * MAXSOI + 3;
 // layer), as formed at soil_water_movement.jl:1287-1293.
 template <class ST>
 __device__ __forceinline__ typename ST::S mf_impedance(double e_ice, int j, int nlayers, ST& X) {
-  if (j == nlayers) return cm_pow(10.0, -e_ice * X.Icefrac(j));
-  return cm_pow(10.0, -e_ice * (0.5 * (X.Icefrac(j) + X.Icefrac(j + 1))));
+  const double ln10 = cm_log(10.0);
+  if (j == nlayers) return cm_pow_lx(10.0, ln10, -e_ice * X.Icefrac(j));
+  return cm_pow_lx(10.0, ln10, -e_ice * (0.5 * (X.Icefrac(j) + X.Icefrac(j + 1))));
 }
 __device__ __forceinline__ double mf_impedance(const Dims& D, const clmgb_soilwater_fields& f, double e_ice,
                                                int64_t c, int j, int nlayers) {
@@ -1023,79 +1031,73 @@ __device__ __forceinline__ void mf_refresh(MfLaneT<typename ST::S>& L, const Dim
   const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
   const int nlayers = L.nlayers;
   const int lower_bc = cfg.lower_boundary_condition;
-  // ---- hydraulic properties (Clapp-Hornberger inlined, :1280-1308) ----
-  S s2[MAXSOI + 2], smp[MAXSOI + 1], dsmpdw[MAXSOI + 1];
-  for (int j = 1; j <= nlayers; j++) {
+  // Level by level: the saturation of level j+1, the hydraulic properties of level j
+  // (Clapp-Hornberger inlined, :1280-1308), then the flux between levels j-1 and j
+  // and its derivatives (:1310-1345), which need both levels' properties.  Every
+  // value is formed by the reference's expression; only the loop order differs, so
+  // no level's arrays are kept beyond the two the flux needs.
+  auto saturation = [&](int j) -> S {
     const S vwc = jl_max(L.liq[j], 1.0e-6) / (L.dzv[j] * DENH2O);
     S s = vwc / X.Watsat(j);
     s = jl_min(s, 1.0);
-    s = jl_max(0.01, s);
-    s2[j] = s;
-  }
+    return jl_max(0.01, s);
+  };
+  S s_j = saturation(1);
+  S hk_p = 0.0, dhkdw_p = 0.0, smp_p = 0.0, dsmpdw_p = 0.0;   // level j-1
+  S hk_j = 0.0, dhkdw_j = 0.0, smp_j = 0.0, dsmpdw_j = 0.0;
   for (int j = 1; j <= nlayers; j++) {
-    S s1 = (j == nlayers) ? s2[j] : 0.5 * (s2[j] + s2[j + 1]);
+    const S s_n = (j < nlayers) ? saturation(j + 1) : s_j;
+    S s1 = (j == nlayers) ? s_j : 0.5 * (s_j + s_n);
     s1 = jl_min(s1, 1.0);
     s1 = jl_max(0.01, s1);
     const S b = X.Bsw(j);
-    const S hkv = L.imp[j] * X.Hksat(j) * cm_pow(s1, 2.0 * b + 3.0);
-    const S dhkds = (2.0 * b + 3.0) * hkv / s1;
-    const S sn = s2[j];
-    const S smpv = -X.Sucsat(j) * cm_pow(sn, -b);
-    const S dsmpds = -b * smpv / sn;
-    L.hk[j] = hkv;
-    smp[j] = smpv;
-    L.dhkdw[j] = dhkds;
-    dsmpdw[j] = dsmpds / X.Watsat(j);
-    LV(f.smp_l, c, j, ld) = VAL(smpv);
-    LV(f.hk_l, c, j, ld) = VAL(hkv);
+    hk_j = L.imp[j] * X.Hksat(j) * cm_pow(s1, 2.0 * b + 3.0);
+    dhkdw_j = (2.0 * b + 3.0) * hk_j / s1;
+    const S sn = s_j;
+    smp_j = -X.Sucsat(j) * cm_pow(sn, -b);
+    const S dsmpds = -b * smp_j / sn;
+    dsmpdw_j = dsmpds / X.Watsat(j);
+    LV(f.smp_l, c, j, ld) = VAL(smp_j);
+    LV(f.hk_l, c, j, ld) = VAL(hk_j);
+    if (j >= 2) {
+      const int k = j - 1;
+      const S dhkds1 = 0.5 * dhkdw_p / X.Watsat(k);
+      const S dhkds2 = 0.5 * dhkdw_p / X.Watsat(k + 1);
+      const S num = smp_j - smp_p;
+      const double den = M_TO_MM * (LVc(f.z, c, joff + k + 1, ld) - LVc(f.z, c, joff + k, ld));
+      L.qout[k] = -hk_p * num / den + hk_p;
+      L.dqodw1[k] = (hk_p * dsmpdw_p - dhkds1 * num) / den + dhkds1;
+      L.dqodw2[k] = (-hk_p * dsmpdw_j - dhkds2 * num) / den + dhkds2;
+    }
+    hk_p = hk_j; dhkdw_p = dhkdw_j; smp_p = smp_j; dsmpdw_p = dsmpdw_j;
+    s_j = s_n;
   }
-  // ---- fluxes and derivatives (:1310-1378) ----
-  for (int j = 1; j <= nlayers; j++) {
-    L.qin[j] = 0.0; L.qout[j] = 0.0; L.dqidw0[j] = 0.0; L.dqidw1[j] = 0.0;
-    L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
-  }
-  for (int j = 1; j <= nlayers - 1; j++) {
-    const S dhkds1 = 0.5 * L.dhkdw[j] / X.Watsat(j);
-    const S dhkds2 = 0.5 * L.dhkdw[j] / X.Watsat(j + 1);
-    const S num = smp[j + 1] - smp[j];
-    const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
-    L.qout[j] = -L.hk[j] * num / den + L.hk[j];
-    L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1 * num) / den + dhkds1;
-    L.dqodw2[j] = (-L.hk[j] * dsmpdw[j + 1] - dhkds2 * num) / den + dhkds2;
-  }
+  L.hk_bot = hk_j;
+  L.dhkdw_bot = dhkdw_j;
+  // ---- bottom level (:1347-1370) ----
   {
     const int j = nlayers;
+    L.qout[j] = 0.0; L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
     if (lower_bc == CLMGB_BC_WATERTABLE) {
       int jwt = nlevsoi;
       for (int jj = 1; jj <= nlevsoi; jj++) {
         if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
       }
-      if (j > jwt) {
-        L.qout[j] = 0.0; L.dqodw1[j] = 0.0; L.dqodw2[j] = 0.0;
-      } else {
-        const S dhkds1l = L.dhkdw[j] / X.Watsat(j);
-        const S num = -smp[j];
+      if (j <= jwt) {
+        const S dhkds1l = dhkdw_j / X.Watsat(j);
+        const S num = -smp_j;
         const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
-        L.qout[j] = -L.hk[j] * num / den + L.hk[j];
-        L.dqodw1[j] = (L.hk[j] * dsmpdw[j] - dhkds1l * num) / den + dhkds1l;
-        L.dqodw2[j] = 0.0;
+        L.qout[j] = -hk_j * num / den + hk_j;
+        L.dqodw1[j] = (hk_j * dsmpdw_j - dhkds1l * num) / den + dhkds1l;
       }
     } else if (lower_bc == CLMGB_BC_FLUX) {
-      L.qout[j] = L.hk[j];
-      L.dqodw1[j] = L.dhkdw[j] / X.Watsat(j);
-    } else {
-      L.qout[j] = 0.0;
-      L.dqodw1[j] = 0.0;
+      L.qout[j] = hk_j;
+      L.dqodw1[j] = dhkdw_j / X.Watsat(j);
     }
   }
-  for (int j = 2; j <= nlayers; j++) {
-    L.qin[j] = L.qout[j - 1];
-    L.dqidw0[j] = L.dqodw1[j - 1];
-    L.dqidw1[j] = L.dqodw2[j - 1];
-  }
-  L.qin[1] = f.qflx_infl[c];
-  L.dqidw1[1] = 0.0;
-  for (int j = 1; j <= nlayers; j++) L.fnet1[j] = L.qin[j] - L.qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
+  L.qin1 = f.qflx_infl[c];
+  L.fnet1[1] = L.qin1 - L.qout[1] - LVc(f.qflx_rootsoi, c, 1, ld);
+  for (int j = 2; j <= nlayers; j++) L.fnet1[j] = L.qout[j - 1] - L.qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
   L.fresh = false;
 }
 
@@ -1141,7 +1143,8 @@ __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dim
   S bet, dwat_prev;
   {
     const S rmx = -L.fnet1[1] * L.dt_dz[1];
-    const S bmx = -1.0 - (-L.dqidw1[1] + L.dqodw1[1]) * L.dt_dz[1];
+    const S dqidw1_1 = 0.0;                                   // no inflow derivative at level 1
+    const S bmx = -1.0 - (-dqidw1_1 + L.dqodw1[1]) * L.dt_dz[1];
     bet = bmx;
     if (abs_lt(VAL(bet), 1.0e-30)) bet = 1.0e-30;
     dwat_prev = rmx / bet;
@@ -1149,8 +1152,8 @@ __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dim
   }
   S cmx_prev = -L.dqodw2[1] * L.dt_dz[1];
   for (int j = 2; j <= nlayers; j++) {
-    const S amx = L.dqidw0[j] * L.dt_dz[j];
-    const S bmx = -1.0 - (-L.dqidw1[j] + L.dqodw1[j]) * L.dt_dz[j];
+    const S amx = L.dqodw1[j - 1] * L.dt_dz[j];
+    const S bmx = -1.0 - (-L.dqodw2[j - 1] + L.dqodw1[j]) * L.dt_dz[j];
     S cmx = 0.0;
     if (j != nlayers) cmx = -L.dqodw2[j] * L.dt_dz[j];
     const S rmx = -L.fnet1[j] * L.dt_dz[j];
@@ -1174,9 +1177,10 @@ __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dim
   for (int j = 1; j <= nlayers; j++) {
     double fnet0;
     if (expensive) {
-      const double qin_test = j == 1 ? VAL(L.qin[j]) + VAL(L.dqidw1[j]) * VAL(L.dwat[j])
-                                     : VAL(L.qin[j]) + VAL(L.dqidw0[j]) * VAL(L.dwat[j - 1]) +
-                                           VAL(L.dqidw1[j]) * VAL(L.dwat[j]);
+      const double dqidw1_1 = 0.0;
+      const double qin_test = j == 1 ? VAL(L.qin1) + dqidw1_1 * VAL(L.dwat[j])
+                                     : VAL(L.qout[j - 1]) + VAL(L.dqodw1[j - 1]) * VAL(L.dwat[j - 1]) +
+                                           VAL(L.dqodw2[j - 1]) * VAL(L.dwat[j]);
       const double qout_test = j == nlayers ? VAL(L.qout[j]) + VAL(L.dqodw1[j]) * VAL(L.dwat[j])
                                             : VAL(L.qout[j]) + VAL(L.dqodw1[j]) * VAL(L.dwat[j]) +
                                                   VAL(L.dqodw2[j]) * VAL(L.dwat[j + 1]);
@@ -1196,7 +1200,7 @@ __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dim
   for (int j = 1; j <= nlayers; j++) L.liq[j] = L.liq[j] + L.dwat[j] * (M_TO_MM * L.dzv[j]);
   L.fresh = true;
   S qcTemp;
-  if (lower_bc == CLMGB_BC_FLUX) qcTemp = L.hk[nlayers] + L.dhkdw[nlayers] * L.dwat[nlayers];
+  if (lower_bc == CLMGB_BC_FLUX) qcTemp = L.hk_bot + L.dhkdw_bot * L.dwat[nlayers];
   else if (lower_bc == CLMGB_BC_ZERO_FLUX) qcTemp = 0.0;
   else qcTemp = L.qout[nlayers] + L.dqodw1[nlayers] * L.dwat[nlayers];
   L.qc += qcTemp * (dtsub / dtime);
