@@ -30,6 +30,7 @@ struct clmgb_handle_s {
   unsigned long long* queue;
   int64_t column_base;          // CLMGB_OPT_COLUMN_BASE
   int64_t defer;                // CLMGB_OPT_QUEUE_DEFER
+  int64_t packed;               // CLMGB_OPT_QUEUE_PACKED_REFRESH
   int64_t step_schedule;        // CLMGB_OPT_STEP_SCHEDULE
   int64_t queue_blocks_per_sm;  // CLMGB_OPT_QUEUE_BLOCKS_PER_SM (0 = occupancy limit)
   int occupancy_blocks;         // occupancy limit of the queue kernel
@@ -56,9 +57,11 @@ static const uint32_t HANDLE_MAGIC = 0xC1A9B300u;
 // M column-steps/s.
 static const int64_t CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM = 2;
 // Lanes of the work-queue kernel that batch the hydraulic block (CLMGB_OPT_QUEUE_FRESH_BATCH).
-// Measured on GB300 at 262,144 columns (2 blocks/SM): 0 -> 10.16, 8 -> 10.36, 16 -> 10.47,
-// 20 -> 10.54, 24 -> 10.51 M column-steps/s.
-static const int64_t CLMGB_DEFAULT_FRESH_BATCH = 20;
+// Measured on GB300 at 262,144 columns (2 blocks/SM), Richards ms per call with the
+// packed refresh: 1 -> 12.73, 2 -> 12.73, 4 -> 12.71, 8 -> 12.77, 12 -> 12.84, 20 -> 13.00
+// (the per-lane refresh: 14.82 at 20, its best; 0 -> 10.16, 8 -> 10.36, 16 -> 10.47,
+// 20 -> 10.54, 24 -> 10.51 M column-steps/s when it was the default).
+static const int64_t CLMGB_DEFAULT_FRESH_BATCH = 4;
 // Attempts after which the work-queue kernel hands a column to the warp-per-column
 // finish (CLMGB_OPT_QUEUE_DEFER).  Measured on GB300, 262,144 columns of the scale
 // workload, 2 blocks/SM, ms per column step: off 27.1, 12 -> 40.3, 16 -> 29.9,
@@ -142,6 +145,7 @@ static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
   // deferred columns keep their state in the wave scratch of the same reservation
   const bool have = h->ws.cap == h->qs.capacity && h->ws.cap > 0;
   q.defer = have ? (int)h->defer : 0;
+  q.packed = (int)h->packed;
   q.d_liq = have ? h->ws.qout : nullptr;
   q.d_dtsub = have ? h->ws.dtsub : nullptr;
   q.d_dtdone = have ? h->ws.dtdone : nullptr;
@@ -204,6 +208,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->last_error = cudaSuccess;
   h->column_base = 0;
   h->defer = CLMGB_DEFAULT_QUEUE_DEFER;
+  h->packed = 1;
   h->step_schedule = CLMGB_SCHEDULE_QUEUE;
   h->queue_blocks_per_sm = CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM;
   h->scratch = nullptr;
@@ -751,6 +756,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value < 0 || value > clmgb::MF_ATTEMPT_CAP) return CLMGB_ERR_CONFIG;
       h->defer = value;
       return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_PACKED_REFRESH:
+      if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
+      h->packed = value;
+      return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
   }
@@ -774,6 +783,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_QUEUE_FRESH_BATCH: *value = h->fresh_batch; return CLMGB_OK;
     case CLMGB_OPT_COLUMN_BASE: *value = h->column_base; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_DEFER: *value = h->defer; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_PACKED_REFRESH: *value = h->packed; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_USED: {
       unsigned int used = 0;

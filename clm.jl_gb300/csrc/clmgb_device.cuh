@@ -933,6 +933,7 @@ __device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_s
 // ===========================================================================
 template <class S>
 struct MfLaneT {
+  static constexpr bool kRefreshInline = true;   // mf_attempt runs mf_refresh itself
   int64_t c;
   int nlayers;
   int nsub;
@@ -1101,15 +1102,15 @@ __device__ __forceinline__ void mf_refresh(MfLaneT<typename ST::S>& L, const Dim
   L.fresh = false;
 }
 
-// one attempt; returns true when the column's substep loop has finished
-template <class ST>
-__device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dims& D,
-                                           const clmgb_soilwater_fields& f, const clmgb_swm_config& cfg,
-                                           double dtime, ST& X) {
+// one attempt; returns true when the column's substep loop has finished.  LT is
+// MfLaneT or a lane whose refresh is run elsewhere (LT::kRefreshInline false: the
+// caller has refreshed it before the attempt).
+template <class LT, class ST>
+__device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soilwater_fields& f,
+                                           const clmgb_swm_config& cfg, double dtime, ST& X) {
   typedef typename ST::S S;
   const int64_t ld = D.ldc;
   const int64_t c = L.c;
-  const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
   const int nlayers = L.nlayers;
   const int lower_bc = cfg.lower_boundary_condition;
   L.nsub += 1;
@@ -1138,7 +1139,9 @@ __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dim
     }
     L.dt_cur = dtsub;
   }
-  if (L.fresh) mf_refresh(L, D, f, cfg, X);
+  if constexpr (LT::kRefreshInline) {
+    if (L.fresh) mf_refresh(L, D, f, cfg, X);
+  }
   // ---- RHS / LHS (:1380-1397) fused into the Thomas forward sweep (:1421-1438) ----
   S bet, dwat_prev;
   {
@@ -1212,9 +1215,8 @@ __device__ __forceinline__ bool mf_attempt(MfLaneT<typename ST::S>& L, const Dim
   return false;
 }
 
-template <class ST>
-__device__ __forceinline__ uint32_t mf_end(MfLaneT<typename ST::S>& L, const Dims& D,
-                                           const clmgb_soilwater_fields& f, ST& X) {
+template <class LT, class ST>
+__device__ __forceinline__ uint32_t mf_end(LT& L, const Dims& D, const clmgb_soilwater_fields& f, ST& X) {
   const int64_t c = L.c;
   const int joff = D.nlevsno;
   uint32_t status = L.status;

@@ -265,6 +265,314 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
   }
 }
 
+// ---------------------------------------------------------------------------
+// The work-queue kernel with a packed hydraulic refresh.  A refresh (the hydraulic
+// properties, fluxes and flux derivatives of an accepted substep's water, mf_refresh)
+// costs about three attempts and runs for the lanes whose substep was just accepted;
+// run lane by lane it leaves the warp's other lanes idle.  Here the warp runs the
+// refresh of all its fresh lanes' columns together: the (column, level) pairs are
+// spread over the 32 lanes, in four passes over the levels (saturation, hydraulic
+// properties, fluxes, net flux), each reading what the pass before wrote.  The
+// arrays other lanes read or write live in the warp's shared memory, laid out
+// [array][level][lane]; within a pass every lane reads its inputs, the warp syncs,
+// then the lanes write, so no level is overwritten before its neighbour has read it.
+// Every value is formed by mf_refresh's expression and the attempts are mf_attempt,
+// so the results are the per-lane kernel's bits.
+
+// level j (1-based) of one lane's array in the warp's shared memory
+struct LevelView {
+  double* p;
+  __device__ __forceinline__ double& operator[](int j) const { return p[(j - 1) * 32]; }
+};
+
+struct MfLaneP {
+  static constexpr bool kRefreshInline = false;   // refreshed by mfp_refresh
+  int64_t c;
+  int nlayers;
+  int nsub;
+  bool fresh;
+  uint32_t status;
+  double dtsub, dtdone, dt_cur;
+  double qc, qin1, hk_bot, dhkdw_bot;
+  double dzv[MAXSOI + 1], dt_dz[MAXSOI + 1];
+  double gam[MAXSOI + 1], dwat[MAXSOI + 1];
+  LevelView liq, qout, dqodw1, dqodw2, fnet1;
+};
+
+// shared-memory doubles per warp: 5 level arrays and the bottom conductivity pair
+__host__ __device__ constexpr int64_t packed_warp_doubles(int nlevsoi) { return (5LL * nlevsoi + 2) * 32; }
+
+// mf_begin for the packed lane (the impedances stay in the cache the refresh reads)
+__device__ __forceinline__ bool mfp_begin(MfLaneP& L, const Dims& D, const clmgb_soilwater_fields& f,
+                                          const clmgb_swm_config& cfg, double dtime, int64_t c,
+                                          const double* dt_init) {
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno;
+  L.c = c;
+  L.status = 0;
+  const int64_t nl = f.col_nbedrock[c];
+  if (nl < 1 || nl > D.nlevsoi) {
+    L.status = CLMGB_COL_LEVEL_RANGE;
+    return false;
+  }
+  const int nlayers = (int)nl;
+  L.nlayers = nlayers;
+  for (int j = 1; j <= nlayers; j++) {
+    L.liq[j] = LV(f.h2osoi_liq, c, joff + j, ld);
+    L.dzv[j] = LVc(f.dz, c, joff + j, ld);
+  }
+  L.nsub = 0;
+  L.dtsub = dtime;
+  if (dt_init) {
+    const double d = dt_init[c];
+    if (d == d) L.dtsub = jl_min(jl_max(d, cfg.dtmin), dtime);   // NaN keeps dtime
+  }
+  L.dtdone = 0.0;
+  L.qc = 0.0;
+  L.fresh = true;
+  L.dt_cur = -1.0;
+  return true;
+}
+
+// The refresh of the lanes in `mask`, called by all 32 lanes of the warp.  wsm: the
+// warp's shared block; nls: D.nlevsoi; imp: impedance cache [nlevsoi][ldi].
+__device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dims& D,
+                                            const clmgb_soilwater_fields& f, const clmgb_swm_config& cfg,
+                                            const double* imp, int64_t ldi, double* wsm, int nls) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
+  const int lower_bc = cfg.lower_boundary_condition;
+  const bool mine = (mask >> lane) & 1u;
+  // (column, level) items: lane k's levels are items off_k .. off_k + nl_k - 1
+  const int nl_own = mine ? L.nlayers : 0;
+  int incl = nl_own;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int off_own = incl - nl_own;
+  const int T = __shfl_sync(FULL, incl, 31);
+  const int64_t c_own = mine ? L.c : 0;
+  double* const sb = wsm + 5LL * nls * 32;                       // hk, dhkdw of the bottom level
+  auto A = [&](int a, int k, int j) -> double& { return wsm[((int64_t)a * nls + (j - 1)) * 32 + k]; };
+  enum { LIQ = 0, QOUT = 1, D1 = 2, D2 = 3, FN = 4 };
+  struct Item { int k, j, nl; int64_t c; bool ok; };
+  auto item = [&](int base) -> Item {
+    const int t = base + lane;
+    int k = 0;                                     // the last lane whose first item is <= t
+    for (int step = 16; step > 0; step >>= 1) {
+      const int oc = __shfl_sync(FULL, off_own, k + step);
+      if (oc <= t) k += step;
+    }
+    Item it;
+    it.k = k;
+    it.c = __shfl_sync(FULL, c_own, k);
+    it.nl = __shfl_sync(FULL, nl_own, k);
+    it.j = t - __shfl_sync(FULL, off_own, k) + 1;
+    it.ok = t < T;
+    return it;
+  };
+  // pass 1: saturation of every level (:1283-1287), kept in FN
+  for (int base = 0; base < T; base += 32) {
+    const Item it = item(base);
+    if (it.ok) {
+      const double vwc = jl_max(A(LIQ, it.k, it.j), 1.0e-6) / (LVc(f.dz, it.c, joff + it.j, ld) * DENH2O);
+      double s = vwc / LVc(f.watsat, it.c, it.j, ld);
+      s = jl_min(s, 1.0);
+      A(FN, it.k, it.j) = jl_max(0.01, s);
+    }
+  }
+  __syncwarp();
+  // pass 2: hydraulic properties (:1288-1308): hk, dhkdw, smp, dsmpdw into QOUT, D1, D2, FN
+  for (int base = 0; base < T; base += 32) {
+    const Item it = item(base);
+    double hkv = 0.0, dhkds = 0.0, smpv = 0.0, dsmpdw = 0.0;
+    if (it.ok) {
+      const int j = it.j;
+      const int64_t c = it.c;
+      const double sj = A(FN, it.k, j);
+      const double sn = (j < it.nl) ? A(FN, it.k, j + 1) : sj;
+      double s1 = (j == it.nl) ? sj : 0.5 * (sj + sn);
+      s1 = jl_min(s1, 1.0);
+      s1 = jl_max(0.01, s1);
+      const double b = LVc(f.bsw, c, j, ld);
+      hkv = imp[(int64_t)(j - 1) * ldi + c] * LVc(f.hksat, c, j, ld) * cm_pow(s1, 2.0 * b + 3.0);
+      dhkds = (2.0 * b + 3.0) * hkv / s1;
+      smpv = -LVc(f.sucsat, c, j, ld) * cm_pow(sj, -b);
+      const double dsmpds = -b * smpv / sj;
+      dsmpdw = dsmpds / LVc(f.watsat, c, j, ld);
+      LV(f.smp_l, c, j, ld) = smpv;
+      LV(f.hk_l, c, j, ld) = hkv;
+    }
+    __syncwarp();
+    if (it.ok) {
+      A(QOUT, it.k, it.j) = hkv;
+      A(D1, it.k, it.j) = dhkds;
+      A(D2, it.k, it.j) = smpv;
+      A(FN, it.k, it.j) = dsmpdw;
+    }
+    __syncwarp();
+  }
+  // pass 3: fluxes and derivatives between levels (:1310-1345) and at the bottom
+  // (:1347-1370), over the properties into QOUT, D1, D2
+  for (int base = 0; base < T; base += 32) {
+    const Item it = item(base);
+    double qo = 0.0, d1 = 0.0, d2 = 0.0;
+    if (it.ok) {
+      const int j = it.j;
+      const int64_t c = it.c;
+      const double hk = A(QOUT, it.k, j), dhkdw = A(D1, it.k, j), smp = A(D2, it.k, j), dsmpdw = A(FN, it.k, j);
+      if (j < it.nl) {
+        const double dhkds1 = 0.5 * dhkdw / LVc(f.watsat, c, j, ld);
+        const double dhkds2 = 0.5 * dhkdw / LVc(f.watsat, c, j + 1, ld);
+        const double num = A(D2, it.k, j + 1) - smp;
+        const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
+        qo = -hk * num / den + hk;
+        d1 = (hk * dsmpdw - dhkds1 * num) / den + dhkds1;
+        d2 = (-hk * A(FN, it.k, j + 1) - dhkds2 * num) / den + dhkds2;
+      } else {
+        sb[it.k] = hk;
+        sb[32 + it.k] = dhkdw;
+        if (lower_bc == CLMGB_BC_WATERTABLE) {
+          int jwt = nlevsoi;
+          for (int jj = 1; jj <= nlevsoi; jj++) {
+            if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
+          }
+          if (j <= jwt) {
+            const double dhkds1l = dhkdw / LVc(f.watsat, c, j, ld);
+            const double num = -smp;
+            const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
+            qo = -hk * num / den + hk;
+            d1 = (hk * dsmpdw - dhkds1l * num) / den + dhkds1l;
+          }
+        } else if (lower_bc == CLMGB_BC_FLUX) {
+          qo = hk;
+          d1 = dhkdw / LVc(f.watsat, c, j, ld);
+        }
+      }
+    }
+    __syncwarp();
+    if (it.ok) {
+      A(QOUT, it.k, it.j) = qo;
+      A(D1, it.k, it.j) = d1;
+      A(D2, it.k, it.j) = d2;
+    }
+    __syncwarp();
+  }
+  // pass 4: net flux of every level (:1372-1378); the inflow of level j > 1 is the
+  // outflow of level j-1
+  for (int base = 0; base < T; base += 32) {
+    const Item it = item(base);
+    if (it.ok) {
+      const double qin = (it.j == 1) ? f.qflx_infl[it.c] : A(QOUT, it.k, it.j - 1);
+      A(FN, it.k, it.j) = qin - A(QOUT, it.k, it.j) - LVc(f.qflx_rootsoi, it.c, it.j, ld);
+    }
+  }
+  __syncwarp();
+  if (mine) {
+    L.qin1 = f.qflx_infl[L.c];
+    L.hk_bot = sb[lane];
+    L.dhkdw_bot = sb[32 + lane];
+    L.fresh = false;
+  }
+  __syncwarp();
+}
+
+// k_moisture_form_queue (LOG false) with the packed refresh; needs the impedance
+// cache.  Dynamic shared memory: packed_warp_doubles(nlevsoi) doubles per warp.
+__global__ void __launch_bounds__(BLOCK)
+k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
+                       uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
+                       const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
+                       int64_t ld_imp, const double* dt_init, int fresh_batch, QueueScratch qs) {
+  extern __shared__ double smem_packed[];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int nls = D.nlevsoi;
+  double* const wsm = smem_packed + (int64_t)(threadIdx.x >> 5) * packed_warp_doubles(nls);
+  const unsigned long long nq = order ? (unsigned long long)(*(volatile const unsigned int*)nlisted_ptr)
+                                      : (unsigned long long)nc;
+  const int batch = fresh_batch > 0 ? fresh_batch : 1;
+  MfLaneP L;
+  L.liq.p = wsm + (0LL * nls) * 32 + lane;
+  L.qout.p = wsm + (1LL * nls) * 32 + lane;
+  L.dqodw1.p = wsm + (2LL * nls) * 32 + lane;
+  L.dqodw2.p = wsm + (3LL * nls) * 32 + lane;
+  L.fnet1.p = wsm + (4LL * nls) * 32 + lane;
+  bool active = false, exhausted = false;
+  for (;;) {
+    const bool need = !active && !exhausted;
+    const unsigned m = __ballot_sync(FULL, need);
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        const unsigned long long k = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+        if (k >= nq) {
+          exhausted = true;
+        } else {
+          const int64_t c = order ? (int64_t)order[k] : (int64_t)k;
+          if (order || f.mask_hydrology[c]) {
+            if (mfp_begin(L, D, f, cfg, dtime, c, dt_init)) {
+              active = true;
+            } else {
+              const uint32_t st = L.status;
+              if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
+              if (st && dev_status) atomicOr(dev_status, st);
+            }
+          } else if (col_status && !or_status) {
+            col_status[c] = 0;
+          }
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) {
+      if (__all_sync(FULL, exhausted)) {
+        if (qs.defer > 0) coop_drain(D, f, cfg, dtime, col_status, or_status, dev_status, qs);
+        break;
+      }
+      continue;
+    }
+    // lanes whose substep was accepted wait for the packed refresh until `batch` of
+    // them need it or no lane can attempt
+    const bool want = active && L.fresh && L.nsub < MF_ATTEMPT_CAP;
+    const unsigned wm = __ballot_sync(FULL, want);
+    const unsigned tm = __ballot_sync(FULL, active && !want);
+    if (wm && (__popc(wm) >= batch || tm == 0)) mfp_refresh(L, wm, D, f, cfg, imp_cache, ld_imp, wsm, nls);
+    const bool can_try = active && !(L.fresh && L.nsub < MF_ATTEMPT_CAP);
+    if (!can_try) continue;
+    FieldState<clmgb_soilwater_fields> X(f, L.c, D.ldc);
+    const bool fin = mf_attempt(L, D, f, cfg, dtime, X);
+    if (!fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer) {
+      // hand the column over: claim a list slot, store the state, then publish
+      const int64_t c = L.c, cap = qs.capacity;
+      const unsigned long long slot = atomicAdd(qs.d_count, 1ULL);
+      for (int j = 1; j <= L.nlayers; j++) qs.d_liq[(int64_t)(j - 1) * cap + c] = L.liq[j];
+      qs.d_dtsub[c] = L.dtsub;
+      qs.d_dtdone[c] = L.dtdone;
+      qs.d_qc[c] = L.qc;
+      qs.d_nsub[c] = L.nsub;
+      qs.d_status[c] = L.status;
+      __threadfence();
+      *(volatile uint32_t*)(qs.d_list + slot) = (uint32_t)c;
+      __threadfence();
+      atomicAdd(qs.d_count + 1, 1ULL);
+      active = false;
+      continue;
+    }
+    if (fin) {
+      const uint32_t st = mf_end(L, D, f, X);
+      if (col_status) col_status[L.c] = or_status ? (col_status[L.c] | st) : st;
+      if (st && dev_status) atomicOr(dev_status, st);
+      active = false;
+    }
+  }
+}
+
 // Ice impedances of every hydrology column, one thread per column, into imp_cache
 // [nlevsoi, ld_imp] (uniform work: no lane waits on another column).
 __global__ void __launch_bounds__(BLOCK)
@@ -509,7 +817,24 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
     k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                       dev_status, queue, ord, nl, imp, ldi, dt_init,
                                                                       *log, qs.fresh_batch, q);
-  else
+  else if (use && qs.packed) {
+    const size_t smem = (size_t)(BLOCK / 32) * (size_t)packed_warp_doubles(D.nlevsoi) * sizeof(double);
+    if ((e = cudaFuncSetAttribute(k_moisture_form_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+      return e;
+    // the blocks that fit on the GPU at once (the kernel's warps wait on one another
+    // only through the bounded waits of the deferred-column list)
+    int dev = 0, nsm = 0, nb = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_moisture_form_packed, BLOCK, smem)) != cudaSuccess)
+      return e;
+    if (nb < 1) return cudaErrorInvalidConfiguration;
+    int gp = grid > 0 ? grid : 1;
+    if (gp > nb * nsm) gp = nb * nsm;
+    k_moisture_form_packed<<<gp, BLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue,
+                                                   ord, nl, imp, ldi, dt_init, qs.fresh_batch, q);
+  } else
     k_moisture_form_queue<false><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                        dev_status, queue, ord, nl, imp, ldi, dt_init,
                                                                        SubstepLogView{nullptr, nullptr, 0, 0},

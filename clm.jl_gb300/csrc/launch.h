@@ -19,6 +19,9 @@ struct QueueScratch {
   unsigned int* bins;
   int longest_first;
   int fresh_batch;   // CLMGB_OPT_QUEUE_FRESH_BATCH (0: refresh at once)
+  // CLMGB_OPT_QUEUE_PACKED_REFRESH: the warp refreshes its fresh lanes' columns
+  // together, (column, level) pairs spread over the 32 lanes (k_moisture_form_packed)
+  int packed;
   // CLMGB_OPT_QUEUE_DEFER: a column still unfinished after `defer` attempts leaves the
   // work queue at its next accepted substep; its state (water [nlevsoi][capacity],
   // dtsub, dtdone, qcharge so far, attempts, status at index c) and its index (list)

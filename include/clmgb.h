@@ -681,12 +681,16 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
 #define   CLMGB_ADJ_ST_RECORDED          1 /*   replayed through the recording scalar and swept */
 #define CLMGB_OPT_QUEUE_FRESH_BATCH   14 /* work-queue Richards kernel: lanes whose substep was accepted wait
                                             for the hydraulic block until this many lanes of the warp need it
-                                            (or no lane can attempt), then run it together; 0 = at once.
-                                            Results do not depend on it. */
+                                            (or no lane can attempt), then run it together (default 4); 0 = at
+                                            once.  Results do not depend on it. */
 #define CLMGB_OPT_QUEUE_DEFER         16 /* work-queue Richards kernel with reserved scratch: a column not done
                                             after this many attempts leaves the queue at its next accepted
                                             substep and is finished by one warp (one level per lane); 0 = off.
                                             Results do not depend on it. */
+#define CLMGB_OPT_QUEUE_PACKED_REFRESH 17 /* work-queue Richards kernel with reserved scratch: 1 (default) = the
+                                            warp runs the hydraulic refresh of its waiting lanes' columns
+                                            together, column levels spread over the 32 lanes; 0 = each lane
+                                            runs its own.  Results do not depend on it. */
 #define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls
                                             receive (default 0).  A caller that runs a column range [c0, c1)
                                             passes column arrays advanced by c0 (same ldc) and the patch
