@@ -510,6 +510,8 @@ def run_ours(args):
     achieved = bytes_launch / (kern_ms / 1000.0) / 1e9
     kname = {abi.SCHEDULE_FUSED: "k_moisture_form", abi.SCHEDULE_QUEUE: "k_moisture_form_queue",
              abi.SCHEDULE_WAVES: "k_moisture_form_waves"}[h.get_option(abi.OPT_STEP_SCHEDULE)]
+    if kname == "k_moisture_form_queue" and h.get_option(abi.OPT_QUEUE_PACKED_REFRESH) and not args.no_reserve:
+        kname = "k_moisture_form_packed"
     tr = profile_traffic()
     traffic = None
     if tr and tr.get(kname + "_bytes_per_column"):
