@@ -62,7 +62,8 @@ def parse():
                     help="run only the adjoint calibration leg and print its JSON (profiling)")
     ap.add_argument("--adj-nc", type=int, default=65536)
     ap.add_argument("--adj-steps", type=int, default=48)
-    ap.add_argument("--adj-k", type=int, default=8, help="checkpoint every k steps")
+    ap.add_argument("--adj-k", type=int, default=2,
+                    help="checkpoint every k steps (2: 24 checkpoints of 0.45 GB at 65,536 columns)")
     ap.add_argument("--adj-slots", type=int, default=65536)
     ap.add_argument("--adj-entries", type=int, default=256,
                     help="tape entries per slot (the recording kernel only; the default adjoint needs none)")

@@ -71,10 +71,15 @@ def _cptr(t):
     return ctypes.cast(ctypes.c_void_p(t.data_ptr()), abi.c_double_p)
 
 
-def copy_state_(dst, src):
-    """dst <- src for every field (device to device)."""
+def copy_state_(dst, src, full=False):
+    """dst <- src (device to device).  Unless `full`, the geometry, parameter and
+    topology fields (hoststep.STATIC) are left as they are: neither the forcing nor the
+    column step writes them, so two states of one trajectory hold the same values
+    there (the states the reverse passes copy between all descend from one state)."""
+    from .hoststep import STATIC
     for k, v in src.arrays.items():
-        dst.arrays[k].copy_(v)
+        if full or k not in STATIC:
+            dst.arrays[k].copy_(v)
 
 
 class Trajectory:

@@ -809,7 +809,10 @@ __device__ __forceinline__ double& cf_sub(const CfSub& S, int64_t slot, int sidx
   return S.sub[((slot >> 5) * ((int64_t)S.maxsub * SUB_REC) + (int64_t)sidx * SUB_REC + j) * 32 + (slot & 31)];
 }
 
-__global__ void __launch_bounds__(CF_BLOCK)
+// 8 blocks of 64 per SM (128 registers): 1,216 resident blocks, so each thread of a
+// 65,536-column launch takes one column and no second round of columns trails the
+// first (6 blocks at the 168 registers the compiler chose otherwise)
+__global__ void __launch_bounds__(CF_BLOCK, 8)
 k_column_step_vjp_cf(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw, clmgb_swm_config cfg,
                      double dtime, int snow_method, double* t_ssbef, double* t_h2osfc_bef, clmgb_step_adjoint adj,
                      CfSub S, SubstepLogView lg, unsigned long long* queue, const uint32_t* order,

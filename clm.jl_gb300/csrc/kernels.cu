@@ -480,13 +480,16 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
   __syncwarp();
 }
 
-// k_moisture_form_queue (LOG false) with the packed refresh; needs the impedance
-// cache.  Dynamic shared memory: packed_warp_doubles(nlevsoi) doubles per warp.
+// k_moisture_form_queue with the packed refresh; needs the impedance cache.  With
+// LOG it writes the same substep log (the starting water of each accepted substep,
+// its dtsub and the time done before it, then the solve's outputs).  Dynamic shared
+// memory: packed_warp_doubles(nlevsoi) doubles per warp.
+template <bool LOG>
 __global__ void __launch_bounds__(BLOCK)
 k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                        uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
                        const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
-                       int64_t ld_imp, const double* dt_init, int fresh_batch, QueueScratch qs) {
+                       int64_t ld_imp, const double* dt_init, SubstepLogView lg, int fresh_batch, QueueScratch qs) {
   extern __shared__ double smem_packed[];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -501,6 +504,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
   L.dqodw1.p = wsm + (2LL * nls) * 32 + lane;
   L.dqodw2.p = wsm + (3LL * nls) * 32 + lane;
   L.fnet1.p = wsm + (4LL * nls) * 32 + lane;
+  int nacc = 0;
   bool active = false, exhausted = false;
   for (;;) {
     const bool need = !active && !exhausted;
@@ -519,6 +523,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
           if (order || f.mask_hydrology[c]) {
             if (mfp_begin(L, D, f, cfg, dtime, c, dt_init)) {
               active = true;
+              nacc = 0;
             } else {
               const uint32_t st = L.status;
               if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
@@ -532,7 +537,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
     }
     if (!__any_sync(FULL, active)) {
       if (__all_sync(FULL, exhausted)) {
-        if (qs.defer > 0) coop_drain(D, f, cfg, dtime, col_status, or_status, dev_status, qs);
+        if (!LOG && qs.defer > 0) coop_drain(D, f, cfg, dtime, col_status, or_status, dev_status, qs);
         break;
       }
       continue;
@@ -542,12 +547,34 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
     const bool want = active && L.fresh && L.nsub < MF_ATTEMPT_CAP;
     const unsigned wm = __ballot_sync(FULL, want);
     const unsigned tm = __ballot_sync(FULL, active && !want);
-    if (wm && (__popc(wm) >= batch || tm == 0)) mfp_refresh(L, wm, D, f, cfg, imp_cache, ld_imp, wsm, nls);
+    if (wm && (__popc(wm) >= batch || tm == 0)) {
+      if (LOG && want && nacc < lg.cap) {
+        double* r0 = lg.rec + L.c * lg.stride + (int64_t)nacc * SUB_REC;
+        for (int j = 1; j <= L.nlayers; j++) r0[j - 1] = L.liq[j];
+      }
+      mfp_refresh(L, wm, D, f, cfg, imp_cache, ld_imp, wsm, nls);
+    }
     const bool can_try = active && !(L.fresh && L.nsub < MF_ATTEMPT_CAP);
     if (!can_try) continue;
+    double* rec = nullptr;
+    double dts = 0.0, dtd = 0.0;
+    if (LOG) {
+      rec = lg.rec + L.c * lg.stride;
+      if (L.fresh && nacc < lg.cap)
+        for (int j = 1; j <= L.nlayers; j++) rec[(int64_t)nacc * SUB_REC + j - 1] = L.liq[j];
+      dts = L.dtsub;
+      dtd = L.dtdone;
+    }
     FieldState<clmgb_soilwater_fields> X(f, L.c, D.ldc);
     const bool fin = mf_attempt(L, D, f, cfg, dtime, X);
-    if (!fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer) {
+    if (LOG && L.dtdone != dtd) {
+      if (nacc < lg.cap) {
+        rec[(int64_t)nacc * SUB_REC + MAXSOI] = dts;
+        rec[(int64_t)nacc * SUB_REC + MAXSOI + 1] = dtd;
+      }
+      nacc++;
+    }
+    if (!LOG && !fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer) {
       // hand the column over: claim a list slot, store the state, then publish
       const int64_t c = L.c, cap = qs.capacity;
       const unsigned long long slot = atomicAdd(qs.d_count, 1ULL);
@@ -566,6 +593,18 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
     }
     if (fin) {
       const uint32_t st = mf_end(L, D, f, X);
+      if (LOG) {
+        double* out = rec + (int64_t)lg.cap * SUB_REC;
+        for (int j = 1; j <= L.nlayers; j++) {
+          out[j - 1] = L.liq[j];
+          out[MAXSOI + j - 1] = LV(f.smp_l, L.c, j, D.ldc);
+          out[2 * MAXSOI + j - 1] = LV(f.hk_l, L.c, j, D.ldc);
+        }
+        out[3 * MAXSOI] = L.qc;
+        out[3 * MAXSOI + 1] = (double)L.nsub;
+        out[3 * MAXSOI + 2] = (double)st;
+        lg.count[L.c] = nacc;
+      }
       if (col_status) col_status[L.c] = or_status ? (col_status[L.c] | st) : st;
       if (st && dev_status) atomicOr(dev_status, st);
       active = false;
@@ -813,28 +852,27 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
     if ((e = cudaMemsetAsync(q.d_count, 0, 3 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(q.d_list, 0xff, (size_t)nc * sizeof(uint32_t), s)) != cudaSuccess) return e;
   }
-  if (log)
-    k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
-                                                                      dev_status, queue, ord, nl, imp, ldi, dt_init,
-                                                                      *log, qs.fresh_batch, q);
-  else if (use && qs.packed) {
+  if (use && qs.packed) {
     const size_t smem = (size_t)(BLOCK / 32) * (size_t)packed_warp_doubles(D.nlevsoi) * sizeof(double);
-    if ((e = cudaFuncSetAttribute(k_moisture_form_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-        cudaSuccess)
+    auto kern = log ? k_moisture_form_packed<true> : k_moisture_form_packed<false>;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
       return e;
     // the blocks that fit on the GPU at once (the kernel's warps wait on one another
     // only through the bounded waits of the deferred-column list)
     int dev = 0, nsm = 0, nb = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_moisture_form_packed, BLOCK, smem)) != cudaSuccess)
-      return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, BLOCK, smem)) != cudaSuccess) return e;
     if (nb < 1) return cudaErrorInvalidConfiguration;
     int gp = grid > 0 ? grid : 1;
     if (gp > nb * nsm) gp = nb * nsm;
-    k_moisture_form_packed<<<gp, BLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue,
-                                                   ord, nl, imp, ldi, dt_init, qs.fresh_batch, q);
-  } else
+    kern<<<gp, BLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue, ord, nl, imp, ldi,
+                                 dt_init, log ? *log : SubstepLogView{nullptr, nullptr, 0, 0}, qs.fresh_batch, q);
+  } else if (log)
+    k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
+                                                                      dev_status, queue, ord, nl, imp, ldi, dt_init,
+                                                                      *log, qs.fresh_batch, q);
+  else
     k_moisture_form_queue<false><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                        dev_status, queue, ord, nl, imp, ldi, dt_init,
                                                                        SubstepLogView{nullptr, nullptr, 0, 0},
