@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--e2e-chunks", type=int, default=1,
                     help="column ranges of the end-to-end step (uploads and read-backs overlap the other ranges)")
+    ap.add_argument("--e2e-readback", default="dma", choices=["kernel", "dma"],
+                    help="how the temperature outputs come back during the Richards solve")
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", type=int, default=None, help="CLMGB_OPT_STEP_SCHEDULE override")
@@ -534,7 +536,7 @@ def run_ours(args):
     if args.e2e_steps > 0:
         from clmgb import hoststep
         host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in st.arrays.items()}
-        hs = hoststep.HostStepper(h, host, d, wl.dtime, cfg, chunks=args.e2e_chunks)
+        hs = hoststep.HostStepper(h, host, d, wl.dtime, cfg, chunks=args.e2e_chunks, readback=args.e2e_readback)
 
         def e2e_step(k):
             G, I = Gd[k % nsteps], Id[k % nsteps]
@@ -557,7 +559,7 @@ def run_ours(args):
         e2e_ms = e0.elapsed_time(e1)
         e2e = {"value": args.e2e_steps * nc * world / (e2e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": hs.h2d_bytes, "d2h_bytes_per_step": hs.d2h_bytes,
-               "chunks": len(hs.ranges),
+               "chunks": len(hs.ranges), "readback": args.e2e_readback,
                "note": "host-resident state: per step H2D of the inputs other modules change, D2H of every "
                        "written field, the soil-temperature outputs read back during the Richards solve "
                        "(with --e2e-chunks > 1 the step runs over column ranges); "

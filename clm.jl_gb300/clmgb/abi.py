@@ -66,6 +66,7 @@ OPT_QUEUE_FRESH_BATCH = 14
 OPT_COLUMN_BASE = 15
 OPT_QUEUE_DEFER = 16
 OPT_QUEUE_PACKED_REFRESH = 17
+MAX_COPY_SEGMENTS = 128
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
 COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY, COL_FILTER, COL_QUEUE_WAIT = 32, 64, 128, 256, 512

@@ -68,3 +68,29 @@ def test_chunked_host_stepper_matches_device_steps(chunks):
         assert h.device_status() == 0
     finally:
         h.close()
+
+
+def test_host_stepper_kernel_readback_matches_device_steps():
+    nsteps = 3
+    wl = synth.make_workload(2, nc=2500, seed=13, nsteps=nsteps)
+    cfg = abi.SwmConfig.clm5_default()
+    h = api.Handle(wl.state.vp)
+    try:
+        h.reserve(wl.state.nc)
+        G, I = wl.forcing_block(range(nsteps))
+        Gd, Id = torch.from_numpy(G).cuda(), torch.from_numpy(I).cuda()
+        d = wl.state.to_device()
+        for t in range(nsteps):
+            api.synth_forcing(h, d, Gd[t], Id[t])
+            api.soil_temperature(h, d, wl.dtime)
+            api.set_soil_water_fractions(h, d)
+            api.soil_water(h, d, wl.dtime, cfg)
+        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in wl.state.arrays.items()}
+        hs = hoststep.HostStepper(h, host, wl.state.to_device(), wl.dtime, cfg, readback="kernel")
+        for t in range(nsteps):
+            hs.step(forcing=lambda dv, t=t: api.synth_forcing(h, dv, Gd[t], Id[t]))
+        torch.cuda.synchronize()
+        for k in set(hoststep.WRITTEN_TEMPERATURE) | set(hoststep.WRITTEN_WATER):
+            assert torch.equal(host[k], d[k].cpu()), k
+    finally:
+        h.close()
