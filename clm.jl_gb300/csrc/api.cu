@@ -218,6 +218,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->qs.imp = nullptr;
   h->qs.order = nullptr;
   h->qs.bins = nullptr;
+  h->qs.pcache = nullptr;
   h->qs.longest_first = 1;
   h->fresh_batch = CLMGB_DEFAULT_FRESH_BATCH;
   memset(&h->ws, 0, sizeof(h->ws));
@@ -716,8 +717,9 @@ int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t lev = al(nsoi * n * sizeof(double));   // one [nlevsoi][n] array
   const size_t col8 = al(n * 8), col4 = al(n * 4);
-  // imp + 5 wave level arrays, 6 per-column doubles, nsub + status, order + 4 lists, bins
-  const size_t total = 6 * lev + 6 * col8 + 2 * col4 + 5 * col4 + al(256 * sizeof(unsigned int));
+  // imp + 5 wave level arrays, the refresh input records (PC_FIELDS level arrays),
+  // 6 per-column doubles, nsub + status, order + 4 lists, bins
+  const size_t total = (6 + clmgb::PC_FIELDS) * lev + 6 * col8 + 2 * col4 + 5 * col4 + al(256 * sizeof(unsigned int));
   void* blk = nullptr;
   cudaError_t ce = cudaDeviceSynchronize();
   if (ce == cudaSuccess) ce = cudaMalloc(&blk, total);
@@ -750,6 +752,7 @@ int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc) {
   h->qs.bins = reinterpret_cast<unsigned int*>(take(al(256 * sizeof(unsigned int))));
   w.counters = h->qs.bins + 192;   // bins use words 0..128
   h->qs.imp = w.imp;
+  h->qs.pcache = reinterpret_cast<double*>(take(clmgb::PC_FIELDS * lev));
   h->qs.capacity = max_nc;
   return CLMGB_OK;
 }

@@ -335,10 +335,11 @@ __device__ __forceinline__ bool mfp_begin(MfLaneP& L, const Dims& D, const clmgb
 }
 
 // The refresh of the lanes in `mask`, called by all 32 lanes of the warp.  wsm: the
-// warp's shared block; nls: D.nlevsoi; imp: impedance cache [nlevsoi][ldi].
+// warp's shared block; nls: D.nlevsoi; pcache: the columns' input records
+// ([column][PC_FIELDS][nls], k_impedance).
 __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dims& D,
                                             const clmgb_soilwater_fields& f, const clmgb_swm_config& cfg,
-                                            const double* imp, int64_t ldi, double* wsm, int nls) {
+                                            const double* pcache, double* wsm, int nls) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t ld = D.ldc;
@@ -357,6 +358,10 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
   const int64_t c_own = mine ? L.c : 0;
   double* const sb = wsm + 5LL * nls * 32;                       // hk, dhkdw of the bottom level
   auto A = [&](int a, int k, int j) -> double& { return wsm[((int64_t)a * nls + (j - 1)) * 32 + k]; };
+  // input `fld` of level j of column c
+  auto P = [&](int64_t c, int fld, int j) -> double {
+    return pcache[c * (int64_t)(PC_FIELDS * nls) + (int64_t)fld * nls + (j - 1)];
+  };
   enum { LIQ = 0, QOUT = 1, D1 = 2, D2 = 3, FN = 4 };
   struct Item { int k, j, nl; int64_t c; bool ok; };
   auto item = [&](int base) -> Item {
@@ -378,8 +383,8 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
   for (int base = 0; base < T; base += 32) {
     const Item it = item(base);
     if (it.ok) {
-      const double vwc = jl_max(A(LIQ, it.k, it.j), 1.0e-6) / (LVc(f.dz, it.c, joff + it.j, ld) * DENH2O);
-      double s = vwc / LVc(f.watsat, it.c, it.j, ld);
+      const double vwc = jl_max(A(LIQ, it.k, it.j), 1.0e-6) / P(it.c, PC_DZW, it.j);
+      double s = vwc / P(it.c, PC_WS, it.j);
       s = jl_min(s, 1.0);
       A(FN, it.k, it.j) = jl_max(0.01, s);
     }
@@ -397,12 +402,12 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
       double s1 = (j == it.nl) ? sj : 0.5 * (sj + sn);
       s1 = jl_min(s1, 1.0);
       s1 = jl_max(0.01, s1);
-      const double b = LVc(f.bsw, c, j, ld);
-      hkv = imp[(int64_t)(j - 1) * ldi + c] * LVc(f.hksat, c, j, ld) * cm_pow(s1, 2.0 * b + 3.0);
+      const double b = P(c, PC_BSW, j);
+      hkv = P(c, PC_IMP, j) * P(c, PC_KS, j) * cm_pow(s1, 2.0 * b + 3.0);
       dhkds = (2.0 * b + 3.0) * hkv / s1;
-      smpv = -LVc(f.sucsat, c, j, ld) * cm_pow(sj, -b);
+      smpv = -P(c, PC_SUC, j) * cm_pow(sj, -b);
       const double dsmpds = -b * smpv / sj;
-      dsmpdw = dsmpds / LVc(f.watsat, c, j, ld);
+      dsmpdw = dsmpds / P(c, PC_WS, j);
       LV(f.smp_l, c, j, ld) = smpv;
       LV(f.hk_l, c, j, ld) = hkv;
     }
@@ -425,10 +430,10 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
       const int64_t c = it.c;
       const double hk = A(QOUT, it.k, j), dhkdw = A(D1, it.k, j), smp = A(D2, it.k, j), dsmpdw = A(FN, it.k, j);
       if (j < it.nl) {
-        const double dhkds1 = 0.5 * dhkdw / LVc(f.watsat, c, j, ld);
-        const double dhkds2 = 0.5 * dhkdw / LVc(f.watsat, c, j + 1, ld);
+        const double dhkds1 = 0.5 * dhkdw / P(c, PC_WS, j);
+        const double dhkds2 = 0.5 * dhkdw / P(c, PC_WS, j + 1);
         const double num = A(D2, it.k, j + 1) - smp;
-        const double den = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
+        const double den = P(c, PC_DEN, j);
         qo = -hk * num / den + hk;
         d1 = (hk * dsmpdw - dhkds1 * num) / den + dhkds1;
         d2 = (-hk * A(FN, it.k, j + 1) - dhkds2 * num) / den + dhkds2;
@@ -441,7 +446,7 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
             if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
           }
           if (j <= jwt) {
-            const double dhkds1l = dhkdw / LVc(f.watsat, c, j, ld);
+            const double dhkds1l = dhkdw / P(c, PC_WS, j);
             const double num = -smp;
             const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
             qo = -hk * num / den + hk;
@@ -449,7 +454,7 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
           }
         } else if (lower_bc == CLMGB_BC_FLUX) {
           qo = hk;
-          d1 = dhkdw / LVc(f.watsat, c, j, ld);
+          d1 = dhkdw / P(c, PC_WS, j);
         }
       }
     }
@@ -467,7 +472,7 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
     const Item it = item(base);
     if (it.ok) {
       const double qin = (it.j == 1) ? f.qflx_infl[it.c] : A(QOUT, it.k, it.j - 1);
-      A(FN, it.k, it.j) = qin - A(QOUT, it.k, it.j) - LVc(f.qflx_rootsoi, it.c, it.j, ld);
+      A(FN, it.k, it.j) = qin - A(QOUT, it.k, it.j) - P(it.c, PC_ROOT, it.j);
     }
   }
   __syncwarp();
@@ -552,7 +557,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
         double* r0 = lg.rec + L.c * lg.stride + (int64_t)nacc * SUB_REC;
         for (int j = 1; j <= L.nlayers; j++) r0[j - 1] = L.liq[j];
       }
-      mfp_refresh(L, wm, D, f, cfg, imp_cache, ld_imp, wsm, nls);
+      mfp_refresh(L, wm, D, f, cfg, qs.pcache, wsm, nls);
     }
     const bool can_try = active && !(L.fresh && L.nsub < MF_ATTEMPT_CAP);
     if (!can_try) continue;
@@ -614,14 +619,34 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
 
 // Ice impedances of every hydrology column, one thread per column, into imp_cache
 // [nlevsoi, ld_imp] (uniform work: no lane waits on another column).
+// With pcache given, also each column's record of the packed refresh's inputs
+// (QueueScratch::pcache), the same values the refresh would read or form.
 __global__ void __launch_bounds__(BLOCK)
-k_impedance(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* imp_cache, int64_t ld_imp) {
+k_impedance(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* imp_cache, int64_t ld_imp,
+            double* pcache) {
   const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
   if (c >= nc || !f.mask_hydrology[c]) return;
   const int64_t nl = f.col_nbedrock[c];
   if (nl < 1 || nl > D.nlevsoi) return;
   const int nlayers = (int)nl;
-  for (int j = 1; j <= nlayers; j++) imp_cache[(int64_t)(j - 1) * ld_imp + c] = mf_impedance(D, f, e_ice, c, j, nlayers);
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno, nls = D.nlevsoi;
+  double* pc = pcache ? pcache + c * (int64_t)(PC_FIELDS * nls) : nullptr;
+  for (int j = 1; j <= nlayers; j++) {
+    const double imp = mf_impedance(D, f, e_ice, c, j, nlayers);
+    imp_cache[(int64_t)(j - 1) * ld_imp + c] = imp;
+    if (pc) {
+      double* q = pc + (j - 1);
+      q[PC_DZW * nls] = LVc(f.dz, c, joff + j, ld) * DENH2O;
+      q[PC_WS * nls] = LVc(f.watsat, c, j, ld);
+      q[PC_BSW * nls] = LVc(f.bsw, c, j, ld);
+      q[PC_KS * nls] = LVc(f.hksat, c, j, ld);
+      q[PC_SUC * nls] = LVc(f.sucsat, c, j, ld);
+      q[PC_IMP * nls] = imp;
+      if (j < nlayers) q[PC_DEN * nls] = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
+      q[PC_ROOT * nls] = LVc(f.qflx_rootsoi, c, j, ld);
+    }
+  }
 }
 
 // Longest-expected-first order of the hydrology columns: counting sort on the
@@ -828,7 +853,8 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   if (log && (e = cudaMemsetAsync(log->count, 0xff, (size_t)nc * sizeof(int32_t), s)) != cudaSuccess) return e;
   const bool use = qs.capacity >= nc && qs.order && qs.bins && qs.imp;
   if (use) {
-    k_impedance<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg.e_ice, qs.imp, qs.capacity);
+    k_impedance<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg.e_ice, qs.imp, qs.capacity,
+                                               qs.packed ? qs.pcache : nullptr);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (qs.longest_first) {
       if ((e = cudaMemsetAsync(qs.bins, 0, (2 * ORDER_BINS + 1) * sizeof(unsigned int), s)) != cudaSuccess) return e;
@@ -852,7 +878,7 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
     if ((e = cudaMemsetAsync(q.d_count, 0, 3 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(q.d_list, 0xff, (size_t)nc * sizeof(uint32_t), s)) != cudaSuccess) return e;
   }
-  if (use && qs.packed) {
+  if (use && qs.packed && qs.pcache) {
     const size_t smem = (size_t)(BLOCK / 32) * (size_t)packed_warp_doubles(D.nlevsoi) * sizeof(double);
     auto kern = log ? k_moisture_form_packed<true> : k_moisture_form_packed<false>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)

@@ -22,6 +22,10 @@ struct QueueScratch {
   // CLMGB_OPT_QUEUE_PACKED_REFRESH: the warp refreshes its fresh lanes' columns
   // together, (column, level) pairs spread over the 32 lanes (k_moisture_form_packed)
   int packed;
+  // the packed refresh's inputs per column, contiguous: [capacity][PC_FIELDS][nlevsoi]
+  // (PcField), filled by k_impedance, so that a pass over one column's levels reads
+  // consecutive addresses and the resident columns' inputs stay in L2
+  double* pcache;
   // CLMGB_OPT_QUEUE_DEFER: a column still unfinished after `defer` attempts leaves the
   // work queue at its next accepted substep; its state (water [nlevsoi][capacity],
   // dtsub, dtdone, qcharge so far, attempts, status at index c) and its index (list)
@@ -70,6 +74,10 @@ struct SubstepLogView {
   int cap;
   int64_t stride;
 };
+
+// fields of QueueScratch::pcache: dz*1000, watsat, bsw, hksat, sucsat, the ice
+// impedance, 1000*(z[j+1]-z[j]) (levels below the bottom one) and qflx_rootsoi
+enum PcField { PC_DZW = 0, PC_WS, PC_BSW, PC_KS, PC_SUC, PC_IMP, PC_DEN, PC_ROOT, PC_FIELDS };
 
 // Segments of one clmgb_copy_segments call (8-byte words).
 struct CopySegments {

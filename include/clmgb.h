@@ -697,10 +697,10 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             arrays whole, since col_patchi/col_patchf and patch_column
                                             hold global indices, and sets this to c0. */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
-/* Gives the handle per-column scratch for up to max_nc columns (about 48*nlevsoi + 80
+/* Gives the handle per-column scratch for up to max_nc columns (about 112*nlevsoi + 80
  * bytes per column): the Richards solve then forms the ice impedances in a uniform
- * pre-pass and hands out columns longest-expected-first, and the WAVES schedule
- * becomes available.  Calls with more columns
+ * pre-pass, gathers each column's refresh inputs into one contiguous record, hands out
+ * columns longest-expected-first, and the WAVES schedule becomes available.  Calls with more columns
  * than reserved run without it.  Synchronises the device; call it at set-up, not
  * inside stream capture. */
 int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc);
