@@ -618,34 +618,61 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
 }
 
 // Ice impedances of every hydrology column, one thread per column, into imp_cache
-// [nlevsoi, ld_imp] (uniform work: no lane waits on another column).
-// With pcache given, also each column's record of the packed refresh's inputs
-// (QueueScratch::pcache), the same values the refresh would read or form.
+// [nlevsoi][ld_imp] (uniform work: no lane waits on another column).
 __global__ void __launch_bounds__(BLOCK)
-k_impedance(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* imp_cache, int64_t ld_imp,
-            double* pcache) {
+k_impedance(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* imp_cache, int64_t ld_imp) {
   const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
   if (c >= nc || !f.mask_hydrology[c]) return;
   const int64_t nl = f.col_nbedrock[c];
   if (nl < 1 || nl > D.nlevsoi) return;
   const int nlayers = (int)nl;
+  for (int j = 1; j <= nlayers; j++) imp_cache[(int64_t)(j - 1) * ld_imp + c] = mf_impedance(D, f, e_ice, c, j, nlayers);
+}
+
+// The impedances (imp_cache, as k_impedance) and each column's record of the packed
+// refresh's inputs (QueueScratch::pcache, [column][PC_FIELDS][nlevsoi]), by tiles of
+// 32 columns: the block reads the tile's levels column-fastest (coalesced), holds them
+// in shared memory, and writes the 32 records as one contiguous range.  Entries of
+// columns the solve skips, and levels below a column's bottom, are written as zero
+// and never read.
+constexpr int REC_COLS = 32, REC_THREADS = 256;
+__global__ void __launch_bounds__(REC_THREADS)
+k_column_records(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* imp_cache, int64_t ld_imp,
+                 double* pcache) {
+  extern __shared__ double tile[];   // [PC_FIELDS][nlevsoi][REC_COLS]
+  const int nls = D.nlevsoi, joff = D.nlevsno;
   const int64_t ld = D.ldc;
-  const int joff = D.nlevsno, nls = D.nlevsoi;
-  double* pc = pcache ? pcache + c * (int64_t)(PC_FIELDS * nls) : nullptr;
-  for (int j = 1; j <= nlayers; j++) {
-    const double imp = mf_impedance(D, f, e_ice, c, j, nlayers);
-    imp_cache[(int64_t)(j - 1) * ld_imp + c] = imp;
-    if (pc) {
-      double* q = pc + (j - 1);
-      q[PC_DZW * nls] = LVc(f.dz, c, joff + j, ld) * DENH2O;
-      q[PC_WS * nls] = LVc(f.watsat, c, j, ld);
-      q[PC_BSW * nls] = LVc(f.bsw, c, j, ld);
-      q[PC_KS * nls] = LVc(f.hksat, c, j, ld);
-      q[PC_SUC * nls] = LVc(f.sucsat, c, j, ld);
-      q[PC_IMP * nls] = imp;
-      if (j < nlayers) q[PC_DEN * nls] = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
-      q[PC_ROOT * nls] = LVc(f.qflx_rootsoi, c, j, ld);
+  const int64_t c0 = (int64_t)blockIdx.x * REC_COLS;
+  for (int idx = threadIdx.x; idx < nls * REC_COLS; idx += REC_THREADS) {
+    const int j = idx / REC_COLS + 1, cl = idx % REC_COLS;
+    const int64_t c = c0 + cl;
+    double v[PC_FIELDS];
+    for (int k = 0; k < PC_FIELDS; k++) v[k] = 0.0;
+    if (c < nc && f.mask_hydrology[c]) {
+      const int64_t nl = f.col_nbedrock[c];
+      if (nl >= 1 && nl <= nls && j <= nl) {
+        const int nlayers = (int)nl;
+        const double imp = mf_impedance(D, f, e_ice, c, j, nlayers);
+        imp_cache[(int64_t)(j - 1) * ld_imp + c] = imp;
+        v[PC_DZW] = LVc(f.dz, c, joff + j, ld) * DENH2O;
+        v[PC_WS] = LVc(f.watsat, c, j, ld);
+        v[PC_BSW] = LVc(f.bsw, c, j, ld);
+        v[PC_KS] = LVc(f.hksat, c, j, ld);
+        v[PC_SUC] = LVc(f.sucsat, c, j, ld);
+        v[PC_IMP] = imp;
+        if (j < nlayers) v[PC_DEN] = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
+        v[PC_ROOT] = LVc(f.qflx_rootsoi, c, j, ld);
+      }
     }
+    for (int k = 0; k < PC_FIELDS; k++) tile[((int64_t)k * nls + (j - 1)) * REC_COLS + cl] = v[k];
+  }
+  __syncthreads();
+  const int rec = PC_FIELDS * nls;
+  const int64_t ncols = (nc - c0) < REC_COLS ? (nc - c0) : REC_COLS;
+  double* out = pcache + c0 * rec;
+  for (int idx = threadIdx.x; idx < ncols * rec; idx += REC_THREADS) {
+    const int cl = idx / rec, r = idx % rec;   // r = field * nls + (j - 1)
+    out[idx] = tile[(int64_t)r * REC_COLS + cl];
   }
 }
 
@@ -853,8 +880,16 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   if (log && (e = cudaMemsetAsync(log->count, 0xff, (size_t)nc * sizeof(int32_t), s)) != cudaSuccess) return e;
   const bool use = qs.capacity >= nc && qs.order && qs.bins && qs.imp;
   if (use) {
-    k_impedance<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg.e_ice, qs.imp, qs.capacity,
-                                               qs.packed ? qs.pcache : nullptr);
+    if (qs.packed && qs.pcache) {
+      const size_t smem = (size_t)PC_FIELDS * D.nlevsoi * REC_COLS * sizeof(double);
+      if ((e = cudaFuncSetAttribute(k_column_records, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+          cudaSuccess)
+        return e;
+      k_column_records<<<(unsigned)((nc + REC_COLS - 1) / REC_COLS), REC_THREADS, smem, s>>>(
+          D, nc, f, cfg.e_ice, qs.imp, qs.capacity, qs.pcache);
+    } else {
+      k_impedance<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg.e_ice, qs.imp, qs.capacity);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (qs.longest_first) {
       if ((e = cudaMemsetAsync(qs.bins, 0, (2 * ORDER_BINS + 1) * sizeof(unsigned int), s)) != cudaSuccess) return e;
