@@ -64,11 +64,12 @@ static const int64_t CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM = 2;
 static const int64_t CLMGB_DEFAULT_FRESH_BATCH = 4;
 // Attempts after which the work-queue kernel hands a column to the warp-per-column
 // finish (CLMGB_OPT_QUEUE_DEFER).  Measured on GB300, 262,144 columns of the scale
-// workload, 2 blocks/SM, ms per column step: off 27.1, 12 -> 40.3, 16 -> 29.9,
-// 18 -> 30.2, 20 -> 25.2, 22 -> 23.8, 24 -> 23.6, 26 -> 23.9, 30 -> 24.4, 36 -> 25.0
-// (3 blocks/SM: 24 -> 23.4).  Below ~20 the deferred backlog, finished at a few
-// times the cost per attempt, outweighs the shorter end of the queue.
-static const int64_t CLMGB_DEFAULT_QUEUE_DEFER = 24;
+// workload, Richards ms per call with the packed refresh: 12 -> 33.3, 16 -> 22.6,
+// 20 -> 14.8, 24 -> 11.64, 26 -> 11.43, 28 -> 11.40, 30 -> 11.45, 32 -> 11.48,
+// 36 -> 11.70.  Below ~20 the deferred backlog, finished at a few times the cost per
+// attempt, outweighs the shorter end of the queue.  (With the per-lane refresh, ms per
+// column step at 2 blocks/SM: off 27.1, 16 -> 29.9, 20 -> 25.2, 24 -> 23.6, 30 -> 24.4.)
+static const int64_t CLMGB_DEFAULT_QUEUE_DEFER = 28;
 
 using clmgb::Dims;
 
