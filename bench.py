@@ -77,6 +77,25 @@ def parse():
     return ap.parse_args()
 
 
+def shard_seed(cfg_id, rank):
+    """Seed of rank `rank`'s column shard: every rank solves its own disjoint set of
+    columns (weak scaling), so a shard's results do not depend on the world size."""
+    from clmgb import synth
+    return synth.CONFIGS[cfg_id]["seed"] + 1000 * rank
+
+
+def aggregate_throughput(elapsed_ms, units_per_rank, world, device="cuda"):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's
+    time (a MAX all-reduce of the timed region; the only collective of the bench).
+    Returns (value, max elapsed ms)."""
+    if world > 1:
+        import torch
+        t = torch.tensor([elapsed_ms], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    return units_per_rank * world / (elapsed_ms / 1000.0), elapsed_ms
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -407,7 +426,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     cfg = abi.SwmConfig.clm5_default()
     nsteps = args.warmup + args.steps
-    seed = synth.CONFIGS[args.cfg]["seed"] + 1000 * rank
+    seed = shard_seed(args.cfg, rank)
     wl = synth.make_workload(args.cfg, nc=args.nc, seed=seed, nsteps=nsteps)
     st = wl.state
     nc = st.nc
@@ -501,11 +520,7 @@ def run_ours(args):
                  "value": gsteps * nc * world / (gms / 1000.0), "launches_per_step": 2,
                  "note": "clmgb_column_step (fused entry) replayed from one captured graph"}
         del g
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    value = args.steps * nc * world / (elapsed_ms / 1000.0)
+    value, elapsed_ms = aggregate_throughput(elapsed_ms, args.steps * nc, world)
 
     # roofline of the dominant kernel: the work-queue Richards solve (soil_water!)
     bytes_launch = bytes_model.richards_bytes_per_call(nc, st.vp.nlevsoi)
