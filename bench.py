@@ -469,6 +469,8 @@ def run_ours(args):
     for t in range(args.warmup):
         step(t)
     torch.cuda.synchronize()
+    # the state entering the timed steps, for the graph leg to replay the same steps from
+    d_timed0 = None if args.no_graph else d.copy()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -509,6 +511,10 @@ def run_ours(args):
         g = autotune.capture_steps(h, d, wl.dtime, Gd, Id, gsteps, first_step=args.warmup, cfg=cfg)
         g.replay()
         torch.cuda.synchronize()
+        for k, v in d_timed0.arrays.items():     # replay the timed steps from their own start
+            d.arrays[k].copy_(v)
+        del d_timed0
+        torch.cuda.synchronize()
         g0 = torch.cuda.Event(enable_timing=True)
         g1 = torch.cuda.Event(enable_timing=True)
         g0.record(stream)
@@ -518,7 +524,8 @@ def run_ours(args):
         gms = g0.elapsed_time(g1)
         graph = {"steps": gsteps, "ms_per_step": gms / gsteps,
                  "value": gsteps * nc * world / (gms / 1000.0), "launches_per_step": 2,
-                 "note": "clmgb_column_step (fused entry) replayed from one captured graph"}
+                 "note": "the timed steps again, from the same state, as clmgb_column_step (fused entry) "
+                         "calls replayed from one captured graph"}
         del g
     value, elapsed_ms = aggregate_throughput(elapsed_ms, args.steps * nc, world)
 
