@@ -295,12 +295,15 @@ struct MfLaneP {
   double dtsub, dtdone, dt_cur;
   double qc, qin1, hk_bot, dhkdw_bot;
   double dzv[MAXSOI + 1], dt_dz[MAXSOI + 1];
-  double gam[MAXSOI + 1], dwat[MAXSOI + 1];
-  LevelView liq, qout, dqodw1, dqodw2, fnet1;
+  double liq[MAXSOI + 1], gam[MAXSOI + 1], dwat[MAXSOI + 1];
+  LevelView qout, dqodw1, dqodw2, fnet1;
 };
 
-// shared-memory doubles per warp: 5 level arrays and the bottom conductivity pair
-__host__ __device__ constexpr int64_t packed_warp_doubles(int nlevsoi) { return (5LL * nlevsoi + 2) * 32; }
+// shared-memory doubles per warp: 4 level arrays and the bottom conductivity pair
+__host__ __device__ constexpr int64_t packed_warp_doubles(int nlevsoi) { return (4LL * nlevsoi + 2) * 32; }
+// threads per block of k_moisture_form_packed: 5 warps at 21 KB of shared memory each
+// (20 levels) put 2 blocks, 10 warps, on an SM
+constexpr int PBLOCK = 160;
 
 // mf_begin for the packed lane (the impedances stay in the cache the refresh reads)
 __device__ __forceinline__ bool mfp_begin(MfLaneP& L, const Dims& D, const clmgb_soilwater_fields& f,
@@ -356,13 +359,13 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
   const int off_own = incl - nl_own;
   const int T = __shfl_sync(FULL, incl, 31);
   const int64_t c_own = mine ? L.c : 0;
-  double* const sb = wsm + 5LL * nls * 32;                       // hk, dhkdw of the bottom level
+  double* const sb = wsm + 4LL * nls * 32;                       // hk, dhkdw of the bottom level
   auto A = [&](int a, int k, int j) -> double& { return wsm[((int64_t)a * nls + (j - 1)) * 32 + k]; };
   // input `fld` of level j of column c
   auto P = [&](int64_t c, int fld, int j) -> double {
     return pcache[c * (int64_t)(PC_FIELDS * nls) + (int64_t)fld * nls + (j - 1)];
   };
-  enum { LIQ = 0, QOUT = 1, D1 = 2, D2 = 3, FN = 4 };
+  enum { QOUT = 0, D1 = 1, D2 = 2, FN = 3 };
   struct Item { int k, j, nl; int64_t c; bool ok; };
   auto item = [&](int base) -> Item {
     const int t = base + lane;
@@ -379,11 +382,16 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
     it.ok = t < T;
     return it;
   };
+  // the refreshed lanes' water (kept in their local memory) into FN, where the other
+  // lanes of the warp can read it; their net fluxes there are about to be re-formed
+  if (mine)
+    for (int j = 1; j <= L.nlayers; j++) A(FN, lane, j) = L.liq[j];
+  __syncwarp();
   // pass 1: saturation of every level (:1283-1287), kept in FN
   for (int base = 0; base < T; base += 32) {
     const Item it = item(base);
     if (it.ok) {
-      const double vwc = jl_max(A(LIQ, it.k, it.j), 1.0e-6) / P(it.c, PC_DZW, it.j);
+      const double vwc = jl_max(A(FN, it.k, it.j), 1.0e-6) / P(it.c, PC_DZW, it.j);
       double s = vwc / P(it.c, PC_WS, it.j);
       s = jl_min(s, 1.0);
       A(FN, it.k, it.j) = jl_max(0.01, s);
@@ -490,7 +498,7 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
 // its dtsub and the time done before it, then the solve's outputs).  Dynamic shared
 // memory: packed_warp_doubles(nlevsoi) doubles per warp.
 template <bool LOG>
-__global__ void __launch_bounds__(BLOCK)
+__global__ void __launch_bounds__(PBLOCK)
 k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                        uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
                        const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
@@ -504,11 +512,10 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
                                       : (unsigned long long)nc;
   const int batch = fresh_batch > 0 ? fresh_batch : 1;
   MfLaneP L;
-  L.liq.p = wsm + (0LL * nls) * 32 + lane;
-  L.qout.p = wsm + (1LL * nls) * 32 + lane;
-  L.dqodw1.p = wsm + (2LL * nls) * 32 + lane;
-  L.dqodw2.p = wsm + (3LL * nls) * 32 + lane;
-  L.fnet1.p = wsm + (4LL * nls) * 32 + lane;
+  L.qout.p = wsm + (0LL * nls) * 32 + lane;
+  L.dqodw1.p = wsm + (1LL * nls) * 32 + lane;
+  L.dqodw2.p = wsm + (2LL * nls) * 32 + lane;
+  L.fnet1.p = wsm + (3LL * nls) * 32 + lane;
   int nacc = 0;
   bool active = false, exhausted = false;
   for (;;) {
@@ -914,7 +921,7 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
     if ((e = cudaMemsetAsync(q.d_list, 0xff, (size_t)nc * sizeof(uint32_t), s)) != cudaSuccess) return e;
   }
   if (use && qs.packed && qs.pcache) {
-    const size_t smem = (size_t)(BLOCK / 32) * (size_t)packed_warp_doubles(D.nlevsoi) * sizeof(double);
+    const size_t smem = (size_t)(PBLOCK / 32) * (size_t)packed_warp_doubles(D.nlevsoi) * sizeof(double);
     auto kern = log ? k_moisture_form_packed<true> : k_moisture_form_packed<false>;
     if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
       return e;
@@ -923,11 +930,11 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
     int dev = 0, nsm = 0, nb = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, BLOCK, smem)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, PBLOCK, smem)) != cudaSuccess) return e;
     if (nb < 1) return cudaErrorInvalidConfiguration;
     int gp = grid > 0 ? grid : 1;
     if (gp > nb * nsm) gp = nb * nsm;
-    kern<<<gp, BLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue, ord, nl, imp, ldi,
+    kern<<<gp, PBLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue, ord, nl, imp, ldi,
                                  dt_init, log ? *log : SubstepLogView{nullptr, nullptr, 0, 0}, qs.fresh_batch, q);
   } else if (log)
     k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
