@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-reserve", action="store_true", help="run without clmgb_reserve scratch")
     ap.add_argument("--queue-order", type=int, default=None)
     ap.add_argument("--fresh-batch", type=int, default=None, help="CLMGB_OPT_QUEUE_FRESH_BATCH override")
+    ap.add_argument("--defer", type=int, default=None, help="CLMGB_OPT_QUEUE_DEFER override")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration leg")
     ap.add_argument("--adjoint-only", action="store_true",
@@ -441,6 +442,8 @@ def run_ours(args):
         h.set_option(abi.OPT_QUEUE_ORDER, args.queue_order)
     if args.fresh_batch is not None:
         h.set_option(abi.OPT_QUEUE_FRESH_BATCH, args.fresh_batch)
+    if args.defer is not None:
+        h.set_option(abi.OPT_QUEUE_DEFER, args.defer)
     d = st.to_device()
     # per-step forcing, resident in HBM before the timed region
     Gd = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")

@@ -63,13 +63,13 @@ static const int64_t CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM = 2;
 // 20 -> 10.54, 24 -> 10.51 M column-steps/s when it was the default).
 static const int64_t CLMGB_DEFAULT_FRESH_BATCH = 4;
 // Attempts after which the work-queue kernel hands a column to the warp-per-column
-// finish (CLMGB_OPT_QUEUE_DEFER).  Measured on GB300, 262,144 columns of the scale
-// workload, Richards ms per call with the packed refresh: 12 -> 33.3, 16 -> 22.6,
-// 20 -> 14.8, 24 -> 11.64, 26 -> 11.43, 28 -> 11.40, 30 -> 11.45, 32 -> 11.48,
-// 36 -> 11.70.  Below ~20 the deferred backlog, finished at a few times the cost per
-// attempt, outweighs the shorter end of the queue.  (With the per-lane refresh, ms per
-// column step at 2 blocks/SM: off 27.1, 16 -> 29.9, 20 -> 25.2, 24 -> 23.6, 30 -> 24.4.)
-static const int64_t CLMGB_DEFAULT_QUEUE_DEFER = 28;
+// finish (CLMGB_OPT_QUEUE_DEFER).  Measured on GB300 over the 100 timed steps of the
+// scale workload (262,144 columns), ms per step with the packed refresh: 12 -> 29.3,
+// 16 -> 19.9, 18 -> 18.6, 20 -> 17.37, 22 -> 17.23, 24 -> 17.56, 28 -> 18.93,
+// 32 -> 20.5.  (Over steps 3-12 alone 28 was best: the later steps hold more long
+// columns.)  Below ~20 the deferred backlog, finished at a few times the cost per
+// attempt, outweighs the shorter end of the queue.
+static const int64_t CLMGB_DEFAULT_QUEUE_DEFER = 22;
 
 using clmgb::Dims;
 
