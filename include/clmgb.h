@@ -684,9 +684,9 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             (or no lane can attempt), then run it together (default 4); 0 = at
                                             once.  Results do not depend on it. */
 #define CLMGB_OPT_QUEUE_DEFER         16 /* work-queue Richards kernel with reserved scratch: a column not done
-                                            after this many attempts leaves the queue at its next accepted
-                                            substep and is finished by one warp (one level per lane); 0 = off.
-                                            Results do not depend on it. */
+                                            after this many attempts (default 22) leaves the queue at its next
+                                            accepted substep and is finished by one warp (one level per lane);
+                                            0 = off.  Results do not depend on it. */
 #define CLMGB_OPT_QUEUE_PACKED_REFRESH 17 /* work-queue Richards kernel with reserved scratch: 1 (default) = the
                                             warp runs the hydraulic refresh of its waiting lanes' columns
                                             together, column levels spread over the 32 lanes; 0 = each lane
