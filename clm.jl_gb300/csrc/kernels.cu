@@ -493,7 +493,8 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
   __syncwarp();
 }
 
-// k_moisture_form_queue with the packed refresh; needs the impedance cache.  With
+// k_moisture_form_queue with the packed refresh; reads the column records
+// (QueueScratch::pcache) k_column_records wrote before it.  With
 // LOG it writes the same substep log (the starting water of each accepted substep,
 // its dtsub and the time done before it, then the solve's outputs).  Dynamic shared
 // memory: packed_warp_doubles(nlevsoi) doubles per warp.
@@ -501,8 +502,8 @@ template <bool LOG>
 __global__ void __launch_bounds__(PBLOCK)
 k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_config cfg, double dtime,
                        uint32_t* col_status, int or_status, uint32_t* dev_status, unsigned long long* queue,
-                       const uint32_t* order, const unsigned int* nlisted_ptr, const double* imp_cache,
-                       int64_t ld_imp, const double* dt_init, SubstepLogView lg, int fresh_batch, QueueScratch qs) {
+                       const uint32_t* order, const unsigned int* nlisted_ptr, const double* dt_init,
+                       SubstepLogView lg, int fresh_batch, QueueScratch qs) {
   extern __shared__ double smem_packed[];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -934,8 +935,8 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
     if (nb < 1) return cudaErrorInvalidConfiguration;
     int gp = grid > 0 ? grid : 1;
     if (gp > nb * nsm) gp = nb * nsm;
-    kern<<<gp, PBLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue, ord, nl, imp, ldi,
-                                 dt_init, log ? *log : SubstepLogView{nullptr, nullptr, 0, 0}, qs.fresh_batch, q);
+    kern<<<gp, PBLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue, ord, nl, dt_init,
+                                 log ? *log : SubstepLogView{nullptr, nullptr, 0, 0}, qs.fresh_batch, q);
   } else if (log)
     k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                       dev_status, queue, ord, nl, imp, ldi, dt_init,
