@@ -66,6 +66,9 @@ OPT_QUEUE_FRESH_BATCH = 14
 OPT_COLUMN_BASE = 15
 OPT_QUEUE_DEFER = 16
 OPT_QUEUE_PACKED_REFRESH = 17
+OPT_ATTEMPT_CAP = 18
+OPT_QUEUE_POLL_LIMIT = 19
+OPT_QUEUE_PUBLISH_DELAY = 20
 MAX_COPY_SEGMENTS = 128
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
@@ -289,6 +292,7 @@ SOILWATER_FIELDS = [
     ("zwt", _f64, "c", None),
     ("qcharge", _f64, "c", None),
     ("num_substeps", _f64, "c", None),
+    ("smpmin", _f64, "c", None),
 ]
 
 # clmgb_rootsink_fields (compute_effec_rootfrac_and_vert_tran_sink!), header order;

@@ -33,7 +33,7 @@ from . import abi, api
 
 STATIC = ("mask_nolakec", "mask_nolakep", "mask_hydrology", "col_nbedrock", "col_itype", "col_landunit",
           "col_patchi", "col_patchf", "lun_itype", "lun_urbpoi", "patch_column", "patch_landunit", "patch_wtcol",
-          "dz", "z", "zi", "watsat", "bsw", "sucsat", "hksat", "tkmg", "tkdry", "csol")
+          "dz", "z", "zi", "watsat", "bsw", "sucsat", "hksat", "tkmg", "tkdry", "csol", "smpmin")
 
 INPUTS = ("col_snl", "frac_veg_nosno", "t_soisno", "t_h2osfc", "t_grnd", "emg", "htvp", "eflx_bot", "dlrad", "cgrnd",
           "eflx_sh_grnd", "eflx_sh_snow", "eflx_sh_soil", "eflx_sh_h2osfc", "h2osoi_liq", "h2osoi_ice", "excess_ice",

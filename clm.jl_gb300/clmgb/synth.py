@@ -265,6 +265,7 @@ def make_workload(cfg_id, nc=None, seed=None, vp=None, nsteps=None):
     fse = a["frac_sno_eff"]
     a["t_grnd"][:] = np.where(snl < 0, fse * top + (1.0 - fse) * a["t_soisno"][joff], a["t_soisno"][joff])
     a["zwt"][:] = zis[nlevsoi]
+    a["smpmin"][:] = -1.0e8          # cold_start.jl:763
     A = None
     if spec["snow"] == "mix":
         A = rng.uniform(50.0, 300.0, nc)

@@ -959,7 +959,7 @@ k_column_step_vjp_cf(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwat
       // ---- the substeps in reverse ----
       if (rich) {
         const int nl = L.nlayers;
-        const double lamQ = adj.lam_qcharge ? adj.lam_qcharge[c] : 0.0;
+        const double lamQ = adj.lam_qcharge && !qcharge_replaced(D, fw, cfg, c) ? adj.lam_qcharge[c] : 0.0;
         double lamL[MAXSOI + 1], liqs[MAXSOI + 1];
         double wsv[MAXSOI + 2], bbv[MAXSOI + 2], sucv[MAXSOI + 2], ksv[MAXSOI + 2];
         RichardsBar RB;

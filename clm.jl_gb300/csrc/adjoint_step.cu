@@ -490,7 +490,7 @@ k_column_step_vjp(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_
         if (rich) {
           double lamL[MAXSOI + 1];
           for (int j = 1; j <= LA.nlayers; j++) lamL[j] = LV(adj.lam_h2osoi_liq, c, joff + j, ld);
-          const double lamQ = adj.lam_qcharge ? adj.lam_qcharge[c] : 0.0;
+          const double lamQ = adj.lam_qcharge && !qcharge_replaced(D, fw, cfg, c) ? adj.lam_qcharge[c] : 0.0;
           if (s_tape.richards_mode == CLMGB_ADJ_RICHARDS_CLOSED_FORM) {
             RichardsBar RB;
             double impv[MAXSOI + 1], liqs[MAXSOI + 1];

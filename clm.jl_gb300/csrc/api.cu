@@ -46,6 +46,9 @@ struct clmgb_handle_s {
   clmgb::AdjTape tape;
   int64_t adj_st_mode;          // CLMGB_OPT_ADJ_SOIL_TEMPERATURE
   int64_t fresh_batch;          // CLMGB_OPT_QUEUE_FRESH_BATCH
+  int64_t attempt_cap;          // CLMGB_OPT_ATTEMPT_CAP
+  int64_t poll_limit;           // CLMGB_OPT_QUEUE_POLL_LIMIT
+  int64_t publish_delay;        // CLMGB_OPT_QUEUE_PUBLISH_DELAY
   cudaError_t last_error;
 };
 
@@ -97,9 +100,10 @@ static int32_t check_bounds(const clmgb_bounds* b, bool need_patches) {
   return CLMGB_OK;
 }
 
-static Dims make_dims(const clmgb_varpar& vp, const clmgb_bounds& b, int64_t c0 = 0) {
+static Dims make_dims(const clmgb_varpar& vp, const clmgb_bounds& b, int64_t c0 = 0, int attempt_cap = clmgb::MF_ATTEMPT_CAP) {
   Dims D;
   D.c0 = c0;
+  D.attempt_cap = attempt_cap;
   D.nlevsno = vp.nlevsno;
   D.nlevgrnd = vp.nlevgrnd;
   D.nlevsoi = vp.nlevsoi;
@@ -109,6 +113,10 @@ static Dims make_dims(const clmgb_varpar& vp, const clmgb_bounds& b, int64_t c0 
   D.ldp = b.ldp;
   D.np = b.np;
   return D;
+}
+
+static Dims hdims(clmgb_handle h, const clmgb_bounds& b) {
+  return make_dims(h->vp, b, h->column_base, (int)h->attempt_cap);
 }
 
 // every pointer member after struct_size must be non-NULL
@@ -131,8 +139,9 @@ static int32_t check_cfg(const clmgb_swm_config* cfg) {
   if (cfg->soilwater_movement_method == CLMGB_ZENGDECKER_2009) return CLMGB_ERR_UNSUPPORTED;
   if (cfg->soilwater_movement_method != CLMGB_MOISTURE_FORM) return CLMGB_ERR_CONFIG;
   if (cfg->upper_boundary_condition != CLMGB_BC_FLUX) return CLMGB_ERR_CONFIG;
+  // soilwm_moisture_form_solve!'s error() for any other lower boundary, BC_AQUIFER included
+  // (soil_water_movement.jl:1502-1505)
   const int lb = cfg->lower_boundary_condition;
-  if (lb == CLMGB_BC_AQUIFER) return CLMGB_ERR_UNSUPPORTED;
   if (!(lb == CLMGB_BC_WATERTABLE || lb == CLMGB_BC_FLUX || lb == CLMGB_BC_ZERO_FLUX)) return CLMGB_ERR_CONFIG;
   if (cfg->flux_calculation != 1 && cfg->flux_calculation != 42) return CLMGB_ERR_CONFIG;
   if (!(cfg->dtmin > 0.0)) return CLMGB_ERR_CONFIG;
@@ -155,6 +164,8 @@ static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
   q.d_status = have ? h->ws.status : nullptr;
   q.d_list = have ? h->ws.listA[0] : nullptr;
   q.d_count = have ? h->scratch + 7 : nullptr;
+  q.poll_limit = (int)h->poll_limit;
+  q.publish_delay = (int)h->publish_delay;
   return q;
 }
 
@@ -222,6 +233,9 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->qs.pcache = nullptr;
   h->qs.longest_first = 1;
   h->fresh_batch = CLMGB_DEFAULT_FRESH_BATCH;
+  h->attempt_cap = clmgb::MF_ATTEMPT_CAP;
+  h->poll_limit = clmgb::DEFER_POLL_LIMIT;
+  h->publish_delay = 0;
   memset(&h->ws, 0, sizeof(h->ws));
   h->waves_blocks = 0;
   h->waves_blocks_per_sm = 0;
@@ -285,7 +299,7 @@ int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (use_excess_ice) return CLMGB_ERR_UNSUPPORTED;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_soil_temperature(make_dims(h->vp, *b, h->column_base), b->nc, *f, dtime, snow_method, col_status,
+  cudaError_t ce = clmgb::launch_soil_temperature(hdims(h, *b), b->nc, *f, dtime, snow_method, col_status,
                                                   h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -298,7 +312,7 @@ int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   if (b->nc == 0 && b->np == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_soil_fluxes(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, dtime, h->dev_status,
+  cudaError_t ce = clmgb::launch_soil_fluxes(hdims(h, *b), b->nc, b->nl, *f, dtime, h->dev_status,
                                              (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -316,7 +330,7 @@ int32_t clmgb_soil_water_zd09(clmgb_handle h, const clmgb_bounds* b, const clmgb
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_zd09(make_dims(h->vp, *b, h->column_base), b->nc, *f, cfg->e_ice, dtime, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_zd09(hdims(h, *b), b->nc, *f, cfg->e_ice, dtime, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -341,7 +355,7 @@ int32_t clmgb_effec_rootfrac_vert_tran_sink(clmgb_handle h, const clmgb_bounds* 
     for (const void* p : hs)
       if (!p) return CLMGB_ERR_NULL_ARG;
   }
-  cudaError_t ce = clmgb::launch_rootsink(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, use_hydrstress ? 1 : 0,
+  cudaError_t ce = clmgb::launch_rootsink(hdims(h, *b), b->nc, b->nl, *f, use_hydrstress ? 1 : 0,
                                           col_status, h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -419,7 +433,7 @@ int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clm
   if (b->nc == 0 || stages == 0) return CLMGB_OK;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!surfhyd_pointers_ok(f, cfg, stages)) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_surface_hydrology(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, *cfg, stages, dtime,
+  cudaError_t ce = clmgb::launch_surface_hydrology(hdims(h, *b), b->nc, b->nl, *f, *cfg, stages, dtime,
                                                    h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -534,7 +548,7 @@ int32_t clmgb_lake_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
     const bool ch4 = member == (const void*)&f->lakeresist || member == (const void*)&f->grnd_ch4_cond;
     if (!q && !(ch4 && !cfg->use_lch4)) return CLMGB_ERR_NULL_ARG;
   }
-  cudaError_t ce = clmgb::launch_lake_temperature(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, h->dev_status,
+  cudaError_t ce = clmgb::launch_lake_temperature(hdims(h, *b), b->nc, *f, *cfg, dtime, h->dev_status,
                                                   (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -585,7 +599,7 @@ int32_t clmgb_snow_layers(clmgb_handle h, const clmgb_bounds* b, const clmgb_sno
   if (f->struct_size != (int64_t)sizeof(clmgb_snowlayer_fields)) return CLMGB_ERR_ABI;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!snowlayer_pointers_ok(f, cfg, stages)) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_snow_layers(make_dims(h->vp, *b, h->column_base), b->nc, b->nl, *f, *cfg, stages, dtime,
+  cudaError_t ce = clmgb::launch_snow_layers(hdims(h, *b), b->nc, b->nl, *f, *cfg, stages, dtime,
                                              h->dev_status, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -597,7 +611,7 @@ int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const 
   if (e) return e;
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
-  cudaError_t ce = clmgb::launch_water_fractions(make_dims(h->vp, *b, h->column_base), b->nc, *f, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_water_fractions(hdims(h, *b), b->nc, *f, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -612,15 +626,18 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soil
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   cudaError_t ce;
   if (h->step_schedule == CLMGB_SCHEDULE_FUSED)
-    ce = clmgb::launch_moisture_form(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, h->dev_status,
+    ce = clmgb::launch_moisture_form(hdims(h, *b), b->nc, *f, *cfg, dtime, col_status, h->dev_status,
                                      (cudaStream_t)stream);
   else if (use_waves(h, b->nc))
-    ce = clmgb::launch_moisture_form_waves(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, 0,
+    ce = clmgb::launch_moisture_form_waves(hdims(h, *b), b->nc, *f, *cfg, dtime, col_status, 0,
                                            h->dev_status, h->ws, waves_grid(h), (cudaStream_t)stream);
   else
-    ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, 0,
+    ce = clmgb::launch_moisture_form_queue(hdims(h, *b), b->nc, *f, *cfg, dtime, col_status, 0,
                                            h->dev_status, h->queue, queue_grid(h), queue_scratch(h),
                                            (cudaStream_t)stream);
+  if (ce == cudaSuccess)
+    ce = clmgb::launch_compute_qcharge(hdims(h, *b), b->nc, *f, *cfg, dtime,
+                                       (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -637,7 +654,7 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   if ((e = check_fields(fw))) return e;
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  const Dims D = make_dims(h->vp, *b, h->column_base);
+  const Dims D = hdims(h, *b);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce;
   if (h->step_schedule == CLMGB_SCHEDULE_FUSED) {
@@ -655,6 +672,7 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
                                                queue_grid(h), queue_scratch(h), s);
     }
   }
+  if (ce == cudaSuccess) ce = clmgb::launch_compute_qcharge(D, b->nc, *fw, *cfg, dtime, s);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -667,7 +685,7 @@ static int32_t phase_change_common(clmgb_handle h, const clmgb_bounds* b, const 
   if ((e = check_fields(f))) return e;
   if (!dhsdT) return CLMGB_ERR_NULL_ARG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_phase_change(make_dims(h->vp, *b, h->column_base), b->nc, *f, dtime, dhsdT, which,
+  cudaError_t ce = clmgb::launch_phase_change(hdims(h, *b), b->nc, *f, dtime, dhsdT, which,
                                               (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -691,7 +709,7 @@ int32_t clmgb_synth_forcing(clmgb_handle h, const clmgb_bounds* b, const clmgb_s
   if ((e = check_fields(ft))) return e;
   if ((e = check_fields(fw))) return e;
   if (!G || !I) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_synth_forcing(make_dims(h->vp, *b, h->column_base), b->nc, *ft, *fw, G, I, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_synth_forcing(hdims(h, *b), b->nc, *ft, *fw, G, I, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -802,6 +820,18 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
       h->packed = value;
       return CLMGB_OK;
+    case CLMGB_OPT_ATTEMPT_CAP:
+      if (value < 1 || value > clmgb::MF_ATTEMPT_CAP) return CLMGB_ERR_CONFIG;
+      h->attempt_cap = value;
+      return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_POLL_LIMIT:
+      if (value < 0 || value > clmgb::DEFER_POLL_LIMIT) return CLMGB_ERR_CONFIG;
+      h->poll_limit = value;
+      return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_PUBLISH_DELAY:
+      if (value < 0 || value > 1000000) return CLMGB_ERR_CONFIG;
+      h->publish_delay = value;
+      return CLMGB_OK;
     default:
       return CLMGB_ERR_CONFIG;
   }
@@ -826,6 +856,9 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_COLUMN_BASE: *value = h->column_base; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_DEFER: *value = h->defer; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_PACKED_REFRESH: *value = h->packed; return CLMGB_OK;
+    case CLMGB_OPT_ATTEMPT_CAP: *value = h->attempt_cap; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_POLL_LIMIT: *value = h->poll_limit; return CLMGB_OK;
+    case CLMGB_OPT_QUEUE_PUBLISH_DELAY: *value = h->publish_delay; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_USED: {
       unsigned int used = 0;
@@ -970,7 +1003,7 @@ int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const cl
   if ((e = check_log(log))) return e;
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  const Dims D = make_dims(h->vp, *b, h->column_base);
+  const Dims D = hdims(h, *b);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce = clmgb::launch_soiltemp_fractions(D, b->nc, *ft, *fw, dtime, snow_method, t_ssbef, t_h2osfc_bef,
                                                     col_status, h->dev_status, s);
@@ -979,6 +1012,7 @@ int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const cl
     ce = clmgb::launch_moisture_form_queue(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->queue,
                                            queue_grid(h), queue_scratch(h), s, nullptr, &lv);
   }
+  if (ce == cudaSuccess) ce = clmgb::launch_compute_qcharge(D, b->nc, *fw, *cfg, dtime, s);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -1010,7 +1044,7 @@ int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, cons
   if (snow_method != CLMGB_SNOW_JORDAN1991 && snow_method != CLMGB_SNOW_STURM1997) return CLMGB_ERR_CONFIG;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!h->tape_block) return CLMGB_ERR_CONFIG;
-  const Dims D = make_dims(h->vp, *b, h->column_base);
+  const Dims D = hdims(h, *b);
   if ((e = check_log(log))) return e;
   cudaError_t ce;
   if (h->adj_st_mode == CLMGB_ADJ_ST_CLOSED_FORM && h->tape.richards_mode == CLMGB_ADJ_RICHARDS_CLOSED_FORM)
@@ -1020,6 +1054,8 @@ int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, cons
   else
     ce = clmgb::launch_column_step_vjp(D, b->nc, *ft, *fw, *cfg, dtime, snow_method, t_ssbef, t_h2osfc_bef, *adj,
                                        h->tape, col_status, h->dev_status, (cudaStream_t)stream);
+  // the replayed step leaves the forward's state, compute_qcharge! included
+  if (ce == cudaSuccess) ce = clmgb::launch_compute_qcharge(D, b->nc, *fw, *cfg, dtime, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -1033,9 +1069,12 @@ int32_t clmgb_soil_water_warm(clmgb_handle h, const clmgb_bounds* b, const clmgb
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
-  cudaError_t ce = clmgb::launch_moisture_form_queue(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, col_status, 0,
+  cudaError_t ce = clmgb::launch_moisture_form_queue(hdims(h, *b), b->nc, *f, *cfg, dtime, col_status, 0,
                                                      h->dev_status, h->queue, queue_grid(h), queue_scratch(h),
                                                      (cudaStream_t)stream, dt_first);
+  if (ce == cudaSuccess)
+    ce = clmgb::launch_compute_qcharge(hdims(h, *b), b->nc, *f, *cfg, dtime,
+                                       (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -1050,8 +1089,11 @@ int32_t clmgb_mlp_samples(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
   if ((e = check_fields(f))) return e;
   if (!(dtime > 0.0) || per_column < 0) return CLMGB_ERR_CONFIG;
   if (!features || !targets || !count || capacity < 0) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_richards_samples(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, per_column, features,
+  cudaError_t ce = clmgb::launch_richards_samples(hdims(h, *b), b->nc, *f, *cfg, dtime, per_column, features,
                                                   targets, count, capacity, col_status, (cudaStream_t)stream);
+  if (ce == cudaSuccess)
+    ce = clmgb::launch_compute_qcharge(hdims(h, *b), b->nc, *f, *cfg, dtime,
+                                       (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -1115,7 +1157,7 @@ int32_t clmgb_mlp_features(clmgb_handle h, const clmgb_bounds* b, const clmgb_so
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(f))) return e;
   if (!mean || !istd || !X) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_mlp_features(make_dims(h->vp, *b, h->column_base), b->nc, *f, *cfg, dtime, mean, istd, X,
+  cudaError_t ce = clmgb::launch_mlp_features(hdims(h, *b), b->nc, *f, *cfg, dtime, mean, istd, X,
                                               (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
@@ -1137,7 +1179,7 @@ int32_t clmgb_balance_begin(clmgb_handle h, const clmgb_bounds* b, const clmgb_s
   if (b->nc == 0) return CLMGB_OK;
   if ((e = check_fields(ft))) return e;
   if (!t_grnd0 || !begwb) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_balance_begin(make_dims(h->vp, *b, h->column_base), b->nc, *ft, t_grnd0, begwb, (cudaStream_t)stream);
+  cudaError_t ce = clmgb::launch_balance_begin(hdims(h, *b), b->nc, *ft, t_grnd0, begwb, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
@@ -1153,7 +1195,7 @@ int32_t clmgb_balance_residuals(clmgb_handle h, const clmgb_bounds* b, const clm
   if ((e = check_fields(fw))) return e;
   if (!(dtime > 0.0)) return CLMGB_ERR_CONFIG;
   if (!t_ssbef || !t_h2osfc_bef || !t_grnd0 || !begwb || !errsoi || !errh2o) return CLMGB_ERR_NULL_ARG;
-  cudaError_t ce = clmgb::launch_balance_residuals(make_dims(h->vp, *b, h->column_base), b->nc, *ft, *fw, dtime, t_ssbef, t_h2osfc_bef,
+  cudaError_t ce = clmgb::launch_balance_residuals(hdims(h, *b), b->nc, *ft, *fw, dtime, t_ssbef, t_h2osfc_bef,
                                                    t_grnd0, begwb, errsoi, errh2o, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }

@@ -47,11 +47,14 @@ constexpr int MAXL = MAXSNO + MAXGRND;       // snow + ground levels
 constexpr int MAXROWS = MAXL + 1;            // + the surface-water row of the band system
 constexpr int MAXSOI = CLMGB_MAX_NLEVSOI;
 constexpr int MF_ATTEMPT_CAP = 4096;         // safety cap on Richards substep attempts
+// polls of a deferred column's list slot before the drain gives it back (richards_coop.cuh)
+constexpr int DEFER_POLL_LIMIT = 1 << 20;
 
 struct Dims {
   int nlevsno, nlevgrnd, nlevsoi, nlevurb, nlevmax;
   int64_t ldc, ldp, np;
   int64_t c0 = 0;    // global index of the call's first column (patch_column holds global indices)
+  int attempt_cap = MF_ATTEMPT_CAP;   // Richards attempts after which a column stops (CLMGB_COL_SUBSTEP_CAP)
 };
 
 // Julia Base.max / Base.min on Float64 (NaN propagates, -0.0 < 0.0).  They only
@@ -1114,7 +1117,7 @@ __device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soi
   const int nlayers = L.nlayers;
   const int lower_bc = cfg.lower_boundary_condition;
   L.nsub += 1;
-  if (L.nsub > MF_ATTEMPT_CAP) {
+  if (L.nsub > D.attempt_cap) {
     L.status |= CLMGB_COL_SUBSTEP_CAP;
     return true;
   }
@@ -1261,6 +1264,68 @@ __device__ inline uint32_t moisture_form_col(const Dims& D, const clmgb_soilwate
                                              const clmgb_swm_config& cfg, double dtime, int64_t c) {
   FieldState<clmgb_soilwater_fields> X(f, c, D.ldc);
   return moisture_form_col(D, f, cfg, dtime, c, X);
+}
+
+// ===========================================================================
+// compute_qcharge! (soil_water_movement.jl:1153-1215) as soilwater_moisture_form! runs it
+// after the solve under use_aquifer_layer(cfg) (:1575-1598; of those lower boundaries the
+// moisture form accepts BC_WATERTABLE only).  The reference hands it freshly zeroed dwat,
+// smp and imped rows, and vwc_liq = max(h2osoi_liq, 1e-6)/(dz*1000) of the solved water on
+// levels 1..min(nbedrock, nlevsoi), zero below.  So the conductivity ka = 0*hksat*s1^(2b+3)
+// is zero and the recharge written is a signed zero, for every column whose water table
+// lies within the soil column (jwt < nlevsoi); the other columns keep the solve's qcharge.
+// ===========================================================================
+// jwt: the number of soil levels above the water table (:1177-1184)
+__device__ __forceinline__ int watertable_level(const Dims& D, const clmgb_soilwater_fields& f, int64_t c) {
+  int jwt = D.nlevsoi;
+  for (int j = 1; j <= D.nlevsoi; j++) {
+    if (f.zwt[c] <= LVc(f.zi, c, D.nlevsno + 1 + j, D.ldc)) {
+      jwt = j - 1;
+      break;
+    }
+  }
+  return jwt;
+}
+
+// True when that pass replaces the solve's qcharge of column c.  The value it writes then
+// depends on no state or parameter (ka is exactly zero), so the qcharge adjoint the
+// step's reverse receives stops there.
+__device__ __forceinline__ bool qcharge_replaced(const Dims& D, const clmgb_soilwater_fields& f,
+                                                 const clmgb_swm_config& cfg, int64_t c) {
+  return cfg.lower_boundary_condition == CLMGB_BC_WATERTABLE && watertable_level(D, f, c) < D.nlevsoi;
+}
+
+// The pass for column c (nbedrock in 1..nlevsoi); returns true when it wrote qcharge.
+__device__ inline bool compute_qcharge_col(const Dims& D, const clmgb_soilwater_fields& f, double dtime,
+                                           int64_t c) {
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno;
+  const int jwt = watertable_level(D, f, c);
+  if (jwt >= D.nlevsoi) return false;
+  const int nlayers = (int)f.col_nbedrock[c];
+  const int jp = jwt + 1;
+  const double zwt = f.zwt[c];
+  const double wh_zwt = -LVc(f.sucsat, c, jp, ld) - zwt * M_TO_MM;
+  const double vwc = jp <= nlayers ? jl_max(LV(f.h2osoi_liq, c, joff + jp, ld), 1.0e-6) /
+                                         (LVc(f.dz, c, joff + jp, ld) * DENH2O)
+                                   : 0.0;
+  double s1 = jl_max(vwc / LVc(f.watsat, c, jp, ld), 0.01);
+  s1 = jl_min(1.0, s1);
+  const double imped = 0.0, smp = 0.0;   // the zeroed scratch rows the reference passes
+  const double b = LVc(f.bsw, c, jp, ld);
+  const double ka = imped * LVc(f.hksat, c, jp, ld) * cm_pow(s1, 2.0 * b + 3.0);
+  const int jm = jwt > 1 ? jwt : 1;
+  const double smp1 = jl_max(__ldg(f.smpmin + c), smp);
+  const double wh = smp1 - LVc(f.z, c, joff + jm, ld) * M_TO_MM;
+  double q;
+  if (jwt == 0)
+    q = -ka * (wh_zwt - wh) / ((zwt + 1.0e-3) * M_TO_MM);
+  else
+    q = -ka * (wh_zwt - wh) / ((zwt - LVc(f.z, c, joff + jwt, ld)) * M_TO_MM * 2.0);
+  q = jl_max(-10.0 / dtime, q);
+  q = jl_min(10.0 / dtime, q);
+  f.qcharge[c] = q;
+  return true;
 }
 
 }  // namespace clmgb

@@ -150,7 +150,7 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
                                       : (unsigned long long)nc;
   MfLane L;
   int nacc = 0;
-  bool active = false, exhausted = false;
+  bool active = false, exhausted = false, kept = false;
   for (;;) {
     const bool need = !active && !exhausted;
     const unsigned m = __ballot_sync(FULL, need);
@@ -169,6 +169,7 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
             if (mf_begin(L, D, f, cfg, dtime, c, imp_cache, ld_imp, dt_init)) {
               active = true;
               nacc = 0;
+              kept = false;
             } else {
               const uint32_t st = L.status;
               if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
@@ -196,7 +197,7 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
     // operations and their order are unchanged.
     bool can_try = active;
     if (fresh_batch > 0) {
-      const bool want = active && L.fresh && L.nsub < MF_ATTEMPT_CAP;
+      const bool want = active && L.fresh && L.nsub < D.attempt_cap;
       const unsigned wm = __ballot_sync(FULL, want);
       const unsigned tm = __ballot_sync(FULL, active && !want);
       if (wm && (__popc(wm) >= fresh_batch || tm == 0) && want) {
@@ -207,7 +208,7 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
         FieldState<clmgb_soilwater_fields> X(f, L.c, D.ldc);
         mf_refresh(L, D, f, cfg, X);
       }
-      can_try = active && !(L.fresh && L.nsub < MF_ATTEMPT_CAP);
+      can_try = active && !(L.fresh && L.nsub < D.attempt_cap);
     }
     if (!can_try) continue;
     double* rec = nullptr;
@@ -227,22 +228,13 @@ k_moisture_form_queue(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
       }
       nacc++;
     }
-    if (!LOG && !fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer) {
-      // hand the column over: claim a list slot, store the state, then publish
-      const int64_t c = L.c, cap = qs.capacity;
-      const unsigned long long slot = atomicAdd(qs.d_count, 1ULL);
-      for (int j = 1; j <= L.nlayers; j++) qs.d_liq[(int64_t)(j - 1) * cap + c] = L.liq[j];
-      qs.d_dtsub[c] = L.dtsub;
-      qs.d_dtdone[c] = L.dtdone;
-      qs.d_qc[c] = L.qc;
-      qs.d_nsub[c] = L.nsub;
-      qs.d_status[c] = L.status;
-      __threadfence();
-      *(volatile uint32_t*)(qs.d_list + slot) = (uint32_t)c;
-      __threadfence();
-      atomicAdd(qs.d_count + 1, 1ULL);
-      active = false;
-      continue;
+    if (!LOG && !fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer && !kept) {
+      // hand the column over; a slot the drain gave back leaves it with this lane
+      if (coop_defer(L, qs)) {
+        active = false;
+        continue;
+      }
+      kept = true;
     }
     if (fin) {
       const uint32_t st = mf_end(L, D, f);
@@ -518,7 +510,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
   L.dqodw2.p = wsm + (2LL * nls) * 32 + lane;
   L.fnet1.p = wsm + (3LL * nls) * 32 + lane;
   int nacc = 0;
-  bool active = false, exhausted = false;
+  bool active = false, exhausted = false, kept = false;
   for (;;) {
     const bool need = !active && !exhausted;
     const unsigned m = __ballot_sync(FULL, need);
@@ -537,6 +529,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
             if (mfp_begin(L, D, f, cfg, dtime, c, dt_init)) {
               active = true;
               nacc = 0;
+              kept = false;
             } else {
               const uint32_t st = L.status;
               if (col_status) col_status[c] = or_status ? (col_status[c] | st) : st;
@@ -557,7 +550,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
     }
     // lanes whose substep was accepted wait for the packed refresh until `batch` of
     // them need it or no lane can attempt
-    const bool want = active && L.fresh && L.nsub < MF_ATTEMPT_CAP;
+    const bool want = active && L.fresh && L.nsub < D.attempt_cap;
     const unsigned wm = __ballot_sync(FULL, want);
     const unsigned tm = __ballot_sync(FULL, active && !want);
     if (wm && (__popc(wm) >= batch || tm == 0)) {
@@ -567,7 +560,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
       }
       mfp_refresh(L, wm, D, f, cfg, qs.pcache, wsm, nls);
     }
-    const bool can_try = active && !(L.fresh && L.nsub < MF_ATTEMPT_CAP);
+    const bool can_try = active && !(L.fresh && L.nsub < D.attempt_cap);
     if (!can_try) continue;
     double* rec = nullptr;
     double dts = 0.0, dtd = 0.0;
@@ -587,22 +580,13 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
       }
       nacc++;
     }
-    if (!LOG && !fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer) {
-      // hand the column over: claim a list slot, store the state, then publish
-      const int64_t c = L.c, cap = qs.capacity;
-      const unsigned long long slot = atomicAdd(qs.d_count, 1ULL);
-      for (int j = 1; j <= L.nlayers; j++) qs.d_liq[(int64_t)(j - 1) * cap + c] = L.liq[j];
-      qs.d_dtsub[c] = L.dtsub;
-      qs.d_dtdone[c] = L.dtdone;
-      qs.d_qc[c] = L.qc;
-      qs.d_nsub[c] = L.nsub;
-      qs.d_status[c] = L.status;
-      __threadfence();
-      *(volatile uint32_t*)(qs.d_list + slot) = (uint32_t)c;
-      __threadfence();
-      atomicAdd(qs.d_count + 1, 1ULL);
-      active = false;
-      continue;
+    if (!LOG && !fin && qs.defer > 0 && L.fresh && L.nsub >= qs.defer && !kept) {
+      // hand the column over; a slot the drain gave back leaves it with this lane
+      if (coop_defer(L, qs)) {
+        active = false;
+        continue;
+      }
+      kept = true;
     }
     if (fin) {
       const uint32_t st = mf_end(L, D, f, X);
@@ -623,6 +607,18 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
       active = false;
     }
   }
+}
+
+// compute_qcharge! after a moisture-form solve with the water-table lower boundary
+// (soil_water_movement.jl:1575-1598): one thread per hydrology column the solve
+// could take (nbedrock in range).
+__global__ void __launch_bounds__(BLOCK)
+k_compute_qcharge(Dims D, int64_t nc, clmgb_soilwater_fields f, double dtime) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc || !f.mask_hydrology[c]) return;
+  const int64_t nl = f.col_nbedrock[c];
+  if (nl < 1 || nl > D.nlevsoi) return;
+  compute_qcharge_col(D, f, dtime, c);
 }
 
 // Ice impedances of every hydrology column, one thread per column, into imp_cache
@@ -968,6 +964,12 @@ __global__ void __launch_bounds__(256) k_copy_segments(CopySegments cs) {
     }
     for (; i < n; i += stride) __stcs(dst + i, __ldcs(src + i));
   }
+}
+cudaError_t launch_compute_qcharge(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                  const clmgb_swm_config& cfg, double dtime, cudaStream_t s) {
+  if (cfg.lower_boundary_condition != CLMGB_BC_WATERTABLE || nc <= 0) return cudaSuccess;
+  k_compute_qcharge<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, dtime);
+  return cudaGetLastError();
 }
 cudaError_t launch_copy_segments(const CopySegments& cs, cudaStream_t s) {
   if (cs.n <= 0) return cudaSuccess;

@@ -37,6 +37,12 @@ struct QueueScratch {
   uint32_t* d_status;
   uint32_t* d_list;
   unsigned long long* d_count;
+  // polls of a list slot whose index is still on its way before the drain gives the
+  // slot back (CLMGB_OPT_QUEUE_POLL_LIMIT), and a delay in ns between a deferral's
+  // claim of an even slot and its publication (CLMGB_OPT_QUEUE_PUBLISH_DELAY, 0 in
+  // production: it lets a test make that wait run out)
+  int poll_limit = DEFER_POLL_LIMIT;
+  int publish_delay = 0;
 };
 
 // Per-column state of the wave-synchronous Richards solve (richards_waves.cu), from
@@ -122,6 +128,10 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
                                        int or_status, uint32_t* dev_status, unsigned long long* queue,
                                        int grid_blocks, const QueueScratch& qs, cudaStream_t s,
                                        const double* dt_init = nullptr, const SubstepLogView* log = nullptr);
+// compute_qcharge! over the solved state when cfg's lower boundary is the water table
+// (a no-op otherwise); every moisture-form entry point runs it after its solve.
+cudaError_t launch_compute_qcharge(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
+                                  const clmgb_swm_config& cfg, double dtime, cudaStream_t s);
 cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                       cudaStream_t s);

@@ -16,9 +16,10 @@
 // or devices sharing a context without ordering) race on the array and must not be
 // issued; serialise them on one stream.
 //
-// The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (once per device, with that device current); make that
-// first call before any stream capture.
+// Every call looks up the array's device address in the current context with
+// cudaGetSymbolAddress, with that device current.  The first call on a device loads
+// the library's module there, which stream capture does not allow: make that first
+// call before any stream capture.
 #include <atomic>
 #include <string.h>
 #include <cuda_runtime.h>
@@ -33,7 +34,6 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 // [0] queue counter, [1] number of listed columns, then the column list (uint32)
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[2 + CLMGB_NOALLOC_MAX_COLUMNS / 2];
 
-static std::atomic<unsigned long long*> g_noalloc_ptr[NOALLOC_MAX_DEVICES];
 static std::atomic<int> g_noalloc_grid[NOALLOC_MAX_DEVICES];
 
 // Lists the columns with mask[c] set (order irrelevant: columns are independent).
@@ -92,29 +92,32 @@ k_noalloc_moisture_form(Dims D, clmgb_soilwater_fields f, clmgb_swm_config cfg, 
   }
 }
 
-// Device address of the scratch array for the current device (looked up once).
+// Device address of the scratch array in the current context, and the grid of the
+// solve kernel on the current device.  The address is looked up on every call: a
+// __device__ array's address belongs to a CUDA context, so a pointer kept from an
+// earlier call would dangle after cudaDeviceReset or under another context on the
+// same device.  Once the library's module is loaded (by the first call) the lookup
+// neither allocates nor synchronises, so later calls may run under stream capture.
+// The occupancy-derived grid depends on the device only and is kept per device.
 static cudaError_t noalloc_setup(unsigned long long** out, int* grid) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-  unsigned long long* p = g_noalloc_ptr[dev].load();
+  void* sym = nullptr;
+  e = cudaGetSymbolAddress(&sym, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
   int g = g_noalloc_grid[dev].load();
-  if (!p || g <= 0) {
-    void* sym = nullptr;
-    e = cudaGetSymbolAddress(&sym, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
+  if (g <= 0) {
     int sms = 0, per_sm = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_noalloc_moisture_form, NOALLOC_BLOCK, 0);
     if (e != cudaSuccess) return e;
-    p = static_cast<unsigned long long*>(sym);
     g = sms * (per_sm > 0 ? per_sm : 1);
-    g_noalloc_ptr[dev].store(p);
     g_noalloc_grid[dev].store(g);
   }
-  *out = p;
+  *out = static_cast<unsigned long long*>(sym);
   *grid = g;
   return cudaSuccess;
 }
@@ -134,7 +137,9 @@ cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soi
   if (e != cudaSuccess) return e;
   const int g = (int)((int64_t)blocks < grid ? blocks : grid);
   k_noalloc_moisture_form<<<g > 0 ? g : 1, NOALLOC_BLOCK, 0, s>>>(D, f, cfg, dtime, col_status, scratch);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_compute_qcharge(D, nc, f, cfg, dtime, s);
 }
 
 }  // namespace clmgb
@@ -152,7 +157,6 @@ extern "C" int32_t clmgb_soil_water_noalloc(const clmgb_varpar* vp, const clmgb_
   if (cfg->soilwater_movement_method == CLMGB_ZENGDECKER_2009) return CLMGB_ERR_UNSUPPORTED;
   if (cfg->soilwater_movement_method != CLMGB_MOISTURE_FORM || cfg->upper_boundary_condition != CLMGB_BC_FLUX)
     return CLMGB_ERR_CONFIG;
-  if (cfg->lower_boundary_condition == CLMGB_BC_AQUIFER) return CLMGB_ERR_UNSUPPORTED;
   if (!(cfg->lower_boundary_condition == CLMGB_BC_WATERTABLE || cfg->lower_boundary_condition == CLMGB_BC_FLUX ||
         cfg->lower_boundary_condition == CLMGB_BC_ZERO_FLUX))
     return CLMGB_ERR_CONFIG;

@@ -20,6 +20,33 @@ namespace clmgb {
 
 constexpr unsigned COOP_FULL = 0xffffffffu;
 constexpr uint32_t DEFER_EMPTY = 0xffffffffu;     // a list slot not written yet
+constexpr uint32_t DEFER_GIVEN_BACK = 0xfffffffeu; // a slot the drain stopped waiting for
+
+// The deferring lane's half of a hand-over: claim a list slot, store the column's state,
+// then write the column's index into the slot and count it published.  Returns false
+// when the drain has already given the slot back (its bounded wait for the index ran
+// out, coop_drain): the lane then keeps the column and finishes it itself, so no column
+// is ever left unfinished.  Each column is handed over at most once, so at most nc
+// slots are claimed.
+template <class LT>
+__device__ __forceinline__ bool coop_defer(const LT& L, const QueueScratch& qs) {
+  const int64_t c = L.c, cap = qs.capacity;
+  const unsigned long long slot = atomicAdd(qs.d_count, 1ULL);
+  for (int j = 1; j <= L.nlayers; j++) qs.d_liq[(int64_t)(j - 1) * cap + c] = L.liq[j];
+  qs.d_dtsub[c] = L.dtsub;
+  qs.d_dtdone[c] = L.dtdone;
+  qs.d_qc[c] = L.qc;
+  qs.d_nsub[c] = L.nsub;
+  qs.d_status[c] = L.status;
+  // test hook: even slots publish late (bounded, <= 1 ms), so later slots overtake them
+  if ((slot & 1ULL) == 0)
+    for (int t = 0; t < qs.publish_delay; t += 500) __nanosleep(500);
+  __threadfence();
+  const uint32_t prev = atomicCAS(qs.d_list + slot, DEFER_EMPTY, (uint32_t)c);
+  __threadfence();
+  atomicAdd(qs.d_count + 1, 1ULL);   // published (a slot given back counts too)
+  return prev == DEFER_EMPTY;
+}
 
 __device__ __forceinline__ double coop_bcast(double v, int src) { return __shfl_sync(COOP_FULL, v, src); }
 
@@ -66,7 +93,7 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
   bool fresh = true;
   for (;;) {
     nsub += 1;
-    if (nsub > MF_ATTEMPT_CAP) {
+    if (nsub > D.attempt_cap) {
       status |= CLMGB_COL_SUBSTEP_CAP;
       break;
     }
@@ -243,8 +270,11 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
 // called by a whole warp whose lanes have no work left.  A slot is claimed only
 // below the published count; its column index may still be in flight from the
 // lane that deferred it (which has already claimed the slot and stores it next), so
-// the wait for it is short, and bounded: past the limit the column is left as it
-// was deferred and CLMGB_COL_QUEUE_WAIT is raised.
+// the wait for it is short, and bounded (qs.poll_limit polls): past the limit the
+// drain gives the slot back with an atomic exchange, the deferring lane then finds it
+// given back and finishes the column itself (coop_defer), and CLMGB_COL_QUEUE_WAIT is
+// raised in the device status to record that the slow path ran.  Results do not
+// depend on which warp finishes a column.
 __device__ __forceinline__ void coop_drain(const Dims& D, const clmgb_soilwater_fields& f, const clmgb_swm_config& cfg,
                                            double dtime, uint32_t* col_status, int or_status, uint32_t* dev_status,
                                            const QueueScratch& qs) {
@@ -270,12 +300,16 @@ __device__ __forceinline__ void coop_drain(const Dims& D, const clmgb_soilwater_
     if (got < 0) return;
     uint32_t cidx = DEFER_EMPTY;
     if (lane == 0) {
-      for (int it = 0; it < (1 << 20); it++) {
+      for (int it = 0; it < qs.poll_limit; it++) {
         cidx = *(volatile uint32_t*)(qs.d_list + got);
         if (cidx != DEFER_EMPTY) break;
         __nanosleep(64);
       }
-      if (cidx == DEFER_EMPTY && dev_status) atomicOr(dev_status, CLMGB_COL_QUEUE_WAIT);
+      if (cidx == DEFER_EMPTY) {
+        // give the slot back, unless the index arrived meanwhile
+        cidx = atomicExch(qs.d_list + got, DEFER_GIVEN_BACK);
+        if (cidx == DEFER_EMPTY && dev_status) atomicOr(dev_status, CLMGB_COL_QUEUE_WAIT);
+      }
       __threadfence();
     }
     cidx = __shfl_sync(COOP_FULL, cidx, 0);

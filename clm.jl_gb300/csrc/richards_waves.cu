@@ -132,7 +132,7 @@ __device__ __forceinline__ int wave_attempt(const Dims& D, const clmgb_soilwater
   const int lower_bc = cfg.lower_boundary_condition;
   int nsub = __ldcg(&w.nsub[c]) + 1;
   __stcg(&w.nsub[c], nsub);
-  if (nsub > MF_ATTEMPT_CAP) {
+  if (nsub > D.attempt_cap) {
     __stcg(&w.status[c], __ldcg(&w.status[c]) | CLMGB_COL_SUBSTEP_CAP);
     return WAVE_DONE;
   }
@@ -307,7 +307,7 @@ k_moisture_form_waves(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_co
   grid.sync();
   int cur = 0;  // list buffer
   int cs = 0;   // counter set
-  for (int round = 0; round <= MF_ATTEMPT_CAP + 1; round++) {
+  for (int round = 0; round <= D.attempt_cap + 1; round++) {
     const unsigned int nHA = cnt[3 * cs], nA = cnt[3 * cs + 1];
     const unsigned int total = nHA + nA;
     if (total == 0) break;

@@ -102,7 +102,7 @@ function soilwater_fields(col, mask_hydrology, sh, ss, wfb, wsb)
                    ptr(ss.watsat_col), ptr(ss.hksat_col), ptr(ss.bsw_col), ptr(ss.sucsat_col),
                    ptr(ss.eff_porosity_col), ptr(sh.icefrac_col), ptr(ss.smp_l_col), ptr(ss.hk_l_col),
                    ptr(wfb.qflx_rootsoi_col), ptr(wfb.wf.qflx_infl_col), ptr(sh.zwt_col),
-                   ptr(sh.qcharge_col), ptr(sh.num_substeps_col)]
+                   ptr(sh.qcharge_col), ptr(sh.num_substeps_col), ptr(ss.smpmin_col)]
     buf = Vector{UInt8}(undef, 8 * (1 + length(p)))
     GC.@preserve buf begin
         unsafe_store!(Ptr{Int64}(pointer(buf)), Int64(length(buf)))

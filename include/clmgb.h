@@ -63,8 +63,10 @@ extern "C" {
                                         of clmgb_reserve_adjoint) */
 #define CLMGB_COL_ADJ_REPLAY   128u  /* step adjoint: a replayed substep was not accepted again
                                         (its adjoint is not valid) */
-#define CLMGB_COL_QUEUE_WAIT   512u  /* Richards work queue: a bounded wait for a deferred column's
-                                        index gave up; the column was left unfinished (not expected) */
+#define CLMGB_COL_QUEUE_WAIT   512u  /* Richards work queue (device status only): a bounded wait for a
+                                        deferred column's index ran out and the slot was given back;
+                                        the lane that deferred the column finished it itself, so
+                                        every result is complete (a record of the slow path) */
 #define CLMGB_COL_FILTER       256u  /* root sink: the column is in two of the reference's filters
                                         (a pervious road on a natural-vegetation landunit) */
 
@@ -242,6 +244,7 @@ typedef struct clmgb_soilwater_fields {
   const double* zwt;                 /* [nc] */
   double* qcharge;                   /* [nc]  W */
   double* num_substeps;              /* [nc]  W (Float64 as in the reference) */
+  const double* smpmin;              /* [nc]  soilstate.smpmin_col, read by compute_qcharge! */
 } clmgb_soilwater_fields;
 
 /* compute_effec_rootfrac_and_vert_tran_sink! (soil_water_plant_sink.jl:341-451): the
@@ -691,6 +694,16 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             warp runs the hydraulic refresh of its waiting lanes' columns
                                             together, column levels spread over the 32 lanes; 0 = each lane
                                             runs its own.  Results do not depend on it. */
+#define CLMGB_OPT_ATTEMPT_CAP         18 /* Richards substep attempts after which a column stops with
+                                            CLMGB_COL_SUBSTEP_CAP (1..4096, default 4096: never reached by a
+                                            valid configuration, whose attempts dtmin bounds) */
+#define CLMGB_OPT_QUEUE_POLL_LIMIT    19 /* polls of a deferred column's list slot before the finishing warp
+                                            gives the slot back to the deferring lane (0..2^20, default
+                                            2^20).  Results do not depend on it. */
+#define CLMGB_OPT_QUEUE_PUBLISH_DELAY 20 /* ns a deferring lane waits between claiming an even list slot
+                                            and publishing it, so that later slots overtake it (0..1e6,
+                                            default 0; for tests of the bounded wait).  Results do not
+                                            depend on it. */
 #define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls
                                             receive (default 0).  A caller that runs a column range [c0, c1)
                                             passes column arrays advanced by c0 (same ldc) and the patch
@@ -727,10 +740,16 @@ int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b,
 int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b,
                                    const clmgb_soilwater_fields* f, void* stream);
 
-/* soil_water! (soil_water_movement.jl:1780) with the moisture-form method: routes to
- * soilwm_moisture_form_solve! (:1498).  ZENGDECKER_2009 -> CLMGB_ERR_UNSUPPORTED;
- * BC_AQUIFER/BC_WATERTABLE need compute_qcharge! (:1575) -> CLMGB_ERR_UNSUPPORTED
- * for AQUIFER; WATERTABLE solves but does not run compute_qcharge!. */
+/* soil_water! (soil_water_movement.jl:1780) with the moisture-form method:
+ * soilwater_moisture_form! (:1532-1601), i.e. soilwm_moisture_form_solve! (:1498) and,
+ * with the BC_WATERTABLE lower boundary (use_aquifer_layer, :707-710), compute_qcharge!
+ * (:1153-1215) over the solved state with the zeroed dwat/smp/imped rows the reference
+ * passes (:1575-1598): qcharge of every column whose water table lies within the soil
+ * column (jwt < nlevsoi) is overwritten.  ZENGDECKER_2009 -> CLMGB_ERR_UNSUPPORTED (use
+ * clmgb_soil_water_zd09); BC_AQUIFER -> CLMGB_ERR_CONFIG (soilwm_moisture_form_solve!
+ * rejects it with error(), :1502-1505).  Every entry point below that runs the moisture-form solve
+ * (column steps, their adjoints, the warm start, the sample recorder, the allocation-free
+ * solve) applies the same compute_qcharge! pass. */
 int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b,
                          const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
                          double dtime, uint32_t* col_status, void* stream);
@@ -817,8 +836,9 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b,
  * is a static device array of 16 bytes plus 4 bytes per column that every GPU
  * loading this library keeps until exit, so nc is limited to
  * CLMGB_NOALLOC_MAX_COLUMNS (larger -> CLMGB_ERR_DIMS).  All calls share that array:
- * calls that overlap on the GPU race, so issue them in order on one stream.  The
- * first call on a device looks up the array's address; make it before any stream
+ * calls that overlap on the GPU race, so issue them in order on one stream.  Each
+ * call looks up the array's address in the current context; the first call on a
+ * device also loads the library's module there, so make it before any stream
  * capture.  col_status (optional, device [nc]) receives the per-column status; there
  * is no accumulated device status word. */
 #define CLMGB_NOALLOC_MAX_COLUMNS (1 << 20)

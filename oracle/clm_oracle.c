@@ -26,6 +26,7 @@
  *   compute_effec_rootfrac_and_vert_tran_sink!  src/biogeophys/soil_water_plant_sink.jl:48-78,
  *                                     :210-245, :341-451
  *   _soilwm_moisture_form_kernel!     src/biogeophys/soil_water_movement.jl:1250-1489
+ *   compute_qcharge! after it         src/biogeophys/soil_water_movement.jl:1153-1215,1575-1598
  *   tridiagonal_solve! / _tridiag_multi_kernel!  src/infrastructure/tridiagonal.jl:35-127
  *   tridiagonal_col!                  src/biogeophys/soil_water_movement.jl:736-773
  *   init_soil_properties!             src/infrastructure/cold_start.jl:225-391
@@ -748,6 +749,9 @@ static uint32_t soiltemp_col(const st_ctx* X, int64_t c)
   const int nlev_total = nlevsno + 1 + nlevmaxurbgrnd;
   if (!f->mask_nolakec[c]) return 0;
   const int64_t snl = f->col_snl[c];
+  /* the reference indexes its level arrays with snl (a BoundsError outside
+   * -nlevsno..0); the column is reported and left untouched, as the kernels do */
+  if (snl > 0 || snl < -nlevsno) return CLMGB_COL_LEVEL_RANGE;
   const int64_t l = f->col_landunit[c] - 1;
   const int64_t it = f->col_itype[c];
   const int64_t lit = f->lun_itype[l];
@@ -3159,6 +3163,56 @@ static uint32_t moisture_form_col(const clmgb_varpar* vp, const clmgb_bounds* b,
   return status;
 }
 
+/* ===================================================================== */
+/* compute_qcharge! (soil_water_movement.jl:1153-1215) as                */
+/* soilwater_moisture_form! calls it after the solve when                */
+/* use_aquifer_layer(cfg) (:1575-1598): dwat, smp and imped are freshly  */
+/* zeroed rows, vwc_liq = smooth_max(h2osoi_liq, 1e-6)/(dz*DENH2O) on    */
+/* levels 1..min(nbedrock, nlevsoi) and zero below (:1583-1590).         */
+/* ===================================================================== */
+static void compute_qcharge_col(const clmgb_varpar* vp, const clmgb_bounds* b,
+                                const clmgb_soilwater_fields* f, double dtime, int64_t c)
+{
+  const int64_t ld = b->ldc;
+  const int nlevsoi = vp->nlevsoi, joff = vp->nlevsno, joff_zi = vp->nlevsno + 1;
+  if (!f->mask_hydrology[c]) return;
+  const int nlayers = (int)f->col_nbedrock[c];
+  if (nlayers < 1 || nlayers > nlevsoi) return;   /* not solved: CLMGB_COL_LEVEL_RANGE */
+  /* the rows the wrapper builds (:1580-1590) */
+  double dwat[ORC_MAXL + 2], smp[ORC_MAXL + 2], imped[ORC_MAXL + 2], vwc[ORC_MAXL + 2];
+  for (int j = 1; j <= nlevsoi; j++) { dwat[j] = 0.0; smp[j] = 0.0; imped[j] = 0.0; vwc[j] = 0.0; }
+  (void)dwat;
+  const int jlast = nlayers < nlevsoi ? nlayers : nlevsoi;
+  for (int j = 1; j <= jlast; j++)
+    vwc[j] = jl_max(IX(f->h2osoi_liq, c, joff + j, ld), 1.0e-6) / (IX(f->dz, c, joff + j, ld) * DENH2O);
+  /* index of the layer above the water table (:1177-1184) */
+  int jwt = nlevsoi;
+  for (int j = 1; j <= nlevsoi; j++) {
+    if (f->zwt[c] <= IX(f->zi, c, joff_zi + j, ld)) { jwt = j - 1; break; }
+  }
+  if (jwt < nlevsoi) {
+    const double wh_zwt = -IX(f->sucsat, c, jwt + 1, ld) - f->zwt[c] * M_TO_MM;
+    double s1 = jl_max(vwc[jwt + 1] / IX(f->watsat, c, jwt + 1, ld), 0.01);
+    s1 = jl_min(1.0, s1);
+    /* soil_hk! of the Clapp-Hornberger curve (swrc_clapp_hornberg.jl:43-55) */
+    const double bsw = IX(f->bsw, c, jwt + 1, ld);
+    const double ka = imped[jwt + 1] * IX(f->hksat, c, jwt + 1, ld) * cm_pow(s1, 2.0 * bsw + 3.0);
+    const int jm = jwt > 1 ? jwt : 1;
+    const double smp1 = jl_max(f->smpmin[c], smp[jm]);
+    const double wh = smp1 - IX(f->z, c, joff + jm, ld) * M_TO_MM;
+    double q;
+    if (jwt == 0)
+      q = -ka * (wh_zwt - wh) / ((f->zwt[c] + 1.0e-3) * M_TO_MM);
+    else
+      q = -ka * (wh_zwt - wh) / ((f->zwt[c] - IX(f->z, c, joff + jwt, ld)) * M_TO_MM * 2.0);
+    q = jl_max(-10.0 / dtime, q);
+    q = jl_min(10.0 / dtime, q);
+    f->qcharge[c] = q;
+  }
+}
+
+/* soilwater_moisture_form! (soil_water_movement.jl:1532-1601): the solve, then
+ * compute_qcharge! under the water-table lower boundary. */
 int orc_soil_water(const clmgb_varpar* vp, const clmgb_bounds* b,
                    const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg, double dtime,
                    uint32_t* col_status, double* cap_qin, double* cap_qout, int32_t nthreads)
@@ -3178,6 +3232,7 @@ int orc_soil_water(const clmgb_varpar* vp, const clmgb_bounds* b,
   for (int64_t c = 0; c < b->nc; c++) {
     uint32_t s = moisture_form_col(vp, b, f, cfg, dtime, c, cap);
     if (col_status) col_status[c] = s;
+    if (cfg->lower_boundary_condition == CLMGB_BC_WATERTABLE) compute_qcharge_col(vp, b, f, dtime, c);
   }
   return 0;
 }
@@ -3208,7 +3263,7 @@ void orc_apply_forcing_col(const clmgb_varpar* vp, const clmgb_bounds* b,
     int64_t p = p1 - 1;
     sabg[p] = G; sabg_soil[p] = G; sabg_snow[p] = G;
     for (int k = 1; k <= nlevsno + 1; k++) IX(sabg_lyr, p, k, ldp) = 0.0;
-    IX(sabg_lyr, p, ft->col_snl[c] + 1 + nlevsno, ldp) = G;
+    if (ft->col_snl[c] <= 0 && ft->col_snl[c] >= -nlevsno) IX(sabg_lyr, p, ft->col_snl[c] + 1 + nlevsno, ldp) = G;
   }
   ((double*)ft->forc_lwrad)[c] = SB * jl_pow4(ft->t_grnd[c]);
   ((double*)fw->qflx_infl)[c] = I;
@@ -3241,6 +3296,7 @@ int orc_run_steps(const clmgb_varpar* vp, const clmgb_bounds* b,
       s |= soiltemp_col(&X, c);
       fractions_col(vp, b, fw, c);
       s |= moisture_form_col(vp, b, fw, cfg, dtime, c, NULL);
+      if (cfg->lower_boundary_condition == CLMGB_BC_WATERTABLE) compute_qcharge_col(vp, b, fw, dtime, c);
     }
     if (col_status) col_status[c] = s;
   }

@@ -69,6 +69,7 @@ def soil_column_fixture(ncols=4):
     a["sabg_lyr"][nlevsno] = g["sabg_lyr_top"]          # Julia index nlevsno+1 = soil layer 1
     a["forc_lwrad"][:] = 300.0
     a["zwt"][:] = a["zi"][joff + vp.nlevsoi]
+    a["smpmin"][:] = -1.0e8
     if ncols >= 2:   # two snow layers (test_soil_temperature.jl:259-287)
         c = 1
         a["col_snl"][c] = -2
@@ -126,6 +127,7 @@ def moisture_fixture():
     a["sucsat"][:] = g["sucsat"]
     a["icefrac"][:] = 0.0
     a["zwt"][:] = nlev * dzv
+    a["smpmin"][:] = -1.0e8
     for j in range(1, nlev + 1):
         a["h2osoi_liq"][joff + j - 1] = (0.30 + 0.01 * j) * g["watsat"] * dzv * 1000.0
     a["qflx_infl"][:] = g["qflx_infl"]

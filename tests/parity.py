@@ -34,3 +34,17 @@ def compare(gpu, ref, rtol=1e-10, atol=1e-12, fields=None):
         if viol.any():
             bad.update(int(c) for c in np.nonzero(viol.reshape(-1, viol.shape[-1]).any(axis=0))[0])
     return rep, bad
+
+
+def bit_mismatches(gpu, ref, fields):
+    """Number of elements per field whose bits differ (NaN payloads and signed zeros
+    included) between two states; {} when every field is identical."""
+    out = {}
+    for k in fields:
+        a, b = np.ascontiguousarray(gpu[k]), np.ascontiguousarray(ref[k])
+        if a.dtype == np.float64:
+            a, b = a.view(np.uint64), b.view(np.uint64)
+        n = int(np.count_nonzero(a != b))
+        if n:
+            out[k] = n
+    return out

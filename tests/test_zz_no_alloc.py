@@ -68,3 +68,127 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     f = st.soilwater_fields()
     rc = lib.clmgb_soil_water_noalloc(C.byref(st.vp), C.byref(big), C.byref(f), C.byref(cfg), 1800.0, None, None)
     assert rc == abi.CLMGB_ERR_DIMS
+
+
+def _padded(st, ldc):
+    """The host state `st` widened to leading dimension ldc > nc (the extra columns
+    filled with a marker), for calls whose bounds say nc columns, ldc stride."""
+    from clmgb.state import ColumnState
+    arrs = {}
+    for k, a in st.arrays.items():
+        if st.spec[k][2] == "c":
+            w = np.full(a.shape[:-1] + (ldc,), 7 if a.dtype != np.float64 else -7.25, dtype=a.dtype)
+            w[..., :st.nc] = a
+            arrs[k] = w
+        else:
+            arrs[k] = a.copy()
+    return ColumnState(st.vp, ldc, st.np, st.nl, arrs)
+
+
+@pytest.mark.parametrize("lower_bc", [abi.BC_ZERO_FLUX, abi.BC_FLUX, abi.BC_WATERTABLE])
+def test_noalloc_matches_oracle_under_each_lower_boundary(lower_bc):
+    """Against the CPU oracle (soilwater_moisture_form!, compute_qcharge! included),
+    bit for bit, with masked columns, ragged bedrock, water tables from the surface to
+    below the column, and a leading dimension larger than the column count."""
+    wl = synth.make_workload(2, nc=6000, seed=77)
+    st = wl.state
+    from oracle import oracle as orc
+    from parity import bit_mismatches
+    orc.soil_water_fractions(st)
+    st["mask_hydrology"][::7] = 0
+    st["col_nbedrock"][:] = 5 + np.arange(st.nc) % (st.vp.nlevsoi - 4)
+    st["zwt"][:] = np.linspace(0.0, 12.0, st.nc)
+    cfg = abi.SwmConfig.clm5_default()
+    cfg.lower_boundary_condition = lower_bc
+    ref = st.copy()
+    assert np.all(orc.soil_water(ref, wl.dtime, cfg) == 0)
+    ldc = st.nc + 37
+    pad = _padded(st, ldc).to_device()
+    lib = api.load()
+    b = abi.Bounds(st.nc, st.np, st.nl, ldc, st.np)
+    f = pad.soilwater_fields()
+    status = torch.full((ldc,), 9, dtype=torch.int32, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = lib.clmgb_soil_water_noalloc(C.byref(st.vp), C.byref(b), C.byref(f), C.byref(cfg), float(wl.dtime),
+                                      C.c_void_p(status.data_ptr()), stream)
+    assert rc == abi.CLMGB_OK
+    torch.cuda.synchronize()
+    got = pad.to_host()
+    cut = {k: got[k][..., :st.nc] for k in FIELDS}
+    assert not bit_mismatches(cut, ref, FIELDS)
+    s = status.cpu().numpy()
+    assert np.all(s[:st.nc] == 0) and np.all(s[st.nc:] == 9)
+    for k in FIELDS:                      # the padding is never touched
+        assert np.all(got[k][..., st.nc:] == -7.25)
+
+
+def test_noalloc_more_columns_than_threads_and_two_calls():
+    """More columns than the solve kernel has threads (each lane takes many columns
+    from the queue), ldc > nc, two calls in a row: the handle entry point's bits."""
+    nc = 400_000
+    wl = synth.make_workload(0, nc=nc, seed=5)
+    st = wl.state
+    st["mask_hydrology"][::17] = 0
+    cfg = abi.SwmConfig.clm5_default()
+    ldc = nc + 5
+    a = _padded(st, ldc).to_device()
+    bdev = _padded(st, ldc).to_device()
+    h = api.Handle(st.vp)
+    b = abi.Bounds(nc, st.np, st.nl, ldc, st.np)
+    from parity import bit_mismatches
+    for call in range(2):
+        for s_ in (a, bdev):
+            f = s_.soilwater_fields()
+            api.check(h.lib.clmgb_soil_water_fractions(h.h, C.byref(b), C.byref(f), None), "fractions")
+        fa = a.soilwater_fields()
+        api.check(h.lib.clmgb_soil_water(h.h, C.byref(b), C.byref(fa), C.byref(cfg), float(wl.dtime), None, None),
+                  "soil_water")
+        fb = bdev.soilwater_fields()
+        rc = h.lib.clmgb_soil_water_noalloc(C.byref(st.vp), C.byref(b), C.byref(fb), C.byref(cfg),
+                                            float(wl.dtime), None, None)
+        assert rc == abi.CLMGB_OK
+        torch.cuda.synchronize()
+        ga, gb = a.to_host(), bdev.to_host()
+        assert not bit_mismatches(gb, ga, FIELDS), call
+    h.close()
+
+
+def test_noalloc_under_stream_capture():
+    """After a first call (which loads the module), the call is captured into a CUDA
+    graph by torch.cuda.graph and replayed: the replay gives the eager call's bits."""
+    wl = synth.make_workload(1, nc=5000, seed=19)
+    st = wl.state
+    cfg = abi.SwmConfig.clm5_default()
+    lib = api.load()
+    eager = st.to_device()
+    status = torch.zeros(st.nc, dtype=torch.int32, device="cuda")
+    assert _noalloc(lib, eager, cfg, wl.dtime, status) == abi.CLMGB_OK      # first call, outside capture
+    torch.cuda.synchronize()
+    want = eager.to_host()
+    cap = st.to_device()
+    start = st.to_device()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            rc = _noalloc(lib, cap, cfg, wl.dtime, status)
+    assert rc == abi.CLMGB_OK
+    torch.cuda.current_stream().wait_stream(s)
+    for k in cap.arrays:              # the graph advances `cap` from the eager run's start state
+        cap[k].copy_(start[k])
+    g.replay()
+    torch.cuda.synchronize()
+    from parity import bit_mismatches
+    assert not bit_mismatches(cap.to_host(), want, FIELDS)
+
+
+def test_noalloc_rejects_the_aquifer_boundary():
+    st = synth.make_workload(0, nc=64).state.to_device()
+    lib = api.load()
+    cfg = abi.SwmConfig.clm5_default()
+    cfg.lower_boundary_condition = abi.BC_AQUIFER
+    f = st.soilwater_fields()
+    b = st.bounds()
+    rc = lib.clmgb_soil_water_noalloc(C.byref(st.vp), C.byref(b), C.byref(f), C.byref(cfg), 1800.0, None, None)
+    assert rc == abi.CLMGB_ERR_CONFIG
