@@ -147,9 +147,9 @@ __device__ __forceinline__ AD cm_pow(const AD& x, const AD& y) {
   const double py = (y.i >= 0 && x.v > 0.0) ? r * ::cm_log(x.v) : 0.0;
   return ad_binary(r, x, px, y, py);
 }
-// x^y for a constant base x with lx = log x formed by the caller: d/dy = r lx
-__device__ __forceinline__ AD cm_pow_lx(double x, double lx, const AD& y) {
-  const double r = ::cm_pow_lx(x, lx, y.v);
+// x^y for a constant base x with log x = lx + lxl formed by the caller: d/dy = r lx
+__device__ __forceinline__ AD cm_pow_lx(double x, double lx, double lxl, const AD& y) {
+  const double r = ::cm_pow_lx(x, lx, lxl, y.v);
   return ad_unary(r, y, r * lx);
 }
 __device__ __forceinline__ AD cm_log10(const AD& x) {

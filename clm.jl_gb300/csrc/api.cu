@@ -829,7 +829,7 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       h->poll_limit = value;
       return CLMGB_OK;
     case CLMGB_OPT_QUEUE_PUBLISH_DELAY:
-      if (value < 0 || value > 1000000) return CLMGB_ERR_CONFIG;
+      if (value < 0 || value > 10000000) return CLMGB_ERR_CONFIG;
       h->publish_delay = value;
       return CLMGB_OK;
     default:

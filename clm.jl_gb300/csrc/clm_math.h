@@ -9,15 +9,24 @@
 // Every operation is an IEEE-754 binary64 add, multiply or fused multiply-add
 // written out explicitly (CUDA: __dadd_rn/__dmul_rn/__fma_rn; C: +, *, fma() built
 // with -ffp-contract=off), so a C build and a CUDA build return the same bits.  On
-// GB300, whose FP64 pipe issues about 1.9 FMA/clk/SM, a pow() here costs ~30 FP64
+// GB300, whose FP64 pipe issues about 1.9 FMA/clk/SM, a pow() here costs about 50 FP64
 // instructions; exponent and table-index handling use the integer pipes.
+//
+// pow and log10 go through a double-double logarithm (cm_log_dd: Tang's table with an
+// extra-precision log(c) and an exactly formed reduced argument, the error-free sums
+// written out) and an exponential of a double-double argument (cm_exp_dd, 256-entry
+// table in two parts), so y*log(x) keeps about 2^-67 of absolute accuracy and the
+// result is rounded once at the end: nearly always the correctly rounded value, as
+// Julia's own Float64 ^ (base/math.jl, double-double log and exp) nearly always is.
+// Integral y in [-4096, 24576] takes Julia's compensated power by squaring instead
+// (Base.Math.pow_body(x::Float64, n::Integer)), as Julia's ^ does.
 //
 // Accuracy (tests/test_math.py checks these against 200-bit mpmath):
 //   cm_log:           absolute error below 1 ulp of max(1, |result|)
-//   cm_log10:         absolute error below 2.5 ulp of max(1, |result|)
+//   cm_log10:         below 0.51 ulp of max(2^-10, |result|) (double-double log)
 //   cm_exp:           relative error below 2 ulp
-//   cm_pow(x, y):     relative error below (3 + |y| + |y*log(x)|) ulp (the product y*log(x)
-//                     is formed in binary64; at most ~3e-14 over the ranges the solve uses)
+//   cm_pow(x, y):     relative error below 0.51 ulp off the integral-y path (below 1 ulp on it);
+//                     the correctly rounded value in all but a few in 10^4 random cases
 //   cm_sin:           error below 1 ulp of max(|result|, 2^-53 |x|) for |x| < 2^20 pi/2
 //   cm_acos:          error below 1.5 ulp on [-1, 1]
 //                     (Cody-Waite reduction; the 2^-53 |x| term covers x near multiples of pi)
@@ -33,6 +42,8 @@
 #define CM_ADD(a, b) __dadd_rn((a), (b))
 #define CM_SUB(a, b) __dsub_rn((a), (b))
 #define CM_SQRT(a) __dsqrt_rn(a)
+#define CM_DIV(a, b) __ddiv_rn((a), (b))
+#define CM_ISFINITE(x) isfinite(x)
 #define CM_AS_U64(x) ((uint64_t)__double_as_longlong(x))
 #define CM_AS_F64(u) __longlong_as_double((long long)(u))
 #define CM_INF __longlong_as_double(0x7ff0000000000000LL)
@@ -49,6 +60,8 @@
 #define CM_ADD(a, b) ((a) + (b))
 #define CM_SUB(a, b) ((a) - (b))
 #define CM_SQRT(a) sqrt(a)
+#define CM_DIV(a, b) ((a) / (b))
+#define CM_ISFINITE(x) isfinite(x)
 static inline uint64_t cm_as_u64_(double x) { uint64_t u; memcpy(&u, &x, 8); return u; }
 static inline double cm_as_f64_(uint64_t u) { double x; memcpy(&x, &u, 8); return x; }
 #define CM_AS_U64(x) cm_as_u64_(x)
@@ -122,44 +135,184 @@ CM_FN double cm_exp(double x) {
   return CM_MUL(CM_AS_F64(CM_AS_U64(res) + ((uint64_t)(n + 1000) << 52)), 0x1p-1000);
 }
 
-// x^y (Julia Base ^ for Float64 arguments).  The tests of the common case look at
-// the bit patterns (integer pipes): y == +-0, x == 1, x or y NaN, 0 < x < Inf.
+// log(x) = hi + *lo (returned: hi) for a positive finite x, subnormals included:
+// |hi + lo - log(x)| below about 2^-67 max(1, |log x|), and below 2^-67 |log x| near 1.
+// x = 2^k z, z in [0.75, 1.5); log(x) = k ln2 + log(1/invc) + log1p(r), r = z*invc - 1
+// formed exactly by one fma (the table's invc has few fractional bits), |r| < 2^-7.
+CM_FN double cm_log_dd(double x, double* lo_out) {
+  uint64_t ix = CM_AS_U64(x);
+  if (ix < 0x0010000000000000ULL) ix = CM_AS_U64(CM_MUL(x, 0x1p54)) - (54ULL << 52);   // subnormal
+  const uint64_t tmp = ix - 0x3fe8000000000000ULL;
+  const int i = (int)((tmp >> 45) & 127);
+  const int64_t k = ((int64_t)tmp) >> 52;
+  const double z = CM_AS_F64(ix - (tmp & 0xfff0000000000000ULL));
+  const double invc = CM_LD(CM_LOGD_INVC[i]);
+  const double lch = CM_LD(CM_LOGD_HI[i]);
+  const double lcl = CM_LD(CM_LOGD_LO[i]);
+  const double r = CM_FMA(z, invc, -1.0);                    // exact
+  const double kd = (double)k;
+  const double t1 = CM_FMA(kd, CM_LN2_HI, lch);              // exact: multiples of 2^-42 below 2^10
+  // s + e = t1 + r exactly (Dekker's Fast2Sum: |t1| >= |r| or t1 == 0, checked by the
+  // table generator for every interval)
+  const double s = CM_ADD(t1, r);
+  const double e = CM_SUB(r, CM_SUB(s, t1));
+  // -r^2/2 = ar2 + e3 exactly
+  const double ar = CM_MUL(-0.5, r);
+  const double ar2 = CM_MUL(ar, r);
+  const double e3 = CM_FMA(ar, r, -ar2);
+  // hi + e2 = s + ar2 exactly (|s| >= |ar2|)
+  const double hi = CM_ADD(s, ar2);
+  const double e2 = CM_ADD(CM_SUB(s, hi), ar2);
+  // r^3 (1/3 - r/4 + ... + r^6/9), truncation below 2^-70
+  double p = CM_FMA(r, CM_LOGD_C9, CM_LOGD_C8);
+  p = CM_FMA(r, p, CM_LOGD_C7);
+  p = CM_FMA(r, p, CM_LOGD_C6);
+  p = CM_FMA(r, p, CM_LOGD_C5);
+  p = CM_FMA(r, p, CM_LOGD_C4);
+  p = CM_FMA(r, p, CM_LOGD_C3);
+  const double r3 = CM_MUL(CM_MUL(r, r), r);
+  const double lo = CM_ADD(CM_ADD(CM_FMA(kd, CM_LN2_LO, lcl), e), CM_FMA(r3, p, CM_ADD(e2, e3)));
+  const double y = CM_ADD(hi, lo);
+  *lo_out = CM_ADD(CM_SUB(hi, y), lo);
+  return y;
+}
+
+// exp(x + xl) for |xl| <= ulp(x): the value before the final rounding is within about
+// 2^-61 relative; x = k ln2/256 + r with k*hi exact, 2^(j/256) = t_hi + t_lo, expm1(r)
+// by its Taylor series to r^5 on |r| <= ln2/512.
+CM_FN double cm_exp_dd(double x, double xl) {
+  const uint64_t ix = CM_AS_U64(x);
+  const uint32_t top = (uint32_t)(ix >> 52) & 0x7ffu;
+  if (top - 0x3c9u >= 0x408u - 0x3c9u) {                   // |x| < 2^-54 or |x| >= 512 or NaN/Inf
+    if (top < 0x3c9u) return CM_ADD(1.0, x);
+    if (x != x) return x;
+    if (x > 709.782712893383973096) return CM_INF;
+    if (x < -745.1332191019412076235) return 0.0;
+  }
+  const double shift = 0x1.8p52;
+  double kd = CM_ADD(CM_MUL(CM_EXPD_INVLN2N, x), shift);
+  const int64_t kk = (int64_t)(CM_AS_U64(kd) - 0x4338000000000000ULL);   // round(x*256/ln2)
+  kd = CM_SUB(kd, shift);
+  double r = CM_FMA(-kd, CM_EXPD_LN2N_HI, x);               // exact
+  r = CM_FMA(-kd, CM_EXPD_LN2N_LO, r);
+  r = CM_ADD(r, xl);
+  const int j = (int)(kk & 255);
+  const int64_t n = kk >> 8;                                // floor(kk / 256)
+  const double th = CM_LD(CM_EXPD_THI[j]);
+  const double tl = CM_LD(CM_EXPD_TLO[j]);
+  double q = CM_FMA(r, CM_EXPD_C5, CM_EXPD_C4);
+  q = CM_FMA(r, q, CM_EXPD_C3);
+  q = CM_FMA(r, q, CM_EXPD_C2);
+  const double pm = CM_FMA(CM_MUL(r, r), q, r);             // expm1(r)
+  const double res = CM_ADD(th, CM_FMA(th, pm, tl));        // 2^(j/256) exp(r), in [0.99, 2.01)
+  if (n >= -1020 && n <= 1020) return CM_AS_F64(CM_AS_U64(res) + ((uint64_t)n << 52));
+  if (n > 0) return CM_MUL(CM_AS_F64(CM_AS_U64(res) + ((uint64_t)(n - 3) << 52)), 8.0);
+  return CM_MUL(CM_AS_F64(CM_AS_U64(res) + ((uint64_t)(n + 1000) << 52)), 0x1p-1000);
+}
+
+// Julia's x^n for an integer n (Base.Math.pow_body(x::Float64, n::Integer)): power by
+// squaring with the products' rounding errors carried in a second word.
+CM_FN double jl_pow_int(double x, int64_t n) {
+  double y = 1.0, xnlo = 0.0, ynlo = 0.0;
+  if (n == 3) return CM_MUL(CM_MUL(x, x), x);
+  if (n < 0) {
+    const double rx = CM_DIV(1.0, x);
+    if (n == -2) return CM_MUL(rx, rx);
+    if (CM_ISFINITE(x)) xnlo = CM_MUL(-CM_FMA(x, rx, -1.0), rx);
+    x = rx;
+    n = -n;
+  }
+  while (n > 1) {
+    if (n & 1) {
+      const double err = CM_FMA(y, xnlo, CM_MUL(x, ynlo));
+      const double yh = CM_MUL(x, y);
+      ynlo = CM_ADD(CM_FMA(x, y, -yh), err);
+      y = yh;
+    }
+    const double err = CM_MUL(CM_MUL(x, 2.0), xnlo);
+    const double xh = CM_MUL(x, x);
+    xnlo = CM_ADD(CM_FMA(x, x, -xh), err);
+    x = xh;
+    n >>= 1;
+  }
+  const double err = CM_FMA(y, xnlo, CM_MUL(x, ynlo));
+  if (CM_ISFINITE(x) && CM_ISFINITE(err)) return CM_FMA(x, y, err);
+  return CM_MUL(x, y);
+}
+
+// Integral y in Julia's power-by-squaring range (Base.Math.use_power_by_squaring)
+CM_FN bool cm_pow_by_squaring(double y, int64_t* n) {
+  const double ay = y < 0.0 ? -y : y;
+  if (!(ay <= 24576.0)) return false;
+  const int64_t m = (int64_t)y;
+  if ((double)m != y || m < -4096) return false;
+  *n = m;
+  return true;
+}
+
+// x^y with Julia Base's rules for Float64 (base/math.jl `^`): x == 1 -> 1; y NaN ->
+// NaN; y integral in [-4096, 24576] -> compensated power by squaring (y == 0 -> 1);
+// x == 0 -> 0 or Inf; x < 0 with non-integral y -> NaN (Julia raises a DomainError);
+// otherwise exp(y log x) in double-double.  The tests of the common case look at bit
+// patterns (integer pipes).
 CM_FN double cm_pow(double x, double y) {
   const uint64_t ux = CM_AS_U64(x), uy = CM_AS_U64(y);
-  if ((uy << 1) == 0) return 1.0;
   if (ux == 0x3ff0000000000000ULL) return 1.0;
-  if ((ux << 1) > 0xffe0000000000000ULL || (uy << 1) > 0xffe0000000000000ULL) return CM_ADD(x, y);
-  if (ux - 1 < 0x7fefffffffffffffULL) return cm_exp(CM_MUL(y, cm_log(x)));
+  if ((uy << 1) > 0xffe0000000000000ULL) return y;          // y NaN
+  int64_t n;
+  if (cm_pow_by_squaring(y, &n)) return n == 0 ? 1.0 : jl_pow_int(x, n);
+  if ((ux << 1) == 0) return y > 0.0 ? 0.0 : CM_INF;       // x = +-0
+  bool neg = false;
   const double ay = y < 0.0 ? -y : y;
-  const bool yint = (ay < 0x1p53) ? ((double)(int64_t)ay == ay) : true;
-  const bool yodd = yint && ay < 0x1p53 && (((int64_t)ay) & 1);
-  if (x == 0.0) {
-    const bool neg = (CM_AS_U64(x) >> 63) && yodd;
-    const double v = y > 0.0 ? 0.0 : CM_INF;
+  if (ux >> 63) {                                           // x < 0 (or -NaN)
+    if (x != x) return x;
+    const bool yint = ay >= 0x1p53 || (double)(int64_t)y == y;
+    if (!yint) return CM_NAN;
+    neg = ay < 0x1p53 && ((int64_t)y & 1);
+    x = -x;
+  }
+  if (x != x) return x;
+  if (x == CM_INF) {
+    const double v = y > 0.0 ? CM_INF : 0.0;
     return neg ? -v : v;
   }
-  if (x == CM_INF) return y > 0.0 ? CM_INF : 0.0;
-  if (x == -CM_INF) {
-    const double v = y > 0.0 ? CM_INF : 0.0;
-    return yodd ? -v : v;
-  }
-  // x < 0: defined for integer y only
-  if (!yint) return CM_NAN;
-  const double v = cm_exp(CM_MUL(y, cm_log(-x)));
-  return yodd ? -v : v;
+  double lxl;
+  const double lxh = cm_log_dd(x, &lxl);
+  const double eh = CM_MUL(y, lxh);
+  const double el = CM_FMA(y, lxl, CM_FMA(y, lxh, -eh));
+  const double v = cm_exp_dd(eh, el);
+  return neg ? -v : v;
 }
 
-// x^y for a positive finite x other than 1 whose logarithm lx = cm_log(x) the caller
-// formed once: the value of cm_pow(x, y) for every y, without forming cm_log(x) again.
-CM_FN double cm_pow_lx(double x, double lx, double y) {
+// x^y for a positive finite x other than 1 whose logarithm lxh + lxl = cm_log_dd(x) the
+// caller formed once: the value of cm_pow(x, y) for every y, without forming the
+// logarithm again.
+CM_FN double cm_pow_lx(double x, double lxh, double lxl, double y) {
   const uint64_t uy = CM_AS_U64(y);
-  if ((uy << 1) == 0) return 1.0;
-  if ((uy << 1) > 0xffe0000000000000ULL) return CM_ADD(x, y);
-  return cm_exp(CM_MUL(y, lx));
+  if ((uy << 1) > 0xffe0000000000000ULL) return y;
+  int64_t n;
+  if (cm_pow_by_squaring(y, &n)) return n == 0 ? 1.0 : jl_pow_int(x, n);
+  const double eh = CM_MUL(y, lxh);
+  const double el = CM_FMA(y, lxl, CM_FMA(y, lxh, -eh));
+  return cm_exp_dd(eh, el);
 }
 
-// Base-10 logarithm.
-CM_FN double cm_log10(double x) { return CM_MUL(cm_log(x), CM_INVLN10); }
+// Base-10 logarithm: the double-double log times 1/ln10 in two parts.
+CM_FN double cm_log10(double x) {
+  const uint64_t ix = CM_AS_U64(x);
+  if (ix - 0x0010000000000000ULL >= 0x7ff0000000000000ULL - 0x0010000000000000ULL) {
+    if (x != x) return x;                                   // NaN
+    if ((ix << 1) == 0) return -CM_INF;                     // +-0
+    if (ix >> 63) return CM_NAN;                            // negative
+    if (ix == 0x7ff0000000000000ULL) return x;              // +Inf
+  }
+  if (ix == 0x3ff0000000000000ULL) return 0.0;
+  double l;
+  const double h = cm_log_dd(x, &l);
+  const double v = CM_MUL(h, CM_INVLN10_HI);
+  const double vl = CM_ADD(CM_FMA(h, CM_INVLN10_HI, -v), CM_FMA(h, CM_INVLN10_LO, CM_MUL(l, CM_INVLN10_HI)));
+  return CM_ADD(v, vl);
+}
 
 // sin and cos of a reduced argument r + lo, |r| <= pi/4, |lo| <= ulp(r) (Taylor
 // polynomials in r^2; lo enters to first order: sin' = cos ~ 1 - r^2/2, cos' = -sin ~ -r).

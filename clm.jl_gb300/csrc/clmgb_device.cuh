@@ -580,7 +580,8 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
 
   // ---- soil_therm_prop!: layer conductivity thk (_soil_snow_tk_kernel! :647-716) ----
   // the logarithms of the two constant bases of tkwat^x and tkice^x, formed once
-  const double ln_tkwat = cm_log(TKWAT), ln_tkice = cm_log(TKICE);
+  double ln_tkwat_lo, ln_tkice_lo;
+  const double ln_tkwat = cm_log_dd(TKWAT, &ln_tkwat_lo), ln_tkice = cm_log_dd(TKICE, &ln_tkice_lo);
   // thk kept in tk[] first, interface conductivity computed in place afterwards.
   for (int jj = jjtop; jj <= nlev; jj++) {
     tt[jj] = X.T(jj);
@@ -608,7 +609,8 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
             const S fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
             const S fl = a1 / fl_denom;
             const S dksat =
-                LVc(f.tkmg, c, j, ld) * cm_pow_lx(TKWAT, ln_tkwat, fl * ws) * cm_pow_lx(TKICE, ln_tkice, (1.0 - fl) * ws);
+                LVc(f.tkmg, c, j, ld) * cm_pow_lx(TKWAT, ln_tkwat, ln_tkwat_lo, fl * ws) *
+                cm_pow_lx(TKICE, ln_tkice, ln_tkice_lo, (1.0 - fl) * ws);
             thkv = dke * dksat + (1.0 - dke) * LVc(f.tkdry, c, j, ld);
           } else {
             thkv = LVc(f.tkdry, c, j, ld);
@@ -968,9 +970,10 @@ constexpr int LOG_FIN = 3 * MAXSOI + 3;
 // layer), as formed at soil_water_movement.jl:1287-1293.
 template <class ST>
 __device__ __forceinline__ typename ST::S mf_impedance(double e_ice, int j, int nlayers, ST& X) {
-  const double ln10 = cm_log(10.0);
-  if (j == nlayers) return cm_pow_lx(10.0, ln10, -e_ice * X.Icefrac(j));
-  return cm_pow_lx(10.0, ln10, -e_ice * (0.5 * (X.Icefrac(j) + X.Icefrac(j + 1))));
+  double ln10_lo;
+  const double ln10 = cm_log_dd(10.0, &ln10_lo);
+  if (j == nlayers) return cm_pow_lx(10.0, ln10, ln10_lo, -e_ice * X.Icefrac(j));
+  return cm_pow_lx(10.0, ln10, ln10_lo, -e_ice * (0.5 * (X.Icefrac(j) + X.Icefrac(j + 1))));
 }
 __device__ __forceinline__ double mf_impedance(const Dims& D, const clmgb_soilwater_fields& f, double e_ice,
                                                int64_t c, int j, int nlayers) {

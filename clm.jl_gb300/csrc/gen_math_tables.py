@@ -25,7 +25,23 @@ quotient that pi/180.0 gives.
 acos: asin's Taylor series on [0, 1/2] (27 terms), with acos(x) = pi/2 - asin(x) for
 |x| <= 1/2 and acos(x) = 2 asin(sqrt((1-x)/2)), pi - 2 asin(sqrt((1+x)/2)) beyond;
 pi and pi/2 in two parts.
+
+Double-double log for pow and log10 (Tang's method with an extra-precision table):
+the same 128 intervals as the log table.  invc_i is the binary64 nearest 1/c_i among
+numbers with few fractional bits, chosen so that r = z*invc_i - 1 is exactly
+representable for every z of the interval (a single fma forms it with no rounding);
+the generator checks this at both ends of every interval (r is monotonic in z).  The
+two intervals next to 1 use invc = 1, so r = z - 1 and log near 1 keeps its relative
+accuracy.  -log(invc_i) = logc_hi + logc_lo with logc_hi a multiple of 2^-42 (so
+k*ln2_hi + logc_hi is exact for |k| < 2^11), and |logc_hi| >= |r| on its interval
+(checked), so adding r to it is error-free by Fast2Sum.  |r| < 2^-7 everywhere; log1p(r) is its
+Taylor series to r^9 (truncation below 2^-70).
+
+exp of a double-double argument (N = 256): 2^(j/256) = t_hi + t_lo (t_hi = RN, t_lo =
+RN of the rest), ln2/256 = hi + lo with 33-bit hi (k*hi exact for |k| < 2^20), and
+expm1 on |r| <= ln2/512 by its Taylor series to r^5 (truncation below 2^-66).
 """
+from fractions import Fraction
 import mpmath as mp
 
 mp.mp.prec = 200
@@ -100,6 +116,8 @@ def main():
     for k in range(1, 28):
         a = mp.factorial(2 * k) / (mp.mpf(4) ** k * mp.factorial(k) ** 2 * (2 * k + 1))
         lines.append("#define CM_ASIN_A%d (%s)" % (k, hexd(a)))
+    lines += logd_tables()
+    lines += expd_tables()
     pi_hi = float(mp.pi)
     lines.append("#define CM_PI_HI (%s)" % hexd(pi_hi))
     lines.append("#define CM_PI_LO (%s)" % hexd(mp.pi - mp.mpf(pi_hi)))
@@ -107,6 +125,93 @@ def main():
     lines.append("#define CM_PIO2_H (%s)" % hexd(p2))
     lines.append("#define CM_PIO2_L (%s)" % hexd(mp.pi / 2 - mp.mpf(p2)))
     print("\n".join(lines))
+
+
+def _interval(i):
+    """The z range [lo, hi) of log interval i and the ulp of its z values."""
+    if i < 64:
+        lo = Fraction(3, 4) + Fraction(i, 256)
+        return lo, lo + Fraction(1, 256), Fraction(1, 2 ** 53)
+    lo = Fraction(1) + Fraction(i - 64, 128)
+    return lo, lo + Fraction(1, 128), Fraction(1, 2 ** 52)
+
+
+def _r_exact_all(zlo, zlast, u, invc):
+    """True when z*invc - 1 is a binary64 number for every binary64 z in [zlo, zlast]
+    (spacing u).  z*invc - 1 is a multiple of u/den(invc) (den a power of two) and its
+    magnitude is largest at an end of the interval, so it suffices that the largest
+    magnitude is below 2^53 such multiples."""
+    step = u / invc.denominator
+    rmax = max(abs(zlo * invc - 1), abs(zlast * invc - 1))
+    return rmax / step < 2 ** 53
+
+
+def logd_tables():
+    out = []
+    invc_l, hi_l, lo_l = [], [], []
+    rmax = Fraction(0)
+    for i in range(128):
+        zlo, zhi, u = _interval(i)
+        zlast = zhi - u
+        if i in (63, 64):
+            invc = Fraction(1)
+        else:
+            c = (zlo + zhi) / 2
+            invc = None
+            for fb in range(40, 4, -1):          # fractional bits of invc, most first
+                cand = Fraction(round(Fraction(2 ** fb) / c), 2 ** fb)
+                if _r_exact_all(zlo, zlast, u, cand):
+                    invc = cand
+                    break
+            assert invc is not None, i
+        rm = max(abs(zlo * invc - 1), abs(zlast * invc - 1))
+        rmax = max(rmax, rm)
+        iv = float(invc)
+        assert Fraction(iv) == invc
+        lg = -mp.log(mp.mpf(iv))
+        hi = float(mp.nint(lg * mp.mpf(2) ** 42) / mp.mpf(2) ** 42)
+        lo = float(lg - mp.mpf(hi))
+        invc_l.append(iv)
+        hi_l.append(hi)
+        lo_l.append(lo)
+        # k*ln2_hi + logc_hi + r is summed error-free by Fast2Sum, which needs
+        # |logc_hi| >= |r| whenever logc_hi != 0 (for k != 0, |k ln2_hi + logc_hi| > 0.28)
+        assert hi == 0.0 or abs(hi) >= float(rm), (i, hi, float(rm))
+    assert rmax < Fraction(1, 128), float(rmax)
+    for name, vals in (("CM_LOGD_INVC", invc_l), ("CM_LOGD_HI", hi_l), ("CM_LOGD_LO", lo_l)):
+        out.append("CM_TABLE(%s, 128) = {" % name)
+        out += ["  %s," % hexd(v) for v in vals]
+        out.append("};")
+    out.append("// max |r| over the intervals: %.6g" % float(rmax))
+    for n in range(3, 10):      # log1p(r) = r - r^2/2 + sum_{n>=3} (-1)^(n+1) r^n / n
+        out.append("#define CM_LOGD_C%d (%s)" % (n, hexd(mp.mpf((-1) ** (n + 1)) / n)))
+    ln10 = mp.log(10)
+    ih = float(1 / ln10)
+    out.append("#define CM_INVLN10_HI (%s)" % hexd(ih))
+    out.append("#define CM_INVLN10_LO (%s)" % hexd(1 / ln10 - mp.mpf(ih)))
+    return out
+
+
+def expd_tables():
+    out = []
+    th, tl = [], []
+    for j in range(256):
+        v = mp.mpf(2) ** (mp.mpf(j) / 256)
+        h = float(v)
+        th.append(h)
+        tl.append(float(v - mp.mpf(h)))
+    for name, vals in (("CM_EXPD_THI", th), ("CM_EXPD_TLO", tl)):
+        out.append("CM_TABLE(%s, 256) = {" % name)
+        out += ["  %s," % hexd(v) for v in vals]
+        out.append("};")
+    ln2n = mp.log(2) / 256
+    hi = round_bits(ln2n, 33)
+    out.append("#define CM_EXPD_LN2N_HI (%s)" % hexd(hi))
+    out.append("#define CM_EXPD_LN2N_LO (%s)" % hexd(ln2n - mp.mpf(hi)))
+    out.append("#define CM_EXPD_INVLN2N (%s)" % hexd(256 / mp.log(2)))
+    for n in range(2, 6):
+        out.append("#define CM_EXPD_C%d (%s)" % (n, hexd(1 / mp.factorial(n))))
+    return out
 
 
 if __name__ == "__main__":

@@ -38,8 +38,8 @@ struct QueueScratch {
   uint32_t* d_list;
   unsigned long long* d_count;
   // polls of a list slot whose index is still on its way before the drain gives the
-  // slot back (CLMGB_OPT_QUEUE_POLL_LIMIT), and a delay in ns between a deferral's
-  // claim of an even slot and its publication (CLMGB_OPT_QUEUE_PUBLISH_DELAY, 0 in
+  // slot back (CLMGB_OPT_QUEUE_POLL_LIMIT), and a delay in ns between the publication
+  // of an even slot and the write of its index (CLMGB_OPT_QUEUE_PUBLISH_DELAY, 0 in
   // production: it lets a test make that wait run out)
   int poll_limit = DEFER_POLL_LIMIT;
   int publish_delay = 0;

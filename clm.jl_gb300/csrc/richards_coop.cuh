@@ -38,13 +38,25 @@ __device__ __forceinline__ bool coop_defer(const LT& L, const QueueScratch& qs) 
   qs.d_qc[c] = L.qc;
   qs.d_nsub[c] = L.nsub;
   qs.d_status[c] = L.status;
-  // test hook: even slots publish late (bounded, <= 1 ms), so later slots overtake them
-  if ((slot & 1ULL) == 0)
-    for (int t = 0; t < qs.publish_delay; t += 500) __nanosleep(500);
   __threadfence();
+  // test hook (CLMGB_OPT_QUEUE_PUBLISH_DELAY): an even slot is counted published before
+  // its index is written; the lane then sleeps until a finishing warp has taken the slot
+  // (or publish_delay ns have passed, <= 10 ms) and 2 us more, so that warp finds the
+  // slot empty
+  const bool late = qs.publish_delay > 0 && (slot & 1ULL) == 0;
+  if (late) {
+    atomicAdd(qs.d_count + 1, 1ULL);
+    for (int t = 0; t < qs.publish_delay; t += 500) {
+      if (*(volatile unsigned long long*)(qs.d_count + 2) > slot) {
+        __nanosleep(2000);
+        break;
+      }
+      __nanosleep(500);
+    }
+  }
   const uint32_t prev = atomicCAS(qs.d_list + slot, DEFER_EMPTY, (uint32_t)c);
   __threadfence();
-  atomicAdd(qs.d_count + 1, 1ULL);   // published (a slot given back counts too)
+  if (!late) atomicAdd(qs.d_count + 1, 1ULL);   // published (a slot given back counts too)
   return prev == DEFER_EMPTY;
 }
 
@@ -281,8 +293,13 @@ __device__ __forceinline__ void coop_drain(const Dims& D, const clmgb_soilwater_
   const int lane = threadIdx.x & 31;
   unsigned long long* published = qs.d_count + 1;
   unsigned long long* consumed = qs.d_count + 2;
+  // test hook (CLMGB_OPT_QUEUE_PUBLISH_DELAY > 0): a warp with nothing to take keeps
+  // looking for up to that many ns, so that it is there to take a slot published before
+  // its index; 0 in production (the warp leaves at once)
+  int linger = qs.publish_delay;
   for (;;) {
     long long got = -1;
+    int pending = 0;
     if (lane == 0) {
       unsigned long long k = *(volatile unsigned long long*)consumed;
       for (;;) {
@@ -295,9 +312,16 @@ __device__ __forceinline__ void coop_drain(const Dims& D, const clmgb_soilwater_
         }
         k = old;
       }
+      if (got < 0 && linger > 0) pending = 1;
     }
     got = __shfl_sync(COOP_FULL, got, 0);
-    if (got < 0) return;
+    pending = __shfl_sync(COOP_FULL, pending, 0);
+    if (got < 0) {
+      if (!pending) return;
+      __nanosleep(500);
+      linger -= 500;
+      continue;
+    }
     uint32_t cidx = DEFER_EMPTY;
     if (lane == 0) {
       for (int it = 0; it < qs.poll_limit; it++) {

@@ -700,10 +700,12 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
 #define CLMGB_OPT_QUEUE_POLL_LIMIT    19 /* polls of a deferred column's list slot before the finishing warp
                                             gives the slot back to the deferring lane (0..2^20, default
                                             2^20).  Results do not depend on it. */
-#define CLMGB_OPT_QUEUE_PUBLISH_DELAY 20 /* ns a deferring lane waits between claiming an even list slot
-                                            and publishing it, so that later slots overtake it (0..1e6,
-                                            default 0; for tests of the bounded wait).  Results do not
-                                            depend on it. */
+#define CLMGB_OPT_QUEUE_PUBLISH_DELAY 20 /* for tests of the bounded wait: a deferring lane counts an even
+                                            list slot published before writing the column's index, and
+                                            writes it once a finishing warp has taken the slot or after
+                                            this many ns; a warp with nothing to finish keeps looking for
+                                            as long (0..1e7, default 0: index first, no lingering).  Results
+                                            do not depend on it. */
 #define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls
                                             receive (default 0).  A caller that runs a column range [c0, c1)
                                             passes column arrays advanced by c0 (same ldc) and the patch

@@ -71,6 +71,58 @@
  * (published method, see clm_math.h), so the oracle and the GPU round identically. */
 #include "../clm.jl_gb300/csrc/clm_math.h"
 
+/* ---- sensitivity hook (test infrastructure): perturbs the results of the hot path's
+ * pow and log10 calls for oracle/perturb_experiment.py, which measures how far one
+ * ulp in those functions moves the path's results.  Off (mode 0) unless
+ * orc_set_perturbation selects a mode:
+ *   1: every result moved by +-1 ulp;
+ *   2: a fraction `frac` of the results moved by +-1 ulp (the rate at which two nearly
+ *      correctly rounded implementations, such as this one and Julia's, disagree);
+ *   3: the results of the previous, single-precision-logarithm library:
+ *      exp(y*log(x)) and log(x)/ln(10) in binary64 (errors up to |y log x| ulp).
+ * Which results move, and in which direction, is a hash of the arguments, so runs are
+ * reproducible whatever the thread schedule. ---- */
+static int g_perturb_mode = 0;
+static double g_perturb_frac = 0.0;
+static unsigned long long g_perturb_salt = 0;
+void orc_set_perturbation(int32_t mode, double frac, uint64_t salt)
+{
+  g_perturb_mode = mode;
+  g_perturb_frac = frac;
+  g_perturb_salt = salt;
+}
+static uint64_t perturb_hash(double x, double y)
+{
+  uint64_t z = cm_as_u64_(x) ^ ((cm_as_u64_(y) << 17) | (cm_as_u64_(y) >> 47)) ^ g_perturb_salt;
+  z += 0x9e3779b97f4a7c15ULL;                       /* splitmix64 finaliser */
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+static double perturb(double v, double x, double y)
+{
+  if (!isfinite(v) || v == 0.0) return v;
+  const uint64_t h = perturb_hash(x, y);
+  if (g_perturb_mode == 2 && (double)(h >> 11) * 0x1p-53 >= g_perturb_frac) return v;
+  const uint64_t b = cm_as_u64_(v);
+  return cm_as_f64_((h & 1) ? b + 1 : b - 1);
+}
+static double o_pow(double x, double y)
+{
+  if (g_perturb_mode == 3) {
+    if (x > 0.0 && isfinite(x) && x != 1.0 && y != 0.0 && isfinite(y)) return cm_exp(y * cm_log(x));
+    return cm_pow(x, y);
+  }
+  const double v = cm_pow(x, y);
+  return g_perturb_mode ? perturb(v, x, y) : v;
+}
+static double o_log10(double x)
+{
+  if (g_perturb_mode == 3) return (x > 0.0 && isfinite(x)) ? cm_log(x) * CM_INVLN10 : cm_log10(x);
+  const double v = cm_log10(x);
+  return g_perturb_mode ? perturb(v, x, 10.0) : v;
+}
+
 /* ---- constants: src/constants/varcon.jl:15-70 ---- */
 #define GRAV   9.80616
 #define SB     5.67e-8
@@ -619,7 +671,7 @@ static void pc_beta_col(const clmgb_varpar* vp, const clmgb_bounds* bd,
         if (IX(T, c, jj, ld) < TFRZ) {
           double tt = IX(T, c, jj, ld);
           double smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
-          supercool[j] = IX(f->watsat, c, j, ld) * cm_pow(smp / IX(f->sucsat, c, j, ld), -1.0 / IX(f->bsw, c, j, ld));
+          supercool[j] = IX(f->watsat, c, j, ld) * o_pow(smp / IX(f->sucsat, c, j, ld), -1.0 / IX(f->bsw, c, j, ld));
           supercool[j] *= IX(f->dz, c, jj, ld) * 1000.0;
         }
       }
@@ -797,11 +849,11 @@ static uint32_t soiltemp_col(const st_ctx* X, int64_t c)
         double thkv;
         if (satw > 1.0e-7) {
           double dke;
-          if (IX(T, c, jj, ld) >= TFRZ) dke = jl_max(0.0, cm_log10(satw) + 1.0);
+          if (IX(T, c, jj, ld) >= TFRZ) dke = jl_max(0.0, o_log10(satw) + 1.0);
           else dke = satw;
           double fl_denom = liq / (DENH2O * dzv) + ice / (DENICE * dzv) + exi / (DENICE * dzv);
           double fl = (liq / (DENH2O * dzv)) / fl_denom;
-          double dksat = IX(f->tkmg, c, j, ld) * cm_pow(TKWAT, fl * ws) * cm_pow(TKICE, (1.0 - fl) * ws);
+          double dksat = IX(f->tkmg, c, j, ld) * o_pow(TKWAT, fl * ws) * o_pow(TKICE, (1.0 - fl) * ws);
           thkv = dke * dksat + (1.0 - dke) * IX(f->tkdry, c, j, ld);
         } else {
           thkv = IX(f->tkdry, c, j, ld);
@@ -3021,18 +3073,18 @@ static uint32_t moisture_form_col(const clmgb_varpar* vp, const clmgb_bounds* b,
       double s1, imp;
       if (j == nlayers) {
         s1 = R[j].s2;
-        imp = cm_pow(10.0, -e_ice * IX(f->icefrac, c, j, ld));
+        imp = o_pow(10.0, -e_ice * IX(f->icefrac, c, j, ld));
       } else {
         s1 = 0.5 * (R[j].s2 + R[j + 1].s2);
-        imp = cm_pow(10.0, -e_ice * (0.5 * (IX(f->icefrac, c, j, ld) + IX(f->icefrac, c, j + 1, ld))));
+        imp = o_pow(10.0, -e_ice * (0.5 * (IX(f->icefrac, c, j, ld) + IX(f->icefrac, c, j + 1, ld))));
       }
       R[j].imped = imp;
       s1 = jl_min(s1, 1.0); s1 = jl_max(0.01, s1);
       double bb = IX(f->bsw, c, j, ld);
-      double hkv = imp * IX(f->hksat, c, j, ld) * cm_pow(s1, 2.0 * bb + 3.0);
+      double hkv = imp * IX(f->hksat, c, j, ld) * o_pow(s1, 2.0 * bb + 3.0);
       double dhkds = (2.0 * bb + 3.0) * hkv / s1;
       double sn = R[j].s2;
-      double smpv = -IX(f->sucsat, c, j, ld) * cm_pow(sn, -bb);
+      double smpv = -IX(f->sucsat, c, j, ld) * o_pow(sn, -bb);
       double dsmpds = -bb * smpv / sn;
       R[j].hk = hkv; R[j].smp = smpv; R[j].dhkdw = dhkds;
       R[j].dsmpdw = dsmpds / IX(f->watsat, c, j, ld);

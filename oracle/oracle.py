@@ -58,6 +58,8 @@ def lib():
         L.orc_tridiagonal_adjoint_multi.argtypes = [C.c_int64, C.c_int64, C.c_int32] + [P] * 11 + [C.c_int32]
         L.orc_batched_band_solve_adjoint.argtypes = [C.c_int64, C.c_int64, C.c_int32] + [P] * 8 + \
             [C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+        L.orc_set_perturbation.argtypes = [C.c_int32, C.c_double, C.c_uint64]
+        L.orc_set_perturbation.restype = None
         _lib = L
     return _lib
 
@@ -250,3 +252,9 @@ def init_soil_properties(sand, clay, om, zsoi):
                                    *[_p(outs[k]) for k in ("watsat", "bsw", "sucsat", "hksat", "tkmg",
                                                            "tkdry", "csol")])
     return outs
+
+
+def set_perturbation(mode=0, frac=0.0, salt=0):
+    """The oracle's pow/log10 sensitivity hook (clm_oracle.c): 0 off, 1 every result
+    +-1 ulp, 2 a fraction `frac` of them, 3 the previous single-precision-log library."""
+    lib().orc_set_perturbation(int(mode), float(frac), int(salt))

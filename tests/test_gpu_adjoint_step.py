@@ -100,12 +100,15 @@ def _params_and_decisions(traj, st0, loss, steps):
 
 
 def _fd_check(traj, st0, loss, steps, grads, params, tol):
-    """Central differences at h = 1e-6 and 1.37e-6 relative (steps that are not
-    commensurate, so a difference quantised to a few ulps of the loss cannot agree
-    with itself by accident).  An entry is resolved when the discrete record matches
-    the base run, the change of the loss is at least ~2e8 ulps of it, and the two
-    quotients agree to 1e-7.  Every resolved entry must satisfy
-    max|g - fd| <= tol * max|fd| over the resolved entries of its column."""
+    """Central differences at h = 1e-6 relative (the calibration workload's step),
+    checked against quotients at 1.37e-6 (not commensurate, so a difference quantised
+    to a few ulps of the loss cannot agree with itself by accident) and at 1e-5 (ten
+    times the step: rounding noise of the loss is ten times smaller there, and two
+    quotients that share the same noise no longer agree).  An entry is resolved when
+    the discrete record matches the base run for every step size, the change of the
+    loss is at least ~2e8 ulps of it, and the three quotients agree to 1e-7.  Every
+    resolved entry must satisfy max|g - fd| <= tol * max|fd| over the resolved entries
+    of its column, fd the quotient at h = 1e-6."""
     base_L, base_n, base_m = _params_and_decisions(traj, st0, loss, steps)
     L0 = base_L.cpu().numpy()
     # dL/dtheta = sum 2 (y - target) dy/dtheta: where |y - target| is at the rounding
@@ -115,13 +118,13 @@ def _fd_check(traj, st0, loss, steps, grads, params, tol):
     conditioned = resid >= 1e-6 * np.abs(Y).max(0)
     nc = st0.nc
     nsoi = st0.vp.nlevsoi
-    G, F1, F2, OK = [], [], [], []
+    G, F1, F2, F3, OK = [], [], [], [], []
     for p in params:
         for j in range(nsoi):
             theta = st0[p][j].clone()
             fds, same = [], torch.ones(nc, dtype=torch.bool, device="cuda")
             dl = None
-            for rel in (1e-6, 1.37e-6):
+            for rel in (1e-6, 1.37e-6, 1e-5):
                 h = rel * theta.abs()
                 res = []
                 for sgn in (1.0, -1.0):
@@ -137,9 +140,11 @@ def _fd_check(traj, st0, loss, steps, grads, params, tol):
             G.append(grads[p][j].cpu().numpy())
             F1.append(fds[0])
             F2.append(fds[1])
+            F3.append(fds[2])
             OK.append(same.cpu().numpy() & (dl >= 4e-8 * np.abs(L0)))
-    G, F1, F2, OK = (np.array(x) for x in (G, F1, F2, OK))     # [nparam, nc]
-    resolved = OK & (np.abs(F1 - F2) <= 1e-7 * np.abs(F1)) & conditioned[None, :]
+    G, F1, F2, F3, OK = (np.array(x) for x in (G, F1, F2, F3, OK))     # [nparam, nc]
+    resolved = (OK & (np.abs(F1 - F2) <= 1e-7 * np.abs(F1)) & (np.abs(F1 - F3) <= 1e-7 * np.abs(F1)) &
+                conditioned[None, :])
     scale = np.max(np.where(resolved, np.abs(F1), 0.0), axis=0)
     err = np.where(resolved, np.abs(G - F1), 0.0) / np.maximum(scale, 1e-300)
     rel = err.max(axis=0)

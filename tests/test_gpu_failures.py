@@ -134,16 +134,17 @@ def test_attempt_cap_option_range():
     with pytest.raises(api.CLMGBError):
         h.set_option(abi.OPT_QUEUE_POLL_LIMIT, -1)
     with pytest.raises(api.CLMGBError):
-        h.set_option(abi.OPT_QUEUE_PUBLISH_DELAY, 2_000_000)
+        h.set_option(abi.OPT_QUEUE_PUBLISH_DELAY, 20_000_000)
     h.close()
 
 
 def test_deferred_slot_wait_runs_out_and_every_column_is_finished():
     """A finishing warp that finds a deferred column's index still on its way waits a
-    bounded number of polls.  With no polls allowed and each deferral publishing 20 us
-    late, the waits run out: the slots are given back, the deferring lanes finish
-    their own columns, CLMGB_COL_QUEUE_WAIT is recorded in the device status, the call
-    returns normally and every result is the oracle's."""
+    bounded number of polls.  With no polls allowed and the index of every even slot
+    written only after a finishing warp has taken the slot (test option), the waits run
+    out: the slots are given back, the deferring lanes finish their own columns,
+    CLMGB_COL_QUEUE_WAIT is recorded in the device status, the call returns normally
+    and every result is the oracle's."""
     wl = synth.make_workload(2, nc=16384, seed=12)
     st = wl.state
     orc.soil_water_fractions(st)
@@ -153,7 +154,7 @@ def test_deferred_slot_wait_runs_out_and_every_column_is_finished():
     orc.soil_water(ref, wl.dtime, cfg)
     runs = {}
     for name, opts in (("normal", ()),
-                       ("given_back", ((abi.OPT_QUEUE_POLL_LIMIT, 0), (abi.OPT_QUEUE_PUBLISH_DELAY, 20000)))):
+                       ("given_back", ((abi.OPT_QUEUE_POLL_LIMIT, 0), (abi.OPT_QUEUE_PUBLISH_DELAY, 5_000_000)))):
         h = api.Handle(st.vp)
         h.reserve(st.nc)
         h.set_option(abi.OPT_QUEUE_DEFER, 4)      # many deferred columns
