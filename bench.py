@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--e2e-readback", default="dma", choices=["kernel", "dma"],
                     help="how the temperature outputs come back during the Richards solve")
     ap.add_argument("--cpu-sample", type=int, default=4096)
+    ap.add_argument("--cpu-steps", type=int, default=5, help="steps of the CPU baseline sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 probe and the work count")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--schedule", type=int, default=None, help="CLMGB_OPT_STEP_SCHEDULE override")
     ap.add_argument("--queue-bps", type=int, default=None, help="CLMGB_OPT_QUEUE_BLOCKS_PER_SM override")
@@ -64,8 +66,11 @@ def parse():
                     help="run only the adjoint calibration leg and print its JSON (profiling)")
     ap.add_argument("--adj-nc", type=int, default=65536)
     ap.add_argument("--adj-steps", type=int, default=48)
-    ap.add_argument("--adj-k", type=int, default=2,
-                    help="checkpoint every k steps (2: 24 checkpoints of 0.45 GB at 65,536 columns)")
+    ap.add_argument("--adj-k", type=int, default=8,
+                    help="checkpoint every k steps (8, the calibration workload's interval: 6 checkpoints of "
+                         "0.45 GB at 65,536 columns)")
+    ap.add_argument("--adj-k2", type=int, default=2,
+                    help="a second checkpoint interval reported beside it (0: none)")
     ap.add_argument("--adj-slots", type=int, default=65536)
     ap.add_argument("--adj-entries", type=int, default=256,
                     help="tape entries per slot (the recording kernel only; the default adjoint needs none)")
@@ -173,6 +178,21 @@ def profile_traffic():
     return None
 
 
+def fp64_probe():
+    """(DFMA/s, divisions/s, pow/s, log10/s) of this device from libclmgb_probe.so, or None."""
+    import ctypes as C
+    from clmgb import build
+    try:
+        lib = C.CDLL(build.build_probe())
+    except OSError:
+        return None
+    out = (C.c_double * 4)()
+    lib.clmgb_probe_fp64.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    if lib.clmgb_probe_fp64(4, out) != 0:
+        return None
+    return [float(v) for v in out]
+
+
 def cpu_baseline_sample(wl, cfg, nsample, nsteps=1):
     """Times the oracle (CPU restatement of the reference path) on the first `nsample`
     columns for `nsteps` steps with every host thread."""
@@ -184,8 +204,11 @@ def cpu_baseline_sample(wl, cfg, nsample, nsteps=1):
     t0 = time.perf_counter()
     orc.run_steps(st, wl.dtime, G, I, cfg, nthreads=threads)
     dt = time.perf_counter() - t0
+    state_mb = sum(a.nbytes for a in st.arrays.values()) / 1e6
     return {"value": len(cols) * nsteps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d columns x %d step(s) of the same workload, OpenMP over columns" % (len(cols), nsteps)}
+            "sample": "%d columns x %d steps of the same workload (its first columns and forcing), OpenMP over "
+                      "columns; the sample's state (%.0f MB) fits in the host's caches, unlike the full "
+                      "workload's, so the rate is an upper bound of the CPU path's" % (len(cols), nsteps, state_mb)}
 
 
 def run_reference(args):
@@ -295,6 +318,22 @@ def adjoint_leg(args):
            "note": "adjoint_over_forward = reverse pass / plain forward; gradients checked against "
                    "complex-step and central differences in tests/test_gpu_adjoint_step.py"}
     h.close()
+    return out
+
+
+def adjoint_legs(args):
+    """The adjoint leg at the calibration workload's checkpoint interval, and at a
+    second interval beside it."""
+    out = adjoint_leg(args)
+    if args.adj_k2 and args.adj_k2 != args.adj_k:
+        import copy
+        import torch
+        torch.cuda.empty_cache()
+        a2 = copy.copy(args)
+        a2.adj_k = args.adj_k2
+        o2 = adjoint_leg(a2)
+        out["other_interval"] = {k: o2[k] for k in ("workload", "forward_ms", "forward_with_checkpoints_ms",
+                                                    "reverse_ms", "adjoint_over_forward", "gradient_over_forward")}
     return out
 
 
@@ -473,6 +512,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     # the state entering the timed steps, for the graph leg to replay the same steps from
     d_timed0 = None if args.no_graph else d.copy()
+    d_count0 = None if args.no_fp64 else d.copy()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
@@ -531,6 +571,26 @@ def run_ours(args):
         del g
     value, elapsed_ms = aggregate_throughput(elapsed_ms, args.steps * nc, world)
 
+    # FP64 work of the timed Richards calls: the same steps again from the same state
+    # (untimed) with the kernel counting the levels of its attempts and refreshes, and
+    # the device's DFMA, division and pow rates from the probe (clmgb/flops_model.py)
+    fp64 = None
+    if d_count0 is not None:
+        for k, v in d_count0.arrays.items():
+            d.arrays[k].copy_(v)
+        del d_count0
+        h.set_option(abi.OPT_COUNT_WORK, 1)
+        for k in range(args.steps):
+            step(args.warmup + k)
+        torch.cuda.synchronize()
+        la = h.get_option(abi.OPT_WORK_LEVEL_ATTEMPTS)
+        lr = h.get_option(abi.OPT_WORK_LEVEL_REFRESHES)
+        h.set_option(abi.OPT_COUNT_WORK, 0)
+        probe = fp64_probe()
+        if probe is not None and la > 0:
+            from clmgb import flops_model
+            fp64 = flops_model.fp64_roofline(la, lr, args.steps, kern_ms, probe)
+
     # roofline of the dominant kernel: the work-queue Richards solve (soil_water!)
     bytes_launch = bytes_model.richards_bytes_per_call(nc, st.vp.nlevsoi)
     peak, peak_kind = measured_peaks()
@@ -550,7 +610,10 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": bytes_launch,
                 "step_algorithmic_bytes": step_bytes,
                 "step_achieved_gbs": step_bytes / (elapsed_ms / args.steps / 1000.0) / 1e9,
-                "note": "FP64-pipe bound on GB300 (1.19 TFLOP/s measured DFMA); see profiles/"}
+                "fp64": fp64, "fp64_frac": fp64["frac"] if fp64 else None,
+                "note": "the kernel is bound by the FP64 pipe, not HBM: fp64 is its work in DFMA-equivalents "
+                        "(clmgb/flops_model.py, levels counted by the kernel) over its time and the DFMA rate "
+                        "the probe measures on this device; ncu summaries in profiles/"}
 
     # end to end with the state in pinned host memory (clmgb.hoststep): each step moves
     # the fields it reads that the rest of the model changes (parameters, geometry and
@@ -592,7 +655,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(wl, cfg, args.cpu_sample, 1)
+        cpu = cpu_baseline_sample(wl, cfg, args.cpu_sample, args.cpu_steps)
 
     state_gb = sum(v.numel() * v.element_size() for v in d.arrays.values()) / 1e9
     adj_line = None
@@ -604,7 +667,7 @@ def run_ours(args):
             warm_line = warm_leg(args, wl)
             torch.cuda.empty_cache()
         if not args.no_adjoint:
-            adj_line = adjoint_leg(args)
+            adj_line = adjoint_legs(args)
 
     # this library's kernels per timed step: forcing, soil temperature, water fractions,
     # then the Richards call (work queue with reserved scratch: the impedance / column
@@ -639,7 +702,7 @@ def run_ours(args):
 def main():
     args = parse()
     if args.adjoint_only:
-        print(json.dumps(adjoint_leg(args)))
+        print(json.dumps(adjoint_legs(args)))
         return
     if args.impl == "reference":
         run_reference(args)

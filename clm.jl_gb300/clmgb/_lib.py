@@ -48,6 +48,7 @@ _SIGS = {
     "clmgb_column_step_logged": ([P, P, P, P, P, F64, I32, P, P, P, P, P], I32),
     "clmgb_effec_rootfrac_vert_tran_sink": ([P, P, P, I32, P, P], I32),
     "clmgb_soil_water_zd09": ([P, P, P, P, F64, P], I32),
+    "clmgb_soil_water_flexible_cn": ([P, P, P, P], I32),
     "clmgb_soil_fluxes": ([P, P, P, F64, P], I32),
     "clmgb_surface_hydrology": ([P, P, P, P, C.c_uint32, F64, P], I32),
     "clmgb_snow_layers": ([P, P, P, P, C.c_uint32, F64, P], I32),

@@ -69,6 +69,9 @@ OPT_QUEUE_PACKED_REFRESH = 17
 OPT_ATTEMPT_CAP = 18
 OPT_QUEUE_POLL_LIMIT = 19
 OPT_QUEUE_PUBLISH_DELAY = 20
+OPT_COUNT_WORK = 21
+OPT_WORK_LEVEL_ATTEMPTS = 22
+OPT_WORK_LEVEL_REFRESHES = 23
 MAX_COPY_SEGMENTS = 128
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
@@ -605,6 +608,16 @@ HYDRSTRESS_ONLY = ("k_soil_root_patch", "smp_l", "vegwp_patch", "frac_veg_nosno"
                    "qflx_hydr_redist_patch")
 
 # Fields of the synthetic step harness that are not in either struct.
+# clmgb_flexcn_fields (soil_water!'s use_flexibleCN step), header order
+FLEXCN_FIELDS = [
+    ("mask_hydrology", _u8, "c", None),
+    ("dz", _f64, "c", "L"),
+    ("h2osoi_liq", _f64, "c", "L"),
+    ("h2osoi_ice", _f64, "c", "L"),
+    ("h2osoi_vol", _f64, "c", "G"),
+    ("wa", _f64, "c", None),
+]
+
 EXTRA_FIELDS = [
     ("t_ssbef", _f64, "c", "L"),
     ("t_h2osfc_bef", _f64, "c", None),
@@ -635,6 +648,7 @@ SnowLayerFields = _mk_struct("SnowLayerFields", SNOWLAYER_FIELDS)
 LakeFields = _mk_struct("LakeFields", LAKE_FIELDS)
 ColBalanceFields = _mk_struct("ColBalanceFields", COLBALANCE_FIELDS)
 SoilFluxFields = _mk_struct("SoilFluxFields", SOILFLUX_FIELDS)
+FlexCnFields = _mk_struct("FlexCnFields", FLEXCN_FIELDS)
 
 
 class SubstepLog(C.Structure):

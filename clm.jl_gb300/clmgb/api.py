@@ -5,6 +5,7 @@ Names and argument meaning follow the reference:
   soil_temperature(...)             soil_temperature!        soil_temperature.jl:358
   set_soil_water_fractions(...)     set_soil_water_fractions! soil_hydrology.jl:394
   soil_water(...)                   soil_water!              soil_water_movement.jl:1780
+  init_soilwater_movement(...)      init_soilwater_movement  soil_water_movement.jl:679
   phase_change_h2osfc / _beta       phase_change_*!          soil_temperature.jl:1857, 2232
   batched_band_solve(...)           batched_band_solve!      band_diagonal.jl:179
   tridiagonal_multi(...)            tridiagonal_multi!       tridiagonal.jl:129
@@ -34,6 +35,30 @@ def _dptr(t, what="tensor"):
     if not t.is_contiguous():
         raise ValueError("%s must be contiguous" % what)
     return C.c_void_p(t.data_ptr())
+
+
+def init_soilwater_movement(use_bedrock=False, **kw):
+    """init_soilwater_movement (soil_water_movement.jl:679-698): a SoilWaterMovementConfig
+    with the reference's defaults (Zeng-Decker 2009, flux upper and aquifer lower
+    boundaries, dtmin 60 s, verySmall 1e-8, tolerances 0.1 / 0.01, inexpensive fluxes,
+    e_ice 6) and keyword overrides, validated as the reference does: Zeng-Decker 2009
+    requires the aquifer lower boundary, and use_bedrock (varctl.use_bedrock) the
+    zero-flux one.  Raises CLMGBError(CLMGB_ERR_CONFIG) where the reference raises."""
+    vals = dict(soilwater_movement_method=abi.ZENGDECKER_2009, upper_boundary_condition=abi.BC_FLUX,
+                lower_boundary_condition=abi.BC_AQUIFER, flux_calculation=1, dtmin=60.0, verySmall=1.0e-8,
+                xTolerUpper=1.0e-1, xTolerLower=1.0e-2, e_ice=6.0)
+    for k, v in kw.items():
+        if k not in vals:
+            raise TypeError("unknown SoilWaterMovementConfig field %r" % k)
+        vals[k] = v
+    cfg = abi.SwmConfig(**vals)
+    if cfg.soilwater_movement_method == abi.ZENGDECKER_2009 and cfg.lower_boundary_condition != abi.BC_AQUIFER:
+        raise CLMGBError(abi.CLMGB_ERR_CONFIG, "init_soilwater_movement: ZD09 must use bc_aquifer lower boundary "
+                                               "condition")
+    if use_bedrock and cfg.lower_boundary_condition != abi.BC_ZERO_FLUX:
+        raise CLMGBError(abi.CLMGB_ERR_CONFIG, "init_soilwater_movement: use_bedrock requires bc_zero_flux lower "
+                                               "boundary condition")
+    return cfg
 
 
 class Handle:

@@ -16,6 +16,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libclmgb.so")
+PROBE_SRC = os.path.join(PKG, "probe", "fp64_probe.cu")
+PROBE_LIB = os.path.join(LIBDIR, "libclmgb_probe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fno-fast-math", "--extended-lambda"]
@@ -46,7 +48,20 @@ def _git_desc():
         return "dev"
 
 
+def build_probe(force=False):
+    """libclmgb_probe.so: the FP64 throughput probe bench.py measures the roofline with."""
+    deps = [PROBE_SRC, os.path.join(CSRC, "clm_math.h"), os.path.join(CSRC, "clm_math_tables.h"), __file__]
+    if not force and os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) > max(map(os.path.getmtime, deps)):
+        return PROBE_LIB
+    os.makedirs(LIBDIR, exist_ok=True)
+    tmp = PROBE_LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call([_nvcc()] + NVCC_FLAGS + ARCH + ["-shared", PROBE_SRC, "-o", tmp])
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
+
+
 def build(force=False, verbose=False, ptxas_v=False):
+    build_probe(force)
     srcs = sources()
     newest = max(os.path.getmtime(p) for p in srcs + _deps() + [__file__])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > newest:

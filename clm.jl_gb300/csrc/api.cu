@@ -49,6 +49,7 @@ struct clmgb_handle_s {
   int64_t attempt_cap;          // CLMGB_OPT_ATTEMPT_CAP
   int64_t poll_limit;           // CLMGB_OPT_QUEUE_POLL_LIMIT
   int64_t publish_delay;        // CLMGB_OPT_QUEUE_PUBLISH_DELAY
+  int64_t count_work;           // CLMGB_OPT_COUNT_WORK (counters in scratch words 10, 11)
   cudaError_t last_error;
 };
 
@@ -166,6 +167,7 @@ static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
   q.d_count = have ? h->scratch + 7 : nullptr;
   q.poll_limit = (int)h->poll_limit;
   q.publish_delay = (int)h->publish_delay;
+  q.work = h->count_work ? h->scratch + 10 : nullptr;
   return q;
 }
 
@@ -236,6 +238,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->attempt_cap = clmgb::MF_ATTEMPT_CAP;
   h->poll_limit = clmgb::DEFER_POLL_LIMIT;
   h->publish_delay = 0;
+  h->count_work = 0;
   memset(&h->ws, 0, sizeof(h->ws));
   h->waves_blocks = 0;
   h->waves_blocks_per_sm = 0;
@@ -641,6 +644,18 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soil
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+int32_t clmgb_soil_water_flexible_cn(clmgb_handle h, const clmgb_bounds* b, const clmgb_flexcn_fields* f,
+                                     void* stream) {
+  if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
+  int32_t e = check_bounds(b, false);
+  if (e) return e;
+  if (b->nc == 0) return CLMGB_OK;
+  if ((e = check_fields(f))) return e;
+  if (h->vp.nlevsoi < 1) return CLMGB_ERR_DIMS;
+  const cudaError_t ce = clmgb::launch_flexible_cn(hdims(h, *b), b->nc, *f, (cudaStream_t)stream);
+  return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
+}
+
 int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
                           const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
                           int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
@@ -832,6 +847,15 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value < 0 || value > 10000000) return CLMGB_ERR_CONFIG;
       h->publish_delay = value;
       return CLMGB_OK;
+    case CLMGB_OPT_COUNT_WORK: {
+      if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
+      if (value && !h->count_work) {    // counting starts from zero
+        const cudaError_t ce = cudaMemset(h->scratch + 10, 0, 2 * sizeof(unsigned long long));
+        if (ce != cudaSuccess) return cuda_fail(h, ce);
+      }
+      h->count_work = value;
+      return CLMGB_OK;
+    }
     default:
       return CLMGB_ERR_CONFIG;
   }
@@ -859,6 +883,15 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_ATTEMPT_CAP: *value = h->attempt_cap; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_POLL_LIMIT: *value = h->poll_limit; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_PUBLISH_DELAY: *value = h->publish_delay; return CLMGB_OK;
+    case CLMGB_OPT_COUNT_WORK: *value = h->count_work; return CLMGB_OK;
+    case CLMGB_OPT_WORK_LEVEL_ATTEMPTS:
+    case CLMGB_OPT_WORK_LEVEL_REFRESHES: {
+      unsigned long long w[2];
+      const cudaError_t ce = cudaMemcpy(w, h->scratch + 10, sizeof(w), cudaMemcpyDeviceToHost);
+      if (ce != cudaSuccess) return cuda_fail(h, ce);
+      *value = (int64_t)w[key == CLMGB_OPT_WORK_LEVEL_ATTEMPTS ? 0 : 1];
+      return CLMGB_OK;
+    }
     case CLMGB_OPT_ADJ_TAPE_ENTRIES: *value = h->tape.entries; return CLMGB_OK;
     case CLMGB_OPT_ADJ_TAPE_USED: {
       unsigned int used = 0;

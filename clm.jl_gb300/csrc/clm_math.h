@@ -9,7 +9,7 @@
 // Every operation is an IEEE-754 binary64 add, multiply or fused multiply-add
 // written out explicitly (CUDA: __dadd_rn/__dmul_rn/__fma_rn; C: +, *, fma() built
 // with -ffp-contract=off), so a C build and a CUDA build return the same bits.  On
-// GB300, whose FP64 pipe issues about 1.9 FMA/clk/SM, a pow() here costs about 50 FP64
+// GB300, whose FP64 pipe issues about 1.9 FMA/clk/SM, a pow() here costs about 40 FP64
 // instructions; exponent and table-index handling use the integer pipes.
 //
 // pow and log10 go through a double-double logarithm (cm_log_dd: Tang's table with an
@@ -137,6 +137,8 @@ CM_FN double cm_exp(double x) {
 
 // log(x) = hi + *lo (returned: hi) for a positive finite x, subnormals included:
 // |hi + lo - log(x)| below about 2^-67 max(1, |log x|), and below 2^-67 |log x| near 1.
+// The pair is not renormalised: |lo| < 2^-20 max(1, |hi|), which the callers (pow and
+// log10, whose products with it are formed exactly or with a single rounding) allow.
 // x = 2^k z, z in [0.75, 1.5); log(x) = k ln2 + log(1/invc) + log1p(r), r = z*invc - 1
 // formed exactly by one fma (the table's invc has few fractional bits), |r| < 2^-7.
 CM_FN double cm_log_dd(double x, double* lo_out) {
@@ -163,18 +165,16 @@ CM_FN double cm_log_dd(double x, double* lo_out) {
   // hi + e2 = s + ar2 exactly (|s| >= |ar2|)
   const double hi = CM_ADD(s, ar2);
   const double e2 = CM_ADD(CM_SUB(s, hi), ar2);
-  // r^3 (1/3 - r/4 + ... + r^6/9), truncation below 2^-70
+  // r^3 (1/3 - r/4 + ... + r^6/9) = (r ar2) (-2/3 + r/2 - ...): the coefficients carry
+  // the factor -2 (exact); truncation below 2^-70
   double p = CM_FMA(r, CM_LOGD_C9, CM_LOGD_C8);
   p = CM_FMA(r, p, CM_LOGD_C7);
   p = CM_FMA(r, p, CM_LOGD_C6);
   p = CM_FMA(r, p, CM_LOGD_C5);
   p = CM_FMA(r, p, CM_LOGD_C4);
   p = CM_FMA(r, p, CM_LOGD_C3);
-  const double r3 = CM_MUL(CM_MUL(r, r), r);
-  const double lo = CM_ADD(CM_ADD(CM_FMA(kd, CM_LN2_LO, lcl), e), CM_FMA(r3, p, CM_ADD(e2, e3)));
-  const double y = CM_ADD(hi, lo);
-  *lo_out = CM_ADD(CM_SUB(hi, y), lo);
-  return y;
+  *lo_out = CM_ADD(CM_ADD(CM_FMA(kd, CM_LN2_LO, lcl), e), CM_FMA(CM_MUL(r, ar2), p, CM_ADD(e2, e3)));
+  return hi;
 }
 
 // exp(x + xl) for |xl| <= ulp(x): the value before the final rounding is within about
@@ -190,7 +190,7 @@ CM_FN double cm_exp_dd(double x, double xl) {
     if (x < -745.1332191019412076235) return 0.0;
   }
   const double shift = 0x1.8p52;
-  double kd = CM_ADD(CM_MUL(CM_EXPD_INVLN2N, x), shift);
+  double kd = CM_FMA(x, CM_EXPD_INVLN2N, shift);
   const int64_t kk = (int64_t)(CM_AS_U64(kd) - 0x4338000000000000ULL);   // round(x*256/ln2)
   kd = CM_SUB(kd, shift);
   double r = CM_FMA(-kd, CM_EXPD_LN2N_HI, x);               // exact
@@ -240,13 +240,22 @@ CM_FN double jl_pow_int(double x, int64_t n) {
   return CM_MUL(x, y);
 }
 
-// Integral y in Julia's power-by-squaring range (Base.Math.use_power_by_squaring)
-CM_FN bool cm_pow_by_squaring(double y, int64_t* n) {
-  const double ay = y < 0.0 ? -y : y;
-  if (!(ay <= 24576.0)) return false;
-  const int64_t m = (int64_t)y;
-  if ((double)m != y || m < -4096) return false;
-  *n = m;
+// Integral y in Julia's power-by-squaring range (Base.Math.use_power_by_squaring),
+// -4096 <= y <= 24576, decided on the bit pattern (integer pipes only).
+CM_FN bool cm_pow_by_squaring(uint64_t uy, int64_t* n) {
+  if ((uy << 1) == 0) {                                     // y = +-0
+    *n = 0;
+    return true;
+  }
+  const int ex = (int)((uy >> 52) & 0x7ff) - 1023;          // |y| in [2^ex, 2^(ex+1))
+  if (ex < 0 || ex > 14) return false;                      // |y| < 1 (not 0), or |y| >= 32768
+  const int sh = 52 - ex;
+  const uint64_t mant = (uy & 0x000fffffffffffffULL) | 0x0010000000000000ULL;
+  if (mant & ((1ULL << sh) - 1)) return false;              // a fraction
+  const int64_t m = (int64_t)(mant >> sh);
+  const int64_t v = (uy >> 63) ? -m : m;
+  if (v < -4096 || v > 24576) return false;
+  *n = v;
   return true;
 }
 
@@ -260,21 +269,22 @@ CM_FN double cm_pow(double x, double y) {
   if (ux == 0x3ff0000000000000ULL) return 1.0;
   if ((uy << 1) > 0xffe0000000000000ULL) return y;          // y NaN
   int64_t n;
-  if (cm_pow_by_squaring(y, &n)) return n == 0 ? 1.0 : jl_pow_int(x, n);
-  if ((ux << 1) == 0) return y > 0.0 ? 0.0 : CM_INF;       // x = +-0
+  if (cm_pow_by_squaring(uy, &n)) return n == 0 ? 1.0 : jl_pow_int(x, n);
   bool neg = false;
-  const double ay = y < 0.0 ? -y : y;
-  if (ux >> 63) {                                           // x < 0 (or -NaN)
-    if (x != x) return x;
-    const bool yint = ay >= 0x1p53 || (double)(int64_t)y == y;
-    if (!yint) return CM_NAN;
-    neg = ay < 0x1p53 && ((int64_t)y & 1);
-    x = -x;
-  }
-  if (x != x) return x;
-  if (x == CM_INF) {
-    const double v = y > 0.0 ? CM_INF : 0.0;
-    return neg ? -v : v;
+  if (ux - 1 >= 0x7fefffffffffffffULL) {                    // not a positive finite nonzero x
+    if ((ux << 1) == 0) return y > 0.0 ? 0.0 : CM_INF;     // x = +-0
+    if ((ux << 1) > 0xffe0000000000000ULL) return x;        // x NaN
+    const double ay = y < 0.0 ? -y : y;
+    if (ux >> 63) {                                         // x < 0
+      const bool yint = ay >= 0x1p53 || (double)(int64_t)y == y;
+      if (!yint) return CM_NAN;
+      neg = ay < 0x1p53 && ((int64_t)y & 1);
+      x = -x;
+    }
+    if (x == CM_INF) {
+      const double v = y > 0.0 ? CM_INF : 0.0;
+      return neg ? -v : v;
+    }
   }
   double lxl;
   const double lxh = cm_log_dd(x, &lxl);
@@ -291,7 +301,7 @@ CM_FN double cm_pow_lx(double x, double lxh, double lxl, double y) {
   const uint64_t uy = CM_AS_U64(y);
   if ((uy << 1) > 0xffe0000000000000ULL) return y;
   int64_t n;
-  if (cm_pow_by_squaring(y, &n)) return n == 0 ? 1.0 : jl_pow_int(x, n);
+  if (cm_pow_by_squaring(uy, &n)) return n == 0 ? 1.0 : jl_pow_int(x, n);
   const double eh = CM_MUL(y, lxh);
   const double el = CM_FMA(y, lxl, CM_FMA(y, lxh, -eh));
   return cm_exp_dd(eh, el);

@@ -35,7 +35,8 @@ two intervals next to 1 use invc = 1, so r = z - 1 and log near 1 keeps its rela
 accuracy.  -log(invc_i) = logc_hi + logc_lo with logc_hi a multiple of 2^-42 (so
 k*ln2_hi + logc_hi is exact for |k| < 2^11), and |logc_hi| >= |r| on its interval
 (checked), so adding r to it is error-free by Fast2Sum.  |r| < 2^-7 everywhere; log1p(r) is its
-Taylor series to r^9 (truncation below 2^-70).
+Taylor series to r^9 (truncation below 2^-70), its r^3 tail evaluated on r * (-r^2/2)
+with the coefficients times -2.
 
 exp of a double-double argument (N = 256): 2^(j/256) = t_hi + t_lo (t_hi = RN, t_lo =
 RN of the rest), ln2/256 = hi + lo with 33-bit hi (k*hi exact for |k| < 2^20), and
@@ -183,8 +184,10 @@ def logd_tables():
         out += ["  %s," % hexd(v) for v in vals]
         out.append("};")
     out.append("// max |r| over the intervals: %.6g" % float(rmax))
-    for n in range(3, 10):      # log1p(r) = r - r^2/2 + sum_{n>=3} (-1)^(n+1) r^n / n
-        out.append("#define CM_LOGD_C%d (%s)" % (n, hexd(mp.mpf((-1) ** (n + 1)) / n)))
+    # log1p(r) = r - r^2/2 + r^3 sum_{n>=3} (-1)^(n+1) r^(n-3) / n, the sum evaluated on
+    # (r * (-r^2/2)) with each coefficient times -2
+    for n in range(3, 10):
+        out.append("#define CM_LOGD_C%d (%s)" % (n, hexd(-2 * mp.mpf((-1) ** (n + 1)) / n)))
     ln10 = mp.log(10)
     ih = float(1 / ln10)
     out.append("#define CM_INVLN10_HI (%s)" % hexd(ih))

@@ -558,9 +558,17 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
         double* r0 = lg.rec + L.c * lg.stride + (int64_t)nacc * SUB_REC;
         for (int j = 1; j <= L.nlayers; j++) r0[j - 1] = L.liq[j];
       }
+      if (qs.work) {
+        const unsigned lv = __reduce_add_sync(FULL, want ? (unsigned)L.nlayers : 0u);
+        if (lane == 0) atomicAdd(qs.work + 1, (unsigned long long)lv);
+      }
       mfp_refresh(L, wm, D, f, cfg, qs.pcache, wsm, nls);
     }
     const bool can_try = active && !(L.fresh && L.nsub < D.attempt_cap);
+    if (qs.work) {
+      const unsigned lv = __reduce_add_sync(FULL, can_try ? (unsigned)L.nlayers : 0u);
+      if (lane == 0) atomicAdd(qs.work, (unsigned long long)lv);
+    }
     if (!can_try) continue;
     double* rec = nullptr;
     double dts = 0.0, dtd = 0.0;
@@ -619,6 +627,35 @@ k_compute_qcharge(Dims D, int64_t nc, clmgb_soilwater_fields f, double dtime) {
   const int64_t nl = f.col_nbedrock[c];
   if (nl < 1 || nl > D.nlevsoi) return;
   compute_qcharge_col(D, f, dtime, c);
+}
+
+// The use_flexibleCN branch of soil_water! (soil_water_movement.jl:1812-1843) for one
+// column: smooth_ifelse on Float64 is the exact branch x >= 0 ? a : b (smooth_ad.jl:253-257).
+__global__ void __launch_bounds__(BLOCK)
+k_flexible_cn(Dims D, int64_t nc, clmgb_flexcn_fields f) {
+  const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  if (c >= nc || !f.mask_hydrology[c]) return;
+  const int64_t ld = D.ldc;
+  const int joff = D.nlevsno, nlevsoi = D.nlevsoi;
+  const double watmin = 0.001;
+  for (int j = 1; j <= nlevsoi - 1; j++) {
+    double& lj = LV(f.h2osoi_liq, c, joff + j, ld);
+    const double xs = lj >= 0.0 ? 0.0 : watmin - lj;
+    lj = lj + xs;
+    double& ln = LV(f.h2osoi_liq, c, joff + j + 1, ld);
+    ln = ln - xs;
+  }
+  {
+    double& lj = LV(f.h2osoi_liq, c, joff + nlevsoi, ld);
+    const double xs = (lj - watmin) >= 0.0 ? 0.0 : watmin - lj;
+    lj = lj + xs;
+    f.wa[c] = f.wa[c] - xs;
+  }
+  for (int j = 1; j <= nlevsoi; j++) {
+    const double dzv = LVc(f.dz, c, joff + j, ld);
+    LV(f.h2osoi_vol, c, j, ld) =
+        LV(f.h2osoi_liq, c, joff + j, ld) / (dzv * DENH2O) + LVc(f.h2osoi_ice, c, joff + j, ld) / (dzv * DENICE);
+  }
 }
 
 // Ice impedances of every hydrology column, one thread per column, into imp_cache
@@ -969,6 +1006,10 @@ cudaError_t launch_compute_qcharge(const Dims& D, int64_t nc, const clmgb_soilwa
                                   const clmgb_swm_config& cfg, double dtime, cudaStream_t s) {
   if (cfg.lower_boundary_condition != CLMGB_BC_WATERTABLE || nc <= 0) return cudaSuccess;
   k_compute_qcharge<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, dtime);
+  return cudaGetLastError();
+}
+cudaError_t launch_flexible_cn(const Dims& D, int64_t nc, const clmgb_flexcn_fields& f, cudaStream_t s) {
+  k_flexible_cn<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f);
   return cudaGetLastError();
 }
 cudaError_t launch_copy_segments(const CopySegments& cs, cudaStream_t s) {

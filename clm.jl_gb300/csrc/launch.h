@@ -43,6 +43,10 @@ struct QueueScratch {
   // production: it lets a test make that wait run out)
   int poll_limit = DEFER_POLL_LIMIT;
   int publish_delay = 0;
+  // CLMGB_OPT_COUNT_WORK: when set, the packed kernel and the warp-per-column finish add
+  // the levels of every substep attempt to work[0] and of every hydraulic refresh to
+  // work[1] (the FP64 work model of the solve, clmgb/flops_model.py); NULL otherwise
+  unsigned long long* work = nullptr;
 };
 
 // Per-column state of the wave-synchronous Richards solve (richards_waves.cu), from
@@ -132,6 +136,7 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
 // (a no-op otherwise); every moisture-form entry point runs it after its solve.
 cudaError_t launch_compute_qcharge(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                   const clmgb_swm_config& cfg, double dtime, cudaStream_t s);
+cudaError_t launch_flexible_cn(const Dims& D, int64_t nc, const clmgb_flexcn_fields& f, cudaStream_t s);
 cudaError_t launch_noalloc_soil_water(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                       const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,
                                       cudaStream_t s);

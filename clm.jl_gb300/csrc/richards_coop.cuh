@@ -115,7 +115,9 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
       dt_dz = dtsub / (M_TO_MM * dzv);
       dt_cur = dtsub;
     }
+    if (qs.work && lane == 0) atomicAdd(qs.work, (unsigned long long)n);   // an attempt over n levels
     if (fresh) {
+      if (qs.work && lane == 0) atomicAdd(qs.work + 1, (unsigned long long)n);
       // hydraulic properties (mf_refresh, :1280-1308)
       double s2 = 0.0;
       if (lv) {

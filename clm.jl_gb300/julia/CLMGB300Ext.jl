@@ -148,7 +148,6 @@ end
 function CLM.soil_water!(col::CLM.ColumnData{<:Any,<:CuArray}, mask_hydrology, mask_urban, sh, ss, wfb,
                          wsb, temp, cs, ef, swrc, cfg::CLM.SoilWaterMovementConfig, dtime;
                          use_flexibleCN::Bool = false)
-    use_flexibleCN && error("use_flexibleCN is not implemented by the GB300 path")
     c = SwmConfig(cfg.soilwater_movement_method, cfg.upper_boundary_condition, cfg.lower_boundary_condition,
                   cfg.flux_calculation, cfg.dtmin, cfg.verySmall, cfg.xTolerUpper, cfg.xTolerLower, cfg.e_ice)
     b = Bounds(length(mask_hydrology), 0, 0, size(col.dz, 1), 0)
@@ -173,6 +172,18 @@ function CLM.soil_water!(col::CLM.ColumnData{<:Any,<:CuArray}, mask_hydrology, m
         check(ccall((:clmgb_soil_water, lib), Int32,
                     (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ref{SwmConfig}, Float64, Ptr{UInt32}, Ptr{Cvoid}),
                     handle(), b, f, c, dtime, C_NULL, CUDA.stream().handle), "clmgb_soil_water")
+    end
+    use_flexibleCN && flexible_cn!(col, mask_hydrology, wsb, b)
+    nothing
+end
+
+# soil_water!'s use_flexibleCN step (soil_water_movement.jl:1812-1843): clmgb_soil_water_flexible_cn
+function flexible_cn!(col, mask_hydrology, wsb, b::Bounds)
+    f = fields_buffer(Ptr{Cvoid}[ptr(mask_hydrology), ptr(col.dz), ptr(wsb.ws.h2osoi_liq_col),
+                                 ptr(wsb.ws.h2osoi_ice_col), ptr(wsb.ws.h2osoi_vol_col), ptr(wsb.ws.wa_col)])
+    GC.@preserve f begin
+        check(ccall((:clmgb_soil_water_flexible_cn, lib), Int32, (Ptr{Cvoid}, Ref{Bounds}, Ptr{UInt8}, Ptr{Cvoid}),
+                    handle(), b, f, CUDA.stream().handle), "clmgb_soil_water_flexible_cn")
     end
     nothing
 end
@@ -466,6 +477,71 @@ function column_balance_check!(errh2o::CuArray, col, wb, wf, wfb, forc_rain_col,
 end
 
 # ---------------------------------------------------------------------------
+# The batched solvers on CuArrays: batched_band_solve! (band_diagonal.jl:179) and
+# tridiagonal_multi! (tridiagonal.jl:129), and the pieces of their reverse rules
+# (CLMGB300ADExt): the forward that keeps its factorisation and the two adjoints.
+# jtop/jbot are the reference's Int vectors, mask its Bool vector (a CuArray{Bool} is
+# one byte per element).
+# ---------------------------------------------------------------------------
+function CLM.batched_band_solve!(tvector::CuArray{Float64,2}, bmatrix, rvector, jtop, jbot, mask,
+                                 kl::Int, ku::Int, nlevsno_off::Int)
+    nc, nlev = size(tvector)
+    check(ccall((:clmgb_batched_band_solve, lib), Int32,
+                (Ptr{Cvoid}, Int64, Int64, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+                 Ptr{Cvoid}, Int32, Int32, Int32, Ptr{Cvoid}),
+                handle(), nc, nc, nlev, ptr(tvector), ptr(bmatrix), ptr(rvector), ptr(jtop), ptr(jbot), ptr(mask),
+                kl, ku, nlevsno_off, CUDA.stream().handle), "clmgb_batched_band_solve")
+    nothing
+end
+
+function band_factor_solve!(tvector::CuArray{Float64,2}, bmatrix, rvector, jtop, jbot, mask, kl, ku, nlevsno_off,
+                            lu::CuArray{Float64,3}, piv::CuArray{UInt8,2})
+    nc, nlev = size(tvector)
+    check(ccall((:clmgb_batched_band_solve_factor, lib), Int32,
+                (Ptr{Cvoid}, Int64, Int64, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+                 Ptr{Cvoid}, Int32, Int32, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                handle(), nc, nc, nlev, ptr(tvector), ptr(bmatrix), ptr(rvector), ptr(jtop), ptr(jbot), ptr(mask),
+                kl, ku, nlevsno_off, ptr(lu), ptr(piv), CUDA.stream().handle), "clmgb_batched_band_solve_factor")
+    nothing
+end
+
+optptr(x) = x === nothing ? C_NULL : ptr(x)
+
+# lambda = A^-T tbar from the kept factors; rbar += lambda, bbar -= lambda x^T (band entries
+# the forward read); tbar consumed.  bbar / rbar may be `nothing` (inactive).
+function band_solve_adjoint!(x::CuArray{Float64,2}, tbar, lu, piv, bbar, rbar, jtop, jbot, mask, kl, ku, nlevsno_off)
+    nc, nlev = size(x)
+    check(ccall((:clmgb_batched_band_solve_adjoint, lib), Int32,
+                (Ptr{Cvoid}, Int64, Int64, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+                 Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int32, Int32, Int32, Ptr{Cvoid}),
+                handle(), nc, nc, nlev, ptr(x), ptr(tbar), ptr(lu), ptr(piv), optptr(bbar), optptr(rbar), ptr(jtop),
+                ptr(jbot), ptr(mask), kl, ku, nlevsno_off, CUDA.stream().handle), "clmgb_batched_band_solve_adjoint")
+    nothing
+end
+
+function CLM.tridiagonal_multi!(u::CuArray{Float64,2}, a, b, c, r, jtop, mask, ncols::Int, nlevs::Int)
+    check(ccall((:clmgb_tridiagonal_multi, lib), Int32,
+                (Ptr{Cvoid}, Int64, Int64, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+                 Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                handle(), ncols, size(u, 1), nlevs, ptr(u), ptr(a), ptr(b), ptr(c), ptr(r), ptr(jtop), ptr(mask),
+                CUDA.stream().handle), "clmgb_tridiagonal_multi")
+    nothing
+end
+
+# enzyme_rules.jl:160-201 per column: lambda = A^-T ubar by Thomas on the transposed bands,
+# rbar += lambda, bbar -= lambda u, abar -= lambda u[j-1], cbar -= lambda u[j+1]; ubar consumed.
+function tridiagonal_adjoint!(u::CuArray{Float64,2}, a, b, c, ubar, abar, bbar, cbar, rbar, jtop, mask,
+                              ncols::Int, nlevs::Int)
+    check(ccall((:clmgb_tridiagonal_adjoint, lib), Int32,
+                (Ptr{Cvoid}, Int64, Int64, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+                 Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                handle(), ncols, size(u, 1), nlevs, ptr(u), ptr(a), ptr(b), ptr(c), ptr(ubar), optptr(abar),
+                optptr(bbar), optptr(cbar), optptr(rbar), ptr(jtop), ptr(mask), CUDA.stream().handle),
+          "clmgb_tridiagonal_adjoint")
+    nothing
+end
+
+# ---------------------------------------------------------------------------
 # Reverse mode.  One column step's vector-Jacobian product (clmgb_column_step_vjp)
 # behind a ChainRulesCore.rrule and an Enzyme reverse rule, the counterparts of the
 # reference's _reverse_step_into! (canopy_fluxes_reverse.jl:447-465).  `StepState`
@@ -550,27 +626,12 @@ function column_step_vjp_logged!(ft_buf, fw_buf, b::Bounds, cfg::SwmConfig, dtim
     nothing
 end
 
-# ChainRulesCore: y = step(x, theta) on a snapshot of the state (the rule replays the
-# step from the snapshot, so the primal is not re-run by the caller).
-#   function ChainRulesCore.rrule(::typeof(CLM.column_step!), st::StepState, theta)
-#       x0 = snapshot(st)                       # device copy of the step's inputs
-#       CLM.column_step!(st, theta)
-#       function pullback(ybar)
-#           lam = adjoint_buffers(ybar); grad = zero_grads(st)
-#           restore!(st_scratch, x0)
-#           column_step_vjp!(fields(st_scratch)..., lam, grad)
-#           return NoTangent(), tangent_of_state(lam), grad
-#       end
-#       return st, pullback
-#   end
-# Enzyme: EnzymeRules.augmented_primal stores the same snapshot as its tape and
-# EnzymeRules.reverse calls column_step_vjp! with the shadow arrays as `lam`/`grad`,
-# exactly as enzyme_rules.jl does for band_solve! (augmented primal keeps A and x,
-# the reverse consumes the output shadow).
+# The ChainRulesCore rrule and the Enzyme rules built on these calls are in
+# CLMGB300ADExt.jl (a second extension, loaded with ChainRulesCore and Enzyme).
 
 # ---------------------------------------------------------------------------
 # Learned warm start: the first substep proposed by the perceptron (its weights are
-# trained by the library's kernels, see INTEGRATION.md), then soil_water! from it.
+# trained by the library's kernels: clmgb_mlp_*), then soil_water! from it.
 # ---------------------------------------------------------------------------
 function soil_water_warm!(fw_buf, b::Bounds, cfg::SwmConfig, dtime, dt_first::CuArray{Float64})
     GC.@preserve fw_buf begin

@@ -302,6 +302,20 @@ typedef struct clmgb_zd09_fields {
   double* qflx_deficit;              /* [nc]  W */
 } clmgb_zd09_fields;
 
+/* The use_flexibleCN branch of soil_water! (soil_water_movement.jl:1812-1843): after the
+ * solve, negative liquid water of soil levels 1..nlevsoi-1 is raised to watmin = 0.001 mm
+ * from the level below, that of level nlevsoi from the aquifer store wa, and h2osoi_vol
+ * is formed from liquid water and ice on levels 1..nlevsoi. */
+typedef struct clmgb_flexcn_fields {
+  int64_t struct_size;               /* sizeof(clmgb_flexcn_fields) */
+  const uint8_t* mask_hydrology;     /* [nc] */
+  const double* dz;                  /* [ldc, L] */
+  double* h2osoi_liq;                /* [ldc, L]  RW (soil part) */
+  const double* h2osoi_ice;          /* [ldc, L] */
+  double* h2osoi_vol;                /* [ldc, G]  W (levels 1..nlevsoi) */
+  double* wa;                        /* [nc]  RW: waterstatebulk.ws.wa_col */
+} clmgb_flexcn_fields;
+
 /* soil_fluxes! (soil_fluxes.jl:553-697): the surface fluxes corrected to the new ground
  * temperature, the evaporation partition, totals, outgoing longwave and the soil
  * energy balance error.  [np] patch vectors, [nc] column vectors, [nl] landunits. */
@@ -706,6 +720,12 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             this many ns; a warp with nothing to finish keeps looking for
                                             as long (0..1e7, default 0: index first, no lingering).  Results
                                             do not depend on it. */
+#define CLMGB_OPT_COUNT_WORK          21 /* 1: the work-queue Richards kernel with reserved scratch (packed
+                                            refresh) and its warp-per-column finish count, over the calls that
+                                            follow, the levels of every substep attempt and of every hydraulic
+                                            refresh (setting 1 zeroes the counts; 0 = off, the default) */
+#define CLMGB_OPT_WORK_LEVEL_ATTEMPTS 22 /* read-only (synchronises): that count of attempt levels */
+#define CLMGB_OPT_WORK_LEVEL_REFRESHES 23 /* read-only (synchronises): that count of refreshed levels */
 #define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls
                                             receive (default 0).  A caller that runs a column range [c0, c1)
                                             passes column arrays advanced by c0 (same ldc) and the patch
@@ -755,6 +775,12 @@ int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b,
 int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b,
                          const clmgb_soilwater_fields* f, const clmgb_swm_config* cfg,
                          double dtime, uint32_t* col_status, void* stream);
+
+/* The use_flexibleCN branch at the end of soil_water! (soil_water_movement.jl:1812-1843),
+ * one thread per hydrology column; a caller running soil_water! with use_flexibleCN calls
+ * it right after clmgb_soil_water (or clmgb_soil_water_zd09). */
+int32_t clmgb_soil_water_flexible_cn(clmgb_handle h, const clmgb_bounds* b, const clmgb_flexcn_fields* f,
+                                     void* stream);
 
 /* soil_fluxes! (soil_fluxes.jl:553-697) in its loop order: the ground temperature
  * change tinc (per column), the flux correction, evaporation partition and limit,

@@ -27,6 +27,7 @@
  *                                     :210-245, :341-451
  *   _soilwm_moisture_form_kernel!     src/biogeophys/soil_water_movement.jl:1250-1489
  *   compute_qcharge! after it         src/biogeophys/soil_water_movement.jl:1153-1215,1575-1598
+ *   soil_water!'s use_flexibleCN step src/biogeophys/soil_water_movement.jl:1812-1843
  *   tridiagonal_solve! / _tridiag_multi_kernel!  src/infrastructure/tridiagonal.jl:35-127
  *   tridiagonal_col!                  src/biogeophys/soil_water_movement.jl:736-773
  *   init_soil_properties!             src/infrastructure/cold_start.jl:225-391
@@ -3216,6 +3217,43 @@ static uint32_t moisture_form_col(const clmgb_varpar* vp, const clmgb_bounds* b,
 }
 
 /* ===================================================================== */
+/* The reference's scalar helpers of the moisture form, restated on one   */
+/* column's vectors (1-based j = index j-1 here):                         */
+/*   compute_RHS_moisture_form! (soil_water_movement.jl:1080-1102)        */
+/*   compute_LHS_moisture_form! (soil_water_movement.jl:1109-1140)        */
+/* The solve restates the same expressions fused into its attempt.        */
+/* ===================================================================== */
+void orc_compute_rhs_moisture_form(int32_t nlayers, const double* vert_trans_sink, const double* vwc_liq,
+                                   const double* qin, const double* qout, const double* dt_dz, double* rmx)
+{
+  (void)vwc_liq;
+  for (int j = 0; j < nlayers; j++) rmx[j] = 0.0;
+  for (int j = 0; j < nlayers; j++) {
+    const double fluxNet = qin[j] - qout[j] - vert_trans_sink[j];
+    rmx[j] = -fluxNet * dt_dz[j];
+  }
+}
+
+void orc_compute_lhs_moisture_form(int32_t nlayers, const double* dt_dz, const double* dqidw0,
+                                   const double* dqidw1, const double* dqodw1, const double* dqodw2,
+                                   double* amx, double* bmx, double* cmx)
+{
+  for (int j = 0; j < nlayers; j++) amx[j] = bmx[j] = cmx[j] = 0.0;
+  amx[0] = 0.0;
+  bmx[0] = -1.0 - (-dqidw1[0] + dqodw1[0]) * dt_dz[0];
+  cmx[0] = -dqodw2[0] * dt_dz[0];
+  for (int j = 1; j < nlayers - 1; j++) {
+    amx[j] = dqidw0[j] * dt_dz[j];
+    bmx[j] = -1.0 - (-dqidw1[j] + dqodw1[j]) * dt_dz[j];
+    cmx[j] = -dqodw2[j] * dt_dz[j];
+  }
+  const int j = nlayers - 1;
+  amx[j] = dqidw0[j] * dt_dz[j];
+  bmx[j] = -1.0 - (-dqidw1[j] + dqodw1[j]) * dt_dz[j];
+  cmx[j] = 0.0;
+}
+
+/* ===================================================================== */
 /* compute_qcharge! (soil_water_movement.jl:1153-1215) as                */
 /* soilwater_moisture_form! calls it after the solve when                */
 /* use_aquifer_layer(cfg) (:1575-1598): dwat, smp and imped are freshly  */
@@ -3261,6 +3299,44 @@ static void compute_qcharge_col(const clmgb_varpar* vp, const clmgb_bounds* b,
     q = jl_min(10.0 / dtime, q);
     f->qcharge[c] = q;
   }
+}
+
+/* ===================================================================== */
+/* The use_flexibleCN branch of soil_water! (soil_water_movement.jl:     */
+/* 1812-1843), loop by loop as the reference writes it (levels outer,    */
+/* columns inner); smooth_ifelse on Float64 is the exact branch          */
+/* (smooth_ad.jl:253-257).                                               */
+/* ===================================================================== */
+int orc_soil_water_flexible_cn(const clmgb_varpar* vp, const clmgb_bounds* b, const clmgb_flexcn_fields* f)
+{
+  const int64_t ld = b->ldc;
+  const int nlevsoi = vp->nlevsoi, joff = vp->nlevsno;
+  const double watmin = 0.001;
+  for (int j = 1; j <= nlevsoi - 1; j++) {
+    for (int64_t c = 0; c < b->nc; c++) {
+      if (!f->mask_hydrology[c]) continue;
+      const double l = IX(f->h2osoi_liq, c, joff + j, ld);
+      const double xs = l >= 0.0 ? 0.0 : watmin - l;
+      IX(f->h2osoi_liq, c, joff + j, ld) = l + xs;
+      IX(f->h2osoi_liq, c, joff + j + 1, ld) = IX(f->h2osoi_liq, c, joff + j + 1, ld) - xs;
+    }
+  }
+  for (int64_t c = 0; c < b->nc; c++) {
+    if (!f->mask_hydrology[c]) continue;
+    const double l = IX(f->h2osoi_liq, c, joff + nlevsoi, ld);
+    const double xs = (l - watmin) >= 0.0 ? 0.0 : watmin - l;
+    IX(f->h2osoi_liq, c, joff + nlevsoi, ld) = l + xs;
+    f->wa[c] = f->wa[c] - xs;
+  }
+  for (int j = 1; j <= nlevsoi; j++) {
+    for (int64_t c = 0; c < b->nc; c++) {
+      if (!f->mask_hydrology[c]) continue;
+      const double dzv = IX(f->dz, c, joff + j, ld);
+      IX(f->h2osoi_vol, c, j, ld) = IX(f->h2osoi_liq, c, joff + j, ld) / (dzv * DENH2O) +
+                                    IX(f->h2osoi_ice, c, joff + j, ld) / (dzv * DENICE);
+    }
+  }
+  return 0;
 }
 
 /* soilwater_moisture_form! (soil_water_movement.jl:1532-1601): the solve, then

@@ -58,6 +58,11 @@ def lib():
         L.orc_tridiagonal_adjoint_multi.argtypes = [C.c_int64, C.c_int64, C.c_int32] + [P] * 11 + [C.c_int32]
         L.orc_batched_band_solve_adjoint.argtypes = [C.c_int64, C.c_int64, C.c_int32] + [P] * 8 + \
             [C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+        L.orc_soil_water_flexible_cn.argtypes = [P, P, P]
+        L.orc_compute_rhs_moisture_form.argtypes = [C.c_int32] + [P] * 6
+        L.orc_compute_rhs_moisture_form.restype = None
+        L.orc_compute_lhs_moisture_form.argtypes = [C.c_int32] + [P] * 8
+        L.orc_compute_lhs_moisture_form.restype = None
         L.orc_set_perturbation.argtypes = [C.c_int32, C.c_double, C.c_uint64]
         L.orc_set_perturbation.restype = None
         _lib = L
@@ -258,3 +263,25 @@ def set_perturbation(mode=0, frac=0.0, salt=0):
     """The oracle's pow/log10 sensitivity hook (clm_oracle.c): 0 off, 1 every result
     +-1 ulp, 2 a fraction `frac` of them, 3 the previous single-precision-log library."""
     lib().orc_set_perturbation(int(mode), float(frac), int(salt))
+
+
+def soil_water_flexible_cn(fs):
+    """soil_water!'s use_flexibleCN step in place on a host FlexCnState."""
+    _chk(lib().orc_soil_water_flexible_cn(C.byref(fs.vp), C.byref(fs.bounds()), C.byref(fs.fields())))
+
+
+def compute_rhs_moisture_form(vert_trans_sink, vwc_liq, qin, qout, dt_dz):
+    """compute_RHS_moisture_form! on one column's vectors; returns rmx."""
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (vert_trans_sink, vwc_liq, qin, qout, dt_dz)]
+    rmx = np.empty(len(a[0]))
+    lib().orc_compute_rhs_moisture_form(len(rmx), *[_p(v) for v in a], _p(rmx))
+    return rmx
+
+
+def compute_lhs_moisture_form(dt_dz, dqidw0, dqidw1, dqodw1, dqodw2):
+    """compute_LHS_moisture_form! on one column's vectors; returns (amx, bmx, cmx)."""
+    a = [np.ascontiguousarray(v, dtype=np.float64) for v in (dt_dz, dqidw0, dqidw1, dqodw1, dqodw2)]
+    n = len(a[0])
+    amx, bmx, cmx = np.empty(n), np.empty(n), np.empty(n)
+    lib().orc_compute_lhs_moisture_form(n, *[_p(v) for v in a], _p(amx), _p(bmx), _p(cmx))
+    return amx, bmx, cmx

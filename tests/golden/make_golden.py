@@ -423,6 +423,24 @@ def main():
     cases["swm_config_defaults"] = dict(dtmin=60.0, verySmall=1.0e-8, xTolerUpper=1.0e-1, xTolerLower=1.0e-2,
                                         expensive=42, inexpensive=1, flux_calculation=1, e_ice=6.0,
                                         source="test/test_soil_water_movement.jl:18-31")
+    cases["rhs_moisture_form"] = dict(nlayers=3, vert_trans_sink=[0.1, 0.2, 0.05], vwc_liq=[0.3, 0.35, 0.25],
+                                      qin=[1.0, 0.8, 0.6], qout=[0.8, 0.6, 0.3], dt_dz=[0.01, 0.012, 0.008],
+                                      expect="rmx[j] = -(qin[j] - qout[j] - vert_trans_sink[j]) * dt_dz[j]",
+                                      atol=1e-15, source="test/test_soil_water_movement.jl:151-170")
+    cases["lhs_moisture_form"] = dict(nlayers=4, dt_dz=[0.01, 0.012, 0.008, 0.01], dqidw0=[0.0, 0.5, 0.4, 0.3],
+                                      dqidw1=[0.1, 0.2, 0.15, 0.12], dqodw1=[0.3, 0.25, 0.2, 0.18],
+                                      dqodw2=[0.4, 0.35, 0.28, 0.0],
+                                      expect="amx[1] = 0, amx[j] = dqidw0[j] dt_dz[j]; "
+                                             "bmx[j] = -1 - (-dqidw1[j] + dqodw1[j]) dt_dz[j]; "
+                                             "cmx[j] = -dqodw2[j] dt_dz[j], cmx[nlayers] = 0",
+                                      rtol=2.0 ** -26, source="test/test_soil_water_movement.jl:172-202")
+    # (method, lower BC, use_bedrock, raises) of init_soilwater_movement's checks
+    cases["init_soilwater_movement"] = dict(
+        default=dict(method=0, upper=1, lower=4),
+        checks=[[0, 1, False, True], [1, 1, False, False], [0, 4, True, True], [1, 2, True, False],
+                [0, 4, False, False]],
+        source="test/test_soil_water_movement.jl:207-256 (ZD09 = 0, MOISTURE_FORM = 1; BC_FLUX = 1, "
+               "BC_ZERO_FLUX = 2, BC_AQUIFER = 4)")
     # test/test_soil_water_movement.jl:272-336
     cases["moisture_form_conservation"] = dict(nc=12, nlev=10, nlevsno=5, dtime=1800.0, dz=0.05,
                                                watsat=0.45, hksat=0.02, bsw=5.0, sucsat=100.0,

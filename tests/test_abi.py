@@ -38,7 +38,8 @@ def test_header_structs_match_ctypes():
                           ("clmgb_surfhyd_fields", abi.SURFHYD_FIELDS),
                           ("clmgb_snowlayer_fields", abi.SNOWLAYER_FIELDS),
                           ("clmgb_lake_fields", abi.LAKE_FIELDS),
-                          ("clmgb_colbalance_fields", abi.COLBALANCE_FIELDS)):
+                          ("clmgb_colbalance_fields", abi.COLBALANCE_FIELDS),
+                          ("clmgb_flexcn_fields", abi.FLEXCN_FIELDS)):
         members = abi.header_struct_members(txt, sname)
         assert members[0] == "struct_size"
         assert members[1:] == [f[0] for f in fields], sname
@@ -60,7 +61,8 @@ def test_header_constants_match_python():
                  "OPT_ADJ_TAPE_ENTRIES", "OPT_STEP_SCHEDULE", "OPT_WAVES_OCCUPANCY", "OPT_ADJ_RICHARDS",
                  "ADJ_RICHARDS_CLOSED_FORM", "ADJ_RICHARDS_RECORDED", "COL_ADJ_REPLAY", "ADJ_MAX_SUBSTEPS",
                  "OPT_ADJ_SOIL_TEMPERATURE", "ADJ_ST_CLOSED_FORM", "ADJ_ST_RECORDED", "OPT_QUEUE_FRESH_BATCH", "OPT_COLUMN_BASE", "OPT_QUEUE_DEFER",
-                 "COL_FILTER"):
+                 "COL_FILTER", "OPT_ATTEMPT_CAP", "OPT_QUEUE_POLL_LIMIT", "OPT_QUEUE_PUBLISH_DELAY",
+                 "OPT_COUNT_WORK", "OPT_WORK_LEVEL_ATTEMPTS", "OPT_WORK_LEVEL_REFRESHES", "COL_QUEUE_WAIT"):
         assert int(consts[name]) == getattr(abi, name), name
     for name in ("SH_FLOODC", "SH_SAT_EXCESS", "SH_QFLX_INPUTS", "SH_INFL_EXCESS", "SH_ROUTE", "SH_UPDATE_H2OSFC",
                  "SH_INFILTRATION", "SH_TOTAL_RUNOFF", "SH_URBAN_PONDING", "SH_ALL", "FSAT_TOPMODEL", "FSAT_VIC",

@@ -295,3 +295,50 @@ def test_oracle_root_sink_filter_error():
     case["col_itype"] = [75]
     rs = RC.build(g, case)
     assert O.rootsink(rs, False) == 1
+
+
+def test_rhs_moisture_form_known_answer():
+    """compute_RHS_moisture_form! (test_soil_water_movement.jl:151-170)."""
+    g = G["rhs_moisture_form"]
+    rmx = orc.compute_rhs_moisture_form(g["vert_trans_sink"], g["vwc_liq"], g["qin"], g["qout"], g["dt_dz"])
+    for j in range(g["nlayers"]):
+        fluxnet = g["qin"][j] - g["qout"][j] - g["vert_trans_sink"][j]
+        assert abs(rmx[j] - (-fluxnet * g["dt_dz"][j])) <= g["atol"]
+
+
+def test_lhs_moisture_form_known_answer():
+    """compute_LHS_moisture_form! (test_soil_water_movement.jl:172-202), the same
+    expressions the solve forms for its matrix (soil_water_movement.jl:1380-1397)."""
+    g = G["lhs_moisture_form"]
+    n, dt, d0, d1, o1, o2 = (g[k] for k in ("nlayers", "dt_dz", "dqidw0", "dqidw1", "dqodw1", "dqodw2"))
+    amx, bmx, cmx = orc.compute_lhs_moisture_form(dt, d0, d1, o1, o2)
+    rt = g["rtol"]
+    assert amx[0] == 0.0 and cmx[n - 1] == 0.0
+    for j in range(n):
+        assert bmx[j] == pytest.approx(-1.0 - (-d1[j] + o1[j]) * dt[j], rel=rt)
+        if j > 0:
+            assert amx[j] == pytest.approx(d0[j] * dt[j], rel=rt)
+        if j < n - 1:
+            assert cmx[j] == pytest.approx(-o2[j] * dt[j], rel=rt)
+
+
+def test_init_soilwater_movement_checks():
+    """init_soilwater_movement's defaults and consistency checks, the use_bedrock one
+    included (test_soil_water_movement.jl:207-256)."""
+    from clmgb import api
+    g = G["init_soilwater_movement"]
+    cfg = api.init_soilwater_movement()
+    d = g["default"]
+    assert (cfg.soilwater_movement_method, cfg.upper_boundary_condition, cfg.lower_boundary_condition) == \
+        (d["method"], d["upper"], d["lower"])
+    assert cfg.dtmin == 60.0 and cfg.e_ice == 6.0 and cfg.flux_calculation == 1
+    for method, lower, bedrock, raises in g["checks"]:
+        if raises:
+            with pytest.raises(api.CLMGBError) as e:
+                api.init_soilwater_movement(use_bedrock=bedrock, soilwater_movement_method=method,
+                                            lower_boundary_condition=lower)
+            assert e.value.code == abi.CLMGB_ERR_CONFIG
+        else:
+            c = api.init_soilwater_movement(use_bedrock=bedrock, soilwater_movement_method=method,
+                                            lower_boundary_condition=lower)
+            assert c.lower_boundary_condition == lower
