@@ -147,10 +147,11 @@ __device__ __forceinline__ AD cm_pow(const AD& x, const AD& y) {
   const double py = (y.i >= 0 && x.v > 0.0) ? r * ::cm_log(x.v) : 0.0;
   return ad_binary(r, x, px, y, py);
 }
-// x^y for a constant base x with log x = lx + lxl formed by the caller: d/dy = r lx
+// x^y for a constant base x with log x = lx + lxl formed by the caller (a pair that is
+// not renormalised: lx alone can be off by 2^-20): d/dy = r log x
 __device__ __forceinline__ AD cm_pow_lx(double x, double lx, double lxl, const AD& y) {
   const double r = ::cm_pow_lx(x, lx, lxl, y.v);
-  return ad_unary(r, y, r * lx);
+  return ad_unary(r, y, r * (lx + lxl));
 }
 __device__ __forceinline__ AD cm_log10(const AD& x) {
   return ad_unary(::cm_log10(x.v), x, 0.43429448190325182765 / x.v);
