@@ -87,6 +87,9 @@ LOG_REC = MAX_NLEVSOI + 2
 LOG_FIN = 3 * MAX_NLEVSOI + 3
 
 
+LOG_ST_STRIDE = 464        # doubles of a column's soil_temperature! record
+
+
 def log_stride(cap):
     """Doubles per column of a substep log with `cap` records (CLMGB_LOG_STRIDE)."""
     return cap * LOG_REC + LOG_FIN
@@ -654,7 +657,7 @@ FlexCnFields = _mk_struct("FlexCnFields", FLEXCN_FIELDS)
 class SubstepLog(C.Structure):
     """clmgb_substep_log."""
     _fields_ = [("struct_size", C.c_int64), ("rec", c_double_p), ("count", C.POINTER(C.c_int32)),
-                ("cap", C.c_int32)]
+                ("cap", C.c_int32), ("st_rec", c_double_p)]
 
 
 def all_fields():

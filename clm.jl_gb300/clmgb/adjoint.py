@@ -127,7 +127,7 @@ def synth_forcing_reverse(t, before, adj):
 
 
 def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_status=None, events=None,
-                      log_cap=24):
+                      log_cap=24, log_soil_temperature=True):
     """Forward through traj from `state` (left holding the final state), keeping a
     checkpoint every `checkpoint_every` steps; then reverse, recomputing each segment's
     step-entry states from its checkpoint.  observe(t, state_after_t) runs after every
@@ -135,14 +135,17 @@ def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_s
     at the start, between the forward and the reverse pass, and at the end.  The
     recomputed steps, and the last step of every segment in the forward pass, write
     substep logs (`log_cap` records per column; 0: no logs) so that no reverse runs the
-    Richards substep loop again.  Returns the adjoint buffers."""
+    Richards substep loop again, and with `log_soil_temperature` the soil_temperature!
+    records too, so that no reverse runs soil_temperature! again.  Returns the adjoint
+    buffers."""
     k = max(1, int(checkpoint_every))
     if events is not None:
         events[0].record()
     ckpt = []
     nseg = (traj.nsteps + k - 1) // k
     # the last step of a segment is not recomputed: the forward pass logs it
-    last_logs = [api.SubstepLog(state.nc, log_cap) for _ in range(nseg)] if log_cap > 0 else []
+    mklog = lambda: api.SubstepLog(state.nc, log_cap, soil_temperature=log_soil_temperature)  # noqa: E731
+    last_logs = [mklog() for _ in range(nseg)] if log_cap > 0 else []
     for t in range(traj.nsteps):
         if t % k == 0:
             ckpt.append(state.copy())
@@ -154,7 +157,7 @@ def multistep_reverse(traj, state, seed, observe=None, checkpoint_every=8, col_s
         events[1].record()
     adj = StepAdjointBuffers(state)
     seg_states = [state.copy() for _ in range(min(k, traj.nsteps))]
-    logs = [api.SubstepLog(state.nc, log_cap) for _ in range(min(k, traj.nsteps) - 1)] if log_cap > 0 else []
+    logs = [mklog() for _ in range(min(k, traj.nsteps) - 1)] if log_cap > 0 else []
     for s in range(len(ckpt) - 1, -1, -1):
         t0, t1 = s * k, min((s + 1) * k, traj.nsteps)
         copy_state_(seg_states[0], ckpt[s])

@@ -151,13 +151,17 @@ def column_step(handle, state, dtime, cfg=None, snow_method=abi.SNOW_JORDAN1991,
 
 
 class SubstepLog:
-    """Device buffers of a clmgb_substep_log for `nc` columns, `cap` records each."""
+    """Device buffers of a clmgb_substep_log for `nc` columns, `cap` records each; with
+    `soil_temperature` (default) also the soil_temperature! records (st_rec), so the
+    reverse runs neither the Richards substep loop nor soil_temperature! again."""
 
-    def __init__(self, nc, cap=24, device="cuda"):
+    def __init__(self, nc, cap=24, device="cuda", soil_temperature=True):
         import torch
         self.nc, self.cap = int(nc), int(cap)
         self.rec = torch.empty(self.nc * abi.log_stride(self.cap), dtype=torch.float64, device=device)
         self.count = torch.full((self.nc,), -1, dtype=torch.int32, device=device)
+        self.st_rec = (torch.empty(self.nc * abi.LOG_ST_STRIDE, dtype=torch.float64, device=device)
+                       if soil_temperature else None)
 
     def struct(self):
         s = abi.SubstepLog()
@@ -165,6 +169,8 @@ class SubstepLog:
         s.rec = C.cast(C.c_void_p(self.rec.data_ptr()), abi.c_double_p)
         s.count = C.cast(C.c_void_p(self.count.data_ptr()), C.POINTER(C.c_int32))
         s.cap = self.cap
+        if self.st_rec is not None:
+            s.st_rec = C.cast(C.c_void_p(self.st_rec.data_ptr()), abi.c_double_p)
         return s
 
 

@@ -46,11 +46,16 @@ namespace clmgb {
 
 constexpr int CF_BLOCK = 64;
 
+// The factorisation of the column's band system: lu/x/piv point at the thread's own
+// storage (soil_temperature! run here) or at the column's soil_temperature! record.
 struct CfBand {
   int n;
-  double lu[MAXROWS * 7];
-  double x[MAXROWS];
-  uint8_t piv[MAXROWS];
+  const double* lu;
+  const double* x;
+  const uint8_t* piv;
+  double lu_s[MAXROWS * 7];
+  double x_s[MAXROWS];
+  uint8_t piv_s[MAXROWS];
 };
 
 // The column's active state in per-thread storage, values only.
@@ -77,10 +82,13 @@ struct CfState {
   __device__ __forceinline__ double Hksat(int j) const { return LVc(ks, c, j, ld); }
   // the production factorisation, keeping the factors, pivots and solution
   __device__ __forceinline__ void band_solve(double* ab, double* x, int n) {
-    band_lu_factor_solve<2, 2>(ab, x, band->piv, n);
+    band_lu_factor_solve<2, 2>(ab, x, band->piv_s, n);
     band->n = n;
-    for (int k = 0; k < n * 7; k++) band->lu[k] = ab[k];
-    for (int r = 0; r < n; r++) band->x[r] = x[r];
+    for (int k = 0; k < n * 7; k++) band->lu_s[k] = ab[k];
+    for (int r = 0; r < n; r++) band->x_s[r] = x[r];
+    band->lu = band->lu_s;
+    band->x = band->x_s;
+    band->piv = band->piv_s;
   }
 };
 
@@ -872,13 +880,31 @@ k_column_step_vjp_cf(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwat
     V.forc = ft.forc_lwrad[c];
     V.qc = fw.qcharge[c];
     const double tg0 = V.tg, th0 = V.th;
-    // ---- soil_temperature! ----
+    // ---- soil_temperature!: run here, or its record read from the log ----
     bool st_full = false;
     if (do_t) {
       if (t_ssbef)
         for (int jj = 1; jj <= nlev; jj++) LV(t_ssbef, c, jj, ld) = V.t[jj];
       if (t_h2osfc_bef) t_h2osfc_bef[c] = V.th;
-      const uint32_t s1 = soil_temperature_col(D, ft, c, dtime, snow_method, V);
+      uint32_t s1;
+      if (lg.st) {
+        const double* rec = lg.st + c * (int64_t)CLMGB_LOG_ST_STRIDE;
+        s1 = (uint32_t)rec[ST_STATUS];
+        band.n = (int)rec[ST_N];
+        band.lu = rec + ST_LU;
+        band.x = rec + ST_X;
+        band.piv = reinterpret_cast<const uint8_t*>(rec + ST_PIV);
+        for (int jj = jjtop; jj <= nlev; jj++) V.t[jj] = rec[ST_T + jj - 1];
+        for (int jj = jjtop; jj <= nw; jj++) {
+          V.liq[jj] = rec[ST_LIQ + jj - 1];
+          V.ice[jj] = rec[ST_ICE + jj - 1];
+          V.fact[jj] = rec[ST_FACT + jj - 1];
+        }
+        V.tg = rec[ST_TG];
+        V.th = rec[ST_TH];
+      } else {
+        s1 = soil_temperature_col(D, ft, c, dtime, snow_method, V);
+      }
       st |= s1;
       st_full = !(s1 & (CLMGB_COL_URBAN | CLMGB_COL_PATCH_RANGE | CLMGB_COL_LEVEL_RANGE)) && band.n > 0;
     }

@@ -5,6 +5,7 @@
 // fallback.  Device-side per-column conditions are OR-ed into the handle's status
 // word, read back with clmgb_device_status().
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <string.h>
 #include <initializer_list>
@@ -1008,17 +1009,25 @@ int32_t clmgb_reserve_adjoint(clmgb_handle h, int64_t slots, int64_t entries) {
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
+// the size of clmgb_substep_log before st_rec was appended
+static constexpr int64_t LOG_SIZE_NO_ST = (int64_t)offsetof(clmgb_substep_log, st_rec);
+
 static int32_t check_log(const clmgb_substep_log* log) {
   if (!log) return CLMGB_OK;
-  if (log->struct_size != (int64_t)sizeof(clmgb_substep_log)) return CLMGB_ERR_ABI;
+  if (log->struct_size != (int64_t)sizeof(clmgb_substep_log) && log->struct_size != LOG_SIZE_NO_ST)
+    return CLMGB_ERR_ABI;
   if (!log->rec || !log->count) return CLMGB_ERR_NULL_ARG;
   if (log->cap < 1 || log->cap > CLMGB_ADJ_MAX_SUBSTEPS) return CLMGB_ERR_CONFIG;
   return CLMGB_OK;
 }
 
+static double* log_st(const clmgb_substep_log* log) {
+  return (log && log->struct_size >= (int64_t)sizeof(clmgb_substep_log)) ? log->st_rec : nullptr;
+}
+
 static clmgb::SubstepLogView log_view(const clmgb_substep_log* log) {
-  if (!log) return clmgb::SubstepLogView{nullptr, nullptr, 0, 0};
-  return clmgb::SubstepLogView{log->rec, log->count, (int)log->cap, CLMGB_LOG_STRIDE(log->cap)};
+  if (!log) return clmgb::SubstepLogView{nullptr, nullptr, 0, 0, nullptr};
+  return clmgb::SubstepLogView{log->rec, log->count, (int)log->cap, CLMGB_LOG_STRIDE(log->cap), log_st(log)};
 }
 
 int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
@@ -1039,7 +1048,7 @@ int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const cl
   const Dims D = hdims(h, *b);
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce = clmgb::launch_soiltemp_fractions(D, b->nc, *ft, *fw, dtime, snow_method, t_ssbef, t_h2osfc_bef,
-                                                    col_status, h->dev_status, s);
+                                                    col_status, h->dev_status, s, log_st(log));
   if (ce == cudaSuccess) {
     const clmgb::SubstepLogView lv = log_view(log);
     ce = clmgb::launch_moisture_form_queue(D, b->nc, *fw, *cfg, dtime, col_status, 1, h->dev_status, h->queue,

@@ -99,12 +99,31 @@ k_column_step(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fiel
   report(st, col_status, dev_status, c);
 }
 
+// The production state accessor whose band solve also keeps the factorisation in the
+// column's soil_temperature! record (StLog); the solution is band_lu_solve's bits.
+struct FieldStateStLog : FieldState<clmgb_soiltemp_fields> {
+  double* rec;
+  __device__ __forceinline__ FieldStateStLog(const clmgb_soiltemp_fields& ff, int64_t cc, int64_t l, double* r)
+      : FieldState<clmgb_soiltemp_fields>(ff, cc, l), rec(r) {}
+  __device__ __forceinline__ void band_solve(double* ab, double* x, int n) const {
+    uint8_t piv[MAXROWS];
+    band_lu_factor_solve<2, 2>(ab, x, piv, n);
+    rec[ST_N] = (double)n;
+    for (int k = 0; k < n * 7; k++) rec[ST_LU + k] = ab[k];
+    for (int r = 0; r < n; r++) rec[ST_X + r] = x[r];
+    uint8_t* pv = reinterpret_cast<uint8_t*>(rec + ST_PIV);
+    for (int r = 0; r < n; r++) pv[r] = piv[r];
+  }
+};
+
 // soil_temperature! then set_soil_water_fractions! for one column per thread (the
 // first half of a column step; the Richards solve follows in k_moisture_form_queue).
+// With LOG every column soil_temperature! runs on also gets its record in st_log.
+template <bool LOG>
 __global__ void __launch_bounds__(BLOCK)
 k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw,
                              double dtime, int snow_method, double* t_ssbef, double* t_h2osfc_bef,
-                             uint32_t* col_status, uint32_t* dev_status) {
+                             uint32_t* col_status, uint32_t* dev_status, double* st_log) {
   const int64_t c = snl_sorted_column(nc, ft.col_snl, D.nlevsno);
   if (c < 0) return;
   uint32_t st = 0;
@@ -114,7 +133,29 @@ k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb
       for (int jj = 1; jj <= L; jj++) LV(t_ssbef, c, jj, D.ldc) = LV(ft.t_soisno, c, jj, D.ldc);
     }
     if (t_h2osfc_bef) t_h2osfc_bef[c] = ft.t_h2osfc[c];
-    st |= soil_temperature_col(D, ft, c, dtime, snow_method);
+    if (LOG) {
+      double* rec = st_log + c * (int64_t)CLMGB_LOG_ST_STRIDE;
+      rec[ST_N] = 0.0;
+      FieldStateStLog X(ft, c, D.ldc, rec);
+      const uint32_t s1 = soil_temperature_col(D, ft, c, dtime, snow_method, X);
+      st |= s1;
+      rec[ST_STATUS] = (double)s1;
+      const int64_t snl = ft.col_snl[c];
+      if (snl <= 0 && snl >= -D.nlevsno) {     // the levels the call may have changed
+        const int jjtop = (int)snl + 1 + D.nlevsno;
+        const int nw = D.nlevsno + D.nlevgrnd, nlev = D.nlevsno + D.nlevmax;
+        for (int jj = jjtop; jj <= nlev; jj++) rec[ST_T + jj - 1] = LV(ft.t_soisno, c, jj, D.ldc);
+        for (int jj = jjtop; jj <= nw; jj++) {
+          rec[ST_LIQ + jj - 1] = LV(ft.h2osoi_liq, c, jj, D.ldc);
+          rec[ST_ICE + jj - 1] = LV(ft.h2osoi_ice, c, jj, D.ldc);
+          rec[ST_FACT + jj - 1] = LV(ft.fact, c, jj, D.ldc);
+        }
+      }
+      rec[ST_TG] = ft.t_grnd[c];
+      rec[ST_TH] = ft.t_h2osfc[c];
+    } else {
+      st |= soil_temperature_col(D, ft, c, dtime, snow_method);
+    }
   }
   if (fw.mask_hydrology[c]) water_fractions_col(D, fw, c);
   report(st, col_status, dev_status, c);
@@ -900,9 +941,13 @@ cudaError_t launch_column_step(const Dims& D, int64_t nc, const clmgb_soiltemp_f
 cudaError_t launch_soiltemp_fractions(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
                                       const clmgb_soilwater_fields& fw, double dtime, int snow_method,
                                       double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
-                                      uint32_t* dev_status, cudaStream_t s) {
-  k_soil_temperature_fractions<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, dtime, snow_method, t_ssbef,
-                                                              t_h2osfc_bef, col_status, dev_status);
+                                      uint32_t* dev_status, cudaStream_t s, double* st_log) {
+  if (st_log)
+    k_soil_temperature_fractions<true><<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, dtime, snow_method, t_ssbef,
+                                                                      t_h2osfc_bef, col_status, dev_status, st_log);
+  else
+    k_soil_temperature_fractions<false><<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, dtime, snow_method, t_ssbef,
+                                                                       t_h2osfc_bef, col_status, dev_status, nullptr);
   return cudaGetLastError();
 }
 int queue_blocks_per_sm() {

@@ -77,13 +77,33 @@ struct AdjTape {
 // of `stride` doubles at rec + c*stride holding up to `cap` records of SUB_REC
 // doubles (the liquid water at the start of an accepted substep, its dtsub and the
 // time done before it) followed by the solve's outputs; count[c] = accepted
-// substeps (-1: the column was not solved).  rec == nullptr: no log.
+// substeps (-1: the column was not solved).  rec == nullptr: no log.  st, when not
+// null, holds per column CLMGB_LOG_ST_STRIDE doubles of soil_temperature! (StLog).
 struct SubstepLogView {
   double* rec;
   int32_t* count;
   int cap;
   int64_t stride;
+  double* st;
 };
+
+// The soil_temperature! record of a column (clmgb_substep_log::st_rec): the band
+// system's size n, the status of the call, t_grnd and t_h2osfc after it, then
+// temperature, liquid water, ice and fact after it (index jj-1 of level jj), the
+// solution x, the factors (n rows of 7, band_lu_factor_solve's layout) and the row
+// exchanges (one byte each).
+enum StLog {
+  ST_N = 0, ST_STATUS = 1, ST_TG = 2, ST_TH = 3,
+  ST_T = 4,
+  ST_LIQ = ST_T + CLMGB_MAX_NLEVSNO + CLMGB_MAX_NLEVGRND,
+  ST_ICE = ST_LIQ + CLMGB_MAX_NLEVSNO + CLMGB_MAX_NLEVGRND,
+  ST_FACT = ST_ICE + CLMGB_MAX_NLEVSNO + CLMGB_MAX_NLEVGRND,
+  ST_X = ST_FACT + CLMGB_MAX_NLEVSNO + CLMGB_MAX_NLEVGRND,
+  ST_LU = ST_X + CLMGB_MAX_NLEVSNO + CLMGB_MAX_NLEVGRND + 1,
+  ST_PIV = ST_LU + 7 * (CLMGB_MAX_NLEVSNO + CLMGB_MAX_NLEVGRND + 1),
+  ST_END = ST_PIV + (CLMGB_MAX_NLEVSNO + CLMGB_MAX_NLEVGRND + 1 + 7) / 8
+};
+static_assert(ST_END <= CLMGB_LOG_ST_STRIDE, "soil_temperature! record exceeds CLMGB_LOG_ST_STRIDE");
 
 // fields of QueueScratch::pcache: dz*1000, watsat, bsw, hksat, sucsat, the ice
 // impedance, 1000*(z[j+1]-z[j]) (levels below the bottom one) and qflx_rootsoi
@@ -122,10 +142,11 @@ cudaError_t launch_synth_forcing(const Dims& D, int64_t nc, const clmgb_soiltemp
                                  const clmgb_soilwater_fields& fw, const double* G, const double* I,
                                  cudaStream_t s);
 
+// st_log (optional): the soil_temperature! records of a substep log (StLog)
 cudaError_t launch_soiltemp_fractions(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
                                       const clmgb_soilwater_fields& fw, double dtime, int snow_method,
                                       double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
-                                      uint32_t* dev_status, cudaStream_t s);
+                                      uint32_t* dev_status, cudaStream_t s, double* st_log = nullptr);
 int queue_blocks_per_sm();
 cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                        const clmgb_swm_config& cfg, double dtime, uint32_t* col_status,

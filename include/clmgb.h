@@ -1004,16 +1004,24 @@ int32_t clmgb_column_step_vjp(clmgb_handle h, const clmgb_bounds* b, const clmgb
  * its dtsub, the time done before it), then CLMGB_LOG_FIN doubles of the solve's
  * outputs (final liquid water, smp_l, hk_l, qcharge, attempts, status).  count[c]
  * (int32, [nc]) gets the accepted substeps, -1 for a column that was not solved; a
- * column with more than cap is reversed by running its substep loop again.  No
- * counterpart in the reference (Enzyme keeps its own tape). */
+ * column with more than cap is reversed by running its substep loop again.
+ * st_rec, when given, gets per column c CLMGB_LOG_ST_STRIDE doubles at
+ * st_rec + c*CLMGB_LOG_ST_STRIDE of soil_temperature!: the factorisation of its band
+ * system (factors, row exchanges, solution) and the column state the call left
+ * (temperature, liquid water, ice, fact, t_grnd, t_h2osfc, status); the reverse then
+ * does not run soil_temperature! again either.  Results are the same bits with or
+ * without it.  No counterpart in the reference (Enzyme keeps its own tape).
+ * struct_size may also be the size without the appended st_rec member. */
 #define CLMGB_LOG_REC (CLMGB_MAX_NLEVSOI + 2)
 #define CLMGB_LOG_FIN (3 * CLMGB_MAX_NLEVSOI + 3)
 #define CLMGB_LOG_STRIDE(cap) ((int64_t)(cap) * CLMGB_LOG_REC + CLMGB_LOG_FIN)
+#define CLMGB_LOG_ST_STRIDE 464
 typedef struct clmgb_substep_log {
   int64_t struct_size;               /* sizeof(clmgb_substep_log) */
   double* rec;                       /* [nc * CLMGB_LOG_STRIDE(cap)] */
   int32_t* count;                    /* [nc] */
   int32_t cap;                       /* records per column, 1..CLMGB_ADJ_MAX_SUBSTEPS */
+  double* st_rec;                    /* [nc * CLMGB_LOG_ST_STRIDE] or NULL */
 } clmgb_substep_log;
 
 /* clmgb_column_step that also writes the substep log (the Richards solve runs on the

@@ -453,7 +453,7 @@ def test_closed_form_step_adjoint_matches_recorded(handle, cfg_id, method, bc):
 def test_substep_log_gives_the_same_bits(handle):
     """The reverse reading the substep log of the recomputed forward, running the
     substep loop itself (no log), or mixing both (a log too small for some columns)
-    gives the same bits."""
+    gives the same bits, with and without the soil_temperature! records."""
     cfg = _cfg_flux()
     nsteps = 6
     wl, G, I = _workload(384, nsteps, seed=808)
@@ -461,12 +461,13 @@ def test_substep_log_gives_the_same_bits(handle):
     st0 = wl.state.to_device()
     lin = _LinearSeed(st0, nsteps, 3)
     res = {}
-    for cap in (0, 24, 2):
-        adj = adjoint.multistep_reverse(traj, st0.copy(), lin.seed, None, checkpoint_every=3, log_cap=cap)
-        res[cap] = _adjoint_arrays(adj)
-    for cap in (24, 2):
-        for k in res[0]:
-            assert torch.equal(res[0][k], res[cap][k]), (cap, k)
+    for cap, stlog in ((0, False), (24, True), (24, False), (2, True)):
+        adj = adjoint.multistep_reverse(traj, st0.copy(), lin.seed, None, checkpoint_every=3, log_cap=cap,
+                                        log_soil_temperature=stlog)
+        res[cap, stlog] = _adjoint_arrays(adj)
+    for key in ((24, True), (24, False), (2, True)):
+        for k in res[0, False]:
+            assert torch.equal(res[0, False][k], res[key][k]), (key, k)
 
 
 def test_logged_step_is_the_production_step(handle):
@@ -495,3 +496,17 @@ def test_logged_step_is_the_production_step(handle):
         hydt = torch.from_numpy(hyd).cuda()
         assert torch.equal(fin[hydt, :nl].T.contiguous(), b["h2osoi_liq"][j0:j0 + nl][:, hydt])
         assert torch.equal(fin[hydt, 3 * abi.MAX_NLEVSOI], b["qcharge"][hydt])
+        # the soil_temperature! record: the state the call left (the Richards solve
+        # changes neither temperature, ice, fact nor t_grnd), the band size and status
+        srec = log.st_rec.view(a.nc, abi.LOG_ST_STRIDE)
+        act = torch.from_numpy(b["mask_nolakec"].cpu().numpy() != 0).cuda()
+        snl = b["col_snl"].cpu().numpy()
+        nw = a.vp.nlevsno + a.vp.nlevgrnd
+        nL = abi.MAX_NLEVSNO + abi.MAX_NLEVGRND
+        assert torch.equal(srec[act, 2], b["t_grnd"][act]) and torch.equal(srec[act, 3], b["t_h2osfc"][act])
+        assert torch.all(srec[act, 1] == 0)
+        for c in np.nonzero(act.cpu().numpy())[0][::7]:
+            jt = int(snl[c]) + j0          # 0-based top level
+            for off, k in ((4, "t_soisno"), (4 + 2 * nL, "h2osoi_ice"), (4 + 3 * nL, "fact")):
+                assert torch.equal(srec[c, off + jt:off + nw], b[k][jt:nw, c]), (t, c, k)
+            assert int(srec[c, 0]) == nw - jt + 1          # snow + ground levels + the surface-water row
