@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--queue-order", type=int, default=None)
     ap.add_argument("--fresh-batch", type=int, default=None, help="CLMGB_OPT_QUEUE_FRESH_BATCH override")
     ap.add_argument("--defer", type=int, default=None, help="CLMGB_OPT_QUEUE_DEFER override")
+    ap.add_argument("--records-tma", type=int, default=None, choices=[0, 1],
+                    help="CLMGB_OPT_RECORDS_TMA override (tensor copies or plain loads in the Richards pre-pass)")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint calibration leg")
     ap.add_argument("--adjoint-only", action="store_true",
@@ -80,6 +82,16 @@ def parse():
     ap.add_argument("--warm-eval-steps", type=int, default=20)
     ap.add_argument("--warm-epochs", type=int, default=3)
     return ap.parse_args()
+
+
+def richards_launch_count(h, nc):
+    """This library's kernels in one clmgb_soil_water call under the handle's schedule."""
+    from clmgb import abi
+    if h.get_option(abi.OPT_STEP_SCHEDULE) == abi.SCHEDULE_QUEUE and h.get_option(abi.OPT_RESERVED_COLUMNS) >= nc:
+        order = 3 if h.get_option(abi.OPT_QUEUE_ORDER) == 1 else 0
+        packed = h.get_option(abi.OPT_QUEUE_PACKED_REFRESH) == 1
+        return 1 + order + 1 + (1 if packed else 0)
+    return 1
 
 
 def shard_seed(cfg_id, rank):
@@ -418,14 +430,48 @@ def warm_leg(args, wl_eval):
     es, eh = api.balance_residuals(h, s2, wl_eval.dtime, tg0, bw)
     warm_balance = {"errsoi_max_abs_w_m2": float(es.abs().max()), "errh2o_max_abs_mm": float(eh.abs().max())}
     del s2
-    # ---- error against the FP64 oracle on a sample of columns ----
+    # ---- the proposal's share of the warm-started step ----
+    s2 = wl_eval.state.to_device()
+    api.synth_forcing(h, s2, G[0], I[0])
+    api.soil_temperature(h, s2, wl_eval.dtime)
+    api.set_soil_water_fractions(h, s2)
+    dtv = torch.empty(s2.nc, dtype=torch.float64, device="cuda")
+    X = torch.empty((s2.nc, mlp.IN), dtype=torch.bfloat16, device="cuda")
+    b, fw = s2.bounds(), s2.soilwater_fields()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        model.propose_first_dt(s2, wl_eval.dtime, cfg, out=dtv)
+    reps = 10
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        model.propose_first_dt(s2, wl_eval.dtime, cfg, out=dtv)
+    e1.record()
+    torch.cuda.synchronize()
+    prop_ms = e0.elapsed_time(e1) / reps
+    model.features(s2, wl_eval.dtime, cfg, out=X)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        model.forward(X)
+    e1.record()
+    torch.cuda.synchronize()
+    layers_ms = e0.elapsed_time(e1) / reps
+    del s2, X
+    # ---- error against the FP64 oracle on a sample of columns, and of both arms
+    #      against a converged solution (the oracle with both tolerances / 100) ----
     from oracle import oracle as orc
     cols = np.linspace(0, wl_eval.state.nc - 1, 256).astype(np.int64)
     sub = wl_eval.state.subset(cols)
     ref = sub.copy()
     Gh, Ih = G.cpu().numpy()[:, cols], I.cpu().numpy()[:, cols]
     orc.run_steps(ref, wl_eval.dtime, Gh[:ne + 2], Ih[:ne + 2], cfg)
-    errs = {}
+    conv_cfg = abi.SwmConfig.clm5_default()
+    conv_cfg.xTolerUpper = cfg.xTolerUpper / 100.0
+    conv_cfg.xTolerLower = cfg.xTolerLower / 100.0
+    conv = sub.copy()
+    orc.run_steps(conv, wl_eval.dtime, Gh[:ne + 2], Ih[:ne + 2], conv_cfg)
+    errs, errs_conv = {}, {}
     for mode in ("plain", "warm"):
         d = sub.to_device()
         Gs, Is = torch.from_numpy(np.ascontiguousarray(Gh)).cuda(), torch.from_numpy(np.ascontiguousarray(Ih)).cuda()
@@ -440,13 +486,19 @@ def warm_leg(args, wl_eval):
                 mlp.soil_water_warm(h, d, wl_eval.dtime, dtv, cfg)
         liq = d["h2osoi_liq"].cpu().numpy()
         errs[mode] = float(np.max(np.abs(liq - ref["h2osoi_liq"])))
+        errs_conv[mode] = float(np.max(np.abs(liq - conv["h2osoi_liq"])))
     out = {"workload": "learned warm start: MLP 64-128-128-21 (SiLU, bf16/fp32), trained on %d pairs from the "
                        "plain solver (%d columns x %d steps, other seed); evaluated on the scale workload, %d steps"
                        % (n_pairs, args.warm_train_nc, args.warm_train_steps, ne),
            "plain": res["plain"], "warm": res["warm"],
            "speedup": res["warm"]["value"] / res["plain"]["value"],
            "attempt_ratio": res["warm"]["attempts_per_column_step"] / res["plain"]["attempts_per_column_step"],
-           "max_abs_liq_error_vs_oracle_mm": errs, "error_sample_columns": 256, "balance": warm_balance,
+           "max_abs_liq_error_vs_oracle_mm": errs,
+           "max_abs_liq_error_vs_converged_mm": errs_conv,
+           "converged_reference": "the oracle with xTolerUpper and xTolerLower / 100",
+           "error_sample_columns": 256, "balance": warm_balance,
+           "proposal_ms": prop_ms, "proposal_share_of_warm_step": prop_ms / res["warm"]["ms_per_step"],
+           "mlp_layers_ms": layers_ms, "mlp_layers_share_of_warm_step": layers_ms / res["warm"]["ms_per_step"],
            "margin": model.margin, "margin_tuning": tune, "train_loss": hist,
            "sample_generation_s": gen_s, "training_s": train_s,
            "note": "both paths meet the same accept tolerance (xTolerUpper); the warm path only changes the "
@@ -482,6 +534,8 @@ def run_ours(args):
         h.set_option(abi.OPT_QUEUE_FRESH_BATCH, args.fresh_batch)
     if args.defer is not None:
         h.set_option(abi.OPT_QUEUE_DEFER, args.defer)
+    if args.records_tma is not None:
+        h.set_option(abi.OPT_RECORDS_TMA, args.records_tma)
     d = st.to_device()
     # per-step forcing, resident in HBM before the timed region
     Gd = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")
@@ -565,7 +619,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         gms = g0.elapsed_time(g1)
         graph = {"steps": gsteps, "ms_per_step": gms / gsteps,
-                 "value": gsteps * nc * world / (gms / 1000.0), "launches_per_step": 2,
+                 "value": gsteps * nc * world / (gms / 1000.0),
+                 "launches_per_step": 2 + richards_launch_count(h, nc),
                  "note": "the timed steps again, from the same state, as clmgb_column_step (fused entry) "
                          "calls replayed from one captured graph"}
         del g
@@ -671,12 +726,10 @@ def run_ours(args):
 
     # this library's kernels per timed step: forcing, soil temperature, water fractions,
     # then the Richards call (work queue with reserved scratch: the impedance / column
-    # record pass, the three longest-first ordering kernels, the solve)
-    sched = h.get_option(abi.OPT_STEP_SCHEDULE)
-    if sched == abi.SCHEDULE_QUEUE and h.get_option(abi.OPT_RESERVED_COLUMNS) >= nc:
-        launches_per_step = 3 + 1 + (3 if h.get_option(abi.OPT_QUEUE_ORDER) == 1 else 0) + 1
-    else:
-        launches_per_step = 3 + 1
+    # record pass, the three longest-first ordering kernels, the solve, and with the
+    # packed refresh the post-pass that writes the columns' outputs from their records)
+    richards_launches = richards_launch_count(h, nc)
+    launches_per_step = 3 + richards_launches
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,

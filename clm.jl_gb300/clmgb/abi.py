@@ -72,10 +72,13 @@ OPT_QUEUE_PUBLISH_DELAY = 20
 OPT_COUNT_WORK = 21
 OPT_WORK_LEVEL_ATTEMPTS = 22
 OPT_WORK_LEVEL_REFRESHES = 23
+OPT_RECORDS_TMA = 24
+OPT_RECORDS_TMA_USED = 25
 MAX_COPY_SEGMENTS = 128
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
 COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY, COL_FILTER, COL_QUEUE_WAIT = 32, 64, 128, 256, 512
+COL_COPY_WAIT = 1024
 ADJ_MAX_SUBSTEPS = 128
 
 CLMGB_NOALLOC_MAX_COLUMNS = 1 << 20

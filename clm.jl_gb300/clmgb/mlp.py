@@ -167,15 +167,20 @@ class WarmStartMLP:
         return hist
 
     # ---- use in the solver ----
-    def propose_first_dt(self, state, dtime, cfg=None, out=None, stream=None):
-        """dt_first [nc] (float64) for the state at the start of soil_water."""
-        torch = self.torch
+    def features(self, state, dtime, cfg=None, out=None, stream=None):
+        """The normalised BF16 feature rows [nc x 64] of the state at the start of soil_water."""
         cfg = cfg or abi.SwmConfig.clm5_default()
-        nc = state.nc
-        X = torch.empty((nc, IN), dtype=torch.bfloat16, device="cuda")
+        X = out if out is not None else self.torch.empty((state.nc, IN), dtype=self.torch.bfloat16, device="cuda")
         b, fw = state.bounds(), state.soilwater_fields()
         check(self.h.lib.clmgb_mlp_features(self.h.h, C.byref(b), C.byref(fw), C.byref(cfg), float(dtime),
                                             _p(self.mean), _p(self.istd), _p(X), _s(stream)), "mlp_features")
+        return X
+
+    def propose_first_dt(self, state, dtime, cfg=None, out=None, stream=None):
+        """dt_first [nc] (float64) for the state at the start of soil_water."""
+        torch = self.torch
+        nc = state.nc
+        X = self.features(state, dtime, cfg, stream=stream)
         Y = self.forward(X, stream=stream)
         dt = out if out is not None else torch.empty(nc, dtype=torch.float64, device="cuda")
         check(self.h.lib.clmgb_mlp_first_dt(self.h.h, nc, _p(Y), float(dtime), float(self.margin), int(self.kmax),

@@ -51,6 +51,8 @@ struct clmgb_handle_s {
   int64_t poll_limit;           // CLMGB_OPT_QUEUE_POLL_LIMIT
   int64_t publish_delay;        // CLMGB_OPT_QUEUE_PUBLISH_DELAY
   int64_t count_work;           // CLMGB_OPT_COUNT_WORK (counters in scratch words 10, 11)
+  int64_t records_tma;          // CLMGB_OPT_RECORDS_TMA
+  int records_tma_used;         // CLMGB_OPT_RECORDS_TMA_USED
   cudaError_t last_error;
 };
 
@@ -169,6 +171,8 @@ static clmgb::QueueScratch queue_scratch(clmgb_handle h) {
   q.poll_limit = (int)h->poll_limit;
   q.publish_delay = (int)h->publish_delay;
   q.work = h->count_work ? h->scratch + 10 : nullptr;
+  q.records_tma = (int)h->records_tma;
+  q.records_tma_used = &h->records_tma_used;
   return q;
 }
 
@@ -224,6 +228,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->column_base = 0;
   h->defer = CLMGB_DEFAULT_QUEUE_DEFER;
   h->packed = 1;
+  h->records_tma = 1;
   h->step_schedule = CLMGB_SCHEDULE_QUEUE;
   h->queue_blocks_per_sm = CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM;
   h->scratch = nullptr;
@@ -752,9 +757,9 @@ int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc) {
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t lev = al(nsoi * n * sizeof(double));   // one [nlevsoi][n] array
   const size_t col8 = al(n * 8), col4 = al(n * 4);
-  // imp + 5 wave level arrays, the refresh input records (PC_FIELDS level arrays),
+  // imp + 5 wave level arrays, the column records (PC_ALL level arrays),
   // 6 per-column doubles, nsub + status, order + 4 lists, bins
-  const size_t total = (6 + clmgb::PC_FIELDS) * lev + 6 * col8 + 2 * col4 + 5 * col4 + al(256 * sizeof(unsigned int));
+  const size_t total = (6 + clmgb::PC_ALL) * lev + 6 * col8 + 2 * col4 + 5 * col4 + al(256 * sizeof(unsigned int));
   void* blk = nullptr;
   cudaError_t ce = cudaDeviceSynchronize();
   if (ce == cudaSuccess) ce = cudaMalloc(&blk, total);
@@ -787,7 +792,7 @@ int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc) {
   h->qs.bins = reinterpret_cast<unsigned int*>(take(al(256 * sizeof(unsigned int))));
   w.counters = h->qs.bins + 192;   // bins use words 0..128
   h->qs.imp = w.imp;
-  h->qs.pcache = reinterpret_cast<double*>(take(clmgb::PC_FIELDS * lev));
+  h->qs.pcache = reinterpret_cast<double*>(take(clmgb::PC_ALL * lev));
   h->qs.capacity = max_nc;
   return CLMGB_OK;
 }
@@ -848,6 +853,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value < 0 || value > 10000000) return CLMGB_ERR_CONFIG;
       h->publish_delay = value;
       return CLMGB_OK;
+    case CLMGB_OPT_RECORDS_TMA:
+      if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
+      h->records_tma = value;
+      return CLMGB_OK;
     case CLMGB_OPT_COUNT_WORK: {
       if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
       if (value && !h->count_work) {    // counting starts from zero
@@ -885,6 +894,8 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_QUEUE_POLL_LIMIT: *value = h->poll_limit; return CLMGB_OK;
     case CLMGB_OPT_QUEUE_PUBLISH_DELAY: *value = h->publish_delay; return CLMGB_OK;
     case CLMGB_OPT_COUNT_WORK: *value = h->count_work; return CLMGB_OK;
+    case CLMGB_OPT_RECORDS_TMA: *value = h->records_tma; return CLMGB_OK;
+    case CLMGB_OPT_RECORDS_TMA_USED: *value = h->records_tma_used; return CLMGB_OK;
     case CLMGB_OPT_WORK_LEVEL_ATTEMPTS:
     case CLMGB_OPT_WORK_LEVEL_REFRESHES: {
       unsigned long long w[2];

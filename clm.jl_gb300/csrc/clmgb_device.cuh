@@ -939,6 +939,7 @@ __device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_s
 template <class S>
 struct MfLaneT {
   static constexpr bool kRefreshInline = true;   // mf_attempt runs mf_refresh itself
+  static constexpr bool kDzw = false;            // dzv holds dz (mf_dzw forms 1000*dz)
   int64_t c;
   int nlayers;
   int nsub;
@@ -958,6 +959,14 @@ struct MfLaneT {
   S gam[MAXSOI + 1], dwat[MAXSOI + 1];
 };
 typedef MfLaneT<double> MfLane;
+
+// 1000*dz of level j of a lane: the product M_TO_MM*dz, or the lane's own copy of it
+// (LT::kDzw), which has the same bits (DENH2O*dz of the column record)
+template <class LT>
+__device__ __forceinline__ double mf_dzw(const LT& L, int j) {
+  if constexpr (LT::kDzw) return L.dzv[j];
+  else return M_TO_MM * L.dzv[j];
+}
 
 // Substep log record (clmgb_substep_log): the liquid water of levels 1..nlevsoi at
 // the start of an accepted substep, its dtsub, the time done before it.  After a
@@ -1138,10 +1147,10 @@ __device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soi
         if (ev + (ea - eb) > 0 && ev + (ea - eb) < 2047 && ev > 0)
           L.dt_dz[j] = __longlong_as_double(v + shift);
         else
-          L.dt_dz[j] = dtsub / (M_TO_MM * L.dzv[j]);
+          L.dt_dz[j] = dtsub / mf_dzw(L, j);
       }
     } else {
-      for (int j = 1; j <= nlayers; j++) L.dt_dz[j] = dtsub / (M_TO_MM * L.dzv[j]);
+      for (int j = 1; j <= nlayers; j++) L.dt_dz[j] = dtsub / mf_dzw(L, j);
     }
     L.dt_cur = dtsub;
   }
@@ -1206,7 +1215,7 @@ __device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soi
     return false;
   }
   // ---- accept (:1466-1483) ----
-  for (int j = 1; j <= nlayers; j++) L.liq[j] = L.liq[j] + L.dwat[j] * (M_TO_MM * L.dzv[j]);
+  for (int j = 1; j <= nlayers; j++) L.liq[j] = L.liq[j] + L.dwat[j] * mf_dzw(L, j);
   L.fresh = true;
   S qcTemp;
   if (lower_bc == CLMGB_BC_FLUX) qcTemp = L.hk_bot + L.dhkdw_bot * L.dwat[nlayers];

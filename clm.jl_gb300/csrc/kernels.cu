@@ -320,6 +320,7 @@ struct LevelView {
 
 struct MfLaneP {
   static constexpr bool kRefreshInline = false;   // refreshed by mfp_refresh
+  static constexpr bool kDzw = true;              // dzv holds 1000*dz (the record's PC_DZW)
   int64_t c;
   int nlayers;
   int nsub;
@@ -332,18 +333,28 @@ struct MfLaneP {
   LevelView qout, dqodw1, dqodw2, fnet1;
 };
 
+// mf_end's destination in the packed kernel: the column's water goes to its record
+// (the post-pass k_column_outputs moves it to the state), qcharge to the state
+struct RecordOut {
+  double* rec;
+  int joff, nls;
+  double* qc;
+  __device__ __forceinline__ double& Liq(int jj) const { return rec[PC_LIQ * nls + (jj - joff) - 1]; }
+  __device__ __forceinline__ double& Qcharge() const { return *qc; }
+};
+
 // shared-memory doubles per warp: 4 level arrays and the bottom conductivity pair
 __host__ __device__ constexpr int64_t packed_warp_doubles(int nlevsoi) { return (4LL * nlevsoi + 2) * 32; }
 // threads per block of k_moisture_form_packed: 5 warps at 21 KB of shared memory each
 // (20 levels) put 2 blocks, 10 warps, on an SM
 constexpr int PBLOCK = 160;
 
-// mf_begin for the packed lane (the impedances stay in the cache the refresh reads)
+// mf_begin for the packed lane (the impedances stay in the cache the refresh reads;
+// the water and 1000*dz come from the column's record)
 __device__ __forceinline__ bool mfp_begin(MfLaneP& L, const Dims& D, const clmgb_soilwater_fields& f,
                                           const clmgb_swm_config& cfg, double dtime, int64_t c,
-                                          const double* dt_init) {
-  const int64_t ld = D.ldc;
-  const int joff = D.nlevsno;
+                                          const double* dt_init, const double* pcache) {
+  const int nls = D.nlevsoi;
   L.c = c;
   L.status = 0;
   const int64_t nl = f.col_nbedrock[c];
@@ -353,9 +364,10 @@ __device__ __forceinline__ bool mfp_begin(MfLaneP& L, const Dims& D, const clmgb
   }
   const int nlayers = (int)nl;
   L.nlayers = nlayers;
+  const double* rec = pcache + c * (int64_t)(PC_ALL * nls);
   for (int j = 1; j <= nlayers; j++) {
-    L.liq[j] = LV(f.h2osoi_liq, c, joff + j, ld);
-    L.dzv[j] = LVc(f.dz, c, joff + j, ld);
+    L.liq[j] = rec[PC_LIQ * nls + j - 1];
+    L.dzv[j] = rec[PC_DZW * nls + j - 1];
   }
   L.nsub = 0;
   L.dtsub = dtime;
@@ -375,7 +387,7 @@ __device__ __forceinline__ bool mfp_begin(MfLaneP& L, const Dims& D, const clmgb
 // ([column][PC_FIELDS][nls], k_impedance).
 __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dims& D,
                                             const clmgb_soilwater_fields& f, const clmgb_swm_config& cfg,
-                                            const double* pcache, double* wsm, int nls) {
+                                            double* pcache, double* wsm, int nls) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t ld = D.ldc;
@@ -396,7 +408,7 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
   auto A = [&](int a, int k, int j) -> double& { return wsm[((int64_t)a * nls + (j - 1)) * 32 + k]; };
   // input `fld` of level j of column c
   auto P = [&](int64_t c, int fld, int j) -> double {
-    return pcache[c * (int64_t)(PC_FIELDS * nls) + (int64_t)fld * nls + (j - 1)];
+    return pcache[c * (int64_t)(PC_ALL * nls) + (int64_t)fld * nls + (j - 1)];
   };
   enum { QOUT = 0, D1 = 1, D2 = 2, FN = 3 };
   struct Item { int k, j, nl; int64_t c; bool ok; };
@@ -449,8 +461,9 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
       smpv = -P(c, PC_SUC, j) * cm_pow(sj, -b);
       const double dsmpds = -b * smpv / sj;
       dsmpdw = dsmpds / P(c, PC_WS, j);
-      LV(f.smp_l, c, j, ld) = smpv;
-      LV(f.hk_l, c, j, ld) = hkv;
+      double* rec = pcache + c * (int64_t)(PC_ALL * nls);
+      rec[PC_SMP * nls + j - 1] = smpv;
+      rec[PC_HK * nls + j - 1] = hkv;
     }
     __syncwarp();
     if (it.ok) {
@@ -527,7 +540,7 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
 }
 
 // k_moisture_form_queue with the packed refresh; reads the column records
-// (QueueScratch::pcache) k_column_records wrote before it.  With
+// (QueueScratch::pcache) k_column_records (records.cu) wrote before it.  With
 // LOG it writes the same substep log (the starting water of each accepted substep,
 // its dtsub and the time done before it, then the solve's outputs).  Dynamic shared
 // memory: packed_warp_doubles(nlevsoi) doubles per warp.
@@ -567,7 +580,7 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
         } else {
           const int64_t c = order ? (int64_t)order[k] : (int64_t)k;
           if (order || f.mask_hydrology[c]) {
-            if (mfp_begin(L, D, f, cfg, dtime, c, dt_init)) {
+            if (mfp_begin(L, D, f, cfg, dtime, c, dt_init, qs.pcache)) {
               active = true;
               nacc = 0;
               kept = false;
@@ -638,13 +651,14 @@ k_moisture_form_packed(Dims D, int64_t nc, clmgb_soilwater_fields f, clmgb_swm_c
       kept = true;
     }
     if (fin) {
-      const uint32_t st = mf_end(L, D, f, X);
+      RecordOut RO{qs.pcache + L.c * (int64_t)(PC_ALL * nls), D.nlevsno, nls, f.qcharge + L.c};
+      const uint32_t st = mf_end(L, D, f, RO);
       if (LOG) {
         double* out = rec + (int64_t)lg.cap * SUB_REC;
         for (int j = 1; j <= L.nlayers; j++) {
           out[j - 1] = L.liq[j];
-          out[MAXSOI + j - 1] = LV(f.smp_l, L.c, j, D.ldc);
-          out[2 * MAXSOI + j - 1] = LV(f.hk_l, L.c, j, D.ldc);
+          out[MAXSOI + j - 1] = RO.rec[PC_SMP * nls + j - 1];
+          out[2 * MAXSOI + j - 1] = RO.rec[PC_HK * nls + j - 1];
         }
         out[3 * MAXSOI] = L.qc;
         out[3 * MAXSOI + 1] = (double)L.nsub;
@@ -709,53 +723,6 @@ k_impedance(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* 
   if (nl < 1 || nl > D.nlevsoi) return;
   const int nlayers = (int)nl;
   for (int j = 1; j <= nlayers; j++) imp_cache[(int64_t)(j - 1) * ld_imp + c] = mf_impedance(D, f, e_ice, c, j, nlayers);
-}
-
-// The impedances (imp_cache, as k_impedance) and each column's record of the packed
-// refresh's inputs (QueueScratch::pcache, [column][PC_FIELDS][nlevsoi]), by tiles of
-// 32 columns: the block reads the tile's levels column-fastest (coalesced), holds them
-// in shared memory, and writes the 32 records as one contiguous range.  Entries of
-// columns the solve skips, and levels below a column's bottom, are written as zero
-// and never read.
-constexpr int REC_COLS = 32, REC_THREADS = 256;
-__global__ void __launch_bounds__(REC_THREADS)
-k_column_records(Dims D, int64_t nc, clmgb_soilwater_fields f, double e_ice, double* imp_cache, int64_t ld_imp,
-                 double* pcache) {
-  extern __shared__ double tile[];   // [PC_FIELDS][nlevsoi][REC_COLS]
-  const int nls = D.nlevsoi, joff = D.nlevsno;
-  const int64_t ld = D.ldc;
-  const int64_t c0 = (int64_t)blockIdx.x * REC_COLS;
-  for (int idx = threadIdx.x; idx < nls * REC_COLS; idx += REC_THREADS) {
-    const int j = idx / REC_COLS + 1, cl = idx % REC_COLS;
-    const int64_t c = c0 + cl;
-    double v[PC_FIELDS];
-    for (int k = 0; k < PC_FIELDS; k++) v[k] = 0.0;
-    if (c < nc && f.mask_hydrology[c]) {
-      const int64_t nl = f.col_nbedrock[c];
-      if (nl >= 1 && nl <= nls && j <= nl) {
-        const int nlayers = (int)nl;
-        const double imp = mf_impedance(D, f, e_ice, c, j, nlayers);
-        imp_cache[(int64_t)(j - 1) * ld_imp + c] = imp;
-        v[PC_DZW] = LVc(f.dz, c, joff + j, ld) * DENH2O;
-        v[PC_WS] = LVc(f.watsat, c, j, ld);
-        v[PC_BSW] = LVc(f.bsw, c, j, ld);
-        v[PC_KS] = LVc(f.hksat, c, j, ld);
-        v[PC_SUC] = LVc(f.sucsat, c, j, ld);
-        v[PC_IMP] = imp;
-        if (j < nlayers) v[PC_DEN] = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
-        v[PC_ROOT] = LVc(f.qflx_rootsoi, c, j, ld);
-      }
-    }
-    for (int k = 0; k < PC_FIELDS; k++) tile[((int64_t)k * nls + (j - 1)) * REC_COLS + cl] = v[k];
-  }
-  __syncthreads();
-  const int rec = PC_FIELDS * nls;
-  const int64_t ncols = (nc - c0) < REC_COLS ? (nc - c0) : REC_COLS;
-  double* out = pcache + c0 * rec;
-  for (int idx = threadIdx.x; idx < ncols * rec; idx += REC_THREADS) {
-    const int cl = idx / rec, r = idx % rec;   // r = field * nls + (j - 1)
-    out[idx] = tile[(int64_t)r * REC_COLS + cl];
-  }
 }
 
 // Longest-expected-first order of the hydrology columns: counting sort on the
@@ -967,12 +934,9 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
   const bool use = qs.capacity >= nc && qs.order && qs.bins && qs.imp;
   if (use) {
     if (qs.packed && qs.pcache) {
-      const size_t smem = (size_t)PC_FIELDS * D.nlevsoi * REC_COLS * sizeof(double);
-      if ((e = cudaFuncSetAttribute(k_column_records, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-          cudaSuccess)
+      if ((e = launch_column_records(D, nc, f, cfg.e_ice, qs.imp, qs.capacity, qs.pcache, qs.records_tma != 0,
+                                     dev_status, s, qs.records_tma_used)) != cudaSuccess)
         return e;
-      k_column_records<<<(unsigned)((nc + REC_COLS - 1) / REC_COLS), REC_THREADS, smem, s>>>(
-          D, nc, f, cfg.e_ice, qs.imp, qs.capacity, qs.pcache);
     } else {
       k_impedance<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, cfg.e_ice, qs.imp, qs.capacity);
     }
@@ -1013,8 +977,12 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
     if (nb < 1) return cudaErrorInvalidConfiguration;
     int gp = grid > 0 ? grid : 1;
     if (gp > nb * nsm) gp = nb * nsm;
+    q.out_records = 1;
     kern<<<gp, PBLOCK, smem, s>>>(D, nc, f, cfg, dtime, col_status, or_status, dev_status, queue, ord, nl, dt_init,
                                  log ? *log : SubstepLogView{nullptr, nullptr, 0, 0}, qs.fresh_batch, q);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // the solved columns' water, smp_l and hk_l from their records to the state
+    if ((e = launch_column_outputs(D, nc, f, qs.pcache, s)) != cudaSuccess) return e;
   } else if (log)
     k_moisture_form_queue<true><<<grid > 0 ? grid : 1, BLOCK, 0, s>>>(D, nc, f, cfg, dtime, col_status, or_status,
                                                                       dev_status, queue, ord, nl, imp, ldi, dt_init,

@@ -22,10 +22,14 @@ struct QueueScratch {
   // CLMGB_OPT_QUEUE_PACKED_REFRESH: the warp refreshes its fresh lanes' columns
   // together, (column, level) pairs spread over the 32 lanes (k_moisture_form_packed)
   int packed;
-  // the packed refresh's inputs per column, contiguous: [capacity][PC_FIELDS][nlevsoi]
-  // (PcField), filled by k_impedance, so that a pass over one column's levels reads
-  // consecutive addresses and the resident columns' inputs stay in L2
+  // one record per column, contiguous: [capacity][PC_ALL][nlevsoi] (PcField): the
+  // packed refresh's inputs (the pre-pass k_column_records fills them), so that a pass
+  // over one column's levels reads consecutive addresses and the resident columns'
+  // inputs stay in L2, and the column's water, smp_l and hk_l during the solve
   double* pcache;
+  // 1 while the solve keeps a column's water, smp_l and hk_l in its record (the packed
+  // kernel); the post-pass k_column_outputs writes them to the state at the end
+  int out_records = 0;
   // CLMGB_OPT_QUEUE_DEFER: a column still unfinished after `defer` attempts leaves the
   // work queue at its next accepted substep; its state (water [nlevsoi][capacity],
   // dtsub, dtdone, qcharge so far, attempts, status at index c) and its index (list)
@@ -47,6 +51,9 @@ struct QueueScratch {
   // the levels of every substep attempt to work[0] and of every hydraulic refresh to
   // work[1] (the FP64 work model of the solve, clmgb/flops_model.py); NULL otherwise
   unsigned long long* work = nullptr;
+  // CLMGB_OPT_RECORDS_TMA: the column-record pre-pass stages its tiles with tensor copies
+  int records_tma = 1;
+  int* records_tma_used = nullptr;   // set to 1 when the last pre-pass used tensor copies
 };
 
 // Per-column state of the wave-synchronous Richards solve (richards_waves.cu), from
@@ -105,9 +112,12 @@ enum StLog {
 };
 static_assert(ST_END <= CLMGB_LOG_ST_STRIDE, "soil_temperature! record exceeds CLMGB_LOG_ST_STRIDE");
 
-// fields of QueueScratch::pcache: dz*1000, watsat, bsw, hksat, sucsat, the ice
-// impedance, 1000*(z[j+1]-z[j]) (levels below the bottom one) and qflx_rootsoi
-enum PcField { PC_DZW = 0, PC_WS, PC_BSW, PC_KS, PC_SUC, PC_IMP, PC_DEN, PC_ROOT, PC_FIELDS };
+// fields of a column record (QueueScratch::pcache): the inputs dz*1000, watsat, bsw,
+// hksat, sucsat, the ice impedance, 1000*(z[j+1]-z[j]) (levels below the bottom one)
+// and qflx_rootsoi; then the column's liquid water (the state's at the start, the
+// solve's at its end), smp_l and hk_l (written at every hydraulic refresh)
+enum PcField { PC_DZW = 0, PC_WS, PC_BSW, PC_KS, PC_SUC, PC_IMP, PC_DEN, PC_ROOT, PC_FIELDS,
+               PC_LIQ = PC_FIELDS, PC_SMP, PC_HK, PC_ALL };
 
 // Segments of one clmgb_copy_segments call (8-byte words).
 struct CopySegments {
@@ -141,6 +151,16 @@ cudaError_t launch_tridiagonal_multi(int64_t ncols, int64_t ldc, int nlevs, doub
 cudaError_t launch_synth_forcing(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
                                  const clmgb_soilwater_fields& fw, const double* G, const double* I,
                                  cudaStream_t s);
+
+// The column-record pre-pass of the work-queue Richards solve (records.cu)
+size_t column_records_smem(int nlevsoi);
+cudaError_t launch_column_records(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f, double e_ice,
+                                  double* imp_cache, int64_t ld_imp, double* pcache, bool tma, uint32_t* dev_status,
+                                  cudaStream_t s, int* tma_used = nullptr);
+bool column_records_tma_available();
+// writes the solved columns' water, smp_l and hk_l from their records to the state
+cudaError_t launch_column_outputs(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f, const double* pcache,
+                                  cudaStream_t s);
 
 // st_log (optional): the soil_temperature! records of a substep log (StLog)
 cudaError_t launch_soiltemp_fractions(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,

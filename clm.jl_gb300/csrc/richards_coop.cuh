@@ -81,6 +81,8 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
   const int n = (int)f.col_nbedrock[c];       // validated when the column was begun
   const int j = lane + 1;                     // this lane's level
   const bool lv = j <= n;
+  // where the water, smp_l and hk_l go: the column's record (packed kernel) or the state
+  double* const orec = qs.out_records ? qs.pcache + c * (int64_t)(PC_ALL * nlevsoi) : nullptr;
   // the column's state at its last accepted substep
   double liq = 0.0, dzv = 1.0, imp = 0.0, ws = 1.0, bsw = 0.0, hksat = 0.0, sucsat = 0.0, zj = 0.0, zj1 = 0.0;
   double root = 0.0;
@@ -140,8 +142,13 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
         smp = smpv;
         dhkdw = dhkds;
         dsmpdw = dsmpds / ws;
-        LV(f.smp_l, c, j, ld) = smpv;
-        LV(f.hk_l, c, j, ld) = hkv;
+        if (orec) {
+          orec[PC_SMP * nlevsoi + j - 1] = smpv;
+          orec[PC_HK * nlevsoi + j - 1] = hkv;
+        } else {
+          LV(f.smp_l, c, j, ld) = smpv;
+          LV(f.hk_l, c, j, ld) = hkv;
+        }
       }
       // fluxes and derivatives (:1310-1378)
       const double smpn = __shfl_down_sync(COOP_FULL, smp, 1);
@@ -270,7 +277,10 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
     dtsub = jl_min(nd, dtime - dtdone);
   }
   // mf_end
-  if (lv) LV(f.h2osoi_liq, c, joff + j, ld) = liq;
+  if (lv) {
+    if (orec) orec[PC_LIQ * nlevsoi + j - 1] = liq;
+    else LV(f.h2osoi_liq, c, joff + j, ld) = liq;
+  }
   if (__any_sync(COOP_FULL, lv && !isfinite(liq))) status |= CLMGB_COL_NONFINITE;
   if (lane == 0) {
     f.qcharge[c] = qc;

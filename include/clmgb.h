@@ -67,6 +67,10 @@ extern "C" {
                                         deferred column's index ran out and the slot was given back;
                                         the lane that deferred the column finished it itself, so
                                         every result is complete (a record of the slow path) */
+#define CLMGB_COL_COPY_WAIT   1024u  /* Richards pre-pass (device status only): a bounded wait for the
+                                        tensor copy of a tile of the column records ran out; that
+                                        tile's records were not written and the call's results are
+                                        not valid */
 #define CLMGB_COL_FILTER       256u  /* root sink: the column is in two of the reference's filters
                                         (a pervious road on a natural-vegetation landunit) */
 
@@ -726,16 +730,25 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             refresh (setting 1 zeroes the counts; 0 = off, the default) */
 #define CLMGB_OPT_WORK_LEVEL_ATTEMPTS 22 /* read-only (synchronises): that count of attempt levels */
 #define CLMGB_OPT_WORK_LEVEL_REFRESHES 23 /* read-only (synchronises): that count of refreshed levels */
+#define CLMGB_OPT_RECORDS_TMA         24 /* the Richards pre-pass stages each tile of 32 columns with 2-D
+                                            tensor copies (TMA, 1, the default) or with plain loads (0);
+                                            arrays the tensor copy cannot address (a base address or a
+                                            row stride not a multiple of 16 bytes) take plain loads.
+                                            Results do not depend on it. */
+#define CLMGB_OPT_RECORDS_TMA_USED    25 /* read-only: 1 if the last pre-pass of this handle used tensor
+                                            copies, 0 if it took plain loads */
 #define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls
                                             receive (default 0).  A caller that runs a column range [c0, c1)
                                             passes column arrays advanced by c0 (same ldc) and the patch
                                             arrays whole, since col_patchi/col_patchf and patch_column
                                             hold global indices, and sets this to c0. */
 int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value);
-/* Gives the handle per-column scratch for up to max_nc columns (about 112*nlevsoi + 80
+/* Gives the handle per-column scratch for up to max_nc columns (about 136*nlevsoi + 80
  * bytes per column): the Richards solve then forms the ice impedances in a uniform
- * pre-pass, gathers each column's refresh inputs into one contiguous record, hands out
- * columns longest-expected-first, and the WAVES schedule becomes available.  Calls with more columns
+ * pre-pass, gathers each column's refresh inputs and water into one contiguous record
+ * (the solve keeps the column's water, smp_l and hk_l there and a post-pass writes
+ * them to the state), hands out columns longest-expected-first, and the WAVES
+ * schedule becomes available.  Calls with more columns
  * than reserved run without it.  Synchronises the device; call it at set-up, not
  * inside stream capture. */
 int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc);

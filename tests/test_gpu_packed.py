@@ -125,3 +125,42 @@ def test_packed_refresh_writes_the_same_substep_log(bc, cap):
     assert np.array_equal(rec, rec_ref, equal_nan=True)
     for k in OUT:
         assert np.array_equal(out[k], ref[k], equal_nan=True), k
+
+
+@pytest.mark.parametrize("nc", [3000, 2999])
+def test_column_records_tensor_copies_and_plain_loads(nc):
+    """The Richards pre-pass stages its tiles of 32 columns with 2-D tensor copies
+    (CLMGB_OPT_RECORDS_TMA = 1) or plain loads (0); both give the oracle's bits.  3000
+    columns end in a partial tile (the copy fills the missing columns with zeros);
+    2999 columns give an odd row stride, which the tensor copy cannot address, so the
+    pre-pass takes plain loads whatever the option says."""
+    wl = _ragged(synth.make_workload(2, nc=nc, seed=21, nsteps=1), 6)
+    cfg = abi.SwmConfig.clm5_default()
+    st = wl.state
+    G, I = wl.forcing_block(range(1))
+    host = None
+    outs = {}
+    for tma in (1, 0):
+        h = api.Handle(st.vp)
+        try:
+            h.reserve(st.nc)
+            h.set_option(abi.OPT_RECORDS_TMA, tma)
+            d = st.to_device()
+            api.synth_forcing(h, d, torch.from_numpy(G[0]).cuda(), torch.from_numpy(I[0]).cuda())
+            api.soil_temperature(h, d, wl.dtime)
+            api.set_soil_water_fractions(h, d)
+            if host is None:
+                host = d.to_host()
+            api.soil_water(h, d, wl.dtime, cfg)
+            torch.cuda.synchronize()
+            assert h.get_option(abi.OPT_RECORDS_TMA_USED) == (1 if (tma and nc % 2 == 0) else 0)
+            assert h.device_status() & abi.COL_COPY_WAIT == 0
+            outs[tma] = d.to_host()
+        finally:
+            h.close()
+    O.soil_water(host, wl.dtime, cfg)
+    m = (host["mask_hydrology"] != 0) & (host["col_nbedrock"] >= 1) & (host["col_nbedrock"] <= st.vp.nlevsoi)
+    for tma in (1, 0):
+        for k in OUT:
+            assert np.array_equal(outs[tma][k][..., m], host[k][..., m]), (tma, k)
+            assert np.array_equal(outs[tma][k], outs[0][k], equal_nan=True), (tma, k)
