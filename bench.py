@@ -549,6 +549,11 @@ def run_ours(args):
     if not args.no_autotune and args.schedule is None and args.queue_bps is None:
         from clmgb import autotune
         tune = autotune.tune_column_step(h, d, wl.dtime, cfg, Gd, Id, steps=2, warm=1)
+        # the tridiagonal solver of clmgb_tridiagonal_multi (Thomas or warp-cooperative
+        # PCR) for soil-water-sized systems at three batch sizes; Thomas is kept (the
+        # reference's bits), the timings say where PCR would be faster
+        tune["tridiagonal"] = [autotune.tune_tridiagonal(h, n, st.vp.nlevsoi, exact=True)
+                               for n in (nc, 4096, 256)]
 
     def step(t, ev=None):
         # one timestep through the drop-in entry points, in the driver's order

@@ -74,6 +74,8 @@ OPT_WORK_LEVEL_ATTEMPTS = 22
 OPT_WORK_LEVEL_REFRESHES = 23
 OPT_RECORDS_TMA = 24
 OPT_RECORDS_TMA_USED = 25
+OPT_TRIDIAG_METHOD = 26
+TRIDIAG_THOMAS, TRIDIAG_PCR = 0, 1
 MAX_COPY_SEGMENTS = 128
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16

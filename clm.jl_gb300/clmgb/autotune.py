@@ -64,3 +64,46 @@ def capture_steps(handle, state, dtime, G, I, nsteps, first_step=0, cfg=None):
                 api.column_step(handle, state, dtime, cfg)
     torch.cuda.current_stream().wait_stream(s)
     return g
+
+
+def diagonally_dominant_systems(ncols, nlevs, seed=0, device="cuda"):
+    """Random tridiagonal systems [nlevs, ncols] with |b| > |a| + |c| (the shape of the
+    soil-water systems), right-hand sides of order one: (a, b, c, r)."""
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    a = -torch.rand((nlevs, ncols), generator=g, dtype=torch.float64)
+    c = -torch.rand((nlevs, ncols), generator=g, dtype=torch.float64)
+    b = 1.0 + a.abs() + c.abs() + torch.rand((nlevs, ncols), generator=g, dtype=torch.float64)
+    r = torch.randn((nlevs, ncols), generator=g, dtype=torch.float64)
+    return tuple(x.to(device) for x in (a, b, c, r))
+
+
+def tune_tridiagonal(handle, ncols, nlevs, exact=True, jtop=1, reps=20, warm=3, stream=None):
+    """Times clmgb_tridiagonal_multi on `ncols` columns of `nlevs` levels with Thomas (one
+    thread per column) and with parallel cyclic reduction (one warp per column), on
+    diagonally dominant systems of that shape.  With exact=False it sets the faster
+    method on the handle; with exact=True (the default) it keeps Thomas, whose results
+    are the reference's bits, and only reports what PCR would give.  Returns
+    {"method": ..., "ms": {"thomas": ..., "pcr": ...}, "faster": ...}."""
+    stream = stream or torch.cuda.current_stream()
+    a, b, c, r = diagonally_dominant_systems(ncols, nlevs)
+    u = torch.zeros_like(r)
+    jt = torch.full((ncols,), int(jtop), dtype=torch.int64, device=r.device)
+    mask = torch.ones(ncols, dtype=torch.uint8, device=r.device)
+    prev = handle.get_option(abi.OPT_TRIDIAG_METHOD)
+    ms = {}
+    for name, method in (("thomas", abi.TRIDIAG_THOMAS), ("pcr", abi.TRIDIAG_PCR)):
+        handle.set_option(abi.OPT_TRIDIAG_METHOD, method)
+        for _ in range(warm):
+            api.tridiagonal_multi(handle, u, a, b, c, r, jt, mask, stream=stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            api.tridiagonal_multi(handle, u, a, b, c, r, jt, mask, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms[name] = e0.elapsed_time(e1) / reps
+    faster = min(ms, key=ms.get)
+    method = abi.TRIDIAG_PCR if (faster == "pcr" and not exact) else abi.TRIDIAG_THOMAS
+    handle.set_option(abi.OPT_TRIDIAG_METHOD, method if not exact else prev)
+    return {"method": "pcr" if method == abi.TRIDIAG_PCR else "thomas", "ms": ms, "faster": faster,
+            "ncols": ncols, "nlevs": nlevs}

@@ -53,6 +53,7 @@ struct clmgb_handle_s {
   int64_t count_work;           // CLMGB_OPT_COUNT_WORK (counters in scratch words 10, 11)
   int64_t records_tma;          // CLMGB_OPT_RECORDS_TMA
   int records_tma_used;         // CLMGB_OPT_RECORDS_TMA_USED
+  int64_t tridiag_method;       // CLMGB_OPT_TRIDIAG_METHOD
   cudaError_t last_error;
 };
 
@@ -857,6 +858,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
       h->records_tma = value;
       return CLMGB_OK;
+    case CLMGB_OPT_TRIDIAG_METHOD:
+      if (value != CLMGB_TRIDIAG_THOMAS && value != CLMGB_TRIDIAG_PCR) return CLMGB_ERR_CONFIG;
+      h->tridiag_method = value;
+      return CLMGB_OK;
     case CLMGB_OPT_COUNT_WORK: {
       if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
       if (value && !h->count_work) {    // counting starts from zero
@@ -896,6 +901,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_COUNT_WORK: *value = h->count_work; return CLMGB_OK;
     case CLMGB_OPT_RECORDS_TMA: *value = h->records_tma; return CLMGB_OK;
     case CLMGB_OPT_RECORDS_TMA_USED: *value = h->records_tma_used; return CLMGB_OK;
+    case CLMGB_OPT_TRIDIAG_METHOD: *value = h->tridiag_method; return CLMGB_OK;
     case CLMGB_OPT_WORK_LEVEL_ATTEMPTS:
     case CLMGB_OPT_WORK_LEVEL_REFRESHES: {
       unsigned long long w[2];
@@ -936,7 +942,7 @@ int32_t clmgb_tridiagonal_multi(clmgb_handle h, int64_t ncols, int64_t ldc, int3
   if (ncols == 0) return CLMGB_OK;
   if (!u || !a || !b || !c || !r || !jtop || !mask) return CLMGB_ERR_NULL_ARG;
   cudaError_t ce = clmgb::launch_tridiagonal_multi(ncols, ldc, nlevs, u, a, b, c, r, jtop, mask,
-                                                   (cudaStream_t)stream);
+                                                   (cudaStream_t)stream, (int)h->tridiag_method);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 

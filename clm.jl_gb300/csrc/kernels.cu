@@ -857,6 +857,88 @@ k_tridiagonal_multi(int64_t ncols, int64_t ld, int nlevs, double* u, const doubl
   }
 }
 
+// The same systems by parallel cyclic reduction, one warp per column (CLMGB_TRIDIAG_PCR):
+// lane l holds rows l and l+32 of the column's n = nlevs - jtop + 1 <= 64 unknowns in
+// registers.  Each round with stride k eliminates the couplings to rows i-k and i+k
+// (rows outside the system act as identity rows), so after ceil(log2 n) rounds every
+// row stands alone and x_i = r_i / b_i.  The divisors get the reference's 1e-30
+// pivot guard.  Without pivoting it is meant for the diagonally dominant systems of the
+// soil-water and lake solves; its rounding differs from the sequential elimination's.
+constexpr int PCR_WARPS = 4;
+// row t (0..32*NH-1) of a value held as v[h] for rows lane + 32h
+template <int NH>
+__device__ __forceinline__ double pcr_row(const double* v, int t) {
+  const double x0 = __shfl_sync(0xffffffffu, v[0], t & 31);
+  if (NH == 1) return x0;
+  const double x1 = __shfl_sync(0xffffffffu, v[NH - 1], t & 31);
+  return (t >> 5) ? x1 : x0;
+}
+__device__ __forceinline__ double pcr_guard(double d) {
+  return fabs(d) < 1e-30 ? copysign(1e-30, d == 0.0 ? 1.0 : d) : d;
+}
+// the system of one column, n <= 32*NH unknowns, rows lane + 32h of this lane
+template <int NH>
+__device__ __forceinline__ void pcr_solve(int64_t col, int64_t ld, int j0, int n, double* u,
+                                          const double* __restrict__ a, const double* __restrict__ b,
+                                          const double* __restrict__ cc, const double* __restrict__ r) {
+  const int lane = threadIdx.x & 31;
+  double A[NH], B[NH], C[NH], R[NH];
+#pragma unroll
+  for (int h = 0; h < NH; h++) {
+    const int i = lane + 32 * h;
+    if (i < n) {
+      const int lev = j0 + i;
+      A[h] = i == 0 ? 0.0 : LVc(a, col, lev, ld);
+      B[h] = LVc(b, col, lev, ld);
+      C[h] = i == n - 1 ? 0.0 : LVc(cc, col, lev, ld);
+      R[h] = LVc(r, col, lev, ld);
+    } else {
+      A[h] = 0.0; B[h] = 1.0; C[h] = 0.0; R[h] = 0.0;
+    }
+  }
+  for (int k = 1; k < n; k <<= 1) {
+    double An[NH], Bn[NH], Cn[NH], Rn[NH];
+#pragma unroll
+    for (int h = 0; h < NH; h++) {
+      const int i = lane + 32 * h;
+      const int lo = i - k, hi = i + k;
+      // rows i-k and i+k (identity rows outside 0..n-1); every lane joins every shuffle
+      const int tl = lo < 0 ? 0 : lo, th = hi > 32 * NH - 1 ? 32 * NH - 1 : hi;
+      double al = pcr_row<NH>(A, tl), bl = pcr_row<NH>(B, tl), cl = pcr_row<NH>(C, tl), rl = pcr_row<NH>(R, tl);
+      double ah = pcr_row<NH>(A, th), bh = pcr_row<NH>(B, th), ch = pcr_row<NH>(C, th), rh = pcr_row<NH>(R, th);
+      if (lo < 0) { al = 0.0; bl = 1.0; cl = 0.0; rl = 0.0; }
+      if (hi >= n) { ah = 0.0; bh = 1.0; ch = 0.0; rh = 0.0; }
+      const double alpha = -A[h] / pcr_guard(bl);
+      const double gamma = -C[h] / pcr_guard(bh);
+      An[h] = alpha * al;
+      Cn[h] = gamma * ch;
+      Bn[h] = B[h] + alpha * cl + gamma * ah;
+      Rn[h] = R[h] + alpha * rl + gamma * rh;
+    }
+#pragma unroll
+    for (int h = 0; h < NH; h++) {
+      A[h] = An[h]; B[h] = Bn[h]; C[h] = Cn[h]; R[h] = Rn[h];
+    }
+  }
+#pragma unroll
+  for (int h = 0; h < NH; h++) {
+    const int i = lane + 32 * h;
+    if (i < n) LV(u, col, j0 + i, ld) = R[h] / pcr_guard(B[h]);
+  }
+}
+__global__ void __launch_bounds__(32 * PCR_WARPS)
+k_tridiagonal_multi_pcr(int64_t ncols, int64_t ld, int nlevs, double* u, const double* __restrict__ a,
+                        const double* __restrict__ b, const double* __restrict__ cc,
+                        const double* __restrict__ r, const int64_t* jtop, const uint8_t* mask) {
+  const int64_t col = (int64_t)blockIdx.x * PCR_WARPS + (threadIdx.x >> 5);
+  if (col >= ncols || !mask[col]) return;             // the whole warp leaves together
+  const int64_t j64 = jtop[col];
+  if (j64 < 1 || j64 > nlevs) return;
+  const int j0 = (int)j64, n = nlevs - j0 + 1;
+  if (n <= 32) pcr_solve<1>(col, ld, j0, n, u, a, b, cc, r);
+  else pcr_solve<2>(col, ld, j0, n, u, a, b, cc, r);
+}
+
 // Synthetic per-step forcing (the upstream radiation / infiltration modules are out
 // of scope): sabg = sabg_soil = sabg_snow = G, sabg_lyr = G on the top active layer
 // and 0 elsewhere, forc_lwrad = SB*t_grnd^4, qflx_infl = I.
@@ -1054,9 +1136,13 @@ cudaError_t launch_band_solve(int64_t nc, int64_t ldc, int nlev, double* tvector
 }
 cudaError_t launch_tridiagonal_multi(int64_t ncols, int64_t ldc, int nlevs, double* u, const double* a,
                                      const double* b, const double* c, const double* r, const int64_t* jtop,
-                                     const uint8_t* mask, cudaStream_t s) {
+                                     const uint8_t* mask, cudaStream_t s, int method) {
   if (nlevs > MAXTRI) return cudaErrorInvalidValue;
-  k_tridiagonal_multi<<<grid_for(ncols), BLOCK, 0, s>>>(ncols, ldc, nlevs, u, a, b, c, r, jtop, mask);
+  if (method == CLMGB_TRIDIAG_PCR)
+    k_tridiagonal_multi_pcr<<<(unsigned)((ncols + PCR_WARPS - 1) / PCR_WARPS), 32 * PCR_WARPS, 0, s>>>(
+        ncols, ldc, nlevs, u, a, b, c, r, jtop, mask);
+  else
+    k_tridiagonal_multi<<<grid_for(ncols), BLOCK, 0, s>>>(ncols, ldc, nlevs, u, a, b, c, r, jtop, mask);
   return cudaGetLastError();
 }
 cudaError_t launch_synth_forcing(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,

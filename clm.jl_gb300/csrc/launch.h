@@ -147,7 +147,8 @@ cudaError_t launch_band_solve(int64_t nc, int64_t ldc, int nlev, double* tvector
                               const uint8_t* mask, int kl, int ku, int nlevsno_off, cudaStream_t s);
 cudaError_t launch_tridiagonal_multi(int64_t ncols, int64_t ldc, int nlevs, double* u, const double* a,
                                      const double* b, const double* c, const double* r, const int64_t* jtop,
-                                     const uint8_t* mask, cudaStream_t s);
+                                     const uint8_t* mask, cudaStream_t s,
+                                     int method = CLMGB_TRIDIAG_THOMAS);
 cudaError_t launch_synth_forcing(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& ft,
                                  const clmgb_soilwater_fields& fw, const double* G, const double* I,
                                  cudaStream_t s);

@@ -737,6 +737,10 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             Results do not depend on it. */
 #define CLMGB_OPT_RECORDS_TMA_USED    25 /* read-only: 1 if the last pre-pass of this handle used tensor
                                             copies, 0 if it took plain loads */
+#define CLMGB_OPT_TRIDIAG_METHOD      26 /* solver of clmgb_tridiagonal_multi: CLMGB_TRIDIAG_THOMAS (default)
+                                            or CLMGB_TRIDIAG_PCR */
+#define CLMGB_TRIDIAG_THOMAS 0
+#define CLMGB_TRIDIAG_PCR    1
 #define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls
                                             receive (default 0).  A caller that runs a column range [c0, c1)
                                             passes column arrays advanced by c0 (same ldc) and the patch
@@ -919,7 +923,12 @@ int32_t clmgb_batched_band_solve(clmgb_handle h, int64_t nc, int64_t ldc, int32_
                                  int32_t kl, int32_t ku, int32_t nlevsno_off, void* stream);
 
 /* tridiagonal_multi! (tridiagonal.jl:129): a,b,c,r,u are [ldc, nlevs]; jtop int64 [nc]
- * 1-based; Thomas with the reference's 1e-30 pivot guard. */
+ * 1-based; nlevs <= 64.  CLMGB_OPT_TRIDIAG_METHOD selects the solver: Thomas, one thread
+ * per column, with the reference's 1e-30 pivot guard (CLMGB_TRIDIAG_THOMAS, the default:
+ * the reference's bits), or parallel cyclic reduction, one warp per column
+ * (CLMGB_TRIDIAG_PCR: log2 rounds instead of a sequential sweep, the same guard on its
+ * divisors, no pivoting; for diagonally dominant systems; rounding differs from the
+ * reference's in the last bits). */
 int32_t clmgb_tridiagonal_multi(clmgb_handle h, int64_t ncols, int64_t ldc, int32_t nlevs,
                                 double* u, const double* a, const double* b, const double* c,
                                 const double* r, const int64_t* jtop, const uint8_t* mask,

@@ -418,3 +418,63 @@ def test_column_step_multistep_vs_oracle(cfg_id, nc, nsteps, mode):
     # GPU and oracle share their transcendentals and operation order: identical bits
     for k in ("t_soisno", "h2osoi_liq", "h2osoi_ice", "num_substeps", "qcharge", "t_grnd", "imelt"):
         assert np.array_equal(got[k], ref[k]), k
+
+
+@pytest.mark.parametrize("nlevs,jt", [(20, 1), (21, 4), (38, 1), (64, 7), (5, 5)])
+def test_tridiagonal_pcr_matches_thomas(nlevs, jt):
+    """CLMGB_TRIDIAG_PCR (one warp per column) against the Thomas path (the oracle's
+    bits) on diagonally dominant systems with ragged masks: agreement to 1e-13
+    relative, masked columns untouched."""
+    from clmgb import autotune
+    ncols = 777
+    a, b, c, r = autotune.diagonally_dominant_systems(ncols, nlevs, seed=nlevs + jt)
+    jtop = torch.full((ncols,), jt, dtype=torch.int64, device="cuda")
+    mask = torch.ones(ncols, dtype=torch.uint8, device="cuda")
+    mask[::11] = 0
+    h = api.Handle(synth.clm5_varpar())
+    out = {}
+    for method in (abi.TRIDIAG_THOMAS, abi.TRIDIAG_PCR):
+        h.set_option(abi.OPT_TRIDIAG_METHOD, method)
+        assert h.get_option(abi.OPT_TRIDIAG_METHOD) == method
+        u = torch.full((nlevs, ncols), 7.0, dtype=torch.float64, device="cuda")
+        api.tridiagonal_multi(h, u, a, b, c, r, jtop, mask)
+        torch.cuda.synchronize()
+        out[method] = u.cpu().numpy()
+    h.close()
+    ut, up = out[abi.TRIDIAG_THOMAS], out[abi.TRIDIAG_PCR]
+    m = mask.cpu().numpy() != 0
+    # Thomas is the oracle's restatement bit for bit
+    u_ref = np.full((nlevs, ncols), 7.0)
+    orc.tridiagonal_multi(u_ref, a.cpu().numpy(), b.cpu().numpy(), c.cpu().numpy(), r.cpu().numpy(),
+                          jtop.cpu().numpy(), mask.cpu().numpy())
+    assert np.array_equal(ut.view(np.uint64), u_ref.view(np.uint64))
+    sl = slice(jt - 1, nlevs)
+    scale = np.max(np.abs(ut[sl][:, m]), axis=0)
+    assert np.max(np.abs(up[sl][:, m] - ut[sl][:, m]) / scale) < 1e-13
+    assert np.all(up[:, ~m] == 7.0) and np.all(up[:jt - 1] == 7.0)
+
+
+def test_tridiagonal_pcr_known_answers():
+    """The reference's tridiagonal known answers (test_tridiagonal.jl, test_soil_water_
+    movement.jl: all-ones solutions, the identity, a partial system below jtop) through
+    the PCR path, within each case's tolerance."""
+    G = golden()
+    h = api.Handle(synth.clm5_varpar())
+    h.set_option(abi.OPT_TRIDIAG_METHOD, abi.TRIDIAG_PCR)
+    ran = 0
+    for name in ("tridiag_3x3", "tridiag_col_3x3", "tridiag_identity", "tridiag_partial"):
+        c = G[name]
+        n, ncols = len(c["b"]), 3
+        arr = {k: _dev(np.repeat(np.array(c[k], dtype=np.float64)[:, None], ncols, 1)) for k in "abcr"}
+        u = torch.zeros((n, ncols), dtype=torch.float64, device="cuda")
+        api.tridiagonal_multi(h, u, arr["a"], arr["b"], arr["c"], arr["r"],
+                              _dev(np.full(ncols, c["jtop"], dtype=np.int64)), _dev(np.ones(ncols, dtype=np.uint8)))
+        torch.cuda.synchronize()
+        got = u.cpu().numpy()
+        for col in range(ncols):
+            for g, want in zip(got[:, col], c["u"]):
+                if want is not None:
+                    assert abs(g - want) <= c["atol"], (name, col, g, want)
+        ran += 1
+    h.close()
+    assert ran == 4
