@@ -510,3 +510,103 @@ def test_logged_step_is_the_production_step(handle):
             for off, k in ((4, "t_soisno"), (4 + 2 * nL, "h2osoi_ice"), (4 + 3 * nL, "fact")):
                 assert torch.equal(srec[c, off + jt:off + nw], b[k][jt:nw, c]), (t, c, k)
             assert int(srec[c, 0]) == nw - jt + 1          # snow + ground levels + the surface-water row
+
+
+@pytest.mark.parametrize("nsteps,min_share", [(1, 0.18), (48, 0.38)])
+def test_calibration_gradient_every_entry_by_batched_differences(handle, nsteps, min_share):
+    """Every one of the 80 parameter entries (watsat, bsw, sucsat, hksat of 20 levels)
+    of 64 columns, each with its own step: the perturbed copies are extra columns of one
+    batched forward run (64 x 80 entries x 7 step sizes x 2 signs), so every entry gets
+    central differences at h = 1e-6, 3e-6, ..., 3e-4, 1e-3 relative.  An entry is resolved
+    at the smallest h whose quotient agrees with the next larger one to 1e-4 relative
+    (quotients across a kink of a clamp drift slowly with h, by 1e-4 to 1e-3 between
+    neighbouring step sizes, and are left out),
+    where neither pair of runs moves a discrete decision (substep counts, melt flags)
+    and the loss changes by at least 1e5 times what one ulp of every observation y_t
+    moves it (sum_t 2 |y_t - target_t| ulp(y_t): a column close to its target has a
+    small loss whose own ulps say nothing about the noise of its quotients); a resolved
+    entry must match the adjoint to 1e-3 relative.  Levels below a column's bedrock take no part in the solve: their
+    adjoint and every quotient must be exactly zero.  Reports the shares."""
+    cfg = _cfg_flux()
+    nc0 = 64
+    wl, G, I = _workload(nc0, nsteps, seed=4242)
+    traj = _traj(handle, wl, G, I, nsteps, cfg)
+    st0 = wl.state.to_device()
+    pert = wl.state.copy()
+    adjoint.perturb_parameters(pert, np.random.default_rng(9))
+    tl = adjoint.CalibrationLoss(st0, wl.dtime)
+    _params_and_decisions(traj, pert.to_device(), tl, nsteps)
+    target = torch.stack(tl.y)                                   # [nsteps, nc0]
+    loss = adjoint.CalibrationLoss(st0, wl.dtime, target)
+    adj = adjoint.multistep_reverse(traj, st0.copy(), loss.seed, loss.observe, checkpoint_every=8)
+    params = adjoint.PARAMS
+    nsoi = wl.state.vp.nlevsoi
+    gr = np.stack([adj.grad[p].cpu().numpy() for p in params])   # [4, nsoi, nc0]
+    rels = np.array([1e-6, 3e-6, 1e-5, 3e-5, 1e-4, 3e-4, 1e-3])
+    K, E = len(rels), len(params) * nsoi
+    # column layout of the batch: the nc0 base columns, then for each (entry, step, sign)
+    # a block of nc0 copies
+    nrep = nc0 + E * K * 2 * nc0
+    base_of = np.tile(np.arange(nc0), nrep // nc0)
+    host = wl.state.subset(base_of)
+    theta0 = {p: host[p].copy() for p in params}
+    blk = 1
+    for e in range(E):
+        p, j = params[e // nsoi], e % nsoi
+        for k in range(K):
+            for sgn in (1.0, -1.0):
+                sl = slice(blk * nc0, (blk + 1) * nc0)
+                host[p][j, sl] = theta0[p][j, sl] * (1.0 + sgn * rels[k])
+                blk += 1
+    st = host.to_device()
+    bo = torch.from_numpy(base_of).cuda()
+    Gr, Ir = G[:, bo].contiguous(), I[:, bo].contiguous()
+    trajr = _traj(handle, wl, Gr, Ir, nsteps, cfg)
+    lossr = adjoint.CalibrationLoss(st, wl.dtime, target[:, bo].contiguous())
+    same = torch.ones(nrep, dtype=torch.bool, device="cuda")
+    for t in range(nsteps):
+        trajr.step(t, st)
+        lossr.observe(t, st)
+        ns, im = st["num_substeps"], st["imelt"]
+        same &= (ns == ns[bo]) & (im == im[:, bo]).all(0)
+    L = lossr.per_column().cpu().numpy()
+    same = same.cpu().numpy()
+    Lr = L[nc0:].reshape(E, K, 2, nc0)
+    okr = same[nc0:].reshape(E, K, 2, nc0).all(2)                # [E, K, nc0]
+    h = rels[None, :, None] * np.abs(np.stack([theta0[params[e // nsoi]][e % nsoi, :nc0]
+                                                for e in range(E)]))[:, None, :]
+    fd = (Lr[:, :, 0] - Lr[:, :, 1]) / (2.0 * h)                 # [E, K, nc0]
+    dl = np.abs(Lr[:, :, 0] - Lr[:, :, 1])
+    g = gr.reshape(E, nc0)
+    Y = torch.stack(lossr.y)[:, :nc0].cpu().numpy()
+    Rz = Y - target.cpu().numpy()
+    conditioned = np.abs(Rz).max(0) >= 1e-6 * np.abs(Y).max(0)
+    noise = (2.0 * np.abs(Rz) * np.abs(Y)).sum(0) * 2.0 ** -52     # loss change per ulp of every y_t
+    resolved = np.zeros((E, nc0), dtype=bool)
+    checked_fd = np.zeros((E, nc0))
+    for k in range(K - 1):
+        agree = (okr[:, k] & okr[:, k + 1] & (dl[:, k] >= 1e5 * noise[None, :]) &
+                 (np.abs(fd[:, k] - fd[:, k + 1]) <= 1e-4 * np.abs(fd[:, k])))
+        new = agree & ~resolved
+        checked_fd[new] = fd[:, k][new]
+        resolved |= agree
+    resolved &= conditioned[None, :]
+    zero = (g == 0.0)
+    nb = wl.state["col_nbedrock"][:nc0]
+    below = np.array([[e % nsoi + 1 > nb[c] for c in range(nc0)] for e in range(E)])
+    assert np.all(g[below] == 0.0) and np.all(fd.transpose(1, 0, 2)[:, below] == 0.0)
+    rel_err = np.abs(g - checked_fd) / np.maximum(np.abs(checked_fd), 1e-300)
+    bad = resolved & (rel_err > 1e-3)
+    if bad.any():
+        lines = []
+        for e, c in np.argwhere(bad)[:6]:
+            lines.append("%s[%d] col %d adj %.10e fd %s ok %s dl/noise %s" % (
+                params[e // nsoi], e % nsoi + 1, c, g[e, c], np.array2string(fd[e, :, c], precision=10),
+                okr[e, :, c], np.array2string(dl[e, :, c] / noise[c], precision=2)))
+        raise AssertionError("%d entries off:\n" % bad.sum() + "\n".join(lines))
+    live = ~zero & conditioned[None, :]
+    share = resolved[live].mean()
+    print("every entry, %d steps: %d of %d nonzero entries resolved (%.1f%%), %d below bedrock (zero), "
+          "max rel err %.2e" % (nsteps, resolved[live].sum(), live.sum(), 100 * share, below.sum(),
+                                rel_err[resolved].max() if resolved.any() else 0.0))
+    assert share >= min_share, share
