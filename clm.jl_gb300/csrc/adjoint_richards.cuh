@@ -30,6 +30,20 @@ struct RichardsBar {
   double ws[MAXSOI + 1], b[MAXSOI + 1], suc[MAXSOI + 1], ks[MAXSOI + 1], imp[MAXSOI + 1];
 };
 
+// The forward values are kept as sixteen level arrays (the saturation powers and logs,
+// the reciprocals, the band and the two sweeps); every other forward quantity is
+// formed again from them where the reverse needs it, by the same expression.  The
+// reverse is one downward sweep that finishes the transposed back substitution, the
+// assembly, the fluxes and the hydraulic properties level by level, with the adjoints
+// of the levels still open (at most three) in registers: at level j, interface j's
+// adjoints are complete once level j's assembly is reversed, level j+1's hydraulic
+// adjoints once interface j is, and level j+2's saturation adjoint once level j+1's
+// hydraulics are.
+struct MfAcc {
+  double smpb, dsmpdwb, hkb, dhkdwb, sb, wsb;
+};
+__device__ __forceinline__ void mf_acc_zero(MfAcc& a) { a.smpb = a.dsmpdwb = a.hkb = a.dhkdwb = a.sb = a.wsb = 0.0; }
+
 static __device__ __noinline__ void mf_substep_reverse(const Dims& D, const clmgb_soilwater_fields& f,
                                                 const clmgb_swm_config& cfg, double dtime, int64_t c, int nl,
                                                 const double* dzv, const double* imp, const double* ws,
@@ -40,218 +54,250 @@ static __device__ __noinline__ void mf_substep_reverse(const Dims& D, const clmg
   const int joff = D.nlevsno, joff_zi = D.nlevsno + 1, nlevsoi = D.nlevsoi;
   const int lower_bc = cfg.lower_boundary_condition;
   // ---- forward values ----
-  double s[MAXSOI + 2], s0[MAXSOI + 2], s1c[MAXSOI + 2], e[MAXSOI + 2], P[MAXSOI + 2], Q[MAXSOI + 2];
-  double hk[MAXSOI + 2], dhkdw[MAXSOI + 2], smp[MAXSOI + 2], dsmpds[MAXSOI + 2], dsmpdw[MAXSOI + 2];
-  bool lpass[MAXSOI + 2], spass[MAXSOI + 2], s1pass[MAXSOI + 2];
-  double rws[MAXSOI + 2], rs[MAXSOI + 2], rs1[MAXSOI + 2], Ls[MAXSOI + 2], L1[MAXSOI + 2], rden[MAXSOI + 2];
-  for (int j = 1; j <= nl; j++) {
-    lpass[j] = liq[j] >= 1.0e-6;         // Julia max(liq, 1e-6) took liq
+  double P[MAXSOI + 2], Q[MAXSOI + 2], Ls[MAXSOI + 2], L1[MAXSOI + 2];
+  double rs[MAXSOI + 2], rs1[MAXSOI + 2], rws[MAXSOI + 2], s0[MAXSOI + 2], rden[MAXSOI + 2];
+  double dtdz[MAXSOI + 2], amx[MAXSOI + 2], bmx[MAXSOI + 2], cmx[MAXSOI + 2], gc[MAXSOI + 2];
+  double dwat[MAXSOI + 2], lam[MAXSOI + 2];
+  uint32_t lpass = 0, spass = 0, s1pass = 0;          // bit j: Julia's max/min took the unclamped value
+  // saturation of level j (:1283-1287)
+  auto saturation = [&](int j) -> double {
     const double vwc = jl_max(liq[j], 1.0e-6) / (dzv[j] * DENH2O);
     s0[j] = vwc / ws[j];
     double sv = jl_min(s0[j], 1.0);
     sv = jl_max(0.01, sv);
-    s[j] = sv;
-    spass[j] = s0[j] <= 1.0 && s0[j] > 0.01;
-    rws[j] = 1.0 / ws[j];
-    rs[j] = 1.0 / sv;
-    Ls[j] = ::cm_log(sv);
-  }
+    if (liq[j] >= 1.0e-6) lpass |= 1u << j;
+    if (s0[j] <= 1.0 && s0[j] > 0.01) spass |= 1u << j;
+    return sv;
+  };
+  // hydraulic properties (:1288-1308), powers as exp(a log s) from the logs the
+  // parameter derivatives need anyway
+  double s_n = saturation(1);
   for (int j = 1; j <= nl; j++) {
-    const double s1r = (j == nl) ? s[j] : 0.5 * (s[j] + s[j + 1]);
+    const double sj = s_n;
+    if (j < nl) s_n = saturation(j + 1);
+    rws[j] = 1.0 / ws[j];
+    rs[j] = 1.0 / sj;
+    Ls[j] = ::cm_log(sj);
+    const double s1r = (j == nl) ? sj : 0.5 * (sj + s_n);
     double sv = jl_min(s1r, 1.0);
     sv = jl_max(0.01, sv);
-    s1c[j] = sv;
-    s1pass[j] = s1r <= 1.0 && s1r > 0.01;
+    if (s1r <= 1.0 && s1r > 0.01) s1pass |= 1u << j;
     rs1[j] = 1.0 / sv;
     L1[j] = ::cm_log(sv);
-    e[j] = 2.0 * bb[j] + 3.0;
-    P[j] = ::cm_exp(e[j] * L1[j]);          // s1^e as a derivative coefficient
-    hk[j] = imp[j] * ks[j] * P[j];
-    dhkdw[j] = e[j] * hk[j] * rs1[j];
+    P[j] = ::cm_exp((2.0 * bb[j] + 3.0) * L1[j]);
     Q[j] = ::cm_exp(-bb[j] * Ls[j]);
-    smp[j] = -suc[j] * Q[j];
-    dsmpds[j] = -bb[j] * smp[j] * rs[j];
-    dsmpdw[j] = dsmpds[j] * rws[j];
   }
-  double qout[MAXSOI + 2], d1[MAXSOI + 2], d2[MAXSOI + 2], den[MAXSOI + 2], num[MAXSOI + 2];
-  for (int j = 1; j <= nl; j++) { qout[j] = 0.0; d1[j] = 0.0; d2[j] = 0.0; }
-  for (int j = 1; j <= nl - 1; j++) {
-    const double dk1 = 0.5 * dhkdw[j] * rws[j];
-    const double dk2 = 0.5 * dhkdw[j] * rws[j + 1];
-    num[j] = smp[j + 1] - smp[j];
-    den[j] = M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld));
-    rden[j] = 1.0 / den[j];
-    qout[j] = -hk[j] * num[j] * rden[j] + hk[j];
-    d1[j] = (hk[j] * dsmpdw[j] - dk1 * num[j]) * rden[j] + dk1;
-    d2[j] = (-hk[j] * dsmpdw[j + 1] - dk2 * num[j]) * rden[j] + dk2;
-  }
+  struct Hyd { double e, hk, dhkdw, smp, dsmpds, dsmpdw; };
+  auto hyd = [&](int j) -> Hyd {
+    Hyd h;
+    h.e = 2.0 * bb[j] + 3.0;
+    h.hk = imp[j] * ks[j] * P[j];
+    h.dhkdw = h.e * h.hk * rs1[j];
+    h.smp = -suc[j] * Q[j];
+    h.dsmpds = -bb[j] * h.smp * rs[j];
+    h.dsmpdw = h.dsmpds * rws[j];
+    return h;
+  };
+  // the water-table boundary is active when the bottom level lies above the table
   bool wt_active = false;
   if (lower_bc == CLMGB_BC_WATERTABLE) {
     int jwt = nlevsoi;
     for (int jj = 1; jj <= nlevsoi; jj++) {
       if (f.zwt[c] <= LVc(f.zi, c, joff_zi + jj, ld)) { jwt = jj - 1; break; }
     }
-    if (nl <= jwt) {
-      wt_active = true;
-      const double dk1l = dhkdw[nl] * rws[nl];
-      num[nl] = -smp[nl];
-      den[nl] = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + nl, ld));
-      rden[nl] = 1.0 / den[nl];
-      qout[nl] = -hk[nl] * num[nl] * rden[nl] + hk[nl];
-      d1[nl] = (hk[nl] * dsmpdw[nl] - dk1l * num[nl]) * rden[nl] + dk1l;
-    }
-  } else if (lower_bc == CLMGB_BC_FLUX) {
-    qout[nl] = hk[nl];
-    d1[nl] = dhkdw[nl] * rws[nl];
+    wt_active = nl <= jwt;
   }
-  double dtdz[MAXSOI + 2], amx[MAXSOI + 2], bmx[MAXSOI + 2], cmx[MAXSOI + 2], dwat[MAXSOI + 2], gam[MAXSOI + 2];
+  // fluxes (:1310-1378), the band (:1380-1412) and the forward Thomas sweep, level by level
+  double qout_p = 0.0, d1_p = 0.0, d2_p = 0.0;          // interface j-1
+  double d1_nl = 0.0;
+  double rbet = 0.0;
+  Hyd hn = hyd(1);
   for (int j = 1; j <= nl; j++) {
-    const double qin = j == 1 ? f.qflx_infl[c] : qout[j - 1];
-    const double i0 = j == 1 ? 0.0 : d1[j - 1];
-    const double i1 = j == 1 ? 0.0 : d2[j - 1];
-    const double fnet = qin - qout[j] - LVc(f.qflx_rootsoi, c, j, ld);
+    const Hyd hj = hn;
+    double qo = 0.0, d1 = 0.0, d2 = 0.0;
+    if (j < nl) {
+      hn = hyd(j + 1);
+      const double dk1 = 0.5 * hj.dhkdw * rws[j];
+      const double dk2 = 0.5 * hj.dhkdw * rws[j + 1];
+      const double num = hn.smp - hj.smp;
+      rden[j] = 1.0 / (M_TO_MM * (LVc(f.z, c, joff + j + 1, ld) - LVc(f.z, c, joff + j, ld)));
+      qo = -hj.hk * num * rden[j] + hj.hk;
+      d1 = (hj.hk * hj.dsmpdw - dk1 * num) * rden[j] + dk1;
+      d2 = (-hj.hk * hn.dsmpdw - dk2 * num) * rden[j] + dk2;
+    } else if (wt_active) {
+      const double dk1l = hj.dhkdw * rws[nl];
+      const double num = -hj.smp;
+      rden[nl] = 1.0 / (M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + nl, ld)));
+      qo = -hj.hk * num * rden[nl] + hj.hk;
+      d1 = (hj.hk * hj.dsmpdw - dk1l * num) * rden[nl] + dk1l;
+    } else if (lower_bc == CLMGB_BC_FLUX) {
+      qo = hj.hk;
+      d1 = hj.dhkdw * rws[nl];
+    }
+    if (j == nl) d1_nl = d1;
+    const double qin = j == 1 ? f.qflx_infl[c] : qout_p;
+    const double i0 = j == 1 ? 0.0 : d1_p;
+    const double i1 = j == 1 ? 0.0 : d2_p;
+    const double fnet = qin - qo - LVc(f.qflx_rootsoi, c, j, ld);
     dtdz[j] = dtsub / (M_TO_MM * dzv[j]);
     amx[j] = i0 * dtdz[j];
-    bmx[j] = -1.0 - (-i1 + d1[j]) * dtdz[j];
-    cmx[j] = j == nl ? 0.0 : -d2[j] * dtdz[j];
-    dwat[j] = -fnet * dtdz[j];     // right-hand side, solved in place below
-  }
-  {
-    double bet = bmx[1];
-    if (abs_lt(bet, 1.0e-30)) bet = 1.0e-30;
-    double rbet = 1.0 / bet;
-    dwat[1] = dwat[1] * rbet;
-    for (int j = 2; j <= nl; j++) {
-      gam[j] = cmx[j - 1] * rbet;
-      bet = bmx[j] - amx[j] * gam[j];
+    bmx[j] = -1.0 - (-i1 + d1) * dtdz[j];
+    cmx[j] = j == nl ? 0.0 : -d2 * dtdz[j];
+    const double rhs = -fnet * dtdz[j];
+    if (j == 1) {
+      double bet = bmx[1];
+      if (abs_lt(bet, 1.0e-30)) bet = 1.0e-30;
+      rbet = 1.0 / bet;
+      dwat[1] = rhs * rbet;
+    } else {
+      gc[j] = cmx[j - 1] * rbet;
+      double bet = bmx[j] - amx[j] * gc[j];
       if (abs_lt(bet, 1.0e-30)) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
       rbet = 1.0 / bet;
-      dwat[j] = (dwat[j] - amx[j] * dwat[j - 1]) * rbet;
+      dwat[j] = (rhs - amx[j] * dwat[j - 1]) * rbet;
     }
-    for (int j = nl - 1; j >= 1; j--) dwat[j] = dwat[j] - gam[j + 1] * dwat[j + 1];
+    qout_p = qo;
+    d1_p = d1;
+    d2_p = d2;
   }
+  for (int j = nl - 1; j >= 1; j--) dwat[j] = dwat[j] - gc[j + 1] * dwat[j + 1];
   // ---- reverse: update and drainage ----
-  double g[MAXSOI + 2], hkb[MAXSOI + 2], dhkdwb[MAXSOI + 2], qoutb[MAXSOI + 2], d1b[MAXSOI + 2], d2b[MAXSOI + 2];
-  for (int j = 1; j <= nl; j++) {
-    g[j] = lamL[j] * (M_TO_MM * dzv[j]);
-    hkb[j] = 0.0; dhkdwb[j] = 0.0; qoutb[j] = 0.0; d1b[j] = 0.0; d2b[j] = 0.0;
-  }
+  MfAcc a0, a1, a2;                                       // levels j, j+1, j+2
+  mf_acc_zero(a0);
+  mf_acc_zero(a1);
+  mf_acc_zero(a2);
+  double QB = 0.0, D1B = 0.0, D2B = 0.0;                 // interface j, carried from level j+1
   const double cq = lamQ * (dtsub / dtime);
+  double gnl = 0.0;
   if (lower_bc == CLMGB_BC_FLUX) {
-    hkb[nl] += cq;
-    dhkdwb[nl] += cq * dwat[nl];
-    g[nl] += cq * dhkdw[nl];
+    a0.hkb += cq;
+    a0.dhkdwb += cq * dwat[nl];
+    gnl = cq * hyd(nl).dhkdw;
   } else if (lower_bc != CLMGB_BC_ZERO_FLUX) {
-    qoutb[nl] += cq;
-    d1b[nl] += cq * dwat[nl];
-    g[nl] += cq * d1[nl];
+    QB += cq;
+    D1B += cq * dwat[nl];
+    gnl = cq * d1_nl;
   }
-  // ---- reverse: the tridiagonal solve (transposed Thomas sweep) ----
-  double lam[MAXSOI + 2];
+  // ---- reverse: the tridiagonal solve, forward sweep on the transposed bands ----
+  // A^T: sub_j = cmx[j-1], diag bmx[j], super_j = amx[j+1]; gc now holds cp
   {
-    double cp[MAXSOI + 2];
-    // A^T: sub_j = cmx[j-1], diag bmx[j], super_j = amx[j+1]
     const double rb1 = 1.0 / bmx[1];
-    cp[1] = (nl > 1 ? amx[2] : 0.0) * rb1;
-    lam[1] = g[1] * rb1;
+    gc[1] = (nl > 1 ? amx[2] : 0.0) * rb1;
+    lam[1] = (lamL[1] * (M_TO_MM * dzv[1]) + (nl == 1 ? gnl : 0.0)) * rb1;
     for (int j = 2; j <= nl; j++) {
       const double sub = cmx[j - 1];
-      const double rdn = 1.0 / (bmx[j] - sub * cp[j - 1]);
-      cp[j] = (j < nl ? amx[j + 1] : 0.0) * rdn;
-      lam[j] = (g[j] - sub * lam[j - 1]) * rdn;
+      const double rdn = 1.0 / (bmx[j] - sub * gc[j - 1]);
+      gc[j] = (j < nl ? amx[j + 1] : 0.0) * rdn;
+      const double gj = lamL[j] * (M_TO_MM * dzv[j]) + (j == nl ? gnl : 0.0);
+      lam[j] = (gj - sub * lam[j - 1]) * rdn;
     }
-    for (int j = nl - 1; j >= 1; j--) lam[j] = lam[j] - cp[j] * lam[j + 1];
   }
-  // ---- reverse: assembly ----
-  for (int j = 1; j <= nl; j++) {
-    const double bmxb = -lam[j] * dwat[j];
-    const double fnetb = -lam[j] * dtdz[j];
-    // fnet_j = qin_j - qout_j - rootsoi_j ; qin_j = qout_{j-1} (j > 1)
-    qoutb[j] -= fnetb;
-    if (j > 1) {
-      qoutb[j - 1] += fnetb;
-      d1b[j - 1] += (-lam[j] * dwat[j - 1]) * dtdz[j];   // amx = dqidw0 dt_dz, dqidw0_j = dqodw1_{j-1}
-      d2b[j - 1] += bmxb * dtdz[j];                       // bmx: -(-dqidw1) dt_dz, dqidw1_j = dqodw2_{j-1}
+  // ---- reverse: one downward sweep (back substitution, assembly, fluxes, hydraulics) ----
+  double lam_n = 0.0;                                     // lambda of level j+1
+  for (int j = nl; j >= -1; j--) {
+    if (j >= 1) {
+      const double lj = (j == nl) ? lam[nl] : lam[j] - gc[j] * lam_n;
+      lam_n = lj;
+      // assembly (:1380-1412) of level j
+      const double bmxb = -lj * dwat[j];
+      const double fnetb = -lj * dtdz[j];
+      QB -= fnetb;
+      D1B -= bmxb * dtdz[j];
+      if (j < nl) D2B -= (-lj * dwat[j + 1]) * dtdz[j];
+      // the contributions of level j to interface j-1: fnet_j = qout_{j-1} - ...,
+      // amx_j = dqodw1_{j-1} dt_dz, bmx_j = -(-dqodw2_{j-1}) dt_dz
+      double QBn = 0.0, D1Bn = 0.0, D2Bn = 0.0;
+      if (j > 1) {
+        QBn = fnetb;
+        D1Bn = (-lj * dwat[j - 1]) * dtdz[j];
+        D2Bn = bmxb * dtdz[j];
+      }
+      // interface j (complete)
+      const Hyd hj = hyd(j);
+      if (j < nl) {
+        const Hyd hn2 = hyd(j + 1);
+        const double dk1 = 0.5 * hj.dhkdw * rws[j];
+        const double dk2 = 0.5 * hj.dhkdw * rws[j + 1];
+        const double num = hn2.smp - hj.smp;
+        const double r = 1.0 - num * rden[j];
+        a0.hkb += QB * r + D1B * hj.dsmpdw * rden[j] - D2B * hn2.dsmpdw * rden[j];
+        const double numb = -QB * hj.hk * rden[j] - D1B * dk1 * rden[j] - D2B * dk2 * rden[j];
+        a0.dsmpdwb += D1B * hj.hk * rden[j];
+        a1.dsmpdwb -= D2B * hj.hk * rden[j];
+        const double dk1b = D1B * r, dk2b = D2B * r;
+        a1.smpb += numb;
+        a0.smpb -= numb;
+        a0.dhkdwb += 0.5 * dk1b * rws[j] + 0.5 * dk2b * rws[j + 1];
+        a0.wsb -= dk1b * dk1 * rws[j];
+        a1.wsb -= dk2b * dk2 * rws[j + 1];
+      } else if (lower_bc == CLMGB_BC_FLUX) {
+        a0.hkb += QB;
+        a0.dhkdwb += D1B * rws[nl];
+        a0.wsb -= D1B * d1_nl * rws[nl];
+      } else if (wt_active) {
+        const double dk1l = hj.dhkdw * rws[nl];
+        const double num = -hj.smp;
+        double numb = QB * (-hj.hk * rden[nl]);
+        a0.hkb += QB * (1.0 - num * rden[nl]);
+        a0.hkb += D1B * hj.dsmpdw * rden[nl];
+        a0.dsmpdwb += D1B * hj.hk * rden[nl];
+        const double dk1lb = D1B * (1.0 - num * rden[nl]);
+        numb += D1B * (-dk1l * rden[nl]);
+        a0.smpb -= numb;
+        a0.dhkdwb += dk1lb * rws[nl];
+        a0.wsb -= dk1lb * dk1l * rws[nl];
+      }
+      QB = QBn;
+      D1B = D1Bn;
+      D2B = D2Bn;
     }
-    d1b[j] -= bmxb * dtdz[j];
-    if (j < nl) d2b[j] -= (-lam[j] * dwat[j + 1]) * dtdz[j];
-  }
-  // ---- reverse: fluxes ----
-  double smpb[MAXSOI + 2], dsmpdwb[MAXSOI + 2];
-  for (int j = 1; j <= nl; j++) { smpb[j] = 0.0; dsmpdwb[j] = 0.0; }
-  double wsb[MAXSOI + 2];
-  for (int j = 1; j <= nl; j++) wsb[j] = 0.0;
-  if (lower_bc == CLMGB_BC_FLUX) {
-    hkb[nl] += qoutb[nl];
-    dhkdwb[nl] += d1b[nl] * rws[nl];
-    wsb[nl] -= d1b[nl] * d1[nl] * rws[nl];
-  } else if (wt_active) {
-    const double dk1l = dhkdw[nl] * rws[nl];
-    double numb = qoutb[nl] * (-hk[nl] * rden[nl]);
-    hkb[nl] += qoutb[nl] * (1.0 - num[nl] * rden[nl]);
-    hkb[nl] += d1b[nl] * dsmpdw[nl] * rden[nl];
-    dsmpdwb[nl] += d1b[nl] * hk[nl] * rden[nl];
-    const double dk1lb = d1b[nl] * (1.0 - num[nl] * rden[nl]);
-    numb += d1b[nl] * (-dk1l * rden[nl]);
-    smpb[nl] -= numb;
-    dhkdwb[nl] += dk1lb * rws[nl];
-    wsb[nl] -= dk1lb * dk1l * rws[nl];
-  }
-  for (int j = 1; j <= nl - 1; j++) {
-    const double dk1 = 0.5 * dhkdw[j] * rws[j];
-    const double dk2 = 0.5 * dhkdw[j] * rws[j + 1];
-    const double r = 1.0 - num[j] * rden[j];
-    hkb[j] += qoutb[j] * r + d1b[j] * dsmpdw[j] * rden[j] - d2b[j] * dsmpdw[j + 1] * rden[j];
-    double numb = -qoutb[j] * hk[j] * rden[j] - d1b[j] * dk1 * rden[j] - d2b[j] * dk2 * rden[j];
-    dsmpdwb[j] += d1b[j] * hk[j] * rden[j];
-    dsmpdwb[j + 1] -= d2b[j] * hk[j] * rden[j];
-    const double dk1b = d1b[j] * r, dk2b = d2b[j] * r;
-    smpb[j + 1] += numb;
-    smpb[j] -= numb;
-    dhkdwb[j] += 0.5 * dk1b * rws[j] + 0.5 * dk2b * rws[j + 1];
-    wsb[j] -= dk1b * dk1 * rws[j];
-    wsb[j + 1] -= dk2b * dk2 * rws[j + 1];
-  }
-  // ---- reverse: hydraulic properties ----
-  double sb[MAXSOI + 2];
-  for (int j = 1; j <= nl; j++) sb[j] = 0.0;
-  for (int j = 1; j <= nl; j++) {
-    const double dsb = dsmpdwb[j] * rws[j];
-    wsb[j] -= dsmpdwb[j] * dsmpdw[j] * rws[j];
-    R.b[j] += dsb * (-smp[j] * rs[j]);
-    smpb[j] += dsb * (-bb[j] * rs[j]);
-    sb[j] += dsb * (-dsmpds[j] * rs[j]);
-    R.suc[j] += smpb[j] * (-Q[j]);
-    const double Qb = smpb[j] * (-suc[j]);
-    sb[j] += Qb * (-bb[j]) * Q[j] * rs[j];
-    if (Qb != 0.0) R.b[j] += Qb * Q[j] * (-Ls[j]);
-    double eb = dhkdwb[j] * hk[j] * rs1[j];
-    hkb[j] += dhkdwb[j] * e[j] * rs1[j];
-    double s1cb = dhkdwb[j] * (-dhkdw[j] * rs1[j]);
-    R.imp[j] += hkb[j] * ks[j] * P[j];
-    R.ks[j] += hkb[j] * imp[j] * P[j];
-    const double Pb = hkb[j] * imp[j] * ks[j];
-    s1cb += Pb * e[j] * P[j] * rs1[j];
-    if (Pb != 0.0) eb += Pb * P[j] * L1[j];
-    R.b[j] += 2.0 * eb;
-    if (s1pass[j]) {
-      if (j == nl) {
-        sb[j] += s1cb;
-      } else {
-        sb[j] += 0.5 * s1cb;
-        sb[j + 1] += 0.5 * s1cb;
+    // hydraulic properties of level m = j+1 (:1288-1308)
+    const int m = j + 1;
+    if (m >= 1 && m <= nl) {
+      const Hyd h = hyd(m);
+      MfAcc& A = a1;
+      const double dsb = A.dsmpdwb * rws[m];
+      A.wsb -= A.dsmpdwb * h.dsmpdw * rws[m];
+      R.b[m] += dsb * (-h.smp * rs[m]);
+      A.smpb += dsb * (-bb[m] * rs[m]);
+      A.sb += dsb * (-h.dsmpds * rs[m]);
+      R.suc[m] += A.smpb * (-Q[m]);
+      const double Qb = A.smpb * (-suc[m]);
+      A.sb += Qb * (-bb[m]) * Q[m] * rs[m];
+      if (Qb != 0.0) R.b[m] += Qb * Q[m] * (-Ls[m]);
+      double eb = A.dhkdwb * h.hk * rs1[m];
+      A.hkb += A.dhkdwb * h.e * rs1[m];
+      double s1cb = A.dhkdwb * (-h.dhkdw * rs1[m]);
+      R.imp[m] += A.hkb * ks[m] * P[m];
+      R.ks[m] += A.hkb * imp[m] * P[m];
+      const double Pb = A.hkb * imp[m] * ks[m];
+      s1cb += Pb * h.e * P[m] * rs1[m];
+      if (Pb != 0.0) eb += Pb * P[m] * L1[m];
+      R.b[m] += 2.0 * eb;
+      if ((s1pass >> m) & 1u) {
+        if (m == nl) {
+          A.sb += s1cb;
+        } else {
+          A.sb += 0.5 * s1cb;
+          a2.sb += 0.5 * s1cb;
+        }
       }
     }
-  }
-  for (int j = 1; j <= nl; j++) {
-    double lb = lamL[j];
-    if (spass[j]) {
-      const double vwcb = sb[j] * rws[j];
-      wsb[j] -= sb[j] * s0[j] * rws[j];
-      if (lpass[j]) lb += vwcb / (dzv[j] * DENH2O);
+    // saturation and the water of level k = j+2 (:1283-1287)
+    const int k = j + 2;
+    if (k >= 1 && k <= nl) {
+      double lb = lamL[k];
+      if ((spass >> k) & 1u) {
+        const double vwcb = a2.sb * rws[k];
+        a2.wsb -= a2.sb * s0[k] * rws[k];
+        if ((lpass >> k) & 1u) lb += vwcb / (dzv[k] * DENH2O);
+      }
+      lamL[k] = lb;
+      R.ws[k] += a2.wsb;
     }
-    lamL[j] = lb;
-    R.ws[j] += wsb[j];
+    a2 = a1;
+    a1 = a0;
+    mf_acc_zero(a0);
   }
 }
 
