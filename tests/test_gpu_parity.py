@@ -478,3 +478,67 @@ def test_tridiagonal_pcr_known_answers():
         ran += 1
     h.close()
     assert ran == 4
+
+
+@pytest.mark.parametrize("mode", ["queue", "queue_reserved", "waves", "fused"])
+@pytest.mark.parametrize("cfg_id", [1, 2])
+def test_column_step_at_maximum_level_counts(cfg_id, mode):
+    """The largest level counts the ABI accepts (12 snow, 25 ground, 25 soil levels:
+    37 levels and a 38-row band system, the Richards solve over 25 levels, the packed
+    refresh's shared block and the record pre-pass at their largest), with ragged bedrock
+    depths and a partial last tile of columns: the oracle's bits after 6 steps."""
+    vp = abi.Varpar(abi.MAX_NLEVSNO, abi.MAX_NLEVGRND, abi.MAX_NLEVSOI, 5, abi.MAX_NLEVGRND, 0)
+    nsteps, nc = 6, 3000
+    wl = synth.make_workload(cfg_id, nc=nc, seed=77 + cfg_id, nsteps=nsteps, vp=vp)
+    st = wl.state
+    rng = np.random.default_rng(cfg_id)
+    st["col_nbedrock"][:] = rng.integers(1, vp.nlevsoi + 1, nc)
+    Gf, If = wl.forcing_block(range(nsteps))
+    ref = st.copy()
+    status_ref = orc.run_steps(ref, wl.dtime, Gf, If)
+    assert np.all(status_ref == 0)
+    d = st.to_device()
+    h = api.Handle(st.vp)
+    h.set_option(abi.OPT_STEP_SCHEDULE, {"fused": abi.SCHEDULE_FUSED, "waves": abi.SCHEDULE_WAVES}.get(
+        mode, abi.SCHEDULE_QUEUE))
+    if mode in ("queue_reserved", "waves"):
+        h.reserve(nc)
+    Gd, Id = _dev(Gf), _dev(If)
+    for t in range(nsteps):
+        api.synth_forcing(h, d, Gd[t], Id[t])
+        api.column_step(h, d, wl.dtime)
+    torch.cuda.synchronize()
+    assert h.device_status() == 0
+    h.close()
+    got = d.to_host()
+    for k in ("t_soisno", "h2osoi_liq", "h2osoi_ice", "num_substeps", "qcharge", "t_grnd", "imelt", "smp_l",
+              "hk_l", "fact", "icefrac"):
+        assert np.array_equal(got[k].view(np.uint64) if got[k].dtype == np.float64 else got[k],
+                              ref[k].view(np.uint64) if ref[k].dtype == np.float64 else ref[k]), k
+
+
+def test_zero_columns_is_a_no_op():
+    """Calls over zero columns return CLMGB_OK before they read a field (the reference's
+    loops over an empty filter do nothing); the handle's device status stays 0."""
+    import ctypes as C
+    vp = synth.clm5_varpar()
+    h = api.Handle(vp)
+    lib = h.lib
+    b = abi.Bounds(0, 0, 0, 0, 0)
+    ft, fw = abi.SoilTempFields(), abi.SoilWaterFields()
+    ft.struct_size, fw.struct_size = C.sizeof(ft), C.sizeof(fw)
+    cfg = abi.SwmConfig.clm5_default()
+    ok = abi.CLMGB_OK
+    assert lib.clmgb_soil_temperature(h.h, C.byref(b), C.byref(ft), 1800.0, 1, 0, None, None) == ok
+    assert lib.clmgb_soil_water_fractions(h.h, C.byref(b), C.byref(fw), None) == ok
+    assert lib.clmgb_soil_water(h.h, C.byref(b), C.byref(fw), C.byref(cfg), 1800.0, None, None) == ok
+    assert lib.clmgb_column_step(h.h, C.byref(b), C.byref(ft), C.byref(fw), C.byref(cfg), 1800.0, 1, None, None,
+                                 None, None) == ok
+    assert lib.clmgb_synth_forcing(h.h, C.byref(b), C.byref(ft), C.byref(fw), None, None, None) == ok
+    assert lib.clmgb_tridiagonal_multi(h.h, 0, 0, 20, None, None, None, None, None, None, None, None) == ok
+    assert lib.clmgb_batched_band_solve(h.h, 0, 0, 38, None, None, None, None, None, None, 2, 2, 12, None) == ok
+    assert lib.clmgb_soil_water_noalloc(C.byref(vp), C.byref(b), C.byref(fw), C.byref(cfg), 1800.0, None,
+                                        None) == ok
+    torch.cuda.synchronize()
+    assert h.device_status() == 0
+    h.close()
