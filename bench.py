@@ -79,7 +79,9 @@ def parse():
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start leg")
     ap.add_argument("--warm-train-nc", type=int, default=262144)
     ap.add_argument("--warm-train-steps", type=int, default=8)
-    ap.add_argument("--warm-eval-steps", type=int, default=20)
+    ap.add_argument("--warm-eval-steps", type=int, default=1000,
+                    help="steps of the warm-start evaluation (the learned warm start's workload: 1,000 steps of "
+                         "the scale workload)")
     ap.add_argument("--warm-epochs", type=int, default=3)
     return ap.parse_args()
 
@@ -464,7 +466,7 @@ def warm_leg(args, wl_eval):
     cols = np.linspace(0, wl_eval.state.nc - 1, 256).astype(np.int64)
     sub = wl_eval.state.subset(cols)
     ref = sub.copy()
-    Gh, Ih = G.cpu().numpy()[:, cols], I.cpu().numpy()[:, cols]
+    Gh, Ih = wl_eval.forcing_block(range(ne + 2), cols=cols)
     orc.run_steps(ref, wl_eval.dtime, Gh[:ne + 2], Ih[:ne + 2], cfg)
     conv_cfg = abi.SwmConfig.clm5_default()
     conv_cfg.xTolerUpper = cfg.xTolerUpper / 100.0
