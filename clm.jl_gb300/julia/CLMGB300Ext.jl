@@ -583,20 +583,24 @@ function column_step_vjp!(ft_buf, fw_buf, b::Bounds, cfg::SwmConfig, dtime, snow
 end
 
 # Substep log (clmgb_substep_log): the forward step writes it, the reverse reads it,
-# so the reverse does not run the Richards substep loop again.  rec holds
-# LOG_STRIDE(cap) Float64 per column, count one Int32 per column.
+# so the reverse runs neither the Richards substep loop nor soil_temperature! again.
+# rec holds LOG_STRIDE(cap) Float64 per column, count one Int32 per column, st_rec
+# LOG_ST_STRIDE Float64 per column (soil_temperature!'s factorisation and end state).
 struct SubstepLog
     struct_size::Int64
     rec::Ptr{Cvoid}
     count::Ptr{Cvoid}
     cap::Int32
+    st_rec::Ptr{Cvoid}
 end
 const LOG_REC = 25 + 2                  # CLMGB_MAX_NLEVSOI + 2
 const LOG_FIN = 3 * 25 + 3
+const LOG_ST_STRIDE = 464               # CLMGB_LOG_ST_STRIDE
 log_stride(cap) = cap * LOG_REC + LOG_FIN
 new_substep_log(nc::Integer, cap::Integer = 24) =
-    (rec = CUDA.zeros(Float64, nc * log_stride(cap)), count = CUDA.fill(Int32(-1), nc), cap = Int32(cap))
-log_struct(lg) = SubstepLog(sizeof(SubstepLog), ptr(lg.rec), ptr(lg.count), lg.cap)
+    (rec = CUDA.zeros(Float64, nc * log_stride(cap)), count = CUDA.fill(Int32(-1), nc), cap = Int32(cap),
+     st_rec = CUDA.zeros(Float64, nc * LOG_ST_STRIDE))
+log_struct(lg) = SubstepLog(sizeof(SubstepLog), ptr(lg.rec), ptr(lg.count), lg.cap, ptr(lg.st_rec))
 
 function column_step_logged!(ft_buf, fw_buf, b::Bounds, cfg::SwmConfig, dtime, snow_method, t_ssbef,
                              t_h2osfc_bef, lg)
