@@ -77,8 +77,10 @@ def parse():
     ap.add_argument("--adj-entries", type=int, default=256,
                     help="tape entries per slot (the recording kernel only; the default adjoint needs none)")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start leg")
-    ap.add_argument("--warm-train-nc", type=int, default=262144)
-    ap.add_argument("--warm-train-steps", type=int, default=8)
+    ap.add_argument("--warm-train-nc", type=int, default=65536)
+    ap.add_argument("--warm-train-steps", type=int, default=1000,
+                    help="length of the training trajectory (pairs recorded every --warm-record-every steps)")
+    ap.add_argument("--warm-record-every", type=int, default=31)
     ap.add_argument("--warm-eval-steps", type=int, default=1000,
                     help="steps of the warm-start evaluation (the learned warm start's workload: 1,000 steps of "
                          "the scale workload)")
@@ -367,7 +369,8 @@ def warm_leg(args, wl_eval):
     Gt, It = wt.forcing_block(range(args.warm_train_steps + 4))
     Gt, It = torch.from_numpy(Gt).cuda(), torch.from_numpy(It).cuda()
     st = wt.state.to_device()
-    F, T = mlp.generate_samples(h, st, Gt, It, args.warm_train_steps, wt.dtime, per_column=1)
+    F, T = mlp.generate_samples(h, st, Gt, It, args.warm_train_steps, wt.dtime, per_column=1,
+                                record_every=args.warm_record_every)
     gen_s = time.time() - t0
     n_pairs = int(F.shape[0])
     model = mlp.WarmStartMLP(h, seed=0)
@@ -399,12 +402,14 @@ def warm_leg(args, wl_eval):
         return e0.elapsed_time(e1), float(nsub.sum()) / (steps * state.nc)
 
     # ---- decision margin, chosen on the training workload ----
+    # (from the state at the end of the training trajectory)
     tune = {}
     for m in (0.0, 0.5, 1.0):
         model.margin = m
-        s2 = wt.state.to_device()
+        s2 = st.copy()
         ms, att = run(s2, Gt, It, 4, True, t_first=args.warm_train_steps)
         tune[m] = {"ms": ms, "attempts": att}
+        del s2
     model.margin = min(tune, key=lambda m: tune[m]["ms"])
     del st
     # ---- evaluation on the scale workload ----
@@ -432,6 +437,20 @@ def warm_leg(args, wl_eval):
     es, eh = api.balance_residuals(h, s2, wl_eval.dtime, tg0, bw)
     warm_balance = {"errsoi_max_abs_w_m2": float(es.abs().max()), "errh2o_max_abs_mm": float(eh.abs().max())}
     del s2
+    # ---- where the time goes: levels of attempts and of hydraulic refreshes per
+    #      column-step in each arm (kernel-counted, an untimed pass of 20 steps) ----
+    work = {}
+    for mode in ("plain", "warm"):
+        s2 = wl_eval.state.to_device()
+        run(s2, G, I, 2, mode == "warm")
+        h.set_option(abi.OPT_COUNT_WORK, 1)
+        run(s2, G, I, 20, mode == "warm", t_first=2)
+        la, lr = h.get_option(abi.OPT_WORK_LEVEL_ATTEMPTS), h.get_option(abi.OPT_WORK_LEVEL_REFRESHES)
+        h.set_option(abi.OPT_COUNT_WORK, 0)
+        nl = float(wl_eval.state["col_nbedrock"].mean())
+        work[mode] = {"attempts_per_column_step": la / (20 * s2.nc * nl),
+                      "refreshes_per_column_step": lr / (20 * s2.nc * nl)}
+        del s2
     # ---- the proposal's share of the warm-started step ----
     s2 = wl_eval.state.to_device()
     api.synth_forcing(h, s2, G[0], I[0])
@@ -461,42 +480,56 @@ def warm_leg(args, wl_eval):
     layers_ms = e0.elapsed_time(e1) / reps
     del s2, X
     # ---- error against the FP64 oracle on a sample of columns, and of both arms
-    #      against a converged solution (the oracle with both tolerances / 100) ----
+    #      against a converged solution (the oracle with both tolerances / 100), after
+    #      one step (the per-step error) and after all the evaluated steps (where the
+    #      trajectories of different tolerances have drifted apart) ----
     from oracle import oracle as orc
     cols = np.linspace(0, wl_eval.state.nc - 1, 256).astype(np.int64)
     sub = wl_eval.state.subset(cols)
-    ref = sub.copy()
     Gh, Ih = wl_eval.forcing_block(range(ne + 2), cols=cols)
-    orc.run_steps(ref, wl_eval.dtime, Gh[:ne + 2], Ih[:ne + 2], cfg)
     conv_cfg = abi.SwmConfig.clm5_default()
     conv_cfg.xTolerUpper = cfg.xTolerUpper / 100.0
     conv_cfg.xTolerLower = cfg.xTolerLower / 100.0
-    conv = sub.copy()
-    orc.run_steps(conv, wl_eval.dtime, Gh[:ne + 2], Ih[:ne + 2], conv_cfg)
-    errs, errs_conv = {}, {}
-    for mode in ("plain", "warm"):
+    Gs, Is = torch.from_numpy(np.ascontiguousarray(Gh)).cuda(), torch.from_numpy(np.ascontiguousarray(Ih)).cuda()
+
+    def gpu_liq(mode, n):
         d = sub.to_device()
-        Gs, Is = torch.from_numpy(np.ascontiguousarray(Gh)).cuda(), torch.from_numpy(np.ascontiguousarray(Ih)).cuda()
         dtv = torch.empty(d.nc, dtype=torch.float64, device="cuda")
-        for t in range(ne + 2):
+        for t in range(n):
             api.synth_forcing(h, d, Gs[t], Is[t])
-            api.column_step(h, d, wl_eval.dtime, cfg) if mode == "plain" else None
-            if mode == "warm":
+            if mode == "plain":
+                api.column_step(h, d, wl_eval.dtime, cfg)
+            else:
                 api.soil_temperature(h, d, wl_eval.dtime)
                 api.set_soil_water_fractions(h, d)
                 model.propose_first_dt(d, wl_eval.dtime, cfg, out=dtv)
                 mlp.soil_water_warm(h, d, wl_eval.dtime, dtv, cfg)
-        liq = d["h2osoi_liq"].cpu().numpy()
-        errs[mode] = float(np.max(np.abs(liq - ref["h2osoi_liq"])))
-        errs_conv[mode] = float(np.max(np.abs(liq - conv["h2osoi_liq"])))
+        return d["h2osoi_liq"].cpu().numpy()
+
+    def oracle_liq(c, n):
+        o = sub.copy()
+        orc.run_steps(o, wl_eval.dtime, Gh[:n], Ih[:n], c)
+        return o["h2osoi_liq"]
+
+    errs, errs_conv, errs1, errs1_conv = {}, {}, {}, {}
+    for n, e_ref, e_conv in ((1, errs1, errs1_conv), (ne + 2, errs, errs_conv)):
+        ref_l, conv_l = oracle_liq(cfg, n), oracle_liq(conv_cfg, n)
+        for mode in ("plain", "warm"):
+            liq = gpu_liq(mode, n)
+            e_ref[mode] = float(np.max(np.abs(liq - ref_l)))
+            e_conv[mode] = float(np.max(np.abs(liq - conv_l)))
     out = {"workload": "learned warm start: MLP 64-128-128-21 (SiLU, bf16/fp32), trained on %d pairs from the "
-                       "plain solver (%d columns x %d steps, other seed); evaluated on the scale workload, %d steps"
-                       % (n_pairs, args.warm_train_nc, args.warm_train_steps, ne),
+                       "plain solver (%d columns, every %d-th of %d steps, other seed); evaluated on the scale "
+                       "workload, %d steps" % (n_pairs, args.warm_train_nc, args.warm_record_every,
+                                               args.warm_train_steps, ne),
            "plain": res["plain"], "warm": res["warm"],
            "speedup": res["warm"]["value"] / res["plain"]["value"],
            "attempt_ratio": res["warm"]["attempts_per_column_step"] / res["plain"]["attempts_per_column_step"],
+           "work_per_column_step": work,
            "max_abs_liq_error_vs_oracle_mm": errs,
            "max_abs_liq_error_vs_converged_mm": errs_conv,
+           "first_step_max_abs_liq_error_vs_oracle_mm": errs1,
+           "first_step_max_abs_liq_error_vs_converged_mm": errs1_conv,
            "converged_reference": "the oracle with xTolerUpper and xTolerLower / 100",
            "error_sample_columns": 256, "balance": warm_balance,
            "proposal_ms": prop_ms, "proposal_share_of_warm_step": prop_ms / res["warm"]["ms_per_step"],

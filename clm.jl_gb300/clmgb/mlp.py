@@ -218,12 +218,15 @@ def soil_water_warm(handle, state, dtime, dt_first, cfg=None, col_status=None, s
 
 
 def generate_samples(handle, state, G, I, nsteps, dtime, per_column=1, capacity=None, cfg=None,
-                     snow_method=abi.SNOW_JORDAN1991):
+                     snow_method=abi.SNOW_JORDAN1991, record_every=1):
     """Runs nsteps plain steps (forcing, soil_temperature!, fractions, and the plain
-    Richards solve that records pairs) and returns (features [n, 64], targets [n, 32])."""
+    Richards solve, which records pairs at every `record_every`-th step, so the pairs
+    cover the states of a long trajectory) and returns (features [n, 64], targets [n, 32])."""
     import torch
     cfg = cfg or abi.SwmConfig.clm5_default()
-    cap = capacity or state.nc * nsteps * per_column
+    every = max(1, int(record_every))
+    nrec = (nsteps + every - 1) // every
+    cap = capacity or state.nc * nrec * per_column
     F = torch.empty((cap, IN), dtype=torch.float32, device="cuda")
     T = torch.empty((cap, OUTP), dtype=torch.float32, device="cuda")
     cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -231,6 +234,9 @@ def generate_samples(handle, state, G, I, nsteps, dtime, per_column=1, capacity=
         api.synth_forcing(handle, state, G[t], I[t])
         api.soil_temperature(handle, state, dtime, snow_method)
         api.set_soil_water_fractions(handle, state)
+        if t % every:
+            api.soil_water(handle, state, dtime, cfg)
+            continue
         check(handle.lib.clmgb_mlp_samples(handle.h, C.byref(state.bounds()), C.byref(state.soilwater_fields()),
                                            C.byref(cfg), float(dtime), int(per_column), _p(F), _p(T), _p(cnt), cap,
                                            None, _s(None)), "mlp_samples")
