@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--queue-order", type=int, default=None)
     ap.add_argument("--fresh-batch", type=int, default=None, help="CLMGB_OPT_QUEUE_FRESH_BATCH override")
     ap.add_argument("--defer", type=int, default=None, help="CLMGB_OPT_QUEUE_DEFER override")
+    ap.add_argument("--st-block", type=int, default=None, choices=[128, 320, 640],
+                    help="CLMGB_OPT_ST_BLOCK override (columns sorted together per soil-temperature block)")
     ap.add_argument("--records-tma", type=int, default=None, choices=[0, 1],
                     help="CLMGB_OPT_RECORDS_TMA override (tensor copies or plain loads in the Richards pre-pass)")
     ap.add_argument("--no-graph", action="store_true")
@@ -571,6 +573,8 @@ def run_ours(args):
         h.set_option(abi.OPT_QUEUE_DEFER, args.defer)
     if args.records_tma is not None:
         h.set_option(abi.OPT_RECORDS_TMA, args.records_tma)
+    if args.st_block is not None:
+        h.set_option(abi.OPT_ST_BLOCK, args.st_block)
     d = st.to_device()
     # per-step forcing, resident in HBM before the timed region
     Gd = torch.empty((nsteps, nc), dtype=torch.float64, device="cuda")

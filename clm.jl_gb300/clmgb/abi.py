@@ -75,6 +75,7 @@ OPT_WORK_LEVEL_REFRESHES = 23
 OPT_RECORDS_TMA = 24
 OPT_RECORDS_TMA_USED = 25
 OPT_TRIDIAG_METHOD = 26
+OPT_ST_BLOCK = 27
 TRIDIAG_THOMAS, TRIDIAG_PCR = 0, 1
 MAX_COPY_SEGMENTS = 128
 

@@ -54,6 +54,7 @@ struct clmgb_handle_s {
   int64_t records_tma;          // CLMGB_OPT_RECORDS_TMA
   int records_tma_used;         // CLMGB_OPT_RECORDS_TMA_USED
   int64_t tridiag_method;       // CLMGB_OPT_TRIDIAG_METHOD
+  int64_t st_block;             // CLMGB_OPT_ST_BLOCK
   cudaError_t last_error;
 };
 
@@ -121,7 +122,9 @@ static Dims make_dims(const clmgb_varpar& vp, const clmgb_bounds& b, int64_t c0 
 }
 
 static Dims hdims(clmgb_handle h, const clmgb_bounds& b) {
-  return make_dims(h->vp, b, h->column_base, (int)h->attempt_cap);
+  Dims D = make_dims(h->vp, b, h->column_base, (int)h->attempt_cap);
+  D.st_block = (int)h->st_block;
+  return D;
 }
 
 // every pointer member after struct_size must be non-NULL
@@ -230,6 +233,7 @@ int32_t clmgb_create(const clmgb_varpar* vp, clmgb_handle* out) {
   h->defer = CLMGB_DEFAULT_QUEUE_DEFER;
   h->packed = 1;
   h->records_tma = 1;
+  h->st_block = 320;
   h->step_schedule = CLMGB_SCHEDULE_QUEUE;
   h->queue_blocks_per_sm = CLMGB_DEFAULT_QUEUE_BLOCKS_PER_SM;
   h->scratch = nullptr;
@@ -862,6 +866,10 @@ int32_t clmgb_set_option(clmgb_handle h, int32_t key, int64_t value) {
       if (value != CLMGB_TRIDIAG_THOMAS && value != CLMGB_TRIDIAG_PCR) return CLMGB_ERR_CONFIG;
       h->tridiag_method = value;
       return CLMGB_OK;
+    case CLMGB_OPT_ST_BLOCK:
+      if (value != 128 && value != 320 && value != 640) return CLMGB_ERR_CONFIG;
+      h->st_block = value;
+      return CLMGB_OK;
     case CLMGB_OPT_COUNT_WORK: {
       if (value != 0 && value != 1) return CLMGB_ERR_CONFIG;
       if (value && !h->count_work) {    // counting starts from zero
@@ -902,6 +910,7 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
     case CLMGB_OPT_RECORDS_TMA: *value = h->records_tma; return CLMGB_OK;
     case CLMGB_OPT_RECORDS_TMA_USED: *value = h->records_tma_used; return CLMGB_OK;
     case CLMGB_OPT_TRIDIAG_METHOD: *value = h->tridiag_method; return CLMGB_OK;
+    case CLMGB_OPT_ST_BLOCK: *value = h->st_block; return CLMGB_OK;
     case CLMGB_OPT_WORK_LEVEL_ATTEMPTS:
     case CLMGB_OPT_WORK_LEVEL_REFRESHES: {
       unsigned long long w[2];

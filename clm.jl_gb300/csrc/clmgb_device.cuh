@@ -55,6 +55,7 @@ struct Dims {
   int64_t ldc, ldp, np;
   int64_t c0 = 0;    // global index of the call's first column (patch_column holds global indices)
   int attempt_cap = MF_ATTEMPT_CAP;   // Richards attempts after which a column stops (CLMGB_COL_SUBSTEP_CAP)
+  int st_block = 320;                 // threads per block of the soil-temperature kernels (CLMGB_OPT_ST_BLOCK)
 };
 
 // Julia Base.max / Base.min on Float64 (NaN propagates, -0.0 < 0.0).  They only

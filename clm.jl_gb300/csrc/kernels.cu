@@ -14,16 +14,17 @@ __device__ __forceinline__ void report(uint32_t st, uint32_t* col_status, uint32
   if (st && dev_status) atomicOr(dev_status, st);
 }
 
-// The column of this thread in the soil-temperature kernels: the block's BLOCK
+// The column of this thread in the soil-temperature kernels: the block's NB
 // consecutive columns, reordered by snow-layer count (a counting sort in shared
 // memory), so the lanes of a warp run level loops and band solves of about the same
 // length.  Accesses stay inside the block's columns; each column's arithmetic is
 // unchanged, so results do not depend on the order.  Every thread of the block must
 // call it; returns -1 past the last column.
+template <int NB>
 __device__ __forceinline__ int64_t snl_sorted_column(int64_t nc, const int64_t* col_snl, int nlevsno) {
   __shared__ unsigned int s_cnt[16];
-  __shared__ unsigned short s_perm[BLOCK];
-  const int64_t base = (int64_t)blockIdx.x * BLOCK;
+  __shared__ unsigned short s_perm[NB];
+  const int64_t base = (int64_t)blockIdx.x * NB;
   if (threadIdx.x < 16) s_cnt[threadIdx.x] = 0;
   __syncthreads();
   const int64_t c0 = base + threadIdx.x;
@@ -49,10 +50,12 @@ __device__ __forceinline__ int64_t snl_sorted_column(int64_t nc, const int64_t* 
   return c < nc ? c : -1;
 }
 
-__global__ void __launch_bounds__(BLOCK)
+// NB threads per block, sorted together; 640 / NB resident blocks (20 warps per SM)
+template <int NB>
+__global__ void __launch_bounds__(NB, 640 / NB)
 k_soil_temperature(Dims D, int64_t nc, clmgb_soiltemp_fields f, double dtime, int snow_method,
                    uint32_t* col_status, uint32_t* dev_status) {
-  const int64_t c = snl_sorted_column(nc, f.col_snl, D.nlevsno);
+  const int64_t c = snl_sorted_column<NB>(nc, f.col_snl, D.nlevsno);
   if (c < 0) return;
   uint32_t st = 0;
   if (f.mask_nolakec[c]) st = soil_temperature_col(D, f, c, dtime, snow_method);
@@ -119,12 +122,12 @@ struct FieldStateStLog : FieldState<clmgb_soiltemp_fields> {
 // soil_temperature! then set_soil_water_fractions! for one column per thread (the
 // first half of a column step; the Richards solve follows in k_moisture_form_queue).
 // With LOG every column soil_temperature! runs on also gets its record in st_log.
-template <bool LOG>
-__global__ void __launch_bounds__(BLOCK)
+template <bool LOG, int NB>
+__global__ void __launch_bounds__(NB, 640 / NB)
 k_soil_temperature_fractions(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fields fw,
                              double dtime, int snow_method, double* t_ssbef, double* t_h2osfc_bef,
                              uint32_t* col_status, uint32_t* dev_status, double* st_log) {
-  const int64_t c = snl_sorted_column(nc, ft.col_snl, D.nlevsno);
+  const int64_t c = snl_sorted_column<NB>(nc, ft.col_snl, D.nlevsno);
   if (c < 0) return;
   uint32_t st = 0;
   if (ft.mask_nolakec[c]) {
@@ -966,7 +969,13 @@ k_synth_forcing(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwater_fi
 cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
                                     int snow_method, uint32_t* col_status, uint32_t* dev_status,
                                     cudaStream_t s) {
-  k_soil_temperature<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f, dtime, snow_method, col_status, dev_status);
+  const unsigned g = (unsigned)((nc + D.st_block - 1) / D.st_block);
+  if (D.st_block == 640)
+    k_soil_temperature<640><<<g, 640, 0, s>>>(D, nc, f, dtime, snow_method, col_status, dev_status);
+  else if (D.st_block == 320)
+    k_soil_temperature<320><<<g, 320, 0, s>>>(D, nc, f, dtime, snow_method, col_status, dev_status);
+  else
+    k_soil_temperature<128><<<g, 128, 0, s>>>(D, nc, f, dtime, snow_method, col_status, dev_status);
   return cudaGetLastError();
 }
 cudaError_t launch_water_fractions(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f, cudaStream_t s) {
@@ -991,12 +1000,21 @@ cudaError_t launch_soiltemp_fractions(const Dims& D, int64_t nc, const clmgb_soi
                                       const clmgb_soilwater_fields& fw, double dtime, int snow_method,
                                       double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
                                       uint32_t* dev_status, cudaStream_t s, double* st_log) {
-  if (st_log)
-    k_soil_temperature_fractions<true><<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, dtime, snow_method, t_ssbef,
-                                                                      t_h2osfc_bef, col_status, dev_status, st_log);
-  else
-    k_soil_temperature_fractions<false><<<grid_for(nc), BLOCK, 0, s>>>(D, nc, ft, fw, dtime, snow_method, t_ssbef,
-                                                                       t_h2osfc_bef, col_status, dev_status, nullptr);
+  const int nb = (D.st_block == 640 || D.st_block == 320) ? D.st_block : 128;
+  const unsigned g = (unsigned)((nc + nb - 1) / nb);
+#define CLMGB_STF(L, NB) \
+  k_soil_temperature_fractions<L, NB><<<g, NB, 0, s>>>(D, nc, ft, fw, dtime, snow_method, t_ssbef, t_h2osfc_bef, \
+                                                      col_status, dev_status, st_log)
+  if (st_log) {
+    if (nb == 640) CLMGB_STF(true, 640);
+    else if (nb == 320) CLMGB_STF(true, 320);
+    else CLMGB_STF(true, 128);
+  } else {
+    if (nb == 640) CLMGB_STF(false, 640);
+    else if (nb == 320) CLMGB_STF(false, 320);
+    else CLMGB_STF(false, 128);
+  }
+#undef CLMGB_STF
   return cudaGetLastError();
 }
 int queue_blocks_per_sm() {

@@ -739,6 +739,9 @@ int32_t clmgb_last_cuda_error(clmgb_handle h);
                                             copies, 0 if it took plain loads */
 #define CLMGB_OPT_TRIDIAG_METHOD      26 /* solver of clmgb_tridiagonal_multi: CLMGB_TRIDIAG_THOMAS (default)
                                             or CLMGB_TRIDIAG_PCR */
+#define CLMGB_OPT_ST_BLOCK            27 /* columns per block of the soil-temperature kernels, sorted together
+                                            by snow-layer count so that a warp's lanes run loops of the same
+                                            length: 128, 320 (default) or 640.  Results do not depend on it. */
 #define CLMGB_TRIDIAG_THOMAS 0
 #define CLMGB_TRIDIAG_PCR    1
 #define CLMGB_OPT_COLUMN_BASE         15 /* global 0-based index of column 0 of the arrays the next calls

@@ -64,7 +64,7 @@ def test_header_constants_match_python():
                  "COL_FILTER", "OPT_ATTEMPT_CAP", "OPT_QUEUE_POLL_LIMIT", "OPT_QUEUE_PUBLISH_DELAY",
                  "OPT_COUNT_WORK", "OPT_WORK_LEVEL_ATTEMPTS", "OPT_WORK_LEVEL_REFRESHES", "COL_QUEUE_WAIT",
                  "LOG_ST_STRIDE", "OPT_RECORDS_TMA", "OPT_RECORDS_TMA_USED", "COL_COPY_WAIT",
-                 "OPT_TRIDIAG_METHOD", "TRIDIAG_THOMAS", "TRIDIAG_PCR"):
+                 "OPT_TRIDIAG_METHOD", "TRIDIAG_THOMAS", "TRIDIAG_PCR", "OPT_ST_BLOCK"):
         assert int(consts[name]) == getattr(abi, name), name
     for name in ("SH_FLOODC", "SH_SAT_EXCESS", "SH_QFLX_INPUTS", "SH_INFL_EXCESS", "SH_ROUTE", "SH_UPDATE_H2OSFC",
                  "SH_INFILTRATION", "SH_TOTAL_RUNOFF", "SH_URBAN_PONDING", "SH_ALL", "FSAT_TOPMODEL", "FSAT_VIC",
