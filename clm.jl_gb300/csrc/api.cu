@@ -11,6 +11,16 @@
 #include <initializer_list>
 #include "clmgb_device.cuh"
 #include "launch.h"
+#include <nvtx3/nvToolsExt.h>
+
+// An NVTX range around each compute entry point, so a profiler's timeline shows the
+// drop-in calls by name (no cost when no tool is attached).
+struct ClmgbRange {
+  explicit ClmgbRange(const char* name) { nvtxRangePushA(name); }
+  ~ClmgbRange() { nvtxRangePop(); }
+  ClmgbRange(const ClmgbRange&) = delete;
+  ClmgbRange& operator=(const ClmgbRange&) = delete;
+};
 
 #ifndef CLMGB_GIT_DESC
 #define CLMGB_GIT_DESC "dev"
@@ -305,6 +315,7 @@ int32_t clmgb_last_cuda_error(clmgb_handle h) {
 int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* f,
                                double dtime, int32_t snow_method, int32_t use_excess_ice,
                                uint32_t* col_status, void* stream) {
+  const ClmgbRange range_("clmgb_soil_temperature");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_bounds(b, true);
   if (e) return e;
@@ -320,6 +331,7 @@ int32_t clmgb_soil_temperature(clmgb_handle h, const clmgb_bounds* b, const clmg
 
 int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilflux_fields* f, double dtime,
                           void* stream) {
+  const ClmgbRange range_("clmgb_soil_fluxes");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_bounds(b, false);
   if (e) return e;
@@ -333,6 +345,7 @@ int32_t clmgb_soil_fluxes(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
 
 int32_t clmgb_soil_water_zd09(clmgb_handle h, const clmgb_bounds* b, const clmgb_zd09_fields* f,
                               const clmgb_swm_config* cfg, double dtime, void* stream) {
+  const ClmgbRange range_("clmgb_soil_water_zd09");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (!cfg) return CLMGB_ERR_NULL_ARG;
   // init_soilwater_movement (soil_water_movement.jl:681-698): ZD09 with the aquifer
@@ -351,6 +364,7 @@ int32_t clmgb_soil_water_zd09(clmgb_handle h, const clmgb_bounds* b, const clmgb
 int32_t clmgb_effec_rootfrac_vert_tran_sink(clmgb_handle h, const clmgb_bounds* b,
                                             const clmgb_rootsink_fields* f, int32_t use_hydrstress,
                                             uint32_t* col_status, void* stream) {
+  const ClmgbRange range_("clmgb_effec_rootfrac_vert_tran_sink");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_bounds(b, true);
   if (e) return e;
@@ -428,6 +442,7 @@ static bool surfhyd_pointers_ok(const clmgb_surfhyd_fields* f, const clmgb_surfh
 
 int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clmgb_surfhyd_fields* f,
                                 const clmgb_surfhyd_config* cfg, uint32_t stages, double dtime, void* stream) {
+  const ClmgbRange range_("clmgb_surface_hydrology");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (!f || !cfg) return CLMGB_ERR_NULL_ARG;
   if (f->struct_size != (int64_t)sizeof(clmgb_surfhyd_fields) ||
@@ -502,6 +517,7 @@ int32_t clmgb_copy_segments(void* const* dst, const void* const* src, const int6
 
 int32_t clmgb_balance_check_columns(clmgb_handle h, const clmgb_bounds* b, const clmgb_colbalance_fields* f,
                                     double dtime, clmgb_balance_report* report, void* stream) {
+  const ClmgbRange range_("clmgb_balance_check_columns");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (!f || !report) return CLMGB_ERR_NULL_ARG;
   if (f->struct_size != (int64_t)sizeof(clmgb_colbalance_fields)) return CLMGB_ERR_ABI;
@@ -543,6 +559,7 @@ int32_t clmgb_balance_check_columns(clmgb_handle h, const clmgb_bounds* b, const
 
 int32_t clmgb_lake_temperature(clmgb_handle h, const clmgb_bounds* b, const clmgb_lake_fields* f,
                                const clmgb_lake_config* cfg, double dtime, void* stream) {
+  const ClmgbRange range_("clmgb_lake_temperature");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (!f || !cfg) return CLMGB_ERR_NULL_ARG;
   if (f->struct_size != (int64_t)sizeof(clmgb_lake_fields) || cfg->struct_size != (int64_t)sizeof(clmgb_lake_config))
@@ -597,6 +614,7 @@ static bool snowlayer_pointers_ok(const clmgb_snowlayer_fields* f, const clmgb_s
 
 int32_t clmgb_snow_layers(clmgb_handle h, const clmgb_bounds* b, const clmgb_snowlayer_fields* f,
                           const clmgb_snowlayer_config* cfg, uint32_t stages, double dtime, void* stream) {
+  const ClmgbRange range_("clmgb_snow_layers");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (!cfg) return CLMGB_ERR_NULL_ARG;
   if (cfg->struct_size != (int64_t)sizeof(clmgb_snowlayer_config)) return CLMGB_ERR_ABI;
@@ -620,6 +638,7 @@ int32_t clmgb_snow_layers(clmgb_handle h, const clmgb_bounds* b, const clmgb_sno
 
 int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
                                    void* stream) {
+  const ClmgbRange range_("clmgb_soil_water_fractions");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_bounds(b, false);
   if (e) return e;
@@ -631,6 +650,7 @@ int32_t clmgb_soil_water_fractions(clmgb_handle h, const clmgb_bounds* b, const 
 
 int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
                          const clmgb_swm_config* cfg, double dtime, uint32_t* col_status, void* stream) {
+  const ClmgbRange range_("clmgb_soil_water");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_cfg(cfg);
   if (e) return e;
@@ -657,6 +677,7 @@ int32_t clmgb_soil_water(clmgb_handle h, const clmgb_bounds* b, const clmgb_soil
 
 int32_t clmgb_soil_water_flexible_cn(clmgb_handle h, const clmgb_bounds* b, const clmgb_flexcn_fields* f,
                                      void* stream) {
+  const ClmgbRange range_("clmgb_soil_water_flexible_cn");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_bounds(b, false);
   if (e) return e;
@@ -671,6 +692,7 @@ int32_t clmgb_column_step(clmgb_handle h, const clmgb_bounds* b, const clmgb_soi
                           const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
                           int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef, uint32_t* col_status,
                           void* stream) {
+  const ClmgbRange range_("clmgb_column_step");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_cfg(cfg);
   if (e) return e;
@@ -718,16 +740,19 @@ static int32_t phase_change_common(clmgb_handle h, const clmgb_bounds* b, const 
 
 int32_t clmgb_phase_change_h2osfc(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* f,
                                   double dtime, const double* dhsdT, void* stream) {
+  const ClmgbRange range_("clmgb_phase_change_h2osfc");
   return phase_change_common(h, b, f, dtime, dhsdT, 0, stream);
 }
 
 int32_t clmgb_phase_change_beta(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* f,
                                 double dtime, const double* dhsdT, void* stream) {
+  const ClmgbRange range_("clmgb_phase_change_beta");
   return phase_change_common(h, b, f, dtime, dhsdT, 1, stream);
 }
 
 int32_t clmgb_synth_forcing(clmgb_handle h, const clmgb_bounds* b, const clmgb_soiltemp_fields* ft,
                             const clmgb_soilwater_fields* fw, const double* G, const double* I, void* stream) {
+  const ClmgbRange range_("clmgb_synth_forcing");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_bounds(b, true);
   if (e) return e;
@@ -743,6 +768,7 @@ int32_t clmgb_batched_band_solve(clmgb_handle h, int64_t nc, int64_t ldc, int32_
                                  const double* bmatrix, const double* rvector, const int64_t* jtop,
                                  const int64_t* jbot, const uint8_t* mask, int32_t kl, int32_t ku,
                                  int32_t nlevsno_off, void* stream) {
+  const ClmgbRange range_("clmgb_batched_band_solve");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (nc < 0 || ldc < nc || nlev < 1 || nlev > clmgb::MAXROWS + 1) return CLMGB_ERR_DIMS;
   if (!((kl == 2 && ku == 2) || (kl == 1 && ku == 1))) return CLMGB_ERR_UNSUPPORTED;
@@ -946,6 +972,7 @@ int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, 
 int32_t clmgb_tridiagonal_multi(clmgb_handle h, int64_t ncols, int64_t ldc, int32_t nlevs, double* u,
                                 const double* a, const double* b, const double* c, const double* r,
                                 const int64_t* jtop, const uint8_t* mask, void* stream) {
+  const ClmgbRange range_("clmgb_tridiagonal_multi");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   if (ncols < 0 || ldc < ncols || nlevs < 1 || nlevs > 64) return CLMGB_ERR_DIMS;
   if (ncols == 0) return CLMGB_OK;
@@ -1060,6 +1087,7 @@ int32_t clmgb_column_step_logged(clmgb_handle h, const clmgb_bounds* b, const cl
                                  const clmgb_soilwater_fields* fw, const clmgb_swm_config* cfg, double dtime,
                                  int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
                                  const clmgb_substep_log* log, uint32_t* col_status, void* stream) {
+  const ClmgbRange range_("clmgb_column_step_logged");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_cfg(cfg);
   if (e) return e;
@@ -1097,6 +1125,7 @@ int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, cons
                                      int32_t snow_method, double* t_ssbef, double* t_h2osfc_bef,
                                      const clmgb_step_adjoint* adj, const clmgb_substep_log* log,
                                      uint32_t* col_status, void* stream) {
+  const ClmgbRange range_("clmgb_column_step_vjp_logged");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_cfg(cfg);
   if (e) return e;
@@ -1130,6 +1159,7 @@ int32_t clmgb_column_step_vjp_logged(clmgb_handle h, const clmgb_bounds* b, cons
 int32_t clmgb_soil_water_warm(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
                               const clmgb_swm_config* cfg, double dtime, const double* dt_first,
                               uint32_t* col_status, void* stream) {
+  const ClmgbRange range_("clmgb_soil_water_warm");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_cfg(cfg);
   if (e) return e;
@@ -1149,6 +1179,7 @@ int32_t clmgb_soil_water_warm(clmgb_handle h, const clmgb_bounds* b, const clmgb
 int32_t clmgb_mlp_samples(clmgb_handle h, const clmgb_bounds* b, const clmgb_soilwater_fields* f,
                           const clmgb_swm_config* cfg, double dtime, int32_t per_column, float* features,
                           float* targets, uint32_t* count, int64_t capacity, uint32_t* col_status, void* stream) {
+  const ClmgbRange range_("clmgb_mlp_samples");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_cfg(cfg);
   if (e) return e;
@@ -1255,6 +1286,7 @@ int32_t clmgb_balance_residuals(clmgb_handle h, const clmgb_bounds* b, const clm
                                 const clmgb_soilwater_fields* fw, double dtime, const double* t_ssbef,
                                 const double* t_h2osfc_bef, const double* t_grnd0, const double* begwb,
                                 double* errsoi, double* errh2o, void* stream) {
+  const ClmgbRange range_("clmgb_balance_residuals");
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
   int32_t e = check_bounds(b, true);
   if (e) return e;
