@@ -44,11 +44,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nc", type=int, default=262144)
     ap.add_argument("--cfg", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=8)
-    ap.add_argument("--e2e-chunks", type=int, default=1,
-                    help="column ranges of the end-to-end step (uploads and read-backs overlap the other ranges)")
-    ap.add_argument("--e2e-readback", default="dma", choices=["kernel", "dma"],
-                    help="how the temperature outputs come back during the Richards solve")
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-sample", type=int, default=4096)
     ap.add_argument("--cpu-steps", type=int, default=5, help="steps of the CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 probe and the work count")
@@ -722,15 +718,11 @@ def run_ours(args):
     if args.e2e_steps > 0:
         from clmgb import hoststep
         host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in st.arrays.items()}
-        hs = hoststep.HostStepper(h, host, d, wl.dtime, cfg, chunks=args.e2e_chunks, readback=args.e2e_readback)
+        hs = hoststep.HostStepper(h, host, d, wl.dtime, cfg)
 
         def e2e_step(k):
             G, I = Gd[k % nsteps], Id[k % nsteps]
-            if len(hs.ranges) > 1:
-                hs.step_chunked(stream, forcing=lambda v: api.synth_forcing(h, v, G[v.c0:v.c1], I[v.c0:v.c1],
-                                                                           stream=stream))
-            else:
-                hs.step(stream, forcing=lambda dv: api.synth_forcing(h, dv, G, I, stream=stream))
+            hs.step(stream, forcing=lambda dv: api.synth_forcing(h, dv, G, I, stream=stream))
 
         for k in range(2):
             e2e_step(k)
@@ -745,10 +737,8 @@ def run_ours(args):
         e2e_ms = e0.elapsed_time(e1)
         e2e = {"value": args.e2e_steps * nc * world / (e2e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": hs.h2d_bytes, "d2h_bytes_per_step": hs.d2h_bytes,
-               "chunks": len(hs.ranges), "readback": args.e2e_readback,
                "note": "host-resident state: per step H2D of the inputs other modules change, D2H of every "
-                       "written field, the soil-temperature outputs read back during the Richards solve "
-                       "(with --e2e-chunks > 1 the step runs over column ranges); "
+                       "written field, the soil-temperature outputs read back during the Richards solve; "
                        "parameters/geometry/topology uploaded once"}
         del host, hs
 

@@ -54,8 +54,6 @@ _SIGS = {
     "clmgb_snow_layers": ([P, P, P, P, C.c_uint32, F64, P], I32),
     "clmgb_lake_temperature": ([P, P, P, P, F64, P], I32),
     "clmgb_balance_check_columns": ([P, P, P, F64, P, P], I32),
-    "clmgb_copy_columns": ([P, I64, P, I64, I64, I64, P], I32),
-    "clmgb_copy_segments": ([P, P, P, I32, P], I32),
     "clmgb_column_step_vjp_logged": ([P, P, P, P, P, F64, I32, P, P, P, P, P, P], I32),
     "clmgb_set_option": ([P, I32, I64], I32),
     "clmgb_reserve": ([P, I64], I32),

@@ -77,7 +77,6 @@ OPT_RECORDS_TMA_USED = 25
 OPT_TRIDIAG_METHOD = 26
 OPT_ST_BLOCK = 27
 TRIDIAG_THOMAS, TRIDIAG_PCR = 0, 1
-MAX_COPY_SEGMENTS = 128
 
 COL_URBAN, COL_SUBSTEP_CAP, COL_NONFINITE, COL_LEVEL_RANGE, COL_PATCH_RANGE = 1, 2, 4, 8, 16
 COL_ADJ_UNSUPPORTED, COL_TAPE_FULL, COL_ADJ_REPLAY, COL_FILTER, COL_QUEUE_WAIT = 32, 64, 128, 256, 512

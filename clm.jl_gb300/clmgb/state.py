@@ -116,3 +116,33 @@ class ColumnState:
     def ptr(self, name):
         f = self.spec[name]
         return self._ptr(name, abi._CT[f[1]])
+
+
+class ColumnRange:
+    """The columns [c0, c1) of a device state, as the drop-in calls see them: column
+    pointers advanced by c0 (same ldc), patch and landunit arrays whole.  A caller that
+    runs the calls on a range also sets CLMGB_OPT_COLUMN_BASE to c0, since patch.column
+    holds global column indices."""
+    on_device = True
+
+    def __init__(self, dev, c0, c1):
+        self.dev, self.c0, self.c1 = dev, c0, c1
+
+    def bounds(self):
+        b = self.dev.bounds()
+        return abi.Bounds(self.c1 - self.c0, b.np, b.nl, b.ldc, b.ldp)
+
+    def _struct(self, cls, fields):
+        st = cls()
+        st.struct_size = C.sizeof(cls)
+        for (n, t, kind, _) in fields:
+            a = self.dev[n]
+            off = self.c0 * a.element_size() if kind == "c" else 0
+            setattr(st, n, C.cast(C.c_void_p(a.data_ptr() + off), abi._CT[t]))
+        return st
+
+    def soiltemp_fields(self):
+        return self._struct(abi.SoilTempFields, abi.SOILTEMP_FIELDS)
+
+    def soilwater_fields(self):
+        return self._struct(abi.SoilWaterFields, abi.SOILWATER_FIELDS)

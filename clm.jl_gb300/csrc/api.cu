@@ -467,54 +467,6 @@ int32_t clmgb_surface_hydrology(clmgb_handle h, const clmgb_bounds* b, const clm
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }
 
-int32_t clmgb_copy_columns(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch, int64_t width,
-                           int64_t rows, void* stream) {
-  if (!dst || !src) return CLMGB_ERR_NULL_ARG;
-  if (width < 0 || rows < 0 || dst_pitch < width || src_pitch < width) return CLMGB_ERR_DIMS;
-  if (width == 0 || rows == 0) return CLMGB_OK;
-  const cudaError_t ce = cudaMemcpy2DAsync(dst, (size_t)dst_pitch, src, (size_t)src_pitch, (size_t)width,
-                                           (size_t)rows, cudaMemcpyDefault, (cudaStream_t)stream);
-  return ce == cudaSuccess ? CLMGB_OK : CLMGB_ERR_CUDA;
-}
-
-// true for device, managed or page-locked host memory the GPU can address at `p`
-static bool device_addressable(const void* p) {
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return true;
-  return a.type == cudaMemoryTypeHost && a.devicePointer == p;
-}
-
-int32_t clmgb_copy_segments(void* const* dst, const void* const* src, const int64_t* bytes, int32_t n,
-                            void* stream) {
-  if (n < 0 || n > CLMGB_MAX_COPY_SEGMENTS) return CLMGB_ERR_DIMS;
-  if (n == 0) return CLMGB_OK;
-  if (!dst || !src || !bytes) return CLMGB_ERR_NULL_ARG;
-  clmgb::CopySegments cs;
-  cs.n = 0;
-  for (int32_t i = 0; i < n; i++) {
-    if (bytes[i] < 0 || bytes[i] % 8) return CLMGB_ERR_DIMS;
-    if (bytes[i] == 0) continue;
-    if (!dst[i] || !src[i]) return CLMGB_ERR_NULL_ARG;
-    if (((uintptr_t)dst[i] | (uintptr_t)src[i]) % 8) return CLMGB_ERR_DIMS;
-    // the last byte of each range must be addressable too (same allocation kind)
-    const char* s_end = (const char*)src[i] + bytes[i] - 1;
-    char* d_end = (char*)dst[i] + bytes[i] - 1;
-    if (!device_addressable(src[i]) || !device_addressable(dst[i]) || !device_addressable(s_end) ||
-        !device_addressable(d_end))
-      return CLMGB_ERR_DIMS;
-    cs.src[cs.n] = (const unsigned long long*)src[i];
-    cs.dst[cs.n] = (unsigned long long*)dst[i];
-    cs.words[cs.n] = bytes[i] / 8;
-    cs.n++;
-  }
-  const cudaError_t ce = clmgb::launch_copy_segments(cs, (cudaStream_t)stream);
-  return ce == cudaSuccess ? CLMGB_OK : CLMGB_ERR_CUDA;
-}
-
 int32_t clmgb_balance_check_columns(clmgb_handle h, const clmgb_bounds* b, const clmgb_colbalance_fields* f,
                                     double dtime, clmgb_balance_report* report, void* stream) {
   const ClmgbRange range_("clmgb_balance_check_columns");

@@ -1094,27 +1094,6 @@ cudaError_t launch_moisture_form_queue(const Dims& D, int64_t nc, const clmgb_so
                                                                        qs.fresh_batch, q);
   return cudaGetLastError();
 }
-// Every block walks every segment; its threads take 8-byte words four at a time with
-// evict-first loads, so the copy leaves a concurrently running kernel's L2 lines alone.
-__global__ void __launch_bounds__(256) k_copy_segments(CopySegments cs) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (int k = 0; k < cs.n; k++) {
-    const unsigned long long* src = cs.src[k];
-    unsigned long long* dst = cs.dst[k];
-    const int64_t n = cs.words[k];
-    int64_t i = t0;
-    for (; i + 3 * stride < n; i += 4 * stride) {
-      const unsigned long long a = __ldcs(src + i), b = __ldcs(src + i + stride);
-      const unsigned long long c = __ldcs(src + i + 2 * stride), d = __ldcs(src + i + 3 * stride);
-      __stcs(dst + i, a);
-      __stcs(dst + i + stride, b);
-      __stcs(dst + i + 2 * stride, c);
-      __stcs(dst + i + 3 * stride, d);
-    }
-    for (; i < n; i += stride) __stcs(dst + i, __ldcs(src + i));
-  }
-}
 cudaError_t launch_compute_qcharge(const Dims& D, int64_t nc, const clmgb_soilwater_fields& f,
                                   const clmgb_swm_config& cfg, double dtime, cudaStream_t s) {
   if (cfg.lower_boundary_condition != CLMGB_BC_WATERTABLE || nc <= 0) return cudaSuccess;
@@ -1123,11 +1102,6 @@ cudaError_t launch_compute_qcharge(const Dims& D, int64_t nc, const clmgb_soilwa
 }
 cudaError_t launch_flexible_cn(const Dims& D, int64_t nc, const clmgb_flexcn_fields& f, cudaStream_t s) {
   k_flexible_cn<<<grid_for(nc), BLOCK, 0, s>>>(D, nc, f);
-  return cudaGetLastError();
-}
-cudaError_t launch_copy_segments(const CopySegments& cs, cudaStream_t s) {
-  if (cs.n <= 0) return cudaSuccess;
-  k_copy_segments<<<152, 256, 0, s>>>(cs);
   return cudaGetLastError();
 }
 cudaError_t launch_math_eval(int op, int64_t n, const double* x, const double* y, double* out, cudaStream_t s) {

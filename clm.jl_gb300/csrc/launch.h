@@ -119,16 +119,7 @@ static_assert(ST_END <= CLMGB_LOG_ST_STRIDE, "soil_temperature! record exceeds C
 enum PcField { PC_DZW = 0, PC_WS, PC_BSW, PC_KS, PC_SUC, PC_IMP, PC_DEN, PC_ROOT, PC_FIELDS,
                PC_LIQ = PC_FIELDS, PC_SMP, PC_HK, PC_ALL };
 
-// Segments of one clmgb_copy_segments call (8-byte words).
-struct CopySegments {
-  const unsigned long long* src[CLMGB_MAX_COPY_SEGMENTS];
-  unsigned long long* dst[CLMGB_MAX_COPY_SEGMENTS];
-  int64_t words[CLMGB_MAX_COPY_SEGMENTS];
-  int n;
-};
-
 // All launchers return the cudaError_t of the launch (cudaGetLastError()).
-cudaError_t launch_copy_segments(const CopySegments& cs, cudaStream_t s);
 cudaError_t launch_soil_temperature(const Dims& D, int64_t nc, const clmgb_soiltemp_fields& f, double dtime,
                                     int snow_method, uint32_t* col_status, uint32_t* dev_status,
                                     cudaStream_t s);

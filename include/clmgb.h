@@ -1188,23 +1188,6 @@ typedef struct clmgb_balance_report {
 #define CLMGB_BAL_SOI_WARN       8u   /* errsoi_max > 1e-5 W/m2, :1352 */
 #define CLMGB_BAL_SOI_ERROR     16u   /* errsoi_max > 1e-4 W/m2, :1356 */
 
-/* Copies `rows` rows of `width` bytes between host and device memory (either direction),
- * stride dst_pitch / src_pitch bytes, asynchronously on `stream`: the columns [c0, c1)
- * of a [ldc, levels] field are rows = levels, width = (c1 - c0) * 8, pitch = ldc * 8.
- * Host memory should be page-locked for the copy to overlap kernels. */
-int32_t clmgb_copy_columns(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch, int64_t width,
-                           int64_t rows, void* stream);
-
-#define CLMGB_MAX_COPY_SEGMENTS 128
-/* Copies n segments, dst[i] <- src[i] (bytes[i] bytes), in one kernel on `stream`.  The
- * loads are marked evict-first, so a copy that runs beside another kernel (a step's
- * outputs going back to page-locked host memory while the next stage computes) takes
- * little of that kernel's L2.  Every pointer is device memory or page-locked host memory
- * (CLMGB_ERR_DIMS otherwise), 8-byte aligned, and bytes[i] a multiple of 8; segments
- * must not overlap.  0 <= n <= CLMGB_MAX_COPY_SEGMENTS. */
-int32_t clmgb_copy_segments(void* const* dst, const void* const* src, const int64_t* bytes, int32_t n,
-                            void* stream);
-
 /* The column part of balance_check!: errh2o (_bc_forc_rainsnow_kernel! and
  * _bc_errh2o_col_kernel!, :723-770) and the maxima and first indices its warn/error scans
  * read (:1124-1160, :1347-1365), reduced on the device.  The report is written to host

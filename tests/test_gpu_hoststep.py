@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from clmgb import abi, api, hoststep, synth
+from clmgb.state import ColumnRange
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -39,9 +40,12 @@ def test_host_stepper_matches_device_steps():
         h.close()
 
 
-@pytest.mark.parametrize("chunks", [2, 3, 7])
-def test_chunked_host_stepper_matches_device_steps(chunks):
-    nsteps = 4
+@pytest.mark.parametrize("ranges", [2, 3, 7])
+def test_column_ranges_match_whole_calls(ranges):
+    """The drop-in calls run over column ranges (column pointers advanced by the range's
+    first column, CLMGB_OPT_COLUMN_BASE set to it, patch arrays whole), as a caller that
+    splits its columns does: the same bits as calls over all columns."""
+    nsteps = 3
     wl = synth.make_workload(2, nc=3001, seed=12, nsteps=nsteps)
     cfg = abi.SwmConfig.clm5_default()
     h = api.Handle(wl.state.vp)
@@ -55,42 +59,20 @@ def test_chunked_host_stepper_matches_device_steps(chunks):
             api.soil_temperature(h, d, wl.dtime)
             api.set_soil_water_fractions(h, d)
             api.soil_water(h, d, wl.dtime, cfg)
-        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in wl.state.arrays.items()}
-        hs = hoststep.HostStepper(h, host, wl.state.to_device(), wl.dtime, cfg, chunks=chunks)
-        assert len(hs.ranges) == chunks
+        r = wl.state.to_device()
+        edges = np.linspace(0, wl.state.nc, ranges + 1).astype(np.int64)
         for t in range(nsteps):
-            hs.step_chunked(forcing=lambda v, t=t: api.synth_forcing(h, v, Gd[t][v.c0:v.c1], Id[t][v.c0:v.c1]))
-        torch.cuda.synchronize()
-        written = set(hoststep.WRITTEN_TEMPERATURE) | set(hoststep.WRITTEN_WATER)
-        for k in written:
-            assert torch.equal(host[k], d[k].cpu()), k
-        assert h.get_option(abi.OPT_COLUMN_BASE) == 0
-        assert h.device_status() == 0
-    finally:
-        h.close()
-
-
-def test_host_stepper_kernel_readback_matches_device_steps():
-    nsteps = 3
-    wl = synth.make_workload(2, nc=2500, seed=13, nsteps=nsteps)
-    cfg = abi.SwmConfig.clm5_default()
-    h = api.Handle(wl.state.vp)
-    try:
-        h.reserve(wl.state.nc)
-        G, I = wl.forcing_block(range(nsteps))
-        Gd, Id = torch.from_numpy(G).cuda(), torch.from_numpy(I).cuda()
-        d = wl.state.to_device()
-        for t in range(nsteps):
-            api.synth_forcing(h, d, Gd[t], Id[t])
-            api.soil_temperature(h, d, wl.dtime)
-            api.set_soil_water_fractions(h, d)
-            api.soil_water(h, d, wl.dtime, cfg)
-        host = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in wl.state.arrays.items()}
-        hs = hoststep.HostStepper(h, host, wl.state.to_device(), wl.dtime, cfg, readback="kernel")
-        for t in range(nsteps):
-            hs.step(forcing=lambda dv, t=t: api.synth_forcing(h, dv, Gd[t], Id[t]))
+            for a, b in zip(edges[:-1], edges[1:]):
+                v = ColumnRange(r, int(a), int(b))
+                h.set_option(abi.OPT_COLUMN_BASE, int(a))
+                api.synth_forcing(h, v, Gd[t][a:b], Id[t][a:b])
+                api.soil_temperature(h, v, wl.dtime)
+                api.set_soil_water_fractions(h, v)
+                api.soil_water(h, v, wl.dtime, cfg)
+        h.set_option(abi.OPT_COLUMN_BASE, 0)
         torch.cuda.synchronize()
         for k in set(hoststep.WRITTEN_TEMPERATURE) | set(hoststep.WRITTEN_WATER):
-            assert torch.equal(host[k], d[k].cpu()), k
+            assert torch.equal(r[k], d[k]), k
+        assert h.device_status() == 0
     finally:
         h.close()
