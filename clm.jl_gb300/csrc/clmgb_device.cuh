@@ -79,6 +79,27 @@ __device__ __forceinline__ double jl_min(double x, double y) {
   if (isnan_bits(y)) return y;
   return ord_key(x) <= ord_key(y) ? x : y;
 }
+// Julia's Float64 x / y (IEEE, round to nearest).  A zero x over a finite nonzero y
+// is a zero whose sign is the xor of the operands' signs; that quotient is formed here
+// from the bits, on the integer pipes, because the hardware division is about 2.6x
+// slower with a zero numerator than with a normal one (measured on GB300: 27 against
+// 70 G divisions/s), and such quotients are common in this solve: the ice of unfrozen
+// levels, the excess ice (zero unless use_excess_ice), the phase-change heat of levels
+// that neither melt nor freeze, and the band system's zero sub-diagonal.  Every other
+// case is the division itself, so results are unchanged.
+__device__ __forceinline__ double jl_div(double x, double y) {
+  const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long by = (unsigned long long)__double_as_longlong(y);
+  // (by << 1) - 1 < 0xffdffffffffffffe: y is nonzero and finite
+  if ((bx << 1) == 0 && (by << 1) - 1ull < 0xffdffffffffffffeull)
+    return __longlong_as_double((long long)((bx ^ by) & 0x8000000000000000ull));
+  return x / y;
+}
+// other scalar types (the recording adjoint's): their own division
+template <class A, class B>
+__device__ __forceinline__ auto jl_div(A x, B y) {
+  return x / y;
+}
 // |x| < t for a positive threshold t, on the integer pipes (false for NaN, as in IEEE).
 __device__ __forceinline__ bool abs_lt(double x, double t) {
   return (__double_as_longlong(x) & 0x7fffffffffffffffLL) < __double_as_longlong(t);
@@ -148,7 +169,7 @@ __device__ __forceinline__ void band_lu_solve(S* ab, S* x, int n) {
       x[piv] = xk;
     }
     for (int i = k + 1; i <= ilast; i++) {
-      const S f = AB(i, k) / akk;
+      const S f = jl_div(AB(i, k), akk);
       for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
       x[i] = x[i] - f * x[k];
     }
@@ -191,7 +212,7 @@ __device__ __forceinline__ void band_lu_factor_solve(double* ab, double* x, uint
       x[p] = xk;
     }
     for (int i = k + 1; i <= ilast; i++) {
-      const double f = AB(i, k) / akk;
+      const double f = jl_div(AB(i, k), akk);
       for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
       x[i] = x[i] - f * x[k];
       AB(i, k) = f;
@@ -475,13 +496,13 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
       if (xm[jj] > 0.0) {
         ice = jl_max(0.0, wice0[jj] - xm[jj]);
         X.Ice(jj) = ice;
-        heatr = hm[jj] - HFUS * (wice0[jj] - ice) / dtime;
+        heatr = hm[jj] - jl_div(HFUS * (wice0[jj] - ice), dtime);
         const S xm2 = xm[jj] - ice;
         if (ice == 0.0) {
           if (wexice0[jj] >= 0.0 && xm2 > 0.0 && j >= 2) {
             const S ex = jl_max(0.0, wexice0[jj] - xm2);
             LV(EXI, c, j, ld) = VAL(ex);
-            heatr = hm[jj] - HFUS * (wexice0[jj] - ex + wice0[jj] - ice) / dtime;
+            heatr = hm[jj] - jl_div(HFUS * (wexice0[jj] - ex + wice0[jj] - ice), dtime);
           }
         }
       } else if (xm[jj] < 0.0) {
@@ -492,7 +513,7 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
           else ice = jl_min(wmass0[jj] - wexice0[jj] - supercool[j], wice0[jj] - xm[jj]);
         }
         X.Ice(jj) = ice;
-        heatr = hm[jj] - HFUS * (wice0[jj] - ice) / dtime;
+        heatr = hm[jj] - jl_div(HFUS * (wice0[jj] - ice), dtime);
       }
       const double ei_val = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
       const S liq = jl_max(0.0, wmass0[jj] - ice - ei_val);
@@ -514,19 +535,19 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
       }
       if (j >= 1) {
         const double ex = LV(EXI, c, j, ld);
-        f.xmf[c] += HFUS * (VAL(wice0[jj]) - VAL(ice)) / dtime + HFUS * (wexice0[jj] - ex) / dtime;
-        LV(f.exice_subs, c, j, ld) = jl_max(0.0, (wexice0[jj] - ex) / DENICE);
+        f.xmf[c] += jl_div(HFUS * (VAL(wice0[jj]) - VAL(ice)), dtime) + jl_div(HFUS * (wexice0[jj] - ex), dtime);
+        LV(f.exice_subs, c, j, ld) = jl_max(0.0, jl_div(wexice0[jj] - ex, DENICE));
       } else {
-        f.xmf[c] += HFUS * (VAL(wice0[jj]) - VAL(ice)) / dtime;
+        f.xmf[c] += jl_div(HFUS * (VAL(wice0[jj]) - VAL(ice)), dtime);
       }
       if (im == 1 && j < 1) {
-        const double q = jl_max(0.0, VAL(wice0[jj]) - VAL(ice)) / dtime;
+        const double q = jl_div(jl_max(0.0, VAL(wice0[jj]) - VAL(ice)), dtime);
         LV(f.qflx_snomelt_lyr, c, jj, ld) = q;
         f.qflx_snomelt[c] += q;
         f.snomelt_accum[c] += q * dtime * 1.0e-3;
       }
       if (im == 2 && j < 1) {
-        const double q = jl_max(0.0, VAL(ice) - VAL(wice0[jj])) / dtime;
+        const double q = jl_div(jl_max(0.0, VAL(ice) - VAL(wice0[jj])), dtime);
         LV(f.qflx_snofrz_lyr, c, jj, ld) = q;
         f.qflx_snofrz[c] += q;
       }
@@ -600,15 +621,15 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
           const double exi = LV(EXI, c, j, ld);
           const double dzv = LVc(DZ, c, jj, ld);
           const S ws = X.Watsat(j);
-          S satw = (liq / DENH2O + ice / DENICE + exi / DENICE) / (dzv * ws);
+          S satw = (jl_div(liq, DENH2O) + jl_div(ice, DENICE) + jl_div(exi, DENICE)) / (dzv * ws);
           satw = jl_min(1.0, satw);
           if (satw > 1.0e-7) {
             S dke;
             if (tt[jj] >= TFRZ) dke = jl_max(0.0, cm_log10(satw) + 1.0);
             else dke = satw;
-            const S a1 = liq / (DENH2O * dzv);
-            const S fl_denom = a1 + ice / (DENICE * dzv) + exi / (DENICE * dzv);
-            const S fl = a1 / fl_denom;
+            const S a1 = jl_div(liq, DENH2O * dzv);
+            const S fl_denom = a1 + jl_div(ice, DENICE * dzv) + jl_div(exi, DENICE * dzv);
+            const S fl = jl_div(a1, fl_denom);
             const S dksat =
                 LVc(f.tkmg, c, j, ld) * cm_pow_lx(TKWAT, ln_tkwat, ln_tkwat_lo, fl * ws) *
                 cm_pow_lx(TKICE, ln_tkice, ln_tkice_lo, (1.0 - fl) * ws);
@@ -685,10 +706,10 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     S fc;
     if (j == jtop) {
       fc = dtime / cv * dzv / (0.5 * (zz[jj] - LVc(ZI, c, jj, ld) + CAPR * (zz[jj + 1] - LVc(ZI, c, jj, ld))));
-      fn[jj] = tk[jj] * (tt[jj + 1] - tt[jj]) / (zz[jj + 1] - zz[jj]);
+      fn[jj] = jl_div(tk[jj] * (tt[jj + 1] - tt[jj]), zz[jj + 1] - zz[jj]);
     } else if (j <= nlevgrnd - 1) {
       fc = dtime / cv;
-      fn[jj] = tk[jj] * (tt[jj + 1] - tt[jj]) / (zz[jj + 1] - zz[jj]);
+      fn[jj] = jl_div(tk[jj] * (tt[jj + 1] - tt[jj]), zz[jj + 1] - zz[jj]);
     } else {
       fc = dtime / cv;
       fn[jj] = f.eflx_bot[c];
@@ -857,7 +878,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     for (int jj = jjtop; jj <= nlev; jj++) {
       const int j = jj - nlevsno;
       double fn1v;
-      if (j <= nlevgrnd - 1) fn1v = VAL(tk[jj]) * (VAL(tt[jj + 1]) - VAL(tt[jj])) / (zz[jj + 1] - zz[jj]);
+      if (j <= nlevgrnd - 1) fn1v = jl_div(VAL(tk[jj]) * (VAL(tt[jj + 1]) - VAL(tt[jj])), zz[jj + 1] - zz[jj]);
       else fn1v = 0.0;
       if (j == 1) f.eflx_fgr12[c] = -CNFAC * VAL(fn[jj]) - (1.0 - CNFAC) * fn1v;
       if (j >= 1 && j < nlevgrnd && issoilcrop) LV(f.eflx_fgr, c, j, ld) = -CNFAC * VAL(fn[jj]) - (1.0 - CNFAC) * fn1v;
@@ -906,11 +927,11 @@ __device__ __forceinline__ void water_fractions_col(const Dims& D, const clmgb_s
   const int joff = D.nlevsno;
   for (int j = 1; j <= D.nlevsoi; j++) {
     const double exi = LV(f.excess_ice, c, j, ld);
-    const double dz_ext = LVc(f.dz, c, j + joff, ld) + exi / DENICE;
+    const double dz_ext = LVc(f.dz, c, j + joff, ld) + jl_div(exi, DENICE);
     const S ws = X.Watsat(j);
-    const S vol_ice = jl_min(ws, (X.Ice(j + joff) + exi) / (dz_ext * DENICE));
+    const S vol_ice = jl_min(ws, jl_div(X.Ice(j + joff) + exi, dz_ext * DENICE));
     LV(f.eff_porosity, c, j, ld) = jl_max(0.01, VAL(ws) - VAL(vol_ice));
-    X.Icefrac(j) = jl_min(1.0, vol_ice / ws);
+    X.Icefrac(j) = jl_min(1.0, jl_div(vol_ice, ws));
   }
 }
 
