@@ -182,14 +182,14 @@ __device__ __noinline__ void phase_change_level_reverse(const PcLevelIn& in, dou
     return;
   }
   // ---- new ice and liquid water (:2090-2140) ----
-  const double xm = hm * dtime / HFUS;
+  const double xm = jl_div(hm * dtime, HFUS);
   double ice = wice0, heatr = 0.0;
   int kind = 0;   // 0 ice unchanged, 1 wice0 - xm, 2 constant, 3 wmass0, 4 wmass0 - sc
   if (xm > 0.0) {
     const double v = wice0 - xm;
     ice = jl_max(0.0, v);
     kind = same_bits(ice, 0.0) ? 2 : 1;
-    heatr = hm - HFUS * (wice0 - ice) / dtime;
+    heatr = hm - jl_div(HFUS * (wice0 - ice), dtime);
   } else if (xm < 0.0) {
     if (j <= 0) {
       const double a = wmass0, b = wice0 - xm;
@@ -205,7 +205,7 @@ __device__ __noinline__ void phase_change_level_reverse(const PcLevelIn& in, dou
         kind = same_bits(ice, a) ? 4 : 1;
       }
     }
-    heatr = hm - HFUS * (wice0 - ice) / dtime;
+    heatr = hm - jl_div(HFUS * (wice0 - ice), dtime);
   }
   const double liqv = wmass0 - ice - 0.0;
   const double liq = jl_max(0.0, liqv);
@@ -351,7 +351,7 @@ __device__ __noinline__ void soil_temperature_reverse(const Dims& D, const clmgb
           const double dzv = LVc(f.dz, c, jj, ld);
           const double ws = LVc(fw.watsat, c, j, ld);
           const double m = dzv * ws;
-          const double satw0 = (liq / DENH2O + ice / DENICE + exi / DENICE) / m;
+          const double satw0 = (jl_div(liq, DENH2O) + jl_div(ice, DENICE) + jl_div(exi, DENICE)) / m;
           const double satw = jl_min(1.0, satw0);
           const bool spass = !same_bits(satw, 1.0);
           if (satw > 1.0e-7) {
@@ -1031,11 +1031,11 @@ k_column_step_vjp_cf(Dims D, int64_t nc, clmgb_soiltemp_fields ft, clmgb_soilwat
         for (int j = 1; j <= nl; j++) {
           if (icefb[j] == 0.0) continue;
           const double exi = LV(ft.excess_ice, c, j, ld);
-          const double dz_ext = LVc(fw.dz, c, j + joff, ld) + exi / DENICE;
+          const double dz_ext = LVc(fw.dz, c, j + joff, ld) + jl_div(exi, DENICE);
           const double ws = wsv[j];
-          const double y = (V.ice[j + joff] + exi) / (dz_ext * DENICE);
+          const double y = jl_div(V.ice[j + joff] + exi, dz_ext * DENICE);
           const double vol_ice = jl_min(ws, y);
-          const double v = vol_ice / ws;
+          const double v = jl_div(vol_ice, ws);
           const double icef = jl_min(1.0, v);
           if (same_bits(icef, 1.0)) continue;
           wsb[j] -= icefb[j] * v / ws;

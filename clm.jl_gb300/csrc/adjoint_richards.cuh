@@ -290,7 +290,7 @@ static __device__ __noinline__ void mf_substep_reverse(const Dims& D, const clmg
       if ((spass >> k) & 1u) {
         const double vwcb = a2.sb * rws[k];
         a2.wsb -= a2.sb * s0[k] * rws[k];
-        if ((lpass >> k) & 1u) lb += vwcb / (dzv[k] * DENH2O);
+        if ((lpass >> k) & 1u) lb += jl_div(vwcb, dzv[k] * DENH2O);
       }
       lamL[k] = lb;
       R.ws[k] += a2.wsb;

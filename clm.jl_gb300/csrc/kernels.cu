@@ -733,7 +733,7 @@ k_flexible_cn(Dims D, int64_t nc, clmgb_flexcn_fields f) {
   for (int j = 1; j <= nlevsoi; j++) {
     const double dzv = LVc(f.dz, c, joff + j, ld);
     LV(f.h2osoi_vol, c, j, ld) =
-        LV(f.h2osoi_liq, c, joff + j, ld) / (dzv * DENH2O) + LVc(f.h2osoi_ice, c, joff + j, ld) / (dzv * DENICE);
+        jl_div(LV(f.h2osoi_liq, c, joff + j, ld), dzv * DENH2O) + jl_div(LVc(f.h2osoi_ice, c, joff + j, ld), dzv * DENICE);
   }
 }
 
