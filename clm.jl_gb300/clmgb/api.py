@@ -300,11 +300,12 @@ def balance_residuals(handle, state, dtime, t_grnd0, begwb, stream=None):
     return es, eh
 
 
-MATH_OPS = {"log": 0, "exp": 1, "pow": 2, "log10": 3, "sin": 4, "acos": 5}
+MATH_OPS = {"log": 0, "exp": 1, "pow": 2, "log10": 3, "sin": 4, "acos": 5, "div": 6}
 
 
 def math_eval(handle, op, x, y=None, out=None, stream=None):
-    """Evaluates the library's binary64 log/exp/pow/log10 on CUDA tensors."""
+    """Evaluates the library's binary64 log/exp/pow/log10/sin/acos, or its division x / y
+    (op "div"), on CUDA tensors."""
     import torch
     if out is None:
         out = torch.empty_like(x)

@@ -914,9 +914,9 @@ int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value) {
 int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y, double* out,
                         void* stream) {
   if (!handle_ok(h)) return CLMGB_ERR_HANDLE;
-  if (op < 0 || op > 5 || n < 0) return CLMGB_ERR_CONFIG;
+  if (op < 0 || op > 6 || n < 0) return CLMGB_ERR_CONFIG;
   if (n == 0) return CLMGB_OK;
-  if (!x || !out || (op == 2 && !y)) return CLMGB_ERR_NULL_ARG;
+  if (!x || !out || ((op == 2 || op == 6) && !y)) return CLMGB_ERR_NULL_ARG;
   cudaError_t ce = clmgb::launch_math_eval(op, n, x, y, out, (cudaStream_t)stream);
   return ce == cudaSuccess ? CLMGB_OK : cuda_fail(h, ce);
 }

@@ -806,7 +806,8 @@ k_math_eval(int op, int64_t n, const double* x, const double* y, double* out) {
   else if (op == 2) r = cm_pow(a, y[i]);
   else if (op == 3) r = cm_log10(a);
   else if (op == 4) r = cm_sin(a);
-  else r = cm_acos(a);
+  else if (op == 5) r = cm_acos(a);
+  else r = jl_div(a, y[i]);
   out[i] = r;
 }
 

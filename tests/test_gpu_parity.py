@@ -385,6 +385,32 @@ def test_math_bit_identical_to_cpu_build(handle_factory, op):
     assert np.array_equal(got[sel].view(np.uint64), ref.view(np.uint64))
 
 
+def test_division_is_ieee_with_zero_numerators(handle_factory):
+    """The kernels' division (a zero numerator over a finite nonzero divisor answered
+    from the sign bits, the rest by the hardware division) against IEEE division on
+    the host, over every pairing of zeros, subnormals, normals, extremes, infinities
+    and NaN, and 200,000 random pairs with a fifth of the numerators zero."""
+    h = handle_factory(synth.clm5_varpar())
+    tiny = np.nextafter(0.0, 1.0)
+    special = np.array([0.0, -0.0, tiny, -tiny, 2.2250738585072014e-308, 1e-300, 1e-20, 0.5, 1.0, 917.0, 3.0e8,
+                        1e300, np.finfo(np.float64).max, -1.0, -917.0, np.inf, -np.inf, np.nan])
+    xs, ys = np.meshgrid(special, special, indexing="ij")
+    rng = np.random.default_rng(61)
+    n = 200000
+    xr = rng.uniform(-50.0, 50.0, n) * 10.0 ** rng.integers(-30, 30, n)
+    xr[rng.random(n) < 0.2] = 0.0
+    xr[rng.random(n) < 0.05] *= -0.0
+    yr = rng.uniform(-50.0, 50.0, n) * 10.0 ** rng.integers(-30, 30, n)
+    x = np.concatenate([xs.ravel(), xr])
+    y = np.concatenate([ys.ravel(), yr])
+    got = api.math_eval(h, "div", _dev(x), _dev(y)).cpu().numpy()
+    with np.errstate(all="ignore"):
+        want = x / y
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(got), nan)                 # NaN payloads differ between hosts
+    assert np.array_equal(got[~nan].view(np.uint64), want[~nan].view(np.uint64))
+
+
 # ---------------------------------------------------------------- multi-step column step
 # ---------------------------------------------------------------- multi-step column step
 @pytest.mark.parametrize("mode", ["queue", "queue_reserved", "waves", "fused"])
