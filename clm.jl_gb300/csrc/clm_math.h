@@ -36,6 +36,7 @@
 #if defined(__CUDACC__)
 #define CM_FN static __device__ __forceinline__
 #define CM_TABLE(name, n) static __device__ const double name[n]
+#define CM_TABLE_U16(name, n) static __device__ const uint16_t name[n]
 #define CM_LD(p) __ldg(&(p))
 #define CM_FMA(a, b, c) __fma_rn((a), (b), (c))
 #define CM_MUL(a, b) __dmul_rn((a), (b))
@@ -54,6 +55,7 @@
 #include <string.h>
 #define CM_FN static inline
 #define CM_TABLE(name, n) static const double name[n]
+#define CM_TABLE_U16(name, n) static const uint16_t name[n]
 #define CM_LD(p) (p)
 #define CM_FMA(a, b, c) fma((a), (b), (c))
 #define CM_MUL(a, b) ((a) * (b))
@@ -71,6 +73,94 @@ static inline double cm_as_f64_(uint64_t u) { double x; memcpy(&x, &u, 8); retur
 #endif
 
 #include "clm_math_tables.h"
+
+// ---- binary64 division on the integer pipes ----
+// The correctly rounded quotient x / y formed with 64-bit integer arithmetic: on GB300
+// an FP64 instruction occupies its sub-partition's FP64 unit for about 64 cycles (2
+// lanes per clock per SM) while a 32-bit integer multiply-add takes about 2, so a
+// division done in integers leaves the FP64 pipe, which bounds the column kernels, to
+// the rest of the arithmetic.  Method: N. Moller and T. Granlund, "Improved division
+// by invariant integers", IEEE Trans. Computers 60(2), 2011: the reciprocal
+// v = floor((2^128 - 1) / d) - 2^64 of a normalised 64-bit divisor d (their
+// reciprocal_word, seeded from CM_RECIP_V0) and the 2/1 division of a two-word
+// numerator by d with v (div_2by1), which gives the exact quotient and remainder.
+// With d = my * 2^11 and the numerator mx * 2^66 (mx, my the 53-bit significands) the
+// quotient is floor(mx * 2^55 / my), 55 or 56 bits, and the remainder says whether
+// anything was cut off: round to nearest even from there.  Zero, subnormal, infinite
+// or NaN operands, and quotients below the normal range or above it, take the
+// ordinary division (CM_DIV), so the result always equals it.
+CM_FN uint64_t cm_umulhi_(uint64_t a, uint64_t b) {
+#if defined(__CUDACC__)
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// floor((2^128 - 1) / d) - 2^64 for d >= 2^63
+CM_FN uint64_t cm_recip_word_(uint64_t d) {
+  const uint64_t d0 = d & 1;
+  const uint64_t d9 = d >> 55;                               // 256..511
+  const uint64_t d40 = (d >> 24) + 1;
+  const uint64_t d63 = (d >> 1) + d0;                        // ceil(d / 2)
+  const uint64_t v0 = CM_LD(CM_RECIP_V0[d9 - 256]);
+  const uint64_t v1 = (v0 << 11) - ((v0 * v0 * d40) >> 40) - 1;
+  const uint64_t v2 = (v1 << 13) + ((v1 * ((1ULL << 60) - v1 * d40)) >> 47);
+  const uint64_t e = ((v2 >> 1) & (0 - d0)) - v2 * d63;    // 2^96 - v2 d63 + floor(v2/2) d0, mod 2^64
+  const uint64_t v3 = (v2 << 31) + (cm_umulhi_(v2, e) >> 1);
+  // v3 - floor((v3 + 2^64 + 1) d / 2^64)
+  const uint64_t lo = v3 * d;
+  const uint64_t lo2 = lo + d;
+  const uint64_t hi = cm_umulhi_(v3, d) + (lo2 < lo) + d;
+  return v3 - hi;
+}
+
+// floor((u1 2^64 + u0) / d) and its remainder, for u1 < d, d >= 2^63, v its reciprocal
+CM_FN uint64_t cm_div2by1_(uint64_t u1, uint64_t u0, uint64_t d, uint64_t v, uint64_t* rem) {
+  uint64_t q0 = v * u1;
+  uint64_t q1 = cm_umulhi_(v, u1);
+  q0 += u0;
+  q1 += u1 + (q0 < u0);
+  q1 += 1;
+  uint64_t r = u0 - q1 * d;
+  if (r > q0) {
+    q1 -= 1;
+    r += d;
+  }
+  if (r >= d) {
+    q1 += 1;
+    r -= d;
+  }
+  *rem = r;
+  return q1;
+}
+
+CM_FN double cm_div(double x, double y) {
+  const uint64_t bx = CM_AS_U64(x), by = CM_AS_U64(y);
+  const uint64_t ex = (bx >> 52) & 0x7ff, ey = (by >> 52) & 0x7ff;
+  if (ex - 1 >= 0x7fe || ey - 1 >= 0x7fe) return CM_DIV(x, y);   // zero, subnormal, Inf or NaN
+  const uint64_t frac = 0x000fffffffffffffULL, hidden = 0x0010000000000000ULL;
+  const uint64_t sign = (bx ^ by) & 0x8000000000000000ULL;
+  const uint64_t mx = (bx & frac) | hidden, my = (by & frac) | hidden;
+  int64_t e = (int64_t)ex - (int64_t)ey + 1023;
+  uint64_t m = mx;                                          // y a power of two: x rescaled
+  if (my != hidden) {
+    const uint64_t d = my << 11;
+    uint64_t r;
+    const uint64_t q = cm_div2by1_(mx << 2, 0, d, cm_recip_word_(d), &r);   // floor(mx 2^55 / my)
+    const int sh = (q >> 55) ? 3 : 2;                       // 56 bits: quotient >= 1
+    if (sh == 2) e -= 1;
+    m = q >> sh;
+    const uint64_t cut = q & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+    if (cut > half || (cut == half && (r != 0 || (m & 1)))) m += 1;
+    if (m >> 53) {
+      m >>= 1;
+      e += 1;
+    }
+  }
+  if (e < 1 || e > 0x7fe) return CM_DIV(x, y);             // subnormal or infinite quotient
+  return CM_AS_F64(sign | ((uint64_t)e << 52) | (m & frac));
+}
 
 // Natural logarithm.
 CM_FN double cm_log(double x) {

@@ -79,21 +79,28 @@ __device__ __forceinline__ double jl_min(double x, double y) {
   if (isnan_bits(y)) return y;
   return ord_key(x) <= ord_key(y) ? x : y;
 }
-// Julia's Float64 x / y (IEEE, round to nearest).  A zero x over a finite nonzero y
-// is a zero whose sign is the xor of the operands' signs; that quotient is formed here
-// from the bits, on the integer pipes, because the hardware division is about 2.6x
-// slower with a zero numerator than with a normal one (measured on GB300: 27 against
-// 70 G divisions/s), and such quotients are common in this solve: the ice of unfrozen
-// levels, the excess ice (zero unless use_excess_ice), the phase-change heat of levels
-// that neither melt nor freeze, and the band system's zero sub-diagonal.  Every other
-// case is the division itself, so results are unchanged.
+// Julia's Float64 x / y (IEEE, round to nearest), formed on the integer pipes.  On
+// GB300 an FP64 instruction holds its sub-partition's FP64 unit for about 64 cycles,
+// and the column kernels are bound by that unit; cm_div (clm_math.h) forms the
+// correctly rounded quotient of normal operands with 64-bit integer arithmetic
+// instead (measured: 141 against 70 G divisions/s alone, and next to FP64 work it
+// costs almost nothing, since it runs on the otherwise idle integer pipes).  A zero x
+// over a finite nonzero y, common in this solve (the ice of unfrozen levels, the
+// excess ice, the phase-change heat of levels that neither melt nor freeze, the band
+// system's zero sub-diagonal), is the zero with the xor of the signs, from the bits;
+// the hardware division is 2.6x slower than usual there (27 against 70 G/s).  Every
+// other case (subnormal, infinite or NaN operands, quotients outside the normal range)
+// is the hardware division.  The result is always the IEEE quotient.
+// (one out-of-line copy of the integer division: inlined at every call site it grew
+// the soil-temperature kernel's stack frame from 4.1 to 5.8 KB)
+static __device__ __noinline__ double cm_div_call(double x, double y) { return cm_div(x, y); }
 __device__ __forceinline__ double jl_div(double x, double y) {
   const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
   const unsigned long long by = (unsigned long long)__double_as_longlong(y);
   // (by << 1) - 1 < 0xffdffffffffffffe: y is nonzero and finite
   if ((bx << 1) == 0 && (by << 1) - 1ull < 0xffdffffffffffffeull)
     return __longlong_as_double((long long)((bx ^ by) & 0x8000000000000000ull));
-  return x / y;
+  return cm_div_call(x, y);
 }
 // other scalar types (the recording adjoint's): their own division
 template <class A, class B>
@@ -178,7 +185,7 @@ __device__ __forceinline__ void band_lu_solve(S* ab, S* x, int n) {
     S s = x[i];
     const int jl = min(n - 1, i + KL + KU);
     for (int j = i + 1; j <= jl; j++) s = s - AB(i, j) * x[j];
-    x[i] = s / AB(i, i);
+    x[i] = jl_div(s, AB(i, i));
   }
 #undef AB
 }
@@ -223,7 +230,7 @@ __device__ __forceinline__ void band_lu_factor_solve(double* ab, double* x, uint
     double s = x[i];
     const int jl = min(n - 1, i + KL + KU);
     for (int j = i + 1; j <= jl; j++) s = s - AB(i, j) * x[j];
-    x[i] = s / AB(i, i);
+    x[i] = jl_div(s, AB(i, i));
   }
 #undef AB
 }
@@ -238,7 +245,7 @@ __device__ __forceinline__ void band_lu_transpose_solve(const double* ab, const 
   for (int i = 0; i < n; i++) {
     double s = w[i];
     for (int j = max(0, i - KL - KU); j < i; j++) s = s - AB(j, i) * w[j];
-    w[i] = s / AB(i, i);
+    w[i] = jl_div(s, AB(i, i));
   }
   for (int k = n - 2; k >= 0; k--) {
     double s = w[k];
@@ -621,7 +628,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
           const double exi = LV(EXI, c, j, ld);
           const double dzv = LVc(DZ, c, jj, ld);
           const S ws = X.Watsat(j);
-          S satw = (jl_div(liq, DENH2O) + jl_div(ice, DENICE) + jl_div(exi, DENICE)) / (dzv * ws);
+          S satw = jl_div(jl_div(liq, DENH2O) + jl_div(ice, DENICE) + jl_div(exi, DENICE), dzv * ws);
           satw = jl_min(1.0, satw);
           if (satw > 1.0e-7) {
             S dke;
@@ -647,7 +654,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     } else {
       // snow layer (snl+1 <= j <= 0) — Jordan1991 or Sturm1997
       const double denom = jl_max(fse, 1.0e-6) * jl_max(LVc(DZ, c, jj, ld), 1.0e-6);
-      const S bwv = (X.Ice(jj) + X.Liq(jj)) / denom;
+      const S bwv = jl_div(X.Ice(jj) + X.Liq(jj), denom);
       LV(f.bw, c, jj, ld) = VAL(bwv);
       if (snow_method == CLMGB_SNOW_JORDAN1991) {
         thkv = TKAIR + (7.75e-5 * bwv + 1.105e-6 * (bwv * bwv)) * (TKICE - TKAIR);
@@ -666,7 +673,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     const double z1 = zz[1 + joff];
     const S tk1 = tk[1 + joff];
     const S denom = TKWAT * z1 + tk1 * zh2osfc;
-    if (denom > 0.0) tk_h2osfc = TKWAT * tk1 * (z1 + zh2osfc) / denom;
+    if (denom > 0.0) tk_h2osfc = jl_div(TKWAT * tk1 * (z1 + zh2osfc), denom);
     else tk_h2osfc = tk1;
   }
   // interface conductivity (_soil_tk_interface_kernel! :599-629), ascending so
@@ -676,7 +683,7 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     if (j <= nlevgrnd - 1) {
       const S tkj = tk[jj], tkj1 = tk[jj + 1];
       const double zj = zz[jj], zj1 = zz[jj + 1], zij1 = LVc(ZI, c, jj + 1, ld);
-      tk[jj] = tkj * tkj1 * (zj1 - zj) / (tkj * (zj1 - zij1) + tkj1 * (zij1 - zj));
+      tk[jj] = jl_div(tkj * tkj1 * (zj1 - zj), tkj * (zj1 - zij1) + tkj1 * (zij1 - zj));
     } else if (j == nlevgrnd) {
       tk[jj] = 0.0;
     }
@@ -699,19 +706,19 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
       if (j == 1 && f.h2osno_no_layers[c] > 0.0) cv += CPICE * f.h2osno_no_layers[c];
     } else {
       if (fse > 0.0)
-        cv = jl_max(THIN_SFCLAYER, (CPLIQ * X.Liq(jj) + CPICE * X.Ice(jj)) / fse);
+        cv = jl_max(THIN_SFCLAYER, jl_div(CPLIQ * X.Liq(jj) + CPICE * X.Ice(jj), fse));
       else
         cv = THIN_SFCLAYER;
     }
     S fc;
     if (j == jtop) {
-      fc = dtime / cv * dzv / (0.5 * (zz[jj] - LVc(ZI, c, jj, ld) + CAPR * (zz[jj + 1] - LVc(ZI, c, jj, ld))));
+      fc = jl_div(jl_div(dtime, cv) * dzv, 0.5 * (zz[jj] - LVc(ZI, c, jj, ld) + CAPR * (zz[jj + 1] - LVc(ZI, c, jj, ld))));
       fn[jj] = jl_div(tk[jj] * (tt[jj + 1] - tt[jj]), zz[jj + 1] - zz[jj]);
     } else if (j <= nlevgrnd - 1) {
-      fc = dtime / cv;
+      fc = jl_div(dtime, cv);
       fn[jj] = jl_div(tk[jj] * (tt[jj + 1] - tt[jj]), zz[jj + 1] - zz[jj]);
     } else {
-      fc = dtime / cv;
+      fc = jl_div(dtime, cv);
       fn[jj] = f.eflx_bot[c];
     }
     fct[jj] = fc;
@@ -793,16 +800,16 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     const double dzp = zz[jj + 1] - zz[jj];
     if (j == jtop) {
       x[r] = tt[jj] + fc * (hs_top_snow - dhsdT * tt[jj] + CNFAC * fn[jj]);
-      ab[r * W + 2] = 1.0 + omc * fc * tk[jj] / dzp - fc * dhsdT;
+      ab[r * W + 2] = 1.0 + jl_div(omc * fc * tk[jj], dzp) - fc * dhsdT;
     } else {
       x[r] = tt[jj] + CNFAC * fc * (fn[jj] - fn[jj - 1]);
       x[r] += fc * sabg_lyr_col[jj];
       const double dzm = zz[jj] - zz[jj - 1];
-      ab[r * W + 1] = -omc * fc * tk[jj - 1] / dzm;
-      ab[r * W + 2] = 1.0 + omc * fc * (tk[jj] / dzp + tk[jj - 1] / dzm);
+      ab[r * W + 1] = jl_div(-omc * fc * tk[jj - 1], dzm);
+      ab[r * W + 2] = 1.0 + omc * fc * (jl_div(tk[jj], dzp) + jl_div(tk[jj - 1], dzm));
     }
-    if (j != 0) ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
-    else ab[r * W + 4] = -omc * fc * tk[jj] / dzp;   // snow-soil coupling skips the h2osfc row
+    if (j != 0) ab[r * W + 3] = jl_div(-omc * fc * tk[jj], dzp);
+    else ab[r * W + 4] = jl_div(-omc * fc * tk[jj], dzp);   // snow-soil coupling skips the h2osfc row
   }
   // surface-water row
   S fn_h2osfc;
@@ -824,28 +831,28 @@ __device__ inline uint32_t soil_temperature_col(const Dims& D, const clmgb_soilt
     if (j == jtop) {   // snl == 0
       const double dzp = zz[jj + 1] - zz[jj];
       x[r] = t0 + fc * (hs_top_snow - dhsdT * t0 + CNFAC * fn[jj]);
-      ab[r * W + 2] = 1.0 + omc * fc * tk[jj] / dzp - fc * dhsdT;
-      ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
+      ab[r * W + 2] = 1.0 + jl_div(omc * fc * tk[jj], dzp) - fc * dhsdT;
+      ab[r * W + 3] = jl_div(-omc * fc * tk[jj], dzp);
     } else if (j == 1) {
       const double dzm = zz[jj] - zz[jj - 1];
       const double dzp = zz[jj + 1] - zz[jj];
       x[r] = t0 + fc * ((1.0 - fse) * (hs_soil - dhsdT * t0) + CNFAC * (fn[jj] - fse * fn[jj - 1]));
       x[r] += fse * fc * sabg_lyr_col[j + nlevsno];
-      ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
-      ab[r * W + 2] = 1.0 + omc * fc * (tk[jj] / dzp + fse * tk[jj - 1] / dzm) - (1.0 - fse) * fc * dhsdT;
-      ab[r * W + 0] = -fse * omc * fc * tk[jj - 1] / dzm;
+      ab[r * W + 3] = jl_div(-omc * fc * tk[jj], dzp);
+      ab[r * W + 2] = 1.0 + omc * fc * (jl_div(tk[jj], dzp) + jl_div(fse * tk[jj - 1], dzm)) - (1.0 - fse) * fc * dhsdT;
+      ab[r * W + 0] = jl_div(-fse * omc * fc * tk[jj - 1], dzm);
     } else if (j <= nlevgrnd - 1) {
       const double dzm = zz[jj] - zz[jj - 1];
       const double dzp = zz[jj + 1] - zz[jj];
       x[r] = t0 + CNFAC * fc * (fn[jj] - fn[jj - 1]);
-      ab[r * W + 3] = -omc * fc * tk[jj] / dzp;
-      ab[r * W + 2] = 1.0 + omc * fc * (tk[jj] / dzp + tk[jj - 1] / dzm);
-      ab[r * W + 1] = -omc * fc * tk[jj - 1] / dzm;
+      ab[r * W + 3] = jl_div(-omc * fc * tk[jj], dzp);
+      ab[r * W + 2] = 1.0 + omc * fc * (jl_div(tk[jj], dzp) + jl_div(tk[jj - 1], dzm));
+      ab[r * W + 1] = jl_div(-omc * fc * tk[jj - 1], dzm);
     } else {
       const double dzm = zz[jj] - zz[jj - 1];
       x[r] = t0 - CNFAC * fc * fn[jj - 1] + fc * fn[jj];
-      ab[r * W + 2] = 1.0 + omc * fc * tk[jj - 1] / dzm;
-      ab[r * W + 1] = -omc * fc * tk[jj - 1] / dzm;
+      ab[r * W + 2] = 1.0 + jl_div(omc * fc * tk[jj - 1], dzm);
+      ab[r * W + 1] = jl_div(-omc * fc * tk[jj - 1], dzm);
     }
   }
   if (fh != 0.0) {   // surface-water corrections to soil layer 1 (:1480-1494, :1689-1707)

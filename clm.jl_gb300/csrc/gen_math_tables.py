@@ -125,6 +125,12 @@ def main():
     p2 = float(mp.pi / 2)
     lines.append("#define CM_PIO2_H (%s)" % hexd(p2))
     lines.append("#define CM_PIO2_L (%s)" % hexd(mp.pi / 2 - mp.mpf(p2)))
+    # seed of the integer reciprocal (Moller and Granlund 2011, reciprocal_word):
+    # floor((2^19 - 3*2^8) / d9) for the top 9 bits d9 = 256..511 of a normalised divisor
+    lines.append("CM_TABLE_U16(CM_RECIP_V0, 256) = {")
+    for i in range(0, 256, 8):
+        lines.append("  " + " ".join("%d," % ((2 ** 19 - 3 * 2 ** 8) // (256 + k)) for k in range(i, i + 8)))
+    lines.append("};")
     print("\n".join(lines))
 
 
