@@ -3495,3 +3495,8 @@ double orc_cm_pow(double x, double y) { return cm_pow(x, y); }
 double orc_cm_log10(double x) { return cm_log10(x); }
 double orc_cm_sin(double x) { return cm_sin(x); }
 double orc_cm_acos(double x) { return cm_acos(x); }
+/* The integer-pipe division the GPU kernels use, over n pairs (for the test that it is
+ * the IEEE quotient). */
+void orc_cm_div_n(int64_t n, const double* x, const double* y, double* out) {
+  for (int64_t i = 0; i < n; i++) out[i] = cm_div(x[i], y[i]);
+}

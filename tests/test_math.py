@@ -205,3 +205,43 @@ def test_acos_accuracy():
         worst = max(worst, float(abs(mp.mpf(got) - ref) / ref) / (2.0 ** -52))
     assert worst < 1.5, worst
     assert facos(1.0) == 0.0 and math.isnan(facos(1.0000000000000002)) and math.isnan(facos(math.nan))
+
+
+def test_integer_division_is_the_ieee_quotient():
+    """cm_div (64-bit integer reciprocal and 2/1 division, Moller and Granlund 2011) is
+    the binary64 quotient x / y bit for bit: random bit patterns (every exponent,
+    subnormals, zeros, infinities, NaN), operands with close exponents, divisors and
+    numerators with short significands, products of random significands (quotients
+    next to a representable value), and powers of two."""
+    f = orc.lib().orc_cm_div_n
+    f.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    f.restype = None
+    rng = np.random.default_rng(71)
+    n = 2_000_000
+    a = rng.integers(0, 2 ** 64, n, dtype=np.uint64)
+    b = rng.integers(0, 2 ** 64, n, dtype=np.uint64)
+    frac = np.uint64(0x000FFFFFFFFFFFFF)
+    sgn = np.uint64(0x8000000000000000)
+    close = rng.integers(1000, 1048, (2, n), dtype=np.uint64) << np.uint64(52)
+    k = n // 5
+    a[k:2 * k] = (a[k:2 * k] & (frac | sgn)) | close[0, k:2 * k]
+    b[k:2 * k] = (b[k:2 * k] & (frac | sgn)) | close[1, k:2 * k]
+    b[2 * k:3 * k] &= ~np.uint64(0x000FFFFFFFFFFF00)            # short divisor significands
+    x = a.view(np.float64)
+    y = b.view(np.float64)
+    q = (rng.integers(0, 2 ** 52, n, dtype=np.uint64) | np.uint64(1023 << 52)).view(np.float64)
+    with np.errstate(all="ignore"):
+        x[3 * k:4 * k] = q[3 * k:4 * k] * y[3 * k:4 * k]           # quotients next to q
+    y[4 * k:4 * k + 1000] = 2.0 ** rng.integers(-1000, 1000, 1000)   # powers of two
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.0, -3.0, 1e300,
+                        1.7976931348623157e308, np.inf, -np.inf, np.nan])
+    sx, sy = np.meshgrid(special, special, indexing="ij")
+    x = np.concatenate([x, sx.ravel()])
+    y = np.concatenate([y, sy.ravel()])
+    out = np.empty_like(x)
+    f(len(x), x.ctypes.data, y.ctypes.data, out.ctypes.data)
+    with np.errstate(all="ignore"):
+        want = x / y
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(out), nan)
+    assert np.array_equal(out[~nan].view(np.uint64), want[~nan].view(np.uint64))
