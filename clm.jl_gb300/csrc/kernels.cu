@@ -460,8 +460,8 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
   for (int base = 0; base < T; base += 32) {
     const Item it = item(base);
     if (it.ok) {
-      const double vwc = jl_max(A(FN, it.k, it.j), 1.0e-6) / P(it.c, PC_DZW, it.j);
-      double s = vwc / P(it.c, PC_WS, it.j);
+      const double vwc = jl_div(jl_max(A(FN, it.k, it.j), 1.0e-6), P(it.c, PC_DZW, it.j));
+      double s = jl_div(vwc, P(it.c, PC_WS, it.j));
       s = jl_min(s, 1.0);
       A(FN, it.k, it.j) = jl_max(0.01, s);
     }
@@ -481,10 +481,10 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
       s1 = jl_max(0.01, s1);
       const double b = P(c, PC_BSW, j);
       hkv = P(c, PC_IMP, j) * P(c, PC_KS, j) * cm_pow(s1, 2.0 * b + 3.0);
-      dhkds = (2.0 * b + 3.0) * hkv / s1;
+      dhkds = jl_div((2.0 * b + 3.0) * hkv, s1);
       smpv = -P(c, PC_SUC, j) * cm_pow(sj, -b);
-      const double dsmpds = -b * smpv / sj;
-      dsmpdw = dsmpds / P(c, PC_WS, j);
+      const double dsmpds = jl_div(-b * smpv, sj);
+      dsmpdw = jl_div(dsmpds, P(c, PC_WS, j));
       double* rec = pcache + c * (int64_t)(PC_ALL * nls);
       rec[PC_SMP * nls + j - 1] = smpv;
       rec[PC_HK * nls + j - 1] = hkv;
@@ -508,13 +508,13 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
       const int64_t c = it.c;
       const double hk = A(QOUT, it.k, j), dhkdw = A(D1, it.k, j), smp = A(D2, it.k, j), dsmpdw = A(FN, it.k, j);
       if (j < it.nl) {
-        const double dhkds1 = 0.5 * dhkdw / P(c, PC_WS, j);
-        const double dhkds2 = 0.5 * dhkdw / P(c, PC_WS, j + 1);
+        const double dhkds1 = jl_div(0.5 * dhkdw, P(c, PC_WS, j));
+        const double dhkds2 = jl_div(0.5 * dhkdw, P(c, PC_WS, j + 1));
         const double num = A(D2, it.k, j + 1) - smp;
         const double den = P(c, PC_DEN, j);
-        qo = -hk * num / den + hk;
-        d1 = (hk * dsmpdw - dhkds1 * num) / den + dhkds1;
-        d2 = (-hk * A(FN, it.k, j + 1) - dhkds2 * num) / den + dhkds2;
+        qo = jl_div(-hk * num, den) + hk;
+        d1 = jl_div(hk * dsmpdw - dhkds1 * num, den) + dhkds1;
+        d2 = jl_div(-hk * A(FN, it.k, j + 1) - dhkds2 * num, den) + dhkds2;
       } else {
         sb[it.k] = hk;
         sb[32 + it.k] = dhkdw;
@@ -527,7 +527,7 @@ __device__ __forceinline__ void mfp_refresh(MfLaneP& L, unsigned mask, const Dim
             const double dhkds1l = dhkdw / P(c, PC_WS, j);
             const double num = -smp;
             const double den = M_TO_MM * (f.zwt[c] - LVc(f.z, c, joff + j, ld));
-            qo = -hk * num / den + hk;
+            qo = jl_div(-hk * num, den) + hk;
             d1 = (hk * dsmpdw - dhkds1l * num) / den + dhkds1l;
           }
         } else if (lower_bc == CLMGB_BC_FLUX) {
