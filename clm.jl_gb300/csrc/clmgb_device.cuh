@@ -1176,10 +1176,10 @@ __device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soi
         if (ev + (ea - eb) > 0 && ev + (ea - eb) < 2047 && ev > 0)
           L.dt_dz[j] = __longlong_as_double(v + shift);
         else
-          L.dt_dz[j] = dtsub / mf_dzw(L, j);
+          L.dt_dz[j] = jl_div(dtsub, mf_dzw(L, j));
       }
     } else {
-      for (int j = 1; j <= nlayers; j++) L.dt_dz[j] = dtsub / mf_dzw(L, j);
+      for (int j = 1; j <= nlayers; j++) L.dt_dz[j] = jl_div(dtsub, mf_dzw(L, j));
     }
     L.dt_cur = dtsub;
   }
@@ -1194,7 +1194,7 @@ __device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soi
     const S bmx = -1.0 - (-dqidw1_1 + L.dqodw1[1]) * L.dt_dz[1];
     bet = bmx;
     if (abs_lt(VAL(bet), 1.0e-30)) bet = 1.0e-30;
-    dwat_prev = rmx / bet;
+    dwat_prev = jl_div(rmx, bet);
     L.dwat[1] = dwat_prev;
   }
   S cmx_prev = -L.dqodw2[1] * L.dt_dz[1];
@@ -1204,10 +1204,10 @@ __device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soi
     S cmx = 0.0;
     if (j != nlayers) cmx = -L.dqodw2[j] * L.dt_dz[j];
     const S rmx = -L.fnet1[j] * L.dt_dz[j];
-    L.gam[j] = cmx_prev / bet;
+    L.gam[j] = jl_div(cmx_prev, bet);
     bet = bmx - amx * L.gam[j];
     if (abs_lt(VAL(bet), 1.0e-30)) bet = copysign(1.0e-30, VAL(bet) == 0.0 ? 1.0 : VAL(bet));
-    dwat_prev = (rmx - amx * dwat_prev) / bet;
+    dwat_prev = jl_div(rmx - amx * dwat_prev, bet);
     L.dwat[j] = dwat_prev;
     cmx_prev = cmx;
   }
@@ -1233,7 +1233,7 @@ __device__ __forceinline__ bool mf_attempt(LT& L, const Dims& D, const clmgb_soi
                                                   VAL(L.dqodw2[j]) * VAL(L.dwat[j + 1]);
       fnet0 = qin_test - qout_test - LVc(f.qflx_rootsoi, c, j, ld);
     } else {
-      fnet0 = VAL(L.dwat[j]) / L.dt_dz[j];
+      fnet0 = jl_div(VAL(L.dwat[j]), L.dt_dz[j]);
     }
     const double ev = fabs(VAL(L.fnet1[j]) - fnet0) * dtsub * 0.5;
     errorMax = jl_max(errorMax, ev);
