@@ -114,7 +114,7 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
     // dt_dz = dtsub / (1000 dz); the work-queue kernel's exponent rescaling of it
     // gives this quotient's bits, so it is divided afresh here
     if (dtsub != dt_cur) {
-      dt_dz = dtsub / (M_TO_MM * dzv);
+      dt_dz = jl_div(dtsub, M_TO_MM * dzv);
       dt_cur = dtsub;
     }
     if (qs.work && lane == 0) atomicAdd(qs.work, (unsigned long long)n);   // an attempt over n levels
@@ -123,8 +123,8 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
       // hydraulic properties (mf_refresh, :1280-1308)
       double s2 = 0.0;
       if (lv) {
-        const double vwc = jl_max(liq, 1.0e-6) / (dzv * DENH2O);
-        s2 = vwc / ws;
+        const double vwc = jl_div(jl_max(liq, 1.0e-6), dzv * DENH2O);
+        s2 = jl_div(vwc, ws);
         s2 = jl_min(s2, 1.0);
         s2 = jl_max(0.01, s2);
       }
@@ -135,13 +135,13 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
         s1 = jl_min(s1, 1.0);
         s1 = jl_max(0.01, s1);
         const double hkv = imp * hksat * cm_pow(s1, 2.0 * bsw + 3.0);
-        const double dhkds = (2.0 * bsw + 3.0) * hkv / s1;
+        const double dhkds = jl_div((2.0 * bsw + 3.0) * hkv, s1);
         const double smpv = -sucsat * cm_pow(s2, -bsw);
-        const double dsmpds = -bsw * smpv / s2;
+        const double dsmpds = jl_div(-bsw * smpv, s2);
         hk = hkv;
         smp = smpv;
         dhkdw = dhkds;
-        dsmpdw = dsmpds / ws;
+        dsmpdw = jl_div(dsmpds, ws);
         if (orec) {
           orec[PC_SMP * nlevsoi + j - 1] = smpv;
           orec[PC_HK * nlevsoi + j - 1] = hkv;
@@ -156,13 +156,13 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
       const double dsmpdwn = __shfl_down_sync(COOP_FULL, dsmpdw, 1);
       qin = qout = dqidw0 = dqidw1 = dqodw1 = dqodw2 = 0.0;
       if (lv && j <= n - 1) {
-        const double dhkds1 = 0.5 * dhkdw / ws;
-        const double dhkds2 = 0.5 * dhkdw / wsn;
+        const double dhkds1 = jl_div(0.5 * dhkdw, ws);
+        const double dhkds2 = jl_div(0.5 * dhkdw, wsn);
         const double num = smpn - smp;
         const double den = M_TO_MM * (zj1 - zj);
-        qout = -hk * num / den + hk;
-        dqodw1 = (hk * dsmpdw - dhkds1 * num) / den + dhkds1;
-        dqodw2 = (-hk * dsmpdwn - dhkds2 * num) / den + dhkds2;
+        qout = jl_div(-hk * num, den) + hk;
+        dqodw1 = jl_div(hk * dsmpdw - dhkds1 * num, den) + dhkds1;
+        dqodw2 = jl_div(-hk * dsmpdwn - dhkds2 * num, den) + dhkds2;
       } else if (lv && j == n) {
         if (lower_bc == CLMGB_BC_WATERTABLE) {
           int jwt = nlevsoi;
@@ -177,16 +177,16 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
             dqodw1 = 0.0;
             dqodw2 = 0.0;
           } else {
-            const double dhkds1l = dhkdw / ws;
+            const double dhkds1l = jl_div(dhkdw, ws);
             const double num = -smp;
             const double den = M_TO_MM * (f.zwt[c] - zj);
-            qout = -hk * num / den + hk;
-            dqodw1 = (hk * dsmpdw - dhkds1l * num) / den + dhkds1l;
+            qout = jl_div(-hk * num, den) + hk;
+            dqodw1 = jl_div(hk * dsmpdw - dhkds1l * num, den) + dhkds1l;
             dqodw2 = 0.0;
           }
         } else if (lower_bc == CLMGB_BC_FLUX) {
           qout = hk;
-          dqodw1 = dhkdw / ws;
+          dqodw1 = jl_div(dhkdw, ws);
         } else {
           qout = 0.0;
           dqodw1 = 0.0;
@@ -214,16 +214,16 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
     const double rmx = -fnet1 * dt_dz;
     double bet = coop_bcast(bmx, 0);
     if (abs_lt(bet, 1.0e-30)) bet = 1.0e-30;
-    double dwat_prev = coop_bcast(rmx, 0) / bet;
+    double dwat_prev = jl_div(coop_bcast(rmx, 0), bet);
     if (lane == 0) dwat = dwat_prev;
     double cmx_prev = coop_bcast(-dqodw2 * dt_dz, 0);
     for (int i = 2; i <= n; i++) {
       const double a_i = coop_bcast(amx, i - 1), b_i = coop_bcast(bmx, i - 1), c_i = coop_bcast(cmx, i - 1);
       const double r_i = coop_bcast(rmx, i - 1);
-      const double g = cmx_prev / bet;
+      const double g = jl_div(cmx_prev, bet);
       bet = b_i - a_i * g;
       if (abs_lt(bet, 1.0e-30)) bet = copysign(1.0e-30, bet == 0.0 ? 1.0 : bet);
-      dwat_prev = (r_i - a_i * dwat_prev) / bet;
+      dwat_prev = jl_div(r_i - a_i * dwat_prev, bet);
       if (lane == i - 1) {
         gam = g;
         dwat = dwat_prev;
@@ -251,7 +251,7 @@ __device__ __noinline__ void coop_finish_column(const Dims& D, const clmgb_soilw
           const double qout_test = j == n ? qout + dqodw1 * dwat : qout + dqodw1 * dwat + dqodw2 * dwn;
           fnet0 = qin_test - qout_test - root;
         } else {
-          fnet0 = dwat / dt_dz;
+          fnet0 = jl_div(dwat, dt_dz);
         }
         ev = fabs(fnet1 - fnet0) * dtsub * 0.5;
       }
