@@ -193,14 +193,15 @@ def profile_traffic():
 
 
 def fp64_probe():
-    """(DFMA/s, divisions/s, pow/s, log10/s) of this device from libclmgb_probe.so, or None."""
+    """(DFMA/s, divisions/s, pow/s, log10/s, integer-pipe divisions/s) of this device from
+    libclmgb_probe.so, or None."""
     import ctypes as C
     from clmgb import build
     try:
         lib = C.CDLL(build.build_probe())
     except OSError:
         return None
-    out = (C.c_double * 4)()
+    out = (C.c_double * 5)()
     lib.clmgb_probe_fp64.argtypes = [C.c_int, C.POINTER(C.c_double)]
     if lib.clmgb_probe_fp64(4, out) != 0:
         return None

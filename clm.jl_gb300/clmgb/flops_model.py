@@ -16,13 +16,16 @@ after every accepted substep, plus that substep's water update):
     flux 2; the accepted substep's water update 3:
     27 add/mul + 10 divisions + 2 pow per level
 
-An add, subtract or multiply is one FP64 pipe instruction, as a DFMA is.  A correctly
-rounded division and a pow (clm_math.h) are sequences of them; their cost in
-DFMA-equivalents is the ratio of the DFMA rate to their rate, both measured on the
-device by the probe (clm.jl_gb300/probe/fp64_probe.cu).  The kernel counts the levels
-of its attempts and refreshes itself (CLMGB_OPT_COUNT_WORK), so
+An add, subtract or multiply is one FP64 pipe instruction, as a DFMA is.  A pow
+(clm_math.h, a double-double logarithm and exponential) is a sequence of them; its cost
+in DFMA-equivalents is the ratio of the DFMA rate to its rate, both measured on the
+device by the probe (clm.jl_gb300/probe/fp64_probe.cu).  The divisions run on the
+integer pipes (jl_div: cm_div's 64-bit reciprocal and 2/1 division), not on the FP64
+pipe, so they add nothing to the FP64 work; they are counted separately.  The kernel
+counts the levels of its attempts and refreshes itself (CLMGB_OPT_COUNT_WORK), so
 
-  DFMA-equivalents = level_attempts * (15 + 3 w_div) + level_refreshes * (27 + 10 w_div + 2 w_pow)
+  DFMA-equivalents = level_attempts * 15 + level_refreshes * (27 + 2 w_pow)
+  integer-pipe divisions = level_attempts * 3 + level_refreshes * 10
 
 and the FP64 fraction of a launch is that work over (launch time x measured DFMA rate).
 """
@@ -39,9 +42,14 @@ def weights(probe):
 
 
 def dfma_equivalents(level_attempts, level_refreshes, w):
-    per_att = ATTEMPT["ops"] + ATTEMPT["div"] * w["div"] + ATTEMPT["pow"] * w["pow"]
-    per_ref = REFRESH["ops"] + REFRESH["div"] * w["div"] + REFRESH["pow"] * w["pow"]
+    """FP64-pipe work; the divisions run on the integer pipes."""
+    per_att = ATTEMPT["ops"] + ATTEMPT["pow"] * w["pow"]
+    per_ref = REFRESH["ops"] + REFRESH["pow"] * w["pow"]
     return level_attempts * per_att + level_refreshes * per_ref
+
+
+def integer_divisions(level_attempts, level_refreshes):
+    return level_attempts * ATTEMPT["div"] + level_refreshes * REFRESH["div"]
 
 
 def fp64_roofline(level_attempts, level_refreshes, launches, kernel_ms, probe):
@@ -53,5 +61,7 @@ def fp64_roofline(level_attempts, level_refreshes, launches, kernel_ms, probe):
             "unit": "TFLOP/s (DFMA-equivalent)", "frac": achieved / probe[0],
             "dfma_equivalents_per_launch": work, "level_attempts_per_launch": level_attempts / launches,
             "level_refreshes_per_launch": level_refreshes / launches,
+            "integer_pipe_divisions_per_launch": integer_divisions(level_attempts, level_refreshes) / launches,
             "weights_dfma_equivalents": w, "probe_rates_per_s": {"dfma": probe[0], "div": probe[1],
-                                                                 "pow": probe[2], "log10": probe[3]}}
+                                                                 "pow": probe[2], "log10": probe[3],
+                                                                 "integer_div": probe[4] if len(probe) > 4 else None}}

@@ -38,6 +38,18 @@ __global__ void __launch_bounds__(THREADS) k_ddiv(int n, double d, double* out) 
   if (s == 12345.678) out[0] = s;
 }
 
+// the integer-pipe division the kernels use (cm_div): 4 independent chains a <- d / a
+__global__ void __launch_bounds__(THREADS) k_idiv(int n, double d, double* out) {
+  double a[4];
+  for (int k = 0; k < 4; k++) a[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+  for (int i = 0; i < n; i++) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) a[k] = cm_div(d, a[k]);
+  }
+  double s = a[0] + a[1] + a[2] + a[3];
+  if (s == 12345.678) out[0] = s;
+}
+
 // cm_pow(x, y) on x in [0.5, 1.5), y non-integral: 4 independent chains
 __global__ void __launch_bounds__(THREADS) k_pow(int n, double y, double* out) {
   double a[4];
@@ -81,7 +93,8 @@ static double time_ms(F launch) {
 }  // namespace
 
 // out[0] DFMA instructions per second (the device), out[1] divisions per second,
-// out[2] cm_pow calls per second, out[3] cm_log10 calls per second.  blocks_per_sm
+// out[2] cm_pow calls per second, out[3] cm_log10 calls per second, out[4] integer-pipe
+// divisions (cm_div) per second.  blocks_per_sm
 // resident 256-thread blocks on every SM.  Returns 0, or the CUDA error code.
 extern "C" int clmgb_probe_fp64(int blocks_per_sm, double* out) {
   int dev = 0, sms = 0;
@@ -97,6 +110,7 @@ extern "C" int clmgb_probe_fp64(int blocks_per_sm, double* out) {
   const double t_div = time_ms([&] { k_ddiv<<<grid, THREADS>>>(nd, 1.0000001, sink); });
   const double t_pow = time_ms([&] { k_pow<<<grid, THREADS>>>(np, 0.9, sink); });
   const double t_l10 = time_ms([&] { k_log10<<<grid, THREADS>>>(nl, sink); });
+  const double t_idiv = time_ms([&] { k_idiv<<<grid, THREADS>>>(nd, 1.0000001, sink); });
   e = cudaGetLastError();
   cudaFree(sink);
   if (e != cudaSuccess) return (int)e;
@@ -104,5 +118,6 @@ extern "C" int clmgb_probe_fp64(int blocks_per_sm, double* out) {
   out[1] = threads * 4 * nd / (t_div * 1e-3);
   out[2] = threads * 4 * np / (t_pow * 1e-3);
   out[3] = threads * 4 * nl / (t_l10 * 1e-3);
+  out[4] = threads * 4 * nd / (t_idiv * 1e-3);
   return 0;
 }
