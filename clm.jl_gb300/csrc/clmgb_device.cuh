@@ -92,8 +92,8 @@ __device__ __forceinline__ double jl_min(double x, double y) {
 // other case (subnormal, infinite or NaN operands, quotients outside the normal range)
 // is the hardware division.  The result is always the IEEE quotient.
 // (one out-of-line copy of the integer division: measured faster than a copy inlined
-// at every call site, 4.1 against about 5.4 ms for the soil-temperature part of a step
-// at 262,144 columns, and 10.5 against 17.7 ms for the Richards solve)
+// at every call site, 4.2 against 5.6 ms for the part of a step at 262,144 columns
+// outside the Richards solve, and 10.5 against 17.7 ms for the Richards solve)
 static __device__ __noinline__ double cm_div_call(double x, double y) { return cm_div(x, y); }
 __device__ __forceinline__ double jl_div(double x, double y) {
   const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
