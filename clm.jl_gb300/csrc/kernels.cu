@@ -62,10 +62,9 @@ k_soil_temperature(Dims D, int64_t nc, clmgb_soiltemp_fields f, double dtime, in
   report(st, col_status, dev_status, c);
 }
 
-// set_soil_water_fractions! (water_fractions_col's arithmetic, in the same order),
-// through restrict-qualified level pointers so that the loads of later levels can be
-// issued before the stores of earlier ones (the inputs and the two outputs are
-// distinct arrays)
+// set_soil_water_fractions! (water_fractions_col's arithmetic, in the same order) over
+// restrict-qualified level pointers (the inputs and the two outputs are distinct
+// arrays); its time is the three divisions per level (jl_div)
 __global__ void __launch_bounds__(BLOCK)
 k_water_fractions(Dims D, int64_t nc, clmgb_soilwater_fields f) {
   const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
