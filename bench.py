@@ -707,9 +707,12 @@ def run_ours(args):
                 "step_algorithmic_bytes": step_bytes,
                 "step_achieved_gbs": step_bytes / (elapsed_ms / args.steps / 1000.0) / 1e9,
                 "fp64": fp64, "fp64_frac": fp64["frac"] if fp64 else None,
-                "note": "the kernel is bound by the FP64 pipe, not HBM: fp64 is its work in DFMA-equivalents "
-                        "(clmgb/flops_model.py, levels counted by the kernel) over its time and the DFMA rate "
-                        "the probe measures on this device; ncu summaries in profiles/"}
+                "note": "HBM is not the bound: the kernel runs thousands of FP64 operations per 2 KB of traffic. "
+                        "fp64 is its FP64-pipe work in DFMA-equivalents (clmgb/flops_model.py, levels counted by "
+                        "the kernel) over its time and the DFMA rate the probe measures on this device; its "
+                        "divisions run on the integer pipes (fp64.integer_pipe_divisions_per_launch), and with "
+                        "them off the FP64 pipe the kernel is bound by latency at 7-10 warps per SM; ncu "
+                        "summaries in profiles/"}
 
     # end to end with the state in pinned host memory (clmgb.hoststep): each step moves
     # the fields it reads that the rest of the model changes (parameters, geometry and
