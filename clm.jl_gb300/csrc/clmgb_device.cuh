@@ -155,33 +155,78 @@ __device__ __forceinline__ double VAL(double x) { return x; }
 template <int KL, int KU, class S>
 __device__ __forceinline__ void band_lu_solve(S* ab, S* x, int n) {
   constexpr int W = 2 * KL + KU + 1;
+  // Partial-pivot elimination: step k picks the largest |A[i,k]| of rows k..k+KL,
+  // swaps it into row k (columns k..k+KL+KU and the right-hand side), and subtracts
+  // f = A[i,k]/A[k,k] times row k from each row below (the same steps as
+  // band_lu_factor_solve below).  Step k touches rows k..k+KL over columns
+  // k..k+KL+KU only; that window is kept in registers (w[i][c] = A[k+i, k+c]), so each
+  // row comes in once from the assembled band and leaves once as its row of U, which
+  // the back substitution reads.
+  constexpr int R = KL + 1, C = KL + KU + 1;
 #define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
+  S w[R][C];
+#pragma unroll
+  for (int i = 0; i < R; i++)
+#pragma unroll
+    for (int c = 0; c < C; c++) w[i][c] = i < n ? AB(i, c) : S(0.0);
   for (int k = 0; k < n - 1; k++) {
-    int piv = k;
-    double maxv = fabs(VAL(AB(k, k)));
-    const int ilast = min(n - 1, k + KL);
-    for (int i = k + 1; i <= ilast; i++) {
-      double v = fabs(VAL(AB(i, k)));
-      if (v > maxv) { maxv = v; piv = i; }
-    }
-    const S akk = AB(piv, k);
-    const int clast = min(n - 1, k + KL + KU);
-    if (piv != k) {
-      for (int col = k; col <= clast; col++) {
-        S akj = AB(k, col), apj = AB(piv, col);
-        AB(k, col) = apj;
-        AB(piv, col) = akj;
+    const int ni = min(n - 1, k + KL) - k;          // rows k+1..k+ni are in the system
+    const int nc = min(n - 1, k + KL + KU) - k;     // columns k..k+nc are in the system
+    int piv = 0;
+    double maxv = fabs(VAL(w[0][0]));
+#pragma unroll
+    for (int i = 1; i < R; i++) {
+      if (i <= ni) {
+        const double v = fabs(VAL(w[i][0]));
+        if (v > maxv) {
+          maxv = v;
+          piv = i;
+        }
       }
-      S xk = x[k], xp = x[piv];
-      x[k] = xp;
-      x[piv] = xk;
     }
-    for (int i = k + 1; i <= ilast; i++) {
-      const S f = jl_div(AB(i, k), akk);
-      for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
-      x[i] = x[i] - f * x[k];
+#pragma unroll
+    for (int i = 1; i < R; i++) {
+      if (i == piv) {
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          if (c <= nc) {
+            const S a = w[0][c];
+            w[0][c] = w[i][c];
+            w[i][c] = a;
+          }
+        }
+        const S xk = x[k], xp = x[k + i];
+        x[k] = xp;
+        x[k + i] = xk;
+      }
     }
+    const S akk = w[0][0];
+#pragma unroll
+    for (int i = 1; i < R; i++) {
+      if (i <= ni) {
+        const S f = jl_div(w[i][0], akk);
+#pragma unroll
+        for (int c = 1; c < C; c++)
+          if (c <= nc) w[i][c] = w[i][c] - f * w[0][c];
+        x[k + i] = x[k + i] - f * x[k];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < C; c++)
+      if (c <= nc) AB(k, k + c) = w[0][c];
+    // slide down a row: the column the window gains comes from storage (no step has
+    // written it yet), and row k+1+KL enters with its band
+#pragma unroll
+    for (int i = 0; i < R - 1; i++) {
+#pragma unroll
+      for (int c = 0; c < C - 1; c++) w[i][c] = w[i + 1][c + 1];
+      w[i][C - 1] = k + 1 + i < n ? AB(k + 1 + i, k + C) : S(0.0);
+    }
+    const int r = k + 1 + KL;
+#pragma unroll
+    for (int c = 0; c < C; c++) w[R - 1][c] = r < n ? AB(r, k + 1 + c) : S(0.0);
   }
+  if (n > 0) AB(n - 1, n - 1) = w[0][0];
   for (int i = n - 1; i >= 0; i--) {
     S s = x[i];
     const int jl = min(n - 1, i + KL + KU);
