@@ -241,37 +241,77 @@ __device__ __forceinline__ void band_lu_solve(S* ab, S* x, int n) {
 // records the row exchange of step k.  x is bit-identical to band_lu_solve's.
 template <int KL, int KU>
 __device__ __forceinline__ void band_lu_factor_solve(double* ab, double* x, uint8_t* piv, int n) {
+  // band_lu_solve's elimination and register window; the multiplier of row k+i leaves
+  // with the window into A[k+i, k], the slot of the entry it eliminated
   constexpr int W = 2 * KL + KU + 1;
+  constexpr int R = KL + 1, C = KL + KU + 1;
 #define AB(r, col) ab[(r) * W + ((col) - (r) + KL)]
+  double w[R][C];
+#pragma unroll
+  for (int i = 0; i < R; i++)
+#pragma unroll
+    for (int c = 0; c < C; c++) w[i][c] = i < n ? AB(i, c) : 0.0;
   for (int k = 0; k < n - 1; k++) {
-    int p = k;
-    double maxv = fabs(AB(k, k));
-    const int ilast = min(n - 1, k + KL);
-    for (int i = k + 1; i <= ilast; i++) {
-      const double v = fabs(AB(i, k));
-      if (v > maxv) { maxv = v; p = i; }
-    }
-    piv[k] = (uint8_t)(p - k);
-    const double akk = AB(p, k);
-    const int clast = min(n - 1, k + KL + KU);
-    if (p != k) {
-      for (int col = k; col <= clast; col++) {
-        const double akj = AB(k, col), apj = AB(p, col);
-        AB(k, col) = apj;
-        AB(p, col) = akj;
+    const int ni = min(n - 1, k + KL) - k;
+    const int nc = min(n - 1, k + KL + KU) - k;
+    int p = 0;
+    double maxv = fabs(w[0][0]);
+#pragma unroll
+    for (int i = 1; i < R; i++) {
+      if (i <= ni) {
+        const double v = fabs(w[i][0]);
+        if (v > maxv) {
+          maxv = v;
+          p = i;
+        }
       }
-      const double xk = x[k], xp = x[p];
-      x[k] = xp;
-      x[p] = xk;
     }
-    for (int i = k + 1; i <= ilast; i++) {
-      const double f = jl_div(AB(i, k), akk);
-      for (int col = k + 1; col <= clast; col++) AB(i, col) = AB(i, col) - f * AB(k, col);
-      x[i] = x[i] - f * x[k];
-      AB(i, k) = f;
+    piv[k] = (uint8_t)p;
+#pragma unroll
+    for (int i = 1; i < R; i++) {
+      if (i == p) {
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          if (c <= nc) {
+            const double a = w[0][c];
+            w[0][c] = w[i][c];
+            w[i][c] = a;
+          }
+        }
+        const double xk = x[k], xp = x[k + i];
+        x[k] = xp;
+        x[k + i] = xk;
+      }
     }
+    const double akk = w[0][0];
+#pragma unroll
+    for (int i = 1; i < R; i++) {
+      if (i <= ni) {
+        const double f = jl_div(w[i][0], akk);
+#pragma unroll
+        for (int c = 1; c < C; c++)
+          if (c <= nc) w[i][c] = w[i][c] - f * w[0][c];
+        x[k + i] = x[k + i] - f * x[k];
+        AB(k + i, k) = f;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < C; c++)
+      if (c <= nc) AB(k, k + c) = w[0][c];
+#pragma unroll
+    for (int i = 0; i < R - 1; i++) {
+#pragma unroll
+      for (int c = 0; c < C - 1; c++) w[i][c] = w[i + 1][c + 1];
+      w[i][C - 1] = k + 1 + i < n ? AB(k + 1 + i, k + C) : 0.0;
+    }
+    const int r = k + 1 + KL;
+#pragma unroll
+    for (int c = 0; c < C; c++) w[R - 1][c] = r < n ? AB(r, k + 1 + c) : 0.0;
   }
-  if (n > 0) piv[n - 1] = 0;
+  if (n > 0) {
+    AB(n - 1, n - 1) = w[0][0];
+    piv[n - 1] = 0;
+  }
   for (int i = n - 1; i >= 0; i--) {
     double s = x[i];
     const int jl = min(n - 1, i + KL + KU);
