@@ -63,6 +63,29 @@ def test_band_solve_bit_exact_vs_oracle(handle_factory, kl):
     assert np.array_equal(got, tv_ref), "max |diff| %g" % np.nanmax(np.abs(got - tv_ref))
 
 
+@pytest.mark.parametrize("kl", [1, 2])
+def test_band_solve_short_systems_and_pivoting_everywhere(handle_factory, kl):
+    """Systems of 1 to 8 rows (the elimination window reaching past the last row) and
+    systems whose every diagonal is weak, so that nearly every step exchanges rows:
+    the bits of the oracle's dense elimination."""
+    h = handle_factory(synth.clm5_varpar())
+    rng = np.random.default_rng(31 + kl)
+    nc, nlev = 4096, 38
+    bm, rv = random_band_system(nc, nlev, kl, kl, rng, pivot_frac=0.0)
+    weak = np.arange(nc) % 2 == 1                            # odd columns: every diagonal weak
+    bm[:, kl, weak] *= 1e-3
+    jtop = rng.integers(1, nlev - 8, nc).astype(np.int64)
+    jbot = jtop + (np.arange(nc) // 2) % 8                   # 1..8 rows
+    jbot[::64] = nlev                                         # and some full-length ones
+    mask = np.ones(nc, dtype=np.uint8)
+    tv_ref = np.full((nlev, nc), -7.0)
+    orc.batched_band_solve(tv_ref, bm, rv, jtop, jbot, mask, kl, kl, -1)
+    tv = _dev(np.full((nlev, nc), -7.0))
+    api.batched_band_solve(h, tv, _dev(bm), _dev(rv), _dev(jtop), _dev(jbot), _dev(mask), kl, kl, -1)
+    got = tv.cpu().numpy()
+    assert np.array_equal(got.view(np.uint64), tv_ref.view(np.uint64))
+
+
 @pytest.mark.parametrize("name", ["band_penta5", "band_penta6", "band_tri4", "band_partial"])
 def test_band_solve_known_answers(handle_factory, name):
     h = handle_factory(synth.clm5_varpar())
