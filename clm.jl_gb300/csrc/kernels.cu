@@ -62,31 +62,11 @@ k_soil_temperature(Dims D, int64_t nc, clmgb_soiltemp_fields f, double dtime, in
   report(st, col_status, dev_status, c);
 }
 
-// set_soil_water_fractions! (water_fractions_col's arithmetic, in the same order) over
-// restrict-qualified level pointers (the inputs and the two outputs are distinct
-// arrays); its time is the three divisions per level (jl_div)
 __global__ void __launch_bounds__(BLOCK)
 k_water_fractions(Dims D, int64_t nc, clmgb_soilwater_fields f) {
   const int64_t c = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-  if (c >= nc || !f.mask_hydrology[c]) return;
-  const int64_t ld = D.ldc;
-  const double* __restrict__ exi_p = f.excess_ice + c;
-  const double* __restrict__ dz_p = f.dz + (int64_t)D.nlevsno * ld + c;
-  const double* __restrict__ ice_p = f.h2osoi_ice + (int64_t)D.nlevsno * ld + c;
-  const double* __restrict__ ws_p = f.watsat + c;
-  double* __restrict__ ep_p = f.eff_porosity + c;
-  double* __restrict__ if_p = f.icefrac + c;
-  const int nls = D.nlevsoi;
-#pragma unroll 4
-  for (int j = 0; j < nls; j++) {
-    const int64_t o = (int64_t)j * ld;
-    const double exi = exi_p[o];
-    const double dz_ext = dz_p[o] + jl_div(exi, DENICE);
-    const double ws = ws_p[o];
-    const double vol_ice = jl_min(ws, jl_div(ice_p[o] + exi, dz_ext * DENICE));
-    ep_p[o] = jl_max(0.01, ws - vol_ice);
-    if_p[o] = jl_min(1.0, jl_div(vol_ice, ws));
-  }
+  if (c >= nc) return;
+  if (f.mask_hydrology[c]) water_fractions_col(D, f, c);
 }
 
 __global__ void __launch_bounds__(BLOCK)
