@@ -409,21 +409,31 @@ def test_math_bit_identical_to_cpu_build(handle_factory, op):
 
 
 def test_division_is_ieee_with_zero_numerators(handle_factory):
-    """The kernels' division (a zero numerator over a finite nonzero divisor answered
-    from the sign bits, the rest by the hardware division) against IEEE division on
-    the host, over every pairing of zeros, subnormals, normals, extremes, infinities
-    and NaN, and 200,000 random pairs with a fifth of the numerators zero."""
+    """The kernels' division (jl_div: a zero numerator over a finite nonzero divisor
+    answered from the sign bits, normal operands by cm_div on the integer pipes, the
+    rest by the hardware division) against IEEE division on the host, over every pairing of zeros, subnormals, normals, extremes, infinities
+    and NaN, and 4 M random pairs: numerators a fifth zero, random bit patterns (every
+    exponent class), divisors with short significands, quotients next to a
+    representable value."""
     h = handle_factory(synth.clm5_varpar())
     tiny = np.nextafter(0.0, 1.0)
     special = np.array([0.0, -0.0, tiny, -tiny, 2.2250738585072014e-308, 1e-300, 1e-20, 0.5, 1.0, 917.0, 3.0e8,
                         1e300, np.finfo(np.float64).max, -1.0, -917.0, np.inf, -np.inf, np.nan])
     xs, ys = np.meshgrid(special, special, indexing="ij")
     rng = np.random.default_rng(61)
-    n = 200000
+    n = 4_000_000
     xr = rng.uniform(-50.0, 50.0, n) * 10.0 ** rng.integers(-30, 30, n)
     xr[rng.random(n) < 0.2] = 0.0
     xr[rng.random(n) < 0.05] *= -0.0
     yr = rng.uniform(-50.0, 50.0, n) * 10.0 ** rng.integers(-30, 30, n)
+    k = n // 4                                                # random bit patterns: every exponent
+    xr[:k] = rng.integers(0, 2 ** 64, k, dtype=np.uint64).view(np.float64)
+    yr[:k] = rng.integers(0, 2 ** 64, k, dtype=np.uint64).view(np.float64)
+    yb = yr[k:2 * k].view(np.uint64)                          # divisors with short significands
+    yb &= ~np.uint64(0x000FFFFFFFFFFF00)
+    q = rng.uniform(1.0, 2.0, k)                              # quotients next to a representable value
+    with np.errstate(all="ignore"):
+        xr[2 * k:3 * k] = q * yr[2 * k:3 * k]
     x = np.concatenate([xs.ravel(), xr])
     y = np.concatenate([ys.ravel(), yr])
     got = api.math_eval(h, "div", _dev(x), _dev(y)).cpu().numpy()
