@@ -475,109 +475,110 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
   const int64_t it = f.col_itype[c];
   const int64_t lit = f.lun_itype[l];
   const bool wallroof = is_wallroof(it);
-  S hm[MAXL + 1], xm[MAXL + 1], wice0[MAXL + 1], wmass0[MAXL + 1];
-  S tinc[MAXL + 1], supercool[MAXGRND + 1];
-  double wexice0[MAXL + 1];
   double* EXI = f.excess_ice;
   const double fse = f.frac_sno_eff[c];
   const double fh = f.frac_h2osfc[c];
+  const bool supercool_type = (lit == ISTSOIL || lit == ISTCROP || it == ICOL_ROAD_PERV);
   f.xmf[c] = 0.0;
   f.qflx_snomelt[c] = 0.0;
   f.qflx_snofrz[c] = 0.0;
   f.qflx_snow_drain[c] = 0.0;
+  // The reference runs three level loops: the levels' starting state, the melt/freeze
+  // decisions, then the phase change itself.  No level reads another's values in
+  // them, and the column sums are formed in ascending level order either way, so one
+  // pass per level gives the same bits with the level's values in registers.
   for (int j = -nlevsno + 1; j <= nlevmax; j++) {
     const int jj = j + joff;
-    tinc[jj] = 0.0;
+    // ---- the level's starting state ----
+    S tinc, hm, xm, wice0, wmass0, sc;
+    tinc = 0.0;
+    hm = 0.0;
+    xm = 0.0;
+    wice0 = 0.0;
+    wmass0 = 0.0;
+    sc = 0.0;
+    double wexice0 = 0.0;
     if (j >= snl + 1) {
       LV(f.imelt, c, jj, ld) = 0;
-      hm[jj] = 0.0;
-      xm[jj] = 0.0;
-      wice0[jj] = X.Ice(jj);
-      wexice0[jj] = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
-      wmass0[jj] = X.Ice(jj) + X.Liq(jj) + wexice0[jj];
+      wice0 = X.Ice(jj);
+      wexice0 = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
+      wmass0 = X.Ice(jj) + X.Liq(jj) + wexice0;
       if (j >= 1) LV(f.exice_subs, c, j, ld) = 0.0;
     }
     if (j <= 0) {
       LV(f.qflx_snomelt_lyr, c, jj, ld) = 0.0;
       LV(f.qflx_snofrz_lyr, c, jj, ld) = 0.0;
     }
-  }
-  for (int j = (int)snl + 1; j <= 0; j++) {
-    const int jj = j + joff;
-    if (X.Ice(jj) > 0.0 && X.T(jj) > TFRZ) {
-      LV(f.imelt, c, jj, ld) = 1;
-      tinc[jj] = TFRZ - X.T(jj);
-      X.T(jj) = TFRZ;
-    }
-    if (X.Liq(jj) > 0.0 && X.T(jj) < TFRZ) {
-      LV(f.imelt, c, jj, ld) = 2;
-      tinc[jj] = TFRZ - X.T(jj);
-      X.T(jj) = TFRZ;
-    }
-  }
-  const bool supercool_type = (lit == ISTSOIL || lit == ISTCROP || it == ICOL_ROAD_PERV);
-  for (int j = 1; j <= nlevmax; j++) {
-    const int jj = j + joff;
-    supercool[j] = 0.0;
+    if (j < snl + 1) continue;
     const bool active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= D.nlevurb);
-    if (!active) continue;
-    if (X.Ice(jj) > 0.0 && X.T(jj) > TFRZ) {
-      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
-    }
-    if (LV(EXI, c, j, ld) > 0.0 && X.T(jj) > TFRZ) {
-      LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
-    }
-    if (supercool_type) {
-      const S tt = X.T(jj);
-      if (tt < TFRZ) {
-        const S smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
-        S sc = X.Watsat(j) * cm_pow(smp / X.Sucsat(j), -1.0 / X.Bsw(j));
-        sc *= LVc(f.dz, c, jj, ld) * 1000.0;
-        supercool[j] = sc;
+    // ---- melt / freeze decision ----
+    if (j <= 0) {
+      if (X.Ice(jj) > 0.0 && X.T(jj) > TFRZ) {
+        LV(f.imelt, c, jj, ld) = 1;
+        tinc = TFRZ - X.T(jj);
+        X.T(jj) = TFRZ;
+      }
+      if (X.Liq(jj) > 0.0 && X.T(jj) < TFRZ) {
+        LV(f.imelt, c, jj, ld) = 2;
+        tinc = TFRZ - X.T(jj);
+        X.T(jj) = TFRZ;
+      }
+    } else if (active) {
+      if (X.Ice(jj) > 0.0 && X.T(jj) > TFRZ) {
+        LV(f.imelt, c, jj, ld) = 1; tinc = TFRZ - X.T(jj); X.T(jj) = TFRZ;
+      }
+      if (LV(EXI, c, j, ld) > 0.0 && X.T(jj) > TFRZ) {
+        LV(f.imelt, c, jj, ld) = 1; tinc = TFRZ - X.T(jj); X.T(jj) = TFRZ;
+      }
+      if (supercool_type) {
+        const S tt = X.T(jj);
+        if (tt < TFRZ) {
+          const S smp = HFUS * (TFRZ - tt) / (GRAV * tt) * 1000.0;
+          S scv = X.Watsat(j) * cm_pow(smp / X.Sucsat(j), -1.0 / X.Bsw(j));
+          scv *= LVc(f.dz, c, jj, ld) * 1000.0;
+          sc = scv;
+        }
+      }
+      if (X.Liq(jj) > sc && X.T(jj) < TFRZ) {
+        LV(f.imelt, c, jj, ld) = 2; tinc = TFRZ - X.T(jj); X.T(jj) = TFRZ;
+      }
+      if (f.h2osno_no_layers[c] > 0.0 && j == 1) {
+        if (X.T(jj) > TFRZ) {
+          LV(f.imelt, c, jj, ld) = 1; tinc = TFRZ - X.T(jj); X.T(jj) = TFRZ;
+        }
       }
     }
-    if (X.Liq(jj) > supercool[j] && X.T(jj) < TFRZ) {
-      LV(f.imelt, c, jj, ld) = 2; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
-    }
-    if (f.h2osno_no_layers[c] > 0.0 && j == 1) {
-      if (X.T(jj) > TFRZ) {
-        LV(f.imelt, c, jj, ld) = 1; tinc[jj] = TFRZ - X.T(jj); X.T(jj) = TFRZ;
-      }
-    }
-  }
-  for (int j = (int)snl + 1; j <= nlevmax; j++) {
-    const int jj = j + joff;
-    const bool active = (!wallroof && j <= nlevgrnd) || (wallroof && j <= D.nlevurb);
     if (!active) continue;
+    // ---- phase change ----
     int64_t im = LV(f.imelt, c, jj, ld);
     const S fct = X.Fact(jj);
     if (im > 0) {
       if (j == snl + 1) {
-        if (j > 0) hm[jj] = dhsdT * tinc[jj] - tinc[jj] / fct;
-        else hm[jj] = fse * (dhsdT * tinc[jj] - tinc[jj] / fct);
-        if (j == 1 && fh != 0.0) hm[jj] -= fh * dhsdT * tinc[jj];
+        if (j > 0) hm = dhsdT * tinc - tinc / fct;
+        else hm = fse * (dhsdT * tinc - tinc / fct);
+        if (j == 1 && fh != 0.0) hm -= fh * dhsdT * tinc;
       } else if (j == 1) {
-        hm[jj] = (1.0 - fse - fh) * dhsdT * tinc[jj] - tinc[jj] / fct;
+        hm = (1.0 - fse - fh) * dhsdT * tinc - tinc / fct;
       } else {
-        if (j < 1) hm[jj] = -fse * tinc[jj] / fct;
-        else hm[jj] = -tinc[jj] / fct;
+        if (j < 1) hm = -fse * tinc / fct;
+        else hm = -tinc / fct;
       }
     }
-    if (im == 1 && hm[jj] < 0.0) { hm[jj] = 0.0; im = 0; }
-    if (im == 2 && hm[jj] > 0.0) { hm[jj] = 0.0; im = 0; }
+    if (im == 1 && hm < 0.0) { hm = 0.0; im = 0; }
+    if (im == 2 && hm > 0.0) { hm = 0.0; im = 0; }
     LV(f.imelt, c, jj, ld) = im;
-    if (im > 0 && fabs(VAL(hm[jj])) > 0.0) {
-      xm[jj] = hm[jj] * dtime / HFUS;
+    if (im > 0 && fabs(VAL(hm)) > 0.0) {
+      xm = hm * dtime / HFUS;
       if (j == 1) {
-        if (f.h2osno_no_layers[c] > 0.0 && xm[jj] > 0.0) {
+        if (f.h2osno_no_layers[c] > 0.0 && xm > 0.0) {
           const double temp1 = f.h2osno_no_layers[c];
-          const S h2n = jl_max(0.0, temp1 - xm[jj]);
+          const S h2n = jl_max(0.0, temp1 - xm);
           f.h2osno_no_layers[c] = VAL(h2n);
           const S propor = h2n / temp1;
           f.snow_depth[c] = VAL(propor * f.snow_depth[c]);
-          const S heatr0 = hm[jj] - HFUS * (temp1 - h2n) / dtime;
-          if (heatr0 > 0.0) { xm[jj] = heatr0 * dtime / HFUS; hm[jj] = heatr0; }
-          else { xm[jj] = 0.0; hm[jj] = 0.0; }
+          const S heatr0 = hm - HFUS * (temp1 - h2n) / dtime;
+          if (heatr0 > 0.0) { xm = heatr0 * dtime / HFUS; hm = heatr0; }
+          else { xm = 0.0; hm = 0.0; }
           const S qsm = jl_max(0.0, temp1 - h2n) / dtime;
           f.qflx_snomelt[c] = VAL(qsm);
           f.xmf[c] = HFUS * VAL(qsm);
@@ -586,30 +587,30 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
       }
       S heatr = 0.0;
       S ice = X.Ice(jj);
-      if (xm[jj] > 0.0) {
-        ice = jl_max(0.0, wice0[jj] - xm[jj]);
+      if (xm > 0.0) {
+        ice = jl_max(0.0, wice0 - xm);
         X.Ice(jj) = ice;
-        heatr = hm[jj] - jl_div(HFUS * (wice0[jj] - ice), dtime);
-        const S xm2 = xm[jj] - ice;
+        heatr = hm - jl_div(HFUS * (wice0 - ice), dtime);
+        const S xm2 = xm - ice;
         if (ice == 0.0) {
-          if (wexice0[jj] >= 0.0 && xm2 > 0.0 && j >= 2) {
-            const S ex = jl_max(0.0, wexice0[jj] - xm2);
+          if (wexice0 >= 0.0 && xm2 > 0.0 && j >= 2) {
+            const S ex = jl_max(0.0, wexice0 - xm2);
             LV(EXI, c, j, ld) = VAL(ex);
-            heatr = hm[jj] - jl_div(HFUS * (wexice0[jj] - ex + wice0[jj] - ice), dtime);
+            heatr = hm - jl_div(HFUS * (wexice0 - ex + wice0 - ice), dtime);
           }
         }
-      } else if (xm[jj] < 0.0) {
+      } else if (xm < 0.0) {
         if (j <= 0) {
-          ice = jl_min(wmass0[jj], wice0[jj] - xm[jj]);
+          ice = jl_min(wmass0, wice0 - xm);
         } else {
-          if (wmass0[jj] - wexice0[jj] < supercool[j]) ice = 0.0;
-          else ice = jl_min(wmass0[jj] - wexice0[jj] - supercool[j], wice0[jj] - xm[jj]);
+          if (wmass0 - wexice0 < sc) ice = 0.0;
+          else ice = jl_min(wmass0 - wexice0 - sc, wice0 - xm);
         }
         X.Ice(jj) = ice;
-        heatr = hm[jj] - jl_div(HFUS * (wice0[jj] - ice), dtime);
+        heatr = hm - jl_div(HFUS * (wice0 - ice), dtime);
       }
       const double ei_val = j >= 1 ? LV(EXI, c, j, ld) : 0.0;
-      const S liq = jl_max(0.0, wmass0[jj] - ice - ei_val);
+      const S liq = jl_max(0.0, wmass0 - ice - ei_val);
       X.Liq(jj) = liq;
       if (fabs(VAL(heatr)) > 0.0) {
         S tt = X.T(jj);
@@ -628,19 +629,19 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
       }
       if (j >= 1) {
         const double ex = LV(EXI, c, j, ld);
-        f.xmf[c] += jl_div(HFUS * (VAL(wice0[jj]) - VAL(ice)), dtime) + jl_div(HFUS * (wexice0[jj] - ex), dtime);
-        LV(f.exice_subs, c, j, ld) = jl_max(0.0, jl_div(wexice0[jj] - ex, DENICE));
+        f.xmf[c] += jl_div(HFUS * (VAL(wice0) - VAL(ice)), dtime) + jl_div(HFUS * (wexice0 - ex), dtime);
+        LV(f.exice_subs, c, j, ld) = jl_max(0.0, jl_div(wexice0 - ex, DENICE));
       } else {
-        f.xmf[c] += jl_div(HFUS * (VAL(wice0[jj]) - VAL(ice)), dtime);
+        f.xmf[c] += jl_div(HFUS * (VAL(wice0) - VAL(ice)), dtime);
       }
       if (im == 1 && j < 1) {
-        const double q = jl_div(jl_max(0.0, VAL(wice0[jj]) - VAL(ice)), dtime);
+        const double q = jl_div(jl_max(0.0, VAL(wice0) - VAL(ice)), dtime);
         LV(f.qflx_snomelt_lyr, c, jj, ld) = q;
         f.qflx_snomelt[c] += q;
         f.snomelt_accum[c] += q * dtime * 1.0e-3;
       }
       if (im == 2 && j < 1) {
-        const double q = jl_div(jl_max(0.0, VAL(ice) - VAL(wice0[jj])), dtime);
+        const double q = jl_div(jl_max(0.0, VAL(ice) - VAL(wice0)), dtime);
         LV(f.qflx_snofrz_lyr, c, jj, ld) = q;
         f.qflx_snofrz[c] += q;
       }
