@@ -460,8 +460,9 @@ __device__ inline void phase_change_h2osfc_col(const Dims& D, const clmgb_soilte
 
 // ===========================================================================
 // phase_change_beta! (soil_temperature.jl:1929-2230), hard Float64 path, column c.
-// The reference's four sequential level loops per thread are kept; the per-call
-// scratch rows (PcbTmp) become per-thread arrays.
+// The reference's four level loops (the levels' starting state, the snow levels' and
+// the soil levels' melt/freeze decisions, the phase change) run as one pass per
+// level, and its per-call scratch rows (PcbTmp) become that level's registers.
 // ===========================================================================
 template <class ST>
 __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp_fields& f, int64_t c,
@@ -483,10 +484,10 @@ __device__ inline void phase_change_beta_col(const Dims& D, const clmgb_soiltemp
   f.qflx_snomelt[c] = 0.0;
   f.qflx_snofrz[c] = 0.0;
   f.qflx_snow_drain[c] = 0.0;
-  // The reference runs three level loops: the levels' starting state, the melt/freeze
-  // decisions, then the phase change itself.  No level reads another's values in
-  // them, and the column sums are formed in ascending level order either way, so one
-  // pass per level gives the same bits with the level's values in registers.
+  // No level reads another level's values in the reference's four loops, and the
+  // column sums (xmf, qflx_snomelt, qflx_snofrz, snomelt_accum, and level 1's
+  // overwrite of the first two) are formed in ascending level order either way, so one
+  // pass per level gives the same bits.
   for (int j = -nlevsno + 1; j <= nlevmax; j++) {
     const int jj = j + joff;
     // ---- the level's starting state ----
