@@ -762,7 +762,7 @@ int32_t clmgb_reserve(clmgb_handle h, int64_t max_nc);
 int32_t clmgb_get_option(clmgb_handle h, int32_t key, int64_t* value);
 
 /* Evaluates the library's binary64 log (op 0), exp (1), pow (2), log10 (3), sin (4), acos (5)
- * or division x / y (6, the kernels' division with its zero-numerator shortcut)
+ * or division x / y (6, the kernels' division: the IEEE quotient, formed on the integer pipes)
  * elementwise on device arrays; y is read for pow and division only.  The oracle and
  * the tests use it to check that the GPU rounds exactly as the CPU build does. */
 int32_t clmgb_math_eval(clmgb_handle h, int32_t op, int64_t n, const double* x, const double* y,
